@@ -1,0 +1,100 @@
+/* msc_gpu.h -- C ABI of the GB300 (sm_103a) discrete-gradient engine.
+ *
+ * Drop-in for the hot path of MSCEER's steepest_lstar / Accurate2D gradient
+ * builder: the per-cell .grad bytes it produces are bit-identical to the
+ * reference's.  Plain pointers and sizes only; no C++ or torch types cross this
+ * boundary.  Every entry returns an int status (MSC_OK or a negative MSC_ERR_*);
+ * msc_last_error_string() describes the last failure on the calling thread.
+ *
+ * Layout (as the reference):
+ *   f     X*Y*Z float32, x fastest (RegularGridTrilinearFunction::LoadImageFromFile,
+ *         gi_regular_grid_trilinear_function.h:246-260)
+ *   grad  one byte per cell of the (2X-1)(2Y-1)(2Z-1) cell complex, x fastest
+ *         (TopologicalRegularGrid3D, gi_topological_regular_grid.h:113-126);
+ *         byte = GradBitfield (gi_discrete_gradient_labeling.h:11-19), LSB first:
+ *         assigned:1 flag:1 pair:3 ldir:3.
+ * 2D uses X*Y floats and (2X-1)(2Y-1) cells.
+ *
+ * Device-pointer entries run on `stream` (a cudaStream_t; NULL = legacy default
+ * stream) and synchronise it to read the kernels' convergence and error flags, so
+ * the output is complete when they return.  The library never frees caller
+ * memory.  Inputs with NaN are rejected with MSC_ERR_NAN_INPUT (the vertex order
+ * the reference uses is not defined for them).
+ */
+#ifndef MSC_GPU_H
+#define MSC_GPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct CUstream_st* msc_stream_t;
+
+#define MSC_OK 0
+#define MSC_ERR_BAD_DIMS (-1)
+#define MSC_ERR_NULL_POINTER (-2)
+#define MSC_ERR_CUDA (-3)
+#define MSC_ERR_OOM (-4)
+#define MSC_ERR_NAN_INPUT (-5)
+#define MSC_ERR_ITER_LIMIT (-6)
+#define MSC_ERR_QUEUE_OVERFLOW (-7)
+
+/* Library ABI version (major*10000 + minor*100 + patch). */
+int msc_version(void);
+
+/* Text of the last error raised on the calling thread ("" if none). */
+const char* msc_last_error_string(void);
+
+/* Ascending-manifold tile passes run by the last .grad / stage-2 call on the
+ * calling thread (a diagnostic; each pass is one kernel launch). */
+int msc_last_ldir_passes(void);
+
+/* Number of cells (= .grad bytes) of the complex: TopologicalRegularGrid3D::numCells
+ * (gi_topological_regular_grid.h:1254).  Returns -1 for invalid dims. */
+int64_t msc_num_cells_3d(const int64_t dims[3]);
+int64_t msc_num_cells_2d(const int64_t dims[2]);
+
+/* Complete .grad of steepest_lstar for a device-resident volume.
+ * Replaces steepest_lstar/steepest_lstar.cxx:129-258:
+ *   RegularGridMaxMinVertexLabeling3D::ComputeOutput (gi_max_vertex_labeling.h:1119),
+ *   SlidingWindowRobinsNoalloc::ComputePairing_sliding (gi_fast_robins_noalloc.h:1254),
+ *   TopologicalGradientUsingAlgorithms::setAscendingManifoldDimensions
+ *     (gi_topological_gradient_using_algorithms.h:430),
+ *   and the flag pass of DiscreteGradientLabeling::outputToFile
+ *     (gi_discrete_gradient_labeling.h:200-218).
+ * f: device, X*Y*Z floats; grad_out: device, msc_num_cells_3d(dims) bytes.
+ * Synchronises `stream` once per ascending-manifold pass (a few per volume). */
+int msc_lower_star_grad_3d(const float* f, const int64_t dims[3], uint8_t* grad_out, msc_stream_t stream);
+
+/* 2D counterpart: Accurate2D::DiscreteGradientBuilder::ComputeDiscreteGradient with
+ * no saddle streamlines (gi_discrete_gradient_computer.h:561-583, 681-689). */
+int msc_lower_star_grad_2d(const float* f, const int64_t dims[2], uint8_t* grad_out, msc_stream_t stream);
+
+/* Stage 1 alone: lower-star pairing of every vertex
+ * (gi_fast_robins_noalloc.h:1254-1535 / gi_modified_robins.h:1281-1402) written as
+ * final bytes except ldir, which holds only the closure roots (critical 1-cells 2,
+ * critical 2-cells 1, critical 3-cells 0, others 3).  Synchronises `stream` once at
+ * the end to read the kernel's error flag (NaN input). */
+int msc_lower_star_pairs_3d(const float* f, const int64_t dims[3], uint8_t* grad_out, msc_stream_t stream);
+int msc_lower_star_pairs_2d(const float* f, const int64_t dims[2], uint8_t* grad_out, msc_stream_t stream);
+
+/* Stage 2 alone: completes the ldir bits of a stage-1 .grad in place
+ * (setAscendingManifoldDimensions, gi_topological_gradient_using_algorithms.h:430-478).
+ * passes_out (optional) receives the number of tile passes run. */
+int msc_ascending_manifold_dims_3d(uint8_t* grad, const int64_t dims[3], msc_stream_t stream, int* passes_out);
+int msc_ascending_manifold_dims_2d(uint8_t* grad, const int64_t dims[2], msc_stream_t stream, int* passes_out);
+
+/* Host-memory convenience with steepest_lstar's semantics: copies f to the GPU,
+ * computes, copies the .grad back.  f_host: X*Y*Z floats; grad_host:
+ * msc_num_cells_3d(dims) bytes.  Blocking.  Runs on the current device and keeps a
+ * per-thread device staging buffer (grown on demand) between calls; pinned host
+ * buffers give the fastest copies. */
+int msc_steepest_lstar_host(const float* f_host, const int64_t dims[3], uint8_t* grad_host);
+int msc_lower_star_grad_2d_host(const float* f_host, const int64_t dims[2], uint8_t* grad_host);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* MSC_GPU_H */

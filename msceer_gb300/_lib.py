@@ -1,0 +1,76 @@
+"""ctypes binding of libmsc_gpu.so (the C ABI declared in include/msc_gpu.h).
+
+The library is built in-tree by :mod:`msceer_gb300.build`.  There is no CPU
+fallback: if the shared object is missing or a call fails, this module raises.
+"""
+from __future__ import annotations
+
+import ctypes
+import threading
+from pathlib import Path
+
+_LIB_PATH = Path(__file__).resolve().parent / "libmsc_gpu.so"
+_lock = threading.Lock()
+_lib = None
+
+MSC_OK = 0
+ERRORS = {
+    -1: "MSC_ERR_BAD_DIMS", -2: "MSC_ERR_NULL_POINTER", -3: "MSC_ERR_CUDA", -4: "MSC_ERR_OOM",
+    -5: "MSC_ERR_NAN_INPUT", -6: "MSC_ERR_ITER_LIMIT", -7: "MSC_ERR_QUEUE_OVERFLOW",
+}
+
+# every symbol include/msc_gpu.h declares: (restype, argtypes)
+_I64P = ctypes.POINTER(ctypes.c_int64)
+_VP = ctypes.c_void_p
+SIGNATURES = {
+    "msc_version": (ctypes.c_int, []),
+    "msc_last_error_string": (ctypes.c_char_p, []),
+    "msc_last_ldir_passes": (ctypes.c_int, []),
+    "msc_num_cells_3d": (ctypes.c_int64, [_I64P]),
+    "msc_num_cells_2d": (ctypes.c_int64, [_I64P]),
+    "msc_lower_star_grad_3d": (ctypes.c_int, [_VP, _I64P, _VP, _VP]),
+    "msc_lower_star_grad_2d": (ctypes.c_int, [_VP, _I64P, _VP, _VP]),
+    "msc_lower_star_pairs_3d": (ctypes.c_int, [_VP, _I64P, _VP, _VP]),
+    "msc_lower_star_pairs_2d": (ctypes.c_int, [_VP, _I64P, _VP, _VP]),
+    "msc_ascending_manifold_dims_3d": (ctypes.c_int, [_VP, _I64P, _VP, ctypes.POINTER(ctypes.c_int)]),
+    "msc_ascending_manifold_dims_2d": (ctypes.c_int, [_VP, _I64P, _VP, ctypes.POINTER(ctypes.c_int)]),
+    "msc_steepest_lstar_host": (ctypes.c_int, [_VP, _I64P, _VP]),
+    "msc_lower_star_grad_2d_host": (ctypes.c_int, [_VP, _I64P, _VP]),
+}
+
+
+class MscError(RuntimeError):
+    def __init__(self, code: int, fn: str, msg: str):
+        super().__init__(f"{fn} failed with {ERRORS.get(code, code)}: {msg}")
+        self.code = code
+
+
+def lib_path() -> Path:
+    return _LIB_PATH
+
+
+def load() -> ctypes.CDLL:
+    """Load libmsc_gpu.so (raises if it has not been built)."""
+    global _lib
+    with _lock:
+        if _lib is None:
+            if not _LIB_PATH.exists():
+                raise RuntimeError(f"{_LIB_PATH} is missing: run `python -m msceer_gb300.build` "
+                                   "(there is no CPU fallback)")
+            lib = ctypes.CDLL(str(_LIB_PATH))
+            for name, (res, args) in SIGNATURES.items():
+                fn = getattr(lib, name)
+                fn.restype = res
+                fn.argtypes = args
+            _lib = lib
+        return _lib
+
+
+def dims_arg(dims) -> ctypes.Array:
+    return (ctypes.c_int64 * len(dims))(*[int(d) for d in dims])
+
+
+def check(rc: int, fn: str) -> None:
+    if rc != MSC_OK:
+        msg = load().msc_last_error_string().decode(errors="replace")
+        raise MscError(rc, fn, msg)

@@ -1,0 +1,225 @@
+"""Host-side mirror of the reference's interface for the .grad path.
+
+* :func:`steepest_lstar` / :func:`lower_star_grad` -- the complete .grad of
+  ``steepest_lstar`` (3D) or of ``Accurate2D::DiscreteGradientBuilder`` without saddle
+  streamlines (2D), computed by libmsc_gpu.so.  Accepts a CUDA ``torch.Tensor``
+  (device-resident, enqueued on the current stream) or a ``numpy`` array (host
+  buffers; copies in and out through the C ABI).
+* :class:`TopologicalRegularGrid3D` / :class:`TopologicalRegularGrid2D` -- the index
+  algebra of gi_topological_regular_grid.h (cellid2Coords :1268, coords2Cellid :1274,
+  dimension :1314, boundaryValue :1291, VertexNumberFromCellID :1337), vectorised.
+* :class:`DiscreteGradientLabeling` -- the per-cell byte accessors of
+  gi_discrete_gradient_labeling.h (getAssigned :71, getPair :87, getCritical :99,
+  getDimAscMan :114, outputToFile :200, load_from_file :229).
+"""
+from __future__ import annotations
+
+import ctypes
+from pathlib import Path
+
+import numpy as np
+
+from . import _lib
+
+
+def _is_torch(x) -> bool:
+    return type(x).__module__.startswith("torch")
+
+
+def _shape_dims(shape):
+    """numpy/torch shape (Z, Y, X) or (Y, X) -> reference dims (X, Y, Z) / (X, Y)."""
+    if len(shape) not in (2, 3):
+        raise ValueError(f"expected a 2D or 3D volume, got shape {tuple(shape)}")
+    return tuple(int(s) for s in shape[::-1])
+
+
+def num_cells(dims) -> int:
+    lib = _lib.load()
+    fn = lib.msc_num_cells_3d if len(dims) == 3 else lib.msc_num_cells_2d
+    n = fn(_lib.dims_arg(dims))
+    if n < 0:
+        raise ValueError(f"invalid dims {dims}")
+    return int(n)
+
+
+def _device_call(name3, name2, f, out):
+    import torch
+
+    if f.dtype != torch.float32:
+        raise TypeError("f must be float32")
+    f = f.contiguous()
+    dims = _shape_dims(f.shape)
+    n = num_cells(dims)
+    if out is None:
+        out = torch.empty(n, dtype=torch.uint8, device=f.device)
+    elif out.dtype != torch.uint8 or out.numel() != n or not out.is_contiguous() or out.device != f.device:
+        raise ValueError("out must be a contiguous uint8 tensor of num_cells bytes on f's device")
+    lib = _lib.load()
+    name = name3 if len(dims) == 3 else name2
+    stream = torch.cuda.current_stream(f.device).cuda_stream
+    with torch.cuda.device(f.device):
+        rc = getattr(lib, name)(ctypes.c_void_p(f.data_ptr()), _lib.dims_arg(dims),
+                                ctypes.c_void_p(out.data_ptr()), ctypes.c_void_p(stream))
+    _lib.check(rc, name)
+    return out
+
+
+def lower_star_grad(f, out=None):
+    """The complete .grad (one byte per cell, x fastest) of a float32 volume."""
+    if _is_torch(f):
+        if not f.is_cuda:
+            f = f.numpy()
+        else:
+            return _device_call("msc_lower_star_grad_3d", "msc_lower_star_grad_2d", f, out)
+    f = np.ascontiguousarray(f, dtype=np.float32)
+    dims = _shape_dims(f.shape)
+    n = num_cells(dims)
+    if out is None:
+        out = np.empty(n, dtype=np.uint8)
+    lib = _lib.load()
+    name = "msc_steepest_lstar_host" if len(dims) == 3 else "msc_lower_star_grad_2d_host"
+    rc = getattr(lib, name)(f.ctypes.data_as(ctypes.c_void_p), _lib.dims_arg(dims),
+                            out.ctypes.data_as(ctypes.c_void_p))
+    _lib.check(rc, name)
+    return out
+
+
+def steepest_lstar(f, out=None):
+    """steepest_lstar's .grad for a 3D volume (numpy host array or CUDA tensor)."""
+    if len(f.shape) != 3:
+        raise ValueError("steepest_lstar takes a 3D volume")
+    return lower_star_grad(f, out)
+
+
+def lower_star_pairs(f, out=None):
+    """Stage 1 only (CUDA tensors): pairs, flag and the ascending-manifold roots."""
+    return _device_call("msc_lower_star_pairs_3d", "msc_lower_star_pairs_2d", f, out)
+
+
+def ascending_manifold_dims(grad, dims) -> int:
+    """Stage 2 only (CUDA uint8 tensor, in place); returns the number of tile passes."""
+    import torch
+
+    lib = _lib.load()
+    name = "msc_ascending_manifold_dims_3d" if len(dims) == 3 else "msc_ascending_manifold_dims_2d"
+    passes = ctypes.c_int(0)
+    stream = torch.cuda.current_stream(grad.device).cuda_stream
+    with torch.cuda.device(grad.device):
+        rc = getattr(lib, name)(ctypes.c_void_p(grad.data_ptr()), _lib.dims_arg(dims),
+                                ctypes.c_void_p(stream), ctypes.byref(passes))
+    _lib.check(rc, name)
+    return passes.value
+
+
+class TopologicalRegularGrid3D:
+    """Cell-complex index algebra of a non-periodic X x Y x Z vertex grid."""
+
+    nd = 3
+
+    def __init__(self, X: int, Y: int, Z: int):
+        self.base = (int(X), int(Y), int(Z))
+        self.xyz = tuple(2 * v - 1 for v in self.base)
+
+    def XYZ(self):
+        return self.xyz
+
+    def numCells(self) -> int:
+        return int(np.prod(self.xyz))
+
+    def maxDim(self) -> int:
+        return self.nd
+
+    def cellid2Coords(self, cellid):
+        c = np.asarray(cellid, dtype=np.int64)
+        dX, dY = self.xyz[0], self.xyz[1]
+        out = [c % dX, (c // dX) % dY]
+        if self.nd == 3:
+            out.append(c // (dX * dY))
+        return np.stack(out, axis=-1)
+
+    def coords2Cellid(self, coords):
+        c = np.asarray(coords, dtype=np.int64)
+        idx = c[..., 0] + c[..., 1] * self.xyz[0]
+        if self.nd == 3:
+            idx = idx + c[..., 2] * self.xyz[0] * self.xyz[1]
+        return idx
+
+    def dimension(self, cellid):
+        return (self.cellid2Coords(cellid) & 1).sum(axis=-1)
+
+    def boundaryValue(self, cellid):
+        c = self.cellid2Coords(cellid)
+        ext = np.asarray(self.xyz[: self.nd])
+        return ((c == 0) | (c == ext - 1)).sum(axis=-1)
+
+    def VertexNumberFromCellID(self, cellid):
+        c = self.cellid2Coords(cellid) // 2
+        v = c[..., 0] + c[..., 1] * self.base[0]
+        if self.nd == 3:
+            v = v + c[..., 2] * self.base[0] * self.base[1]
+        return v
+
+    def adjacency_offsets(self):
+        """m_adjacency_offsets: +x, -x, +y, -y[, +z, -z] (gi_topological_regular_grid.h:167-172)."""
+        s = [1, self.xyz[0], self.xyz[0] * self.xyz[1]][: self.nd]
+        return [o for st in s for o in (st, -st)]
+
+
+class TopologicalRegularGrid2D(TopologicalRegularGrid3D):
+    nd = 2
+
+    def __init__(self, X: int, Y: int):
+        self.base = (int(X), int(Y))
+        self.xyz = tuple(2 * v - 1 for v in self.base)
+
+
+class DiscreteGradientLabeling:
+    """One GradBitfield byte per cell: assigned:1 flag:1 pair:3 ldir:3 (LSB first)."""
+
+    def __init__(self, mesh: TopologicalRegularGrid3D, data=None):
+        self.mesh = mesh
+        n = mesh.numCells()
+        if data is None:
+            data = np.zeros(n, dtype=np.uint8)
+        data = np.asarray(data, dtype=np.uint8).reshape(-1)
+        if data.size != n:
+            raise ValueError(f"expected {n} bytes, got {data.size}")
+        self.data = data
+
+    def ClearAllGradient(self):
+        self.data[:] = 0
+
+    def getAssigned(self, cellid):
+        return self.data[cellid] & 1
+
+    def getCritical(self, cellid):
+        return ((self.data[cellid] >> 2) & 7) == 7
+
+    def getPair(self, cellid):
+        code = (self.data[cellid] >> 2) & 7
+        offs = np.asarray(self.mesh.adjacency_offsets() + [0] * (8 - 2 * self.mesh.nd), dtype=np.int64)
+        return np.asarray(cellid, dtype=np.int64) + offs[code]
+
+    def getDimAscMan(self, cellid):
+        return self.data[cellid] >> 5
+
+    def getFlag(self, cellid):
+        return (self.data[cellid] >> 1) & 1
+
+    def outputToFile(self, filename):
+        Path(filename).write_bytes(self.data.tobytes())
+
+    def load_from_file(self, filename) -> bool:
+        p = Path(filename)
+        if not p.exists():
+            return False
+        raw = np.fromfile(p, dtype=np.uint8, count=self.mesh.numCells())
+        self.data[: raw.size] = raw
+        return True
+
+    def critical_counts(self):
+        """Critical cells per dimension (count_critical_points,
+        gi_topological_gradient_using_algorithms.h:141)."""
+        ids = np.nonzero(((self.data >> 2) & 7) == 7)[0]
+        dims = self.mesh.dimension(ids)
+        return [int((dims == d).sum()) for d in range(self.mesh.nd + 1)]

@@ -1,0 +1,281 @@
+// extern "C" entry points of libmsc_gpu.so (declared in include/msc_gpu.h).
+//
+// Host-side orchestration of the .grad pipeline: argument checks, per-call scratch
+// (two status words), kernel launches on the caller's stream, the ascending-manifold
+// pass loop and error reporting.  Status codes only; nothing throws across the ABI.
+#include <cuda_runtime.h>
+
+#include <cstdio>
+#include <cstring>
+#include <string>
+
+#include "msc_device.cuh"
+#include "../../include/msc_gpu.h"
+
+namespace {
+
+thread_local std::string g_last_error;
+thread_local int g_last_passes = 0;
+
+int fail(int code, const std::string& msg) {
+  g_last_error = msg;
+  return code;
+}
+
+int cuda_fail(cudaError_t e, const char* what) {
+  return fail(e == cudaErrorMemoryAllocation ? MSC_ERR_OOM : MSC_ERR_CUDA,
+              std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+#define MSC_CUDA(call, what)                  \
+  do {                                        \
+    cudaError_t e_ = (call);                  \
+    if (e_ != cudaSuccess) return cuda_fail(e_, what); \
+  } while (0)
+
+int num_sms() {
+  int dev = 0, n = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return 148;
+  if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n <= 0) return 148;
+  return n;
+}
+
+// Builds the mesh description, including the pair-code maps that reproduce the
+// reference encoder when an axis has a single vertex
+// (Compress6NeighborOffsetToByte, gi_topological_regular_grid.h:1182-1192: the
+// first axis whose stride equals the offset wins).  Returns false on bad dims.
+bool make_dims(int nd, const int64_t* dims, msc::GradDims* D) {
+  if (!dims) return false;
+  int64_t v[3] = {dims[0], dims[1], nd == 3 ? dims[2] : 1};
+  for (int a = 0; a < 3; a++)
+    if (v[a] < 1 || v[a] > (int64_t)1 << 30) return false;
+  msc::GradDims d{};
+  for (int a = 0; a < 3; a++) {
+    d.v[a] = v[a];
+    d.d[a] = 2 * v[a] - 1;
+  }
+  d.cs[0] = 1;
+  d.cs[1] = d.d[0];
+  d.cs[2] = d.d[0] * d.d[1];
+  d.ncells = d.d[0] * d.d[1] * d.d[2];
+  if (d.ncells / d.d[2] != d.d[0] * d.d[1]) return false;  // overflow
+  uint32_t enc = 0, dec = 0;
+  for (int c = 0; c < 6; c++) {
+    const int a = c >> 1, s = c & 1;
+    int e = c, t = c;
+    if (nd == 3) {
+      for (int b = 0; b < 3; b++)
+        if (d.cs[b] == d.cs[a]) { e = 2 * b + s; break; }
+      for (int b = 2; b >= 0; b--)
+        if (d.cs[b] == d.cs[a]) { t = 2 * b + s; break; }
+    }
+    enc |= (uint32_t)e << (3 * c);
+    dec |= (uint32_t)t << (3 * c);
+  }
+  d.enc_map = enc;
+  d.dec_map = dec;
+  *D = d;
+  return true;
+}
+
+struct Scratch {
+  int* words = nullptr;  // [0] error bits, [1] changed flag
+  cudaStream_t stream = nullptr;
+  ~Scratch() {
+    if (words) cudaFreeAsync(words, stream);
+  }
+};
+
+int alloc_scratch(Scratch& s, cudaStream_t stream) {
+  s.stream = stream;
+  MSC_CUDA(cudaMallocAsync((void**)&s.words, 2 * sizeof(int), stream), "cudaMallocAsync(status words)");
+  MSC_CUDA(cudaMemsetAsync(s.words, 0, 2 * sizeof(int), stream), "cudaMemsetAsync(status words)");
+  return MSC_OK;
+}
+
+int check_errors(const Scratch& s, cudaStream_t stream) {
+  int err = 0;
+  MSC_CUDA(cudaMemcpyAsync(&err, s.words, sizeof(int), cudaMemcpyDeviceToHost, stream), "read status");
+  MSC_CUDA(cudaStreamSynchronize(stream), "cudaStreamSynchronize");
+  if (err & msc::kErrNaN) return fail(MSC_ERR_NAN_INPUT, "input contains NaN");
+  if (err & msc::kErrLocalQueue) return fail(MSC_ERR_QUEUE_OVERFLOW, "ldir tile queue overflow");
+  if (err & msc::kErrPassLimit) return fail(MSC_ERR_ITER_LIMIT, "ldir closure did not converge");
+  return MSC_OK;
+}
+
+int pairs_impl(int nd, const float* f, const int64_t* dims, uint8_t* g, cudaStream_t stream, Scratch& s) {
+  msc::GradDims D;
+  if (!make_dims(nd, dims, &D)) return fail(MSC_ERR_BAD_DIMS, "invalid dims");
+  if (!f || !g) return fail(MSC_ERR_NULL_POINTER, "null buffer");
+  MSC_CUDA(msc::launch_lstar(nd, f, g, D, s.words, num_sms(), stream), "lower-star kernel launch");
+  return MSC_OK;
+}
+
+int ldir_impl(int nd, uint8_t* g, const int64_t* dims, cudaStream_t stream, Scratch& s, int* passes_out) {
+  msc::GradDims D;
+  if (!make_dims(nd, dims, &D)) return fail(MSC_ERR_BAD_DIMS, "invalid dims");
+  if (!g) return fail(MSC_ERR_NULL_POINTER, "null buffer");
+  // a path crosses each tile at most once per pass that makes progress, so the
+  // closure converges within (number of tiles + 1) passes
+  const int64_t limit = msc::ldir_num_tiles(nd, D) + 2;
+  const int sms = num_sms();
+  int passes = 0;
+  while (true) {
+    MSC_CUDA(cudaMemsetAsync(s.words + 1, 0, sizeof(int), stream), "reset changed flag");
+    MSC_CUDA(msc::launch_ldir_pass(nd, g, D, s.words + 1, s.words, sms, stream), "ldir kernel launch");
+    passes++;
+    int changed = 0;
+    MSC_CUDA(cudaMemcpyAsync(&changed, s.words + 1, sizeof(int), cudaMemcpyDeviceToHost, stream), "read changed");
+    MSC_CUDA(cudaStreamSynchronize(stream), "cudaStreamSynchronize");
+    if (!changed) break;
+    if (passes >= limit) return fail(MSC_ERR_ITER_LIMIT, "ldir closure did not converge");
+  }
+  if (passes_out) *passes_out = passes;
+  g_last_passes = passes;
+  return MSC_OK;
+}
+
+int validate(int nd, const int64_t* dims, const void* a, const void* b) {
+  msc::GradDims D;
+  if (!make_dims(nd, dims, &D)) return fail(MSC_ERR_BAD_DIMS, "invalid dims");
+  if (!a || !b) return fail(MSC_ERR_NULL_POINTER, "null buffer");
+  return MSC_OK;
+}
+
+int grad_impl(int nd, const float* f, const int64_t* dims, uint8_t* g, cudaStream_t stream) {
+  if (int rc = validate(nd, dims, f, g)) return rc;
+  Scratch s;
+  int rc = alloc_scratch(s, stream);
+  if (rc) return rc;
+  rc = pairs_impl(nd, f, dims, g, stream, s);
+  if (rc) return rc;
+  rc = ldir_impl(nd, g, dims, stream, s, nullptr);
+  if (rc) return rc;
+  return check_errors(s, stream);
+}
+
+// Per-thread device staging for the host-buffer entries: grown on demand and kept
+// between calls so repeated calls do not pay for allocation.
+struct HostStaging {
+  int dev = -1;
+  float* f = nullptr;
+  size_t fcap = 0;
+  uint8_t* g = nullptr;
+  size_t gcap = 0;
+  cudaStream_t stream = nullptr;
+};
+thread_local HostStaging t_stage;
+
+int ensure_staging(size_t fbytes, size_t gbytes) {
+  int dev = 0;
+  MSC_CUDA(cudaGetDevice(&dev), "cudaGetDevice");
+  HostStaging& h = t_stage;
+  if (h.dev != dev) {  // a different device: start over (old buffers belong to the old device)
+    h = HostStaging{};
+    h.dev = dev;
+  }
+  if (!h.stream) MSC_CUDA(cudaStreamCreateWithFlags(&h.stream, cudaStreamNonBlocking), "cudaStreamCreate");
+  if (h.fcap < fbytes) {
+    if (h.f) cudaFree(h.f);
+    h.f = nullptr;
+    h.fcap = 0;
+    MSC_CUDA(cudaMalloc((void**)&h.f, fbytes), "cudaMalloc(f staging)");
+    h.fcap = fbytes;
+  }
+  if (h.gcap < gbytes) {
+    if (h.g) cudaFree(h.g);
+    h.g = nullptr;
+    h.gcap = 0;
+    MSC_CUDA(cudaMalloc((void**)&h.g, gbytes), "cudaMalloc(grad staging)");
+    h.gcap = gbytes;
+  }
+  return MSC_OK;
+}
+
+int host_impl(int nd, const float* fh, const int64_t* dims, uint8_t* gh) {
+  msc::GradDims D;
+  if (!make_dims(nd, dims, &D)) return fail(MSC_ERR_BAD_DIMS, "invalid dims");
+  if (!fh || !gh) return fail(MSC_ERR_NULL_POINTER, "null buffer");
+  const size_t nv = (size_t)(D.v[0] * D.v[1] * D.v[2]);
+  if (int rc = ensure_staging(nv * sizeof(float), (size_t)D.ncells)) return rc;
+  HostStaging& h = t_stage;
+  MSC_CUDA(cudaMemcpyAsync(h.f, fh, nv * sizeof(float), cudaMemcpyHostToDevice, h.stream), "copy f to device");
+  if (int rc = grad_impl(nd, h.f, dims, h.g, h.stream)) return rc;
+  MSC_CUDA(cudaMemcpyAsync(gh, h.g, (size_t)D.ncells, cudaMemcpyDeviceToHost, h.stream), "copy grad to host");
+  MSC_CUDA(cudaStreamSynchronize(h.stream), "cudaStreamSynchronize");
+  return MSC_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int msc_version(void) { return 100; }
+
+const char* msc_last_error_string(void) { return g_last_error.c_str(); }
+
+int msc_last_ldir_passes(void) { return g_last_passes; }
+
+int64_t msc_num_cells_3d(const int64_t dims[3]) {
+  msc::GradDims D;
+  return make_dims(3, dims, &D) ? D.ncells : -1;
+}
+
+int64_t msc_num_cells_2d(const int64_t dims[2]) {
+  msc::GradDims D;
+  return make_dims(2, dims, &D) ? D.ncells : -1;
+}
+
+int msc_lower_star_grad_3d(const float* f, const int64_t dims[3], uint8_t* g, msc_stream_t stream) {
+  return grad_impl(3, f, dims, g, (cudaStream_t)stream);
+}
+
+int msc_lower_star_grad_2d(const float* f, const int64_t dims[2], uint8_t* g, msc_stream_t stream) {
+  return grad_impl(2, f, dims, g, (cudaStream_t)stream);
+}
+
+int msc_lower_star_pairs_3d(const float* f, const int64_t dims[3], uint8_t* g, msc_stream_t stream) {
+  if (int rc = validate(3, dims, f, g)) return rc;
+  Scratch s;
+  int rc = alloc_scratch(s, (cudaStream_t)stream);
+  if (!rc) rc = pairs_impl(3, f, dims, g, (cudaStream_t)stream, s);
+  if (!rc) rc = check_errors(s, (cudaStream_t)stream);
+  return rc;
+}
+
+int msc_lower_star_pairs_2d(const float* f, const int64_t dims[2], uint8_t* g, msc_stream_t stream) {
+  if (int rc = validate(2, dims, f, g)) return rc;
+  Scratch s;
+  int rc = alloc_scratch(s, (cudaStream_t)stream);
+  if (!rc) rc = pairs_impl(2, f, dims, g, (cudaStream_t)stream, s);
+  if (!rc) rc = check_errors(s, (cudaStream_t)stream);
+  return rc;
+}
+
+int msc_ascending_manifold_dims_3d(uint8_t* g, const int64_t dims[3], msc_stream_t stream, int* passes_out) {
+  if (int rc = validate(3, dims, g, g)) return rc;
+  Scratch s;
+  int rc = alloc_scratch(s, (cudaStream_t)stream);
+  if (!rc) rc = ldir_impl(3, g, dims, (cudaStream_t)stream, s, passes_out);
+  if (!rc) rc = check_errors(s, (cudaStream_t)stream);
+  return rc;
+}
+
+int msc_ascending_manifold_dims_2d(uint8_t* g, const int64_t dims[2], msc_stream_t stream, int* passes_out) {
+  if (int rc = validate(2, dims, g, g)) return rc;
+  Scratch s;
+  int rc = alloc_scratch(s, (cudaStream_t)stream);
+  if (!rc) rc = ldir_impl(2, g, dims, (cudaStream_t)stream, s, passes_out);
+  if (!rc) rc = check_errors(s, (cudaStream_t)stream);
+  return rc;
+}
+
+int msc_steepest_lstar_host(const float* f_host, const int64_t dims[3], uint8_t* grad_host) {
+  return host_impl(3, f_host, dims, grad_host);
+}
+
+int msc_lower_star_grad_2d_host(const float* f_host, const int64_t dims[2], uint8_t* grad_host) {
+  return host_impl(2, f_host, dims, grad_host);
+}
+
+}  // extern "C"

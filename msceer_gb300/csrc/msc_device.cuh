@@ -1,0 +1,58 @@
+// Device-side definitions shared by the .grad kernels (sm_103a).
+//
+// The cell complex of an X x Y x Z vertex grid is the (2X-1)(2Y-1)(2Z-1) index
+// lattice of TopologicalRegularGrid3D (gi_topological_regular_grid.h:113-126):
+// cell (cx,cy,cz) has id cx + cy*dX + cz*dX*dY, dimension = number of odd
+// coordinates, and vertex (x,y,z) is cell (2x,2y,2z).  One .grad byte per cell
+// (GradBitfield, gi_discrete_gradient_labeling.h:11-19), LSB first:
+//   bit 0 assigned, bit 1 flag (boundary), bits 2-4 pair direction
+//   (0..5 = +x,-x,+y,-y,+z,-z, 7 = critical), bits 5-7 ldir.
+#pragma once
+#include <cstdint>
+
+namespace msc {
+
+enum : int {
+  kErrNone = 0,
+  kErrNaN = 1 << 0,          // input contains NaN (outside the order's contract)
+  kErrPassLimit = 1 << 1,    // ldir closure did not converge within the pass bound
+  kErrLocalQueue = 1 << 2,   // shared-memory BFS queue overflow (cannot happen by construction)
+};
+
+struct GradDims {
+  int64_t v[3];     // vertices per axis (v[2] = 1 in 2D)
+  int64_t d[3];     // cells per axis, 2v-1
+  int64_t cs[3];    // cell-id strides: 1, dX, dX*dY
+  int64_t ncells;
+  // local pair code (0..5 = +x,-x,+y,-y,+z,-z) -> code stored in the .grad byte.
+  // Identity unless an axis has a single vertex, where the reference's encoder
+  // (Compress6NeighborOffsetToByte, gi_topological_regular_grid.h:1182-1192)
+  // reports the first axis whose stride is equal.  3 bits per code.
+  uint32_t enc_map;
+  // stored code -> true axis*2+sign, the inverse of enc_map for decoding.
+  uint32_t dec_map;
+};
+
+__host__ __device__ inline int map3(uint32_t m, int c) { return (int)((m >> (3 * c)) & 7u); }
+
+// The (value, then vertex index) total order of IsGreater
+// (gi_regular_grid_trilinear_function.h:309-314): true when vertex a comes
+// before (is lower than) vertex b.  Positions a, b index the same 3^ND
+// neighbourhood; position order equals global vertex-index order there.
+__device__ __forceinline__ bool before(float fa, int a, float fb, int b) {
+  if (fb > fa) return true;
+  if (fa > fb) return false;
+  return b > a;
+}
+
+}  // namespace msc
+
+#include <cuda_runtime.h>
+namespace msc {
+// launchers (defined next to their kernels)
+cudaError_t launch_lstar(int nd, const float* f, uint8_t* g, const GradDims& D, int* err, int num_sms,
+                         cudaStream_t stream);
+int64_t ldir_num_tiles(int nd, const GradDims& D);
+cudaError_t launch_ldir_pass(int nd, uint8_t* g, const GradDims& D, int* changed, int* err, int num_sms,
+                             cudaStream_t stream);
+}  // namespace msc

@@ -1,0 +1,39 @@
+/* CPU oracle for the MSCEER lower-star discrete gradient (.grad) path.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This is a plain-C restatement of the reference
+ * algorithm used as the checker for the CUDA path: only tests/, bench.py's CPU
+ * baseline legs and __graft_entry__.smoke() may load it.  The product never
+ * links it and never falls back to it.
+ *
+ * Layout: f is float32 with x fastest.  The cell complex has (2X-1)(2Y-1)(2Z-1)
+ * cells (x fastest), one .grad byte per cell (GradBitfield, LSB first:
+ * assigned:1, flag:1, pair:3, ldir:3).
+ */
+#ifndef MSC_ORACLE_H
+#define MSC_ORACLE_H
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Lower-star pairing (assigned + pair bits, ldir=0, flag=0) for every cell. */
+int oracle_lstar_pairs_3d(const float* f, int64_t X, int64_t Y, int64_t Z, uint8_t* grad, int nthreads);
+int oracle_lstar_pairs_2d(const float* f, int64_t X, int64_t Y, uint8_t* grad, int nthreads);
+
+/* Ascending-manifold dimension (ldir bits) on a paired gradient. */
+int oracle_ldir_3d(int64_t X, int64_t Y, int64_t Z, uint8_t* grad);
+int oracle_ldir_2d(int64_t X, int64_t Y, uint8_t* grad);
+
+/* flag bit = (boundaryValue(cell) != 0), as written by outputToFile. */
+int oracle_flag_3d(int64_t X, int64_t Y, int64_t Z, uint8_t* grad);
+int oracle_flag_2d(int64_t X, int64_t Y, uint8_t* grad);
+
+/* The complete .grad file of steepest_lstar (3D) / the 2D builder. */
+int oracle_grad_3d(const float* f, int64_t X, int64_t Y, int64_t Z, uint8_t* grad, int nthreads);
+int oracle_grad_2d(const float* f, int64_t X, int64_t Y, uint8_t* grad, int nthreads);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,153 @@
+// Test-only harness: drives the reference MSCEER classes (compiled from the
+// reference's own headers and src/*.cxx, see oracle/Makefile) and exposes them
+// through a C ABI so the tests can pin the oracle restatement against the real
+// reference.  Never linked into the product and never shipped to the GPU host.
+//
+// Pipelines reproduced (each step calls the reference class named):
+//   ref_steepest_lstar_3d  == steepest_lstar/steepest_lstar.cxx:89-258
+//       RegularGridMaxMinVertexLabeling3D::ComputeOutput   (gi_max_vertex_labeling.h:1119)
+//       SlidingWindowRobinsNoalloc::ComputePairing_sliding (gi_fast_robins_noalloc.h:1254)
+//       TopologicalGradientUsingAlgorithms::setAscendingManifoldDimensions
+//                                                          (gi_topological_gradient_using_algorithms.h:430)
+//       DiscreteGradientLabeling::outputToFile             (gi_discrete_gradient_labeling.h:200)
+//   ref_lstar_grad_2d      == Accurate2D::DiscreteGradientBuilder::ComputeDiscreteGradient
+//       without saddle streamlines (gi_discrete_gradient_computer.h:538-686)
+//
+// The only deviation from the shipped program: the mesh type is a thin subclass of
+// TopologicalRegularGrid3D that adds a no-op cellid2Coords(INDEX_TYPE, Vec2l&)
+// overload.  gi_modified_robins.h:1005-1013 builds an unused vector<Vec2l> through
+// that overload, which the 3D mesh lacks, so the shipped headers do not compile for
+// the 3D mesh.  The overload only feeds that dead vector; no algorithm step changes.
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <string>
+#include <vector>
+#include <queue>
+#include <omp.h>
+
+#include "gi_timing.h"
+#include "gi_topological_explicit_mesh_function.h"
+#include "gi_topological_gradient_using_algorithms.h"
+#include "gi_topological_regular_grid_restricted.h"
+#include "gi_topological_utility_functions.h"
+#include "gi_numeric_integrator_expanding_region_stop.h"
+#include "gi_topological_regular_masked_grid.h"
+#include "gi_topological_regular_masked_restricted_grid.h"
+#include "gi_max_vertex_labeling.h"
+#include "gi_topological_max_vertex_mesh_function.h"
+#include "gi_modified_robins.h"
+#include "gi_fast_robins_noalloc.h"
+#include "gi_discrete_gradient_computer.h"
+
+using namespace GInt;
+
+namespace refharness {
+
+class Mesh3D : public TopologicalRegularGrid3D {
+public:
+	explicit Mesh3D(RegularGrid3D* g) : TopologicalRegularGrid3D(g) {}
+	using TopologicalRegularGrid3D::cellid2Coords;
+	// feeds only the unused vector at gi_modified_robins.h:1005-1013
+	inline void cellid2Coords(INDEX_TYPE, Vec2l& c) const { c[0] = 0; c[1] = 0; }
+};
+
+typedef RegularGrid3D GridType;
+typedef RegularGridTrilinearFunction GridFuncType;
+typedef Mesh3D MeshType;
+typedef DiscreteGradientLabeling<MeshType> GradType;
+typedef RegularGridMaxMinVertexLabeling3D<MeshType, GridFuncType> MaxVLType;
+typedef TopologicalMaxVertexMeshFunction<MeshType, MaxVLType, GridFuncType, float> TopoFuncType;
+typedef SlidingWindowRobinsNoalloc<GridType, GridFuncType, MeshType, MaxVLType, GradType> NewRobinsType;
+
+}  // namespace refharness
+
+extern "C" {
+
+// Runs the steepest_lstar pipeline on an in-memory float32 volume (x fastest) and
+// writes the .grad file with the reference's own writer.  Returns 0 on success.
+// stage_ms (optional, 3 doubles) receives max/min, Robins and ldir wall times.
+int ref_steepest_lstar_3d(const float* f, long long X, long long Y, long long Z,
+                          int nthreads, const char* grad_path, double* stage_ms) {
+	using namespace refharness;
+	if (nthreads > 0) omp_set_num_threads(nthreads);
+	GridType* grid = new GridType(Vec3l(X, Y, Z), Vec3b(0, 0, 0));
+	std::vector<float> img(f, f + X * Y * Z);
+	GridFuncType* func = new GridFuncType(grid, img.data());
+	MeshType* mesh = new MeshType(grid);
+
+	auto t0 = std::chrono::steady_clock::now();
+	MaxVLType* maxv = new MaxVLType(mesh, func);
+	maxv->ComputeOutput();
+	auto t1 = std::chrono::steady_clock::now();
+	TopoFuncType* topofunc = new TopoFuncType();
+	topofunc->setMeshAndFuncAndMaxVLabeling(mesh, func, maxv);
+	GradType* labeling = new GradType(mesh);
+	labeling->ClearAllGradient();
+	NewRobinsType* robins = new NewRobinsType(grid, func, mesh, maxv, labeling);
+	robins->ComputePairing_sliding();
+	auto t2 = std::chrono::steady_clock::now();
+	TopologicalGradientUsingAlgorithms<MeshType, TopoFuncType, GradType>* algs =
+		new TopologicalGradientUsingAlgorithms<MeshType, TopoFuncType, GradType>(topofunc, mesh, labeling);
+	algs->setAscendingManifoldDimensions();
+	auto t3 = std::chrono::steady_clock::now();
+	labeling->outputToFile(grad_path);
+	if (stage_ms) {
+		stage_ms[0] = std::chrono::duration<double, std::milli>(t1 - t0).count();
+		stage_ms[1] = std::chrono::duration<double, std::milli>(t2 - t1).count();
+		stage_ms[2] = std::chrono::duration<double, std::milli>(t3 - t2).count();
+	}
+	delete algs;
+	delete robins;
+	delete labeling;
+	delete topofunc;
+	delete maxv;
+	delete mesh;
+	delete func;
+	delete grid;
+	return 0;
+}
+
+// The 2D lower-star gradient of Accurate2D::DiscreteGradientBuilder with no saddle
+// streamlines requested (gi_discrete_gradient_computer.h:561-583, 681-689).
+int ref_lstar_grad_2d(const float* f, long long X, long long Y, int nthreads,
+                      const char* grad_path, double* stage_ms) {
+	using namespace Accurate2D;
+	if (nthreads > 0) omp_set_num_threads(nthreads);
+	GridType* grid = new GridType(Vec2i((int)X, (int)Y), Vec2b(0, 0));
+	std::vector<float> img(f, f + X * Y);
+	GridFuncType* func = new GridFuncType(grid, img.data());
+	MeshType* mesh = new MeshType(grid);
+	auto t0 = std::chrono::steady_clock::now();
+	MaxVLType* maxv = new MaxVLType(mesh, func);
+	maxv->ComputeOutput();
+	auto t1 = std::chrono::steady_clock::now();
+	MeshFuncType* topofunc = new MeshFuncType();
+	topofunc->setMeshAndFuncAndMaxVLabeling(mesh, func, maxv);
+	GradType* grad = new GradType(mesh);
+	grad->ClearAllGradient();
+	RobinsType* robins = new RobinsType(mesh, maxv, grad);
+	robins->ComputePairing();
+	auto t2 = std::chrono::steady_clock::now();
+	TopologicalGradientUsingAlgorithms<MeshType, MeshFuncType, GradType>* algs =
+		new TopologicalGradientUsingAlgorithms<MeshType, MeshFuncType, GradType>(topofunc, mesh, grad);
+	algs->setAscendingManifoldDimensions();
+	auto t3 = std::chrono::steady_clock::now();
+	grad->outputToFile(grad_path);
+	if (stage_ms) {
+		stage_ms[0] = std::chrono::duration<double, std::milli>(t1 - t0).count();
+		stage_ms[1] = std::chrono::duration<double, std::milli>(t2 - t1).count();
+		stage_ms[2] = std::chrono::duration<double, std::milli>(t3 - t2).count();
+	}
+	delete algs;
+	delete robins;
+	delete grad;
+	delete topofunc;
+	delete maxv;
+	delete mesh;
+	delete func;
+	delete grid;
+	return 0;
+}
+
+}  // extern "C"

@@ -1,0 +1,77 @@
+"""The CPU oracle against the reference's own outputs (no GPU needed)."""
+import hashlib
+import json
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+import oracle_lib
+from msceer_gb300 import fields
+
+GOLDEN = Path(__file__).resolve().parent / "golden"
+
+
+@pytest.mark.parametrize("case", oracle_lib.load_golden_small(), ids=lambda c: c[0])
+def test_oracle_matches_reference_golden(oracle, case):
+    name, f, want = case
+    got = oracle.grad(f, nthreads=2)
+    assert np.array_equal(got, want), oracle_lib.describe_mismatch(got, want, f.shape[::-1])
+
+
+def _regenerate(spec):
+    return eval("fields." + spec["generator"], {"fields": fields})
+
+
+@pytest.mark.parametrize("key", ["gauss16_64", "k3_96x80x72", "k3_2d_512x384"])
+def test_oracle_matches_reference_large_hash(oracle, key):
+    spec = json.loads((GOLDEN / "grad_large.json").read_text())[key]
+    f = _regenerate(spec)
+    if hashlib.sha256(f.tobytes()).hexdigest() != spec["f_sha256"]:
+        pytest.skip("this platform's generator output differs from the fixture's input")
+    g = oracle.grad(f)
+    assert hashlib.sha256(g.tobytes()).hexdigest() == spec["sha256"]
+
+
+def test_oracle_stages_compose(oracle):
+    f = fields.power_law_field((24, 20, 18), seed=11)
+    g = oracle.pairs(f)
+    g = oracle.ldir(g, f.shape[::-1])
+    dims = f.shape[::-1]
+    oracle.lib.oracle_flag_3d(*dims, g.ctypes.data)
+    assert np.array_equal(g, oracle.grad(f))
+
+
+def test_oracle_thread_count_invariant(oracle):
+    f = fields.quantized(fields.power_law_field((40, 33, 29), seed=2), 5)
+    assert np.array_equal(oracle.grad(f, nthreads=1), oracle.grad(f, nthreads=4))
+
+
+def test_comparison_detects_planted_mistake(oracle):
+    """Plant a one-bit mistake in the oracle's output: the parity check must see it."""
+    _, f, want = oracle_lib.load_golden_small()[0]
+    got = oracle.grad(f)
+    got[len(got) // 2] ^= 0x04
+    assert not np.array_equal(got, want)
+    assert "1 cells differ" in oracle_lib.describe_mismatch(got, want, f.shape[::-1])
+
+
+def test_oracle_against_compiled_reference_random():
+    ref = oracle_lib.load_ref()
+    if ref is None:
+        pytest.skip("reference sources not on this machine")
+    orc = oracle_lib.load()
+    rng = np.random.default_rng(1234)
+    for trial in range(12):
+        shape = tuple(int(s) for s in rng.integers(2, 14, size=3))
+        f = rng.standard_normal(shape[::-1]).astype(np.float32)
+        if trial % 2:
+            f = fields.quantized(f, int(rng.integers(2, 6)))
+        want = oracle_lib.ref_grad(ref, f)
+        got = orc.grad(f)
+        assert np.array_equal(got, want), (shape, oracle_lib.describe_mismatch(got, want, shape))
+    for trial in range(6):
+        shape = tuple(int(s) for s in rng.integers(2, 40, size=2))
+        f = fields.quantized(rng.standard_normal(shape[::-1]).astype(np.float32), 3)
+        want = oracle_lib.ref_grad(ref, f)
+        assert np.array_equal(orc.grad(f), want), shape
