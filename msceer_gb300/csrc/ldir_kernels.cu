@@ -16,8 +16,11 @@
 // plus a 2-cell halo in shared memory (every rule reaches at most 2 cells), seeds a
 // shared-memory queue with the marked items, runs the value-2 walk to its local
 // fixpoint, then the value-1 walk, and writes back the tile's changed bytes.  Marks
-// in the halo stay local.  Passes repeat until no byte changes anywhere; paths that
-// leave a tile are picked up by the neighbouring tile's next pass through its halo.
+// in the halo stay local.  The first pass seeds every marked item; later passes only
+// revisit tiles whose halo changed (a neighbour wrote a cell within 2 cells of the
+// shared border) and seed only from the halo, because everything reachable from the
+// interior was already walked.  The closure is complete when a pass changes no cell
+// near any tile border.
 #include "msc_device.cuh"
 
 namespace msc {
@@ -45,6 +48,8 @@ __device__ __forceinline__ void lcoords(int i, int& lx, int& ly, int& lz) {
 
 template <int ND, int TX, int TY, int TZ, int BS>
 __global__ void __launch_bounds__(BS) ldir_pass_kernel(uint8_t* __restrict__ g, const GradDims D,
+                                                       const uint8_t* __restrict__ dirty_in,
+                                                       uint8_t* __restrict__ dirty_out,
                                                        int* __restrict__ changed, int* __restrict__ err) {
   using T = LdirTile<ND, TX, TY, TZ>;
   constexpr int NL = T::NL;
@@ -54,7 +59,7 @@ __global__ void __launch_bounds__(BS) ldir_pass_kernel(uint8_t* __restrict__ g, 
   uint8_t* sg = s_dyn + (size_t)NL * 2;
   uint32_t* s_vis = reinterpret_cast<uint32_t*>(s_dyn + (size_t)NL * 2 + ((NL + 3) / 4) * 4);
   uint32_t* s_dirty = s_vis + T::NW;
-  __shared__ int s_qtail, s_changed;
+  __shared__ int s_qtail, s_border;
 
   const int tid = threadIdx.x;
   const int64_t dX = D.d[0], dY = D.d[1], dZ = D.d[2];
@@ -62,10 +67,13 @@ __global__ void __launch_bounds__(BS) ldir_pass_kernel(uint8_t* __restrict__ g, 
   const int64_t ntz = (ND == 3) ? (dZ + TZ - 1) / TZ : 1;
   const int64_t ntiles = ntx * nty * ntz;
 
+  const bool first = (dirty_in == nullptr);
   for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
-    const int64_t ox = (tile % ntx) * TX - T::H;
-    const int64_t oy = ((tile / ntx) % nty) * TY - T::H;
-    const int64_t oz = (ND == 3) ? (tile / (ntx * nty)) * TZ - T::H : 0;
+    if (!first && !dirty_in[tile]) continue;
+    const int64_t tx = tile % ntx, ty = (tile / ntx) % nty, tz = (ND == 3) ? tile / (ntx * nty) : 0;
+    const int64_t ox = tx * TX - T::H;
+    const int64_t oy = ty * TY - T::H;
+    const int64_t oz = (ND == 3) ? tz * TZ - T::H : 0;
 
     // stage the tile + halo; cells outside the complex read as 0 (unassigned)
     for (int i = tid; i < NL; i += BS) {
@@ -78,7 +86,7 @@ __global__ void __launch_bounds__(BS) ldir_pass_kernel(uint8_t* __restrict__ g, 
       sg[i] = b;
     }
     for (int w = tid; w < T::NW; w += BS) s_dirty[w] = 0;
-    if (tid == 0) s_changed = 0;
+    if (tid == 0) s_border = 0;
 
     // two walks: value 2 over edge items, then value 1 over quad items
 #pragma unroll 1
@@ -88,12 +96,16 @@ __global__ void __launch_bounds__(BS) ldir_pass_kernel(uint8_t* __restrict__ g, 
       for (int w = tid; w < T::NW; w += BS) s_vis[w] = 0;
       if (tid == 0) s_qtail = 0;
       __syncthreads();
-      // seeds: every marked item of this walk in the staged box
+      // seeds: every marked item of this walk in the staged box (first pass), or in
+      // its halo only (later passes: the interior was walked already)
       for (int i = tid; i < NL; i += BS) {
         const uint8_t b = sg[i];
         if (!(b & 1u) || (unsigned)(b >> 5) != value) continue;
         int lx, ly, lz;
         lcoords<T>(i, lx, ly, lz);
+        if (!first && lx >= T::H && lx < T::H + TX && ly >= T::H && ly < T::H + TY &&
+            (ND == 2 || (lz >= T::H && lz < T::H + TZ)))
+          continue;
         const int dim = (int)((ox + lx) & 1) + (int)((oy + ly) & 1) + (ND == 3 ? (int)((oz + lz) & 1) : 0);
         if (dim != item_dim) continue;
         atomicOr(&s_vis[i >> 5], 1u << (i & 31));
@@ -185,10 +197,22 @@ __global__ void __launch_bounds__(BS) ldir_pass_kernel(uint8_t* __restrict__ g, 
       if (ND == 3 && (lz < T::H || lz >= T::H + TZ)) continue;
       const int64_t gx = ox + lx, gy = oy + ly, gz = oz + lz;
       g[gx + gy * D.cs[1] + gz * D.cs[2]] = b;
-      s_changed = 1;
+      // a change within reach (2 cells) of a neighbour's halo reopens that neighbour
+      if (lx < 2 * T::H || lx >= TX || ly < 2 * T::H || ly >= TY || (ND == 3 && (lz < 2 * T::H || lz >= TZ)))
+        s_border = 1;
     }
     __syncthreads();
-    if (tid == 0 && s_changed) atomicOr(changed, 1);
+    if (s_border) {
+      // reopen the existing neighbour tiles for the next pass
+      const int nn = (ND == 3) ? 27 : 9;
+      for (int k = tid; k < nn; k += BS) {
+        const int64_t nx = tx + (k % 3) - 1, ny = ty + (k / 3) % 3 - 1, nz = (ND == 3) ? tz + k / 9 - 1 : 0;
+        if (k == nn / 2 || nx < 0 || nx >= ntx || ny < 0 || ny >= nty || nz < 0 || nz >= ntz) continue;
+        dirty_out[nx + ny * ntx + nz * ntx * nty] = 1;
+      }
+      if (tid == 0) atomicOr(changed, 1);
+    }
+    __syncthreads();
   }
 }
 
@@ -204,8 +228,8 @@ int64_t ldir_num_tiles(int nd, const GradDims& D) {
   return ((D.d[0] + kTX2 - 1) / kTX2) * ((D.d[1] + kTY2 - 1) / kTY2);
 }
 
-cudaError_t launch_ldir_pass(int nd, uint8_t* g, const GradDims& D, int* changed, int* err, int num_sms,
-                             cudaStream_t stream) {
+cudaError_t launch_ldir_pass(int nd, uint8_t* g, const GradDims& D, const uint8_t* dirty_in, uint8_t* dirty_out,
+                             int* changed, int* err, int num_sms, cudaStream_t stream) {
   const int64_t nt = ldir_num_tiles(nd, D);
   const int64_t cap = (int64_t)num_sms * 4;
   const int grid = (int)(nt < cap ? nt : cap);
@@ -215,13 +239,13 @@ cudaError_t launch_ldir_pass(int nd, uint8_t* g, const GradDims& D, int* changed
     const size_t sm = Tile3::smem_bytes();
     cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
     if (e != cudaSuccess) return e;
-    k<<<grid, kBS3, sm, stream>>>(g, D, changed, err);
+    k<<<grid, kBS3, sm, stream>>>(g, D, dirty_in, dirty_out, changed, err);
   } else {
     auto k = ldir_pass_kernel<2, kTX2, kTY2, 1, kBS2>;
     const size_t sm = Tile2::smem_bytes();
     cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
     if (e != cudaSuccess) return e;
-    k<<<grid, kBS2, sm, stream>>>(g, D, changed, err);
+    k<<<grid, kBS2, sm, stream>>>(g, D, dirty_in, dirty_out, changed, err);
   }
   return cudaGetLastError();
 }

@@ -1,0 +1,388 @@
+// Per-vertex lower-star pairing on 27-bit (3D) / 9-bit (2D) neighbourhood masks.
+// Host+device: the CUDA kernel (lstar_kernels.cu) runs it one thread per vertex and
+// the CPU test harness (tests/lstar_core_host.cpp) runs the very same code against
+// the oracle.
+//
+// Neighbourhood position p = (dx+1) + 3(dy+1) + 9(dz+1), offsets in {-1,0,1}: the
+// order of TopologicalRegularGrid3D::AdjacentCellsIterator
+// (gi_topological_regular_grid.h:196-205, 687-790).  The same index names the
+// vertex at vertex offset (dx,dy,dz) and the cell at cell offset (dx,dy,dz) around
+// the centre vertex; a cell's vertices are the positions whose offsets are 0 or
+// equal to the cell's on every axis.
+//
+// HomotopyExpand (gi_fast_robins_noalloc.h:147-321; gi_modified_robins.h:999-1199)
+// restated on sets.  With all lower-dimensional cells processed, a (d+1)-cell c is
+// a pairing candidate for its d-facet q exactly when c is in the class S, not yet
+// processed, and q is its only unprocessed facet in S (num_missing == 1).  Calling
+// those cells "ready" (set R), the reference's restart-from-the-first-cell scan picks
+// the first q, in star order, that is the remaining facet of some ready cell -- the
+// lowest set bit of Q = facets(R) -- and pairs it with the ready cofacet whose lowest
+// vertex comes first (cofacet order +x,-x,+y,-y,+z,-z, first wins ties,
+// PickLowestCandidate :130-143).  With no ready cell, the unprocessed d-cell with the
+// first lowest vertex becomes critical (:293-310).  Each step costs a few dozen bit
+// operations instead of a rescan of the class.
+#pragma once
+#include <cstdint>
+
+#if defined(__CUDACC__)
+#define MSC_HD __host__ __device__ __forceinline__
+#else
+#define MSC_HD inline
+#endif
+
+namespace msc {
+
+MSC_HD int ffs32(uint32_t x) {
+#if defined(__CUDA_ARCH__)
+  return __ffs((int)x);
+#else
+  return __builtin_ffs((int)x);
+#endif
+}
+
+MSC_HD int popc32(uint32_t x) {
+#if defined(__CUDA_ARCH__)
+  return __popc(x);
+#else
+  return __builtin_popcount(x);
+#endif
+}
+
+// The (value, then vertex index) order of IsGreater
+// (gi_regular_grid_trilinear_function.h:309-314): a comes before (is lower than) b.
+// Position order equals global vertex-index order inside a neighbourhood.
+MSC_HD bool before(float fa, int a, float fb, int b) {
+  if (fb > fa) return true;
+  if (fa > fb) return false;
+  return b > a;
+}
+
+template <int ND>
+struct Nb {
+  static constexpr int NPOS = (ND == 3) ? 27 : 9;
+  static constexpr int CENTER = (ND == 3) ? 13 : 4;
+  MSC_HD static constexpr int d(int p, int a) {
+    return a == 0 ? p % 3 - 1 : (a == 1 ? (p / 3) % 3 - 1 : p / 9 - 1);
+  }
+  MSC_HD static constexpr int stride(int a) { return a == 0 ? 1 : (a == 1 ? 3 : 9); }
+  MSC_HD static constexpr int dim(int p) {
+    int s = 0;
+    for (int a = 0; a < ND; a++) s += d(p, a) != 0;
+    return s;
+  }
+  MSC_HD static constexpr uint32_t dim_mask(int k) {
+    uint32_t m = 0;
+    for (int p = 0; p < NPOS; p++)
+      if (dim(p) == k) m |= 1u << p;
+    return m;
+  }
+  MSC_HD static constexpr uint32_t axis_mask(int a, int val) {
+    uint32_t m = 0;
+    if (a >= ND) return val == 0 ? dim_mask(0) | dim_mask(1) | dim_mask(2) | dim_mask(3) : 0u;
+    for (int p = 0; p < NPOS; p++)
+      if (d(p, a) == val) m |= 1u << p;
+    return m;
+  }
+  // vertices of cell p
+  MSC_HD static constexpr uint32_t vertex_mask(int p) {
+    uint32_t m = 0;
+    for (int q = 0; q < NPOS; q++) {
+      bool ok = true;
+      for (int a = 0; a < ND; a++) ok = ok && (d(q, a) == 0 || d(q, a) == d(p, a));
+      if (ok) m |= 1u << q;
+    }
+    return m;
+  }
+  // AND-fold along axis A: keep bit p only if the bit of p with axis A zeroed is set
+  template <int A>
+  MSC_HD static uint32_t fold(uint32_t m) {
+    constexpr int s = stride(A);
+    constexpr uint32_t mp = axis_mask(A, 1), mm = axis_mask(A, -1), m0 = axis_mask(A, 0);
+    return m & (((m << s) & mp) | ((m >> s) & mm) | m0);
+  }
+  // bit c set when c's facet along axis A (the one toward the centre) is in m
+  template <int A>
+  MSC_HD static uint32_t facet_in(uint32_t m) {
+    constexpr int s = stride(A);
+    constexpr uint32_t mp = axis_mask(A, 1), mm = axis_mask(A, -1);
+    return ((m << s) & mp) | ((m >> s) & mm);
+  }
+  // facets along axis A of the cells in r whose A-facet is flagged in f
+  template <int A>
+  MSC_HD static uint32_t facet_of(uint32_t r, uint32_t f) {
+    constexpr int s = stride(A);
+    constexpr uint32_t mp = axis_mask(A, 1), mm = axis_mask(A, -1);
+    return ((r & f & mp) >> s) | ((r & f & mm) << s);
+  }
+};
+
+// Reads the neighbourhood value at a position.  Device: a per-thread column in
+// shared memory; host: a plain array.
+struct ColumnVals {
+  const float* base;
+  int stride;
+  MSC_HD float operator()(int p) const { return base[p * stride]; }
+};
+
+template <int ND, class Vals>
+struct LowerStarState {
+  using N = Nb<ND>;
+  Vals val;
+  const uint32_t* vm;  // vertex masks per position
+  uint32_t P = 0;      // processed cells
+  uint32_t K = 0;      // critical cells
+  uint32_t C0 = 0, C1 = 0, C2 = 0;  // pair-direction code bit-planes
+
+  MSC_HD LowerStarState(Vals v, const uint32_t* vmask) : val(v), vm(vmask) {}
+
+  // Cell2LowestVertex: the first vertex of the cell in the (value, index) order
+  MSC_HD int lowv(int q) const {
+    uint32_t m = vm[q];
+    int best = ffs32(m) - 1;
+    float fb = val(best);
+    m &= m - 1;
+    while (m) {
+      const int p = ffs32(m) - 1;
+      m &= m - 1;
+      const float fp = val(p);
+      if (before(fp, p, fb, best)) {
+        best = p;
+        fb = fp;
+      }
+    }
+    return best;
+  }
+
+  MSC_HD void set_code(int q, int code) {
+    C0 |= (uint32_t)(code & 1) << q;
+    C1 |= (uint32_t)((code >> 1) & 1) << q;
+    C2 |= (uint32_t)((code >> 2) & 1) << q;
+  }
+  // direction code of the pair partner at delta = partner - cell: +x,-x,+y,-y,+z,-z
+  MSC_HD static int dir_code(int delta) {
+    const int ad = delta < 0 ? -delta : delta;
+    return (delta < 0 ? 1 : 0) | (ad == 3 ? 2 : (ad == 9 ? 4 : 0));
+  }
+  MSC_HD void make_pair(int q, int r) {
+    P |= (1u << q) | (1u << r);
+    set_code(q, dir_code(r - q));
+    set_code(r, dir_code(q - r));
+  }
+  MSC_HD void make_critical(int q) {
+    P |= 1u << q;
+    K |= 1u << q;
+  }
+
+  // the cell of U whose lowest vertex comes first (first in star order wins ties)
+  MSC_HD int lowest_of(uint32_t U) const {
+    int q = ffs32(U) - 1;
+    uint32_t W = U & (U - 1);
+    if (W) {
+      int lv = lowv(q);
+      float fl = val(lv);
+      while (W) {
+        const int o = ffs32(W) - 1;
+        W &= W - 1;
+        const int olv = lowv(o);
+        const float fo = val(olv);
+        if (before(fo, olv, fl, lv)) {
+          q = o;
+          lv = olv;
+          fl = fo;
+        }
+      }
+    }
+    return q;
+  }
+
+  // HomotopyExpand of one boundary class S of the lower star.
+  MSC_HD void expand(uint32_t S) {
+    constexpr int C = N::CENTER;
+    constexpr uint32_t EDGES = N::dim_mask(1);
+    if (S & (1u << C)) {
+      // the vertex pairs with the edge to its lowest neighbour (steepest descent)
+      uint32_t E = S & EDGES;
+      if (!E) {
+        make_critical(C);
+      } else {
+        int best = ffs32(E) - 1;
+        float fb = val(best);
+        E &= E - 1;
+        while (E) {
+          const int e = ffs32(E) - 1;
+          E &= E - 1;
+          const float fe = val(e);
+          if (before(fe, e, fb, best)) {
+            best = e;
+            fb = fe;
+          }
+        }
+        make_pair(C, best);
+      }
+    }
+    constexpr uint32_t DM1 = N::dim_mask(1), DM2 = N::dim_mask(2), DM3 = N::dim_mask(3);
+    constexpr uint32_t AX0 = N::axis_mask(0, 0), AX1 = N::axis_mask(1, 0), AX2 = N::axis_mask(2, 0);
+    for (int dd = 1; dd <= ND; dd++) {
+      const uint32_t DMd = dd == 1 ? DM1 : (dd == 2 ? DM2 : DM3);
+      const uint32_t DMu = dd == 1 ? DM2 : (dd == 2 ? DM3 : 0u);
+      uint32_t U = S & DMd & ~P;
+      while (U) {
+        const uint32_t A = S & ~P;  // unprocessed cells of the class
+        const uint32_t F0 = N::template facet_in<0>(A);
+        const uint32_t F1 = N::template facet_in<1>(A);
+        const uint32_t F2 = (ND == 3) ? N::template facet_in<2>(A) : 0u;
+        const uint32_t one = (F0 ^ F1 ^ F2) & ~(F0 & F1 & F2);  // exactly one unprocessed facet
+        const uint32_t R = A & DMu & one;                       // ready (d+1)-cells
+        uint32_t Q = N::template facet_of<0>(R, F0) | N::template facet_of<1>(R, F1);
+        if (ND == 3) Q |= N::template facet_of<2>(R, F2);
+        if (Q) {
+          const int q = ffs32(Q) - 1;
+          int best = -1, bestlv = -1;
+          float fb = 0.f;
+          const uint32_t even[3] = {AX0, AX1, AX2};
+#pragma unroll
+          for (int a = 0; a < ND; a++) {
+            if (!((even[a] >> q) & 1u)) continue;
+#pragma unroll
+            for (int s = 0; s < 2; s++) {
+              const int c = s == 0 ? q + N::stride(a) : q - N::stride(a);
+              if (!((R >> c) & 1u)) continue;
+              if (best < 0) {
+                best = c;
+              } else {
+                if (bestlv < 0) {
+                  bestlv = lowv(best);
+                  fb = val(bestlv);
+                }
+                const int lv = lowv(c);
+                const float fl = val(lv);
+                if (before(fl, lv, fb, bestlv)) {
+                  best = c;
+                  bestlv = lv;
+                  fb = fl;
+                }
+              }
+            }
+          }
+          make_pair(q, best);
+          U &= ~(1u << q);
+        } else {
+          const int q = lowest_of(U);
+          make_critical(q);
+          U &= ~(1u << q);
+        }
+      }
+    }
+  }
+};
+
+template <int ND>
+struct VertexMasks {
+  uint32_t vm[27];
+};
+
+template <int ND>
+constexpr VertexMasks<ND> make_vertex_masks() {
+  VertexMasks<ND> t{};
+  for (int p = 0; p < 27; p++) t.vm[p] = p < Nb<ND>::NPOS ? Nb<ND>::vertex_mask(p) : 0u;
+  return t;
+}
+
+// Lower star from the mask of neighbours that come before the centre: the cells all
+// of whose other vertices are lower (three separable AND-folds).  Out-of-range
+// neighbours are never "lower", so cells outside the complex drop out too.
+template <int ND>
+MSC_HD uint32_t lower_star_mask(uint32_t lower) {
+  using N = Nb<ND>;
+  uint32_t L = lower | (1u << N::CENTER);
+  L = N::template fold<0>(L);
+  L = N::template fold<1>(L);
+  if (ND == 3) L = N::template fold<2>(L);
+  return L;
+}
+
+// Runs every boundary class of one vertex's lower star.  bx/by/bz: the vertex lies
+// on the first or last plane of that axis.  Class k = cells on the boundary of
+// exactly k axes (boundaryValue, gi_topological_regular_grid.h:1291-1297; the split
+// is MyRobinsNoalloc::ComputeLowerStar, gi_modified_robins.h:1305-1324).
+template <int ND, class State>
+MSC_HD uint32_t run_classes(State& st, uint32_t L, bool bx, bool by, bool bz) {
+  using N = Nb<ND>;
+  constexpr uint32_t A0x = N::axis_mask(0, 0), A0y = N::axis_mask(1, 0), A0z = N::axis_mask(2, 0);
+  const uint32_t B0 = bx ? A0x : 0u;
+  const uint32_t B1 = by ? A0y : 0u;
+  const uint32_t B2 = (ND == 3 && bz) ? A0z : 0u;
+  const uint32_t Bany = B0 | B1 | B2;
+  if (!Bany) {
+    st.expand(L);
+  } else {
+    const uint32_t all3 = B0 & B1 & B2;
+    const uint32_t two = ((B0 & B1) | (B0 & B2) | (B1 & B2)) & ~all3;
+    const uint32_t one = (B0 ^ B1 ^ B2) & ~all3;
+    uint32_t c;
+    if ((c = L & ~Bany)) st.expand(c);
+    if ((c = L & one)) st.expand(c);
+    if ((c = L & two)) st.expand(c);
+    if ((c = L & all3)) st.expand(c);
+  }
+  return Bany;
+}
+
+// Final .grad byte of the cell at position p of a processed lower star.
+//   code: 7 if critical, else the (axis-remapped) pair direction
+//   ldir: roots of the ascending-manifold closure -- critical 1-cells 2, critical
+//         2-cells 1, critical 3-cells 0 (gi_topological_gradient_using_algorithms.h:
+//         460-477) -- and 3 everywhere else
+//   flag: cell on the boundary (outputToFile, gi_discrete_gradient_labeling.h:206-211)
+template <int ND, class State>
+MSC_HD uint8_t cell_byte(const State& st, int p, uint32_t Bany, uint32_t enc_map) {
+  const bool crit = (st.K >> p) & 1u;
+  const int lc = (int)(((st.C0 >> p) & 1u) | (((st.C1 >> p) & 1u) << 1) | (((st.C2 >> p) & 1u) << 2));
+  const int code = crit ? 7 : (int)((enc_map >> (3 * lc)) & 7u);
+  const int dimp = Nb<ND>::dim(p);
+  const int ldir = crit ? (dimp == 1 ? 2 : (dimp == 2 ? 1 : (dimp == 3 ? 0 : 3))) : 3;
+  const int flag = (Bany >> p) & 1u;
+  return (uint8_t)(1 | (flag << 1) | (code << 2) | (ldir << 5));
+}
+
+// One vertex, end to end: gather its 3^ND neighbourhood through `load(p)` (returns
+// false outside the grid), write the values to the column `col` (stride `cs`),
+// build the lower star, expand every boundary class and emit each owned cell's
+// byte through `store(p, byte)`.  Returns true if a NaN was seen.
+template <int ND, class Load, class Store>
+MSC_HD bool process_vertex(int64_t x, int64_t y, int64_t z, int64_t X, int64_t Y, int64_t Z, const Load& load,
+                           float* col, int cs, const uint32_t* vm, uint32_t enc_map, const Store& store) {
+  using N = Nb<ND>;
+  constexpr int NPOS = N::NPOS;
+  constexpr int C = N::CENTER;
+  float fc = 0.f;
+  load(C, fc);
+  col[C * cs] = fc;
+  uint32_t lower = 0;
+  bool nan = (fc != fc);
+#pragma unroll
+  for (int p = 0; p < NPOS; p++) {
+    if (p == C) continue;
+    const int dx = N::d(p, 0), dy = N::d(p, 1), dz = (ND == 3) ? N::d(p, 2) : 0;
+    const bool ok = (x + dx >= 0) && (x + dx < X) && (y + dy >= 0) && (y + dy < Y) &&
+                    (ND == 2 || ((z + dz >= 0) && (z + dz < Z)));
+    if (ok) {
+      float v = 0.f;
+      load(p, v);
+      col[p * cs] = v;
+      nan |= (v != v);
+      if (before(v, p, fc, C)) lower |= 1u << p;
+    }
+  }
+  const uint32_t L = lower_star_mask<ND>(lower);
+  LowerStarState<ND, ColumnVals> st(ColumnVals{col, cs}, vm);
+  const uint32_t Bany = run_classes<ND>(st, L, x == 0 || x == X - 1, y == 0 || y == Y - 1,
+                                        ND == 3 && (z == 0 || z == Z - 1));
+#pragma unroll
+  for (int p = 0; p < NPOS; p++) {
+    if ((L >> p) & 1u) store(p, cell_byte<ND>(st, p, Bany, enc_map));
+  }
+  return nan;
+}
+
+}  // namespace msc

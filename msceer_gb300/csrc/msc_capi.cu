@@ -115,20 +115,34 @@ int ldir_impl(int nd, uint8_t* g, const int64_t* dims, cudaStream_t stream, Scra
   msc::GradDims D;
   if (!make_dims(nd, dims, &D)) return fail(MSC_ERR_BAD_DIMS, "invalid dims");
   if (!g) return fail(MSC_ERR_NULL_POINTER, "null buffer");
-  // a path crosses each tile at most once per pass that makes progress, so the
-  // closure converges within (number of tiles + 1) passes
-  const int64_t limit = msc::ldir_num_tiles(nd, D) + 2;
+  const int64_t ntiles = msc::ldir_num_tiles(nd, D);
+  // one "reopened" byte per tile, double-buffered between passes
+  uint8_t* dirty = nullptr;
+  MSC_CUDA(cudaMallocAsync((void**)&dirty, (size_t)(2 * ntiles), stream), "cudaMallocAsync(tile flags)");
+  struct Free {
+    uint8_t* p;
+    cudaStream_t st;
+    ~Free() { cudaFreeAsync(p, st); }
+  } free_dirty{dirty, stream};
+  // a path that needs another pass crosses a tile border, so the closure completes
+  // within (number of tiles + 1) passes
+  const int64_t limit = ntiles + 2;
   const int sms = num_sms();
   int passes = 0;
+  const uint8_t* din = nullptr;
+  uint8_t* dout = dirty;
   while (true) {
     MSC_CUDA(cudaMemsetAsync(s.words + 1, 0, sizeof(int), stream), "reset changed flag");
-    MSC_CUDA(msc::launch_ldir_pass(nd, g, D, s.words + 1, s.words, sms, stream), "ldir kernel launch");
+    MSC_CUDA(cudaMemsetAsync(dout, 0, (size_t)ntiles, stream), "reset tile flags");
+    MSC_CUDA(msc::launch_ldir_pass(nd, g, D, din, dout, s.words + 1, s.words, sms, stream), "ldir kernel launch");
     passes++;
     int changed = 0;
     MSC_CUDA(cudaMemcpyAsync(&changed, s.words + 1, sizeof(int), cudaMemcpyDeviceToHost, stream), "read changed");
     MSC_CUDA(cudaStreamSynchronize(stream), "cudaStreamSynchronize");
     if (!changed) break;
     if (passes >= limit) return fail(MSC_ERR_ITER_LIMIT, "ldir closure did not converge");
+    din = dout;
+    dout = (dout == dirty) ? dirty + ntiles : dirty;
   }
   if (passes_out) *passes_out = passes;
   g_last_passes = passes;

@@ -35,16 +35,6 @@ struct GradDims {
 
 __host__ __device__ inline int map3(uint32_t m, int c) { return (int)((m >> (3 * c)) & 7u); }
 
-// The (value, then vertex index) total order of IsGreater
-// (gi_regular_grid_trilinear_function.h:309-314): true when vertex a comes
-// before (is lower than) vertex b.  Positions a, b index the same 3^ND
-// neighbourhood; position order equals global vertex-index order there.
-__device__ __forceinline__ bool before(float fa, int a, float fb, int b) {
-  if (fb > fa) return true;
-  if (fa > fb) return false;
-  return b > a;
-}
-
 }  // namespace msc
 
 #include <cuda_runtime.h>
@@ -53,6 +43,6 @@ namespace msc {
 cudaError_t launch_lstar(int nd, const float* f, uint8_t* g, const GradDims& D, int* err, int num_sms,
                          cudaStream_t stream);
 int64_t ldir_num_tiles(int nd, const GradDims& D);
-cudaError_t launch_ldir_pass(int nd, uint8_t* g, const GradDims& D, int* changed, int* err, int num_sms,
-                             cudaStream_t stream);
+cudaError_t launch_ldir_pass(int nd, uint8_t* g, const GradDims& D, const uint8_t* dirty_in, uint8_t* dirty_out,
+                             int* changed, int* err, int num_sms, cudaStream_t stream);
 }  // namespace msc
