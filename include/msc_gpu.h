@@ -86,6 +86,18 @@ int msc_lower_star_pairs_2d(const float* f, const int64_t dims[2], uint8_t* grad
 int msc_ascending_manifold_dims_3d(uint8_t* grad, const int64_t dims[3], msc_stream_t stream, int* passes_out);
 int msc_ascending_manifold_dims_2d(uint8_t* grad, const int64_t dims[2], msc_stream_t stream, int* passes_out);
 
+/* Central-difference gradient of the image: RegularGridTrilinearFunction::
+ * ComputeGradFromImage(1) (gi_regular_grid_trilinear_function.h:285-341): per axis
+ * 0.5*(f[+1] - f[-1]) inside, 0 on the first and last plane.  f32 output rounds that
+ * once (within half an ulp of the reference's double); layout 0 stores x,y,z per
+ * vertex (12 bytes), layout 1 x,y,z,0 (16 bytes, one vector load per vertex; 2D:
+ * layout 0 and 1 both store x,y).  The _f64 variants store x,y,z doubles per vertex,
+ * the reference's Vec3d array, bit for bit.  Asynchronous on `stream`. */
+int msc_central_diff_grad_3d(const float* f, const int64_t dims[3], float* g_out, int layout, msc_stream_t stream);
+int msc_central_diff_grad_2d(const float* f, const int64_t dims[2], float* g_out, int layout, msc_stream_t stream);
+int msc_central_diff_grad_3d_f64(const float* f, const int64_t dims[3], double* g_out, msc_stream_t stream);
+int msc_central_diff_grad_2d_f64(const float* f, const int64_t dims[2], double* g_out, msc_stream_t stream);
+
 /* Host-memory convenience with steepest_lstar's semantics: copies f to the GPU,
  * computes, copies the .grad back.  f_host: X*Y*Z floats; grad_host:
  * msc_num_cells_3d(dims) bytes.  Blocking.  Runs on the current device and keeps a

@@ -34,6 +34,10 @@ SIGNATURES = {
     "msc_lower_star_pairs_2d": (ctypes.c_int, [_VP, _I64P, _VP, _VP]),
     "msc_ascending_manifold_dims_3d": (ctypes.c_int, [_VP, _I64P, _VP, ctypes.POINTER(ctypes.c_int)]),
     "msc_ascending_manifold_dims_2d": (ctypes.c_int, [_VP, _I64P, _VP, ctypes.POINTER(ctypes.c_int)]),
+    "msc_central_diff_grad_3d": (ctypes.c_int, [_VP, _I64P, _VP, ctypes.c_int, _VP]),
+    "msc_central_diff_grad_2d": (ctypes.c_int, [_VP, _I64P, _VP, ctypes.c_int, _VP]),
+    "msc_central_diff_grad_3d_f64": (ctypes.c_int, [_VP, _I64P, _VP, _VP]),
+    "msc_central_diff_grad_2d_f64": (ctypes.c_int, [_VP, _I64P, _VP, _VP]),
     "msc_steepest_lstar_host": (ctypes.c_int, [_VP, _I64P, _VP]),
     "msc_lower_star_grad_2d_host": (ctypes.c_int, [_VP, _I64P, _VP]),
 }

@@ -284,6 +284,40 @@ int msc_ascending_manifold_dims_2d(uint8_t* g, const int64_t dims[2], msc_stream
   return rc;
 }
 
+int msc_central_diff_grad_3d(const float* f, const int64_t dims[3], float* g, int layout, msc_stream_t stream) {
+  if (int rc = validate(3, dims, f, g)) return rc;
+  if (layout != 0 && layout != 1) return fail(MSC_ERR_BAD_DIMS, "layout must be 0 (xyz) or 1 (xyzw)");
+  msc::GradDims D;
+  make_dims(3, dims, &D);
+  MSC_CUDA(msc::launch_central_diff(3, layout, f, g, D, num_sms(), (cudaStream_t)stream), "gradient kernel launch");
+  return MSC_OK;
+}
+
+int msc_central_diff_grad_2d(const float* f, const int64_t dims[2], float* g, int layout, msc_stream_t stream) {
+  if (int rc = validate(2, dims, f, g)) return rc;
+  if (layout != 0 && layout != 1) return fail(MSC_ERR_BAD_DIMS, "layout must be 0 (xy) or 1 (xy, 8-byte aligned pairs)");
+  msc::GradDims D;
+  make_dims(2, dims, &D);
+  MSC_CUDA(msc::launch_central_diff(2, layout, f, g, D, num_sms(), (cudaStream_t)stream), "gradient kernel launch");
+  return MSC_OK;
+}
+
+int msc_central_diff_grad_3d_f64(const float* f, const int64_t dims[3], double* g, msc_stream_t stream) {
+  if (int rc = validate(3, dims, f, g)) return rc;
+  msc::GradDims D;
+  make_dims(3, dims, &D);
+  MSC_CUDA(msc::launch_central_diff(3, 2, f, g, D, num_sms(), (cudaStream_t)stream), "gradient kernel launch");
+  return MSC_OK;
+}
+
+int msc_central_diff_grad_2d_f64(const float* f, const int64_t dims[2], double* g, msc_stream_t stream) {
+  if (int rc = validate(2, dims, f, g)) return rc;
+  msc::GradDims D;
+  make_dims(2, dims, &D);
+  MSC_CUDA(msc::launch_central_diff(2, 2, f, g, D, num_sms(), (cudaStream_t)stream), "gradient kernel launch");
+  return MSC_OK;
+}
+
 int msc_steepest_lstar_host(const float* f_host, const int64_t dims[3], uint8_t* grad_host) {
   return host_impl(3, f_host, dims, grad_host);
 }

@@ -45,4 +45,6 @@ cudaError_t launch_lstar(int nd, const float* f, uint8_t* g, const GradDims& D, 
 int64_t ldir_num_tiles(int nd, const GradDims& D);
 cudaError_t launch_ldir_pass(int nd, uint8_t* g, const GradDims& D, const uint8_t* dirty_in, uint8_t* dirty_out,
                              int* changed, int* err, int num_sms, cudaStream_t stream);
+cudaError_t launch_central_diff(int nd, int layout, const float* f, void* out, const GradDims& D, int num_sms,
+                                cudaStream_t stream);
 }  // namespace msc

@@ -441,3 +441,44 @@ int oracle_grad_2d(const float* f, int64_t X, int64_t Y, uint8_t* g, int nt) {
 	if (!rc) rc = oracle_flag_2d(X, Y, g);
 	return rc;
 }
+
+/* RegularGridTrilinearFunction::ComputeGradFromImage(1)
+ * (gi_regular_grid_trilinear_function.h:285-341): per axis the products
+ * kRKCoefficients[k][i] * f (float, src/gi_regular_grid_trilinear_function.cxx:5-11)
+ * summed in double; k = min(1, distance to the boundary) (Gather1DNeighborhood,
+ * gi_regular_grid.h:270-303), so the k = 0 row makes the component 0.0 + 0.0f*f. */
+static double central_component(const float* f, int64_t idx, int64_t coord, int64_t n, int64_t stride) {
+	static const float k1[3] = { -1.0f / 2.0f, 0.0f, 1.0f / 2.0f };
+	int64_t dist = coord < (n - 1 - coord) ? coord : (n - 1 - coord);
+	if (dist < 1) return 0.0 + (double)(0.0f * f[idx]);
+	double r = 0.0;
+	r += (double)(k1[0] * f[idx - stride]);
+	r += (double)(k1[1] * f[idx]);
+	r += (double)(k1[2] * f[idx + stride]);
+	return r;
+}
+
+int oracle_central_diff_3d(const float* f, int64_t X, int64_t Y, int64_t Z, double* g) {
+	if (X < 1 || Y < 1 || Z < 1) return -1;
+	for (int64_t z = 0; z < Z; z++)
+		for (int64_t y = 0; y < Y; y++)
+			for (int64_t x = 0; x < X; x++) {
+				int64_t v = x + X * (y + Y * z);
+				g[3 * v + 0] = central_component(f, v, x, X, 1);
+				g[3 * v + 1] = central_component(f, v, y, Y, X);
+				g[3 * v + 2] = central_component(f, v, z, Z, X * Y);
+			}
+	return 0;
+}
+
+int oracle_central_diff_2d(const float* f, int64_t X, int64_t Y, double* g) {
+	if (X < 1 || Y < 1) return -1;
+	for (int64_t y = 0; y < Y; y++)
+		for (int64_t x = 0; x < X; x++) {
+			int64_t v = x + X * y;
+			g[2 * v + 0] = central_component(f, v, x, X, 1);
+			g[2 * v + 1] = central_component(f, v, y, Y, X);
+		}
+	return 0;
+}
+

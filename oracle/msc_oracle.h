@@ -33,6 +33,28 @@ int oracle_flag_2d(int64_t X, int64_t Y, uint8_t* grad);
 int oracle_grad_3d(const float* f, int64_t X, int64_t Y, int64_t Z, uint8_t* grad, int nthreads);
 int oracle_grad_2d(const float* f, int64_t X, int64_t Y, uint8_t* grad, int nthreads);
 
+/* Central-difference gradient, x,y,z (x,y) doubles per vertex, as the reference's
+ * Vec3d array after ComputeGradFromImage(1). */
+int oracle_central_diff_3d(const float* f, int64_t X, int64_t Y, int64_t Z, double* g);
+int oracle_central_diff_2d(const float* f, int64_t X, int64_t Y, double* g);
+
+/* Integrated labels (msc_labels_oracle.c). */
+typedef struct {
+	float error_threshold;     /* accepted |two half steps - one full step|^2 */
+	float gradient_threshold;  /* stop when |grad f| falls below this */
+	int iteration_limit;       /* Euler steps per streamline */
+	double max_step;           /* MAX_STEP_IN_GRID_CELLS */
+	float presimp_threshold;   /* persistence up to which extrema merge */
+} oracle_label_params;
+
+/* Certain terminal regions grown from the (merged) extrema; dir -1 ASC, +1 DSC. */
+int oracle_terminal_regions_3d(const float* f, const uint8_t* grad, int64_t X, int64_t Y, int64_t Z, int dir,
+                               float presimp_threshold, int32_t* labels);
+/* Full labeling chain; dirs bit 0 ASC, bit 1 DSC (DSC after ASC on the shared gradient). */
+int oracle_labels_3d(const float* f, const uint8_t* grad, int64_t X, int64_t Y, int64_t Z, int dirs,
+                     const oracle_label_params* P, int32_t* labels_asc, int32_t* labels_dsc,
+                     int32_t* stage_labels);
+
 #ifdef __cplusplus
 }
 #endif

@@ -39,6 +39,9 @@
 #include "gi_modified_robins.h"
 #include "gi_fast_robins_noalloc.h"
 #include "gi_discrete_gradient_computer.h"
+#include "gi_extrema_region_builder.h"
+#include "gi_numeric_integrator_path_compressing.h"
+#include "gi_isolated_region_remover.h"
 
 using namespace GInt;
 
@@ -148,6 +151,109 @@ int ref_lstar_grad_2d(const float* f, long long X, long long Y, int nthreads,
 	delete func;
 	delete grid;
 	return 0;
+}
+
+// RegularGridTrilinearFunction::ComputeGradFromImage(1) on an in-memory volume;
+// writes the Vec3d gradient array (3 doubles per vertex).
+int ref_central_diff_3d(const float* f, long long X, long long Y, long long Z, double* out) {
+	RegularGrid3D* grid = new RegularGrid3D(Vec3l(X, Y, Z), Vec3b(0, 0, 0));
+	std::vector<float> img(f, f + X * Y * Z);
+	RegularGridTrilinearFunction* func = new RegularGridTrilinearFunction(grid, img.data());
+	func->ComputeGradFromImage(1);
+	const long long n = X * Y * Z;
+	for (long long v = 0; v < n; v++) {
+		Vec3d gv = func->SampleGrad(Vec3l(v % X, (v / X) % Y, v / (X * Y)));
+		out[3 * v + 0] = gv[0];
+		out[3 * v + 1] = gv[1];
+		out[3 * v + 2] = gv[2];
+	}
+	delete func;
+	delete grid;
+	return 0;
+}
+
+// ondemandaccurate's ASC and DSC 3-manifold labels (ondemandaccurate.cxx:795-948)
+// with one OpenMP thread, which makes the reference deterministic.  Labels are the
+// reference's unique-id numbers mapped to the smallest seed vertex of their region
+// (the reference draws the numbers from unordered_map order).  stage (optional, 4*N):
+// terminal and integrated labels, ASC then DSC, mapped the same way.
+int ref_labels_3d(const float* f, long long X, long long Y, long long Z, float error_threshold,
+                  float gradient_threshold, int iteration_limit, float presimp, int* asc, int* dsc, int* stage) {
+	using namespace refharness;
+	typedef IndexCompareLessThan<GridFuncType> ComparerASC;
+	typedef IndexCompareGreaterThan<GridFuncType> ComparerDSC;
+	typedef NumericIntegratorPathCompressingToTerminal<AdaptiveEulerAdvector3D<GridFuncType, -1>, GridFuncType> IntASC;
+	typedef NumericIntegratorPathCompressingToTerminal<AdaptiveEulerAdvector3D<GridFuncType, 1>, GridFuncType> IntDSC;
+	omp_set_num_threads(1);
+	GridType* grid = new GridType(Vec3l(X, Y, Z), Vec3b(0, 0, 0));
+	std::vector<float> img(f, f + X * Y * Z);
+	GridFuncType* func = new GridFuncType(grid, img.data());
+	MeshType* mesh = new MeshType(grid);
+	MaxVLType* maxv = new MaxVLType(mesh, func);
+	maxv->ComputeOutput();
+	TopoFuncType* topofunc = new TopoFuncType();
+	topofunc->setMeshAndFuncAndMaxVLabeling(mesh, func, maxv);
+	GradType* labeling = new GradType(mesh);
+	labeling->ClearAllGradient();
+	NewRobinsType* robins = new NewRobinsType(grid, func, mesh, maxv, labeling);
+	robins->ComputePairing_sliding();
+	func->ComputeGradFromImage(1);
+	SimplifiedExtremumGraph<MeshType, TopoFuncType, GradType>* seg =
+		new SimplifiedExtremumGraph<MeshType, TopoFuncType, GradType>(mesh, topofunc, labeling);
+	seg->SetMode(SimplifiedExtremumGraph<MeshType, TopoFuncType, GradType>::EXTGRAPHMODE::BOTH);
+	seg->ComputeMinMapFromGradient(presimp);
+	const long long N = X * Y * Z;
+
+	auto canon = [&](const std::unordered_map<INT_TYPE, std::vector<INDEX_TYPE> >& idmap, DenseLabeling<int>* terminal) {
+		std::unordered_map<int, long long> c;
+		for (auto& kv : idmap) {
+			long long mn = -1;
+			for (auto v : kv.second) if (mn < 0 || v < mn) mn = v;
+			c[terminal->GetLabel(kv.second[0])] = mn;
+		}
+		return c;
+	};
+	auto write = [&](int* out, DenseLabeling<int>* lab, std::unordered_map<int, long long>& c) {
+		for (long long v = 0; v < N; v++) {
+			int l = lab->GetLabel(v);
+			out[v] = (l < 0) ? -1 : (int)c[l];
+		}
+	};
+
+	{
+		std::unordered_map<INDEX_TYPE, INT_TYPE> ext;
+		for (auto p : seg->mMinGraph->mCellIndexToListIdMap) ext[p.first] = seg->mMinGraph->Representative(p.second);
+		GridSimplifiedExtremalRegionBuilder<ComparerASC, GridFuncType, MeshType>* rb =
+			new GridSimplifiedExtremalRegionBuilder<ComparerASC, GridFuncType, MeshType>(func, grid, mesh);
+		rb->BeginIntegration(ext);
+		auto c = canon(rb->GetIdMap(), rb->GetOutputLabels());
+		if (stage) write(stage, rb->GetOutputLabels(), c);
+		IntASC* integ = new IntASC(func, grid, error_threshold, gradient_threshold, iteration_limit);
+		integ->BeginIntegration(rb->GetIdMap(), rb->GetOutputLabels(), false);
+		if (stage) write(stage + N, integ->GetOutputLabels(), c);
+		IsolatedCCRegionRemoverNEW<ComparerASC, GridFuncType>* cl =
+			new IsolatedCCRegionRemoverNEW<ComparerASC, GridFuncType>(func, integ->GetOutputLabels());
+		cl->ComputeOutput();
+		write(asc, integ->GetOutputLabels(), c);
+	}
+	{
+		std::unordered_map<INDEX_TYPE, INT_TYPE> ext;
+		for (auto p : seg->mMaxGraph->mCellIndexToListIdMap)
+			ext[maxv->Cell2HighestVertex(p.first)] = seg->mMaxGraph->Representative(p.second);
+		GridSimplifiedExtremalRegionBuilder<ComparerDSC, GridFuncType, MeshType>* rb =
+			new GridSimplifiedExtremalRegionBuilder<ComparerDSC, GridFuncType, MeshType>(func, grid, mesh);
+		rb->BeginIntegration(ext);
+		auto c = canon(rb->GetIdMap(), rb->GetOutputLabels());
+		if (stage) write(stage + 2 * N, rb->GetOutputLabels(), c);
+		IntDSC* integ = new IntDSC(func, grid, error_threshold, gradient_threshold, iteration_limit);
+		integ->BeginIntegration(rb->GetIdMap(), rb->GetOutputLabels(), false);
+		if (stage) write(stage + 3 * N, integ->GetOutputLabels(), c);
+		IsolatedCCRegionRemoverNEW<ComparerDSC, GridFuncType>* cl =
+			new IsolatedCCRegionRemoverNEW<ComparerDSC, GridFuncType>(func, integ->GetOutputLabels());
+		cl->ComputeOutput();
+		write(dsc, integ->GetOutputLabels(), c);
+	}
+	return 0;   // the reference objects are left to the process (their destructors double-free shared labels)
 }
 
 }  // extern "C"

@@ -18,6 +18,16 @@ _I64 = ctypes.c_int64
 _VP = ctypes.c_void_p
 
 
+class LabelParams(ctypes.Structure):
+    """oracle_label_params (oracle/msc_oracle.h)."""
+    _fields_ = [("error_threshold", ctypes.c_float), ("gradient_threshold", ctypes.c_float),
+                ("iteration_limit", ctypes.c_int), ("max_step", ctypes.c_double),
+                ("presimp_threshold", ctypes.c_float)]
+
+
+STAGES = ("asc_terminal", "asc_integrated", "dsc_terminal", "dsc_integrated")
+
+
 class Oracle:
     def __init__(self, lib):
         self.lib = lib
@@ -29,6 +39,37 @@ class Oracle:
         lib.oracle_ldir_2d.argtypes = [_I64, _I64, _VP]
         lib.oracle_flag_3d.argtypes = [_I64, _I64, _I64, _VP]
         lib.oracle_flag_2d.argtypes = [_I64, _I64, _VP]
+        lib.oracle_central_diff_3d.argtypes = [_VP, _I64, _I64, _I64, _VP]
+        lib.oracle_central_diff_2d.argtypes = [_VP, _I64, _I64, _VP]
+        lib.oracle_labels_3d.argtypes = [_VP, _VP, _I64, _I64, _I64, ctypes.c_int, ctypes.POINTER(LabelParams),
+                                         _VP, _VP, _VP]
+        lib.oracle_terminal_regions_3d.argtypes = [_VP, _VP, _I64, _I64, _I64, ctypes.c_int, ctypes.c_float, _VP]
+
+    def labels(self, f, grad, error_threshold, gradient_threshold, iteration_limit, max_step, presimp):
+        """ASC and DSC labels (regions named by their smallest seed vertex) plus stages."""
+        f = np.ascontiguousarray(f, dtype=np.float32)
+        n = f.size
+        asc = np.empty(n, np.int32)
+        dsc = np.empty(n, np.int32)
+        st = np.empty(4 * n, np.int32)
+        p = LabelParams(error_threshold, gradient_threshold, iteration_limit, max_step, presimp)
+        rc = self.lib.oracle_labels_3d(f.ctypes.data, grad.ctypes.data, *f.shape[::-1], 3, ctypes.byref(p),
+                                       asc.ctypes.data, dsc.ctypes.data, st.ctypes.data)
+        assert rc == 0
+        out = {"asc": asc, "dsc": dsc}
+        for i, k in enumerate(STAGES):
+            out[k] = st[i * n:(i + 1) * n]
+        return out
+
+    def central_diff(self, f: np.ndarray) -> np.ndarray:
+        """(..., ND) float64 gradient, the reference's Vec3d array."""
+        f = np.ascontiguousarray(f, dtype=np.float32)
+        g = np.empty(f.shape + (f.ndim,), dtype=np.float64)
+        if f.ndim == 3:
+            assert self.lib.oracle_central_diff_3d(f.ctypes.data, *f.shape[::-1], g.ctypes.data) == 0
+        else:
+            assert self.lib.oracle_central_diff_2d(f.ctypes.data, *f.shape[::-1], g.ctypes.data) == 0
+        return g
 
     def grad(self, f: np.ndarray, nthreads: int = 0) -> np.ndarray:
         f = np.ascontiguousarray(f, dtype=np.float32)
@@ -77,7 +118,26 @@ def load_ref():
                                           ctypes.c_int, ctypes.c_char_p, _VP]
     lib.ref_lstar_grad_2d.argtypes = [_VP, ctypes.c_longlong, ctypes.c_longlong, ctypes.c_int,
                                       ctypes.c_char_p, _VP]
+    lib.ref_central_diff_3d.argtypes = [_VP, ctypes.c_longlong, ctypes.c_longlong, ctypes.c_longlong, _VP]
+    lib.ref_labels_3d.argtypes = [_VP, ctypes.c_longlong, ctypes.c_longlong, ctypes.c_longlong, ctypes.c_float,
+                                  ctypes.c_float, ctypes.c_int, ctypes.c_float, _VP, _VP, _VP]
     return lib
+
+
+def ref_labels(lib, f, error_threshold, gradient_threshold, iteration_limit, presimp):
+    """The reference's ondemandaccurate ASC/DSC labels at one thread (built with
+    MAX_STEP_IN_GRID_CELLS = 0.25), regions named by their smallest seed vertex."""
+    f = np.ascontiguousarray(f, dtype=np.float32)
+    n = f.size
+    asc = np.empty(n, np.int32)
+    dsc = np.empty(n, np.int32)
+    st = np.empty(4 * n, np.int32)
+    assert lib.ref_labels_3d(f.ctypes.data, *f.shape[::-1], error_threshold, gradient_threshold, iteration_limit,
+                             presimp, asc.ctypes.data, dsc.ctypes.data, st.ctypes.data) == 0
+    out = {"asc": asc, "dsc": dsc}
+    for i, k in enumerate(STAGES):
+        out[k] = st[i * n:(i + 1) * n]
+    return out
 
 
 def ref_grad(lib, f: np.ndarray, nthreads: int = 4) -> np.ndarray:

@@ -75,3 +75,39 @@ def test_oracle_against_compiled_reference_random():
         f = fields.quantized(rng.standard_normal(shape[::-1]).astype(np.float32), 3)
         want = oracle_lib.ref_grad(ref, f)
         assert np.array_equal(orc.grad(f), want), shape
+
+
+def test_central_diff_oracle_against_reference(oracle):
+    ref = oracle_lib.load_ref()
+    if ref is None:
+        pytest.skip("reference sources not on this machine")
+    for shape in [(5, 4, 3), (1, 7, 2), (33, 20, 17), (2, 2, 2)]:
+        f = fields.power_law_field(shape, seed=4)
+        f.flat[::7] *= -1.0
+        want = np.zeros(f.shape + (3,))
+        ref.ref_central_diff_3d(f.ctypes.data, *shape, want.ctypes.data)
+        got = oracle.central_diff(f)
+        assert np.array_equal(got.view(np.uint64), want.view(np.uint64)), shape
+
+
+def test_central_diff_oracle_boundary_zero(oracle):
+    f = fields.gaussian_sum((9, 8, 7), 3, seed=1)
+    g = oracle.central_diff(f)
+    assert (g[0, :, :, 2] == 0).all() and (g[-1, :, :, 2] == 0).all()
+    assert (g[:, :, 0, 0] == 0).all() and (g[:, :, -1, 0] == 0).all()
+    x = 3
+    assert g[4, 4, x, 0] == 0.5 * float(f[4, 4, x + 1]) - 0.5 * float(f[4, 4, x - 1])
+
+
+def test_label_oracle_against_compiled_reference(oracle):
+    """The FP64 labeling oracle equals the single-thread reference at every stage."""
+    ref = oracle_lib.load_ref()
+    if ref is None:
+        pytest.skip("reference sources not on this machine")
+    for f in (fields.gaussian_sum((14, 12, 10), 4, seed=1), fields.power_law_field((16, 15, 13), seed=2),
+              fields.gaussian_sum((30, 28, 26), 8, seed=3)):
+        gt = 1e-6 * float(np.abs(f).max())
+        want = oracle_lib.ref_labels(ref, f, 1e-4, gt, 4000, 0.0)
+        got = oracle.labels(f, oracle.grad(f), 1e-4, gt, 4000, 0.25, 0.0)
+        for k in want:
+            assert np.array_equal(got[k], want[k]), (f.shape, k, int((got[k] != want[k]).sum()))
