@@ -46,6 +46,82 @@ __device__ __forceinline__ void lcoords(int i, int& lx, int& ly, int& lz) {
   lz = i / (T::LX * T::LY);
 }
 
+// Walk one item: visit its cofacets (CofacetsIterator order), mark them, follow
+// their partners.  Returns one newly reached item for the calling thread to chase
+// and queues any further ones.  All coordinates are local to the staged box, whose
+// origin is even on every axis, so local parity is the cell's dimension parity.
+template <class T, int ND>
+struct LdirWalk {
+  uint8_t* sg;
+  uint16_t* sq;
+  uint32_t* vis;
+  uint32_t* dirty;
+  int* qtail;
+  int* err;
+  int lmin[3], lmax[3];  // in-complex local range per axis
+  uint32_t dec_map;
+
+  __device__ __forceinline__ void touch(int c) { atomicOr(&dirty[c >> 5], 1u << (c & 31)); }
+
+  __device__ __forceinline__ int step(int i, int phase) {
+    const unsigned value = phase == 0 ? 2u : 1u;
+    int l[3];
+    lcoords<T>(i, l[0], l[1], l[2]);
+    constexpr int LE[3] = {T::LX, T::LY, T::LZ};
+    int next = -1;
+#pragma unroll
+    for (int a = 0; a < ND; a++) {
+      if (l[a] & 1) continue;  // cofacets only along even axes
+#pragma unroll
+      for (int s = 0; s < 2; s++) {
+        const int sgn = s == 0 ? 1 : -1;  // +axis first
+        const int la = l[a] + sgn;
+        if (la < lmin[a] || la >= lmax[a]) continue;
+        const int t = i + sgn * T::ls(a);
+        const uint8_t bt = sg[t];
+        const unsigned code = (bt >> 2) & 7u;
+        if (!(bt & 1u) || code == 7u) continue;  // unassigned or critical
+        if (phase == 0) {
+          if ((bt >> 5) == 3u) { sg[t] = (uint8_t)((bt & 0x1Fu) | (2u << 5)); touch(t); }
+        } else {
+          if ((bt >> 5) != 1u) { sg[t] = (uint8_t)((bt & 0x1Fu) | (1u << 5)); touch(t); }
+        }
+        const int pc = map3(dec_map, (int)code);
+        const int pa = pc >> 1, psg = (pc & 1) ? -1 : 1;
+        int lp[3] = {l[0], l[1], l[2]};
+        lp[a] += sgn;
+        lp[pa] += psg;
+        if (lp[pa] < 0 || lp[pa] >= LE[pa]) continue;  // partner outside the box
+        const int tp = t + psg * T::ls(pa);
+        if (tp == i) continue;
+        const uint8_t bp = sg[tp];
+        if (phase == 0) {
+          if ((bp >> 5) != 3u) continue;  // already marked: seeded or queued
+          const int pdim = (lp[0] & 1) + (lp[1] & 1) + (ND == 3 ? (lp[2] & 1) : 0);
+          if (pdim != 1) {  // a hex: the path ends here
+            sg[tp] = (uint8_t)((bp & 0x1Fu) | (2u << 5));
+            touch(tp);
+            continue;
+          }
+        } else {
+          if ((bp >> 5) == 1u) continue;
+        }
+        const uint32_t bit = 1u << (tp & 31);
+        if (atomicOr(&vis[tp >> 5], bit) & bit) continue;
+        sg[tp] = (uint8_t)((bp & 0x1Fu) | (value << 5));
+        touch(tp);
+        if (next < 0) {
+          next = tp;
+        } else {
+          const int slot = atomicAdd(qtail, 1);
+          if (slot < T::NL) sq[slot] = (uint16_t)tp; else atomicOr(err, kErrLocalQueue);
+        }
+      }
+    }
+    return next;
+  }
+};
+
 template <int ND, int TX, int TY, int TZ, int BS>
 __global__ void __launch_bounds__(BS) ldir_pass_kernel(uint8_t* __restrict__ g, const GradDims D,
                                                        const uint8_t* __restrict__ dirty_in,
@@ -54,156 +130,130 @@ __global__ void __launch_bounds__(BS) ldir_pass_kernel(uint8_t* __restrict__ g, 
   using T = LdirTile<ND, TX, TY, TZ>;
   constexpr int NL = T::NL;
   static_assert(NL < 65536, "local ids are 16-bit");
+  static_assert(TX % 2 == 0 && TY % 2 == 0 && (ND == 2 || TZ % 2 == 0) && T::H % 2 == 0, "box origins must be even");
   extern __shared__ __align__(16) unsigned char s_dyn[];
   uint16_t* sq = reinterpret_cast<uint16_t*>(s_dyn);
   uint8_t* sg = s_dyn + (size_t)NL * 2;
   uint32_t* s_vis = reinterpret_cast<uint32_t*>(s_dyn + (size_t)NL * 2 + ((NL + 3) / 4) * 4);
   uint32_t* s_dirty = s_vis + T::NW;
-  __shared__ int s_qtail, s_border;
+  __shared__ int s_qtail, s_qseed, s_border;
 
-  const int tid = threadIdx.x;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  constexpr int NWARPS = BS / 32;
   const int64_t dX = D.d[0], dY = D.d[1], dZ = D.d[2];
   const int64_t ntx = (dX + TX - 1) / TX, nty = (dY + TY - 1) / TY;
   const int64_t ntz = (ND == 3) ? (dZ + TZ - 1) / TZ : 1;
   const int64_t ntiles = ntx * nty * ntz;
-
   const bool first = (dirty_in == nullptr);
+
+  LdirWalk<T, ND> W;
+  W.sg = sg;
+  W.sq = sq;
+  W.vis = s_vis;
+  W.dirty = s_dirty;
+  W.qtail = &s_qtail;
+  W.err = err;
+  W.dec_map = D.dec_map;
+
   for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
     if (!first && !dirty_in[tile]) continue;
     const int64_t tx = tile % ntx, ty = (tile / ntx) % nty, tz = (ND == 3) ? tile / (ntx * nty) : 0;
-    const int64_t ox = tx * TX - T::H;
-    const int64_t oy = ty * TY - T::H;
-    const int64_t oz = (ND == 3) ? tz * TZ - T::H : 0;
-
-    // stage the tile + halo; cells outside the complex read as 0 (unassigned)
-    for (int i = tid; i < NL; i += BS) {
-      int lx, ly, lz;
-      lcoords<T>(i, lx, ly, lz);
-      const int64_t gx = ox + lx, gy = oy + ly, gz = oz + lz;
-      uint8_t b = 0;
-      if (gx >= 0 && gx < dX && gy >= 0 && gy < dY && gz >= 0 && gz < dZ)
-        b = g[gx + gy * D.cs[1] + gz * D.cs[2]];
-      sg[i] = b;
+    const int64_t o[3] = {tx * TX - T::H, ty * TY - T::H, (ND == 3) ? tz * TZ - T::H : 0};
+    const int64_t dd[3] = {dX, dY, dZ};
+    constexpr int LE[3] = {T::LX, T::LY, T::LZ};
+#pragma unroll
+    for (int a = 0; a < 3; a++) {
+      W.lmin[a] = (int)(o[a] < 0 ? -o[a] : 0);
+      const int64_t hi = dd[a] - o[a];
+      W.lmax[a] = (int)(hi < LE[a] ? hi : LE[a]);
     }
-    for (int w = tid; w < T::NW; w += BS) s_dirty[w] = 0;
-    if (tid == 0) s_border = 0;
+    if (tid == 0) {
+      s_qtail = 0;
+      s_qseed = NL;
+      s_border = 0;
+    }
+    for (int w = tid; w < T::NW; w += BS) {
+      s_vis[w] = 0;
+      s_dirty[w] = 0;
+    }
+    __syncthreads();
 
-    // two walks: value 2 over edge items, then value 1 over quad items
+    // stage the box row by row (cells outside the complex read as 0 = unassigned)
+    // and collect the seeds: marked items of both walks (first pass), or of the
+    // halo only (later passes: the interior was walked already)
+    for (int row = warp; row < T::LY * T::LZ; row += NWARPS) {
+      const int ly = row % T::LY, lz = row / T::LY;
+      const bool rin = ly >= W.lmin[1] && ly < W.lmax[1] && lz >= W.lmin[2] && lz < W.lmax[2];
+      const uint8_t* grow = g + ((o[1] + ly) * D.cs[1] + (o[2] + lz) * D.cs[2] + o[0]);
+      const bool row_halo = ly < T::H || ly >= T::H + TY || (ND == 3 && (lz < T::H || lz >= T::H + TZ));
+      for (int lx = lane; lx < T::LX; lx += 32) {
+        const int i = lx + T::LX * row;
+        uint8_t b = 0;
+        if (rin && lx >= W.lmin[0] && lx < W.lmax[0]) b = grow[lx];
+        sg[i] = b;
+        if (!(b & 1u)) continue;
+        const unsigned ld = b >> 5;
+        const int dim = (lx & 1) + (ly & 1) + (ND == 3 ? (lz & 1) : 0);
+        if (!first && !(row_halo || lx < T::H || lx >= T::H + TX)) continue;
+        if (dim == 1 && ld == 2u) {
+          atomicOr(&s_vis[i >> 5], 1u << (i & 31));
+          sq[atomicAdd(&s_qtail, 1)] = (uint16_t)i;
+        } else if (dim == 2 && ld == 1u) {
+          sq[atomicSub(&s_qseed, 1) - 1] = (uint16_t)i;
+        }
+      }
+    }
+    __syncthreads();
+
+    // value-2 walk, then value-1 walk; a thread chases the first partner it reaches
+    // and queues the rest, so chains cost no barriers
 #pragma unroll 1
     for (int phase = 0; phase < 2; phase++) {
-      const int item_dim = phase == 0 ? 1 : 2;
-      const unsigned value = phase == 0 ? 2u : 1u;
-      for (int w = tid; w < T::NW; w += BS) s_vis[w] = 0;
-      if (tid == 0) s_qtail = 0;
-      __syncthreads();
-      // seeds: every marked item of this walk in the staged box (first pass), or in
-      // its halo only (later passes: the interior was walked already)
-      for (int i = tid; i < NL; i += BS) {
-        const uint8_t b = sg[i];
-        if (!(b & 1u) || (unsigned)(b >> 5) != value) continue;
-        int lx, ly, lz;
-        lcoords<T>(i, lx, ly, lz);
-        if (!first && lx >= T::H && lx < T::H + TX && ly >= T::H && ly < T::H + TY &&
-            (ND == 2 || (lz >= T::H && lz < T::H + TZ)))
-          continue;
-        const int dim = (int)((ox + lx) & 1) + (int)((oy + ly) & 1) + (ND == 3 ? (int)((oz + lz) & 1) : 0);
-        if (dim != item_dim) continue;
-        atomicOr(&s_vis[i >> 5], 1u << (i & 31));
-        sq[atomicAdd(&s_qtail, 1)] = (uint16_t)i;
-      }
-      __syncthreads();
-      int start = 0;
-#pragma unroll 1
-      while (true) {
-        const int end = s_qtail;
+      int lo = phase == 0 ? 0 : s_qseed;
+      int hi = phase == 0 ? s_qtail : NL;
+      if (phase == 1) {
         __syncthreads();
-        if (start == end) break;
-        for (int k = start + tid; k < end; k += BS) {
-          const int i = sq[k];
-          int lc[3];
-          lcoords<T>(i, lc[0], lc[1], lc[2]);
-          const int64_t gc[3] = {ox + lc[0], oy + lc[1], oz + lc[2]};
-          const int lext[3] = {T::LX, T::LY, T::LZ};
-#pragma unroll
-          for (int a = 0; a < ND; a++) {
-            if (gc[a] & 1) continue;  // cofacets only along even axes
-#pragma unroll
-            for (int s = 0; s < 2; s++) {
-              const int sgn = s == 0 ? 1 : -1;  // +axis first, as CofacetsIterator
-              const int64_t ga = gc[a] + sgn;
-              const int la = lc[a] + sgn;
-              if (ga < 0 || ga >= D.d[a] || la < 0 || la >= lext[a]) continue;
-              const int t = i + sgn * T::ls(a);
-              const uint8_t bt = sg[t];
-              const unsigned code = (bt >> 2) & 7u;
-              if (!(bt & 1u) || code == 7u) continue;  // unassigned or critical
-              // the cofacet itself is marked whatever its partner is
-              if (phase == 0) {
-                // t is a quad: 3 -> 2; a 1 from the value-1 walk is final
-                if ((bt >> 5) == 3u) {
-                  sg[t] = (uint8_t)((bt & 0x1Fu) | (2u << 5));
-                  atomicOr(&s_dirty[t >> 5], 1u << (t & 31));
-                }
-              } else {
-                // t is a hex: -> 1
-                if ((bt >> 5) != 1u) {
-                  sg[t] = (uint8_t)((bt & 0x1Fu) | (1u << 5));
-                  atomicOr(&s_dirty[t >> 5], 1u << (t & 31));
-                }
-              }
-              // pair(t): decode the stored direction to the true axis
-              const int pc = map3(D.dec_map, (int)code);
-              const int pa = pc >> 1, psg = (pc & 1) ? -1 : 1;
-              int lpc[3] = {lc[0], lc[1], lc[2]};
-              lpc[a] += sgn;
-              lpc[pa] += psg;
-              if (lpc[pa] < 0 || lpc[pa] >= lext[pa]) continue;  // partner outside the box
-              const int tp = t + psg * T::ls(pa);
-              if (tp == i) continue;
-              const uint8_t bp = sg[tp];
-              if (phase == 0) {
-                if ((bp >> 5) != 3u) continue;  // already marked: seeded or queued
-                const int pdim = (int)((gc[0] + (lpc[0] - lc[0])) & 1) + (int)((gc[1] + (lpc[1] - lc[1])) & 1) +
-                                 (ND == 3 ? (int)((gc[2] + (lpc[2] - lc[2])) & 1) : 0);
-                if (pdim != 1) {
-                  sg[tp] = (uint8_t)((bp & 0x1Fu) | (2u << 5));  // hex: the path ends here
-                  atomicOr(&s_dirty[tp >> 5], 1u << (tp & 31));
-                  continue;
-                }
-              } else {
-                if ((bp >> 5) == 1u) continue;
-              }
-              const uint32_t bit = 1u << (tp & 31);
-              if (atomicOr(&s_vis[tp >> 5], bit) & bit) continue;
-              sg[tp] = (uint8_t)((bp & 0x1Fu) | (value << 5));
-              atomicOr(&s_dirty[tp >> 5], 1u << (tp & 31));
-              const int slot = atomicAdd(&s_qtail, 1);
-              if (slot < NL) sq[slot] = (uint16_t)tp; else atomicOr(err, kErrLocalQueue);
-            }
-          }
+        for (int w = tid; w < T::NW; w += BS) s_vis[w] = 0;
+        __syncthreads();
+        for (int k = lo + tid; k < hi; k += BS) atomicOr(&s_vis[sq[k] >> 5], 1u << (sq[k] & 31));
+        if (tid == 0) s_qtail = 0;
+        __syncthreads();
+      }
+#pragma unroll 1
+      while (lo < hi) {
+        for (int k = lo + tid; k < hi; k += BS) {
+          int it = sq[k];
+          while (it >= 0) it = W.step(it, phase);
         }
         __syncthreads();
-        start = end;
+        // the first value-1 wave came from the seed region; later waves from 0
+        const int nlo = (phase == 1 && hi == NL) ? 0 : hi;
+        const int nhi = s_qtail;
+        __syncthreads();
+        lo = nlo;
+        hi = nhi;
       }
     }
+    __syncthreads();
 
-    // write back the tile interior
-    for (int i = tid; i < NL; i += BS) {
-      if (!((s_dirty[i >> 5] >> (i & 31)) & 1u)) continue;
-      const uint8_t b = sg[i];
-      int lx, ly, lz;
-      lcoords<T>(i, lx, ly, lz);
-      if (lx < T::H || lx >= T::H + TX || ly < T::H || ly >= T::H + TY) continue;
-      if (ND == 3 && (lz < T::H || lz >= T::H + TZ)) continue;
-      const int64_t gx = ox + lx, gy = oy + ly, gz = oz + lz;
-      g[gx + gy * D.cs[1] + gz * D.cs[2]] = b;
-      // a change within reach (2 cells) of a neighbour's halo reopens that neighbour
-      if (lx < 2 * T::H || lx >= TX || ly < 2 * T::H || ly >= TY || (ND == 3 && (lz < 2 * T::H || lz >= TZ)))
-        s_border = 1;
+    // write back the changed interior cells
+    for (int w = tid; w < T::NW; w += BS) {
+      uint32_t m = s_dirty[w];
+      while (m) {
+        const int i = w * 32 + __ffs(m) - 1;
+        m &= m - 1;
+        int lx, ly, lz;
+        lcoords<T>(i, lx, ly, lz);
+        if (lx < T::H || lx >= T::H + TX || ly < T::H || ly >= T::H + TY) continue;
+        if (ND == 3 && (lz < T::H || lz >= T::H + TZ)) continue;
+        g[(o[0] + lx) + (o[1] + ly) * D.cs[1] + (o[2] + lz) * D.cs[2]] = sg[i];
+        // a change within reach (2 cells) of a neighbour's halo reopens that neighbour
+        if (lx < 2 * T::H || lx >= TX || ly < 2 * T::H || ly >= TY || (ND == 3 && (lz < 2 * T::H || lz >= TZ)))
+          s_border = 1;
+      }
     }
     __syncthreads();
     if (s_border) {
-      // reopen the existing neighbour tiles for the next pass
       const int nn = (ND == 3) ? 27 : 9;
       for (int k = tid; k < nn; k += BS) {
         const int64_t nx = tx + (k % 3) - 1, ny = ty + (k / 3) % 3 - 1, nz = (ND == 3) ? tz + k / 9 - 1 : 0;

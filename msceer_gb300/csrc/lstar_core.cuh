@@ -239,10 +239,10 @@ struct LowerStarState {
           const int q = ffs32(Q) - 1;
           int best = -1, bestlv = -1;
           float fb = 0.f;
-          const uint32_t even[3] = {AX0, AX1, AX2};
 #pragma unroll
           for (int a = 0; a < ND; a++) {
-            if (!((even[a] >> q) & 1u)) continue;
+            const uint32_t even = a == 0 ? AX0 : (a == 1 ? AX1 : AX2);
+            if (!((even >> q) & 1u)) continue;
 #pragma unroll
             for (int s = 0; s < 2; s++) {
               const int c = s == 0 ? q + N::stride(a) : q - N::stride(a);
@@ -345,13 +345,15 @@ MSC_HD uint8_t cell_byte(const State& st, int p, uint32_t Bany, uint32_t enc_map
   return (uint8_t)(1 | (flag << 1) | (code << 2) | (ldir << 5));
 }
 
-// One vertex, end to end: gather its 3^ND neighbourhood through `load(p)` (returns
-// false outside the grid), write the values to the column `col` (stride `cs`),
-// build the lower star, expand every boundary class and emit each owned cell's
-// byte through `store(p, byte)`.  Returns true if a NaN was seen.
+// One vertex, end to end: gather its 3^ND neighbourhood through `load(p)`, write the
+// values to the column `col` (stride `cs`), build the lower star, expand every
+// boundary class and emit each owned cell's byte through `store(p, byte)`.
+// `interior`: the vertex is at least one vertex away from every face (no bounds
+// checks, a single boundary class).  Returns true if a NaN was seen.
 template <int ND, class Load, class Store>
-MSC_HD bool process_vertex(int64_t x, int64_t y, int64_t z, int64_t X, int64_t Y, int64_t Z, const Load& load,
-                           float* col, int cs, const uint32_t* vm, uint32_t enc_map, const Store& store) {
+MSC_HD bool process_vertex(int64_t x, int64_t y, int64_t z, int64_t X, int64_t Y, int64_t Z, bool interior,
+                           const Load& load, float* col, int cs, const uint32_t* vm, uint32_t enc_map,
+                           const Store& store) {
   using N = Nb<ND>;
   constexpr int NPOS = N::NPOS;
   constexpr int C = N::CENTER;
@@ -360,13 +362,28 @@ MSC_HD bool process_vertex(int64_t x, int64_t y, int64_t z, int64_t X, int64_t Y
   col[C * cs] = fc;
   uint32_t lower = 0;
   bool nan = (fc != fc);
+  if (interior) {
 #pragma unroll
-  for (int p = 0; p < NPOS; p++) {
-    if (p == C) continue;
-    const int dx = N::d(p, 0), dy = N::d(p, 1), dz = (ND == 3) ? N::d(p, 2) : 0;
-    const bool ok = (x + dx >= 0) && (x + dx < X) && (y + dy >= 0) && (y + dy < Y) &&
-                    (ND == 2 || ((z + dz >= 0) && (z + dz < Z)));
-    if (ok) {
+    for (int p = 0; p < NPOS; p++) {
+      if (p == C) continue;
+      float v = 0.f;
+      load(p, v);
+      col[p * cs] = v;
+      nan |= (v != v);
+      if (before(v, p, fc, C)) lower |= 1u << p;
+    }
+  } else {
+    // out-of-range neighbours are left out of `lower`, so no cell outside the
+    // complex enters the lower star
+    const uint32_t okx = (x > 0 ? N::axis_mask(0, -1) : 0u) | N::axis_mask(0, 0) | (x < X - 1 ? N::axis_mask(0, 1) : 0u);
+    const uint32_t oky = (y > 0 ? N::axis_mask(1, -1) : 0u) | N::axis_mask(1, 0) | (y < Y - 1 ? N::axis_mask(1, 1) : 0u);
+    const uint32_t okz = (ND == 2) ? ~0u
+                                   : ((z > 0 ? N::axis_mask(2, -1) : 0u) | N::axis_mask(2, 0) |
+                                      (z < Z - 1 ? N::axis_mask(2, 1) : 0u));
+    const uint32_t ok = okx & oky & okz;
+#pragma unroll
+    for (int p = 0; p < NPOS; p++) {
+      if (p == C || !((ok >> p) & 1u)) continue;
       float v = 0.f;
       load(p, v);
       col[p * cs] = v;
@@ -376,11 +393,39 @@ MSC_HD bool process_vertex(int64_t x, int64_t y, int64_t z, int64_t X, int64_t Y
   }
   const uint32_t L = lower_star_mask<ND>(lower);
   LowerStarState<ND, ColumnVals> st(ColumnVals{col, cs}, vm);
-  const uint32_t Bany = run_classes<ND>(st, L, x == 0 || x == X - 1, y == 0 || y == Y - 1,
-                                        ND == 3 && (z == 0 || z == Z - 1));
+  uint32_t Bany = 0;
+  if (interior)
+    st.expand(L);
+  else
+    Bany = run_classes<ND>(st, L, x == 0 || x == X - 1, y == 0 || y == Y - 1, ND == 3 && (z == 0 || z == Z - 1));
+  // byte bit-planes: assigned | flag | pair code (7 if critical) | ldir, where ldir
+  // is 2 / 1 / 0 for critical 1- / 2- / 3-cells and 3 otherwise
+  constexpr uint32_t D0 = N::dim_mask(0), D1 = N::dim_mask(1), D2 = N::dim_mask(2);
+  const uint32_t K = st.K;
+  uint32_t p0 = st.C0, p1 = st.C1, p2 = st.C2;
+  if (enc_map != 0x2C688u) {  // not the identity (0,1,2,3,4,5): remap the non-critical codes
+    uint32_t q0 = 0, q1 = 0, q2 = 0;
+    uint32_t m = L & ~K;
+    while (m) {
+      const int p = ffs32(m) - 1;
+      m &= m - 1;
+      const int lc = (int)(((p0 >> p) & 1u) | (((p1 >> p) & 1u) << 1) | (((p2 >> p) & 1u) << 2));
+      const uint32_t e = (enc_map >> (3 * lc)) & 7u;
+      q0 |= (e & 1u) << p;
+      q1 |= ((e >> 1) & 1u) << p;
+      q2 |= ((e >> 2) & 1u) << p;
+    }
+    p0 = q0; p1 = q1; p2 = q2;
+  }
+  p0 |= K; p1 |= K; p2 |= K;
+  const uint32_t l0 = ~K | (K & (D0 | D2));
+  const uint32_t l1 = ~K | (K & (D0 | D1));
 #pragma unroll
   for (int p = 0; p < NPOS; p++) {
-    if ((L >> p) & 1u) store(p, cell_byte<ND>(st, p, Bany, enc_map));
+    if (!((L >> p) & 1u)) continue;
+    const uint32_t b = 1u | (((Bany >> p) & 1u) << 1) | (((p0 >> p) & 1u) << 2) | (((p1 >> p) & 1u) << 3) |
+                       (((p2 >> p) & 1u) << 4) | (((l0 >> p) & 1u) << 5) | (((l1 >> p) & 1u) << 6);
+    store(p, (uint8_t)b);
   }
   return nan;
 }

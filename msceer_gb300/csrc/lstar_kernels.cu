@@ -26,8 +26,9 @@ namespace msc {
 __constant__ VertexMasks<3> c_vm3 = make_vertex_masks<3>();
 __constant__ VertexMasks<2> c_vm2 = make_vertex_masks<2>();
 
-// Block = BS threads = 32 consecutive x by BS/32 (y,z) rows; grid-stride over
-// (x-block, row-block) pairs.
+// Block = 32 consecutive x by BS/32 consecutive y at one z; grid (x-blocks,
+// y-blocks, z), looping over z when Z exceeds the grid's z extent.  Neighbour and
+// cell offsets are 32-bit; only the per-vertex base addresses are 64-bit.
 template <int ND, int BS>
 __global__ void __launch_bounds__(BS) lstar_kernel(const float* __restrict__ f, uint8_t* __restrict__ g,
                                                    const GradDims D, int* __restrict__ err) {
@@ -41,41 +42,34 @@ __global__ void __launch_bounds__(BS) lstar_kernel(const float* __restrict__ f, 
   __syncthreads();
 
   const int64_t X = D.v[0], Y = D.v[1], Z = D.v[2];
-  const int64_t nrows = Y * Z;
-  const int64_t xblocks = (X + 31) / 32;
-  const int64_t nblocks = xblocks * ((nrows + ROWS - 1) / ROWS);
-  const int lane = tid & 31, row = tid >> 5;
-  const int64_t cs1 = D.cs[1], cs2 = D.cs[2];
+  const int x = blockIdx.x * 32 + (tid & 31);
+  const int y = blockIdx.y * ROWS + (tid >> 5);
+  if (x >= X || y >= Y) return;
+  const int sX = (int)X, sXY = (int)(X * Y);
+  const int c1 = (int)D.cs[1], c2 = (int)D.cs[2];
   float* col = s_val + tid;
   bool nan = false;
-
-  for (int64_t blk = blockIdx.x; blk < nblocks; blk += gridDim.x) {
-    const int64_t x = (blk % xblocks) * 32 + lane;
-    const int64_t r = (blk / xblocks) * ROWS + row;
-    if (x >= X || r >= nrows) continue;
-    const int64_t y = r % Y, z = r / Y;
-    const float* fv = f + (x + X * r);
-    uint8_t* gc = g + (2 * x + 2 * y * cs1 + 2 * z * cs2);
-    const int64_t XY = X * Y;
-    auto load = [&](int p, float& v) {
-      v = __ldg(fv + N::d(p, 0) + N::d(p, 1) * X + ((ND == 3) ? N::d(p, 2) : 0) * XY);
-    };
-    auto store = [&](int p, uint8_t b) {
-      gc[N::d(p, 0) + N::d(p, 1) * cs1 + ((ND == 3) ? N::d(p, 2) : 0) * cs2] = b;
-    };
-    nan |= process_vertex<ND>(x, y, z, X, Y, Z, load, col, BS, s_vm, D.enc_map, store);
+  for (int64_t z = blockIdx.z; z < Z; z += gridDim.z) {
+    const float* fv = f + (x + X * (y + Y * z));
+    uint8_t* gc = g + (2 * (int64_t)x + 2 * (int64_t)y * D.cs[1] + 2 * z * D.cs[2]);
+    auto load = [&](int p, float& v) { v = __ldg(fv + (N::d(p, 0) + N::d(p, 1) * sX + (ND == 3 ? N::d(p, 2) : 0) * sXY)); };
+    auto store = [&](int p, uint8_t b) { gc[N::d(p, 0) + N::d(p, 1) * c1 + (ND == 3 ? N::d(p, 2) : 0) * c2] = b; };
+    const bool interior = x > 0 && x < X - 1 && y > 0 && y < Y - 1 && (ND == 2 || (z > 0 && z < Z - 1));
+    nan |= process_vertex<ND>(x, y, z, X, Y, Z, interior, load, col, BS, s_vm, D.enc_map, store);
   }
-  if (__any_sync(0xffffffffu, nan) && (tid & 31) == 0) atomicOr(err, kErrNaN);
+  if (nan) atomicOr(err, kErrNaN);
 }
 
 cudaError_t launch_lstar(int nd, const float* f, uint8_t* g, const GradDims& D, int* err, int num_sms,
                          cudaStream_t stream) {
+  (void)num_sms;
   constexpr int BS = 128;
-  const int64_t rows = D.v[1] * D.v[2];
-  const int64_t nblocks = ((D.v[0] + 31) / 32) * ((rows + BS / 32 - 1) / (BS / 32));
-  const int64_t cap = (int64_t)num_sms * 16;
-  const int grid = (int)(nblocks < cap ? nblocks : cap);
-  if (grid <= 0) return cudaSuccess;
+  if (D.v[0] > (int64_t)1 << 30 || D.v[1] > (int64_t)1 << 30 || D.v[0] * D.v[1] > ((int64_t)1 << 31) - 1 ||
+      D.cs[2] > ((int64_t)1 << 31) - 1)
+    return cudaErrorInvalidValue;  // a z-plane of cells must be addressable with 32-bit offsets
+  const dim3 grid((unsigned)((D.v[0] + 31) / 32), (unsigned)((D.v[1] + BS / 32 - 1) / (BS / 32)),
+                  (unsigned)(D.v[2] < 65535 ? D.v[2] : 65535));
+  if (grid.y > 65535u) return cudaErrorInvalidValue;
   if (nd == 3)
     lstar_kernel<3, BS><<<grid, BS, 0, stream>>>(f, g, D, err);
   else

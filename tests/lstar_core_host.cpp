@@ -24,7 +24,8 @@ static int run(const float* f, int64_t X, int64_t Y, int64_t Z, uint8_t* g, uint
         auto store = [&](int p, uint8_t b) {
           gc[N::d(p, 0) + N::d(p, 1) * cs1 + (ND == 3 ? N::d(p, 2) : 0) * cs2] = b;
         };
-        nan |= msc::process_vertex<ND>(x, y, z, X, Y, Z, load, col, 1, vm.vm, enc_map, store);
+        const bool interior = x > 0 && x < X - 1 && y > 0 && y < Y - 1 && (ND == 2 || (z > 0 && z < Z - 1));
+        nan |= msc::process_vertex<ND>(x, y, z, X, Y, Z, interior, load, col, 1, vm.vm, enc_map, store);
       }
   return nan;
 }
