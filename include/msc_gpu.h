@@ -98,6 +98,40 @@ int msc_central_diff_grad_2d(const float* f, const int64_t dims[2], float* g_out
 int msc_central_diff_grad_3d_f64(const float* f, const int64_t dims[3], double* g_out, msc_stream_t stream);
 int msc_central_diff_grad_2d_f64(const float* f, const int64_t dims[2], double* g_out, msc_stream_t stream);
 
+/* Parameters of the integrated labels (the ondemandaccurate arguments,
+ * ondemandaccurate.cxx:159-175, plus the step bound MAX_STEP_IN_GRID_CELLS). */
+typedef struct {
+  float error_threshold;     /* accept two half steps when |difference|^2 < this (e.g. 1e-4) */
+  float gradient_threshold;  /* stop where the interpolated |grad f| falls below this */
+  int iteration_limit;       /* Euler steps per streamline (e.g. 4000) */
+  float max_step;            /* largest step, in voxels (reference default 0.5) */
+  float presimp_threshold;   /* extrema joined by a saddle of lower persistence merge (0 = none) */
+} msc_integ_params;
+
+/* Ascending (minima basins) and descending (maxima mountains) 3-manifold labels of
+ * ondemandaccurate (ondemandaccurate.cxx:795-948): extremum graph
+ * (SimplifiedExtremumGraph, gi_extrema_region_builder.h:271-565), certain terminal
+ * regions (GridSimplifiedExtremalRegionBuilder, :753-1045), path-compressing
+ * adaptive-Euler integration of the central-difference gradient
+ * (NumericIntegratorPathCompressingToTerminal, gi_numeric_integrator_path_compressing.h:
+ * 75-433) and the isolated-region cleaner (IsolatedCCRegionRemoverNEW,
+ * gi_isolated_region_remover.h:17-196).  f: device, X*Y*Z floats; grad: the device
+ * .grad of msc_lower_star_grad_3d; labels_*: device int32 per vertex or NULL to skip
+ * a direction (the descending pass runs after the ascending one on the gradient the
+ * ascending pass zeroed at the minima, as the reference does).  A label is the
+ * vertex id of its region's extremum (smallest seed vertex of a merged group), -1
+ * for none.  The first integration pass runs in FP32; vertices next to a label
+ * boundary are re-decided in FP64 with the reference's arithmetic.  Blocking. */
+int msc_integrated_labels_3d(const float* f, const uint8_t* grad, const int64_t dims[3], const msc_integ_params* params,
+                             int32_t* labels_asc, int32_t* labels_dsc, msc_stream_t stream);
+/* Same, also writing 4*X*Y*Z stage labels: terminal and integrated (before the
+ * cleaner), ascending then descending.  For validation. */
+int msc_integrated_labels_3d_stages(const float* f, const uint8_t* grad, const int64_t dims[3],
+                                    const msc_integ_params* params, int32_t* labels_asc, int32_t* labels_dsc,
+                                    int32_t* stages, msc_stream_t stream);
+/* Error text of the last failed labeling call on the calling thread. */
+const char* msc_labels_last_error_string(void);
+
 /* Host-memory convenience with steepest_lstar's semantics: copies f to the GPU,
  * computes, copies the .grad back.  f_host: X*Y*Z floats; grad_host:
  * msc_num_cells_3d(dims) bytes.  Blocking.  Runs on the current device and keeps a

@@ -10,6 +10,7 @@ from .api import (  # noqa: F401
     TopologicalRegularGrid2D,
     TopologicalRegularGrid3D,
     ascending_manifold_dims,
+    integrated_labels,
     lower_star_grad,
     lower_star_pairs,
     num_cells,

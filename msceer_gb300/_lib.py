@@ -38,9 +38,19 @@ SIGNATURES = {
     "msc_central_diff_grad_2d": (ctypes.c_int, [_VP, _I64P, _VP, ctypes.c_int, _VP]),
     "msc_central_diff_grad_3d_f64": (ctypes.c_int, [_VP, _I64P, _VP, _VP]),
     "msc_central_diff_grad_2d_f64": (ctypes.c_int, [_VP, _I64P, _VP, _VP]),
+    "msc_integrated_labels_3d": (ctypes.c_int, [_VP, _VP, _I64P, _VP, _VP, _VP, _VP]),
+    "msc_integrated_labels_3d_stages": (ctypes.c_int, [_VP, _VP, _I64P, _VP, _VP, _VP, _VP, _VP]),
+    "msc_labels_last_error_string": (ctypes.c_char_p, []),
     "msc_steepest_lstar_host": (ctypes.c_int, [_VP, _I64P, _VP]),
     "msc_lower_star_grad_2d_host": (ctypes.c_int, [_VP, _I64P, _VP]),
 }
+
+
+class IntegParams(ctypes.Structure):
+    """msc_integ_params (include/msc_gpu.h)."""
+    _fields_ = [("error_threshold", ctypes.c_float), ("gradient_threshold", ctypes.c_float),
+                ("iteration_limit", ctypes.c_int), ("max_step", ctypes.c_float),
+                ("presimp_threshold", ctypes.c_float)]
 
 
 class MscError(RuntimeError):
@@ -76,5 +86,6 @@ def dims_arg(dims) -> ctypes.Array:
 
 def check(rc: int, fn: str) -> None:
     if rc != MSC_OK:
-        msg = load().msc_last_error_string().decode(errors="replace")
-        raise MscError(rc, fn, msg)
+        lib = load()
+        err = lib.msc_labels_last_error_string if "labels" in fn else lib.msc_last_error_string
+        raise MscError(rc, fn, err().decode(errors="replace"))

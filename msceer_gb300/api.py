@@ -111,6 +111,51 @@ def ascending_manifold_dims(grad, dims) -> int:
     return passes.value
 
 
+def integrated_labels(f, grad, error_threshold=1e-4, gradient_threshold=None, iteration_limit=4000,
+                      max_step=0.25, presimp_threshold=0.0, ascending=True, descending=True, stages=False):
+    """ondemandaccurate's ascending / descending 3-manifold labels of a device volume.
+
+    ``f``: CUDA float32 (Z, Y, X); ``grad``: its .grad from :func:`lower_star_grad`.
+    ``gradient_threshold`` defaults to 1e-6 of max|f|.  Returns a dict with "asc" and/or
+    "dsc" int32 tensors (a label is the vertex id of the region's extremum, -1 none)
+    and, with ``stages``, the terminal / integrated labels of each direction."""
+    import torch
+
+    if not (f.is_cuda and grad.is_cuda):
+        raise ValueError("integrated_labels takes CUDA tensors")
+    f = f.contiguous()
+    dims = _shape_dims(f.shape)
+    if len(dims) != 3:
+        raise ValueError("integrated labels are defined for 3D volumes")
+    if gradient_threshold is None:
+        gradient_threshold = 1e-6 * float(f.abs().max())
+    p = _lib.IntegParams(error_threshold, gradient_threshold, iteration_limit, max_step, presimp_threshold)
+    n = f.numel()
+    asc = torch.empty(n, dtype=torch.int32, device=f.device) if ascending else None
+    dsc = torch.empty(n, dtype=torch.int32, device=f.device) if descending else None
+    st = torch.empty(4 * n, dtype=torch.int32, device=f.device) if stages else None
+    lib = _lib.load()
+    stream = torch.cuda.current_stream(f.device).cuda_stream
+    ptr = lambda t: ctypes.c_void_p(t.data_ptr()) if t is not None else None  # noqa: E731
+    with torch.cuda.device(f.device):
+        if stages:
+            rc = lib.msc_integrated_labels_3d_stages(ptr(f), ptr(grad), _lib.dims_arg(dims), ctypes.byref(p),
+                                                     ptr(asc), ptr(dsc), ptr(st), ctypes.c_void_p(stream))
+        else:
+            rc = lib.msc_integrated_labels_3d(ptr(f), ptr(grad), _lib.dims_arg(dims), ctypes.byref(p), ptr(asc),
+                                              ptr(dsc), ctypes.c_void_p(stream))
+    _lib.check(rc, "msc_integrated_labels_3d")
+    out = {}
+    if asc is not None:
+        out["asc"] = asc
+    if dsc is not None:
+        out["dsc"] = dsc
+    if stages:
+        for i, k in enumerate(("asc_terminal", "asc_integrated", "dsc_terminal", "dsc_integrated")):
+            out[k] = st[i * n:(i + 1) * n]
+    return out
+
+
 class TopologicalRegularGrid3D:
     """Cell-complex index algebra of a non-periodic X x Y x Z vertex grid."""
 

@@ -1,0 +1,491 @@
+// K4: numerical streamline integration to destination labels, and the K5c cleaner.
+//
+// NumericIntegratorPathCompressingToTerminal::BeginIntegration
+// (gi_numeric_integrator_path_compressing.h:75-433) with AdaptiveEulerAdvector3D
+// (gi_adaptive_euler_advector.h:51-305):
+//   pass 1   every unassigned vertex integrates (FP32) until its nearest vertex is
+//            assigned or terminal, runs out of gradient or of iterations; every vertex
+//            it passed takes the destination label (path compression).  One streamline
+//            per thread; the vertices are visited in the reference's spread order so
+//            early paths compress later ones.
+//   fix-up   vertices with a differently labelled 6-neighbour re-integrate until a
+//            certain terminal region, in FP64 with the reference's operation order
+//            (explicit _rn intrinsics: no contraction), so that basin boundaries are
+//            decided as the FP64 oracle decides them; changed labels reopen their
+//            neighbours, in waves to a fixpoint.
+// IsolatedCCRegionRemoverNEW::ComputeOutput (gi_isolated_region_remover.h:155-192):
+//   same-label 6-connected components by a lock-free union-find whose roots are the
+//   components' first vertices in the walk order; every component that does not hold
+//   its region's extremum joins the component of its first earlier neighbour from
+//   another region; chains resolve by pointer jumping.
+#include "label_common.cuh"
+
+namespace msc {
+
+enum { EV_NONE = 0, EV_OUT_OF_VOXEL, EV_OVER_MAX_ITERATIONS, EV_LOW_GRADIENT, EV_HIT_EXTREMUM, EV_HIT_PREASSIGNED };
+
+struct IntegParams {
+  float ethresh, gthresh;
+  int iteration_limit;
+  double max_step;
+  int step_mult;  // -1: flow downhill (ascending manifolds of minima), +1 uphill
+};
+
+__device__ __forceinline__ int64_t vid(const VolDims& V, int64_t x, int64_t y, int64_t z) { return x + V.X * (y + V.Y * z); }
+
+// ---- FP32 advector (pass 1) ------------------------------------------------------------
+
+struct F3 {
+  float x, y, z;
+};
+__device__ __forceinline__ F3 lerp3(F3 a, F3 b, float t) {
+  const float u = 1.f - t;
+  return {a.x * u + b.x * t, a.y * u + b.y * t, a.z * u + b.z * t};
+}
+__device__ __forceinline__ float clampf_ext(float v, int64_t n) {
+  if (v < 0.f) v = 0.f;
+  if (v >= (float)n) v = (float)n - 1.f;
+  return v;
+}
+
+struct Adv32 {
+  const float4* G;
+  VolDims V;
+  IntegParams P;
+  const int32_t* lab;  // pass-1 stop: nearest vertex labelled (assigned or terminal)
+
+  __device__ __forceinline__ F3 corner(int64_t x, int64_t y, int64_t z) const {
+    const float4 g = __ldg(G + vid(V, x, y, z));
+    return {g.x, g.y, g.z};
+  }
+  __device__ __forceinline__ void surround(const int64_t b[3], bool clamp, F3 c[8]) const {
+    int64_t vv[3][2];
+    const int64_t ext[3] = {V.X, V.Y, V.Z};
+#pragma unroll
+    for (int a = 0; a < 3; a++) {
+      vv[a][0] = b[a];
+      vv[a][1] = b[a] + 1;
+      if (clamp) {
+        if (b[a] < 0) vv[a][0] = 0;
+        if (b[a] >= ext[a] - 1) vv[a][0] = vv[a][1] = ext[a] - 1;
+      }
+    }
+#pragma unroll
+    for (int n = 0; n < 8; n++) c[n] = corner(vv[0][n & 1], vv[1][(n >> 1) & 1], vv[2][n >> 2]);
+  }
+  __device__ __forceinline__ static F3 trilin(F3 s, const int64_t b[3], const F3 c[8]) {
+    const float fx = s.x - (float)b[0], fy = s.y - (float)b[1], fz = s.z - (float)b[2];
+    const F3 x0 = lerp3(c[0], c[1], fx), x1 = lerp3(c[2], c[3], fx), x2 = lerp3(c[4], c[5], fx), x3 = lerp3(c[6], c[7], fx);
+    return lerp3(lerp3(x0, x1, fy), lerp3(x2, x3, fy), fz);
+  }
+  // Vec3l(p + 0.5), clamped into the grid (the reference clamps only near the
+  // boundary, where its own points can leave it; elsewhere clamping changes nothing)
+  __device__ __forceinline__ int64_t nearest(F3 p, bool) const {
+    return vid(V, (int64_t)clampf_ext(p.x + 0.5f, V.X), (int64_t)clampf_ext(p.y + 0.5f, V.Y),
+               (int64_t)clampf_ext(p.z + 0.5f, V.Z));
+  }
+  __device__ int advect(F3& cur, int& iters, bool nearb) const {
+    F3 c[8];
+    F3 old = cur;
+    int64_t b[3];
+    if (nearb) {
+      b[0] = (int64_t)clampf_ext(cur.x, V.X);
+      b[1] = (int64_t)clampf_ext(cur.y, V.Y);
+      b[2] = (int64_t)clampf_ext(cur.z, V.Z);
+    } else {
+      b[0] = (int64_t)fminf(fmaxf(cur.x, 0.f), (float)(V.X - 2));
+      b[1] = (int64_t)fminf(fmaxf(cur.y, 0.f), (float)(V.Y - 2));
+      b[2] = (int64_t)fminf(fmaxf(cur.z, 0.f), (float)(V.Z - 2));
+    }
+    surround(b, nearb, c);
+    F3 g = trilin(cur, b, c);
+    float gm = sqrtf(g.x * g.x + g.y * g.y + g.z * g.z);
+    if (!(gm > 0.f) || !isfinite(gm)) return EV_LOW_GRADIENT;  // no direction to follow
+    const float ms = (float)P.max_step;
+    float step = ms / gm;
+    while (iters-- > 0) {
+      if (!(old.x == cur.x && old.y == cur.y && old.z == cur.z)) {
+        if ((int)cur.x != (int)old.x || (int)cur.y != (int)old.y || (int)cur.z != (int)old.z) return EV_OUT_OF_VOXEL;
+        g = trilin(cur, b, c);
+        gm = sqrtf(g.x * g.x + g.y * g.y + g.z * g.z);
+        if (!(gm > 0.f) || !isfinite(gm)) return EV_LOW_GRADIENT;
+        if (gm * step > ms) step = ms / gm;
+        old = cur;
+      }
+      if (gm < P.gthresh) return EV_LOW_GRADIENT;
+      const float sm = (float)P.step_mult * step;
+      const F3 e1 = {g.x * sm, g.y * sm, g.z * sm};
+      const float hs = sm * 0.5f;
+      const F3 hd = {g.x * hs, g.y * hs, g.z * hs};
+      const F3 hg = trilin({cur.x + hd.x, cur.y + hd.y, cur.z + hd.z}, b, c);
+      const F3 e2 = {hg.x * hs + hd.x, hg.y * hs + hd.y, hg.z * hs + hd.z};
+      const float dx = e2.x - e1.x, dy = e2.y - e1.y, dz = e2.z - e1.z;
+      if (dx * dx + dy * dy + dz * dz < P.ethresh) {
+        F3 np = {cur.x + e2.x, cur.y + e2.y, cur.z + e2.z};
+        if (nearb) {
+          np.x = clampf_ext(np.x, V.X);
+          np.y = clampf_ext(np.y, V.Y);
+          np.z = clampf_ext(np.z, V.Z);
+        }
+        cur = np;
+        step = fminf(step * 1.8f, ms / gm);
+        if (lab[nearest(cur, nearb)] != -1) return EV_HIT_PREASSIGNED;
+      } else {
+        step = step * 0.5f;
+      }
+    }
+    return EV_OVER_MAX_ITERATIONS;
+  }
+};
+
+__device__ __forceinline__ int dist_to_boundary(const VolDims& V, int64_t x, int64_t y, int64_t z) {
+  int64_t m = x < V.X - 1 - x ? x : V.X - 1 - x;
+  const int64_t my = y < V.Y - 1 - y ? y : V.Y - 1 - y;
+  const int64_t mz = z < V.Z - 1 - z ? z : V.Z - 1 - z;
+  if (my < m) m = my;
+  if (mz < m) m = mz;
+  return (int)m;
+}
+
+// Spread visiting order of the first pass (:166-174 with one thread): level L
+// visits start_L + j * stride_L.  Host-computed tables, levels in order.
+struct SpreadOrder {
+  int nlev;
+  int64_t start[48], stride[48], offset[49];
+};
+
+constexpr int kPathCap = 48;
+
+__global__ void __launch_bounds__(128) integrate_pass1_kernel(const Adv32 A, const SpreadOrder S,
+                                                              int32_t* __restrict__ lab, int* __restrict__ n_steps) {
+  const VolDims& V = A.V;
+  const int64_t total = S.offset[S.nlev];
+  int path[kPathCap];
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+    int L = 0;
+    while (L + 1 < S.nlev && S.offset[L + 1] <= t) L++;
+    const int64_t i = S.start[L] + (t - S.offset[L]) * S.stride[L];
+    if (lab[i] != -1) continue;
+    int64_t x = i % V.X, y = (i / V.X) % V.Y, z = i / (V.X * V.Y);
+    F3 cur = {(float)x, (float)y, (float)z};
+    int iters = A.P.iteration_limit;
+    int np = 0;
+    path[np++] = (int)i;
+    int64_t end = i;
+    while (true) {
+      const bool nb = dist_to_boundary(V, x, y, z) <= 1;
+      const int ev = A.advect(cur, iters, nb);
+      end = A.nearest(cur, nb);
+      x = end % V.X;
+      y = (end / V.X) % V.Y;
+      z = end / (V.X * V.Y);
+      if (np < kPathCap) path[np++] = (int)end;
+      if (ev != EV_OUT_OF_VOXEL) break;
+    }
+    int32_t dest = lab[end];
+    if (dest == -1) dest = kLabelNone;  // reached no region: assigned to nothing
+    for (int k = 0; k < np; k++) atomicCAS(&lab[path[k]], -1, dest);
+  }
+  (void)n_steps;
+}
+
+// ---- FP64 advector (fix-up), the reference's arithmetic --------------------------------
+
+struct D3 {
+  double x, y, z;
+};
+__device__ __forceinline__ double dm(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ double da(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ double ds(double a, double b) { return __dsub_rn(a, b); }
+__device__ __forceinline__ D3 dlerp(D3 a, D3 b, double t) {
+  const double u = ds(1.0, t);
+  return {da(dm(a.x, u), dm(b.x, t)), da(dm(a.y, u), dm(b.y, t)), da(dm(a.z, u), dm(b.z, t))};
+}
+__device__ __forceinline__ double magsq(D3 a) { return da(da(dm(a.x, a.x), dm(a.y, a.y)), dm(a.z, a.z)); }
+__device__ __forceinline__ double clampd_ext(double v, int64_t n) {
+  if (v < 0) v = 0;
+  if (v >= (double)n) v = (double)n - 1;
+  return v;
+}
+
+struct Adv64 {
+  const double* G;  // x,y,z doubles per vertex (ComputeGradFromImage(1), zeroed at the seeds)
+  VolDims V;
+  IntegParams P;
+  const uint8_t* state;  // fix-up stop: certain terminal
+
+  __device__ __forceinline__ D3 corner(int64_t x, int64_t y, int64_t z) const {
+    const double* p = G + 3 * vid(V, x, y, z);
+    return {p[0], p[1], p[2]};
+  }
+  __device__ __forceinline__ void surround(const int64_t b[3], bool clamp, D3 c[8]) const {
+    int64_t vv[3][2];
+    const int64_t ext[3] = {V.X, V.Y, V.Z};
+#pragma unroll
+    for (int a = 0; a < 3; a++) {
+      vv[a][0] = b[a];
+      vv[a][1] = b[a] + 1;
+      if (clamp) {
+        if (b[a] < 0) vv[a][0] = 0;
+        if (b[a] >= ext[a] - 1) vv[a][0] = vv[a][1] = ext[a] - 1;
+      }
+    }
+#pragma unroll
+    for (int n = 0; n < 8; n++) c[n] = corner(vv[0][n & 1], vv[1][(n >> 1) & 1], vv[2][n >> 2]);
+  }
+  __device__ __forceinline__ static D3 trilin(D3 s, const int64_t b[3], const D3 c[8]) {
+    const double fx = ds(s.x, (double)b[0]), fy = ds(s.y, (double)b[1]), fz = ds(s.z, (double)b[2]);
+    const D3 x0 = dlerp(c[0], c[1], fx), x1 = dlerp(c[2], c[3], fx), x2 = dlerp(c[4], c[5], fx), x3 = dlerp(c[6], c[7], fx);
+    return dlerp(dlerp(x0, x1, fy), dlerp(x2, x3, fy), fz);
+  }
+  __device__ __forceinline__ int64_t nearest(D3 p, bool) const {
+    return vid(V, (int64_t)clampd_ext(da(p.x, 0.5), V.X), (int64_t)clampd_ext(da(p.y, 0.5), V.Y),
+               (int64_t)clampd_ext(da(p.z, 0.5), V.Z));
+  }
+  __device__ int advect(D3& cur, int& iters, bool nearb) const {
+    D3 c[8];
+    D3 old = cur;
+    int64_t b[3];
+    if (nearb) {
+      b[0] = (int64_t)clampd_ext(cur.x, V.X);
+      b[1] = (int64_t)clampd_ext(cur.y, V.Y);
+      b[2] = (int64_t)clampd_ext(cur.z, V.Z);
+    } else {
+      b[0] = (int64_t)fmin(fmax(cur.x, 0.0), (double)(V.X - 2));
+      b[1] = (int64_t)fmin(fmax(cur.y, 0.0), (double)(V.Y - 2));
+      b[2] = (int64_t)fmin(fmax(cur.z, 0.0), (double)(V.Z - 2));
+    }
+    surround(b, nearb, c);
+    D3 g = trilin(cur, b, c);
+    float gm = __double2float_rn(__dsqrt_rn(magsq(g)));
+    if (!(gm > 0.f) || !isfinite(gm)) return EV_LOW_GRADIENT;  // no direction to follow
+    float step = __double2float_rn(__ddiv_rn(P.max_step, (double)gm));
+    while (iters-- > 0) {
+      if (!(old.x == cur.x && old.y == cur.y && old.z == cur.z)) {
+        if ((int)cur.x != (int)old.x || (int)cur.y != (int)old.y || (int)cur.z != (int)old.z) return EV_OUT_OF_VOXEL;
+        g = trilin(cur, b, c);
+        gm = __double2float_rn(__dsqrt_rn(magsq(g)));
+        if (!(gm > 0.f) || !isfinite(gm)) return EV_LOW_GRADIENT;
+        if ((double)__fmul_rn(gm, step) > P.max_step) step = __double2float_rn(__ddiv_rn(P.max_step, (double)gm));
+        old = cur;
+      }
+      if (gm < P.gthresh) return EV_LOW_GRADIENT;
+      // full step: Vec3d * float multiplies in float (gi_vectors.h:250)
+      const float sm = __fmul_rn((float)P.step_mult, step);
+      const D3 e1 = {(double)__fmul_rn(__double2float_rn(g.x), sm), (double)__fmul_rn(__double2float_rn(g.y), sm),
+                     (double)__fmul_rn(__double2float_rn(g.z), sm)};
+      const double hs = dm((double)step, (double)P.step_mult * 0.5);
+      const D3 hd = {dm(g.x, hs), dm(g.y, hs), dm(g.z, hs)};
+      const D3 hg = trilin({da(cur.x, hd.x), da(cur.y, hd.y), da(cur.z, hd.z)}, b, c);
+      const D3 e2 = {da(dm(hg.x, hs), hd.x), da(dm(hg.y, hs), hd.y), da(dm(hg.z, hs), hd.z)};
+      const D3 df = {ds(e2.x, e1.x), ds(e2.y, e1.y), ds(e2.z, e1.z)};
+      const float err = __double2float_rn(magsq(df));
+      if (err < P.ethresh) {
+        D3 np = {da(cur.x, e2.x), da(cur.y, e2.y), da(cur.z, e2.z)};
+        if (nearb) {
+          np.x = clampd_ext(np.x, V.X);
+          np.y = clampd_ext(np.y, V.Y);
+          np.z = clampd_ext(np.z, V.Z);
+        }
+        cur = np;
+        const float a = __double2float_rn(dm((double)step, 1.8));
+        const float bb = __double2float_rn(__ddiv_rn(P.max_step, (double)gm));
+        step = a < bb ? a : bb;
+        const uint8_t st = state[nearest(cur, nearb)];
+        if (st == kStSeed || st == kStTerminal) return EV_HIT_PREASSIGNED;
+      } else {
+        step = __double2float_rn(dm((double)step, 0.5));
+      }
+    }
+    return EV_OVER_MAX_ITERATIONS;
+  }
+};
+
+// Vertices assigned in pass 1 with a differently labelled 6-neighbour (:279-307).
+__global__ void boundary_set_kernel(const int32_t* __restrict__ lab, const uint8_t* __restrict__ state, const VolDims V,
+                                    int64_t* __restrict__ list, int* __restrict__ n, uint32_t* __restrict__ queued) {
+  const int64_t N = V.X * V.Y * V.Z;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < N; i += (int64_t)gridDim.x * blockDim.x) {
+    if (state[i] != kStUnassigned) continue;
+    const int64_t x = i % V.X, y = (i / V.X) % V.Y, z = i / (V.X * V.Y);
+    const int32_t l = lab[i];
+    bool diff = false;
+    if (x < V.X - 1) diff |= lab[i + 1] != l;
+    if (x > 0) diff |= lab[i - 1] != l;
+    if (y < V.Y - 1) diff |= lab[i + V.X] != l;
+    if (y > 0) diff |= lab[i - V.X] != l;
+    if (z < V.Z - 1) diff |= lab[i + V.X * V.Y] != l;
+    if (z > 0) diff |= lab[i - V.X * V.Y] != l;
+    if (!diff) continue;
+    atomicOr(&queued[i >> 5], 1u << (i & 31));
+    list[atomicAdd(n, 1)] = i;
+  }
+}
+
+// One fix-up wave (:330-415): re-integrate, stopping only at certain terminals.
+__global__ void __launch_bounds__(128) fixup_kernel(const Adv64 A, int32_t* __restrict__ lab, uint8_t* __restrict__ state,
+                                                    const int64_t* __restrict__ list, int n, int64_t* __restrict__ next,
+                                                    int* __restrict__ n_next, uint32_t* __restrict__ queued) {
+  const VolDims& V = A.V;
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+    const int64_t v = list[k];
+    atomicAnd(&queued[v >> 5], ~(1u << (v & 31)));
+    const int32_t init = lab[v];
+    int64_t x = v % V.X, y = (v / V.X) % V.Y, z = v / (V.X * V.Y);
+    D3 cur = {(double)x, (double)y, (double)z};
+    int iters = A.P.iteration_limit;
+    int64_t end = v;
+    while (true) {
+      const bool nb = dist_to_boundary(V, x, y, z) <= 1;
+      const int ev = A.advect(cur, iters, nb);
+      end = A.nearest(cur, nb);
+      x = end % V.X;
+      y = (end / V.X) % V.Y;
+      z = end / (V.X * V.Y);
+      if (ev != EV_OUT_OF_VOXEL) break;
+    }
+    int32_t nl = lab[end];
+    if (nl == -1) nl = kLabelNone;
+    lab[v] = nl;
+    state[v] = kStNonterminal;
+    if (nl == init) continue;
+    x = v % V.X;
+    y = (v / V.X) % V.Y;
+    z = v / (V.X * V.Y);
+    const int64_t nbr[6] = {x < V.X - 1 ? v + 1 : -1, x > 0 ? v - 1 : -1, y < V.Y - 1 ? v + V.X : -1,
+                            y > 0 ? v - V.X : -1, z < V.Z - 1 ? v + V.X * V.Y : -1, z > 0 ? v - V.X * V.Y : -1};
+#pragma unroll
+    for (int j = 0; j < 6; j++) {
+      const int64_t u = nbr[j];
+      if (u < 0 || state[u] != kStUnassigned || lab[u] == nl) continue;
+      const uint32_t bit = 1u << (u & 31);
+      if (atomicOr(&queued[u >> 5], bit) & bit) continue;
+      next[atomicAdd(n_next, 1)] = u;
+    }
+  }
+}
+
+// ---- K5c: isolated-region cleaner --------------------------------------------------------
+
+__device__ __forceinline__ bool comes_before(const float* f, int dir, int64_t a, int64_t b) {
+  return dir < 0 ? vgreater(f, b, a) : vgreater(f, a, b);
+}
+
+__device__ __forceinline__ int64_t uf_find(int64_t* parent, int64_t v) {
+  int64_t p = parent[v];
+  while (p != v) {
+    const int64_t gp = parent[p];
+    if (gp != p) parent[v] = gp;  // path halving
+    v = p;
+    p = gp;
+  }
+  return v;
+}
+
+__global__ void uf_init_kernel(int64_t* __restrict__ parent, int64_t N) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < N; i += (int64_t)gridDim.x * blockDim.x)
+    parent[i] = i;
+}
+
+// MergeWithSameNeighbors + MergeByOrder: the earlier root (walk order) stays root
+__global__ void uf_hook_kernel(const int32_t* __restrict__ lab, const float* __restrict__ f, const VolDims V, int dir,
+                               int64_t* __restrict__ parent) {
+  const int64_t N = V.X * V.Y * V.Z;
+  for (int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v < N; v += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t x = v % V.X, y = (v / V.X) % V.Y, z = v / (V.X * V.Y);
+    const int64_t nbr[3] = {x < V.X - 1 ? v + 1 : -1, y < V.Y - 1 ? v + V.X : -1, z < V.Z - 1 ? v + V.X * V.Y : -1};
+    for (int j = 0; j < 3; j++) {
+      const int64_t u = nbr[j];
+      if (u < 0 || lab[u] != lab[v]) continue;
+      for (int guard = 0; guard < 1 << 20; guard++) {
+        const int64_t ru = uf_find(parent, u), rv = uf_find(parent, v);
+        if (ru == rv) break;
+        const int64_t early = comes_before(f, dir, ru, rv) ? ru : rv;
+        const int64_t late = early == ru ? rv : ru;
+        if ((int64_t)atomicCAS((unsigned long long*)&parent[late], (unsigned long long)late,
+                               (unsigned long long)early) == late)
+          break;
+      }
+    }
+  }
+}
+
+__global__ void uf_flatten_kernel(int64_t* __restrict__ parent, int64_t N) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < N; i += (int64_t)gridDim.x * blockDim.x)
+    parent[i] = uf_find(parent, i);
+}
+
+// MergeBoundaryExtrema: a component root joins the component of its first earlier
+// neighbour from another region (itself if there is none, i.e. an extremum's component)
+__global__ void clean_target_kernel(const int32_t* __restrict__ lab, const float* __restrict__ f, const VolDims V, int dir,
+                                    const int64_t* __restrict__ parent, int64_t* __restrict__ target) {
+  const int64_t N = V.X * V.Y * V.Z;
+  for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < N; r += (int64_t)gridDim.x * blockDim.x) {
+    if (parent[r] != r) continue;
+    const int64_t x = r % V.X, y = (r / V.X) % V.Y, z = r / (V.X * V.Y);
+    const int64_t nbr[6] = {x < V.X - 1 ? r + 1 : -1, x > 0 ? r - 1 : -1, y < V.Y - 1 ? r + V.X : -1,
+                            y > 0 ? r - V.X : -1, z < V.Z - 1 ? r + V.X * V.Y : -1, z > 0 ? r - V.X * V.Y : -1};
+    int64_t earliest = r;
+    for (int j = 0; j < 6; j++) {
+      const int64_t u = nbr[j];
+      if (u < 0 || !comes_before(f, dir, u, r) || lab[u] == lab[r]) continue;
+      if (comes_before(f, dir, u, earliest)) earliest = u;
+    }
+    target[r] = parent[earliest];
+  }
+}
+
+__global__ void clean_resolve_kernel(const int32_t* __restrict__ lab, const VolDims V, const int64_t* __restrict__ parent,
+                                     const int64_t* __restrict__ target, int32_t* __restrict__ out) {
+  const int64_t N = V.X * V.Y * V.Z;
+  for (int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v < N; v += (int64_t)gridDim.x * blockDim.x) {
+    int64_t r = parent[v];
+    for (int64_t guard = 0; guard < N && target[r] != r; guard++) r = target[r];  // strictly earlier each hop
+    const int32_t l = lab[v];
+    const int32_t lr = lab[r];
+    // vertices that reached no region keep "none"; the rest take their final root's region
+    int32_t o = (l == kLabelNone) ? -1 : lr;
+    if (o == kLabelNone) o = -1;
+    out[v] = o;
+  }
+}
+
+// ---- launchers ---------------------------------------------------------------------------
+
+cudaError_t launch_integrate_pass1(const float4* G, const VolDims& V, const IntegParams& P, const SpreadOrder& S,
+                                   int32_t* lab, int num_sms, cudaStream_t stream) {
+  Adv32 A{G, V, P, lab};
+  integrate_pass1_kernel<<<num_sms * 16, 128, 0, stream>>>(A, S, lab, nullptr);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_boundary_set(const int32_t* lab, const uint8_t* state, const VolDims& V, int64_t* list, int* n,
+                                uint32_t* queued, int num_sms, cudaStream_t stream) {
+  boundary_set_kernel<<<num_sms * 8, 256, 0, stream>>>(lab, state, V, list, n, queued);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_fixup(const double* G, const VolDims& V, const IntegParams& P, int32_t* lab, uint8_t* state,
+                         const int64_t* list, int n, int64_t* next, int* n_next, uint32_t* queued, int num_sms,
+                         cudaStream_t stream) {
+  if (n <= 0) return cudaSuccess;
+  Adv64 A{G, V, P, state};
+  const int blocks = (n + 127) / 128;
+  fixup_kernel<<<blocks < num_sms * 16 ? blocks : num_sms * 16, 128, 0, stream>>>(A, lab, state, list, n, next, n_next,
+                                                                                  queued);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_clean(const int32_t* lab, const float* f, const VolDims& V, int dir, int64_t* parent, int64_t* target,
+                         int32_t* out, int num_sms, cudaStream_t stream) {
+  const int64_t N = V.X * V.Y * V.Z;
+  const int grid = num_sms * 8;
+  uf_init_kernel<<<grid, 256, 0, stream>>>(parent, N);
+  uf_hook_kernel<<<grid, 256, 0, stream>>>(lab, f, V, dir, parent);
+  uf_flatten_kernel<<<grid, 256, 0, stream>>>(parent, N);
+  clean_target_kernel<<<grid, 256, 0, stream>>>(lab, f, V, dir, parent, target);
+  clean_resolve_kernel<<<grid, 256, 0, stream>>>(lab, V, parent, target, out);
+  return cudaGetLastError();
+}
+
+}  // namespace msc

@@ -1,0 +1,91 @@
+// Shared definitions of the labeling kernels (label_kernels.cu, integrate_kernels.cu).
+#pragma once
+#include <cstdint>
+
+#include "msc_device.cuh"
+
+namespace msc {
+
+// Vertex grid and its cell complex.
+struct VolDims {
+  int64_t X, Y, Z;     // vertices
+  int64_t dX, dY, dZ;  // cells
+  int64_t cs1, cs2;    // cell-id strides
+};
+
+// A saddle arc between two extrema (MergeArc, gi_extrema_region_builder.h:43-61).
+struct Arc {
+  int64_t saddle;
+  int32_t e1, e2;
+  float sval, pers;
+};
+
+// Per-vertex integration state (DestType, gi_basic_types.h:43-49, plus "seed": a
+// certain terminal whose gradient is zeroed, gi_numeric_integrator_path_compressing.h:118-123).
+enum : uint8_t {
+  kStUnassigned = 0,
+  kStSeed = 1,
+  kStTerminal = 2,
+  kStAssigned = 3,
+  kStNonterminal = 4,
+};
+
+// Label of a vertex that a first-pass streamline reached without finding a region.
+constexpr int32_t kLabelNone = -2;
+
+__host__ __device__ inline void cell_coords(const VolDims& V, int64_t id, int64_t k[3]) {
+  k[0] = id % V.dX;
+  k[1] = (id / V.dX) % V.dY;
+  k[2] = id / (V.dX * V.dY);
+}
+
+__host__ __device__ inline int boundary_value(const VolDims& V, const int64_t k[3]) {
+  return (k[0] == 0 || k[0] == V.dX - 1) + (k[1] == 0 || k[1] == V.dY - 1) + (k[2] == 0 || k[2] == V.dZ - 1);
+}
+
+// getPair: UncompressByteTo6NeighborOffset (the labeling path needs X, Y, Z >= 2,
+// where stored codes name their true axis)
+__host__ __device__ inline int64_t decode_pair(const VolDims& V, int64_t id, unsigned code) {
+  const int64_t off = (code >> 1) == 0 ? 1 : ((code >> 1) == 1 ? V.cs1 : V.cs2);
+  return (code & 1) ? id - off : id + off;
+}
+
+// IsGreater (gi_regular_grid_trilinear_function.h:309-314) on vertex indices
+__device__ __forceinline__ bool vgreater(const float* f, int64_t a, int64_t b) {
+  const float fa = f[a], fb = f[b];
+  if (fa > fb) return true;
+  if (fb > fa) return false;
+  return a > b;
+}
+
+// Cell2HighestVertex as a vertex index
+__device__ inline int64_t highest_vertex(const VolDims& V, const float* f, int64_t cell) {
+  int64_t k[3];
+  cell_coords(V, cell, k);
+  const int64_t bx = k[0] >> 1, by = k[1] >> 1, bz = k[2] >> 1;
+  const int ox = (int)(k[0] & 1), oy = (int)(k[1] & 1), oz = (int)(k[2] & 1);
+  int64_t best = -1;
+  for (int s = 0; s < 8; s++) {
+    const int dx = s & 1, dy = (s >> 1) & 1, dz = (s >> 2) & 1;
+    if ((dx && !ox) || (dy && !oy) || (dz && !oz)) continue;
+    const int64_t v = (bx + dx) + (by + dy) * V.X + (bz + dz) * V.X * V.Y;
+    if (best < 0 || vgreater(f, v, best)) best = v;
+  }
+  return best;
+}
+
+cudaError_t launch_find_critical(const uint8_t* g, const VolDims& V, int dir, int32_t* ext_id_of_key,
+                                 int64_t* ext_cells, int* n_ext, int64_t* saddles, int* n_sad, int num_sms,
+                                 cudaStream_t stream);
+cudaError_t launch_trace_arcs(const uint8_t* g, const float* f, const VolDims& V, int dir, const int64_t* saddles,
+                              int n_sad, const int32_t* ext_id_of_key, float threshold, Arc* arcs, int* n_arcs,
+                              int* err, int num_sms, cudaStream_t stream);
+cudaError_t launch_extremum_info(const float* f, const VolDims& V, int dir, const int64_t* ext_cells, int n_ext,
+                                 int64_t* hv, float* fval, int64_t* seed, int num_sms, cudaStream_t stream);
+cudaError_t launch_group_seeds(const int32_t* rep, const int64_t* seed, int n_ext, int32_t* name, int32_t* lab,
+                               uint8_t* state, int num_sms, cudaStream_t stream);
+int64_t terminal_num_tiles(const VolDims& V);
+cudaError_t launch_terminal_pass(const float* f, int32_t* lab, const VolDims& V, int dir, const uint8_t* dirty_in,
+                                 uint8_t* dirty_out, int* changed, int* err, int num_sms, cudaStream_t stream);
+
+}  // namespace msc

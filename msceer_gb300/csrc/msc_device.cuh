@@ -17,6 +17,7 @@ enum : int {
   kErrNaN = 1 << 0,          // input contains NaN (outside the order's contract)
   kErrPassLimit = 1 << 1,    // ldir closure did not converge within the pass bound
   kErrLocalQueue = 1 << 2,   // shared-memory BFS queue overflow (cannot happen by construction)
+  kErrIterLimit = 1 << 3,    // a bounded walk hit its step limit (invalid gradient input)
 };
 
 struct GradDims {

@@ -1,0 +1,53 @@
+"""The CUDA labeling chain against the FP64 oracle (itself equal to the reference
+at one thread).  Terminal regions are exact; integrated labels are compared as
+partitions (regions are named by their extremum vertex on both sides) and the
+fraction of differing vertices is bounded -- the reference's own multi-threaded
+runs differ from each other by ~1e-4 of the vertices before and ~3.5e-3 after
+its cleaner."""
+import numpy as np
+import pytest
+
+import oracle_lib
+from msceer_gb300 import fields
+
+pytestmark = pytest.mark.gpu
+
+# stated tolerances: fraction of vertices whose label differs from the FP64 oracle
+TOL_INTEGRATED = 0.02
+TOL_FINAL = 0.02
+
+
+def run_both(f, device, oracle):
+    import torch
+    from msceer_gb300 import integrated_labels, lower_star_grad
+    gt = 1e-6 * float(np.abs(f).max())
+    t = torch.from_numpy(f).to(device)
+    g = lower_star_grad(t)
+    got = integrated_labels(t, g, 1e-4, gt, 4000, 0.25, 0.0, stages=True)
+    got = {k: v.cpu().numpy() for k, v in got.items()}
+    want = oracle.labels(f, g.cpu().numpy(), 1e-4, gt, 4000, 0.25, 0.0)
+    return got, want
+
+
+FIELDS = {
+    "gauss40": lambda: fields.gaussian_sum((40, 36, 32), 8, seed=5),
+    "k3_32": lambda: fields.power_law_field((32, 30, 28), seed=6),
+    "gauss64_cfg0": lambda: fields.gaussian_sum((64, 64, 64), 16, seed=0),
+}
+
+
+@pytest.mark.parametrize("name", list(FIELDS))
+def test_labels_vs_oracle(gpu, oracle, name):
+    f = FIELDS[name]()
+    got, want = run_both(f, gpu, oracle)
+    report = {}
+    for k in ("asc_terminal", "dsc_terminal", "asc_integrated", "dsc_integrated", "asc", "dsc"):
+        report[k] = float((got[k] != want[k]).mean())
+    print(name, report)
+    assert report["asc_terminal"] == 0.0 and report["dsc_terminal"] == 0.0, report
+    assert report["asc_integrated"] <= TOL_INTEGRATED and report["dsc_integrated"] <= TOL_INTEGRATED, report
+    assert report["asc"] <= TOL_FINAL and report["dsc"] <= TOL_FINAL, report
+    # every label names an extremum vertex of the right kind
+    for k in ("asc", "dsc"):
+        labs = np.unique(got[k])
+        assert (labs >= -1).all()
