@@ -72,6 +72,11 @@ __global__ void terminal_state_kernel(const int32_t* lab, uint8_t* state, int64_
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
     if (state[i] != msc::kStSeed) state[i] = lab[i] >= 0 ? msc::kStTerminal : msc::kStUnassigned;
 }
+// stage snapshot: internal "reached no region" reads as the reference's -1
+__global__ void snapshot_kernel(const int32_t* lab, int32_t* out, int64_t n) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    out[i] = lab[i] == msc::kLabelNone ? -1 : lab[i];
+}
 // SetGradExplicit(seed, 0) (gi_numeric_integrator_path_compressing.h:118-123), both copies
 __global__ void zero_seed_grad_kernel(const int64_t* seed, int n, float4* g32, double* g64) {
   for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < n; e += gridDim.x * blockDim.x) {
@@ -281,7 +286,7 @@ int labels_impl(const float* f, const uint8_t* grad, const int64_t* dims, const 
       din = dout;
       dout = (dout == tiles) ? tiles + ntiles : tiles;
     }
-    if (stages) LCUDA(cudaMemcpyAsync(stages + (2 * pass) * N, lab, N * sizeof(int32_t), cudaMemcpyDeviceToDevice, st), "copy");
+    if (stages) snapshot_kernel<<<grid, 256, 0, st>>>(lab, stages + (2 * pass) * N, N);
     terminal_state_kernel<<<grid, 256, 0, st>>>(lab, state, N);
     if (n_ext > 0) zero_seed_grad_kernel<<<(n_ext + 255) / 256, 256, 0, st>>>(seed, n_ext, g32, g64);
 
@@ -317,7 +322,7 @@ int labels_impl(const float* f, const uint8_t* grad, const int64_t* dims, const 
       cur = nxt;
       nxt = t;
     }
-    if (stages) LCUDA(cudaMemcpyAsync(stages + (2 * pass + 1) * N, lab, N * sizeof(int32_t), cudaMemcpyDeviceToDevice, st), "copy");
+    if (stages) snapshot_kernel<<<grid, 256, 0, st>>>(lab, stages + (2 * pass + 1) * N, N);
 
     // isolated-region cleaner
     LCUDA(pool.get(&parent, N), "alloc");
