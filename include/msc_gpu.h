@@ -40,6 +40,7 @@ typedef struct CUstream_st* msc_stream_t;
 #define MSC_ERR_NAN_INPUT (-5)
 #define MSC_ERR_ITER_LIMIT (-6)
 #define MSC_ERR_QUEUE_OVERFLOW (-7)
+#define MSC_ERR_TOO_LARGE (-8)
 
 /* Library ABI version (major*10000 + minor*100 + patch). */
 int msc_version(void);
@@ -131,6 +132,18 @@ int msc_integrated_labels_3d_stages(const float* f, const uint8_t* grad, const i
                                     int32_t* stages, msc_stream_t stream);
 /* Error text of the last failed labeling call on the calling thread. */
 const char* msc_labels_last_error_string(void);
+
+/* Stage 2 for callers that may not allocate device memory: the same result as
+ * msc_ascending_manifold_dims_3d, with the pass scratch (tile flags, status words)
+ * in a fixed 1 MiB array inside the library instead of allocated memory.  No
+ * counterpart in the reference (its CPU closure needs no device memory).  Meant for
+ * applications that hand out all device memory through their own pool and do not
+ * let libraries call cudaMalloc.  Limit: 524,288 ldir tiles of 32x32x16 cells
+ * (volumes up to about 1000^3 vertices); larger volumes return MSC_ERR_TOO_LARGE.
+ * The first call on a device looks up the array's device address; make that call
+ * before any stream capture.  Every call shares the array: calls whose work
+ * overlaps on the GPU race.  Calls no cudaMalloc / cudaFree. */
+int msc_ascending_manifold_dims_3d_static(uint8_t* grad, const int64_t dims[3], msc_stream_t stream, int* passes_out);
 
 /* Host-memory convenience with steepest_lstar's semantics: copies f to the GPU,
  * computes, copies the .grad back.  f_host: X*Y*Z floats; grad_host:

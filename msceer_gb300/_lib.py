@@ -16,7 +16,7 @@ _lib = None
 MSC_OK = 0
 ERRORS = {
     -1: "MSC_ERR_BAD_DIMS", -2: "MSC_ERR_NULL_POINTER", -3: "MSC_ERR_CUDA", -4: "MSC_ERR_OOM",
-    -5: "MSC_ERR_NAN_INPUT", -6: "MSC_ERR_ITER_LIMIT", -7: "MSC_ERR_QUEUE_OVERFLOW",
+    -5: "MSC_ERR_NAN_INPUT", -6: "MSC_ERR_ITER_LIMIT", -7: "MSC_ERR_QUEUE_OVERFLOW", -8: "MSC_ERR_TOO_LARGE",
 }
 
 # every symbol include/msc_gpu.h declares: (restype, argtypes)
@@ -34,6 +34,7 @@ SIGNATURES = {
     "msc_lower_star_pairs_2d": (ctypes.c_int, [_VP, _I64P, _VP, _VP]),
     "msc_ascending_manifold_dims_3d": (ctypes.c_int, [_VP, _I64P, _VP, ctypes.POINTER(ctypes.c_int)]),
     "msc_ascending_manifold_dims_2d": (ctypes.c_int, [_VP, _I64P, _VP, ctypes.POINTER(ctypes.c_int)]),
+    "msc_ascending_manifold_dims_3d_static": (ctypes.c_int, [_VP, _I64P, _VP, ctypes.POINTER(ctypes.c_int)]),
     "msc_central_diff_grad_3d": (ctypes.c_int, [_VP, _I64P, _VP, ctypes.c_int, _VP]),
     "msc_central_diff_grad_2d": (ctypes.c_int, [_VP, _I64P, _VP, ctypes.c_int, _VP]),
     "msc_central_diff_grad_3d_f64": (ctypes.c_int, [_VP, _I64P, _VP, _VP]),

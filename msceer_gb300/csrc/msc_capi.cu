@@ -222,6 +222,11 @@ int host_impl(int nd, const float* fh, const int64_t* dims, uint8_t* gh) {
 
 }  // namespace
 
+namespace msc {
+// Records the calling thread's error text for msc_last_error_string().
+int set_last_error(int code, const char* msg) { return fail(code, msg); }
+}  // namespace msc
+
 extern "C" {
 
 int msc_version(void) { return 100; }
