@@ -46,10 +46,27 @@ __device__ __forceinline__ void lcoords(int i, int& lx, int& ly, int& lz) {
   lz = i / (T::LX * T::LY);
 }
 
-// Walk one item: visit its cofacets (CofacetsIterator order), mark them, follow
-// their partners.  Returns one newly reached item for the calling thread to chase
-// and queues any further ones.  All coordinates are local to the staged box, whose
-// origin is even on every axis, so local parity is the cell's dimension parity.
+// Queue append for the lanes of a warp that are converged here: one shared-memory
+// atomic per warp instead of one per pushed item.
+__device__ __forceinline__ void warp_push(uint16_t* sq, int* qtail, int cap, int* err, bool want, int item) {
+  const unsigned act = __activemask();
+  const unsigned m = __ballot_sync(act, want);
+  if (!m) return;
+  const int lane = threadIdx.x & 31;
+  const int leader = __ffs(m) - 1;
+  int base = 0;
+  if (lane == leader) base = atomicAdd(qtail, __popc(m));
+  base = __shfl_sync(act, base, leader);
+  if (want) {
+    const int slot = base + __popc(m & ((1u << lane) - 1u));
+    if (slot < cap) sq[slot] = (uint16_t)item; else atomicOr(err, kErrLocalQueue);
+  }
+}
+
+// Walk one item: visit its cofacets (CofacetsIterator order), mark them, follow their
+// partners and queue the newly reached items.  All coordinates are local to the
+// staged box, whose origin is even on every axis, so local parity is the cell's
+// dimension parity.
 template <class T, int ND>
 struct LdirWalk {
   uint8_t* sg;
@@ -63,62 +80,60 @@ struct LdirWalk {
 
   __device__ __forceinline__ void touch(int c) { atomicOr(&dirty[c >> 5], 1u << (c & 31)); }
 
-  __device__ __forceinline__ int step(int i, int phase) {
+  // returns the item to queue, or -1
+  __device__ __forceinline__ int visit(int i, int l[3], int a, int sgn, int phase) {
     const unsigned value = phase == 0 ? 2u : 1u;
+    constexpr int LE[3] = {T::LX, T::LY, T::LZ};
+    const int la = l[a] + sgn;
+    if (la < lmin[a] || la >= lmax[a]) return -1;
+    const int t = i + sgn * T::ls(a);
+    const uint8_t bt = sg[t];
+    const unsigned code = (bt >> 2) & 7u;
+    if (!(bt & 1u) || code == 7u) return -1;  // unassigned or critical
+    if (phase == 0) {
+      if ((bt >> 5) == 3u) { sg[t] = (uint8_t)((bt & 0x1Fu) | (2u << 5)); touch(t); }
+    } else {
+      if ((bt >> 5) != 1u) { sg[t] = (uint8_t)((bt & 0x1Fu) | (1u << 5)); touch(t); }
+    }
+    const int pc = map3(dec_map, (int)code);
+    const int pa = pc >> 1, psg = (pc & 1) ? -1 : 1;
+    int lp[3] = {l[0], l[1], l[2]};
+    lp[a] += sgn;
+    lp[pa] += psg;
+    if (lp[pa] < 0 || lp[pa] >= LE[pa]) return -1;  // partner outside the box
+    const int tp = t + psg * T::ls(pa);
+    if (tp == i) return -1;
+    const uint8_t bp = sg[tp];
+    if (phase == 0) {
+      if ((bp >> 5) != 3u) return -1;  // already marked: seeded or queued
+      const int pdim = (lp[0] & 1) + (lp[1] & 1) + (ND == 3 ? (lp[2] & 1) : 0);
+      if (pdim != 1) {  // a hex: the path ends here
+        sg[tp] = (uint8_t)((bp & 0x1Fu) | (2u << 5));
+        touch(tp);
+        return -1;
+      }
+    } else {
+      if ((bp >> 5) == 1u) return -1;
+    }
+    const uint32_t bit = 1u << (tp & 31);
+    if (atomicOr(&vis[tp >> 5], bit) & bit) return -1;
+    sg[tp] = (uint8_t)((bp & 0x1Fu) | (value << 5));
+    touch(tp);
+    return tp;
+  }
+
+  __device__ __forceinline__ void step(int i, int phase) {
     int l[3];
     lcoords<T>(i, l[0], l[1], l[2]);
-    constexpr int LE[3] = {T::LX, T::LY, T::LZ};
-    int next = -1;
 #pragma unroll
     for (int a = 0; a < ND; a++) {
-      if (l[a] & 1) continue;  // cofacets only along even axes
 #pragma unroll
       for (int s = 0; s < 2; s++) {
-        const int sgn = s == 0 ? 1 : -1;  // +axis first
-        const int la = l[a] + sgn;
-        if (la < lmin[a] || la >= lmax[a]) continue;
-        const int t = i + sgn * T::ls(a);
-        const uint8_t bt = sg[t];
-        const unsigned code = (bt >> 2) & 7u;
-        if (!(bt & 1u) || code == 7u) continue;  // unassigned or critical
-        if (phase == 0) {
-          if ((bt >> 5) == 3u) { sg[t] = (uint8_t)((bt & 0x1Fu) | (2u << 5)); touch(t); }
-        } else {
-          if ((bt >> 5) != 1u) { sg[t] = (uint8_t)((bt & 0x1Fu) | (1u << 5)); touch(t); }
-        }
-        const int pc = map3(dec_map, (int)code);
-        const int pa = pc >> 1, psg = (pc & 1) ? -1 : 1;
-        int lp[3] = {l[0], l[1], l[2]};
-        lp[a] += sgn;
-        lp[pa] += psg;
-        if (lp[pa] < 0 || lp[pa] >= LE[pa]) continue;  // partner outside the box
-        const int tp = t + psg * T::ls(pa);
-        if (tp == i) continue;
-        const uint8_t bp = sg[tp];
-        if (phase == 0) {
-          if ((bp >> 5) != 3u) continue;  // already marked: seeded or queued
-          const int pdim = (lp[0] & 1) + (lp[1] & 1) + (ND == 3 ? (lp[2] & 1) : 0);
-          if (pdim != 1) {  // a hex: the path ends here
-            sg[tp] = (uint8_t)((bp & 0x1Fu) | (2u << 5));
-            touch(tp);
-            continue;
-          }
-        } else {
-          if ((bp >> 5) == 1u) continue;
-        }
-        const uint32_t bit = 1u << (tp & 31);
-        if (atomicOr(&vis[tp >> 5], bit) & bit) continue;
-        sg[tp] = (uint8_t)((bp & 0x1Fu) | (value << 5));
-        touch(tp);
-        if (next < 0) {
-          next = tp;
-        } else {
-          const int slot = atomicAdd(qtail, 1);
-          if (slot < T::NL) sq[slot] = (uint16_t)tp; else atomicOr(err, kErrLocalQueue);
-        }
+        // cofacets only along even axes, +axis first
+        const int nx = (l[a] & 1) ? -1 : visit(i, l, a, s == 0 ? 1 : -1, phase);
+        warp_push(sq, qtail, T::NL, err, nx >= 0, nx);
       }
     }
-    return next;
   }
 };
 
@@ -180,33 +195,55 @@ __global__ void __launch_bounds__(BS) ldir_pass_kernel(uint8_t* __restrict__ g, 
 
     // stage the box row by row (cells outside the complex read as 0 = unassigned)
     // and collect the seeds: marked items of both walks (first pass), or of the
-    // halo only (later passes: the interior was walked already)
-    for (int row = warp; row < T::LY * T::LZ; row += NWARPS) {
-      const int ly = row % T::LY, lz = row / T::LY;
-      const bool rin = ly >= W.lmin[1] && ly < W.lmax[1] && lz >= W.lmin[2] && lz < W.lmax[2];
-      const uint8_t* grow = g + ((o[1] + ly) * D.cs[1] + (o[2] + lz) * D.cs[2] + o[0]);
-      const bool row_halo = ly < T::H || ly >= T::H + TY || (ND == 3 && (lz < T::H || lz >= T::H + TZ));
-      for (int lx = lane; lx < T::LX; lx += 32) {
-        const int i = lx + T::LX * row;
-        uint8_t b = 0;
-        if (rin && lx >= W.lmin[0] && lx < W.lmax[0]) b = grow[lx];
-        sg[i] = b;
-        if (!(b & 1u)) continue;
-        const unsigned ld = b >> 5;
-        const int dim = (lx & 1) + (ly & 1) + (ND == 3 ? (lz & 1) : 0);
-        if (!first && !(row_halo || lx < T::H || lx >= T::H + TX)) continue;
-        if (dim == 1 && ld == 2u) {
-          atomicOr(&s_vis[i >> 5], 1u << (i & 31));
-          sq[atomicAdd(&s_qtail, 1)] = (uint16_t)i;
-        } else if (dim == 2 && ld == 1u) {
-          sq[atomicSub(&s_qseed, 1) - 1] = (uint16_t)i;
+    // halo only (later passes: the interior was walked already).  Seeds need no
+    // visited bit: being marked already stops a walk from queueing them again.
+    constexpr int RPW = 4;  // rows per warp in flight
+    for (int row0 = warp * RPW; row0 < T::LY * T::LZ; row0 += NWARPS * RPW) {
+      uint8_t b[RPW][(T::LX + 31) / 32];
+#pragma unroll
+      for (int r = 0; r < RPW; r++) {
+        const int row = row0 + r;
+        const int ly = row % T::LY, lz = row / T::LY;
+        const bool rin = row < T::LY * T::LZ && ly >= W.lmin[1] && ly < W.lmax[1] && lz >= W.lmin[2] && lz < W.lmax[2];
+        const uint8_t* grow = g + ((o[1] + ly) * D.cs[1] + (o[2] + lz) * D.cs[2] + o[0]);
+#pragma unroll
+        for (int c = 0; c < (T::LX + 31) / 32; c++) {
+          const int lx = lane + 32 * c;
+          b[r][c] = (rin && lx < T::LX && lx >= W.lmin[0] && lx < W.lmax[0]) ? grow[lx] : (uint8_t)0;
+        }
+      }
+#pragma unroll
+      for (int r = 0; r < RPW; r++) {
+        const int row = row0 + r;
+        if (row >= T::LY * T::LZ) break;
+        const int ly = row % T::LY, lz = row / T::LY;
+        const bool row_halo = ly < T::H || ly >= T::H + TY || (ND == 3 && (lz < T::H || lz >= T::H + TZ));
+#pragma unroll
+        for (int c = 0; c < (T::LX + 31) / 32; c++) {
+          const int lx = lane + 32 * c;
+          const int i = lx + T::LX * row;
+          const uint8_t v = b[r][c];
+          if (lx < T::LX) sg[i] = v;
+          const unsigned ld = v >> 5;
+          const int dim = (lx & 1) + (ly & 1) + (ND == 3 ? (lz & 1) : 0);
+          const bool keep = lx < T::LX && (v & 1u) && (first || row_halo || lx < T::H || lx >= T::H + TX);
+          const bool s0 = keep && dim == 1 && ld == 2u;
+          const bool s1 = keep && dim == 2 && ld == 1u;
+          warp_push(sq, &s_qtail, NL, err, s0, i);
+          // value-1 seeds grow down from the top of the queue
+          const unsigned m1 = __ballot_sync(0xffffffffu, s1);
+          if (m1) {
+            int base = 0;
+            if (lane == 0) base = atomicSub(&s_qseed, __popc(m1));
+            base = __shfl_sync(0xffffffffu, base, 0);
+            if (s1) sq[base - 1 - __popc(m1 & ((1u << lane) - 1u))] = (uint16_t)i;
+          }
         }
       }
     }
     __syncthreads();
 
-    // value-2 walk, then value-1 walk; a thread chases the first partner it reaches
-    // and queues the rest, so chains cost no barriers
+    // value-2 walk, then value-1 walk, level by level
 #pragma unroll 1
     for (int phase = 0; phase < 2; phase++) {
       int lo = phase == 0 ? 0 : s_qseed;
@@ -214,19 +251,17 @@ __global__ void __launch_bounds__(BS) ldir_pass_kernel(uint8_t* __restrict__ g, 
       if (phase == 1) {
         __syncthreads();
         for (int w = tid; w < T::NW; w += BS) s_vis[w] = 0;
-        __syncthreads();
-        for (int k = lo + tid; k < hi; k += BS) atomicOr(&s_vis[sq[k] >> 5], 1u << (sq[k] & 31));
         if (tid == 0) s_qtail = 0;
         __syncthreads();
       }
 #pragma unroll 1
       while (lo < hi) {
-        for (int k = lo + tid; k < hi; k += BS) {
-          int it = sq[k];
-          while (it >= 0) it = W.step(it, phase);
+        for (int k0 = lo; k0 < hi; k0 += BS) {
+          const int k = k0 + tid;
+          if (k < hi) W.step(sq[k], phase);
         }
         __syncthreads();
-        // the first value-1 wave came from the seed region; later waves from 0
+        // the first value-1 level came from the seed region; later levels from 0
         const int nlo = (phase == 1 && hi == NL) ? 0 : hi;
         const int nhi = s_qtail;
         __syncthreads();

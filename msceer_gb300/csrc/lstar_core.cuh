@@ -222,55 +222,58 @@ struct LowerStarState {
     }
     constexpr uint32_t DM1 = N::dim_mask(1), DM2 = N::dim_mask(2), DM3 = N::dim_mask(3);
     constexpr uint32_t AX0 = N::axis_mask(0, 0), AX1 = N::axis_mask(1, 0), AX2 = N::axis_mask(2, 0);
-    for (int dd = 1; dd <= ND; dd++) {
-      const uint32_t DMd = dd == 1 ? DM1 : (dd == 2 ? DM2 : DM3);
-      const uint32_t DMu = dd == 1 ? DM2 : (dd == 2 ? DM3 : 0u);
-      uint32_t U = S & DMd & ~P;
-      while (U) {
-        const uint32_t A = S & ~P;  // unprocessed cells of the class
-        const uint32_t F0 = N::template facet_in<0>(A);
-        const uint32_t F1 = N::template facet_in<1>(A);
-        const uint32_t F2 = (ND == 3) ? N::template facet_in<2>(A) : 0u;
-        const uint32_t one = (F0 ^ F1 ^ F2) & ~(F0 & F1 & F2);  // exactly one unprocessed facet
-        const uint32_t R = A & DMu & one;                       // ready (d+1)-cells
-        uint32_t Q = N::template facet_of<0>(R, F0) | N::template facet_of<1>(R, F1);
-        if (ND == 3) Q |= N::template facet_of<2>(R, F2);
-        if (Q) {
-          const int q = ffs32(Q) - 1;
-          int best = -1, bestlv = -1;
+    // One step per iteration, always in the lowest dimension that still has
+    // unprocessed cells -- the order of the reference's per-dimension loops -- so the
+    // loop body is the same straight-line set algebra for every thread of a warp.
+    for (int guard = 0; guard < N::NPOS; guard++) {
+      const uint32_t A = S & ~P;  // unprocessed cells of the class
+      if (!A) break;
+      const bool d1 = (A & DM1) != 0u, d2 = !d1 && (A & DM2) != 0u;
+      const uint32_t DMd = d1 ? DM1 : (d2 ? DM2 : DM3);
+      const uint32_t DMu = d1 ? DM2 : (d2 ? DM3 : 0u);
+      const uint32_t F0 = N::template facet_in<0>(A);
+      const uint32_t F1 = N::template facet_in<1>(A);
+      const uint32_t F2 = (ND == 3) ? N::template facet_in<2>(A) : 0u;
+      const uint32_t one = (F0 ^ F1 ^ F2) & ~(F0 & F1 & F2);  // exactly one unprocessed facet
+      const uint32_t R = A & DMu & one;                       // ready (d+1)-cells
+      uint32_t Q = N::template facet_of<0>(R, F0) | N::template facet_of<1>(R, F1);
+      if (ND == 3) Q |= N::template facet_of<2>(R, F2);
+      if (Q) {
+        const int q = ffs32(Q) - 1;
+        // ready cofacets of q, i.e. its candidates
+        uint32_t cm = 0;
+#pragma unroll
+        for (int a = 0; a < ND; a++) {
+          const uint32_t even = a == 0 ? AX0 : (a == 1 ? AX1 : AX2);
+          if ((even >> q) & 1u) cm |= (1u << (q + N::stride(a))) | (1u << (q - N::stride(a)));
+        }
+        cm &= R;
+        int best = ffs32(cm) - 1;
+        if (cm & (cm - 1)) {
+          // several: the first in cofacet order (+x,-x,+y,-y,+z,-z) whose lowest
+          // vertex comes first wins (PickLowestCandidate)
+          best = -1;
+          int bestlv = -1;
           float fb = 0.f;
 #pragma unroll
           for (int a = 0; a < ND; a++) {
-            const uint32_t even = a == 0 ? AX0 : (a == 1 ? AX1 : AX2);
-            if (!((even >> q) & 1u)) continue;
 #pragma unroll
-            for (int s = 0; s < 2; s++) {
-              const int c = s == 0 ? q + N::stride(a) : q - N::stride(a);
-              if (!((R >> c) & 1u)) continue;
-              if (best < 0) {
+            for (int sgn = 0; sgn < 2; sgn++) {
+              const int c = q + (sgn == 0 ? N::stride(a) : -N::stride(a));
+              if (c < 0 || c >= N::NPOS || !((cm >> c) & 1u)) continue;
+              const int lv = lowv(c);
+              const float fl = val(lv);
+              if (best < 0 || before(fl, lv, fb, bestlv)) {
                 best = c;
-              } else {
-                if (bestlv < 0) {
-                  bestlv = lowv(best);
-                  fb = val(bestlv);
-                }
-                const int lv = lowv(c);
-                const float fl = val(lv);
-                if (before(fl, lv, fb, bestlv)) {
-                  best = c;
-                  bestlv = lv;
-                  fb = fl;
-                }
+                bestlv = lv;
+                fb = fl;
               }
             }
           }
-          make_pair(q, best);
-          U &= ~(1u << q);
-        } else {
-          const int q = lowest_of(U);
-          make_critical(q);
-          U &= ~(1u << q);
         }
+        make_pair(q, best);
+      } else {
+        make_critical(lowest_of(A & DMd));
       }
     }
   }
