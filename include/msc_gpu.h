@@ -48,8 +48,9 @@ int msc_version(void);
 /* Text of the last error raised on the calling thread ("" if none). */
 const char* msc_last_error_string(void);
 
-/* Ascending-manifold tile passes run by the last .grad / stage-2 call on the
- * calling thread (a diagnostic; each pass is one kernel launch). */
+/* Kernel launches of the ascending-manifold stage in the last .grad / stage-2 call
+ * on the calling thread (a diagnostic: one tile pass, one halo check, then one
+ * launch per round of frontier walks). */
 int msc_last_ldir_passes(void);
 
 /* Number of cells (= .grad bytes) of the complex: TopologicalRegularGrid3D::numCells
@@ -83,7 +84,7 @@ int msc_lower_star_pairs_2d(const float* f, const int64_t dims[2], uint8_t* grad
 
 /* Stage 2 alone: completes the ldir bits of a stage-1 .grad in place
  * (setAscendingManifoldDimensions, gi_topological_gradient_using_algorithms.h:430-478).
- * passes_out (optional) receives the number of tile passes run. */
+ * passes_out (optional) receives the number of kernel launches of the stage. */
 int msc_ascending_manifold_dims_3d(uint8_t* grad, const int64_t dims[3], msc_stream_t stream, int* passes_out);
 int msc_ascending_manifold_dims_2d(uint8_t* grad, const int64_t dims[2], msc_stream_t stream, int* passes_out);
 
@@ -107,6 +108,11 @@ typedef struct {
   int iteration_limit;       /* Euler steps per streamline (e.g. 4000) */
   float max_step;            /* largest step, in voxels (reference default 0.5) */
   float presimp_threshold;   /* extrema joined by a saddle of lower persistence merge (0 = none) */
+  int precision;             /* boundary re-decisions.  0 (default): FP32, and FP64 for streamlines
+                                that stop at low gradient or within 1/64 voxel of the plane where
+                                their nearest vertex would change to one of another certain region;
+                                2: FP32, FP64 for every ending at low gradient or in a voxel
+                                touching two certain regions; 1: all in FP64 (slow on GB300) */
 } msc_integ_params;
 
 /* Ascending (minima basins) and descending (maxima mountains) 3-manifold labels of
@@ -122,7 +128,9 @@ typedef struct {
  * ascending pass zeroed at the minima, as the reference does).  A label is the
  * vertex id of its region's extremum (smallest seed vertex of a merged group), -1
  * for none.  The first integration pass runs in FP32; vertices next to a label
- * boundary are re-decided in FP64 with the reference's arithmetic.  Blocking. */
+ * boundary are re-decided in FP32, and those whose FP32 streamline ends
+ * ambiguously (see msc_integ_params.precision) again in FP64 with the reference's
+ * arithmetic.  Blocking. */
 int msc_integrated_labels_3d(const float* f, const uint8_t* grad, const int64_t dims[3], const msc_integ_params* params,
                              int32_t* labels_asc, int32_t* labels_dsc, msc_stream_t stream);
 /* Same, also writing 4*X*Y*Z stage labels: terminal and integrated (before the
@@ -132,6 +140,9 @@ int msc_integrated_labels_3d_stages(const float* f, const uint8_t* grad, const i
                                     int32_t* stages, msc_stream_t stream);
 /* Error text of the last failed labeling call on the calling thread. */
 const char* msc_labels_last_error_string(void);
+/* Work counts of the last labeling call on the calling thread: boundary
+ * re-decisions (ascending), of which in FP64, then the same for descending. */
+void msc_labels_last_stats(int64_t out[4]);
 
 /* Stage 2 for callers that may not allocate device memory: the same result as
  * msc_ascending_manifold_dims_3d, with the pass scratch (tile flags, status words)

@@ -42,6 +42,13 @@ SIGNATURES = {
     "msc_integrated_labels_3d": (ctypes.c_int, [_VP, _VP, _I64P, _VP, _VP, _VP, _VP]),
     "msc_integrated_labels_3d_stages": (ctypes.c_int, [_VP, _VP, _I64P, _VP, _VP, _VP, _VP, _VP]),
     "msc_labels_last_error_string": (ctypes.c_char_p, []),
+    "msc_labels_last_stats": (None, [_I64P]),
+    "msc_triage_last_error_string": (ctypes.c_char_p, []),
+    "msc_triage_features_3d": (ctypes.c_int, [_VP, _VP, _I64P, _VP, _VP, _VP, _VP]),
+    "msc_triage_forward_3d": (ctypes.c_int, [_VP, _I64P, _VP, _VP, _VP, _VP, _VP]),
+    "msc_triage_backward_3d": (ctypes.c_int, [_VP, _VP, _VP, _VP, _VP, _I64P, _VP, ctypes.c_float, _VP, _VP, _VP]),
+    "msc_triage_adam_step": (ctypes.c_int, [_VP, _VP, _VP, _VP, ctypes.c_int, ctypes.c_float, _VP]),
+    "msc_triage_labels_3d": (ctypes.c_int, [_VP, _VP, _I64P, _VP, _VP, _VP, _VP, _I64P, _VP]),
     "msc_steepest_lstar_host": (ctypes.c_int, [_VP, _I64P, _VP]),
     "msc_lower_star_grad_2d_host": (ctypes.c_int, [_VP, _I64P, _VP]),
 }
@@ -51,7 +58,7 @@ class IntegParams(ctypes.Structure):
     """msc_integ_params (include/msc_gpu.h)."""
     _fields_ = [("error_threshold", ctypes.c_float), ("gradient_threshold", ctypes.c_float),
                 ("iteration_limit", ctypes.c_int), ("max_step", ctypes.c_float),
-                ("presimp_threshold", ctypes.c_float)]
+                ("presimp_threshold", ctypes.c_float), ("precision", ctypes.c_int)]
 
 
 class MscError(RuntimeError):

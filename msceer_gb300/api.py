@@ -112,13 +112,17 @@ def ascending_manifold_dims(grad, dims) -> int:
 
 
 def integrated_labels(f, grad, error_threshold=1e-4, gradient_threshold=None, iteration_limit=4000,
-                      max_step=0.25, presimp_threshold=0.0, ascending=True, descending=True, stages=False):
+                      max_step=0.25, presimp_threshold=0.0, ascending=True, descending=True, stages=False,
+                      precision=0):
     """ondemandaccurate's ascending / descending 3-manifold labels of a device volume.
 
     ``f``: CUDA float32 (Z, Y, X); ``grad``: its .grad from :func:`lower_star_grad`.
-    ``gradient_threshold`` defaults to 1e-6 of max|f|.  Returns a dict with "asc" and/or
-    "dsc" int32 tensors (a label is the vertex id of the region's extremum, -1 none)
-    and, with ``stages``, the terminal / integrated labels of each direction."""
+    ``gradient_threshold`` defaults to 1e-6 of max|f|.  ``precision`` 0 re-decides
+    boundary vertices in FP32 and the ambiguous ones in FP64; 1 re-decides all of them
+    in FP64.  Returns a dict with "asc" and/or "dsc" int32 tensors (a label is the
+    vertex id of the region's extremum, -1 none), "stats" (boundary re-decisions and
+    FP64 ones per direction) and, with ``stages``, the terminal / integrated labels of
+    each direction."""
     import torch
 
     if not (f.is_cuda and grad.is_cuda):
@@ -129,7 +133,8 @@ def integrated_labels(f, grad, error_threshold=1e-4, gradient_threshold=None, it
         raise ValueError("integrated labels are defined for 3D volumes")
     if gradient_threshold is None:
         gradient_threshold = 1e-6 * float(f.abs().max())
-    p = _lib.IntegParams(error_threshold, gradient_threshold, iteration_limit, max_step, presimp_threshold)
+    p = _lib.IntegParams(error_threshold, gradient_threshold, iteration_limit, max_step, presimp_threshold,
+                         int(precision))
     n = f.numel()
     asc = torch.empty(n, dtype=torch.int32, device=f.device) if ascending else None
     dsc = torch.empty(n, dtype=torch.int32, device=f.device) if descending else None
@@ -145,7 +150,10 @@ def integrated_labels(f, grad, error_threshold=1e-4, gradient_threshold=None, it
             rc = lib.msc_integrated_labels_3d(ptr(f), ptr(grad), _lib.dims_arg(dims), ctypes.byref(p), ptr(asc),
                                               ptr(dsc), ctypes.c_void_p(stream))
     _lib.check(rc, "msc_integrated_labels_3d")
-    out = {}
+    stats = (ctypes.c_int64 * 4)()
+    lib.msc_labels_last_stats(stats)
+    out = {"stats": {"asc_redecided": stats[0], "asc_fp64": stats[1], "dsc_redecided": stats[2],
+                     "dsc_fp64": stats[3]}}
     if asc is not None:
         out["asc"] = asc
     if dsc is not None:

@@ -24,12 +24,6 @@ namespace msc {
 
 enum { EV_NONE = 0, EV_OUT_OF_VOXEL, EV_OVER_MAX_ITERATIONS, EV_LOW_GRADIENT, EV_HIT_EXTREMUM, EV_HIT_PREASSIGNED };
 
-struct IntegParams {
-  float ethresh, gthresh;
-  int iteration_limit;
-  double max_step;
-  int step_mult;  // -1: flow downhill (ascending manifolds of minima), +1 uphill
-};
 
 __device__ __forceinline__ int64_t vid(const VolDims& V, int64_t x, int64_t y, int64_t z) { return x + V.X * (y + V.Y * z); }
 
@@ -52,7 +46,8 @@ struct Adv32 {
   const float4* G;
   VolDims V;
   IntegParams P;
-  const int32_t* lab;  // pass-1 stop: nearest vertex labelled (assigned or terminal)
+  const int32_t* lab;     // pass-1 stop: nearest vertex labelled (assigned or terminal)
+  const uint8_t* state;  // fix-up stop (when set): nearest vertex certain terminal
 
   __device__ __forceinline__ F3 corner(int64_t x, int64_t y, int64_t z) const {
     const float4 g = __ldg(G + vid(V, x, y, z));
@@ -129,7 +124,13 @@ struct Adv32 {
         }
         cur = np;
         step = fminf(step * 1.8f, ms / gm);
-        if (lab[nearest(cur, nearb)] != -1) return EV_HIT_PREASSIGNED;
+        const int64_t nv = nearest(cur, nearb);
+        if (state) {
+          const uint8_t st = state[nv];
+          if (st == kStSeed || st == kStTerminal) return EV_HIT_PREASSIGNED;
+        } else if (lab[nv] != -1) {
+          return EV_HIT_PREASSIGNED;
+        }
       } else {
         step = step * 0.5f;
       }
@@ -147,12 +148,6 @@ __device__ __forceinline__ int dist_to_boundary(const VolDims& V, int64_t x, int
   return (int)m;
 }
 
-// Spread visiting order of the first pass (:166-174 with one thread): level L
-// visits start_L + j * stride_L.  Host-computed tables, levels in order.
-struct SpreadOrder {
-  int nlev;
-  int64_t start[48], stride[48], offset[49];
-};
 
 constexpr int kPathCap = 48;
 
@@ -365,6 +360,97 @@ __global__ void __launch_bounds__(128) fixup_kernel(const Adv64 A, int32_t* __re
   }
 }
 
+// One FP32 fix-up wave.  A streamline whose FP32 ending is ambiguous goes to the FP64
+// list instead of being decided here:
+//   it stopped at low gradient (the FP64 stop test decides), or
+//   amb_mode 0: its final point lies within 1/64 voxel of the plane where the
+//     nearest vertex changes, and the vertex across that plane belongs to a
+//     different certain region (FP32 rounding may have picked the wrong side);
+//   amb_mode 2: its final voxel touches two different certain regions (any ending
+//     within half a voxel of a basin boundary).
+__global__ void __launch_bounds__(128) fixup32_kernel(const Adv32 A, int32_t* __restrict__ lab,
+                                                      uint8_t* __restrict__ state, const int64_t* __restrict__ list,
+                                                      int n, int64_t* __restrict__ next, int* __restrict__ n_next,
+                                                      uint32_t* __restrict__ queued, int64_t* __restrict__ amb,
+                                                      int* __restrict__ n_amb, int amb_mode) {
+  const VolDims& V = A.V;
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+    const int64_t v = list[k];
+    const int32_t init = lab[v];
+    int64_t x = v % V.X, y = (v / V.X) % V.Y, z = v / (V.X * V.Y);
+    F3 cur = {(float)x, (float)y, (float)z};
+    int iters = A.P.iteration_limit;
+    int64_t end = v;
+    int ev;
+    while (true) {
+      const bool nb = dist_to_boundary(V, x, y, z) <= 1;
+      ev = A.advect(cur, iters, nb);
+      end = A.nearest(cur, nb);
+      x = end % V.X;
+      y = (end / V.X) % V.Y;
+      z = end / (V.X * V.Y);
+      if (ev != EV_OUT_OF_VOXEL) break;
+    }
+    bool ambiguous = ev == EV_LOW_GRADIENT;
+    if (!ambiguous && ev == EV_HIT_PREASSIGNED && amb_mode == 0) {
+      const float pc[3] = {cur.x, cur.y, cur.z};
+      const int64_t ext[3] = {V.X, V.Y, V.Z};
+      const int64_t ev3[3] = {x, y, z};
+      const int32_t le = lab[end];
+#pragma unroll
+      for (int a = 0; a < 3; a++) {
+        const float q = pc[a] + 0.5f;
+        const float r = q - floorf(q);
+        if (fminf(r, 1.f - r) >= (1.f / 64.f)) continue;
+        const int64_t alt_c = ev3[a] + (r < 0.5f ? -1 : 1);
+        if (alt_c < 0 || alt_c >= ext[a]) continue;
+        int64_t ac[3] = {ev3[0], ev3[1], ev3[2]};
+        ac[a] = alt_c;
+        const int64_t u = vid(V, ac[0], ac[1], ac[2]);
+        const uint8_t st = state[u];
+        if ((st == kStSeed || st == kStTerminal) && lab[u] != le) ambiguous = true;
+      }
+    } else if (!ambiguous && ev == EV_HIT_PREASSIGNED) {
+      const int64_t b[3] = {(int64_t)fminf(fmaxf(cur.x, 0.f), (float)(V.X - 2)),
+                            (int64_t)fminf(fmaxf(cur.y, 0.f), (float)(V.Y - 2)),
+                            (int64_t)fminf(fmaxf(cur.z, 0.f), (float)(V.Z - 2))};
+      int32_t seen = kLabelNone;
+#pragma unroll
+      for (int c = 0; c < 8; c++) {
+        const int64_t u = vid(V, b[0] + (c & 1), b[1] + ((c >> 1) & 1), b[2] + (c >> 2));
+        const uint8_t st = state[u];
+        if (st != kStSeed && st != kStTerminal) continue;
+        const int32_t l = lab[u];
+        if (seen == kLabelNone) seen = l;
+        else if (l != seen) ambiguous = true;
+      }
+    }
+    if (ambiguous) {
+      amb[atomicAdd(n_amb, 1)] = v;  // keeps its queued bit until the FP64 wave
+      continue;
+    }
+    atomicAnd(&queued[v >> 5], ~(1u << (v & 31)));
+    int32_t nl = lab[end];
+    if (nl == -1) nl = kLabelNone;
+    lab[v] = nl;
+    state[v] = kStNonterminal;
+    if (nl == init) continue;
+    x = v % V.X;
+    y = (v / V.X) % V.Y;
+    z = v / (V.X * V.Y);
+    const int64_t nbr[6] = {x < V.X - 1 ? v + 1 : -1, x > 0 ? v - 1 : -1, y < V.Y - 1 ? v + V.X : -1,
+                            y > 0 ? v - V.X : -1, z < V.Z - 1 ? v + V.X * V.Y : -1, z > 0 ? v - V.X * V.Y : -1};
+#pragma unroll
+    for (int j = 0; j < 6; j++) {
+      const int64_t u = nbr[j];
+      if (u < 0 || state[u] != kStUnassigned || lab[u] == nl) continue;
+      const uint32_t bit = 1u << (u & 31);
+      if (atomicOr(&queued[u >> 5], bit) & bit) continue;
+      next[atomicAdd(n_next, 1)] = u;
+    }
+  }
+}
+
 // ---- K5c: isolated-region cleaner --------------------------------------------------------
 
 __device__ __forceinline__ bool comes_before(const float* f, int dir, int64_t a, int64_t b) {
@@ -454,7 +540,7 @@ __global__ void clean_resolve_kernel(const int32_t* __restrict__ lab, const VolD
 
 cudaError_t launch_integrate_pass1(const float4* G, const VolDims& V, const IntegParams& P, const SpreadOrder& S,
                                    int32_t* lab, int num_sms, cudaStream_t stream) {
-  Adv32 A{G, V, P, lab};
+  Adv32 A{G, V, P, lab, nullptr};
   integrate_pass1_kernel<<<num_sms * 16, 128, 0, stream>>>(A, S, lab, nullptr);
   return cudaGetLastError();
 }
@@ -473,6 +559,18 @@ cudaError_t launch_fixup(const double* G, const VolDims& V, const IntegParams& P
   const int blocks = (n + 127) / 128;
   fixup_kernel<<<blocks < num_sms * 16 ? blocks : num_sms * 16, 128, 0, stream>>>(A, lab, state, list, n, next, n_next,
                                                                                   queued);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_fixup32(const float4* G, const VolDims& V, const IntegParams& P, int32_t* lab, uint8_t* state,
+                           const int64_t* list, int n, int64_t* next, int* n_next, uint32_t* queued, int64_t* amb,
+                           int* n_amb, int amb_mode, int num_sms, cudaStream_t stream) {
+  if (n <= 0) return cudaSuccess;
+  Adv32 A{G, V, P, lab, state};
+  const int blocks = (n + 127) / 128;
+  fixup32_kernel<<<blocks < num_sms * 16 ? blocks : num_sms * 16, 128, 0, stream>>>(A, lab, state, list, n, next,
+                                                                                    n_next, queued, amb, n_amb,
+                                                                                    amb_mode);
   return cudaGetLastError();
 }
 

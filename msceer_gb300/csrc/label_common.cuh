@@ -88,4 +88,32 @@ int64_t terminal_num_tiles(const VolDims& V);
 cudaError_t launch_terminal_pass(const float* f, int32_t* lab, const VolDims& V, int dir, const uint8_t* dirty_in,
                                  uint8_t* dirty_out, int* changed, int* err, int num_sms, cudaStream_t stream);
 
+// ---- K4 streamline integration (integrate_kernels.cu) ----------------------------------------
+struct IntegParams {
+  float ethresh, gthresh;
+  int iteration_limit;
+  double max_step;
+  int step_mult;  // -1: flow downhill (ascending manifolds of minima), +1 uphill
+};
+
+// Spread visiting order of the first pass (:166-174 with one thread): level L
+// visits start_L + j * stride_L.  Host-computed tables, levels in order.
+struct SpreadOrder {
+  int nlev;
+  int64_t start[48], stride[48], offset[49];
+};
+
+cudaError_t launch_integrate_pass1(const float4* G, const VolDims& V, const IntegParams& P, const SpreadOrder& S,
+                                   int32_t* lab, int num_sms, cudaStream_t stream);
+cudaError_t launch_boundary_set(const int32_t* lab, const uint8_t* state, const VolDims& V, int64_t* list, int* n,
+                                uint32_t* queued, int num_sms, cudaStream_t stream);
+cudaError_t launch_fixup(const double* G, const VolDims& V, const IntegParams& P, int32_t* lab, uint8_t* state,
+                         const int64_t* list, int n, int64_t* next, int* n_next, uint32_t* queued, int num_sms,
+                         cudaStream_t stream);
+cudaError_t launch_fixup32(const float4* G, const VolDims& V, const IntegParams& P, int32_t* lab, uint8_t* state,
+                           const int64_t* list, int n, int64_t* next, int* n_next, uint32_t* queued, int64_t* amb,
+                           int* n_amb, int amb_mode, int num_sms, cudaStream_t stream);
+cudaError_t launch_clean(const int32_t* lab, const float* f, const VolDims& V, int dir, int64_t* parent, int64_t* target,
+                         int32_t* out, int num_sms, cudaStream_t stream);
+
 }  // namespace msc

@@ -12,15 +12,19 @@
 // (items quads, cofacets hexes).  K1 already wrote the roots (critical 1-cells = 2,
 // critical 2-cells = 1, critical 3-cells = 0, everything else 3).
 //
-// GPU form: repeated passes of a tile kernel.  A CTA stages a tile of .grad bytes
-// plus a 2-cell halo in shared memory (every rule reaches at most 2 cells), seeds a
-// shared-memory queue with the marked items, runs the value-2 walk to its local
-// fixpoint, then the value-1 walk, and writes back the tile's changed bytes.  Marks
-// in the halo stay local.  The first pass seeds every marked item; later passes only
-// revisit tiles whose halo changed (a neighbour wrote a cell within 2 cells of the
-// shared border) and seed only from the halo, because everything reachable from the
-// interior was already walked.  The closure is complete when a pass changes no cell
-// near any tile border.
+// GPU form: a tile kernel.  A CTA stages a tile of .grad bytes plus a 2-cell halo in
+// shared memory (every rule reaches at most 2 cells), seeds a shared-memory queue
+// with the marked items, runs the value-2 walk to its local fixpoint, then the
+// value-1 walk, and writes back the tile.  Marks in the halo stay local.  Two ways
+// finish the closure across tile borders:
+//   single pass (default)  one tile pass saves every tile's final box; a check kernel
+//       lowers the cells some neighbour's saved halo holds lower and queues the
+//       lowered items; a walk kernel finishes their walks in global memory.
+//   multi pass (fallback, and the allocation-free entry)  repeated tile passes; later
+//       passes revisit only tiles whose halo changed (a neighbour wrote a cell within
+//       2 cells of the shared border) and seed only from the halo, because everything
+//       reachable from the interior was already walked.  The closure is complete when
+//       a pass changes no cell near any tile border.
 #include "msc_device.cuh"
 
 namespace msc {
@@ -78,7 +82,9 @@ struct LdirWalk {
   int lmin[3], lmax[3];  // in-complex local range per axis
   uint32_t dec_map;
 
-  __device__ __forceinline__ void touch(int c) { atomicOr(&dirty[c >> 5], 1u << (c & 31)); }
+  __device__ __forceinline__ void touch(int c) {
+    if (dirty) atomicOr(&dirty[c >> 5], 1u << (c & 31));
+  }
 
   // returns the item to queue, or -1
   __device__ __forceinline__ int visit(int i, int l[3], int a, int sgn, int phase) {
@@ -301,6 +307,318 @@ __global__ void __launch_bounds__(BS) ldir_pass_kernel(uint8_t* __restrict__ g, 
   }
 }
 
+// ---- single-pass form: one tile pass, a halo check, a global frontier walk -------------------
+//
+// A tile's walk is complete for every item of its interior (all of an item's rule
+// reaches lies within 2 cells), so after one pass over all tiles the only missing
+// marks are those a tile made in its halo that the halo's owner did not make itself.
+// The pass therefore saves each tile's final box; the check kernel lowers every
+// global cell that some tile's saved halo holds lower, and queues the lowered items,
+// whose walk may need to continue beyond that tile's box; the walk kernel finishes
+// those walks in global memory.  Concurrent lowering of a byte uses a compare-and-swap
+// on its aligned 32-bit word (the low five bits never change, so the ldir field only
+// ever decreases); bytes whose word is not wholly inside the .grad array go through a
+// bounded spin lock instead.
+
+struct GradView {
+  uint8_t* g;
+  uintptr_t lo, hi;  // [first, last) byte address of the array
+  int* lock;
+  int* err;
+};
+
+// ldir(c) = min(ldir(c), val); true if this call lowered it
+__device__ __forceinline__ bool lower_ldir(const GradView& G, int64_t c, unsigned val) {
+  const uintptr_t a = reinterpret_cast<uintptr_t>(G.g + c);
+  const uintptr_t wa = a & ~uintptr_t(3);
+  if (wa >= G.lo && wa + 4 <= G.hi) {
+    uint32_t* w = reinterpret_cast<uint32_t*>(wa);
+    const int sh = (int)(a & 3u) * 8;
+    uint32_t cur = *reinterpret_cast<volatile uint32_t*>(w);
+    for (int guard = 0; guard < 64; guard++) {
+      const uint32_t b = (cur >> sh) & 0xFFu;
+      if ((b >> 5) <= val) return false;
+      const uint32_t nb = (b & 0x1Fu) | (val << 5);
+      const uint32_t nw = (cur & ~(0xFFu << sh)) | (nb << sh);
+      const uint32_t prev = atomicCAS(w, cur, nw);
+      if (prev == cur) return true;
+      cur = prev;
+    }
+    atomicOr(G.err, kErrPassLimit);
+    return false;
+  }
+  // a word that reaches outside the array: serialise on the lock
+  bool got = false;
+  for (int guard = 0; guard < (1 << 20) && !got; guard++) got = atomicCAS(G.lock, 0, 1) == 0;
+  if (!got) {
+    atomicOr(G.err, kErrPassLimit);
+    return false;
+  }
+  __threadfence();
+  volatile uint8_t* p = G.g + c;
+  const uint8_t b = *p;
+  const bool lowered = (unsigned)(b >> 5) > val;
+  if (lowered) *p = (uint8_t)((b & 0x1Fu) | (val << 5));
+  __threadfence();
+  atomicExch(G.lock, 0);
+  return lowered;
+}
+
+template <int ND, int TX, int TY, int TZ, int BS>
+__global__ void __launch_bounds__(BS) ldir_tile_kernel(uint8_t* __restrict__ g, const GradDims D,
+                                                       uint8_t* __restrict__ saved, int* __restrict__ err) {
+  using T = LdirTile<ND, TX, TY, TZ>;
+  constexpr int NL = T::NL;
+  static_assert(NL < 65536, "local ids are 16-bit");
+  extern __shared__ __align__(16) unsigned char s_dyn[];
+  uint16_t* sq = reinterpret_cast<uint16_t*>(s_dyn);
+  uint8_t* sg = s_dyn + (size_t)NL * 2;
+  uint32_t* s_vis = reinterpret_cast<uint32_t*>(s_dyn + (size_t)NL * 2 + ((NL + 3) / 4) * 4);
+  __shared__ int s_qtail, s_qseed;
+
+  const int tid = threadIdx.x, lane = tid & 31;
+  const int64_t dX = D.d[0], dY = D.d[1], dZ = D.d[2];
+  const int64_t ntx = (dX + TX - 1) / TX, nty = (dY + TY - 1) / TY;
+  const int64_t ntz = (ND == 3) ? (dZ + TZ - 1) / TZ : 1;
+  const int64_t ntiles = ntx * nty * ntz;
+
+  LdirWalk<T, ND> W;
+  W.sg = sg;
+  W.sq = sq;
+  W.vis = s_vis;
+  W.dirty = nullptr;
+  W.qtail = &s_qtail;
+  W.err = err;
+  W.dec_map = D.dec_map;
+
+  for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+    const int64_t tx = tile % ntx, ty = (tile / ntx) % nty, tz = (ND == 3) ? tile / (ntx * nty) : 0;
+    const int64_t o[3] = {tx * TX - T::H, ty * TY - T::H, (ND == 3) ? tz * TZ - T::H : 0};
+    const int64_t dd[3] = {dX, dY, dZ};
+    constexpr int LE[3] = {T::LX, T::LY, T::LZ};
+#pragma unroll
+    for (int a = 0; a < 3; a++) {
+      W.lmin[a] = (int)(o[a] < 0 ? -o[a] : 0);
+      const int64_t hi = dd[a] - o[a];
+      W.lmax[a] = (int)(hi < LE[a] ? hi : LE[a]);
+    }
+    if (tid == 0) {
+      s_qtail = 0;
+      s_qseed = NL;
+    }
+    for (int w = tid; w < T::NW; w += BS) s_vis[w] = 0;
+    __syncthreads();
+
+    // stage the box (cells outside the complex read as 0 = unassigned), many loads in
+    // flight per thread, and queue every marked item as a seed
+    constexpr int PER = (NL + BS - 1) / BS;
+    constexpr int U = 8;
+#pragma unroll 1
+    for (int j0 = 0; j0 < PER; j0 += U) {
+      uint8_t v[U];
+#pragma unroll
+      for (int u = 0; u < U; u++) {
+        const int k = (j0 + u) * BS + tid;
+        v[u] = 0;
+        if (j0 + u < PER && k < NL) {
+          const int lx = k % T::LX, row = k / T::LX;
+          const int ly = row % T::LY, lz = row / T::LY;
+          if (lx >= W.lmin[0] && lx < W.lmax[0] && ly >= W.lmin[1] && ly < W.lmax[1] && lz >= W.lmin[2] &&
+              lz < W.lmax[2])
+            v[u] = g[(o[0] + lx) + (o[1] + ly) * D.cs[1] + (o[2] + lz) * D.cs[2]];
+        }
+      }
+#pragma unroll
+      for (int u = 0; u < U; u++) {
+        const int k = (j0 + u) * BS + tid;
+        const bool valid = j0 + u < PER && k < NL;
+        int dim = 0;
+        if (valid) {
+          sg[k] = v[u];
+          const int lx = k % T::LX, row = k / T::LX;
+          const int ly = row % T::LY, lz = row / T::LY;
+          dim = (lx & 1) + (ly & 1) + (ND == 3 ? (lz & 1) : 0);
+        }
+        const unsigned ld = v[u] >> 5;
+        const bool s0 = valid && (v[u] & 1u) && dim == 1 && ld == 2u;
+        const bool s1 = valid && (v[u] & 1u) && dim == 2 && ld == 1u;
+        warp_push(sq, &s_qtail, NL, err, s0, k);
+        const unsigned m1 = __ballot_sync(0xffffffffu, s1);
+        if (m1) {
+          int base = 0;
+          if (lane == 0) base = atomicSub(&s_qseed, __popc(m1));
+          base = __shfl_sync(0xffffffffu, base, 0);
+          if (s1) sq[base - 1 - __popc(m1 & ((1u << lane) - 1u))] = (uint16_t)k;
+        }
+      }
+    }
+    __syncthreads();
+
+#pragma unroll 1
+    for (int phase = 0; phase < 2; phase++) {
+      int lo = phase == 0 ? 0 : s_qseed;
+      int hi = phase == 0 ? s_qtail : NL;
+      if (phase == 1) {
+        __syncthreads();
+        for (int w = tid; w < T::NW; w += BS) s_vis[w] = 0;
+        if (tid == 0) s_qtail = 0;
+        __syncthreads();
+      }
+#pragma unroll 1
+      while (lo < hi) {
+        for (int k0 = lo; k0 < hi; k0 += BS) {
+          const int k = k0 + tid;
+          if (k < hi) W.step(sq[k], phase);
+        }
+        __syncthreads();
+        const int nlo = (phase == 1 && hi == NL) ? 0 : hi;
+        const int nhi = s_qtail;
+        __syncthreads();
+        lo = nlo;
+        hi = nhi;
+      }
+    }
+    __syncthreads();
+
+    // write back the interior, a row per warp instruction, and save the whole box
+    constexpr int NI = TX * TY * (ND == 3 ? TZ : 1);
+    for (int k = tid; k < NI; k += BS) {
+      const int ix = k % TX, r = k / TX;
+      const int iy = r % TY, iz = r / TY;
+      const int64_t gx = o[0] + T::H + ix, gy = o[1] + T::H + iy, gz = o[2] + (ND == 3 ? T::H : 0) + iz;
+      if (gx < dX && gy < dY && gz < dZ)
+        g[gx + gy * D.cs[1] + gz * D.cs[2]] = sg[(ix + T::H) + T::LX * ((iy + T::H) + T::LY * (iz + (ND == 3 ? T::H : 0)))];
+    }
+    uint8_t* sv = saved + tile * (int64_t)NL;
+    for (int k = tid; k < NL; k += BS) sv[k] = sg[k];
+    __syncthreads();
+  }
+}
+
+// k-th halo cell of the box -> box index (z slabs, then y rows, then x columns)
+template <class T, int ND>
+__device__ __forceinline__ int halo_cell(int h) {
+  constexpr int H = T::H, LX = T::LX, LY = T::LY, LZ = T::LZ;
+  int lz = 0;
+  if (ND == 3) {
+    constexpr int SLAB = 2 * H * LX * LY;  // z < H and z >= LZ - H
+    if (h < SLAB) {
+      const int s = h / (LX * LY), r = h % (LX * LY);
+      lz = s < H ? s : LZ - 2 * H + s;
+      return r + LX * LY * lz;
+    }
+    h -= SLAB;
+  }
+  constexpr int P = 2 * H * LX + 2 * H * (LY - 2 * H);  // halo cells of one inner plane
+  lz = (ND == 3 ? H : 0) + h / P;
+  int r = h % P;
+  int lx, ly;
+  if (r < 2 * H * LX) {
+    const int s = r / LX;
+    ly = s < H ? s : LY - 2 * H + s;
+    lx = r % LX;
+  } else {
+    r -= 2 * H * LX;
+    const int s = r / (LY - 2 * H);
+    lx = s < H ? s : LX - 2 * H + s;
+    ly = H + r % (LY - 2 * H);
+  }
+  return lx + LX * (ly + LY * lz);
+}
+
+template <class T, int ND>
+__host__ __device__ constexpr int halo_count() {
+  return (ND == 3 ? 2 * T::H * T::LX * T::LY : 0) +
+         (ND == 3 ? (T::LZ - 2 * T::H) : 1) * (2 * T::H * T::LX + 2 * T::H * (T::LY - 2 * T::H));
+}
+
+__device__ __forceinline__ void push_item(int64_t* q, int* n, int cap, int* err, int64_t c) {
+  const int slot = atomicAdd(n, 1);
+  if (slot < cap) q[slot] = c; else atomicOr(err, kErrLocalQueue);
+}
+
+template <int ND, int TX, int TY, int TZ>
+__global__ void ldir_check_kernel(const GradView G, const GradDims D, const uint8_t* __restrict__ saved,
+                                  int64_t* __restrict__ queue, int* __restrict__ n_queue, int cap) {
+  using T = LdirTile<ND, TX, TY, TZ>;
+  constexpr int NH = halo_count<T, ND>();
+  const int64_t dX = D.d[0], dY = D.d[1], dZ = D.d[2];
+  const int64_t ntx = (dX + TX - 1) / TX, nty = (dY + TY - 1) / TY;
+  const int64_t ntz = (ND == 3) ? (dZ + TZ - 1) / TZ : 1;
+  const int64_t total = ntx * nty * ntz * NH;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t tile = e / NH;
+    const int b = halo_cell<T, ND>((int)(e % NH));
+    const uint8_t s = saved[tile * T::NL + b];
+    if (!(s & 1u)) continue;  // outside the complex, or nothing there
+    const int64_t tx = tile % ntx, ty = (tile / ntx) % nty, tz = (ND == 3) ? tile / (ntx * nty) : 0;
+    const int lx = b % T::LX, ly = (b / T::LX) % T::LY, lz = b / (T::LX * T::LY);
+    const int64_t gx = tx * TX - T::H + lx, gy = ty * TY - T::H + ly, gz = (ND == 3) ? tz * TZ - T::H + lz : 0;
+    const int64_t c = gx + gy * D.cs[1] + gz * D.cs[2];
+    const unsigned v = s >> 5;
+    if ((unsigned)(G.g[c] >> 5) <= v) continue;
+    if (!lower_ldir(G, c, v)) continue;
+    const int dim = (int)((gx & 1) + (gy & 1) + (gz & 1));
+    if ((dim == 1 && v == 2u) || (dim == 2 && v == 1u)) push_item(queue, n_queue, cap, G.err, c);
+  }
+}
+
+// Finish the walks of queued items in global memory, depth first with a short
+// per-thread stack; what does not fit goes to the next round's queue.
+template <int ND>
+__global__ void __launch_bounds__(128) ldir_walk_kernel(const GradView G, const GradDims D,
+                                                        const int64_t* __restrict__ qin, int n_in,
+                                                        int64_t* __restrict__ qout, int* __restrict__ n_out, int cap) {
+  constexpr int SD = 24;
+  int64_t stack[SD];
+  const int64_t st[3] = {D.cs[0], D.cs[1], D.cs[2]};
+  const int64_t dd[3] = {D.d[0], D.d[1], D.d[2]};
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n_in; k += gridDim.x * blockDim.x) {
+    int sp = 0;
+    stack[sp++] = qin[k];
+    while (sp > 0) {
+      const int64_t i = stack[--sp];
+      int64_t l[3];
+      l[0] = i % dd[0];
+      l[1] = (i / dd[0]) % dd[1];
+      l[2] = (ND == 3) ? i / (dd[0] * dd[1]) : 0;
+      const int dim = (int)((l[0] & 1) + (l[1] & 1) + (l[2] & 1));
+      const unsigned value = dim == 1 ? 2u : 1u;  // edges walk the value-2 closure, quads value 1
+#pragma unroll
+      for (int a = 0; a < ND; a++) {
+        if (l[a] & 1) continue;  // cofacets only along even axes, +axis first
+#pragma unroll
+        for (int s = 0; s < 2; s++) {
+          const int sgn = s == 0 ? 1 : -1;
+          const int64_t la = l[a] + sgn;
+          if (la < 0 || la >= dd[a]) continue;
+          const int64_t t = i + sgn * st[a];
+          const uint8_t bt = *reinterpret_cast<volatile uint8_t*>(G.g + t);
+          const unsigned code = (bt >> 2) & 7u;
+          if (!(bt & 1u) || code == 7u) continue;
+          lower_ldir(G, t, value);
+          const int pc = map3(D.dec_map, (int)code);
+          const int pa = pc >> 1;
+          const int64_t tp = t + ((pc & 1) ? -st[pa] : st[pa]);
+          if (tp == i) continue;
+          int64_t lp[3] = {l[0], l[1], l[2]};
+          lp[a] += sgn;
+          lp[pa] += (pc & 1) ? -1 : 1;
+          if (lp[pa] < 0 || lp[pa] >= dd[pa]) continue;  // a pair code pointing out of the complex
+          const int pdim = (int)((lp[0] & 1) + (lp[1] & 1) + (lp[2] & 1));
+          if (value == 2u && pdim != 1) {  // a hex ends the value-2 path
+            lower_ldir(G, tp, 2u);
+            continue;
+          }
+          if (!lower_ldir(G, tp, value)) continue;
+          if (sp < SD) stack[sp++] = tp;
+          else push_item(qout, n_out, cap, G.err, tp);
+        }
+      }
+    }
+  }
+}
+
 namespace {
 constexpr int kTX3 = 32, kTY3 = 32, kTZ3 = 16, kBS3 = 512;
 constexpr int kTX2 = 128, kTY2 = 64, kBS2 = 256;
@@ -311,6 +629,53 @@ using Tile2 = LdirTile<2, kTX2, kTY2, 1>;
 int64_t ldir_num_tiles(int nd, const GradDims& D) {
   if (nd == 3) return ((D.d[0] + kTX3 - 1) / kTX3) * ((D.d[1] + kTY3 - 1) / kTY3) * ((D.d[2] + kTZ3 - 1) / kTZ3);
   return ((D.d[0] + kTX2 - 1) / kTX2) * ((D.d[1] + kTY2 - 1) / kTY2);
+}
+
+int64_t ldir_box_bytes(int nd) { return nd == 3 ? Tile3::NL : Tile2::NL; }
+
+cudaError_t launch_ldir_tile(int nd, uint8_t* g, const GradDims& D, uint8_t* saved, int* err, int num_sms,
+                             cudaStream_t stream) {
+  const int64_t nt = ldir_num_tiles(nd, D);
+  const int64_t cap = (int64_t)num_sms * 4;
+  const int grid = (int)(nt < cap ? nt : cap);
+  if (grid <= 0) return cudaSuccess;
+  if (nd == 3) {
+    auto k = ldir_tile_kernel<3, kTX3, kTY3, kTZ3, kBS3>;
+    const size_t sm = Tile3::smem_bytes();
+    cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    if (e != cudaSuccess) return e;
+    k<<<grid, kBS3, sm, stream>>>(g, D, saved, err);
+  } else {
+    auto k = ldir_tile_kernel<2, kTX2, kTY2, 1, kBS2>;
+    const size_t sm = Tile2::smem_bytes();
+    cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    if (e != cudaSuccess) return e;
+    k<<<grid, kBS2, sm, stream>>>(g, D, saved, err);
+  }
+  return cudaGetLastError();
+}
+
+cudaError_t launch_ldir_check(int nd, uint8_t* g, const GradDims& D, const uint8_t* saved, int64_t* queue, int* n_queue,
+                              int cap, int* lock, int* err, int num_sms, cudaStream_t stream) {
+  const GradView G{g, reinterpret_cast<uintptr_t>(g), reinterpret_cast<uintptr_t>(g + D.ncells), lock, err};
+  if (nd == 3)
+    ldir_check_kernel<3, kTX3, kTY3, kTZ3><<<num_sms * 8, 256, 0, stream>>>(G, D, saved, queue, n_queue, cap);
+  else
+    ldir_check_kernel<2, kTX2, kTY2, 1><<<num_sms * 8, 256, 0, stream>>>(G, D, saved, queue, n_queue, cap);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_ldir_walk(int nd, uint8_t* g, const GradDims& D, const int64_t* qin, int n_in, int64_t* qout,
+                             int* n_out, int cap, int* lock, int* err, int num_sms, cudaStream_t stream) {
+  if (n_in <= 0) return cudaSuccess;
+  const GradView G{g, reinterpret_cast<uintptr_t>(g), reinterpret_cast<uintptr_t>(g + D.ncells), lock, err};
+  const int blocks = (n_in + 127) / 128;
+  const int grid = blocks < num_sms * 16 ? blocks : num_sms * 16;
+  if (nd == 3)
+    ldir_walk_kernel<3><<<grid, 128, 0, stream>>>(G, D, qin, n_in, qout, n_out, cap);
+  else
+    ldir_walk_kernel<2><<<grid, 128, 0, stream>>>(G, D, qin, n_in, qout, n_out, cap);
+  return cudaGetLastError();
 }
 
 cudaError_t launch_ldir_pass(int nd, uint8_t* g, const GradDims& D, const uint8_t* dirty_in, uint8_t* dirty_out,

@@ -5,6 +5,9 @@
 // pass loop and error reporting.  Status codes only; nothing throws across the ABI.
 #include <cuda_runtime.h>
 
+#include <algorithm>
+#include <cstdlib>
+
 #include <cstdio>
 #include <cstring>
 #include <string>
@@ -111,10 +114,9 @@ int pairs_impl(int nd, const float* f, const int64_t* dims, uint8_t* g, cudaStre
   return MSC_OK;
 }
 
-int ldir_impl(int nd, uint8_t* g, const int64_t* dims, cudaStream_t stream, Scratch& s, int* passes_out) {
-  msc::GradDims D;
-  if (!make_dims(nd, dims, &D)) return fail(MSC_ERR_BAD_DIMS, "invalid dims");
-  if (!g) return fail(MSC_ERR_NULL_POINTER, "null buffer");
+// Multi-pass form: tile passes until no pass changes a cell near a tile border.
+// `launches` counts kernel launches.
+int ldir_passes(int nd, uint8_t* g, const msc::GradDims& D, cudaStream_t stream, Scratch& s, int* launches) {
   const int64_t ntiles = msc::ldir_num_tiles(nd, D);
   // one "reopened" byte per tile, double-buffered between passes
   uint8_t* dirty = nullptr;
@@ -144,8 +146,77 @@ int ldir_impl(int nd, uint8_t* g, const int64_t* dims, cudaStream_t stream, Scra
     din = dout;
     dout = (dout == dirty) ? dirty + ntiles : dirty;
   }
-  if (passes_out) *passes_out = passes;
-  g_last_passes = passes;
+  *launches += passes;
+  return MSC_OK;
+}
+
+// Single-pass form: one tile pass that saves every tile's final box, a check of the
+// saved halos against the owners' cells, and global walks from the items the check
+// lowered.  Should a frontier queue overflow, the multi-pass form finishes the
+// closure from wherever it stands (the closure is monotone, so any intermediate
+// state is a valid start).
+int ldir_impl(int nd, uint8_t* g, const int64_t* dims, cudaStream_t stream, Scratch& s, int* passes_out) {
+  msc::GradDims D;
+  if (!make_dims(nd, dims, &D)) return fail(MSC_ERR_BAD_DIMS, "invalid dims");
+  if (!g) return fail(MSC_ERR_NULL_POINTER, "null buffer");
+  const int64_t ntiles = msc::ldir_num_tiles(nd, D);
+  const int64_t box = msc::ldir_box_bytes(nd);
+  const int sms = num_sms();
+  int cap = (int)std::min<int64_t>(std::max<int64_t>(ntiles * 256, 1 << 16), (int64_t)1 << 30);
+  // MSC_LDIR_QUEUE_CAP lowers the frontier capacity (tests of the multi-pass fallback)
+  if (const char* e = std::getenv("MSC_LDIR_QUEUE_CAP")) {
+    const long v = std::strtol(e, nullptr, 10);
+    if (v > 0 && v < cap) cap = (int)v;
+  }
+  uint8_t* saved = nullptr;
+  int64_t* queues = nullptr;
+  int* ctr = nullptr;  // [0] queue a [1] queue b [2] lock [3] frontier overflow / CAS limit
+  MSC_CUDA(cudaMallocAsync((void**)&saved, (size_t)(ntiles * box), stream), "cudaMallocAsync(saved boxes)");
+  struct FreeAll {
+    void* p[3];
+    cudaStream_t st;
+    ~FreeAll() {
+      for (void* q : p)
+        if (q) cudaFreeAsync(q, st);
+    }
+  } fr{{saved, nullptr, nullptr}, stream};
+  MSC_CUDA(cudaMallocAsync((void**)&queues, (size_t)cap * 2 * sizeof(int64_t), stream), "cudaMallocAsync(queues)");
+  fr.p[1] = queues;
+  MSC_CUDA(cudaMallocAsync((void**)&ctr, 4 * sizeof(int), stream), "cudaMallocAsync(counters)");
+  fr.p[2] = ctr;
+  MSC_CUDA(cudaMemsetAsync(ctr, 0, 4 * sizeof(int), stream), "cudaMemsetAsync(counters)");
+
+  int launches = 0;
+  MSC_CUDA(msc::launch_ldir_tile(nd, g, D, saved, s.words, sms, stream), "ldir tile kernel launch");
+  MSC_CUDA(msc::launch_ldir_check(nd, g, D, saved, queues, ctr, cap, ctr + 2, ctr + 3, sms, stream),
+           "ldir check kernel launch");
+  launches += 2;
+  int64_t* qa = queues;
+  int64_t* qb = queues + cap;
+  bool overflow = false;
+  for (int round = 0;; round++) {
+    int h[4];
+    MSC_CUDA(cudaMemcpyAsync(h, ctr, 4 * sizeof(int), cudaMemcpyDeviceToHost, stream), "read counters");
+    MSC_CUDA(cudaStreamSynchronize(stream), "cudaStreamSynchronize");
+    const int n = round % 2 == 0 ? h[0] : h[1];
+    if (h[3] || n > cap) {
+      overflow = true;
+      break;
+    }
+    if (n == 0) break;
+    if (round > 4096) return fail(MSC_ERR_ITER_LIMIT, "ldir frontier walk did not converge");
+    int* n_out = round % 2 == 0 ? ctr + 1 : ctr;
+    MSC_CUDA(cudaMemsetAsync(n_out, 0, sizeof(int), stream), "reset queue");
+    MSC_CUDA(msc::launch_ldir_walk(nd, g, D, qa, n, qb, n_out, cap, ctr + 2, ctr + 3, sms, stream),
+             "ldir walk kernel launch");
+    launches++;
+    std::swap(qa, qb);
+  }
+  if (overflow) {
+    if (int rc = ldir_passes(nd, g, D, stream, s, &launches)) return rc;
+  }
+  if (passes_out) *passes_out = launches;
+  g_last_passes = launches;
   return MSC_OK;
 }
 

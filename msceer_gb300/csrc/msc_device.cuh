@@ -44,6 +44,13 @@ namespace msc {
 cudaError_t launch_lstar(int nd, const float* f, uint8_t* g, const GradDims& D, int* err, int num_sms,
                          cudaStream_t stream);
 int64_t ldir_num_tiles(int nd, const GradDims& D);
+int64_t ldir_box_bytes(int nd);
+cudaError_t launch_ldir_tile(int nd, uint8_t* g, const GradDims& D, uint8_t* saved, int* err, int num_sms,
+                             cudaStream_t stream);
+cudaError_t launch_ldir_check(int nd, uint8_t* g, const GradDims& D, const uint8_t* saved, int64_t* queue, int* n_queue,
+                              int cap, int* lock, int* err, int num_sms, cudaStream_t stream);
+cudaError_t launch_ldir_walk(int nd, uint8_t* g, const GradDims& D, const int64_t* qin, int n_in, int64_t* qout,
+                             int* n_out, int cap, int* lock, int* err, int num_sms, cudaStream_t stream);
 cudaError_t launch_ldir_pass(int nd, uint8_t* g, const GradDims& D, const uint8_t* dirty_in, uint8_t* dirty_out,
                              int* changed, int* err, int num_sms, cudaStream_t stream);
 cudaError_t launch_central_diff(int nd, int layout, const float* f, void* out, const GradDims& D, int num_sms,

@@ -8,38 +8,20 @@
 #include <cstring>
 #include <queue>
 #include <string>
+#include <utility>
 #include <vector>
 
 #include "../../include/msc_gpu.h"
+#include "../../include/msc_triage.h"
 #include "label_common.cuh"
+#include "triage.cuh"
 
-namespace msc {
-struct IntegParams {
-  float ethresh, gthresh;
-  int iteration_limit;
-  double max_step;
-  int step_mult;
-};
-struct SpreadOrder {
-  int nlev;
-  int64_t start[48], stride[48], offset[49];
-};
-cudaError_t launch_integrate_pass1(const float4* G, const VolDims& V, const IntegParams& P, const SpreadOrder& S,
-                                   int32_t* lab, int num_sms, cudaStream_t stream);
-cudaError_t launch_boundary_set(const int32_t* lab, const uint8_t* state, const VolDims& V, int64_t* list, int* n,
-                                uint32_t* queued, int num_sms, cudaStream_t stream);
-cudaError_t launch_fixup(const double* G, const VolDims& V, const IntegParams& P, int32_t* lab, uint8_t* state,
-                         const int64_t* list, int n, int64_t* next, int* n_next, uint32_t* queued, int num_sms,
-                         cudaStream_t stream);
-cudaError_t launch_clean(const int32_t* lab, const float* f, const VolDims& V, int dir, int64_t* parent, int64_t* target,
-                         int32_t* out, int num_sms, cudaStream_t stream);
-cudaError_t launch_central_diff(int nd, int layout, const float* f, void* out, const GradDims& D, int num_sms,
-                                cudaStream_t stream);
-}  // namespace msc
 
 namespace {
 
 thread_local std::string t_err;
+// per direction (asc, dsc): fix-up re-decisions, of which in FP64
+thread_local int64_t t_stats[4];
 
 int fail(int code, const std::string& m) {
   t_err = m;
@@ -184,156 +166,333 @@ int read_int(const int* d, int* h, cudaStream_t st) {
   return MSC_OK;
 }
 
-int labels_impl(const float* f, const uint8_t* grad, const int64_t* dims, const msc_integ_params* p, int32_t* out_asc,
-                int32_t* out_dsc, int32_t* stages, cudaStream_t st) {
+// Shared state of one labeling call.
+struct LabelCtx {
+  cudaStream_t st;
+  Pool pool;
+  int sms = 0, grid = 0;
+  msc::VolDims V{};
+  int64_t N = 0, ntiles = 0;
+  const float* f = nullptr;
+  const uint8_t* grad = nullptr;
+  const msc_integ_params* p = nullptr;
+  float4* g32 = nullptr;
+  double* g64 = nullptr;
+  int32_t* key = nullptr;
+  int64_t *ext_cells = nullptr, *saddles = nullptr, *list_a = nullptr, *list_b = nullptr, *amb = nullptr;
+  uint32_t* queued = nullptr;
+  uint8_t* tiles = nullptr;
+  int* counters = nullptr;  // [0] n_ext [1] n_sad [2] n_arcs [3] changed [4] err [5] n_list [6] n_next [7] n_amb
+  explicit LabelCtx(cudaStream_t s) : st(s), pool(s) {}
+};
+
+// One direction's labels between the phases.
+struct DirLabels {
+  int dir = -1;
+  int32_t* lab = nullptr;
+  uint8_t* state = nullptr;
+  int64_t* seed = nullptr;
+  int n_ext = 0;
+};
+
+int setup_ctx(LabelCtx& c, const float* f, const uint8_t* grad, const int64_t* dims, const msc_integ_params* p) {
   if (!dims || dims[0] < 2 || dims[1] < 2 || dims[2] < 2 || dims[0] > (1 << 20) || dims[1] > (1 << 20) ||
       dims[2] > (1 << 20))
     return fail(MSC_ERR_BAD_DIMS, "labeling needs 2 <= X, Y, Z");
-  if (!f || !grad || !p || (!out_asc && !out_dsc)) return fail(MSC_ERR_NULL_POINTER, "null argument");
-  msc::VolDims V{dims[0], dims[1], dims[2], 2 * dims[0] - 1, 2 * dims[1] - 1, 2 * dims[2] - 1, 0, 0};
-  V.cs1 = V.dX;
-  V.cs2 = V.dX * V.dY;
-  const int64_t N = V.X * V.Y * V.Z;
-  if (N >= ((int64_t)1 << 31)) return fail(MSC_ERR_BAD_DIMS, "labeling supports fewer than 2^31 vertices");
-  const int sms = sm_count();
-  const int grid = sms * 8;
-  Pool pool(st);
-  float4* g32;
-  double* g64;
-  int32_t *lab, *key, *rep, *name;
-  uint8_t *state, *tiles;
-  int64_t *ext_cells, *saddles, *hv, *seed, *list_a, *list_b, *parent, *target;
-  float* fval;
-  msc::Arc* arcs;
-  uint32_t* queued;
-  int* counters;  // [0] n_ext [1] n_sad [2] n_arcs [3] changed [4] err [5] n_list [6] n_next
-  const int64_t ntiles = msc::terminal_num_tiles(V);
-  LCUDA(pool.get(&g32, N), "alloc");
-  LCUDA(pool.get(&g64, 3 * N), "alloc");
-  LCUDA(pool.get(&lab, N), "alloc");
-  LCUDA(pool.get(&key, N), "alloc");
-  LCUDA(pool.get(&state, N), "alloc");
-  LCUDA(pool.get(&ext_cells, N), "alloc");
-  LCUDA(pool.get(&saddles, 3 * N), "alloc");
-  LCUDA(pool.get(&list_a, N), "alloc");
-  LCUDA(pool.get(&list_b, N), "alloc");
-  LCUDA(pool.get(&queued, N / 32 + 1), "alloc");
-  LCUDA(pool.get(&tiles, 2 * ntiles), "alloc");
-  LCUDA(pool.get(&counters, 8), "alloc");
+  if (!f || !grad || !p) return fail(MSC_ERR_NULL_POINTER, "null argument");
+  c.V = msc::VolDims{dims[0], dims[1], dims[2], 2 * dims[0] - 1, 2 * dims[1] - 1, 2 * dims[2] - 1, 0, 0};
+  c.V.cs1 = c.V.dX;
+  c.V.cs2 = c.V.dX * c.V.dY;
+  c.N = c.V.X * c.V.Y * c.V.Z;
+  if (c.N >= ((int64_t)1 << 31)) return fail(MSC_ERR_BAD_DIMS, "labeling supports fewer than 2^31 vertices");
+  c.f = f;
+  c.grad = grad;
+  c.p = p;
+  c.sms = sm_count();
+  c.grid = c.sms * 8;
+  c.ntiles = msc::terminal_num_tiles(c.V);
+  const int64_t N = c.N;
+  LCUDA(c.pool.get(&c.g32, N), "alloc");
+  LCUDA(c.pool.get(&c.g64, 3 * N), "alloc");
+  LCUDA(c.pool.get(&c.key, N), "alloc");
+  LCUDA(c.pool.get(&c.ext_cells, N), "alloc");
+  LCUDA(c.pool.get(&c.saddles, 3 * N), "alloc");
+  LCUDA(c.pool.get(&c.list_a, N), "alloc");
+  LCUDA(c.pool.get(&c.list_b, N), "alloc");
+  LCUDA(c.pool.get(&c.amb, N), "alloc");
+  LCUDA(c.pool.get(&c.queued, N / 32 + 1), "alloc");
+  LCUDA(c.pool.get(&c.tiles, 2 * c.ntiles), "alloc");
+  LCUDA(c.pool.get(&c.counters, 8), "alloc");
+  LCUDA(cudaMemsetAsync(c.counters, 0, 8 * sizeof(int), c.st), "memset");
   msc::GradDims GD{};
   for (int a = 0; a < 3; a++) {
     GD.v[a] = dims[a];
     GD.d[a] = 2 * dims[a] - 1;
   }
-  LCUDA(msc::launch_central_diff(3, 1, f, g32, GD, sms, st), "gradient f32");
-  LCUDA(msc::launch_central_diff(3, 2, f, g64, GD, sms, st), "gradient f64");
+  LCUDA(msc::launch_central_diff(3, 1, f, c.g32, GD, c.sms, c.st), "gradient f32");
+  LCUDA(msc::launch_central_diff(3, 2, f, c.g64, GD, c.sms, c.st), "gradient f64");
+  return MSC_OK;
+}
 
-  for (int pass = 0; pass < 2; pass++) {
-    int32_t* out = pass == 0 ? out_asc : out_dsc;
-    if (!out) continue;
-    const int dir = pass == 0 ? -1 : 1;
-    LCUDA(cudaMemsetAsync(counters, 0, 8 * sizeof(int), st), "memset");
-    fill_i32_kernel<<<grid, 256, 0, st>>>(key, N, -1);
-    LCUDA(msc::launch_find_critical(grad, V, dir, key, ext_cells, counters, saddles, counters + 1, sms, st), "critical");
-    int h[8];
-    LCUDA(cudaMemcpyAsync(h, counters, 2 * sizeof(int), cudaMemcpyDeviceToHost, st), "read");
+// Extremum graph, merge, seeds and certain terminal regions of one direction; leaves
+// d.lab (terminal labels, -1 elsewhere) and d.state.
+int prepare_direction(LabelCtx& c, DirLabels& d, int32_t* stage_terminal) {
+  const int64_t N = c.N;
+  const msc::VolDims& V = c.V;
+  cudaStream_t st = c.st;
+  const int dir = d.dir;
+  int32_t *rep, *name;
+  int64_t* hv;
+  float* fval;
+  msc::Arc* arcs;
+  LCUDA(c.pool.get(&d.lab, N), "alloc");
+  LCUDA(c.pool.get(&d.state, N), "alloc");
+  LCUDA(cudaMemsetAsync(c.counters, 0, 3 * sizeof(int), st), "memset");
+  fill_i32_kernel<<<c.grid, 256, 0, st>>>(c.key, N, -1);
+  LCUDA(msc::launch_find_critical(c.grad, V, dir, c.key, c.ext_cells, c.counters, c.saddles, c.counters + 1, c.sms, st),
+        "critical");
+  int h[2];
+  LCUDA(cudaMemcpyAsync(h, c.counters, 2 * sizeof(int), cudaMemcpyDeviceToHost, st), "read");
+  LCUDA(cudaStreamSynchronize(st), "sync");
+  const int n_ext = h[0], n_sad = h[1];
+  d.n_ext = n_ext;
+  LCUDA(c.pool.get(&hv, n_ext + 1), "alloc");
+  LCUDA(c.pool.get(&fval, n_ext + 1), "alloc");
+  LCUDA(c.pool.get(&d.seed, n_ext + 1), "alloc");
+  LCUDA(c.pool.get(&rep, n_ext + 1), "alloc");
+  LCUDA(c.pool.get(&name, n_ext + 1), "alloc");
+  LCUDA(c.pool.get(&arcs, n_sad + 1), "alloc");
+  LCUDA(msc::launch_extremum_info(c.f, V, dir, c.ext_cells, n_ext, hv, fval, d.seed, c.sms, st), "extremum info");
+  LCUDA(msc::launch_trace_arcs(c.grad, c.f, V, dir, c.saddles, n_sad, c.key, c.p->presimp_threshold, arcs,
+                               c.counters + 2, c.counters + 4, c.sms, st),
+        "trace arcs");
+  int n_arcs = 0;
+  if (int rc = read_int(c.counters + 2, &n_arcs, st)) return rc;
+  if (n_ext > 0) iota_kernel<<<(n_ext + 255) / 256, 256, 0, st>>>(rep, n_ext);
+  if (n_arcs > 0) {
+    // the few arcs that can merge: exact priority-queue simplification on the host
+    std::vector<msc::Arc> ha(n_arcs);
+    std::vector<int64_t> hcells(n_ext), hhv(n_ext);
+    std::vector<float> hf(n_ext);
+    LCUDA(cudaMemcpyAsync(ha.data(), arcs, n_arcs * sizeof(msc::Arc), cudaMemcpyDeviceToHost, st), "read arcs");
+    LCUDA(cudaMemcpyAsync(hcells.data(), c.ext_cells, n_ext * sizeof(int64_t), cudaMemcpyDeviceToHost, st), "read");
+    LCUDA(cudaMemcpyAsync(hhv.data(), hv, n_ext * sizeof(int64_t), cudaMemcpyDeviceToHost, st), "read");
+    LCUDA(cudaMemcpyAsync(hf.data(), fval, n_ext * sizeof(float), cudaMemcpyDeviceToHost, st), "read");
     LCUDA(cudaStreamSynchronize(st), "sync");
-    const int n_ext = h[0], n_sad = h[1];
-    LCUDA(pool.get(&hv, n_ext + 1), "alloc");
-    LCUDA(pool.get(&fval, n_ext + 1), "alloc");
-    LCUDA(pool.get(&seed, n_ext + 1), "alloc");
-    LCUDA(pool.get(&rep, n_ext + 1), "alloc");
-    LCUDA(pool.get(&name, n_ext + 1), "alloc");
-    LCUDA(pool.get(&arcs, n_sad + 1), "alloc");
-    LCUDA(msc::launch_extremum_info(f, V, dir, ext_cells, n_ext, hv, fval, seed, sms, st), "extremum info");
-    LCUDA(msc::launch_trace_arcs(grad, f, V, dir, saddles, n_sad, key, p->presimp_threshold, arcs, counters + 2,
-                                 counters + 4, sms, st),
-          "trace arcs");
-    int n_arcs = 0;
-    if (int rc = read_int(counters + 2, &n_arcs, st)) return rc;
-    if (n_ext > 0) iota_kernel<<<(n_ext + 255) / 256, 256, 0, st>>>(rep, n_ext);
-    if (n_arcs > 0) {
-      // the few arcs that can merge: exact priority-queue simplification on the host
-      std::vector<msc::Arc> ha(n_arcs);
-      std::vector<int64_t> hcells(n_ext), hhv(n_ext);
-      std::vector<float> hf(n_ext);
-      LCUDA(cudaMemcpyAsync(ha.data(), arcs, n_arcs * sizeof(msc::Arc), cudaMemcpyDeviceToHost, st), "read arcs");
-      LCUDA(cudaMemcpyAsync(hcells.data(), ext_cells, n_ext * sizeof(int64_t), cudaMemcpyDeviceToHost, st), "read");
-      LCUDA(cudaMemcpyAsync(hhv.data(), hv, n_ext * sizeof(int64_t), cudaMemcpyDeviceToHost, st), "read");
-      LCUDA(cudaMemcpyAsync(hf.data(), fval, n_ext * sizeof(float), cudaMemcpyDeviceToHost, st), "read");
-      LCUDA(cudaStreamSynchronize(st), "sync");
-      std::vector<int32_t> hrep;
-      host_merge(dir, p->presimp_threshold, ha, hcells, hhv, hf, hrep);
-      LCUDA(cudaMemcpyAsync(rep, hrep.data(), n_ext * sizeof(int32_t), cudaMemcpyHostToDevice, st), "write rep");
-      LCUDA(cudaStreamSynchronize(st), "sync");
-    }
-    fill_i32_kernel<<<grid, 256, 0, st>>>(lab, N, -1);
-    fill_i32_kernel<<<(n_ext + 256) / 256, 256, 0, st>>>(name, n_ext + 1, INT_MAX);
-    LCUDA(cudaMemsetAsync(state, 0, (size_t)N, st), "memset");
-    LCUDA(msc::launch_group_seeds(rep, seed, n_ext, name, lab, state, sms, st), "seeds");
-
-    // certain terminal regions: tile passes to the fixpoint
-    const uint8_t* din = nullptr;
-    uint8_t* dout = tiles;
-    for (int64_t passes = 0;; passes++) {
-      LCUDA(cudaMemsetAsync(counters + 3, 0, sizeof(int), st), "memset");
-      LCUDA(cudaMemsetAsync(dout, 0, (size_t)ntiles, st), "memset");
-      LCUDA(msc::launch_terminal_pass(f, lab, V, dir, din, dout, counters + 3, counters + 4, sms, st), "regions");
-      int changed = 0;
-      if (int rc = read_int(counters + 3, &changed, st)) return rc;
-      if (!changed) break;
-      if (passes > ntiles + 2) return fail(MSC_ERR_ITER_LIMIT, "terminal regions did not converge");
-      din = dout;
-      dout = (dout == tiles) ? tiles + ntiles : tiles;
-    }
-    if (stages) snapshot_kernel<<<grid, 256, 0, st>>>(lab, stages + (2 * pass) * N, N);
-    terminal_state_kernel<<<grid, 256, 0, st>>>(lab, state, N);
-    if (n_ext > 0) zero_seed_grad_kernel<<<(n_ext + 255) / 256, 256, 0, st>>>(seed, n_ext, g32, g64);
-
-    // first pass with path compression, in the reference's spread order
-    msc::IntegParams P{p->error_threshold, p->gradient_threshold, p->iteration_limit, (double)p->max_step, dir};
-    msc::SpreadOrder S{};
-    S.nlev = 0;
-    S.offset[0] = 0;
-    for (int64_t kk = 1; kk <= N * 4 && S.nlev < 48; kk *= 2) {
-      const int64_t start = N / kk, stride = (N * 2) / kk;
-      if (stride == 0 || start >= N) continue;
-      S.start[S.nlev] = start;
-      S.stride[S.nlev] = stride;
-      S.offset[S.nlev + 1] = S.offset[S.nlev] + (N - start + stride - 1) / stride;
-      S.nlev++;
-    }
-    LCUDA(msc::launch_integrate_pass1(g32, V, P, S, lab, sms, st), "integrate");
-
-    // fix-up waves (FP64) until no label changes reopen a neighbour
-    LCUDA(cudaMemsetAsync(queued, 0, (N / 32 + 1) * sizeof(uint32_t), st), "memset");
-    LCUDA(cudaMemsetAsync(counters + 5, 0, 2 * sizeof(int), st), "memset");
-    LCUDA(msc::launch_boundary_set(lab, state, V, list_a, counters + 5, queued, sms, st), "boundary set");
-    int n_list = 0;
-    if (int rc = read_int(counters + 5, &n_list, st)) return rc;
-    int64_t* cur = list_a;
-    int64_t* nxt = list_b;
-    for (int64_t waves = 0; n_list > 0; waves++) {
-      if (waves > N) return fail(MSC_ERR_ITER_LIMIT, "fix-up did not converge");
-      LCUDA(cudaMemsetAsync(counters + 6, 0, sizeof(int), st), "memset");
-      LCUDA(msc::launch_fixup(g64, V, P, lab, state, cur, n_list, nxt, counters + 6, queued, sms, st), "fix-up");
-      if (int rc = read_int(counters + 6, &n_list, st)) return rc;
-      int64_t* t = cur;
-      cur = nxt;
-      nxt = t;
-    }
-    if (stages) snapshot_kernel<<<grid, 256, 0, st>>>(lab, stages + (2 * pass + 1) * N, N);
-
-    // isolated-region cleaner
-    LCUDA(pool.get(&parent, N), "alloc");
-    LCUDA(pool.get(&target, N), "alloc");
-    LCUDA(msc::launch_clean(lab, f, V, dir, parent, target, out, sms, st), "clean");
+    std::vector<int32_t> hrep;
+    host_merge(dir, c.p->presimp_threshold, ha, hcells, hhv, hf, hrep);
+    LCUDA(cudaMemcpyAsync(rep, hrep.data(), n_ext * sizeof(int32_t), cudaMemcpyHostToDevice, st), "write rep");
+    LCUDA(cudaStreamSynchronize(st), "sync");
   }
+  fill_i32_kernel<<<c.grid, 256, 0, st>>>(d.lab, N, -1);
+  fill_i32_kernel<<<(n_ext + 256) / 256, 256, 0, st>>>(name, n_ext + 1, INT_MAX);
+  LCUDA(cudaMemsetAsync(d.state, 0, (size_t)N, st), "memset");
+  LCUDA(msc::launch_group_seeds(rep, d.seed, n_ext, name, d.lab, d.state, c.sms, st), "seeds");
+
+  // certain terminal regions: tile passes to the fixpoint
+  const uint8_t* din = nullptr;
+  uint8_t* dout = c.tiles;
+  for (int64_t passes = 0;; passes++) {
+    LCUDA(cudaMemsetAsync(c.counters + 3, 0, sizeof(int), st), "memset");
+    LCUDA(cudaMemsetAsync(dout, 0, (size_t)c.ntiles, st), "memset");
+    LCUDA(msc::launch_terminal_pass(c.f, d.lab, V, dir, din, dout, c.counters + 3, c.counters + 4, c.sms, st),
+          "regions");
+    int changed = 0;
+    if (int rc = read_int(c.counters + 3, &changed, st)) return rc;
+    if (!changed) break;
+    if (passes > c.ntiles + 2) return fail(MSC_ERR_ITER_LIMIT, "terminal regions did not converge");
+    din = dout;
+    dout = (dout == c.tiles) ? c.tiles + c.ntiles : c.tiles;
+  }
+  if (stage_terminal) snapshot_kernel<<<c.grid, 256, 0, st>>>(d.lab, stage_terminal, N);
+  terminal_state_kernel<<<c.grid, 256, 0, st>>>(d.lab, d.state, N);
+  return MSC_OK;
+}
+
+// Streamline integration of the vertices still unassigned (-1), boundary fix-up and
+// the cleaner; `out` receives the final labels.
+int integrate_direction(LabelCtx& c, DirLabels& d, int32_t* out, int32_t* stage_integrated, int64_t stats[2]) {
+  const int64_t N = c.N;
+  const msc::VolDims& V = c.V;
+  cudaStream_t st = c.st;
+  const msc_integ_params* p = c.p;
+  const int sms = c.sms;
+  if (d.n_ext > 0) zero_seed_grad_kernel<<<(d.n_ext + 255) / 256, 256, 0, st>>>(d.seed, d.n_ext, c.g32, c.g64);
+
+  // first pass with path compression, in the reference's spread order
+  msc::IntegParams P{p->error_threshold, p->gradient_threshold, p->iteration_limit, (double)p->max_step, d.dir};
+  msc::SpreadOrder S{};
+  S.nlev = 0;
+  S.offset[0] = 0;
+  for (int64_t kk = 1; kk <= N * 4 && S.nlev < 48; kk *= 2) {
+    const int64_t start = N / kk, stride = (N * 2) / kk;
+    if (stride == 0 || start >= N) continue;
+    S.start[S.nlev] = start;
+    S.stride[S.nlev] = stride;
+    S.offset[S.nlev + 1] = S.offset[S.nlev] + (N - start + stride - 1) / stride;
+    S.nlev++;
+  }
+  LCUDA(msc::launch_integrate_pass1(c.g32, V, P, S, d.lab, sms, st), "integrate");
+
+  // fix-up waves until no label changes reopen a neighbour: FP32 re-decisions, and
+  // FP64 ones for the streamlines whose FP32 ending was ambiguous
+  LCUDA(cudaMemsetAsync(c.queued, 0, (N / 32 + 1) * sizeof(uint32_t), st), "memset");
+  LCUDA(cudaMemsetAsync(c.counters + 5, 0, 3 * sizeof(int), st), "memset");
+  LCUDA(msc::launch_boundary_set(d.lab, d.state, V, c.list_a, c.counters + 5, c.queued, sms, st), "boundary set");
+  int n_list = 0;
+  if (int rc = read_int(c.counters + 5, &n_list, st)) return rc;
+  int64_t* cur = c.list_a;
+  int64_t* nxt = c.list_b;
+  stats[0] = stats[1] = 0;
+  for (int64_t waves = 0; n_list > 0; waves++) {
+    if (waves > N) return fail(MSC_ERR_ITER_LIMIT, "fix-up did not converge");
+    LCUDA(cudaMemsetAsync(c.counters + 6, 0, 2 * sizeof(int), st), "memset");
+    if (p->precision == 1) {
+      LCUDA(msc::launch_fixup(c.g64, V, P, d.lab, d.state, cur, n_list, nxt, c.counters + 6, c.queued, sms, st),
+            "fix-up");
+    } else {
+      LCUDA(msc::launch_fixup32(c.g32, V, P, d.lab, d.state, cur, n_list, nxt, c.counters + 6, c.queued, c.amb,
+                                c.counters + 7, p->precision == 2 ? 2 : 0, sms, st),
+            "fix-up");
+      int n_amb = 0;
+      if (int rc = read_int(c.counters + 7, &n_amb, st)) return rc;
+      stats[1] += n_amb;
+      LCUDA(msc::launch_fixup(c.g64, V, P, d.lab, d.state, c.amb, n_amb, nxt, c.counters + 6, c.queued, sms, st),
+            "fix-up");
+    }
+    stats[0] += n_list;
+    if (int rc = read_int(c.counters + 6, &n_list, st)) return rc;
+    std::swap(cur, nxt);
+  }
+  if (stage_integrated) snapshot_kernel<<<c.grid, 256, 0, st>>>(d.lab, stage_integrated, N);
+
+  // isolated-region cleaner
+  int64_t *parent, *target;
+  LCUDA(c.pool.get(&parent, N), "alloc");
+  LCUDA(c.pool.get(&target, N), "alloc");
+  LCUDA(msc::launch_clean(d.lab, c.f, V, d.dir, parent, target, out, sms, st), "clean");
+  return MSC_OK;
+}
+
+int finish_errors(LabelCtx& c) {
   int err = 0;
-  if (int rc = read_int(counters + 4, &err, st)) return rc;
+  if (int rc = read_int(c.counters + 4, &err, c.st)) return rc;
   if (err & msc::kErrLocalQueue) return fail(MSC_ERR_QUEUE_OVERFLOW, "tile queue overflow");
   if (err & msc::kErrIterLimit) return fail(MSC_ERR_ITER_LIMIT, "V-path walk exceeded its bound (invalid gradient?)");
   return MSC_OK;
+}
+
+int labels_impl(const float* f, const uint8_t* grad, const int64_t* dims, const msc_integ_params* p, int32_t* out_asc,
+                int32_t* out_dsc, int32_t* stages, cudaStream_t st) {
+  if (!out_asc && !out_dsc) return fail(MSC_ERR_NULL_POINTER, "null argument");
+  LabelCtx c(st);
+  if (int rc = setup_ctx(c, f, grad, dims, p)) return rc;
+  for (int k = 0; k < 4; k++) t_stats[k] = 0;
+  for (int pass = 0; pass < 2; pass++) {
+    int32_t* out = pass == 0 ? out_asc : out_dsc;
+    if (!out) continue;
+    DirLabels d;
+    d.dir = pass == 0 ? -1 : 1;
+    if (int rc = prepare_direction(c, d, stages ? stages + (2 * pass) * c.N : nullptr)) return rc;
+    if (int rc = integrate_direction(c, d, out, stages ? stages + (2 * pass + 1) * c.N : nullptr, t_stats + 2 * pass))
+      return rc;
+  }
+  return finish_errors(c);
+}
+
+// Terminal regions of both directions, the combinatorial labels and the network
+// features (the triage's inputs).
+struct TriageInputs {
+  DirLabels asc, dsc;
+  int32_t* comb = nullptr;  // [2][N]
+  __nv_bfloat16* feat = nullptr;
+};
+
+int triage_inputs(LabelCtx& c, TriageInputs& t) {
+  const int64_t N = c.N;
+  t.asc.dir = -1;
+  t.dsc.dir = 1;
+  if (int rc = prepare_direction(c, t.asc, nullptr)) return rc;
+  if (int rc = prepare_direction(c, t.dsc, nullptr)) return rc;
+  int32_t* succ;
+  double* sums;
+  LCUDA(c.pool.get(&succ, N), "alloc");
+  LCUDA(c.pool.get(&sums, 3), "alloc");
+  if (!t.comb) LCUDA(c.pool.get(&t.comb, 2 * N), "alloc");
+  if (!t.feat) LCUDA(c.pool.get(&t.feat, 16 * N), "alloc");
+  LCUDA(msc::launch_comb_labels(c.f, t.asc.lab, c.V, -1, succ, t.comb, c.counters + 3, c.sms, c.st), "comb labels");
+  LCUDA(msc::launch_comb_labels(c.f, t.dsc.lab, c.V, 1, succ, t.comb + N, c.counters + 3, c.sms, c.st), "comb labels");
+  LCUDA(msc::launch_features(c.f, c.g32, t.comb, t.comb + N, t.asc.state, t.dsc.state, c.V, sums, t.feat, c.sms, c.st),
+        "features");
+  return MSC_OK;
+}
+
+__global__ void comb_out_kernel(const int32_t* comb, int32_t* out, int64_t n) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    out[i] = comb[i] == msc::kLabelNone ? -1 : comb[i];
+}
+
+int triage_features_impl(const float* f, const uint8_t* grad, const int64_t* dims, const msc_integ_params* p,
+                         uint16_t* features, int32_t* comb, cudaStream_t st) {
+  if (!features || !comb) return fail(MSC_ERR_NULL_POINTER, "null argument");
+  LabelCtx c(st);
+  if (int rc = setup_ctx(c, f, grad, dims, p)) return rc;
+  TriageInputs t;
+  t.feat = reinterpret_cast<__nv_bfloat16*>(features);
+  if (int rc = triage_inputs(c, t)) return rc;
+  comb_out_kernel<<<c.grid, 256, 0, st>>>(t.comb, comb, 2 * c.N);
+  return finish_errors(c);
+}
+
+int triage_labels_impl(const float* f, const uint8_t* grad, const int64_t* dims, const msc_integ_params* p,
+                       const msc_triage_params* tp, int32_t* out_asc, int32_t* out_dsc, int64_t* stats,
+                       cudaStream_t st) {
+  if (!out_asc || !out_dsc || !tp || !tp->weights) return fail(MSC_ERR_NULL_POINTER, "null argument");
+  LabelCtx c(st);
+  if (int rc = setup_ctx(c, f, grad, dims, p)) return rc;
+  const int64_t N = c.N;
+  TriageInputs t;
+  if (int rc = triage_inputs(c, t)) return rc;
+  // the network: one forward pass gives both directions' logits
+  uint8_t *blobs, *flags;
+  __nv_bfloat16 *act1, *act2;
+  float* logits;
+  unsigned long long* counts;  // per direction: flagged, audited, audit mismatches
+  LCUDA(c.pool.get(&blobs, msc::kTriageBlobBytes), "alloc");
+  LCUDA(c.pool.get(&act1, 16 * N), "alloc");
+  LCUDA(c.pool.get(&act2, 16 * N), "alloc");
+  LCUDA(c.pool.get(&logits, 2 * N), "alloc");
+  LCUDA(c.pool.get(&flags, 2 * N), "alloc");
+  LCUDA(c.pool.get(&counts, 6), "alloc");
+  LCUDA(cudaMemsetAsync(counts, 0, 6 * sizeof(unsigned long long), st), "memset");
+  const msc::ConvDims D{c.V.X, c.V.Y, c.V.Z, N};
+  LCUDA(msc::triage_forward(t.feat, D, tp->weights, blobs, act1, act2, logits, c.counters + 4, st), "triage forward");
+  DirLabels* dl[2] = {&t.asc, &t.dsc};
+  const float thr[2] = {tp->logit_threshold_asc, tp->logit_threshold_dsc};
+  for (int k = 0; k < 2; k++)
+    LCUDA(msc::launch_triage_apply(logits + k * N, thr[k], t.comb + k * N, dl[k]->lab, dl[k]->state, flags + k * N, N,
+                                   tp->audit_fraction, tp->audit_seed + (uint64_t)k, counts + 3 * k, c.sms, st),
+          "triage apply");
+  int64_t fix[4] = {0, 0, 0, 0};
+  int32_t* outs[2] = {out_asc, out_dsc};
+  for (int k = 0; k < 2; k++) {
+    if (int rc = integrate_direction(c, *dl[k], outs[k], nullptr, fix + 2 * k)) return rc;
+    LCUDA(msc::launch_audit_count(dl[k]->lab, t.comb + k * N, flags + k * N, N, counts + 3 * k + 2, c.sms, st),
+          "audit");
+  }
+  for (int k = 0; k < 4; k++) t_stats[k] = fix[k];
+  if (stats) {
+    unsigned long long h[6];
+    LCUDA(cudaMemcpyAsync(h, counts, sizeof(h), cudaMemcpyDeviceToHost, st), "read counts");
+    LCUDA(cudaStreamSynchronize(st), "sync");
+    for (int k = 0; k < 2; k++) {
+      stats[4 * k + 0] = (int64_t)h[3 * k];
+      stats[4 * k + 1] = (int64_t)h[3 * k + 1];
+      stats[4 * k + 2] = (int64_t)h[3 * k + 2];
+      stats[4 * k + 3] = fix[2 * k];
+    }
+  }
+  return finish_errors(c);
 }
 
 }  // namespace
@@ -341,6 +500,11 @@ int labels_impl(const float* f, const uint8_t* grad, const int64_t* dims, const 
 extern "C" {
 
 const char* msc_labels_last_error_string(void) { return t_err.c_str(); }
+
+void msc_labels_last_stats(int64_t out[4]) {
+  if (out)
+    for (int k = 0; k < 4; k++) out[k] = t_stats[k];
+}
 
 int msc_integrated_labels_3d(const float* f, const uint8_t* grad, const int64_t dims[3], const msc_integ_params* params,
                              int32_t* labels_asc, int32_t* labels_dsc, msc_stream_t stream) {
@@ -351,6 +515,17 @@ int msc_integrated_labels_3d_stages(const float* f, const uint8_t* grad, const i
                                     const msc_integ_params* params, int32_t* labels_asc, int32_t* labels_dsc,
                                     int32_t* stages, msc_stream_t stream) {
   return labels_impl(f, grad, dims, params, labels_asc, labels_dsc, stages, (cudaStream_t)stream);
+}
+
+int msc_triage_features_3d(const float* f, const uint8_t* grad, const int64_t dims[3], const msc_integ_params* params,
+                           uint16_t* features, int32_t* comb, msc_stream_t stream) {
+  return triage_features_impl(f, grad, dims, params, features, comb, (cudaStream_t)stream);
+}
+
+int msc_triage_labels_3d(const float* f, const uint8_t* grad, const int64_t dims[3], const msc_integ_params* params,
+                         const msc_triage_params* triage, int32_t* labels_asc, int32_t* labels_dsc, int64_t stats[8],
+                         msc_stream_t stream) {
+  return triage_labels_impl(f, grad, dims, params, triage, labels_asc, labels_dsc, stats, (cudaStream_t)stream);
 }
 
 }  // extern "C"

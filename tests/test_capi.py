@@ -19,13 +19,14 @@ def lib():
 
 
 def declared_symbols():
-    text = (ROOT / "include" / "msc_gpu.h").read_text()
-    return sorted(set(re.findall(r"^\s*(?:int|int64_t|const char\*)\s+(msc_\w+)\s*\(", text, re.M)))
+    text = "\n".join(p.read_text() for p in sorted((ROOT / "include").glob("*.h")))
+    return sorted(set(re.findall(r"^\s*(?:int|int64_t|void|const char\*)\s+(msc_\w+)\s*\(", text, re.M)))
 
 
 def test_header_declares_entry_points():
     syms = declared_symbols()
     assert "msc_lower_star_grad_3d" in syms and "msc_steepest_lstar_host" in syms
+    assert "msc_triage_labels_3d" in syms and "msc_labels_last_stats" in syms
     assert len(syms) >= 12
 
 

@@ -188,3 +188,25 @@ def test_8192_squared_properties(gpu):
     f = torch.from_numpy(fields.power_law_field((8192, 8192), seed=0)).to(gpu)
     g = lower_star_grad(f)
     _properties(g, (8192, 8192))
+
+
+@pytest.mark.parametrize("shape", [(96, 80, 72), (700, 900)], ids=["3d", "2d"])
+def test_frontier_overflow_falls_back_to_passes(gpu, oracle, monkeypatch, shape):
+    """A frontier queue too small for the cross-tile walks hands the closure to the
+    multi-pass form, which finishes it from the intermediate state."""
+    monkeypatch.setenv("MSC_LDIR_QUEUE_CAP", "8")
+    from msceer_gb300 import _lib
+    f = fields.power_law_field(shape, seed=12)
+    got = dev_grad(f, gpu)
+    assert _lib.load().msc_last_ldir_passes() >= 3  # tile + check + at least one full tile pass
+    assert np.array_equal(got, oracle.grad(f))
+
+
+def test_ascending_manifold_dims_idempotent(gpu, oracle):
+    import torch
+    from msceer_gb300 import ascending_manifold_dims
+    f = fields.power_law_field((64, 72, 80), seed=13)
+    want = oracle.grad(f)
+    g = torch.from_numpy(want.copy()).to(gpu)
+    ascending_manifold_dims(g, f.shape[::-1])
+    assert np.array_equal(g.cpu().numpy(), want)

@@ -17,14 +17,16 @@ TOL_INTEGRATED = 0.02
 TOL_FINAL = 0.02
 
 
-def run_both(f, device, oracle):
+def run_both(f, device, oracle, precision=0):
     import torch
     from msceer_gb300 import integrated_labels, lower_star_grad
     gt = 1e-6 * float(np.abs(f).max())
     t = torch.from_numpy(f).to(device)
     g = lower_star_grad(t)
-    got = integrated_labels(t, g, 1e-4, gt, 4000, 0.25, 0.0, stages=True)
+    got = integrated_labels(t, g, 1e-4, gt, 4000, 0.25, 0.0, stages=True, precision=precision)
+    stats = got.pop("stats")
     got = {k: v.cpu().numpy() for k, v in got.items()}
+    got["stats"] = stats
     want = oracle.labels(f, g.cpu().numpy(), 1e-4, gt, 4000, 0.25, 0.0)
     return got, want
 
@@ -36,14 +38,15 @@ FIELDS = {
 }
 
 
+@pytest.mark.parametrize("precision", [0, 1])
 @pytest.mark.parametrize("name", list(FIELDS))
-def test_labels_vs_oracle(gpu, oracle, name):
+def test_labels_vs_oracle(gpu, oracle, name, precision):
     f = FIELDS[name]()
-    got, want = run_both(f, gpu, oracle)
+    got, want = run_both(f, gpu, oracle, precision)
     report = {}
     for k in ("asc_terminal", "dsc_terminal", "asc_integrated", "dsc_integrated", "asc", "dsc"):
         report[k] = float((got[k] != want[k]).mean())
-    print(name, report)
+    print(name, "precision", precision, report, got["stats"])
     assert report["asc_terminal"] == 0.0 and report["dsc_terminal"] == 0.0, report
     assert report["asc_integrated"] <= TOL_INTEGRATED and report["dsc_integrated"] <= TOL_INTEGRATED, report
     assert report["asc"] <= TOL_FINAL and report["dsc"] <= TOL_FINAL, report
