@@ -1,20 +1,28 @@
 #!/usr/bin/env python
-"""Throughput of the lower-star .grad path on GB300 (one JSON line on rank 0).
+"""Throughput of the .grad + integrated-labels path on GB300 (one JSON line on rank 0).
 
 Workload (default): the 512^3 float32 Gaussian random field with a k^-3 power
-spectrum, seed 0 -- the scale configuration the MSCEER steepest_lstar path is
-quoted on.  One step = the complete .grad of the volume (lower-star pairing +
-ascending-manifold dimensions + boundary flag), bit-identical to the reference.
+spectrum, seed = rank (held out from the triage network's training fields).  One
+step = the complete lower-star .grad of the volume (bit-identical to steepest_lstar)
+plus the ascending and descending integrated labels of ondemandaccurate (error
+threshold 1e-4, gradient threshold 1e-6 max|f|, 4000 iterations, 0.25-voxel steps),
+with the learned triage when its trained weights are present, else the plain full
+integration.
 
-  value   Gvert/s with the volume already resident in HBM (CUDA events on the
-          launching stream, K steps between barriers + synchronisation, max over
-          ranks; every rank runs its own replica -- the path needs no collective)
-  e2e     the same metric through the C ABI host entry (msc_steepest_lstar_host)
-          with pinned host buffers: H2D of f, compute, D2H of the .grad per step
-  roofline  the dominant kernel's algorithmic bytes / its measured duration
-          against the measured HBM copy bandwidth (MEASURED_PEAKS.json)
-  cpu_baseline  the CPU port of the reference algorithm (oracle/) on a bounded
-          z-slab sample of the same volume, all host threads
+  value       Gvert/s of the step with the volume already resident in HBM (CUDA
+              events on the launching stream, K steps between barriers +
+              synchronisation, max over ranks; every rank runs its own replica --
+              the path needs no collective)
+  plain       the same step with the plain full integration, and the label mismatch
+              between the two (the plain path is the judge of the triage)
+  e2e         the same metric through the C ABI host entry msc_ondemand_labels_host:
+              H2D of f, .grad, labels, D2H of both label volumes per step
+  grad        the .grad alone: Gvert/s and its per-kernel breakdown
+  roofline    the dominant .grad kernel's algorithmic bytes / its measured duration
+              against the measured HBM copy bandwidth (MEASURED_PEAKS.json)
+  cpu_baseline  the CPU port of the reference algorithm (oracle/) on bounded samples
+              of the same volume: .grad on a z-slab (all threads), labels on small
+              sub-volumes (one process per core)
 
 `--impl reference` times the reference's CPU algorithm alone (the port: the
 reference's own sources are not on the GPU host) on the same metric.
@@ -41,6 +49,7 @@ sys.path.insert(0, str(ROOT / "tests"))
 METRIC = "Gvert/s: lower-star .grad + integrated labels, learned vs plain @<=0.1% mismatch"
 UNIT = "Gvert/s"
 L2_BYTES = 129 * 1024 * 1024
+INTEG = dict(error_threshold=1e-4, iteration_limit=4000, max_step=0.25, presimp_threshold=0.0)
 
 
 def parse_args():
@@ -51,6 +60,8 @@ def parse_args():
     p.add_argument("--impl", choices=["ours", "reference"], default="ours")
     p.add_argument("--size", type=int, default=512, help="edge of the cubic volume")
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--no-triage", action="store_true", help="time the plain full integration as the step")
+    p.add_argument("--grad-only", action="store_true", help="time the .grad alone as the step")
     return p.parse_args()
 
 
@@ -133,52 +144,94 @@ class ClockSampler:
                 "reasons": reasons, "samples": len(rows)}
 
 
-def cpu_baseline(f: np.ndarray, slab: int, reps: int = 1):
-    """The oracle port of the reference algorithm on a z-slab of the volume."""
+def _label_crop_worker(args):
+    """One oracle labeling of a sub-volume (run in a spawned process)."""
+    crop, = args
     import oracle_lib
     orc = oracle_lib.load()
-    sample = np.ascontiguousarray(f[:slab])
+    g = orc.grad(crop, nthreads=1)
+    gt = 1e-6 * float(np.abs(crop).max())
+    t0 = time.perf_counter()
+    orc.labels(crop, g, INTEG["error_threshold"], gt, INTEG["iteration_limit"], INTEG["max_step"],
+               INTEG["presimp_threshold"])
+    return crop.size, time.perf_counter() - t0
+
+
+def cpu_baseline(f: np.ndarray, grad_only: bool = False):
+    """The oracle port of the reference algorithm on bounded samples of the volume:
+    the .grad of a z-slab with all host threads, and the labels (single-threaded
+    restatement) of one 40^3 sub-volume per host core in parallel processes."""
+    import multiprocessing as mp
+
+    import oracle_lib
+    orc = oracle_lib.load()
+    n = f.shape[0]
+    slab = np.ascontiguousarray(f[: max(2, n // 8)])
     nthreads = os.cpu_count() or 1
-    times = []
-    for _ in range(reps):
-        t0 = time.perf_counter()
-        orc.grad(sample, nthreads=nthreads)
-        times.append(time.perf_counter() - t0)
-    t = statistics.median(times)
-    nv = sample.size
-    return {"value": nv / t / 1e9, "unit": UNIT, "cores": nthreads, "kind": "port",
-            "sample": f"z-slab {sample.shape[2]}x{sample.shape[1]}x{sample.shape[0]} of the volume "
-                      f"({nv} vertices), oracle/msc_oracle.c with {nthreads} OpenMP threads, "
-                      f"median of {reps}: {t:.2f} s"}
+    t0 = time.perf_counter()
+    orc.grad(slab, nthreads=nthreads)
+    t_grad = time.perf_counter() - t0
+    g_grad = slab.size / t_grad / 1e9
+    out = {"unit": UNIT, "cores": nthreads, "kind": "port", "grad_gvps": g_grad}
+    desc = (f".grad of a z-slab {slab.shape[2]}x{slab.shape[1]}x{slab.shape[0]} ({slab.size} vertices) with "
+            f"{nthreads} OpenMP threads: {t_grad:.2f} s")
+    if grad_only:
+        out["value"] = g_grad
+        out["sample"] = desc
+        return out
+    c = 40
+    crops = []
+    for i in range(nthreads):
+        z0, y0, x0 = (i * 37) % (n - c), (i * 53) % (n - c), (i * 71) % (n - c)
+        crops.append((np.ascontiguousarray(f[z0:z0 + c, y0:y0 + c, x0:x0 + c]),))
+    ctx = mp.get_context("spawn")
+    t1 = time.perf_counter()
+    with ctx.Pool(nthreads) as pool:
+        res = pool.map(_label_crop_worker, crops)
+    wall = time.perf_counter() - t1
+    nv = sum(r[0] for r in res)
+    busy = max(r[1] for r in res)
+    g_lab = nv / busy / 1e9
+    out["labels_gvps"] = g_lab
+    out["value"] = 1.0 / (1.0 / g_grad + 1.0 / g_lab)
+    out["sample"] = (desc + f"; labels (FP64 oracle, path compression) of {len(crops)} sub-volumes of {c}^3 in "
+                     f"{len(crops)} spawned processes, slowest {busy:.2f} s (pool wall {wall:.2f} s); "
+                     "value = harmonic combination of the two rates")
+    return out
 
 
 def run_reference(args, ws, rank):
     if rank != 0:
         return
     f = make_volume(args.size)
-    slab = max(2, args.size // 8)
     vals = []
+    r = None
     for i in range(args.warmup + args.steps):
-        r = cpu_baseline(f, slab)
+        r = cpu_baseline(f, grad_only=args.grad_only)
         if i >= args.warmup:
             vals.append(r["value"])
     v = statistics.mean(vals)
-    nv = f[:slab].size
     line = {"metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": nv / (v * 1e9) * 1e3, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "impl": "reference",
-            "config": {"workload": f"steepest_lstar .grad, {args.size}^3 k^-3 GRF seed 0",
-                       "sample": f"z-slab of {slab} planes per step"},
-            "cpu_baseline": {"value": v, "unit": UNIT, "cores": r["cores"], "kind": "port",
-                             "sample": r["sample"]},
+            "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32" if args.grad_only else "f32+f64",
+            "data": "synthetic", "impl": "reference",
+            "config": {"workload": f"{'.grad' if args.grad_only else '.grad + integrated labels'}, "
+                                   f"{args.size}^3 k^-3 GRF seed 0, bounded CPU samples per step",
+                       "sample": r["sample"]},
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": r["cores"], "kind": "port", "sample": r["sample"]},
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
 
+def _events(n):
+    import torch
+    return [torch.cuda.Event(enable_timing=True) for _ in range(n)]
+
+
 def run_ours(args, ws, rank, local):
     import torch
-    from msceer_gb300 import _lib, ascending_manifold_dims, lower_star_grad, lower_star_pairs, num_cells
+    from msceer_gb300 import _lib, ascending_manifold_dims, integrated_labels, lower_star_grad, lower_star_pairs, \
+        num_cells, triage
 
     dev = torch.device("cuda", local)
     torch.cuda.set_device(dev)
@@ -198,6 +251,20 @@ def run_ours(args, ws, rank, local):
     f_dev = f_host.to(dev)
     g_dev = torch.empty(C, dtype=torch.uint8, device=dev)
     stream = torch.cuda.current_stream(dev)
+    gt = 1e-6 * float(np.abs(f_np).max())
+    integ = dict(INTEG, gradient_threshold=gt)
+
+    net = None
+    if not args.grad_only and not args.no_triage and triage.WEIGHTS_FILE.exists():
+        net = triage.TriageNet.load(device=dev)
+
+    def step():
+        lower_star_grad(f_dev, out=g_dev)
+        if args.grad_only:
+            return None
+        if net is not None:
+            return triage.triage_labels(f_dev, g_dev, net, **integ)
+        return integrated_labels(f_dev, g_dev, **integ)
 
     def barrier():
         if pg is not None:
@@ -205,8 +272,7 @@ def run_ours(args, ws, rank, local):
         torch.cuda.synchronize(dev)
 
     for _ in range(args.warmup):
-        lower_star_grad(f_dev, out=g_dev)
-    passes = lib.msc_last_ldir_passes()
+        step()
     barrier()
 
     gpu_id = None
@@ -214,93 +280,152 @@ def run_ours(args, ws, rank, local):
         gpu_id = "GPU-" + str(torch.cuda.get_device_properties(dev).uuid)
     except Exception:
         gpu_id = None
+    launches = 0
     with ClockSampler(gpu_id) as clk:
         barrier()
-        e0 = torch.cuda.Event(enable_timing=True)
-        e1 = torch.cuda.Event(enable_timing=True)
+        e0, e1 = _events(2)
         e0.record(stream)
-        total_passes = 0
         for _ in range(args.steps):
-            lower_star_grad(f_dev, out=g_dev)
-            total_passes += lib.msc_last_ldir_passes()
+            res = step()
+            launches += 1 + lib.msc_last_ldir_passes()
         e1.record(stream)
         barrier()
     ms = e0.elapsed_time(e1) / args.steps
     clocks = clk.summary()
+    # launches of the library's kernels in one step, counted outside the timed region
+    try:
+        from torch.profiler import ProfilerActivity, profile
+        with profile(activities=[ProfilerActivity.CUDA]) as prof:
+            step()
+            torch.cuda.synchronize(dev)
+        per_step = sum(e.count for e in prof.key_averages() if "msc" in e.key or "ldir" in e.key or "lstar" in e.key)
+        if per_step > 0:
+            launches = per_step * args.steps
+    except Exception:
+        pass
     if pg is not None:
         t = torch.tensor([ms], device=dev)
         pg.all_reduce(t, op=pg.ReduceOp.MAX)
         ms = float(t.item())
     value = ws * V / (ms * 1e-3) / 1e9
 
-    # per-stage breakdown on the launching stream
-    reps = max(3, args.steps)
-    s0, s1, s2 = (torch.cuda.Event(enable_timing=True) for _ in range(3))
-    t_pairs = t_ldir = 0.0
-    npass = 0
+    # the .grad alone and its stages, on the launching stream
+    reps = max(3, min(args.steps, 10))
+    s0, s1, s2 = _events(3)
+    t_pairs = t_ldir = t_grad = 0.0
+    nlaunch = 0
     for _ in range(reps):
         s0.record(stream)
         lower_star_pairs(f_dev, out=g_dev)
         s1.record(stream)
-        npass += ascending_manifold_dims(g_dev, dims)
+        nlaunch += ascending_manifold_dims(g_dev, dims)
         s2.record(stream)
         torch.cuda.synchronize(dev)
         t_pairs += s0.elapsed_time(s1)
         t_ldir += s1.elapsed_time(s2)
     t_pairs /= reps
-    t_ldir_pass = t_ldir / npass
     t_ldir /= reps
+    for _ in range(reps):
+        s0.record(stream)
+        lower_star_grad(f_dev, out=g_dev)
+        s1.record(stream)
+        torch.cuda.synchronize(dev)
+        t_grad += s0.elapsed_time(s1)
+    t_grad /= reps
+
+    line_extra = {}
+    if not args.grad_only:
+        # the plain full integration (once) and the mismatch of the timed labels against it
+        torch.cuda.synchronize(dev)
+        p0, p1 = _events(2)
+        p0.record(stream)
+        lower_star_grad(f_dev, out=g_dev)
+        plain = integrated_labels(f_dev, g_dev, **integ)
+        p1.record(stream)
+        torch.cuda.synchronize(dev)
+        ms_plain = p0.elapsed_time(p1)
+        mism = {k: float((res[k] != plain[k]).float().mean().item()) for k in ("asc", "dsc")}
+        line_extra["plain"] = {"value": V / (ms_plain * 1e-3) / 1e9, "unit": UNIT, "ms_per_step": ms_plain,
+                               "redecided": plain["stats"]}
+        line_extra["labels"] = {"mode": "learned triage" if net is not None else "plain full integration",
+                                "mismatch_vs_plain": mism,
+                                "stats": res["stats"],
+                                "speedup_vs_plain": ms_plain / ms}
+        if net is not None:
+            line_extra["labels"]["thresholds"] = [net.threshold_asc, net.threshold_dsc]
 
     # end to end through the C ABI host entry, pinned host buffers
-    g_host = torch.empty(C, dtype=torch.uint8).pin_memory()
-    fptr = ctypes.c_void_p(f_host.data_ptr())
-    gptr = ctypes.c_void_p(g_host.data_ptr())
-    dptr = _lib.dims_arg(dims)
-    _lib.check(lib.msc_steepest_lstar_host(fptr, dptr, gptr), "msc_steepest_lstar_host")
+    e2e_reps = max(1, min(args.steps, 3))
+    if args.grad_only:
+        g_host = torch.empty(C, dtype=torch.uint8).pin_memory()
+        fn = lambda: _lib.check(lib.msc_steepest_lstar_host(ctypes.c_void_p(f_host.data_ptr()), _lib.dims_arg(dims),  # noqa: E731
+                                                            ctypes.c_void_p(g_host.data_ptr())), "msc_steepest_lstar_host")
+        h2d, d2h, api = 4 * V, C, "msc_steepest_lstar_host"
+    else:
+        a_host = torch.empty(V, dtype=torch.int32).pin_memory()
+        d_host = torch.empty(V, dtype=torch.int32).pin_memory()
+        p = _lib.IntegParams(integ["error_threshold"], gt, integ["iteration_limit"], integ["max_step"],
+                             integ["presimp_threshold"], 0)
+        tp = None
+        if net is not None:
+            tp = triage.TriageParams(net.weights.data_ptr(), net.threshold_asc, net.threshold_dsc, 0.01, 12345)
+
+        def fn():
+            rc = lib.msc_ondemand_labels_host(ctypes.c_void_p(f_host.data_ptr()), _lib.dims_arg(dims), ctypes.byref(p),
+                                              ctypes.byref(tp) if tp is not None else None,
+                                              ctypes.c_void_p(a_host.data_ptr()), ctypes.c_void_p(d_host.data_ptr()))
+            _lib.check(rc, "msc_ondemand_labels_host")
+        h2d, d2h, api = 4 * V, 8 * V, "msc_ondemand_labels_host"
+    fn()
     barrier()
     t0 = time.perf_counter()
-    for _ in range(args.steps):
-        _lib.check(lib.msc_steepest_lstar_host(fptr, dptr, gptr), "msc_steepest_lstar_host")
-    t_e2e = (time.perf_counter() - t0) / args.steps
+    for _ in range(e2e_reps):
+        fn()
+    t_e2e = (time.perf_counter() - t0) / e2e_reps
     if pg is not None:
         t = torch.tensor([t_e2e], device=dev)
         pg.all_reduce(t, op=pg.ReduceOp.MAX)
         t_e2e = float(t.item())
     e2e = ws * V / t_e2e / 1e9
-    assert torch.equal(g_host.to(dev), g_dev), "host and device paths disagree"
 
     peak, peak_kind = load_peaks()
     alg_pairs = 4 * V + C            # read f once, write every .grad byte once
-    alg_pass = 2 * C                 # one ascending-manifold pass reads and writes the .grad
+    alg_ldir = 2 * C                 # the ascending-manifold stage reads and writes the .grad
     kernels = {
         "lstar_kernel": {"launches_per_step": 1, "ms_per_launch": t_pairs,
                          "algorithmic_bytes": alg_pairs, "gbs": alg_pairs / (t_pairs * 1e-3) / 1e9},
-        "ldir_pass_kernel": {"launches_per_step": npass / reps, "ms_per_launch": t_ldir_pass,
-                             "algorithmic_bytes": alg_pass, "gbs": alg_pass / (t_ldir_pass * 1e-3) / 1e9},
+        "ldir_stage": {"launches_per_step": nlaunch / reps, "ms_per_stage": t_ldir,
+                       "algorithmic_bytes": alg_ldir, "gbs": alg_ldir / (t_ldir * 1e-3) / 1e9,
+                       "kernels": "ldir_tile_kernel + ldir_check_kernel + ldir_walk_kernel"},
     }
-    dom = max(kernels, key=lambda k: kernels[k]["ms_per_launch"] * kernels[k]["launches_per_step"])
+    dom = "lstar_kernel" if t_pairs >= t_ldir else "ldir_stage"
     kd = kernels[dom]
     traffic = TRAFFIC_PER_LAUNCH.get((dom, n))
     roofline = {"kernel": dom, "bound": "hbm", "achieved": kd["gbs"], "peak": peak, "unit": "GB/s",
-                "frac": kd["gbs"] / peak, "peak_kind": f"{peak_kind} hbm_gbs",
-                "traffic": traffic}
+                "frac": kd["gbs"] / peak, "peak_kind": f"{peak_kind} hbm_gbs", "traffic": traffic,
+                "scope": "dominant kernel of the .grad; the label integration that dominates the full step is "
+                         "FP32/FP64 issue-bound, neither HBM nor tensor bound"}
 
     if rank == 0:
+        mode = ".grad only" if args.grad_only else (
+            ".grad + learned-triage labels" if net is not None else ".grad + plain integrated labels")
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
-                "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-                "config": {"workload": f"steepest_lstar .grad (lower star + ldir + flag), {n}^3 float32 "
-                                       f"k^-3 Gaussian random field, seed = rank",
+                "vs_baseline": None, "dtype": "f32" if args.grad_only else "f32+f64", "data": "synthetic",
+                "config": {"workload": f"{mode}, {n}^3 float32 k^-3 Gaussian random field, seed = rank",
                            "vertices": V, "cells": C, "parallelism": f"replicas x{ws}",
+                           "labels": "error 1e-4, gradient threshold 1e-6 max|f|, 4000 iterations, 0.25 voxel",
                            "l2": "inputs larger than L2 (f 512 MiB, .grad 1 GiB at 512^3); no flush"},
-                "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": 4 * V, "d2h_bytes_per_step": C,
-                        "ms_per_step": t_e2e * 1e3, "api": "msc_steepest_lstar_host"},
+                "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                        "ms_per_step": t_e2e * 1e3, "api": api},
+                "grad": {"value": V / (t_grad * 1e-3) / 1e9, "unit": UNIT, "ms_per_step": t_grad},
                 "roofline": roofline,
                 "kernels": kernels,
-                "gpu_launches": args.steps * 1 + total_passes,
+                "gpu_launches": launches,
                 "clocks": clocks}
+        line.update(line_extra)
         if ws == 1 and not args.no_cpu_baseline:
-            line["cpu_baseline"] = cpu_baseline(f_np, max(2, n // 8))
+            line["cpu_baseline"] = cpu_baseline(f_np, grad_only=args.grad_only)
         print(json.dumps(line), flush=True)
     if pg is not None:
         pg.destroy_process_group()

@@ -76,6 +76,15 @@ int msc_triage_labels_3d(const float* f, const uint8_t* grad, const int64_t dims
                          const msc_triage_params* triage, int32_t* labels_asc, int32_t* labels_dsc, int64_t stats[8],
                          msc_stream_t stream);
 
+/* The whole ondemandaccurate labeling from host memory, for hosts without device
+ * buffers: copies f (X*Y*Z floats) to the device, computes the lower-star .grad and
+ * the ascending and descending labels -- with triage when `triage` is not NULL
+ * (its weights stay a device pointer), plain full integration otherwise -- and copies
+ * the labels back (X*Y*Z int32 each).  Replaces the compute of ondemandaccurate.cxx
+ * between loading the image and writing the labels.  Blocking. */
+int msc_ondemand_labels_host(const float* f, const int64_t dims[3], const msc_integ_params* params,
+                             const msc_triage_params* triage, int32_t* labels_asc, int32_t* labels_dsc);
+
 #ifdef __cplusplus
 }
 #endif

@@ -49,6 +49,7 @@ SIGNATURES = {
     "msc_triage_backward_3d": (ctypes.c_int, [_VP, _VP, _VP, _VP, _VP, _I64P, _VP, ctypes.c_float, _VP, _VP, _VP]),
     "msc_triage_adam_step": (ctypes.c_int, [_VP, _VP, _VP, _VP, ctypes.c_int, ctypes.c_float, _VP]),
     "msc_triage_labels_3d": (ctypes.c_int, [_VP, _VP, _I64P, _VP, _VP, _VP, _VP, _I64P, _VP]),
+    "msc_ondemand_labels_host": (ctypes.c_int, [_VP, _I64P, _VP, _VP, _VP, _VP]),
     "msc_steepest_lstar_host": (ctypes.c_int, [_VP, _I64P, _VP]),
     "msc_lower_star_grad_2d_host": (ctypes.c_int, [_VP, _I64P, _VP]),
 }

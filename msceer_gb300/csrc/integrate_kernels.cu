@@ -79,7 +79,8 @@ struct Adv32 {
     return vid(V, (int64_t)clampf_ext(p.x + 0.5f, V.X), (int64_t)clampf_ext(p.y + 0.5f, V.Y),
                (int64_t)clampf_ext(p.z + 0.5f, V.Z));
   }
-  __device__ int advect(F3& cur, int& iters, bool nearb) const {
+  // gm_end: the gradient magnitude at a low-gradient stop
+  __device__ int advect(F3& cur, int& iters, bool nearb, float& gm_end) const {
     F3 c[8];
     F3 old = cur;
     int64_t b[3];
@@ -95,6 +96,7 @@ struct Adv32 {
     surround(b, nearb, c);
     F3 g = trilin(cur, b, c);
     float gm = sqrtf(g.x * g.x + g.y * g.y + g.z * g.z);
+    gm_end = 0.f;
     if (!(gm > 0.f) || !isfinite(gm)) return EV_LOW_GRADIENT;  // no direction to follow
     const float ms = (float)P.max_step;
     float step = ms / gm;
@@ -107,7 +109,10 @@ struct Adv32 {
         if (gm * step > ms) step = ms / gm;
         old = cur;
       }
-      if (gm < P.gthresh) return EV_LOW_GRADIENT;
+      if (gm < P.gthresh) {
+        gm_end = gm;
+        return EV_LOW_GRADIENT;
+      }
       const float sm = (float)P.step_mult * step;
       const F3 e1 = {g.x * sm, g.y * sm, g.z * sm};
       const float hs = sm * 0.5f;
@@ -167,9 +172,10 @@ __global__ void __launch_bounds__(128) integrate_pass1_kernel(const Adv32 A, con
     int np = 0;
     path[np++] = (int)i;
     int64_t end = i;
+    float gm_end;
     while (true) {
       const bool nb = dist_to_boundary(V, x, y, z) <= 1;
-      const int ev = A.advect(cur, iters, nb);
+      const int ev = A.advect(cur, iters, nb, gm_end);
       end = A.nearest(cur, nb);
       x = end % V.X;
       y = (end / V.X) % V.Y;
@@ -362,7 +368,8 @@ __global__ void __launch_bounds__(128) fixup_kernel(const Adv64 A, int32_t* __re
 
 // One FP32 fix-up wave.  A streamline whose FP32 ending is ambiguous goes to the FP64
 // list instead of being decided here:
-//   it stopped at low gradient (the FP64 stop test decides), or
+//   it stopped at a gradient magnitude within a factor 2 of the threshold (the FP64
+//   stop test decides), or
 //   amb_mode 0: its final point lies within 1/64 voxel of the plane where the
 //     nearest vertex changes, and the vertex across that plane belongs to a
 //     different certain region (FP32 rounding may have picked the wrong side);
@@ -382,16 +389,19 @@ __global__ void __launch_bounds__(128) fixup32_kernel(const Adv32 A, int32_t* __
     int iters = A.P.iteration_limit;
     int64_t end = v;
     int ev;
+    float gm_end = 0.f;
     while (true) {
       const bool nb = dist_to_boundary(V, x, y, z) <= 1;
-      ev = A.advect(cur, iters, nb);
+      ev = A.advect(cur, iters, nb, gm_end);
       end = A.nearest(cur, nb);
       x = end % V.X;
       y = (end / V.X) % V.Y;
       z = end / (V.X * V.Y);
       if (ev != EV_OUT_OF_VOXEL) break;
     }
-    bool ambiguous = ev == EV_LOW_GRADIENT;
+    // a low-gradient stop whose FP32 magnitude is within a factor 2 of the threshold
+    // (a zero or far smaller magnitude is the same stop in FP64)
+    bool ambiguous = ev == EV_LOW_GRADIENT && gm_end >= 0.5f * A.P.gthresh;
     if (!ambiguous && ev == EV_HIT_PREASSIGNED && amb_mode == 0) {
       const float pc[3] = {cur.x, cur.y, cur.z};
       const int64_t ext[3] = {V.X, V.Y, V.Z};

@@ -57,6 +57,26 @@ MSC_HD bool before(float fa, int a, float fb, int b) {
   return b > a;
 }
 
+MSC_HD uint32_t float_bits(float v) {
+#if defined(__CUDA_ARCH__)
+  return __float_as_uint(v);
+#else
+  uint32_t u;
+  __builtin_memcpy(&u, &v, 4);
+  return u;
+#endif
+}
+
+// The same order as one integer: the value's order bits (negative zero taken as
+// zero, as the float comparison does) above the neighbourhood position, so that
+// key(a) < key(b) exactly when before(a, b).  Inputs are NaN-free (checked).
+MSC_HD uint64_t order_key(float v, int p) {
+  if (v == 0.0f) v = 0.0f;
+  uint32_t u = float_bits(v);
+  u = (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+  return ((uint64_t)u << 5) | (uint64_t)p;
+}
+
 template <int ND>
 struct Nb {
   static constexpr int NPOS = (ND == 3) ? 27 : 9;
@@ -116,42 +136,23 @@ struct Nb {
   }
 };
 
-// Reads the neighbourhood value at a position.  Device: a per-thread column in
-// shared memory; host: a plain array.
-struct ColumnVals {
-  const float* base;
+// Per-cell key of the cell's lowest vertex (order_key), indexed by neighbourhood
+// position.  Device: a per-thread column in shared memory; host: a plain array.
+struct KeyCol {
+  uint64_t* base;
   int stride;
-  MSC_HD float operator()(int p) const { return base[p * stride]; }
+  MSC_HD uint64_t operator()(int p) const { return base[p * stride]; }
 };
 
-template <int ND, class Vals>
+template <int ND, class Keys>
 struct LowerStarState {
   using N = Nb<ND>;
-  Vals val;
-  const uint32_t* vm;  // vertex masks per position
+  Keys lk;             // lowest-vertex key per cell
   uint32_t P = 0;      // processed cells
   uint32_t K = 0;      // critical cells
   uint32_t C0 = 0, C1 = 0, C2 = 0;  // pair-direction code bit-planes
 
-  MSC_HD LowerStarState(Vals v, const uint32_t* vmask) : val(v), vm(vmask) {}
-
-  // Cell2LowestVertex: the first vertex of the cell in the (value, index) order
-  MSC_HD int lowv(int q) const {
-    uint32_t m = vm[q];
-    int best = ffs32(m) - 1;
-    float fb = val(best);
-    m &= m - 1;
-    while (m) {
-      const int p = ffs32(m) - 1;
-      m &= m - 1;
-      const float fp = val(p);
-      if (before(fp, p, fb, best)) {
-        best = p;
-        fb = fp;
-      }
-    }
-    return best;
-  }
+  MSC_HD explicit LowerStarState(Keys k) : lk(k) {}
 
   MSC_HD void set_code(int q, int code) {
     C0 |= (uint32_t)(code & 1) << q;
@@ -176,20 +177,15 @@ struct LowerStarState {
   // the cell of U whose lowest vertex comes first (first in star order wins ties)
   MSC_HD int lowest_of(uint32_t U) const {
     int q = ffs32(U) - 1;
+    uint64_t kb = lk(q);
     uint32_t W = U & (U - 1);
-    if (W) {
-      int lv = lowv(q);
-      float fl = val(lv);
-      while (W) {
-        const int o = ffs32(W) - 1;
-        W &= W - 1;
-        const int olv = lowv(o);
-        const float fo = val(olv);
-        if (before(fo, olv, fl, lv)) {
-          q = o;
-          lv = olv;
-          fl = fo;
-        }
+    while (W) {
+      const int o = ffs32(W) - 1;
+      W &= W - 1;
+      const uint64_t ko = lk(o);
+      if (ko < kb) {
+        q = o;
+        kb = ko;
       }
     }
     return q;
@@ -201,24 +197,9 @@ struct LowerStarState {
     constexpr uint32_t EDGES = N::dim_mask(1);
     if (S & (1u << C)) {
       // the vertex pairs with the edge to its lowest neighbour (steepest descent)
-      uint32_t E = S & EDGES;
-      if (!E) {
-        make_critical(C);
-      } else {
-        int best = ffs32(E) - 1;
-        float fb = val(best);
-        E &= E - 1;
-        while (E) {
-          const int e = ffs32(E) - 1;
-          E &= E - 1;
-          const float fe = val(e);
-          if (before(fe, e, fb, best)) {
-            best = e;
-            fb = fe;
-          }
-        }
-        make_pair(C, best);
-      }
+      const uint32_t E = S & EDGES;
+      if (!E) make_critical(C);
+      else make_pair(C, lowest_of(E));  // an edge's lowest vertex is its other end
     }
     constexpr uint32_t DM1 = N::dim_mask(1), DM2 = N::dim_mask(2), DM3 = N::dim_mask(3);
     constexpr uint32_t AX0 = N::axis_mask(0, 0), AX1 = N::axis_mask(1, 0), AX2 = N::axis_mask(2, 0);
@@ -253,20 +234,17 @@ struct LowerStarState {
           // several: the first in cofacet order (+x,-x,+y,-y,+z,-z) whose lowest
           // vertex comes first wins (PickLowestCandidate)
           best = -1;
-          int bestlv = -1;
-          float fb = 0.f;
+          uint64_t kb = ~0ull;
 #pragma unroll
           for (int a = 0; a < ND; a++) {
 #pragma unroll
             for (int sgn = 0; sgn < 2; sgn++) {
               const int c = q + (sgn == 0 ? N::stride(a) : -N::stride(a));
               if (c < 0 || c >= N::NPOS || !((cm >> c) & 1u)) continue;
-              const int lv = lowv(c);
-              const float fl = val(lv);
-              if (best < 0 || before(fl, lv, fb, bestlv)) {
+              const uint64_t kc = lk(c);
+              if (best < 0 || kc < kb) {
                 best = c;
-                bestlv = lv;
-                fb = fl;
+                kb = kc;
               }
             }
           }
@@ -278,18 +256,6 @@ struct LowerStarState {
     }
   }
 };
-
-template <int ND>
-struct VertexMasks {
-  uint32_t vm[27];
-};
-
-template <int ND>
-constexpr VertexMasks<ND> make_vertex_masks() {
-  VertexMasks<ND> t{};
-  for (int p = 0; p < 27; p++) t.vm[p] = p < Nb<ND>::NPOS ? Nb<ND>::vertex_mask(p) : 0u;
-  return t;
-}
 
 // Lower star from the mask of neighbours that come before the centre: the cells all
 // of whose other vertices are lower (three separable AND-folds).  Out-of-range
@@ -355,14 +321,14 @@ MSC_HD uint8_t cell_byte(const State& st, int p, uint32_t Bany, uint32_t enc_map
 // checks, a single boundary class).  Returns true if a NaN was seen.
 template <int ND, class Load, class Store>
 MSC_HD bool process_vertex(int64_t x, int64_t y, int64_t z, int64_t X, int64_t Y, int64_t Z, bool interior,
-                           const Load& load, float* col, int cs, const uint32_t* vm, uint32_t enc_map,
-                           const Store& store) {
+                           const Load& load, uint64_t* col, int cs, uint32_t enc_map, const Store& store) {
   using N = Nb<ND>;
   constexpr int NPOS = N::NPOS;
   constexpr int C = N::CENTER;
   float fc = 0.f;
   load(C, fc);
-  col[C * cs] = fc;
+  uint64_t k[NPOS];  // vertex keys, folded below into the cells' lowest-vertex keys
+  k[C] = order_key(fc, C);
   uint32_t lower = 0;
   bool nan = (fc != fc);
   if (interior) {
@@ -371,9 +337,9 @@ MSC_HD bool process_vertex(int64_t x, int64_t y, int64_t z, int64_t X, int64_t Y
       if (p == C) continue;
       float v = 0.f;
       load(p, v);
-      col[p * cs] = v;
       nan |= (v != v);
-      if (before(v, p, fc, C)) lower |= 1u << p;
+      k[p] = order_key(v, p);
+      if (k[p] < k[C]) lower |= 1u << p;
     }
   } else {
     // out-of-range neighbours are left out of `lower`, so no cell outside the
@@ -386,16 +352,31 @@ MSC_HD bool process_vertex(int64_t x, int64_t y, int64_t z, int64_t X, int64_t Y
     const uint32_t ok = okx & oky & okz;
 #pragma unroll
     for (int p = 0; p < NPOS; p++) {
-      if (p == C || !((ok >> p) & 1u)) continue;
+      if (p == C) continue;
+      k[p] = ~0ull;
+      if (!((ok >> p) & 1u)) continue;
       float v = 0.f;
       load(p, v);
-      col[p * cs] = v;
       nan |= (v != v);
-      if (before(v, p, fc, C)) lower |= 1u << p;
+      k[p] = order_key(v, p);
+      if (k[p] < k[C]) lower |= 1u << p;
     }
   }
+  // lowest vertex of every cell: a cell's vertices form the box between the centre
+  // and the vertex at its own offset, so three separable min-folds give them all
+#pragma unroll
+  for (int a = 0; a < ND; a++) {
+#pragma unroll
+    for (int p = 0; p < NPOS; p++) {
+      if (N::d(p, a) == 0) continue;
+      const int q = p - N::d(p, a) * N::stride(a);
+      if (k[q] < k[p]) k[p] = k[q];
+    }
+  }
+#pragma unroll
+  for (int p = 0; p < NPOS; p++) col[p * cs] = k[p];
   const uint32_t L = lower_star_mask<ND>(lower);
-  LowerStarState<ND, ColumnVals> st(ColumnVals{col, cs}, vm);
+  LowerStarState<ND, KeyCol> st(KeyCol{col, cs});
   uint32_t Bany = 0;
   if (interior)
     st.expand(L);

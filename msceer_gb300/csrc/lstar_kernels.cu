@@ -14,17 +14,15 @@
 //
 // The max/min vertex labeling is never materialised: the per-vertex work
 // (lstar_core.cuh) derives the lower star from the neighbours below the vertex and
-// expands it on bitmasks.  Neighbour values live in a per-thread shared-memory
-// column so the lowest-vertex comparisons can index them.  Each cell is owned by
-// exactly one vertex (its highest), so its final byte is written once with a plain
-// store; for one neighbour position the 32 stores of a warp fall in one 64-byte span.
+// expands it on bitmasks.  The lowest-vertex key of every cell of the neighbourhood
+// lives in a per-thread shared-memory column so the comparisons can index it.  Each
+// cell is owned by exactly one vertex (its highest), so its final byte is written
+// once with a plain store; for one neighbour position the 32 stores of a warp fall in
+// one 64-byte span.
 #include "lstar_core.cuh"
 #include "msc_device.cuh"
 
 namespace msc {
-
-__constant__ VertexMasks<3> c_vm3 = make_vertex_masks<3>();
-__constant__ VertexMasks<2> c_vm2 = make_vertex_masks<2>();
 
 // Block = 32 consecutive x by BS/32 consecutive y at one z; grid (x-blocks,
 // y-blocks, z), looping over z when Z exceeds the grid's z extent.  Neighbour and
@@ -35,11 +33,8 @@ __global__ void __launch_bounds__(BS) lstar_kernel(const float* __restrict__ f, 
   using N = Nb<ND>;
   constexpr int NPOS = N::NPOS;
   constexpr int ROWS = BS / 32;
-  __shared__ float s_val[NPOS * BS];
-  __shared__ uint32_t s_vm[NPOS];
+  __shared__ uint64_t s_key[NPOS * BS];
   const int tid = threadIdx.x;
-  if (tid < NPOS) s_vm[tid] = (ND == 3) ? c_vm3.vm[tid] : c_vm2.vm[tid];
-  __syncthreads();
 
   const int64_t X = D.v[0], Y = D.v[1], Z = D.v[2];
   const int x = blockIdx.x * 32 + (tid & 31);
@@ -47,7 +42,7 @@ __global__ void __launch_bounds__(BS) lstar_kernel(const float* __restrict__ f, 
   if (x >= X || y >= Y) return;
   const int sX = (int)X, sXY = (int)(X * Y);
   const int c1 = (int)D.cs[1], c2 = (int)D.cs[2];
-  float* col = s_val + tid;
+  uint64_t* col = s_key + tid;
   bool nan = false;
   for (int64_t z = blockIdx.z; z < Z; z += gridDim.z) {
     const float* fv = f + (x + X * (y + Y * z));
@@ -55,7 +50,7 @@ __global__ void __launch_bounds__(BS) lstar_kernel(const float* __restrict__ f, 
     auto load = [&](int p, float& v) { v = __ldg(fv + (N::d(p, 0) + N::d(p, 1) * sX + (ND == 3 ? N::d(p, 2) : 0) * sXY)); };
     auto store = [&](int p, uint8_t b) { gc[N::d(p, 0) + N::d(p, 1) * c1 + (ND == 3 ? N::d(p, 2) : 0) * c2] = b; };
     const bool interior = x > 0 && x < X - 1 && y > 0 && y < Y - 1 && (ND == 2 || (z > 0 && z < Z - 1));
-    nan |= process_vertex<ND>(x, y, z, X, Y, Z, interior, load, col, BS, s_vm, D.enc_map, store);
+    nan |= process_vertex<ND>(x, y, z, X, Y, Z, interior, load, col, BS, D.enc_map, store);
   }
   if (nan) atomicOr(err, kErrNaN);
 }

@@ -495,6 +495,61 @@ int triage_labels_impl(const float* f, const uint8_t* grad, const int64_t* dims,
   return finish_errors(c);
 }
 
+// Per-thread device staging of the host-buffer entry, kept between calls.
+struct LabelStaging {
+  int dev = -1;
+  cudaStream_t st = nullptr;
+  size_t nv = 0, nc = 0;
+  float* f = nullptr;
+  uint8_t* g = nullptr;
+  int32_t* lab = nullptr;  // [2][N]
+};
+thread_local LabelStaging t_lstage;
+
+int labels_host_impl(const float* fh, const int64_t* dims, const msc_integ_params* p, const msc_triage_params* tp,
+                     int32_t* asc_h, int32_t* dsc_h) {
+  if (!fh || !dims || !p || !asc_h || !dsc_h) return fail(MSC_ERR_NULL_POINTER, "null argument");
+  if (dims[0] < 2 || dims[1] < 2 || dims[2] < 2) return fail(MSC_ERR_BAD_DIMS, "labeling needs 2 <= X, Y, Z");
+  const size_t nv = (size_t)(dims[0] * dims[1] * dims[2]);
+  const int64_t nc64 = msc_num_cells_3d(dims);
+  if (nc64 < 0) return fail(MSC_ERR_BAD_DIMS, "invalid dims");
+  const size_t nc = (size_t)nc64;
+  int dev = 0;
+  LCUDA(cudaGetDevice(&dev), "cudaGetDevice");
+  LabelStaging& h = t_lstage;
+  if (h.dev != dev) {
+    h = LabelStaging{};
+    h.dev = dev;
+  }
+  if (!h.st) LCUDA(cudaStreamCreateWithFlags(&h.st, cudaStreamNonBlocking), "cudaStreamCreate");
+  if (h.nv < nv) {
+    if (h.f) cudaFree(h.f);
+    if (h.lab) cudaFree(h.lab);
+    h.f = nullptr;
+    h.lab = nullptr;
+    h.nv = 0;
+    LCUDA(cudaMalloc((void**)&h.f, nv * sizeof(float)), "cudaMalloc(f staging)");
+    LCUDA(cudaMalloc((void**)&h.lab, 2 * nv * sizeof(int32_t)), "cudaMalloc(label staging)");
+    h.nv = nv;
+  }
+  if (h.nc < nc) {
+    if (h.g) cudaFree(h.g);
+    h.g = nullptr;
+    h.nc = 0;
+    LCUDA(cudaMalloc((void**)&h.g, nc), "cudaMalloc(grad staging)");
+    h.nc = nc;
+  }
+  LCUDA(cudaMemcpyAsync(h.f, fh, nv * sizeof(float), cudaMemcpyHostToDevice, h.st), "copy f to device");
+  if (int rc = msc_lower_star_grad_3d(h.f, dims, h.g, h.st)) return fail(rc, msc_last_error_string());
+  int rc = tp ? triage_labels_impl(h.f, h.g, dims, p, tp, h.lab, h.lab + nv, nullptr, h.st)
+              : labels_impl(h.f, h.g, dims, p, h.lab, h.lab + nv, nullptr, h.st);
+  if (rc) return rc;
+  LCUDA(cudaMemcpyAsync(asc_h, h.lab, nv * sizeof(int32_t), cudaMemcpyDeviceToHost, h.st), "copy labels to host");
+  LCUDA(cudaMemcpyAsync(dsc_h, h.lab + nv, nv * sizeof(int32_t), cudaMemcpyDeviceToHost, h.st), "copy labels to host");
+  LCUDA(cudaStreamSynchronize(h.st), "cudaStreamSynchronize");
+  return MSC_OK;
+}
+
 }  // namespace
 
 extern "C" {
@@ -526,6 +581,11 @@ int msc_triage_labels_3d(const float* f, const uint8_t* grad, const int64_t dims
                          const msc_triage_params* triage, int32_t* labels_asc, int32_t* labels_dsc, int64_t stats[8],
                          msc_stream_t stream) {
   return triage_labels_impl(f, grad, dims, params, triage, labels_asc, labels_dsc, stats, (cudaStream_t)stream);
+}
+
+int msc_ondemand_labels_host(const float* f, const int64_t dims[3], const msc_integ_params* params,
+                             const msc_triage_params* triage, int32_t* labels_asc, int32_t* labels_dsc) {
+  return labels_host_impl(f, dims, params, triage, labels_asc, labels_dsc);
 }
 
 }  // extern "C"

@@ -1,11 +1,13 @@
 // Learned triage, CUDA-core side: combinatorial steepest-path labels, input features,
 // flags, and the training kernels (loss, weight gradients, Adam, weight packing).
 //
-// Combinatorial label of a vertex: follow the steepest 6-neighbour step (downhill for
-// the ascending manifolds of minima, uphill for the descending ones) -- the 0-1 pair
-// of the lower-star gradient, i.e. rec_td / rec_tu (gi_extrema_region_builder.h:286-352)
-// restricted to vertices -- until a vertex of a certain terminal region, and take its
-// region.  Pointer jumping resolves the chains.
+// Combinatorial label of a vertex: follow the steepest discrete step (downhill for the
+// ascending manifolds of minima, uphill for the descending ones) until a vertex of a
+// certain terminal region, and take its region.  The step is taken over the 26
+// neighbours with the drop normalised by distance -- a discrete stand-in for the
+// streamline, closer to it than the 6-neighbour V-path of the lower-star gradient
+// (rec_td / rec_tu, gi_extrema_region_builder.h:286-352).  Pointer jumping resolves
+// the chains.
 #include "label_common.cuh"
 #include "triage.cuh"
 
@@ -13,24 +15,38 @@ namespace msc {
 
 // ---- combinatorial labels --------------------------------------------------------------------
 
+// Steepest discrete step over the 26 neighbours: the largest value drop per unit
+// distance among the neighbours that come before v in the vertex order (after it,
+// uphill), first in position order on ties.  Every step moves strictly along the
+// order, so the chains are acyclic and end at an extremum or a terminal vertex.
 __global__ void comb_succ_kernel(const float* __restrict__ f, const int32_t* __restrict__ lab, const VolDims V, int dir,
                                  int32_t* __restrict__ succ) {
   const int64_t N = V.X * V.Y * V.Z;
+  const float inv_d[4] = {0.f, 1.f, 0.70710678f, 0.57735027f};
   for (int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v < N; v += (int64_t)gridDim.x * blockDim.x) {
     if (lab[v] >= 0) {
       succ[v] = (int32_t)v;
       continue;
     }
     const int64_t x = v % V.X, y = (v / V.X) % V.Y, z = v / (V.X * V.Y);
-    const int64_t nbr[6] = {x < V.X - 1 ? v + 1 : -1, x > 0 ? v - 1 : -1, y < V.Y - 1 ? v + V.X : -1,
-                            y > 0 ? v - V.X : -1, z < V.Z - 1 ? v + V.X * V.Y : -1, z > 0 ? v - V.X * V.Y : -1};
+    const float fv = f[v];
     int64_t best = v;
-#pragma unroll
-    for (int j = 0; j < 6; j++) {
-      const int64_t u = nbr[j];
-      if (u < 0) continue;
-      // downhill: the lowest neighbour below v; uphill: the highest above
-      if (dir < 0 ? vgreater(f, best, u) : vgreater(f, u, best)) best = u;
+    float best_slope = -1.f;
+    for (int dz = -1; dz <= 1; dz++) {
+      if (z + dz < 0 || z + dz >= V.Z) continue;
+      for (int dy = -1; dy <= 1; dy++) {
+        if (y + dy < 0 || y + dy >= V.Y) continue;
+        for (int dx = -1; dx <= 1; dx++) {
+          if ((dx | dy | dz) == 0 || x + dx < 0 || x + dx >= V.X) continue;
+          const int64_t u = v + dx + V.X * (dy + V.Y * dz);
+          if (dir < 0 ? !vgreater(f, v, u) : !vgreater(f, u, v)) continue;  // not on the way
+          const float slope = (dir < 0 ? fv - f[u] : f[u] - fv) * inv_d[(dx != 0) + (dy != 0) + (dz != 0)];
+          if (slope > best_slope) {
+            best_slope = slope;
+            best = u;
+          }
+        }
+      }
     }
     succ[v] = (int32_t)best;
   }

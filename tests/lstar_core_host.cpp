@@ -8,10 +8,9 @@
 template <int ND>
 static int run(const float* f, int64_t X, int64_t Y, int64_t Z, uint8_t* g, uint32_t enc_map) {
   using N = msc::Nb<ND>;
-  const msc::VertexMasks<ND> vm = msc::make_vertex_masks<ND>();
   const int64_t dX = 2 * X - 1, dY = 2 * Y - 1;
   const int64_t cs1 = dX, cs2 = dX * dY;
-  float col[27];
+  uint64_t col[27];
   int nan = 0;
   for (int64_t z = 0; z < Z; z++)
     for (int64_t y = 0; y < Y; y++)
@@ -25,7 +24,7 @@ static int run(const float* f, int64_t X, int64_t Y, int64_t Z, uint8_t* g, uint
           gc[N::d(p, 0) + N::d(p, 1) * cs1 + (ND == 3 ? N::d(p, 2) : 0) * cs2] = b;
         };
         const bool interior = x > 0 && x < X - 1 && y > 0 && y < Y - 1 && (ND == 2 || (z > 0 && z < Z - 1));
-        nan |= msc::process_vertex<ND>(x, y, z, X, Y, Z, interior, load, col, 1, vm.vm, enc_map, store);
+        nan |= msc::process_vertex<ND>(x, y, z, X, Y, Z, interior, load, col, 1, enc_map, store);
       }
   return nan;
 }
