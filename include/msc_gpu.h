@@ -109,11 +109,11 @@ typedef struct {
   float max_step;            /* largest step, in voxels (reference default 0.5) */
   float presimp_threshold;   /* extrema joined by a saddle of lower persistence merge (0 = none) */
   int precision;             /* boundary re-decisions.  0 (default): FP32, and FP64 for streamlines
-                                that stop at a gradient magnitude within a factor 2 of the
-                                threshold, or within 1/64 voxel of the plane where their nearest
-                                vertex would change to one of another certain region; 2: the
-                                same, but FP64 for every ending in a voxel touching two certain
-                                regions; 1: all in FP64 (slow on GB300) */
+                                that stop at a gradient magnitude within 2^-8 below the threshold,
+                                or within 1/64 voxel of the plane where their nearest vertex would
+                                change to one of another certain region; 2: the same, but FP64 for
+                                every ending in a voxel touching two certain regions; 1: all in
+                                FP64 (slow on GB300); 3: none (first pass only, for diagnostics) */
 } msc_integ_params;
 
 /* Ascending (minima basins) and descending (maxima mountains) 3-manifold labels of

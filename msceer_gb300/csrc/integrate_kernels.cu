@@ -368,8 +368,8 @@ __global__ void __launch_bounds__(128) fixup_kernel(const Adv64 A, int32_t* __re
 
 // One FP32 fix-up wave.  A streamline whose FP32 ending is ambiguous goes to the FP64
 // list instead of being decided here:
-//   it stopped at a gradient magnitude within a factor 2 of the threshold (the FP64
-//   stop test decides), or
+//   it stopped at a gradient magnitude within 2^-8 (relative) below the threshold
+//   (the FP64 stop test decides), or
 //   amb_mode 0: its final point lies within 1/64 voxel of the plane where the
 //     nearest vertex changes, and the vertex across that plane belongs to a
 //     different certain region (FP32 rounding may have picked the wrong side);
@@ -399,9 +399,11 @@ __global__ void __launch_bounds__(128) fixup32_kernel(const Adv32 A, int32_t* __
       z = end / (V.X * V.Y);
       if (ev != EV_OUT_OF_VOXEL) break;
     }
-    // a low-gradient stop whose FP32 magnitude is within a factor 2 of the threshold
-    // (a zero or far smaller magnitude is the same stop in FP64)
-    bool ambiguous = ev == EV_LOW_GRADIENT && gm_end >= 0.5f * A.P.gthresh;
+    // a low-gradient stop whose FP32 magnitude lies within 2^-8 (relative) of the
+    // threshold: FP32 rounding could have taken the other side of the stop test.  A
+    // streamline that decelerates into an extremum crosses the threshold well inside
+    // that test's FP32 accuracy otherwise, and FP64 would stop it at the same step.
+    bool ambiguous = ev == EV_LOW_GRADIENT && gm_end >= A.P.gthresh * (1.f - 1.f / 256.f);
     if (!ambiguous && ev == EV_HIT_PREASSIGNED && amb_mode == 0) {
       const float pc[3] = {cur.x, cur.y, cur.z};
       const int64_t ext[3] = {V.X, V.Y, V.Z};

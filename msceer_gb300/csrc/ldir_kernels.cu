@@ -38,8 +38,10 @@ struct LdirTile {
   static constexpr int NL = LX * LY * LZ;
   static constexpr int ls(int a) { return a == 0 ? 1 : (a == 1 ? LX : LX * LY); }
   static constexpr int NW = (NL + 31) / 32;
-  // dynamic shared memory: queue (u16) | bytes | visited bits | changed bits
+  // dynamic shared memory of the pass kernel: queue (u16) | bytes | visited bits | changed bits
   static constexpr size_t smem_bytes() { return (size_t)NL * 2 + ((NL + 3) / 4) * 4 + (size_t)NW * 8; }
+  // of the tile kernel: queue (u16) | bytes | value-2 marks | visited bits
+  static constexpr size_t tile_smem_bytes() { return (size_t)NL * 2 + ((NL + 3) / 4) * 8 + (size_t)NW * 4; }
 };
 
 // local index -> local coords
@@ -364,6 +366,74 @@ __device__ __forceinline__ bool lower_ldir(const GradView& G, int64_t c, unsigne
   return lowered;
 }
 
+// Both closures in the same walk.  The value-2 closure (items: edges) keeps its marks
+// in a byte plane of its own, m2, and the value-1 closure (items: quads) in the .grad
+// bytes, so the two never race on a byte and run in the same BFS levels; an item's
+// dimension says which closure it walks.  The final byte is the .grad byte with ldir
+// lowered to 2 where m2 is set.
+template <class T, int ND>
+struct LdirWalk2 {
+  uint8_t* sg;
+  uint8_t* m2;
+  uint16_t* sq;
+  uint32_t* vis;
+  int* qtail;
+  int* err;
+  int lmin[3], lmax[3];
+  uint32_t dec_map;
+
+  __device__ __forceinline__ int visit(int i, int l[3], int a, int sgn, bool r2) {
+    constexpr int LE[3] = {T::LX, T::LY, T::LZ};
+    const int la = l[a] + sgn;
+    if (la < lmin[a] || la >= lmax[a]) return -1;
+    const int t = i + sgn * T::ls(a);
+    const uint8_t bt = sg[t];
+    const unsigned code = (bt >> 2) & 7u;
+    if (!(bt & 1u) || code == 7u) return -1;  // unassigned or critical
+    if (r2) m2[t] = 1;
+    else if ((bt >> 5) != 1u) sg[t] = (uint8_t)((bt & 0x1Fu) | (1u << 5));
+    const int pc = map3(dec_map, (int)code);
+    const int pa = pc >> 1, psg = (pc & 1) ? -1 : 1;
+    int lp[3] = {l[0], l[1], l[2]};
+    lp[a] += sgn;
+    lp[pa] += psg;
+    if (lp[pa] < 0 || lp[pa] >= LE[pa]) return -1;  // partner outside the box
+    const int tp = t + psg * T::ls(pa);
+    if (tp == i) return -1;
+    const uint8_t bp = sg[tp];
+    if (r2) {
+      const int pdim = (lp[0] & 1) + (lp[1] & 1) + (ND == 3 ? (lp[2] & 1) : 0);
+      if (pdim != 1) {  // a hex: the value-2 path ends here
+        m2[tp] = 1;
+        return -1;
+      }
+      if ((bp >> 5) == 2u || m2[tp]) return -1;  // a root, or marked already
+    } else {
+      if ((bp >> 5) == 1u) return -1;
+    }
+    const uint32_t bit = 1u << (tp & 31);
+    if (atomicOr(&vis[tp >> 5], bit) & bit) return -1;
+    if (r2) m2[tp] = 1;
+    else sg[tp] = (uint8_t)((bp & 0x1Fu) | (1u << 5));
+    return tp;
+  }
+
+  __device__ __forceinline__ void step(int i) {
+    int l[3];
+    lcoords<T>(i, l[0], l[1], l[2]);
+    const bool r2 = ((l[0] & 1) + (l[1] & 1) + (ND == 3 ? (l[2] & 1) : 0)) == 1;
+#pragma unroll
+    for (int a = 0; a < ND; a++) {
+#pragma unroll
+      for (int s = 0; s < 2; s++) {
+        // cofacets only along even axes, +axis first
+        const int nx = (l[a] & 1) ? -1 : visit(i, l, a, s == 0 ? 1 : -1, r2);
+        warp_push(sq, qtail, T::NL, err, nx >= 0, nx);
+      }
+    }
+  }
+};
+
 template <int ND, int TX, int TY, int TZ, int BS>
 __global__ void __launch_bounds__(BS) ldir_tile_kernel(uint8_t* __restrict__ g, const GradDims D,
                                                        uint8_t* __restrict__ saved, int* __restrict__ err) {
@@ -371,22 +441,24 @@ __global__ void __launch_bounds__(BS) ldir_tile_kernel(uint8_t* __restrict__ g, 
   constexpr int NL = T::NL;
   static_assert(NL < 65536, "local ids are 16-bit");
   extern __shared__ __align__(16) unsigned char s_dyn[];
+  // queue (u16) | .grad bytes | value-2 marks | visited bits
   uint16_t* sq = reinterpret_cast<uint16_t*>(s_dyn);
   uint8_t* sg = s_dyn + (size_t)NL * 2;
-  uint32_t* s_vis = reinterpret_cast<uint32_t*>(s_dyn + (size_t)NL * 2 + ((NL + 3) / 4) * 4);
-  __shared__ int s_qtail, s_qseed;
+  uint8_t* m2 = sg + ((NL + 3) / 4) * 4;
+  uint32_t* s_vis = reinterpret_cast<uint32_t*>(m2 + ((NL + 3) / 4) * 4);
+  __shared__ int s_qtail;
 
-  const int tid = threadIdx.x, lane = tid & 31;
+  const int tid = threadIdx.x;
   const int64_t dX = D.d[0], dY = D.d[1], dZ = D.d[2];
   const int64_t ntx = (dX + TX - 1) / TX, nty = (dY + TY - 1) / TY;
   const int64_t ntz = (ND == 3) ? (dZ + TZ - 1) / TZ : 1;
   const int64_t ntiles = ntx * nty * ntz;
 
-  LdirWalk<T, ND> W;
+  LdirWalk2<T, ND> W;
   W.sg = sg;
+  W.m2 = m2;
   W.sq = sq;
   W.vis = s_vis;
-  W.dirty = nullptr;
   W.qtail = &s_qtail;
   W.err = err;
   W.dec_map = D.dec_map;
@@ -402,15 +474,12 @@ __global__ void __launch_bounds__(BS) ldir_tile_kernel(uint8_t* __restrict__ g, 
       const int64_t hi = dd[a] - o[a];
       W.lmax[a] = (int)(hi < LE[a] ? hi : LE[a]);
     }
-    if (tid == 0) {
-      s_qtail = 0;
-      s_qseed = NL;
-    }
+    if (tid == 0) s_qtail = 0;
     for (int w = tid; w < T::NW; w += BS) s_vis[w] = 0;
     __syncthreads();
 
     // stage the box (cells outside the complex read as 0 = unassigned), many loads in
-    // flight per thread, and queue every marked item as a seed
+    // flight per thread, and queue every marked item -- the roots -- as a seed
     constexpr int PER = (NL + BS - 1) / BS;
     constexpr int U = 8;
 #pragma unroll 1
@@ -435,48 +504,37 @@ __global__ void __launch_bounds__(BS) ldir_tile_kernel(uint8_t* __restrict__ g, 
         int dim = 0;
         if (valid) {
           sg[k] = v[u];
+          m2[k] = 0;
           const int lx = k % T::LX, row = k / T::LX;
           const int ly = row % T::LY, lz = row / T::LY;
           dim = (lx & 1) + (ly & 1) + (ND == 3 ? (lz & 1) : 0);
         }
         const unsigned ld = v[u] >> 5;
-        const bool s0 = valid && (v[u] & 1u) && dim == 1 && ld == 2u;
-        const bool s1 = valid && (v[u] & 1u) && dim == 2 && ld == 1u;
-        warp_push(sq, &s_qtail, NL, err, s0, k);
-        const unsigned m1 = __ballot_sync(0xffffffffu, s1);
-        if (m1) {
-          int base = 0;
-          if (lane == 0) base = atomicSub(&s_qseed, __popc(m1));
-          base = __shfl_sync(0xffffffffu, base, 0);
-          if (s1) sq[base - 1 - __popc(m1 & ((1u << lane) - 1u))] = (uint16_t)k;
-        }
+        const bool seed = valid && (v[u] & 1u) && ((dim == 1 && ld == 2u) || (dim == 2 && ld == 1u));
+        warp_push(sq, &s_qtail, NL, err, seed, k);
       }
     }
     __syncthreads();
 
+    // both closures, level by level
+    int lo = 0, hi = s_qtail;
 #pragma unroll 1
-    for (int phase = 0; phase < 2; phase++) {
-      int lo = phase == 0 ? 0 : s_qseed;
-      int hi = phase == 0 ? s_qtail : NL;
-      if (phase == 1) {
-        __syncthreads();
-        for (int w = tid; w < T::NW; w += BS) s_vis[w] = 0;
-        if (tid == 0) s_qtail = 0;
-        __syncthreads();
+    while (lo < hi) {
+      for (int k0 = lo; k0 < hi; k0 += BS) {
+        const int k = k0 + tid;
+        if (k < hi) W.step(sq[k]);
       }
-#pragma unroll 1
-      while (lo < hi) {
-        for (int k0 = lo; k0 < hi; k0 += BS) {
-          const int k = k0 + tid;
-          if (k < hi) W.step(sq[k], phase);
-        }
-        __syncthreads();
-        const int nlo = (phase == 1 && hi == NL) ? 0 : hi;
-        const int nhi = s_qtail;
-        __syncthreads();
-        lo = nlo;
-        hi = nhi;
-      }
+      __syncthreads();
+      const int nhi = s_qtail;
+      __syncthreads();
+      lo = hi;
+      hi = nhi;
+    }
+
+    // fold the value-2 marks into the bytes
+    for (int k = tid; k < NL; k += BS) {
+      const uint8_t b = sg[k];
+      if (m2[k] && (b >> 5) == 3u) sg[k] = (uint8_t)((b & 0x1Fu) | (2u << 5));
     }
     __syncthreads();
 
@@ -641,13 +699,13 @@ cudaError_t launch_ldir_tile(int nd, uint8_t* g, const GradDims& D, uint8_t* sav
   if (grid <= 0) return cudaSuccess;
   if (nd == 3) {
     auto k = ldir_tile_kernel<3, kTX3, kTY3, kTZ3, kBS3>;
-    const size_t sm = Tile3::smem_bytes();
+    const size_t sm = Tile3::tile_smem_bytes();
     cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
     if (e != cudaSuccess) return e;
     k<<<grid, kBS3, sm, stream>>>(g, D, saved, err);
   } else {
     auto k = ldir_tile_kernel<2, kTX2, kTY2, 1, kBS2>;
-    const size_t sm = Tile2::smem_bytes();
+    const size_t sm = Tile2::tile_smem_bytes();
     cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
     if (e != cudaSuccess) return e;
     k<<<grid, kBS2, sm, stream>>>(g, D, saved, err);

@@ -341,6 +341,7 @@ int integrate_direction(LabelCtx& c, DirLabels& d, int32_t* out, int32_t* stage_
   LCUDA(msc::launch_boundary_set(d.lab, d.state, V, c.list_a, c.counters + 5, c.queued, sms, st), "boundary set");
   int n_list = 0;
   if (int rc = read_int(c.counters + 5, &n_list, st)) return rc;
+  if (p->precision == 3) n_list = 0;  // first pass only
   int64_t* cur = c.list_a;
   int64_t* nxt = c.list_b;
   stats[0] = stats[1] = 0;
