@@ -74,6 +74,14 @@ int msc_lower_star_grad_3d(const float* f, const int64_t dims[3], uint8_t* grad_
  * no saddle streamlines (gi_discrete_gradient_computer.h:561-583, 681-689). */
 int msc_lower_star_grad_2d(const float* f, const int64_t dims[2], uint8_t* grad_out, msc_stream_t stream);
 
+/* Many 3D volumes of different sizes in one call (no counterpart in the reference,
+ * which runs one process per volume): f[i], grad[i] are device buffers of volume i
+ * with dims[3*i..3*i+2]; every .grad equals msc_lower_star_grad_3d's.  Up to 64
+ * volumes share each kernel launch (a flat grid over all their blocks / tiles, the
+ * volume table passed in the launch parameters).  Synchronises `stream` at the end. */
+int msc_lower_star_grad_batch_3d(int n, const float* const* f, const int64_t* dims, uint8_t* const* grad,
+                                 msc_stream_t stream);
+
 /* Stage 1 alone: lower-star pairing of every vertex
  * (gi_fast_robins_noalloc.h:1254-1535 / gi_modified_robins.h:1281-1402) written as
  * final bytes except ldir, which holds only the closure roots (critical 1-cells 2,

@@ -1,21 +1,26 @@
 /* Learned triage for the integrated labels of libmsc_gpu.so.
  *
- * No counterpart in the reference: MSCEER integrates every vertex.  A small 3D
- * convolutional network (three 3x3x3 layers, 6 -> 16 -> 16 -> 2 channels, BF16
- * weights and activations with FP32 accumulation on the tensor cores) predicts, per
- * vertex and direction, whether the integrated destination differs from the
- * combinatorial steepest-path destination.  Only flagged vertices plus a random audit
- * sample are integrated; the others take the combinatorial label.  The plain path
- * (msc_integrated_labels_3d) stays the drop-in and the judge of the triage's mismatch.
+ * No counterpart in the reference: MSCEER re-decides every vertex next to a label
+ * boundary.  The labeling has a cheap first pass (FP32 streamlines with path
+ * compression) and an expensive boundary fix-up (every vertex with a differently
+ * labelled 6-neighbour re-integrated until it reaches a certain region, in waves),
+ * which takes about nine tenths of the time and changes about one first-pass label in
+ * ten.  A small 3D convolutional network (three 3x3x3 layers, 6 -> 16 -> 16 -> 2
+ * channels, BF16 weights and activations with FP32 accumulation on the tensor cores)
+ * predicts, per vertex, whether the fix-up would change its first-pass label; only
+ * flagged vertices plus a random audit sample are re-decided, the rest keep the
+ * first-pass label.  The plain path (msc_integrated_labels_3d) stays the drop-in and
+ * the judge of the triage's mismatch.  One network serves both directions: the
+ * features of the descending direction see -f.
  *
  * Tensors:
  *   features / activations   BF16, "row-planar" [Z][Y][2][X][8] (16 channels per
  *                            vertex, channels 0-7 then 8-15 of each row), X*Y*Z*32 bytes
- *   logits                   FP32 [2][X*Y*Z]: ascending then descending
- *   targets                  uint8 [2][X*Y*Z]: 1 where the label differs
+ *   logits                   FP32 [2][X*Y*Z]; channel 0 decides, channel 1 is trained alike
+ *   targets                  uint8 [2][X*Y*Z]: 1 where the fix-up changes the label (both rows)
  *   weights                  FP32 [MSC_TRIAGE_PARAMS]: W1, W2, W3 as [27 taps][16 cin][16 cout]
  *                            (tap = dx + 3 dy + 9 dz, offsets -1..1), then b1, b2, b3 [16];
- *                            channels beyond 6 inputs / 2 outputs must be zero
+ *                            channels beyond 10 inputs / 2 outputs must be zero
  * All pointers are device memory; every call runs on `stream`, synchronises it, and
  * returns MSC_OK or a negative MSC_ERR_* code (text: msc_triage_last_error_string()
  * for the network entries, msc_labels_last_error_string() for the labeling ones). */
@@ -30,7 +35,7 @@
 extern "C" {
 #endif
 
-#define MSC_TRIAGE_IN_CHANNELS 6
+#define MSC_TRIAGE_IN_CHANNELS 10
 #define MSC_TRIAGE_OUT_CHANNELS 2
 #define MSC_TRIAGE_PARAMS (3 * 27 * 16 * 16 + 3 * 16)
 
@@ -42,11 +47,12 @@ typedef struct {
   uint64_t audit_seed;
 } msc_triage_params;
 
-/* Network inputs of a volume: runs the labeling chain up to the certain terminal
- * regions of both directions, the combinatorial labels (comb: int32 [2][X*Y*Z],
- * -1 = none) and the features. */
+/* Training data of a volume: for the ascending then the descending direction, the
+ * network features after the first pass (features: 2 row-planar tensors, 2*X*Y*Z*32
+ * bytes) and, when `targets` is not NULL, the targets of the full fix-up (uint8
+ * [2 directions][2][X*Y*Z]). */
 int msc_triage_features_3d(const float* f, const uint8_t* grad, const int64_t dims[3], const msc_integ_params* params,
-                           uint16_t* features, int32_t* comb, msc_stream_t stream);
+                           uint16_t* features, uint8_t* targets, msc_stream_t stream);
 
 /* Error text of the last failed network call on the calling thread. */
 const char* msc_triage_last_error_string(void);
@@ -68,10 +74,11 @@ int msc_triage_backward_3d(const uint16_t* features, const uint16_t* act1, const
 int msc_triage_adam_step(float* weights, const float* grads, float* m, float* v, int step, float lr,
                          msc_stream_t stream);
 
-/* Integrated labels with triage: as msc_integrated_labels_3d, integrating only
- * flagged and audited vertices.  stats (host, optional) receives per direction
- * (ascending, then descending): flagged, audited, audited whose integrated label
- * differs from the combinatorial one, boundary re-decisions. */
+/* Integrated labels with triage: as msc_integrated_labels_3d, with the boundary
+ * fix-up restricted to flagged and audited vertices.  stats (host, optional)
+ * receives per direction (ascending, then descending): flagged, audited, audited
+ * whose label the fix-up changed (the misses the network would have made there),
+ * boundary re-decisions. */
 int msc_triage_labels_3d(const float* f, const uint8_t* grad, const int64_t dims[3], const msc_integ_params* params,
                          const msc_triage_params* triage, int32_t* labels_asc, int32_t* labels_dsc, int64_t stats[8],
                          msc_stream_t stream);

@@ -12,6 +12,7 @@ from .api import (  # noqa: F401
     ascending_manifold_dims,
     integrated_labels,
     lower_star_grad,
+    lower_star_grad_batch,
     lower_star_pairs,
     num_cells,
     steepest_lstar,

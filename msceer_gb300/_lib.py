@@ -41,10 +41,11 @@ SIGNATURES = {
     "msc_central_diff_grad_2d_f64": (ctypes.c_int, [_VP, _I64P, _VP, _VP]),
     "msc_integrated_labels_3d": (ctypes.c_int, [_VP, _VP, _I64P, _VP, _VP, _VP, _VP]),
     "msc_integrated_labels_3d_stages": (ctypes.c_int, [_VP, _VP, _I64P, _VP, _VP, _VP, _VP, _VP]),
+    "msc_lower_star_grad_batch_3d": (ctypes.c_int, [ctypes.c_int, _VP, _I64P, _VP, _VP]),
     "msc_labels_last_error_string": (ctypes.c_char_p, []),
     "msc_labels_last_stats": (None, [_I64P]),
     "msc_triage_last_error_string": (ctypes.c_char_p, []),
-    "msc_triage_features_3d": (ctypes.c_int, [_VP, _VP, _I64P, _VP, _VP, _VP, _VP]),
+    "msc_triage_features_3d": (ctypes.c_int, [_VP, _VP, _I64P, _VP, _VP, _VP, _VP]),  # f grad dims p feat tgt st
     "msc_triage_forward_3d": (ctypes.c_int, [_VP, _I64P, _VP, _VP, _VP, _VP, _VP]),
     "msc_triage_backward_3d": (ctypes.c_int, [_VP, _VP, _VP, _VP, _VP, _I64P, _VP, ctypes.c_float, _VP, _VP, _VP]),
     "msc_triage_adam_step": (ctypes.c_int, [_VP, _VP, _VP, _VP, ctypes.c_int, ctypes.c_float, _VP]),

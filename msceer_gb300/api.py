@@ -84,6 +84,33 @@ def lower_star_grad(f, out=None):
     return out
 
 
+def lower_star_grad_batch(volumes, outs=None, threads: int = 0):
+    """The .grad of many 3D CUDA float32 volumes of different sizes in shared launches
+    (msc_lower_star_grad_batch_3d).  Returns the list of uint8 tensors."""
+    import torch
+
+    vols = [v.contiguous() for v in volumes]
+    if not vols:
+        return []
+    dev = vols[0].device
+    dims = [_shape_dims(v.shape) for v in vols]
+    if any(len(d) != 3 for d in dims):
+        raise ValueError("batched volumes must be 3D")
+    if outs is None:
+        outs = [torch.empty(num_cells(d), dtype=torch.uint8, device=dev) for d in dims]
+    n = len(vols)
+    fp = (ctypes.c_void_p * n)(*[v.data_ptr() for v in vols])
+    gp = (ctypes.c_void_p * n)(*[o.data_ptr() for o in outs])
+    dd = (ctypes.c_int64 * (3 * n))(*[x for d in dims for x in d])
+    lib = _lib.load()
+    stream = torch.cuda.current_stream(dev).cuda_stream
+    with torch.cuda.device(dev):
+        rc = lib.msc_lower_star_grad_batch_3d(n, ctypes.cast(fp, ctypes.c_void_p), dd,
+                                              ctypes.cast(gp, ctypes.c_void_p), ctypes.c_void_p(stream))
+    _lib.check(rc, "msc_lower_star_grad_batch_3d")
+    return outs
+
+
 def steepest_lstar(f, out=None):
     """steepest_lstar's .grad for a 3D volume (numpy host array or CUDA tensor)."""
     if len(f.shape) != 3:

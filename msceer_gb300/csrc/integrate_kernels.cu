@@ -46,7 +46,9 @@ struct Adv32 {
   const float4* G;
   VolDims V;
   IntegParams P;
-  const int32_t* lab;     // pass-1 stop: nearest vertex labelled (assigned or terminal)
+  const int32_t* lab;     // pass-1 stop: nearest vertex labelled (assigned or terminal) ...
+  const uint8_t* lvl;    // ... in an earlier level of the spread order (level array, when set)
+  int level;
   const uint8_t* state;  // fix-up stop (when set): nearest vertex certain terminal
 
   __device__ __forceinline__ F3 corner(int64_t x, int64_t y, int64_t z) const {
@@ -133,6 +135,8 @@ struct Adv32 {
         if (state) {
           const uint8_t st = state[nv];
           if (st == kStSeed || st == kStTerminal) return EV_HIT_PREASSIGNED;
+        } else if (lvl) {
+          if (lvl[nv] < level) return EV_HIT_PREASSIGNED;
         } else if (lab[nv] != -1) {
           return EV_HIT_PREASSIGNED;
         }
@@ -156,16 +160,20 @@ __device__ __forceinline__ int dist_to_boundary(const VolDims& V, int64_t x, int
 
 constexpr int kPathCap = 48;
 
-__global__ void __launch_bounds__(128) integrate_pass1_kernel(const Adv32 A, const SpreadOrder S,
-                                                              int32_t* __restrict__ lab, int* __restrict__ n_steps) {
+// One level of the spread order.  Streamlines of a level see only the labels of
+// earlier levels (lvl[v] < level; terminals are level 0, unlabelled vertices 255),
+// so a level's outcome does not depend on thread timing; where several streamlines
+// of the level pass the same unlabelled vertex, the smallest label wins (unsigned
+// atomicMin: a region's id < "reached no region" < unlabelled).  Level by level the
+// pass is therefore deterministic.
+__global__ void __launch_bounds__(128) integrate_level_kernel(const Adv32 A, int64_t start, int64_t stride, int64_t count,
+                                                              int32_t* __restrict__ lab, uint8_t* __restrict__ lvl) {
   const VolDims& V = A.V;
-  const int64_t total = S.offset[S.nlev];
+  const int level = A.level;
   int path[kPathCap];
-  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
-    int L = 0;
-    while (L + 1 < S.nlev && S.offset[L + 1] <= t) L++;
-    const int64_t i = S.start[L] + (t - S.offset[L]) * S.stride[L];
-    if (lab[i] != -1) continue;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < count; t += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i = start + t * stride;
+    if (lvl[i] < level) continue;  // labelled already
     int64_t x = i % V.X, y = (i / V.X) % V.Y, z = i / (V.X * V.Y);
     F3 cur = {(float)x, (float)y, (float)z};
     int iters = A.P.iteration_limit;
@@ -183,11 +191,20 @@ __global__ void __launch_bounds__(128) integrate_pass1_kernel(const Adv32 A, con
       if (np < kPathCap) path[np++] = (int)end;
       if (ev != EV_OUT_OF_VOXEL) break;
     }
-    int32_t dest = lab[end];
+    int32_t dest = lvl[end] < level ? lab[end] : -1;
     if (dest == -1) dest = kLabelNone;  // reached no region: assigned to nothing
-    for (int k = 0; k < np; k++) atomicCAS(&lab[path[k]], -1, dest);
+    for (int k = 0; k < np; k++) {
+      const int p = path[k];
+      if (lvl[p] < level) continue;  // labelled in an earlier level: keep
+      atomicMin(reinterpret_cast<unsigned int*>(&lab[p]), (unsigned int)dest);
+      lvl[p] = (uint8_t)level;
+    }
   }
-  (void)n_steps;
+}
+
+__global__ void init_levels_kernel(const int32_t* __restrict__ lab, uint8_t* __restrict__ lvl, int64_t N) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < N; i += (int64_t)gridDim.x * blockDim.x)
+    lvl[i] = lab[i] == -1 ? 255 : 0;
 }
 
 // ---- FP64 advector (fix-up), the reference's arithmetic --------------------------------
@@ -323,8 +340,13 @@ __global__ void boundary_set_kernel(const int32_t* __restrict__ lab, const uint8
   }
 }
 
-// One fix-up wave (:330-415): re-integrate, stopping only at certain terminals.
-__global__ void __launch_bounds__(128) fixup_kernel(const Adv64 A, int32_t* __restrict__ lab, uint8_t* __restrict__ state,
+// One fix-up wave (:330-415): re-integrate, stopping only at certain terminals.  The
+// decided label is read from lab0, the labels as the first pass left them: at a
+// certain terminal that is the region's label (never changed), and at any other
+// ending (low gradient, iteration limit) it is a value no concurrent re-decision can
+// be rewriting, so every wave's outcome is independent of thread timing.
+__global__ void __launch_bounds__(128) fixup_kernel(const Adv64 A, int32_t* __restrict__ lab,
+                                                    const int32_t* __restrict__ lab0, uint8_t* __restrict__ state,
                                                     const int64_t* __restrict__ list, int n, int64_t* __restrict__ next,
                                                     int* __restrict__ n_next, uint32_t* __restrict__ queued) {
   const VolDims& V = A.V;
@@ -345,7 +367,7 @@ __global__ void __launch_bounds__(128) fixup_kernel(const Adv64 A, int32_t* __re
       z = end / (V.X * V.Y);
       if (ev != EV_OUT_OF_VOXEL) break;
     }
-    int32_t nl = lab[end];
+    int32_t nl = lab0[end];
     if (nl == -1) nl = kLabelNone;
     lab[v] = nl;
     state[v] = kStNonterminal;
@@ -376,8 +398,9 @@ __global__ void __launch_bounds__(128) fixup_kernel(const Adv64 A, int32_t* __re
 //   amb_mode 2: its final voxel touches two different certain regions (any ending
 //     within half a voxel of a basin boundary).
 __global__ void __launch_bounds__(128) fixup32_kernel(const Adv32 A, int32_t* __restrict__ lab,
-                                                      uint8_t* __restrict__ state, const int64_t* __restrict__ list,
-                                                      int n, int64_t* __restrict__ next, int* __restrict__ n_next,
+                                                      const int32_t* __restrict__ lab0, uint8_t* __restrict__ state,
+                                                      const int64_t* __restrict__ list, int n,
+                                                      int64_t* __restrict__ next, int* __restrict__ n_next,
                                                       uint32_t* __restrict__ queued, int64_t* __restrict__ amb,
                                                       int* __restrict__ n_amb, int amb_mode) {
   const VolDims& V = A.V;
@@ -408,7 +431,7 @@ __global__ void __launch_bounds__(128) fixup32_kernel(const Adv32 A, int32_t* __
       const float pc[3] = {cur.x, cur.y, cur.z};
       const int64_t ext[3] = {V.X, V.Y, V.Z};
       const int64_t ev3[3] = {x, y, z};
-      const int32_t le = lab[end];
+      const int32_t le = lab0[end];
 #pragma unroll
       for (int a = 0; a < 3; a++) {
         const float q = pc[a] + 0.5f;
@@ -420,7 +443,7 @@ __global__ void __launch_bounds__(128) fixup32_kernel(const Adv32 A, int32_t* __
         ac[a] = alt_c;
         const int64_t u = vid(V, ac[0], ac[1], ac[2]);
         const uint8_t st = state[u];
-        if ((st == kStSeed || st == kStTerminal) && lab[u] != le) ambiguous = true;
+        if ((st == kStSeed || st == kStTerminal) && lab0[u] != le) ambiguous = true;
       }
     } else if (!ambiguous && ev == EV_HIT_PREASSIGNED) {
       const int64_t b[3] = {(int64_t)fminf(fmaxf(cur.x, 0.f), (float)(V.X - 2)),
@@ -432,7 +455,7 @@ __global__ void __launch_bounds__(128) fixup32_kernel(const Adv32 A, int32_t* __
         const int64_t u = vid(V, b[0] + (c & 1), b[1] + ((c >> 1) & 1), b[2] + (c >> 2));
         const uint8_t st = state[u];
         if (st != kStSeed && st != kStTerminal) continue;
-        const int32_t l = lab[u];
+        const int32_t l = lab0[u];
         if (seen == kLabelNone) seen = l;
         else if (l != seen) ambiguous = true;
       }
@@ -442,7 +465,7 @@ __global__ void __launch_bounds__(128) fixup32_kernel(const Adv32 A, int32_t* __
       continue;
     }
     atomicAnd(&queued[v >> 5], ~(1u << (v & 31)));
-    int32_t nl = lab[end];
+    int32_t nl = lab0[end];
     if (nl == -1) nl = kLabelNone;
     lab[v] = nl;
     state[v] = kStNonterminal;
@@ -508,9 +531,14 @@ __global__ void uf_hook_kernel(const int32_t* __restrict__ lab, const float* __r
   }
 }
 
-__global__ void uf_flatten_kernel(int64_t* __restrict__ parent, int64_t N) {
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < N; i += (int64_t)gridDim.x * blockDim.x)
-    parent[i] = uf_find(parent, i);
+// Root of every vertex by a read-only walk up the finished forest (path halving here
+// would race with the other threads' walks and could leave a non-root behind).
+__global__ void uf_roots_kernel(const int64_t* __restrict__ parent, int64_t* __restrict__ root, int64_t N) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < N; i += (int64_t)gridDim.x * blockDim.x) {
+    int64_t r = i;
+    for (int64_t guard = 0; guard < N && parent[r] != r; guard++) r = parent[r];  // strictly earlier each hop
+    root[i] = r;
+  }
 }
 
 // MergeBoundaryExtrema: a component root joins the component of its first earlier
@@ -519,7 +547,10 @@ __global__ void clean_target_kernel(const int32_t* __restrict__ lab, const float
                                     const int64_t* __restrict__ parent, int64_t* __restrict__ target) {
   const int64_t N = V.X * V.Y * V.Z;
   for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < N; r += (int64_t)gridDim.x * blockDim.x) {
-    if (parent[r] != r) continue;
+    if (parent[r] != r) {
+      target[r] = r;  // only roots are followed; keep the rest defined
+      continue;
+    }
     const int64_t x = r % V.X, y = (r / V.X) % V.Y, z = r / (V.X * V.Y);
     const int64_t nbr[6] = {x < V.X - 1 ? r + 1 : -1, x > 0 ? r - 1 : -1, y < V.Y - 1 ? r + V.X : -1,
                             y > 0 ? r - V.X : -1, z < V.Z - 1 ? r + V.X * V.Y : -1, z > 0 ? r - V.X * V.Y : -1};
@@ -551,9 +582,17 @@ __global__ void clean_resolve_kernel(const int32_t* __restrict__ lab, const VolD
 // ---- launchers ---------------------------------------------------------------------------
 
 cudaError_t launch_integrate_pass1(const float4* G, const VolDims& V, const IntegParams& P, const SpreadOrder& S,
-                                   int32_t* lab, int num_sms, cudaStream_t stream) {
-  Adv32 A{G, V, P, lab, nullptr};
-  integrate_pass1_kernel<<<num_sms * 16, 128, 0, stream>>>(A, S, lab, nullptr);
+                                   int32_t* lab, uint8_t* lvl, int num_sms, cudaStream_t stream) {
+  const int64_t N = V.X * V.Y * V.Z;
+  init_levels_kernel<<<num_sms * 8, 256, 0, stream>>>(lab, lvl, N);
+  for (int L = 0; L < S.nlev; L++) {
+    const int64_t count = S.offset[L + 1] - S.offset[L];
+    if (count <= 0) continue;
+    Adv32 A{G, V, P, lab, lvl, L + 1, nullptr};
+    const int64_t blocks = (count + 127) / 128;
+    const int grid = (int)(blocks < num_sms * 16 ? blocks : num_sms * 16);
+    integrate_level_kernel<<<grid, 128, 0, stream>>>(A, S.start[L], S.stride[L], count, lab, lvl);
+  }
   return cudaGetLastError();
 }
 
@@ -563,24 +602,24 @@ cudaError_t launch_boundary_set(const int32_t* lab, const uint8_t* state, const 
   return cudaGetLastError();
 }
 
-cudaError_t launch_fixup(const double* G, const VolDims& V, const IntegParams& P, int32_t* lab, uint8_t* state,
-                         const int64_t* list, int n, int64_t* next, int* n_next, uint32_t* queued, int num_sms,
-                         cudaStream_t stream) {
+cudaError_t launch_fixup(const double* G, const VolDims& V, const IntegParams& P, int32_t* lab, const int32_t* lab0,
+                         uint8_t* state, const int64_t* list, int n, int64_t* next, int* n_next, uint32_t* queued,
+                         int num_sms, cudaStream_t stream) {
   if (n <= 0) return cudaSuccess;
   Adv64 A{G, V, P, state};
   const int blocks = (n + 127) / 128;
-  fixup_kernel<<<blocks < num_sms * 16 ? blocks : num_sms * 16, 128, 0, stream>>>(A, lab, state, list, n, next, n_next,
-                                                                                  queued);
+  fixup_kernel<<<blocks < num_sms * 16 ? blocks : num_sms * 16, 128, 0, stream>>>(A, lab, lab0, state, list, n, next,
+                                                                                  n_next, queued);
   return cudaGetLastError();
 }
 
-cudaError_t launch_fixup32(const float4* G, const VolDims& V, const IntegParams& P, int32_t* lab, uint8_t* state,
-                           const int64_t* list, int n, int64_t* next, int* n_next, uint32_t* queued, int64_t* amb,
-                           int* n_amb, int amb_mode, int num_sms, cudaStream_t stream) {
+cudaError_t launch_fixup32(const float4* G, const VolDims& V, const IntegParams& P, int32_t* lab, const int32_t* lab0,
+                           uint8_t* state, const int64_t* list, int n, int64_t* next, int* n_next, uint32_t* queued,
+                           int64_t* amb, int* n_amb, int amb_mode, int num_sms, cudaStream_t stream) {
   if (n <= 0) return cudaSuccess;
-  Adv32 A{G, V, P, lab, state};
+  Adv32 A{G, V, P, lab, nullptr, 0, state};
   const int blocks = (n + 127) / 128;
-  fixup32_kernel<<<blocks < num_sms * 16 ? blocks : num_sms * 16, 128, 0, stream>>>(A, lab, state, list, n, next,
+  fixup32_kernel<<<blocks < num_sms * 16 ? blocks : num_sms * 16, 128, 0, stream>>>(A, lab, lab0, state, list, n, next,
                                                                                     n_next, queued, amb, n_amb,
                                                                                     amb_mode);
   return cudaGetLastError();
@@ -592,9 +631,10 @@ cudaError_t launch_clean(const int32_t* lab, const float* f, const VolDims& V, i
   const int grid = num_sms * 8;
   uf_init_kernel<<<grid, 256, 0, stream>>>(parent, N);
   uf_hook_kernel<<<grid, 256, 0, stream>>>(lab, f, V, dir, parent);
-  uf_flatten_kernel<<<grid, 256, 0, stream>>>(parent, N);
-  clean_target_kernel<<<grid, 256, 0, stream>>>(lab, f, V, dir, parent, target);
-  clean_resolve_kernel<<<grid, 256, 0, stream>>>(lab, V, parent, target, out);
+  // roots into `target`; from there on `target` holds the roots and `parent` the merge targets
+  uf_roots_kernel<<<grid, 256, 0, stream>>>(parent, target, N);
+  clean_target_kernel<<<grid, 256, 0, stream>>>(lab, f, V, dir, target, parent);
+  clean_resolve_kernel<<<grid, 256, 0, stream>>>(lab, V, target, parent, out);
   return cudaGetLastError();
 }
 

@@ -434,9 +434,18 @@ struct LdirWalk2 {
   }
 };
 
+__device__ __forceinline__ int batch_volume(const LdirBatch& B, int64_t flat_tile) {
+  int lo = 0, hi = B.n - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (B.v[mid].tile0 <= flat_tile) lo = mid; else hi = mid - 1;
+  }
+  return lo;
+}
+
 template <int ND, int TX, int TY, int TZ, int BS>
-__global__ void __launch_bounds__(BS) ldir_tile_kernel(uint8_t* __restrict__ g, const GradDims D,
-                                                       uint8_t* __restrict__ saved, int* __restrict__ err) {
+__global__ void __launch_bounds__(BS) ldir_tile_kernel(const LdirBatch B, uint8_t* __restrict__ saved,
+                                                       int* __restrict__ err) {
   using T = LdirTile<ND, TX, TY, TZ>;
   constexpr int NL = T::NL;
   static_assert(NL < 65536, "local ids are 16-bit");
@@ -449,10 +458,6 @@ __global__ void __launch_bounds__(BS) ldir_tile_kernel(uint8_t* __restrict__ g, 
   __shared__ int s_qtail;
 
   const int tid = threadIdx.x;
-  const int64_t dX = D.d[0], dY = D.d[1], dZ = D.d[2];
-  const int64_t ntx = (dX + TX - 1) / TX, nty = (dY + TY - 1) / TY;
-  const int64_t ntz = (ND == 3) ? (dZ + TZ - 1) / TZ : 1;
-  const int64_t ntiles = ntx * nty * ntz;
 
   LdirWalk2<T, ND> W;
   W.sg = sg;
@@ -461,9 +466,15 @@ __global__ void __launch_bounds__(BS) ldir_tile_kernel(uint8_t* __restrict__ g, 
   W.vis = s_vis;
   W.qtail = &s_qtail;
   W.err = err;
-  W.dec_map = D.dec_map;
 
-  for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+  for (int64_t flat = blockIdx.x; flat < B.total_tiles; flat += gridDim.x) {
+    const LdirVol& vol = B.v[batch_volume(B, flat)];
+    uint8_t* __restrict__ g = vol.g;
+    const GradDims& D = vol.D;
+    W.dec_map = D.dec_map;
+    const int64_t dX = D.d[0], dY = D.d[1], dZ = D.d[2];
+    const int64_t ntx = (dX + TX - 1) / TX, nty = (dY + TY - 1) / TY;
+    const int64_t tile = flat - vol.tile0;
     const int64_t tx = tile % ntx, ty = (tile / ntx) % nty, tz = (ND == 3) ? tile / (ntx * nty) : 0;
     const int64_t o[3] = {tx * TX - T::H, ty * TY - T::H, (ND == 3) ? tz * TZ - T::H : 0};
     const int64_t dd[3] = {dX, dY, dZ};
@@ -547,7 +558,7 @@ __global__ void __launch_bounds__(BS) ldir_tile_kernel(uint8_t* __restrict__ g, 
       if (gx < dX && gy < dY && gz < dZ)
         g[gx + gy * D.cs[1] + gz * D.cs[2]] = sg[(ix + T::H) + T::LX * ((iy + T::H) + T::LY * (iz + (ND == 3 ? T::H : 0)))];
     }
-    uint8_t* sv = saved + tile * (int64_t)NL;
+    uint8_t* sv = saved + flat * (int64_t)NL;
     for (int k = tid; k < NL; k += BS) sv[k] = sg[k];
     __syncthreads();
   }
@@ -595,45 +606,62 @@ __device__ __forceinline__ void push_item(int64_t* q, int* n, int cap, int* err,
   if (slot < cap) q[slot] = c; else atomicOr(err, kErrLocalQueue);
 }
 
+// frontier entries carry their volume in the top bits
+constexpr int kVolShift = 58;
+constexpr int64_t kCellMask = ((int64_t)1 << kVolShift) - 1;
+
+__device__ __forceinline__ GradView volume_view(const LdirVol& v, int* lock, int* err) {
+  return GradView{v.g, reinterpret_cast<uintptr_t>(v.g), reinterpret_cast<uintptr_t>(v.g + v.D.ncells), lock, err};
+}
+
 template <int ND, int TX, int TY, int TZ>
-__global__ void ldir_check_kernel(const GradView G, const GradDims D, const uint8_t* __restrict__ saved,
-                                  int64_t* __restrict__ queue, int* __restrict__ n_queue, int cap) {
+__global__ void ldir_check_kernel(const LdirBatch B, const uint8_t* __restrict__ saved, int64_t* __restrict__ queue,
+                                  int* __restrict__ n_queue, int cap, int* lock, int* err) {
   using T = LdirTile<ND, TX, TY, TZ>;
   constexpr int NH = halo_count<T, ND>();
-  const int64_t dX = D.d[0], dY = D.d[1], dZ = D.d[2];
-  const int64_t ntx = (dX + TX - 1) / TX, nty = (dY + TY - 1) / TY;
-  const int64_t ntz = (ND == 3) ? (dZ + TZ - 1) / TZ : 1;
-  const int64_t total = ntx * nty * ntz * NH;
+  const int64_t total = B.total_tiles * NH;
   for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t tile = e / NH;
+    const int64_t flat = e / NH;
     const int b = halo_cell<T, ND>((int)(e % NH));
-    const uint8_t s = saved[tile * T::NL + b];
+    const uint8_t s = saved[flat * T::NL + b];
     if (!(s & 1u)) continue;  // outside the complex, or nothing there
+    const int vi = batch_volume(B, flat);
+    const LdirVol& vol = B.v[vi];
+    const GradDims& D = vol.D;
+    const int64_t ntx = (D.d[0] + TX - 1) / TX, nty = (D.d[1] + TY - 1) / TY;
+    const int64_t tile = flat - vol.tile0;
     const int64_t tx = tile % ntx, ty = (tile / ntx) % nty, tz = (ND == 3) ? tile / (ntx * nty) : 0;
     const int lx = b % T::LX, ly = (b / T::LX) % T::LY, lz = b / (T::LX * T::LY);
     const int64_t gx = tx * TX - T::H + lx, gy = ty * TY - T::H + ly, gz = (ND == 3) ? tz * TZ - T::H + lz : 0;
     const int64_t c = gx + gy * D.cs[1] + gz * D.cs[2];
     const unsigned v = s >> 5;
-    if ((unsigned)(G.g[c] >> 5) <= v) continue;
+    if ((unsigned)(vol.g[c] >> 5) <= v) continue;
+    const GradView G = volume_view(vol, lock, err);
     if (!lower_ldir(G, c, v)) continue;
     const int dim = (int)((gx & 1) + (gy & 1) + (gz & 1));
-    if ((dim == 1 && v == 2u) || (dim == 2 && v == 1u)) push_item(queue, n_queue, cap, G.err, c);
+    if ((dim == 1 && v == 2u) || (dim == 2 && v == 1u))
+      push_item(queue, n_queue, cap, err, ((int64_t)vi << kVolShift) | c);
   }
 }
 
 // Finish the walks of queued items in global memory, depth first with a short
 // per-thread stack; what does not fit goes to the next round's queue.
 template <int ND>
-__global__ void __launch_bounds__(128) ldir_walk_kernel(const GradView G, const GradDims D,
-                                                        const int64_t* __restrict__ qin, int n_in,
-                                                        int64_t* __restrict__ qout, int* __restrict__ n_out, int cap) {
+__global__ void __launch_bounds__(128) ldir_walk_kernel(const LdirBatch B, const int64_t* __restrict__ qin, int n_in,
+                                                        int64_t* __restrict__ qout, int* __restrict__ n_out, int cap,
+                                                        int* lock, int* err) {
   constexpr int SD = 24;
   int64_t stack[SD];
-  const int64_t st[3] = {D.cs[0], D.cs[1], D.cs[2]};
-  const int64_t dd[3] = {D.d[0], D.d[1], D.d[2]};
   for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n_in; k += gridDim.x * blockDim.x) {
+    const int64_t entry = qin[k];
+    const int vi = (int)(entry >> kVolShift);
+    const LdirVol& vol = B.v[vi];
+    const GradDims& D = vol.D;
+    const GradView G = volume_view(vol, lock, err);
+    const int64_t st[3] = {D.cs[0], D.cs[1], D.cs[2]};
+    const int64_t dd[3] = {D.d[0], D.d[1], D.d[2]};
     int sp = 0;
-    stack[sp++] = qin[k];
+    stack[sp++] = entry & kCellMask;
     while (sp > 0) {
       const int64_t i = stack[--sp];
       int64_t l[3];
@@ -670,7 +698,7 @@ __global__ void __launch_bounds__(128) ldir_walk_kernel(const GradView G, const 
           }
           if (!lower_ldir(G, tp, value)) continue;
           if (sp < SD) stack[sp++] = tp;
-          else push_item(qout, n_out, cap, G.err, tp);
+          else push_item(qout, n_out, cap, err, ((int64_t)vi << kVolShift) | tp);
         }
       }
     }
@@ -691,48 +719,58 @@ int64_t ldir_num_tiles(int nd, const GradDims& D) {
 
 int64_t ldir_box_bytes(int nd) { return nd == 3 ? Tile3::NL : Tile2::NL; }
 
-cudaError_t launch_ldir_tile(int nd, uint8_t* g, const GradDims& D, uint8_t* saved, int* err, int num_sms,
-                             cudaStream_t stream) {
-  const int64_t nt = ldir_num_tiles(nd, D);
+cudaError_t make_ldir_batch(int nd, int n, uint8_t* const* g, const GradDims* D, LdirBatch* B) {
+  if (n < 1 || n > kMaxBatch || (nd == 2 && n != 1)) return cudaErrorInvalidValue;
+  B->n = n;
+  int64_t off = 0;
+  for (int i = 0; i < n; i++) {
+    B->v[i].g = g[i];
+    B->v[i].D = D[i];
+    B->v[i].tile0 = off;
+    off += ldir_num_tiles(nd, D[i]);
+  }
+  B->total_tiles = off;
+  return cudaSuccess;
+}
+
+cudaError_t launch_ldir_tile(int nd, const LdirBatch& B, uint8_t* saved, int* err, int num_sms, cudaStream_t stream) {
   const int64_t cap = (int64_t)num_sms * 4;
-  const int grid = (int)(nt < cap ? nt : cap);
+  const int grid = (int)(B.total_tiles < cap ? B.total_tiles : cap);
   if (grid <= 0) return cudaSuccess;
   if (nd == 3) {
     auto k = ldir_tile_kernel<3, kTX3, kTY3, kTZ3, kBS3>;
     const size_t sm = Tile3::tile_smem_bytes();
     cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
     if (e != cudaSuccess) return e;
-    k<<<grid, kBS3, sm, stream>>>(g, D, saved, err);
+    k<<<grid, kBS3, sm, stream>>>(B, saved, err);
   } else {
     auto k = ldir_tile_kernel<2, kTX2, kTY2, 1, kBS2>;
     const size_t sm = Tile2::tile_smem_bytes();
     cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
     if (e != cudaSuccess) return e;
-    k<<<grid, kBS2, sm, stream>>>(g, D, saved, err);
+    k<<<grid, kBS2, sm, stream>>>(B, saved, err);
   }
   return cudaGetLastError();
 }
 
-cudaError_t launch_ldir_check(int nd, uint8_t* g, const GradDims& D, const uint8_t* saved, int64_t* queue, int* n_queue,
-                              int cap, int* lock, int* err, int num_sms, cudaStream_t stream) {
-  const GradView G{g, reinterpret_cast<uintptr_t>(g), reinterpret_cast<uintptr_t>(g + D.ncells), lock, err};
+cudaError_t launch_ldir_check(int nd, const LdirBatch& B, const uint8_t* saved, int64_t* queue, int* n_queue, int cap,
+                              int* lock, int* err, int num_sms, cudaStream_t stream) {
   if (nd == 3)
-    ldir_check_kernel<3, kTX3, kTY3, kTZ3><<<num_sms * 8, 256, 0, stream>>>(G, D, saved, queue, n_queue, cap);
+    ldir_check_kernel<3, kTX3, kTY3, kTZ3><<<num_sms * 8, 256, 0, stream>>>(B, saved, queue, n_queue, cap, lock, err);
   else
-    ldir_check_kernel<2, kTX2, kTY2, 1><<<num_sms * 8, 256, 0, stream>>>(G, D, saved, queue, n_queue, cap);
+    ldir_check_kernel<2, kTX2, kTY2, 1><<<num_sms * 8, 256, 0, stream>>>(B, saved, queue, n_queue, cap, lock, err);
   return cudaGetLastError();
 }
 
-cudaError_t launch_ldir_walk(int nd, uint8_t* g, const GradDims& D, const int64_t* qin, int n_in, int64_t* qout,
-                             int* n_out, int cap, int* lock, int* err, int num_sms, cudaStream_t stream) {
+cudaError_t launch_ldir_walk(int nd, const LdirBatch& B, const int64_t* qin, int n_in, int64_t* qout, int* n_out,
+                             int cap, int* lock, int* err, int num_sms, cudaStream_t stream) {
   if (n_in <= 0) return cudaSuccess;
-  const GradView G{g, reinterpret_cast<uintptr_t>(g), reinterpret_cast<uintptr_t>(g + D.ncells), lock, err};
   const int blocks = (n_in + 127) / 128;
   const int grid = blocks < num_sms * 16 ? blocks : num_sms * 16;
   if (nd == 3)
-    ldir_walk_kernel<3><<<grid, 128, 0, stream>>>(G, D, qin, n_in, qout, n_out, cap);
+    ldir_walk_kernel<3><<<grid, 128, 0, stream>>>(B, qin, n_in, qout, n_out, cap, lock, err);
   else
-    ldir_walk_kernel<2><<<grid, 128, 0, stream>>>(G, D, qin, n_in, qout, n_out, cap);
+    ldir_walk_kernel<2><<<grid, 128, 0, stream>>>(B, qin, n_in, qout, n_out, cap, lock, err);
   return cudaGetLastError();
 }
 

@@ -24,44 +24,73 @@
 
 namespace msc {
 
-// Block = 32 consecutive x by BS/32 consecutive y at one z; grid (x-blocks,
-// y-blocks, z), looping over z when Z exceeds the grid's z extent.  Neighbour and
-// cell offsets are 32-bit; only the per-vertex base addresses are 64-bit.
+// One block's work: 32 consecutive x by BS/32 consecutive y at one z of volume (f, g,
+// D).  Neighbour and cell offsets are 32-bit; only the per-vertex base addresses are
+// 64-bit.
+template <int ND, int BS>
+__device__ __forceinline__ bool lstar_block(const float* __restrict__ f, uint8_t* __restrict__ g, const GradDims& D,
+                                            int64_t bx, int64_t by, int64_t z, uint64_t* s_key) {
+  using N = Nb<ND>;
+  constexpr int ROWS = BS / 32;
+  const int tid = threadIdx.x;
+  const int64_t X = D.v[0], Y = D.v[1], Z = D.v[2];
+  const int64_t x = bx * 32 + (tid & 31);
+  const int64_t y = by * ROWS + (tid >> 5);
+  if (x >= X || y >= Y) return false;
+  const int sX = (int)X, sXY = (int)(X * Y);
+  const int c1 = (int)D.cs[1], c2 = (int)D.cs[2];
+  const float* fv = f + (x + X * (y + Y * z));
+  uint8_t* gc = g + (2 * x + 2 * y * D.cs[1] + 2 * z * D.cs[2]);
+  auto load = [&](int p, float& v) { v = __ldg(fv + (N::d(p, 0) + N::d(p, 1) * sX + (ND == 3 ? N::d(p, 2) : 0) * sXY)); };
+  auto store = [&](int p, uint8_t b) { gc[N::d(p, 0) + N::d(p, 1) * c1 + (ND == 3 ? N::d(p, 2) : 0) * c2] = b; };
+  const bool interior = x > 0 && x < X - 1 && y > 0 && y < Y - 1 && (ND == 2 || (z > 0 && z < Z - 1));
+  return process_vertex<ND>(x, y, z, X, Y, Z, interior, load, s_key + tid, BS, D.enc_map, store);
+}
+
+// One volume: grid (x-blocks, y-blocks, z), looping over z when Z exceeds the grid.
 template <int ND, int BS>
 __global__ void __launch_bounds__(BS) lstar_kernel(const float* __restrict__ f, uint8_t* __restrict__ g,
                                                    const GradDims D, int* __restrict__ err) {
-  using N = Nb<ND>;
-  constexpr int NPOS = N::NPOS;
-  constexpr int ROWS = BS / 32;
-  __shared__ uint64_t s_key[NPOS * BS];
-  const int tid = threadIdx.x;
-
-  const int64_t X = D.v[0], Y = D.v[1], Z = D.v[2];
-  const int x = blockIdx.x * 32 + (tid & 31);
-  const int y = blockIdx.y * ROWS + (tid >> 5);
-  if (x >= X || y >= Y) return;
-  const int sX = (int)X, sXY = (int)(X * Y);
-  const int c1 = (int)D.cs[1], c2 = (int)D.cs[2];
-  uint64_t* col = s_key + tid;
+  __shared__ uint64_t s_key[Nb<ND>::NPOS * BS];
   bool nan = false;
-  for (int64_t z = blockIdx.z; z < Z; z += gridDim.z) {
-    const float* fv = f + (x + X * (y + Y * z));
-    uint8_t* gc = g + (2 * (int64_t)x + 2 * (int64_t)y * D.cs[1] + 2 * z * D.cs[2]);
-    auto load = [&](int p, float& v) { v = __ldg(fv + (N::d(p, 0) + N::d(p, 1) * sX + (ND == 3 ? N::d(p, 2) : 0) * sXY)); };
-    auto store = [&](int p, uint8_t b) { gc[N::d(p, 0) + N::d(p, 1) * c1 + (ND == 3 ? N::d(p, 2) : 0) * c2] = b; };
-    const bool interior = x > 0 && x < X - 1 && y > 0 && y < Y - 1 && (ND == 2 || (z > 0 && z < Z - 1));
-    nan |= process_vertex<ND>(x, y, z, X, Y, Z, interior, load, col, BS, D.enc_map, store);
+  for (int64_t z = blockIdx.z; z < D.v[2]; z += gridDim.z) nan |= lstar_block<ND, BS>(f, g, D, blockIdx.x, blockIdx.y, z, s_key);
+  if (nan) atomicOr(err, kErrNaN);
+}
+
+// Many volumes in one launch: a flat grid over every volume's (x-block, y-block, z)
+// triples; a block finds its volume by binary search over the volumes' first blocks.
+template <int BS>
+__global__ void __launch_bounds__(BS) lstar_batch_kernel(const LstarBatch B, int* __restrict__ err) {
+  __shared__ uint64_t s_key[27 * BS];
+  bool nan = false;
+  for (int64_t blk = blockIdx.x; blk < B.total_blocks; blk += gridDim.x) {
+    int lo = 0, hi = B.n - 1;
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (B.v[mid].block0 <= blk) lo = mid; else hi = mid - 1;
+    }
+    const LstarVol& V = B.v[lo];
+    const int64_t r = blk - V.block0;
+    const int64_t bx = r % V.gx, by = (r / V.gx) % V.gy, z = r / ((int64_t)V.gx * V.gy);
+    nan |= lstar_block<3, BS>(V.f, V.g, V.D, bx, by, z, s_key);
   }
   if (nan) atomicOr(err, kErrNaN);
 }
 
+namespace {
+constexpr int kLstarBS = 128;
+bool lstar_dims_ok(const GradDims& D) {
+  // a z-plane of cells must be addressable with 32-bit offsets
+  return !(D.v[0] > (int64_t)1 << 30 || D.v[1] > (int64_t)1 << 30 || D.v[0] * D.v[1] > ((int64_t)1 << 31) - 1 ||
+           D.cs[2] > ((int64_t)1 << 31) - 1);
+}
+}  // namespace
+
 cudaError_t launch_lstar(int nd, const float* f, uint8_t* g, const GradDims& D, int* err, int num_sms,
                          cudaStream_t stream) {
   (void)num_sms;
-  constexpr int BS = 128;
-  if (D.v[0] > (int64_t)1 << 30 || D.v[1] > (int64_t)1 << 30 || D.v[0] * D.v[1] > ((int64_t)1 << 31) - 1 ||
-      D.cs[2] > ((int64_t)1 << 31) - 1)
-    return cudaErrorInvalidValue;  // a z-plane of cells must be addressable with 32-bit offsets
+  constexpr int BS = kLstarBS;
+  if (!lstar_dims_ok(D)) return cudaErrorInvalidValue;
   const dim3 grid((unsigned)((D.v[0] + 31) / 32), (unsigned)((D.v[1] + BS / 32 - 1) / (BS / 32)),
                   (unsigned)(D.v[2] < 65535 ? D.v[2] : 65535));
   if (grid.y > 65535u) return cudaErrorInvalidValue;
@@ -69,6 +98,33 @@ cudaError_t launch_lstar(int nd, const float* f, uint8_t* g, const GradDims& D, 
     lstar_kernel<3, BS><<<grid, BS, 0, stream>>>(f, g, D, err);
   else
     lstar_kernel<2, BS><<<grid, BS, 0, stream>>>(f, g, D, err);
+  return cudaGetLastError();
+}
+
+cudaError_t make_lstar_batch(int n, const float* const* f, uint8_t* const* g, const GradDims* D, LstarBatch* B) {
+  if (n < 1 || n > kMaxBatch) return cudaErrorInvalidValue;
+  B->n = n;
+  int64_t off = 0;
+  for (int i = 0; i < n; i++) {
+    if (!lstar_dims_ok(D[i])) return cudaErrorInvalidValue;
+    LstarVol& v = B->v[i];
+    v.f = f[i];
+    v.g = g[i];
+    v.D = D[i];
+    v.gx = (int)((D[i].v[0] + 31) / 32);
+    v.gy = (int)((D[i].v[1] + kLstarBS / 32 - 1) / (kLstarBS / 32));
+    v.block0 = off;
+    off += (int64_t)v.gx * v.gy * D[i].v[2];
+  }
+  B->total_blocks = off;
+  return cudaSuccess;
+}
+
+cudaError_t launch_lstar_batch(const LstarBatch& B, int* err, int num_sms, cudaStream_t stream) {
+  const int64_t cap = (int64_t)num_sms * 64;
+  const int grid = (int)(B.total_blocks < cap ? B.total_blocks : cap);
+  if (grid <= 0) return cudaSuccess;
+  lstar_batch_kernel<kLstarBS><<<grid, kLstarBS, 0, stream>>>(B, err);
   return cudaGetLastError();
 }
 

@@ -11,6 +11,7 @@
 #include <cstdio>
 #include <cstring>
 #include <string>
+#include <vector>
 
 #include "msc_device.cuh"
 #include "../../include/msc_gpu.h"
@@ -155,11 +156,8 @@ int ldir_passes(int nd, uint8_t* g, const msc::GradDims& D, cudaStream_t stream,
 // lowered.  Should a frontier queue overflow, the multi-pass form finishes the
 // closure from wherever it stands (the closure is monotone, so any intermediate
 // state is a valid start).
-int ldir_impl(int nd, uint8_t* g, const int64_t* dims, cudaStream_t stream, Scratch& s, int* passes_out) {
-  msc::GradDims D;
-  if (!make_dims(nd, dims, &D)) return fail(MSC_ERR_BAD_DIMS, "invalid dims");
-  if (!g) return fail(MSC_ERR_NULL_POINTER, "null buffer");
-  const int64_t ntiles = msc::ldir_num_tiles(nd, D);
+int ldir_batch_impl(int nd, const msc::LdirBatch& B, cudaStream_t stream, Scratch& s, int* passes_out) {
+  const int64_t ntiles = B.total_tiles;
   const int64_t box = msc::ldir_box_bytes(nd);
   const int sms = num_sms();
   int cap = (int)std::min<int64_t>(std::max<int64_t>(ntiles * 256, 1 << 16), (int64_t)1 << 30);
@@ -187,8 +185,8 @@ int ldir_impl(int nd, uint8_t* g, const int64_t* dims, cudaStream_t stream, Scra
   MSC_CUDA(cudaMemsetAsync(ctr, 0, 4 * sizeof(int), stream), "cudaMemsetAsync(counters)");
 
   int launches = 0;
-  MSC_CUDA(msc::launch_ldir_tile(nd, g, D, saved, s.words, sms, stream), "ldir tile kernel launch");
-  MSC_CUDA(msc::launch_ldir_check(nd, g, D, saved, queues, ctr, cap, ctr + 2, ctr + 3, sms, stream),
+  MSC_CUDA(msc::launch_ldir_tile(nd, B, saved, s.words, sms, stream), "ldir tile kernel launch");
+  MSC_CUDA(msc::launch_ldir_check(nd, B, saved, queues, ctr, cap, ctr + 2, ctr + 3, sms, stream),
            "ldir check kernel launch");
   launches += 2;
   int64_t* qa = queues;
@@ -207,17 +205,27 @@ int ldir_impl(int nd, uint8_t* g, const int64_t* dims, cudaStream_t stream, Scra
     if (round > 4096) return fail(MSC_ERR_ITER_LIMIT, "ldir frontier walk did not converge");
     int* n_out = round % 2 == 0 ? ctr + 1 : ctr;
     MSC_CUDA(cudaMemsetAsync(n_out, 0, sizeof(int), stream), "reset queue");
-    MSC_CUDA(msc::launch_ldir_walk(nd, g, D, qa, n, qb, n_out, cap, ctr + 2, ctr + 3, sms, stream),
+    MSC_CUDA(msc::launch_ldir_walk(nd, B, qa, n, qb, n_out, cap, ctr + 2, ctr + 3, sms, stream),
              "ldir walk kernel launch");
     launches++;
     std::swap(qa, qb);
   }
   if (overflow) {
-    if (int rc = ldir_passes(nd, g, D, stream, s, &launches)) return rc;
+    for (int i = 0; i < B.n; i++)
+      if (int rc = ldir_passes(nd, B.v[i].g, B.v[i].D, stream, s, &launches)) return rc;
   }
   if (passes_out) *passes_out = launches;
   g_last_passes = launches;
   return MSC_OK;
+}
+
+int ldir_impl(int nd, uint8_t* g, const int64_t* dims, cudaStream_t stream, Scratch& s, int* passes_out) {
+  msc::GradDims D;
+  if (!make_dims(nd, dims, &D)) return fail(MSC_ERR_BAD_DIMS, "invalid dims");
+  if (!g) return fail(MSC_ERR_NULL_POINTER, "null buffer");
+  msc::LdirBatch B;
+  MSC_CUDA(msc::make_ldir_batch(nd, 1, &g, &D, &B), "ldir batch");
+  return ldir_batch_impl(nd, B, stream, s, passes_out);
 }
 
 int validate(int nd, const int64_t* dims, const void* a, const void* b) {
@@ -291,6 +299,36 @@ int host_impl(int nd, const float* fh, const int64_t* dims, uint8_t* gh) {
   return MSC_OK;
 }
 
+// Many 3D volumes: one K1 launch and one ldir tile / check / walk sequence per chunk
+// of up to kMaxBatch volumes.
+int grad_batch_impl(int n, const float* const* f, const int64_t* dims, uint8_t* const* g, cudaStream_t stream) {
+  if (n < 0) return fail(MSC_ERR_BAD_DIMS, "negative batch size");
+  if (n == 0) return MSC_OK;
+  if (!f || !dims || !g) return fail(MSC_ERR_NULL_POINTER, "null argument");
+  std::vector<msc::GradDims> D(n);
+  for (int i = 0; i < n; i++) {
+    if (!make_dims(3, dims + 3 * i, &D[i])) return fail(MSC_ERR_BAD_DIMS, "invalid dims of volume " + std::to_string(i));
+    if (!f[i] || !g[i]) return fail(MSC_ERR_NULL_POINTER, "null buffer of volume " + std::to_string(i));
+  }
+  Scratch s;
+  if (int rc = alloc_scratch(s, stream)) return rc;
+  const int sms = num_sms();
+  int launches = 0;
+  for (int i0 = 0; i0 < n; i0 += msc::kMaxBatch) {
+    const int m = std::min(n - i0, msc::kMaxBatch);
+    msc::LstarBatch LB;
+    MSC_CUDA(msc::make_lstar_batch(m, f + i0, g + i0, D.data() + i0, &LB), "lower-star batch (plane too large)");
+    MSC_CUDA(msc::launch_lstar_batch(LB, s.words, sms, stream), "lower-star batch kernel launch");
+    msc::LdirBatch B;
+    MSC_CUDA(msc::make_ldir_batch(3, m, g + i0, D.data() + i0, &B), "ldir batch");
+    int l = 0;
+    if (int rc = ldir_batch_impl(3, B, stream, s, &l)) return rc;
+    launches += 1 + l;
+  }
+  g_last_passes = launches;
+  return check_errors(s, stream);
+}
+
 }  // namespace
 
 namespace msc {
@@ -318,6 +356,11 @@ int64_t msc_num_cells_2d(const int64_t dims[2]) {
 
 int msc_lower_star_grad_3d(const float* f, const int64_t dims[3], uint8_t* g, msc_stream_t stream) {
   return grad_impl(3, f, dims, g, (cudaStream_t)stream);
+}
+
+int msc_lower_star_grad_batch_3d(int n, const float* const* f, const int64_t* dims, uint8_t* const* grad,
+                                 msc_stream_t stream) {
+  return grad_batch_impl(n, f, dims, grad, (cudaStream_t)stream);
 }
 
 int msc_lower_star_grad_2d(const float* f, const int64_t dims[2], uint8_t* g, msc_stream_t stream) {

@@ -43,14 +43,41 @@ namespace msc {
 // launchers (defined next to their kernels)
 cudaError_t launch_lstar(int nd, const float* f, uint8_t* g, const GradDims& D, int* err, int num_sms,
                          cudaStream_t stream);
+
+// Batches of 3D volumes, passed by value in the launch parameters (no device table).
+constexpr int kMaxBatch = 64;
+struct LstarVol {
+  const float* f;
+  uint8_t* g;
+  GradDims D;
+  int64_t block0;  // first flat block of the volume
+  int gx, gy;      // x-blocks per row, y-blocks per plane
+};
+struct LstarBatch {
+  int n;
+  int64_t total_blocks;
+  LstarVol v[kMaxBatch];
+};
+cudaError_t make_lstar_batch(int n, const float* const* f, uint8_t* const* g, const GradDims* D, LstarBatch* B);
+cudaError_t launch_lstar_batch(const LstarBatch& B, int* err, int num_sms, cudaStream_t stream);
 int64_t ldir_num_tiles(int nd, const GradDims& D);
 int64_t ldir_box_bytes(int nd);
-cudaError_t launch_ldir_tile(int nd, uint8_t* g, const GradDims& D, uint8_t* saved, int* err, int num_sms,
-                             cudaStream_t stream);
-cudaError_t launch_ldir_check(int nd, uint8_t* g, const GradDims& D, const uint8_t* saved, int64_t* queue, int* n_queue,
-                              int cap, int* lock, int* err, int num_sms, cudaStream_t stream);
-cudaError_t launch_ldir_walk(int nd, uint8_t* g, const GradDims& D, const int64_t* qin, int n_in, int64_t* qout,
-                             int* n_out, int cap, int* lock, int* err, int num_sms, cudaStream_t stream);
+struct LdirVol {
+  uint8_t* g;
+  GradDims D;
+  int64_t tile0;  // first flat tile of the volume
+};
+struct LdirBatch {
+  int n;
+  int64_t total_tiles;
+  LdirVol v[kMaxBatch];
+};
+cudaError_t make_ldir_batch(int nd, int n, uint8_t* const* g, const GradDims* D, LdirBatch* B);
+cudaError_t launch_ldir_tile(int nd, const LdirBatch& B, uint8_t* saved, int* err, int num_sms, cudaStream_t stream);
+cudaError_t launch_ldir_check(int nd, const LdirBatch& B, const uint8_t* saved, int64_t* queue, int* n_queue, int cap,
+                              int* lock, int* err, int num_sms, cudaStream_t stream);
+cudaError_t launch_ldir_walk(int nd, const LdirBatch& B, const int64_t* qin, int n_in, int64_t* qout, int* n_out,
+                             int cap, int* lock, int* err, int num_sms, cudaStream_t stream);
 cudaError_t launch_ldir_pass(int nd, uint8_t* g, const GradDims& D, const uint8_t* dirty_in, uint8_t* dirty_out,
                              int* changed, int* err, int num_sms, cudaStream_t stream);
 cudaError_t launch_central_diff(int nd, int layout, const float* f, void* out, const GradDims& D, int num_sms,

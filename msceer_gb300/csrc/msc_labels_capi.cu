@@ -309,18 +309,17 @@ int prepare_direction(LabelCtx& c, DirLabels& d, int32_t* stage_terminal) {
   return MSC_OK;
 }
 
-// Streamline integration of the vertices still unassigned (-1), boundary fix-up and
-// the cleaner; `out` receives the final labels.
-int integrate_direction(LabelCtx& c, DirLabels& d, int32_t* out, int32_t* stage_integrated, int64_t stats[2]) {
-  const int64_t N = c.N;
-  const msc::VolDims& V = c.V;
-  cudaStream_t st = c.st;
-  const msc_integ_params* p = c.p;
-  const int sms = c.sms;
-  if (d.n_ext > 0) zero_seed_grad_kernel<<<(d.n_ext + 255) / 256, 256, 0, st>>>(d.seed, d.n_ext, c.g32, c.g64);
+msc::IntegParams integ_params(const msc_integ_params* p, int dir) {
+  return msc::IntegParams{p->error_threshold, p->gradient_threshold, p->iteration_limit, (double)p->max_step, dir};
+}
 
-  // first pass with path compression, in the reference's spread order
-  msc::IntegParams P{p->error_threshold, p->gradient_threshold, p->iteration_limit, (double)p->max_step, d.dir};
+// First integration pass of the vertices still unassigned (-1), deterministic, in
+// the reference's spread order, after zeroing the gradient at this direction's seeds.
+int first_pass(LabelCtx& c, DirLabels& d) {
+  const int64_t N = c.N;
+  cudaStream_t st = c.st;
+  if (d.n_ext > 0) zero_seed_grad_kernel<<<(d.n_ext + 255) / 256, 256, 0, st>>>(d.seed, d.n_ext, c.g32, c.g64);
+  const msc::IntegParams P = integ_params(c.p, d.dir);
   msc::SpreadOrder S{};
   S.nlev = 0;
   S.offset[0] = 0;
@@ -332,10 +331,28 @@ int integrate_direction(LabelCtx& c, DirLabels& d, int32_t* out, int32_t* stage_
     S.offset[S.nlev + 1] = S.offset[S.nlev] + (N - start + stride - 1) / stride;
     S.nlev++;
   }
-  LCUDA(msc::launch_integrate_pass1(c.g32, V, P, S, d.lab, sms, st), "integrate");
+  uint8_t* lvl;
+  LCUDA(c.pool.get(&lvl, N), "alloc");
+  LCUDA(msc::launch_integrate_pass1(c.g32, c.V, P, S, d.lab, lvl, c.sms, st), "integrate");
+  return MSC_OK;
+}
+
+// Boundary fix-up of the vertices still marked unassigned in d.state, then the
+// cleaner; `out` receives the final labels.
+int finish_direction(LabelCtx& c, DirLabels& d, int32_t* out, int32_t* stage_integrated, int64_t stats[2]) {
+  const int64_t N = c.N;
+  const msc::VolDims& V = c.V;
+  cudaStream_t st = c.st;
+  const msc_integ_params* p = c.p;
+  const int sms = c.sms;
+  const msc::IntegParams P = integ_params(p, d.dir);
 
   // fix-up waves until no label changes reopen a neighbour: FP32 re-decisions, and
-  // FP64 ones for the streamlines whose FP32 ending was ambiguous
+  // FP64 ones for the streamlines whose FP32 ending was ambiguous; decisions read the
+  // first-pass labels (lab0)
+  int32_t* lab0;
+  LCUDA(c.pool.get(&lab0, N), "alloc");
+  LCUDA(cudaMemcpyAsync(lab0, d.lab, N * sizeof(int32_t), cudaMemcpyDeviceToDevice, st), "copy");
   LCUDA(cudaMemsetAsync(c.queued, 0, (N / 32 + 1) * sizeof(uint32_t), st), "memset");
   LCUDA(cudaMemsetAsync(c.counters + 5, 0, 3 * sizeof(int), st), "memset");
   LCUDA(msc::launch_boundary_set(d.lab, d.state, V, c.list_a, c.counters + 5, c.queued, sms, st), "boundary set");
@@ -349,16 +366,17 @@ int integrate_direction(LabelCtx& c, DirLabels& d, int32_t* out, int32_t* stage_
     if (waves > N) return fail(MSC_ERR_ITER_LIMIT, "fix-up did not converge");
     LCUDA(cudaMemsetAsync(c.counters + 6, 0, 2 * sizeof(int), st), "memset");
     if (p->precision == 1) {
-      LCUDA(msc::launch_fixup(c.g64, V, P, d.lab, d.state, cur, n_list, nxt, c.counters + 6, c.queued, sms, st),
+      LCUDA(msc::launch_fixup(c.g64, V, P, d.lab, lab0, d.state, cur, n_list, nxt, c.counters + 6, c.queued, sms, st),
             "fix-up");
     } else {
-      LCUDA(msc::launch_fixup32(c.g32, V, P, d.lab, d.state, cur, n_list, nxt, c.counters + 6, c.queued, c.amb,
+      LCUDA(msc::launch_fixup32(c.g32, V, P, d.lab, lab0, d.state, cur, n_list, nxt, c.counters + 6, c.queued, c.amb,
                                 c.counters + 7, p->precision == 2 ? 2 : 0, sms, st),
             "fix-up");
       int n_amb = 0;
       if (int rc = read_int(c.counters + 7, &n_amb, st)) return rc;
       stats[1] += n_amb;
-      LCUDA(msc::launch_fixup(c.g64, V, P, d.lab, d.state, c.amb, n_amb, nxt, c.counters + 6, c.queued, sms, st),
+      LCUDA(msc::launch_fixup(c.g64, V, P, d.lab, lab0, d.state, c.amb, n_amb, nxt, c.counters + 6, c.queued, sms,
+                              st),
             "fix-up");
     }
     stats[0] += n_list;
@@ -366,6 +384,7 @@ int integrate_direction(LabelCtx& c, DirLabels& d, int32_t* out, int32_t* stage_
     std::swap(cur, nxt);
   }
   if (stage_integrated) snapshot_kernel<<<c.grid, 256, 0, st>>>(d.lab, stage_integrated, N);
+  if (!out) return MSC_OK;
 
   // isolated-region cleaner
   int64_t *parent, *target;
@@ -373,6 +392,11 @@ int integrate_direction(LabelCtx& c, DirLabels& d, int32_t* out, int32_t* stage_
   LCUDA(c.pool.get(&target, N), "alloc");
   LCUDA(msc::launch_clean(d.lab, c.f, V, d.dir, parent, target, out, sms, st), "clean");
   return MSC_OK;
+}
+
+int integrate_direction(LabelCtx& c, DirLabels& d, int32_t* out, int32_t* stage_integrated, int64_t stats[2]) {
+  if (int rc = first_pass(c, d)) return rc;
+  return finish_direction(c, d, out, stage_integrated, stats);
 }
 
 int finish_errors(LabelCtx& c) {
@@ -401,47 +425,38 @@ int labels_impl(const float* f, const uint8_t* grad, const int64_t* dims, const 
   return finish_errors(c);
 }
 
-// Terminal regions of both directions, the combinatorial labels and the network
-// features (the triage's inputs).
-struct TriageInputs {
-  DirLabels asc, dsc;
-  int32_t* comb = nullptr;  // [2][N]
-  __nv_bfloat16* feat = nullptr;
-};
-
-int triage_inputs(LabelCtx& c, TriageInputs& t) {
-  const int64_t N = c.N;
-  t.asc.dir = -1;
-  t.dsc.dir = 1;
-  if (int rc = prepare_direction(c, t.asc, nullptr)) return rc;
-  if (int rc = prepare_direction(c, t.dsc, nullptr)) return rc;
-  int32_t* succ;
+// Network features of one direction from its first-pass labels (triage_prep.cu).
+int direction_features(LabelCtx& c, DirLabels& d, __nv_bfloat16* feat) {
   double* sums;
-  LCUDA(c.pool.get(&succ, N), "alloc");
   LCUDA(c.pool.get(&sums, 3), "alloc");
-  if (!t.comb) LCUDA(c.pool.get(&t.comb, 2 * N), "alloc");
-  if (!t.feat) LCUDA(c.pool.get(&t.feat, 16 * N), "alloc");
-  LCUDA(msc::launch_comb_labels(c.f, t.asc.lab, c.V, -1, succ, t.comb, c.counters + 3, c.sms, c.st), "comb labels");
-  LCUDA(msc::launch_comb_labels(c.f, t.dsc.lab, c.V, 1, succ, t.comb + N, c.counters + 3, c.sms, c.st), "comb labels");
-  LCUDA(msc::launch_features(c.f, c.g32, t.comb, t.comb + N, t.asc.state, t.dsc.state, c.V, sums, t.feat, c.sms, c.st),
-        "features");
+  LCUDA(msc::launch_features(c.f, c.g32, d.lab, d.state, c.V, d.dir, sums, feat, c.sms, c.st), "features");
   return MSC_OK;
 }
 
-__global__ void comb_out_kernel(const int32_t* comb, int32_t* out, int64_t n) {
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
-    out[i] = comb[i] == msc::kLabelNone ? -1 : comb[i];
-}
-
+// Training data: per direction, the features after the first pass and the targets
+// (1 where the full boundary fix-up changes the first-pass label).  The directions
+// run one after the other, as the plain labeling does.
 int triage_features_impl(const float* f, const uint8_t* grad, const int64_t* dims, const msc_integ_params* p,
-                         uint16_t* features, int32_t* comb, cudaStream_t st) {
-  if (!features || !comb) return fail(MSC_ERR_NULL_POINTER, "null argument");
+                         uint16_t* features, uint8_t* targets, cudaStream_t st) {
+  if (!features) return fail(MSC_ERR_NULL_POINTER, "null argument");
   LabelCtx c(st);
   if (int rc = setup_ctx(c, f, grad, dims, p)) return rc;
-  TriageInputs t;
-  t.feat = reinterpret_cast<__nv_bfloat16*>(features);
-  if (int rc = triage_inputs(c, t)) return rc;
-  comb_out_kernel<<<c.grid, 256, 0, st>>>(t.comb, comb, 2 * c.N);
+  const int64_t N = c.N;
+  int32_t* first;
+  LCUDA(c.pool.get(&first, N), "alloc");
+  for (int k = 0; k < 2; k++) {
+    DirLabels d;
+    d.dir = k == 0 ? -1 : 1;
+    if (int rc = prepare_direction(c, d, nullptr)) return rc;
+    if (int rc = first_pass(c, d)) return rc;
+    if (int rc = direction_features(c, d, reinterpret_cast<__nv_bfloat16*>(features) + (size_t)k * 16 * N)) return rc;
+    if (targets) {
+      LCUDA(cudaMemcpyAsync(first, d.lab, N * sizeof(int32_t), cudaMemcpyDeviceToDevice, st), "copy");
+      int64_t fx[2];
+      if (int rc = finish_direction(c, d, nullptr, nullptr, fx)) return rc;
+      LCUDA(msc::launch_change_targets(d.lab, first, N, targets + (size_t)k * 2 * N, c.sms, st), "targets");
+    }
+  }
   return finish_errors(c);
 }
 
@@ -452,34 +467,37 @@ int triage_labels_impl(const float* f, const uint8_t* grad, const int64_t* dims,
   LabelCtx c(st);
   if (int rc = setup_ctx(c, f, grad, dims, p)) return rc;
   const int64_t N = c.N;
-  TriageInputs t;
-  if (int rc = triage_inputs(c, t)) return rc;
-  // the network: one forward pass gives both directions' logits
   uint8_t *blobs, *flags;
-  __nv_bfloat16 *act1, *act2;
+  __nv_bfloat16 *feat, *act1, *act2;
   float* logits;
-  unsigned long long* counts;  // per direction: flagged, audited, audit mismatches
+  int32_t* first;
+  unsigned long long* counts;  // per direction: flagged, audited, audited the fix-up changed
   LCUDA(c.pool.get(&blobs, msc::kTriageBlobBytes), "alloc");
+  LCUDA(c.pool.get(&feat, 16 * N), "alloc");
   LCUDA(c.pool.get(&act1, 16 * N), "alloc");
   LCUDA(c.pool.get(&act2, 16 * N), "alloc");
   LCUDA(c.pool.get(&logits, 2 * N), "alloc");
-  LCUDA(c.pool.get(&flags, 2 * N), "alloc");
+  LCUDA(c.pool.get(&flags, N), "alloc");
+  LCUDA(c.pool.get(&first, N), "alloc");
   LCUDA(c.pool.get(&counts, 6), "alloc");
   LCUDA(cudaMemsetAsync(counts, 0, 6 * sizeof(unsigned long long), st), "memset");
   const msc::ConvDims D{c.V.X, c.V.Y, c.V.Z, N};
-  LCUDA(msc::triage_forward(t.feat, D, tp->weights, blobs, act1, act2, logits, c.counters + 4, st), "triage forward");
-  DirLabels* dl[2] = {&t.asc, &t.dsc};
   const float thr[2] = {tp->logit_threshold_asc, tp->logit_threshold_dsc};
-  for (int k = 0; k < 2; k++)
-    LCUDA(msc::launch_triage_apply(logits + k * N, thr[k], t.comb + k * N, dl[k]->lab, dl[k]->state, flags + k * N, N,
-                                   tp->audit_fraction, tp->audit_seed + (uint64_t)k, counts + 3 * k, c.sms, st),
-          "triage apply");
-  int64_t fix[4] = {0, 0, 0, 0};
   int32_t* outs[2] = {out_asc, out_dsc};
+  int64_t fix[4] = {0, 0, 0, 0};
   for (int k = 0; k < 2; k++) {
-    if (int rc = integrate_direction(c, *dl[k], outs[k], nullptr, fix + 2 * k)) return rc;
-    LCUDA(msc::launch_audit_count(dl[k]->lab, t.comb + k * N, flags + k * N, N, counts + 3 * k + 2, c.sms, st),
-          "audit");
+    DirLabels d;
+    d.dir = k == 0 ? -1 : 1;
+    if (int rc = prepare_direction(c, d, nullptr)) return rc;
+    if (int rc = first_pass(c, d)) return rc;
+    if (int rc = direction_features(c, d, feat)) return rc;
+    LCUDA(msc::triage_forward(feat, D, tp->weights, blobs, act1, act2, logits, c.counters + 4, st), "triage forward");
+    LCUDA(cudaMemcpyAsync(first, d.lab, N * sizeof(int32_t), cudaMemcpyDeviceToDevice, st), "copy");
+    LCUDA(msc::launch_triage_apply(logits, thr[k], d.state, flags, N, tp->audit_fraction, tp->audit_seed + (uint64_t)k,
+                                   counts + 3 * k, c.sms, st),
+          "triage apply");
+    if (int rc = finish_direction(c, d, outs[k], nullptr, fix + 2 * k)) return rc;
+    LCUDA(msc::launch_audit_count(d.lab, first, flags, N, counts + 3 * k + 2, c.sms, st), "audit");
   }
   for (int k = 0; k < 4; k++) t_stats[k] = fix[k];
   if (stats) {
@@ -574,8 +592,8 @@ int msc_integrated_labels_3d_stages(const float* f, const uint8_t* grad, const i
 }
 
 int msc_triage_features_3d(const float* f, const uint8_t* grad, const int64_t dims[3], const msc_integ_params* params,
-                           uint16_t* features, int32_t* comb, msc_stream_t stream) {
-  return triage_features_impl(f, grad, dims, params, features, comb, (cudaStream_t)stream);
+                           uint16_t* features, uint8_t* targets, msc_stream_t stream) {
+  return triage_features_impl(f, grad, dims, params, features, targets, (cudaStream_t)stream);
 }
 
 int msc_triage_labels_3d(const float* f, const uint8_t* grad, const int64_t dims[3], const msc_integ_params* params,

@@ -15,9 +15,9 @@ struct ConvDims {
 
 enum { kEpiReluBf16 = 0, kEpiLogits = 1, kEpiMaskBf16 = 2 };
 
-constexpr int kTriageCin = 6;   // input features: f, |grad f|, asc / dsc combinatorial boundary, asc / dsc terminal
+constexpr int kTriageCin = 10;  // input features of one direction (triage_prep.cu: features_kernel)
 constexpr int kTriageHidden = 16;
-constexpr int kTriageOut = 2;   // P(asc label differs), P(dsc label differs)
+constexpr int kTriageOut = 2;   // logit 0: P(the fix-up changes the first-pass label); logit 1 trained alike
 // FP32 master parameters: W1[27][16][16] W2[27][16][16] W3[27][16][16] (cin x cout,
 // unused input / output channels zero), b1[16] b2[16] b3[16]
 constexpr int kTriageW = 27 * 16 * 16;
@@ -31,16 +31,15 @@ cudaError_t launch_conv3_tc(int epi, const CUtensorMap& in_map, const uint8_t* w
                             const __nv_bfloat16* mask_act, int* err, cudaStream_t st);
 
 struct VolDims;
-cudaError_t launch_comb_labels(const float* f, const int32_t* lab, const VolDims& V, int dir, int32_t* succ,
-                               int32_t* comb, int* changed, int num_sms, cudaStream_t st);
-cudaError_t launch_features(const float* f, const float4* g, const int32_t* comb_asc, const int32_t* comb_dsc,
-                            const uint8_t* st_asc, const uint8_t* st_dsc, const VolDims& V, double* sums,
-                            __nv_bfloat16* out, int num_sms, cudaStream_t st);
-cudaError_t launch_triage_apply(const float* logits, float logit_threshold, const int32_t* comb, int32_t* lab,
-                                uint8_t* state, uint8_t* flags, int64_t N, float audit_frac, uint64_t audit_seed,
-                                unsigned long long* counts, int num_sms, cudaStream_t st);
-cudaError_t launch_audit_count(const int32_t* lab, const int32_t* comb, const uint8_t* flags, int64_t N,
+cudaError_t launch_features(const float* f, const float4* g, const int32_t* lab, const uint8_t* state, const VolDims& V,
+                            int dir, double* sums, __nv_bfloat16* out, int num_sms, cudaStream_t st);
+cudaError_t launch_triage_apply(const float* logits, float logit_threshold, uint8_t* state, uint8_t* flags, int64_t N,
+                                float audit_frac, uint64_t audit_seed, unsigned long long* counts, int num_sms,
+                                cudaStream_t st);
+cudaError_t launch_audit_count(const int32_t* lab, const int32_t* first, const uint8_t* flags, int64_t N,
                                unsigned long long* count, int num_sms, cudaStream_t st);
+cudaError_t launch_change_targets(const int32_t* lab, const int32_t* first, int64_t N, uint8_t* targets, int num_sms,
+                                  cudaStream_t st);
 cudaError_t launch_pack_weights(const float* params, uint8_t* blobs, cudaStream_t st);
 cudaError_t launch_bce_loss(const float* logits, const uint8_t* target, const ConvDims& D, float pos_weight,
                             float scale, __nv_bfloat16* dY, double* loss, int num_sms, cudaStream_t st);

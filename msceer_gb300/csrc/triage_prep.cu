@@ -1,77 +1,17 @@
-// Learned triage, CUDA-core side: combinatorial steepest-path labels, input features,
-// flags, and the training kernels (loss, weight gradients, Adam, weight packing).
+// Learned triage, CUDA-core side: the network's input features, the flags, and the
+// training kernels (loss, weight gradients, Adam, weight packing).
 //
-// Combinatorial label of a vertex: follow the steepest discrete step (downhill for the
-// ascending manifolds of minima, uphill for the descending ones) until a vertex of a
-// certain terminal region, and take its region.  The step is taken over the 26
-// neighbours with the drop normalised by distance -- a discrete stand-in for the
-// streamline, closer to it than the 6-neighbour V-path of the lower-star gradient
-// (rec_td / rec_tu, gi_extrema_region_builder.h:286-352).  Pointer jumping resolves
-// the chains.
+// The triage decides which vertices the boundary fix-up re-decides.  Every vertex
+// gets the cheap first-pass label (FP32, path compression); the fix-up -- re-
+// integrating every vertex that has a differently labelled neighbour until it reaches
+// a certain region, in waves -- costs about nine tenths of the labeling and changes
+// about one label in ten.  The network predicts, per vertex, whether the fix-up would
+// change its first-pass label; only flagged vertices plus a random audit sample are
+// re-decided, the rest keep their first-pass label.
 #include "label_common.cuh"
 #include "triage.cuh"
 
 namespace msc {
-
-// ---- combinatorial labels --------------------------------------------------------------------
-
-// Steepest discrete step over the 26 neighbours: the largest value drop per unit
-// distance among the neighbours that come before v in the vertex order (after it,
-// uphill), first in position order on ties.  Every step moves strictly along the
-// order, so the chains are acyclic and end at an extremum or a terminal vertex.
-__global__ void comb_succ_kernel(const float* __restrict__ f, const int32_t* __restrict__ lab, const VolDims V, int dir,
-                                 int32_t* __restrict__ succ) {
-  const int64_t N = V.X * V.Y * V.Z;
-  const float inv_d[4] = {0.f, 1.f, 0.70710678f, 0.57735027f};
-  for (int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v < N; v += (int64_t)gridDim.x * blockDim.x) {
-    if (lab[v] >= 0) {
-      succ[v] = (int32_t)v;
-      continue;
-    }
-    const int64_t x = v % V.X, y = (v / V.X) % V.Y, z = v / (V.X * V.Y);
-    const float fv = f[v];
-    int64_t best = v;
-    float best_slope = -1.f;
-    for (int dz = -1; dz <= 1; dz++) {
-      if (z + dz < 0 || z + dz >= V.Z) continue;
-      for (int dy = -1; dy <= 1; dy++) {
-        if (y + dy < 0 || y + dy >= V.Y) continue;
-        for (int dx = -1; dx <= 1; dx++) {
-          if ((dx | dy | dz) == 0 || x + dx < 0 || x + dx >= V.X) continue;
-          const int64_t u = v + dx + V.X * (dy + V.Y * dz);
-          if (dir < 0 ? !vgreater(f, v, u) : !vgreater(f, u, v)) continue;  // not on the way
-          const float slope = (dir < 0 ? fv - f[u] : f[u] - fv) * inv_d[(dx != 0) + (dy != 0) + (dz != 0)];
-          if (slope > best_slope) {
-            best_slope = slope;
-            best = u;
-          }
-        }
-      }
-    }
-    succ[v] = (int32_t)best;
-  }
-}
-
-__global__ void comb_jump_kernel(int32_t* __restrict__ succ, int64_t N, int* __restrict__ changed) {
-  bool any = false;
-  for (int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v < N; v += (int64_t)gridDim.x * blockDim.x) {
-    const int32_t s = succ[v];
-    const int32_t ss = succ[s];
-    if (ss != s) {
-      succ[v] = ss;
-      any = true;
-    }
-  }
-  if (__syncthreads_or(any) && threadIdx.x == 0) atomicOr(changed, 1);
-}
-
-__global__ void comb_label_kernel(const int32_t* __restrict__ succ, const int32_t* __restrict__ lab, int64_t N,
-                                  int32_t* __restrict__ comb) {
-  for (int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v < N; v += (int64_t)gridDim.x * blockDim.x) {
-    const int32_t l = lab[succ[v]];
-    comb[v] = l >= 0 ? l : kLabelNone;
-  }
-}
 
 // ---- features --------------------------------------------------------------------------------
 
@@ -130,33 +70,65 @@ __device__ __forceinline__ bool label_boundary(const int32_t* lab, const VolDims
   return d;
 }
 
-// Row-planar BF16 features: f standardised, |grad f| over its mean (clipped), the
-// combinatorial label boundary and the certain-terminal indicator of each direction.
+// Row-planar BF16 features of one direction from its first-pass labels:
+//   0  f standardised and signed so that the flow runs downhill in both directions
+//   1  |grad f| over its mean (clipped)
+//   2-4  the unit flow direction (-grad f / |grad f| for the ascending labels, +grad f
+//        / |grad f| for the descending ones)
+//   5  a 6-neighbour has another first-pass label
+//   6  the certain-terminal indicator
+//   7  the "reached no region" indicator
+//   8  the fraction of differently labelled 6-neighbours
+//   9  the vertex nearest to one voxel downstream has another first-pass label
 __global__ void features_kernel(const float* __restrict__ f, const float4* __restrict__ g,
-                                const int32_t* __restrict__ comb_asc, const int32_t* __restrict__ comb_dsc,
-                                const uint8_t* __restrict__ st_asc, const uint8_t* __restrict__ st_dsc, const VolDims V,
-                                const double* __restrict__ sums, __nv_bfloat16* __restrict__ out) {
+                                const int32_t* __restrict__ lab, const uint8_t* __restrict__ state, const VolDims V,
+                                int dir, const double* __restrict__ sums, __nv_bfloat16* __restrict__ out) {
   const int64_t N = V.X * V.Y * V.Z;
   const double mean = sums[0] / (double)N;
   const double var = sums[1] / (double)N - mean * mean;
-  const float inv_std = var > 0 ? (float)(1.0 / sqrt(var)) : 1.f;
+  const float inv_std = (var > 0 ? (float)(1.0 / sqrt(var)) : 1.f) * (dir < 0 ? 1.f : -1.f);
   const float inv_g = sums[2] > 0 ? (float)((double)N / sums[2]) : 1.f;
+  const float flow = dir < 0 ? -1.f : 1.f;
   for (int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v < N; v += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t x = v % V.X, row = v / V.X;
+    const int64_t x = v % V.X, y = (v / V.X) % V.Y, z = v / (V.X * V.Y), row = v / V.X;
     const float4 gv = g[v];
-    float c[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-    c[0] = (f[v] - (float)mean) * inv_std;
-    c[1] = fminf(sqrtf(gv.x * gv.x + gv.y * gv.y + gv.z * gv.z) * inv_g, 16.f);
-    c[2] = label_boundary(comb_asc, V, v) ? 1.f : 0.f;
-    c[3] = label_boundary(comb_dsc, V, v) ? 1.f : 0.f;
-    c[4] = (st_asc[v] == kStSeed || st_asc[v] == kStTerminal) ? 1.f : 0.f;
-    c[5] = (st_dsc[v] == kStSeed || st_dsc[v] == kStTerminal) ? 1.f : 0.f;
-    __align__(16) __nv_bfloat16 h[8];
+    const int32_t l = lab[v];
+    int diff = 0, nn = 0;
+    const int64_t nbr[6] = {x < V.X - 1 ? v + 1 : -1, x > 0 ? v - 1 : -1, y < V.Y - 1 ? v + V.X : -1,
+                            y > 0 ? v - V.X : -1, z < V.Z - 1 ? v + V.X * V.Y : -1, z > 0 ? v - V.X * V.Y : -1};
 #pragma unroll
-    for (int k = 0; k < 8; k++) h[k] = __float2bfloat16_rn(c[k]);
+    for (int j = 0; j < 6; j++) {
+      if (nbr[j] < 0) continue;
+      nn++;
+      diff += lab[nbr[j]] != l;
+    }
+    const float gm = sqrtf(gv.x * gv.x + gv.y * gv.y + gv.z * gv.z);
+    const float inv_gm = gm > 0.f ? flow / gm : 0.f;
+    const float ux = gv.x * inv_gm, uy = gv.y * inv_gm, uz = gv.z * inv_gm;
+    auto clampi = [](float p, int64_t n) {
+      int64_t q = (int64_t)floorf(p + 0.5f);
+      return q < 0 ? (int64_t)0 : (q >= n ? n - 1 : q);
+    };
+    const int64_t d = clampi((float)x + ux, V.X) + V.X * (clampi((float)y + uy, V.Y) + V.Y * clampi((float)z + uz, V.Z));
+    float c[16];
+#pragma unroll
+    for (int k = 0; k < 16; k++) c[k] = 0.f;
+    c[0] = (f[v] - (float)mean) * inv_std;
+    c[1] = fminf(gm * inv_g, 16.f);
+    c[2] = ux;
+    c[3] = uy;
+    c[4] = uz;
+    c[5] = diff > 0 ? 1.f : 0.f;
+    c[6] = (state[v] == kStSeed || state[v] == kStTerminal) ? 1.f : 0.f;
+    c[7] = l == kLabelNone ? 1.f : 0.f;
+    c[8] = nn > 0 ? (float)diff / (float)nn : 0.f;
+    c[9] = lab[d] != l ? 1.f : 0.f;
+    __align__(16) __nv_bfloat16 h[16];
+#pragma unroll
+    for (int k = 0; k < 16; k++) h[k] = __float2bfloat16_rn(c[k]);
     __nv_bfloat16* o = out + row * 2 * V.X * 8;
-    *reinterpret_cast<uint4*>(o + x * 8) = *reinterpret_cast<const uint4*>(h);
-    *reinterpret_cast<uint4*>(o + (V.X + x) * 8) = make_uint4(0, 0, 0, 0);
+    *reinterpret_cast<uint4*>(o + x * 8) = *reinterpret_cast<const uint4*>(&h[0]);
+    *reinterpret_cast<uint4*>(o + (V.X + x) * 8) = *reinterpret_cast<const uint4*>(&h[8]);
   }
 }
 
@@ -170,13 +142,12 @@ __device__ __forceinline__ uint64_t mix64(uint64_t z) {
   return z ^ (z >> 31);
 }
 
-// For one direction: unflagged, unaudited non-terminal vertices take their
-// combinatorial label and leave the integration; the rest stay to be integrated.
+// For one direction: unflagged, unaudited vertices still open to the fix-up keep
+// their first-pass label and leave the fix-up (state assigned); the rest stay open.
 // flags: bit 0 = flagged by the network, bit 1 = audit sample.
-__global__ void triage_apply_kernel(const float* __restrict__ logits, float logit_threshold,
-                                    const int32_t* __restrict__ comb, int32_t* __restrict__ lab,
-                                    uint8_t* __restrict__ state, uint8_t* __restrict__ flags, int64_t N,
-                                    uint32_t audit_q32, uint64_t audit_seed, unsigned long long* __restrict__ counts) {
+__global__ void triage_apply_kernel(const float* __restrict__ logits, float logit_threshold, uint8_t* __restrict__ state,
+                                    uint8_t* __restrict__ flags, int64_t N, uint32_t audit_q32, uint64_t audit_seed,
+                                    unsigned long long* __restrict__ counts) {
   unsigned long long nf = 0, na = 0;
   for (int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v < N; v += (int64_t)gridDim.x * blockDim.x) {
     uint8_t fl = 0;
@@ -186,10 +157,7 @@ __global__ void triage_apply_kernel(const float* __restrict__ logits, float logi
       fl = (flagged ? 1 : 0) | (audit ? 2 : 0);
       nf += flagged;
       na += audit;
-      if (!fl) {
-        lab[v] = comb[v];
-        state[v] = kStAssigned;
-      }
+      if (!fl) state[v] = kStAssigned;
     }
     flags[v] = fl;
   }
@@ -203,14 +171,24 @@ __global__ void triage_apply_kernel(const float* __restrict__ logits, float logi
   }
 }
 
-// audit result: sampled vertices whose integrated label differs from the combinatorial one
-__global__ void audit_count_kernel(const int32_t* __restrict__ lab, const int32_t* __restrict__ comb,
+// audit result: sampled (unflagged) vertices whose label the fix-up changed
+__global__ void audit_count_kernel(const int32_t* __restrict__ lab, const int32_t* __restrict__ first,
                                    const uint8_t* __restrict__ flags, int64_t N, unsigned long long* __restrict__ count) {
   unsigned long long n = 0;
   for (int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v < N; v += (int64_t)gridDim.x * blockDim.x)
-    n += (flags[v] == 2 && lab[v] != comb[v]);
+    n += (flags[v] == 2 && lab[v] != first[v]);
   for (int o = 16; o; o >>= 1) n += __shfl_xor_sync(0xffffffffu, n, o);
   if ((threadIdx.x & 31) == 0) atomicAdd(count, n);
+}
+
+// training targets: 1 where the fix-up changed the first-pass label (both output rows)
+__global__ void change_targets_kernel(const int32_t* __restrict__ lab, const int32_t* __restrict__ first, int64_t N,
+                                      uint8_t* __restrict__ targets) {
+  for (int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v < N; v += (int64_t)gridDim.x * blockDim.x) {
+    const uint8_t y = lab[v] != first[v];
+    targets[v] = y;
+    targets[N + v] = y;
+  }
 }
 
 // ---- weights ---------------------------------------------------------------------------------
@@ -368,48 +346,34 @@ __global__ void adam_kernel(float* __restrict__ p, const float* __restrict__ g, 
 
 // ---- launchers -------------------------------------------------------------------------------
 
-cudaError_t launch_comb_labels(const float* f, const int32_t* lab, const VolDims& V, int dir, int32_t* succ,
-                               int32_t* comb, int* changed, int num_sms, cudaStream_t st) {
-  const int64_t N = V.X * V.Y * V.Z;
-  const int grid = num_sms * 8;
-  comb_succ_kernel<<<grid, 256, 0, st>>>(f, lab, V, dir, succ);
-  for (int round = 0; round < 64; round++) {
-    cudaError_t e = cudaMemsetAsync(changed, 0, sizeof(int), st);
-    if (e != cudaSuccess) return e;
-    comb_jump_kernel<<<grid, 256, 0, st>>>(succ, N, changed);
-    int h = 0;
-    e = cudaMemcpyAsync(&h, changed, sizeof(int), cudaMemcpyDeviceToHost, st);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
-    if (e != cudaSuccess) return e;
-    if (!h) break;
-  }
-  comb_label_kernel<<<grid, 256, 0, st>>>(succ, lab, N, comb);
-  return cudaGetLastError();
-}
-
-cudaError_t launch_features(const float* f, const float4* g, const int32_t* comb_asc, const int32_t* comb_dsc,
-                            const uint8_t* st_asc, const uint8_t* st_dsc, const VolDims& V, double* sums,
-                            __nv_bfloat16* out, int num_sms, cudaStream_t st) {
+cudaError_t launch_features(const float* f, const float4* g, const int32_t* lab, const uint8_t* state, const VolDims& V,
+                            int dir, double* sums, __nv_bfloat16* out, int num_sms, cudaStream_t st) {
   const int64_t N = V.X * V.Y * V.Z;
   cudaError_t e = cudaMemsetAsync(sums, 0, 3 * sizeof(double), st);
   if (e != cudaSuccess) return e;
   feature_stats_kernel<<<num_sms * 4, 256, 0, st>>>(f, g, N, sums);
-  features_kernel<<<num_sms * 8, 256, 0, st>>>(f, g, comb_asc, comb_dsc, st_asc, st_dsc, V, sums, out);
+  features_kernel<<<num_sms * 8, 256, 0, st>>>(f, g, lab, state, V, dir, sums, out);
   return cudaGetLastError();
 }
 
-cudaError_t launch_triage_apply(const float* logits, float logit_threshold, const int32_t* comb, int32_t* lab,
-                                uint8_t* state, uint8_t* flags, int64_t N, float audit_frac, uint64_t audit_seed,
-                                unsigned long long* counts, int num_sms, cudaStream_t st) {
+cudaError_t launch_triage_apply(const float* logits, float logit_threshold, uint8_t* state, uint8_t* flags, int64_t N,
+                                float audit_frac, uint64_t audit_seed, unsigned long long* counts, int num_sms,
+                                cudaStream_t st) {
   const double q = audit_frac <= 0.f ? 0.0 : (audit_frac >= 1.f ? 4294967295.0 : (double)audit_frac * 4294967296.0);
-  triage_apply_kernel<<<num_sms * 8, 256, 0, st>>>(logits, logit_threshold, comb, lab, state, flags, N, (uint32_t)q,
-                                                   audit_seed, counts);
+  triage_apply_kernel<<<num_sms * 8, 256, 0, st>>>(logits, logit_threshold, state, flags, N, (uint32_t)q, audit_seed,
+                                                   counts);
   return cudaGetLastError();
 }
 
-cudaError_t launch_audit_count(const int32_t* lab, const int32_t* comb, const uint8_t* flags, int64_t N,
+cudaError_t launch_audit_count(const int32_t* lab, const int32_t* first, const uint8_t* flags, int64_t N,
                                unsigned long long* count, int num_sms, cudaStream_t st) {
-  audit_count_kernel<<<num_sms * 8, 256, 0, st>>>(lab, comb, flags, N, count);
+  audit_count_kernel<<<num_sms * 8, 256, 0, st>>>(lab, first, flags, N, count);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_change_targets(const int32_t* lab, const int32_t* first, int64_t N, uint8_t* targets, int num_sms,
+                                  cudaStream_t st) {
+  change_targets_kernel<<<num_sms * 8, 256, 0, st>>>(lab, first, N, targets);
   return cudaGetLastError();
 }
 

@@ -3,13 +3,14 @@
     python -m msceer_gb300.train_triage [--fields 200] [--size 128] [--eval-size 512]
 
 Training data: k^-3 Gaussian random fields (seeds 1000.., `--size`^3 vertices); for
-each, the plain full integration gives the integrated labels and the network inputs
-give the combinatorial ones; the target is where they differ.  The last tenth of the
-fields is held out to pick the decision thresholds (the largest logit thresholds that
-leave at most `--miss` of all vertices wrongly unflagged).  The trained weights and
-thresholds go to msceer_gb300/data/triage_cnn.npz; an evaluation on a held-out field
-(seed 0, `--eval-size`^3) reports the time of both labelings and their mismatch.
-Everything runs on the library's CUDA kernels.
+each field and direction the library runs the first pass, records the network
+features, then runs the full boundary fix-up and records where it changed the
+first-pass label (the target).  The last tenth of the fields is held out to pick the
+decision thresholds (per direction, the largest logit threshold that leaves at most
+`--miss` of all vertices wrongly unflagged).  The trained weights and thresholds go to
+msceer_gb300/data/triage_cnn.npz; an evaluation on a held-out field (seed 0,
+`--eval-size`^3) reports the time of the plain and the triaged labeling and their
+mismatch.  Everything runs on the library's CUDA kernels.
 """
 from __future__ import annotations
 
@@ -20,15 +21,14 @@ import time
 import numpy as np
 
 
-def make_sample(n, seed, integ):
+def make_samples(n, seed, integ):
+    """(ascending sample, descending sample) of one field: (features, targets, shape)."""
     import torch
-    from . import fields, integrated_labels, lower_star_grad, triage
+    from . import fields, lower_star_grad, triage
     f = torch.from_numpy(fields.power_law_field((n, n, n), seed=seed)).cuda()
     g = lower_star_grad(f)
-    plain = integrated_labels(f, g, **integ)
-    feat, comb = triage.features(f, g, **integ)
-    tgt = triage.targets_from(plain["asc"], plain["dsc"], comb)
-    return feat, tgt.contiguous(), (n, n, n)
+    feat, tgt = triage.features(f, g, **integ)
+    return [(feat[k].contiguous(), tgt[k].contiguous(), (n, n, n)) for k in range(2)]
 
 
 def main(argv=None):
@@ -49,12 +49,13 @@ def main(argv=None):
     log = lambda m: print(m, flush=True)  # noqa: E731
 
     t0 = time.perf_counter()
-    samples = [make_sample(a.size, 1000 + i, integ) for i in range(a.fields)]
+    per_field = [make_samples(a.size, 1000 + i, integ) for i in range(a.fields)]
     n_val = max(1, a.fields // 10)
-    train_set, val_set = samples[:-n_val], samples[-n_val:]
-    pos = [float(t.float().mean()) for _, t, _ in samples]
+    train_set = [s for fs in per_field[:-n_val] for s in fs]
+    val_by_dir = [[fs[k] for fs in per_field[-n_val:]] for k in range(2)]
+    pos = [float(t[0].float().mean()) for fs in per_field for _, t, _ in fs]
     log(f"generated {a.fields} fields of {a.size}^3 in {time.perf_counter() - t0:.1f} s; "
-        f"positive fraction {np.mean(pos):.4f}")
+        f"fraction the fix-up changes {np.mean(pos):.4f}")
 
     t1 = time.perf_counter()
     steps = max(1, int(a.epochs * len(train_set)))
@@ -62,15 +63,8 @@ def main(argv=None):
     torch.cuda.synchronize()
     log(f"trained {steps} steps in {time.perf_counter() - t1:.1f} s; loss {hist[0]:.4f} -> {hist[-1]:.4f}")
 
-    thr = triage.choose_thresholds(val_set, w, a.miss)
-    flagged = []
-    for k in range(2):
-        nf, nt = 0, 0
-        for feat, tgt, shape in val_set:
-            _, _, logits = triage.forward(feat, shape, w)
-            nf += int((logits[k] > thr[k]).sum().item())
-            nt += logits.shape[1]
-        flagged.append(nf / nt)
+    thr = triage.choose_thresholds(val_by_dir, w, a.miss)
+    flagged = [triage.flagged_fraction(val_by_dir[k], w, thr[k]) for k in range(2)]
     log(f"thresholds {thr}, validation flagged fraction {flagged}")
     net = triage.TriageNet(w, thr[0], thr[1], {"fields": a.fields, "size": a.size, "steps": steps})
     net.save(a.out)

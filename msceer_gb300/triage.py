@@ -1,12 +1,14 @@
 """Learned triage for the integrated labels (include/msc_triage.h).
 
-A three-layer 3x3x3 network (6 -> 16 -> 16 -> 2 channels, BF16 on the tensor cores)
-flags the vertices whose integrated destination differs from their combinatorial
-steepest-path destination; only those (plus a random audit sample) are integrated.
-Everything here drives the library's own CUDA kernels through the C ABI: feature
-extraction, forward and backward passes, the Adam step and the triaged labeling.
-The plain full integration (:func:`msceer_gb300.integrated_labels`) generates the
-training labels and stays the judge of the triage's mismatch.
+The labeling's first pass (FP32 streamlines with path compression) is cheap; the
+boundary fix-up that re-decides every vertex next to a label boundary takes about
+nine tenths of the time and changes about one first-pass label in ten.  A three-layer
+3x3x3 network (10 -> 16 -> 16 -> 2 channels, BF16 on the tensor cores) predicts which
+first-pass labels the fix-up would change; only those vertices (plus a random audit
+sample) are re-decided.  Everything here drives the library's own CUDA kernels through
+the C ABI: feature extraction, forward and backward passes, the Adam step and the
+triaged labeling.  The plain full integration (:func:`msceer_gb300.integrated_labels`)
+is the drop-in and the judge of the triage's mismatch.
 """
 from __future__ import annotations
 
@@ -21,7 +23,7 @@ from . import _lib
 
 PARAMS = 3 * 27 * 16 * 16 + 3 * 16
 NW = 27 * 16 * 16
-CIN, COUT = 6, 2
+CIN, COUT = 10, 2
 WEIGHTS_FILE = Path(__file__).resolve().parent / "data" / "triage_cnn.npz"
 
 
@@ -73,22 +75,24 @@ def init_weights(seed: int = 0):
     return torch.from_numpy(p).cuda()
 
 
-def features(f, grad, error_threshold=1e-4, gradient_threshold=None, iteration_limit=4000, max_step=0.25,
-             presimp_threshold=0.0):
-    """Network inputs of a device volume: (features uint16 row-planar [N*16], comb int32 [2, N])."""
+def features(f, grad, targets=True, error_threshold=1e-4, gradient_threshold=None, iteration_limit=4000,
+             max_step=0.25, presimp_threshold=0.0):
+    """Per direction (ascending, descending): the network features after the first pass
+    (int16 [2, 16 N], row-planar BF16) and, with `targets`, where the full fix-up changes
+    the first-pass label (uint8 [2, 2, N])."""
     import torch
     f = f.contiguous()
     if gradient_threshold is None:
         gradient_threshold = 1e-6 * float(f.abs().max())
     n = f.numel()
-    feat = torch.empty(16 * n, dtype=torch.int16, device=f.device)
-    comb = torch.empty(2 * n, dtype=torch.int32, device=f.device)
+    feat = torch.empty(2, 16 * n, dtype=torch.int16, device=f.device)
+    tgt = torch.empty(2, 2, n, dtype=torch.uint8, device=f.device) if targets else None
     p = _params(error_threshold, gradient_threshold, iteration_limit, max_step, presimp_threshold, 0)
     with torch.cuda.device(f.device):
         rc = _lib.load().msc_triage_features_3d(_ptr(f), _ptr(grad), _dims(f.shape), ctypes.byref(p), _ptr(feat),
-                                                _ptr(comb), _stream(f.device))
+                                                _ptr(tgt), _stream(f.device))
     _check(rc, "msc_triage_features_3d")
-    return feat, comb.view(2, n)
+    return feat, tgt
 
 
 def forward(feat, shape, weights, act1=None, act2=None):
@@ -153,13 +157,6 @@ class TriageNet:
         return cls(w, float(z["threshold_asc"]), float(z["threshold_dsc"]), {"source": str(path)})
 
 
-def targets_from(plain_asc, plain_dsc, comb):
-    """uint8 [2, N]: 1 where the integrated (plain) label differs from the combinatorial one."""
-    import torch
-    t = torch.stack([plain_asc.view(-1) != comb[0], plain_dsc.view(-1) != comb[1]])
-    return t.to(torch.uint8)
-
-
 def train(samples, steps, lr=3e-3, pos_weight=None, seed=0, weights=None, log=None):
     """Adam on a list of (feat, targets, shape) samples held on the device; one sample per
     step, cycling.  Returns the weights and the loss history."""
@@ -183,16 +180,16 @@ def train(samples, steps, lr=3e-3, pos_weight=None, seed=0, weights=None, log=No
     return weights, hist, pos_weight
 
 
-def choose_thresholds(samples, weights, miss_budget):
-    """Per direction, the largest logit threshold whose unflagged positives stay within
-    `miss_budget` (a fraction of all vertices) on the given samples."""
+def choose_thresholds(samples_by_dir, weights, miss_budget):
+    """Per direction, the largest logit threshold (channel 0) whose unflagged positives
+    stay within `miss_budget` (a fraction of all vertices) on the given samples."""
     import torch
     out = []
-    for k in range(2):
+    for samples in samples_by_dir:
         z_pos, total = [], 0
         for feat, tgt, shape in samples:
             _, _, logits = forward(feat, shape, weights)
-            z_pos.append(logits[k][tgt[k] > 0].float())
+            z_pos.append(logits[0][tgt[0] > 0].float())
             total += logits.shape[1]
         zp = torch.sort(torch.cat(z_pos)).values
         allowed = int(miss_budget * total)
@@ -204,6 +201,15 @@ def choose_thresholds(samples, weights, miss_budget):
             # flag logits > thr; positives with logit <= thr are missed
             out.append(float(zp[allowed].item()) - 1e-6 if allowed > 0 else float(zp[0].item()) - 1e-6)
     return out
+
+
+def flagged_fraction(samples, weights, threshold):
+    n, tot = 0, 0
+    for feat, _, shape in samples:
+        _, _, logits = forward(feat, shape, weights)
+        n += int((logits[0] > threshold).sum().item())
+        tot += logits.shape[1]
+    return n / max(tot, 1)
 
 
 def triage_labels(f, grad, net: TriageNet, error_threshold=1e-4, gradient_threshold=None, iteration_limit=4000,
@@ -223,6 +229,6 @@ def triage_labels(f, grad, net: TriageNet, error_threshold=1e-4, gradient_thresh
         rc = _lib.load().msc_triage_labels_3d(_ptr(f), _ptr(grad), _dims(f.shape), ctypes.byref(p), ctypes.byref(tp),
                                               _ptr(asc), _ptr(dsc), stats, _stream(f.device))
     _check(rc, "msc_triage_labels_3d")
-    names = ("flagged", "audited", "audit_mismatch", "redecided")
+    names = ("flagged", "audited", "audit_changed", "redecided")
     st = {f"{d}_{k}": int(stats[4 * i + j]) for i, d in enumerate(("asc", "dsc")) for j, k in enumerate(names)}
     return {"asc": asc, "dsc": dsc, "stats": st}

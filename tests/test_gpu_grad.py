@@ -210,3 +210,16 @@ def test_ascending_manifold_dims_idempotent(gpu, oracle):
     g = torch.from_numpy(want.copy()).to(gpu)
     ascending_manifold_dims(g, f.shape[::-1])
     assert np.array_equal(g.cpu().numpy(), want)
+
+
+def test_batch_of_uneven_volumes_equals_single_calls(gpu):
+    """msc_lower_star_grad_batch_3d: volumes of different shapes in shared launches give
+    the same bytes as one call per volume."""
+    import torch
+    from msceer_gb300 import lower_star_grad, lower_star_grad_batch
+    rng = np.random.default_rng(21)
+    shapes = [tuple(int(v) for v in rng.integers(3, 70, size=3)) for _ in range(9)] + [(2, 2, 2), (1, 5, 7)]
+    vols = [torch.from_numpy(fields.power_law_field(s, seed=i)).to(gpu) for i, s in enumerate(shapes)]
+    got = lower_star_grad_batch(vols)
+    for v, g in zip(vols, got):
+        assert torch.equal(g, lower_star_grad(v))

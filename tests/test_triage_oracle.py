@@ -12,10 +12,10 @@ import triage_oracle as T  # noqa: E402
 def small_problem(seed=0, shape=(5, 6, 7)):
     rng = np.random.default_rng(seed)
     feat = np.zeros(shape + (16,), dtype=np.float64)
-    feat[..., :6] = rng.normal(size=shape + (6,))
+    feat[..., :10] = rng.normal(size=shape + (10,))
     p = rng.normal(scale=0.2, size=T.NPARAMS)
     W, b = T.unpack(p.astype(np.float32))
-    p[: T.NW].reshape(27, 16, 16)[:, 6:, :] = 0            # layer 1: 6 real inputs
+    p[: T.NW].reshape(27, 16, 16)[:, 10:, :] = 0           # layer 1: 10 real inputs
     p[2 * T.NW: 3 * T.NW].reshape(27, 16, 16)[:, :, 2:] = 0  # layer 3: 2 real outputs
     p[3 * T.NW + 34:] = 0
     y = (rng.random((2,) + shape) < 0.2).astype(np.uint8)
