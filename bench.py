@@ -62,6 +62,7 @@ def parse_args():
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-triage", action="store_true", help="time the plain full integration as the step")
     p.add_argument("--grad-only", action="store_true", help="time the .grad alone as the step")
+    p.add_argument("--no-batch", action="store_true", help="skip the 64-volume batching measurement")
     return p.parse_args()
 
 
@@ -280,29 +281,18 @@ def run_ours(args, ws, rank, local):
         gpu_id = "GPU-" + str(torch.cuda.get_device_properties(dev).uuid)
     except Exception:
         gpu_id = None
-    launches = 0
     with ClockSampler(gpu_id) as clk:
         barrier()
         e0, e1 = _events(2)
+        l0 = lib.msc_kernel_launches()
         e0.record(stream)
         for _ in range(args.steps):
             res = step()
-            launches += 1 + lib.msc_last_ldir_passes()
         e1.record(stream)
         barrier()
+        launches = lib.msc_kernel_launches() - l0
     ms = e0.elapsed_time(e1) / args.steps
     clocks = clk.summary()
-    # launches of the library's kernels in one step, counted outside the timed region
-    try:
-        from torch.profiler import ProfilerActivity, profile
-        with profile(activities=[ProfilerActivity.CUDA]) as prof:
-            step()
-            torch.cuda.synchronize(dev)
-        per_step = sum(e.count for e in prof.key_averages() if "msc" in e.key or "ldir" in e.key or "lstar" in e.key)
-        if per_step > 0:
-            launches = per_step * args.steps
-    except Exception:
-        pass
     if pg is not None:
         t = torch.tensor([ms], device=dev)
         pg.all_reduce(t, op=pg.ReduceOp.MAX)
@@ -388,6 +378,34 @@ def run_ours(args, ws, rank, local):
         t_e2e = float(t.item())
     e2e = ws * V / t_e2e / 1e9
 
+    # batching: 64 volumes with edge lengths log-uniform in [32, 256] per axis (k^-3 fields,
+    # seeds 0..63): the .grad of all of them in shared launches vs one call per volume
+    batch = None
+    if not args.no_batch:
+        from msceer_gb300 import fields, lower_star_grad_batch
+        rng = np.random.default_rng(0)
+        shapes = [tuple(int(round(np.exp(rng.uniform(np.log(32), np.log(256))))) for _ in range(3)) for _ in range(64)]
+        vols = [torch.from_numpy(fields.power_law_field(sh, seed=i)).to(dev) for i, sh in enumerate(shapes)]
+        nvb = sum(int(np.prod(sh)) for sh in shapes)
+        outs = lower_star_grad_batch(vols)
+        singles = [lower_star_grad(v) for v in vols]
+        same = all(torch.equal(a, b) for a, b in zip(outs, singles))
+        b0, b1, b2 = _events(3)
+        b0.record(stream)
+        for _ in range(3):
+            lower_star_grad_batch(vols, outs)
+        b1.record(stream)
+        for _ in range(3):
+            for v, o in zip(vols, singles):
+                lower_star_grad(v, out=o)
+        b2.record(stream)
+        torch.cuda.synchronize(dev)
+        tb, tl = b0.elapsed_time(b1) / 3, b1.elapsed_time(b2) / 3
+        batch = {"workload": "64 k^-3 volumes, edges log-uniform in [32, 256], seeds 0..63, .grad",
+                 "vertices": nvb, "batched": {"value": nvb / (tb * 1e-3) / 1e9, "unit": UNIT, "ms": tb},
+                 "looped": {"value": nvb / (tl * 1e-3) / 1e9, "unit": UNIT, "ms": tl}, "bit_identical": same}
+        del vols, outs, singles
+
     peak, peak_kind = load_peaks()
     alg_pairs = 4 * V + C            # read f once, write every .grad byte once
     alg_ldir = 2 * C                 # the ascending-manifold stage reads and writes the .grad
@@ -424,6 +442,8 @@ def run_ours(args, ws, rank, local):
                 "gpu_launches": launches,
                 "clocks": clocks}
         line.update(line_extra)
+        if batch is not None:
+            line["batch"] = batch
         if ws == 1 and not args.no_cpu_baseline:
             line["cpu_baseline"] = cpu_baseline(f_np, grad_only=args.grad_only)
         print(json.dumps(line), flush=True)

@@ -53,6 +53,10 @@ const char* msc_last_error_string(void);
  * launch per round of frontier walks). */
 int msc_last_ldir_passes(void);
 
+/* Number of the library's kernel launches so far in this process, all threads (a
+ * diagnostic for profiling and benchmarks). */
+int64_t msc_kernel_launches(void);
+
 /* Number of cells (= .grad bytes) of the complex: TopologicalRegularGrid3D::numCells
  * (gi_topological_regular_grid.h:1254).  Returns -1 for invalid dims. */
 int64_t msc_num_cells_3d(const int64_t dims[3]);

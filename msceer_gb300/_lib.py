@@ -42,6 +42,7 @@ SIGNATURES = {
     "msc_integrated_labels_3d": (ctypes.c_int, [_VP, _VP, _I64P, _VP, _VP, _VP, _VP]),
     "msc_integrated_labels_3d_stages": (ctypes.c_int, [_VP, _VP, _I64P, _VP, _VP, _VP, _VP, _VP]),
     "msc_lower_star_grad_batch_3d": (ctypes.c_int, [ctypes.c_int, _VP, _I64P, _VP, _VP]),
+    "msc_kernel_launches": (ctypes.c_int64, []),
     "msc_labels_last_error_string": (ctypes.c_char_p, []),
     "msc_labels_last_stats": (None, [_I64P]),
     "msc_triage_last_error_string": (ctypes.c_char_p, []),

@@ -75,7 +75,7 @@ cudaError_t launch_central_diff(int nd, int layout, const float* f, void* out, c
   const int grid = (int)(blocks < cap ? blocks : cap);
   if (grid <= 0) return cudaSuccess;
   const int64_t X = D.v[0], Y = D.v[1], Z = D.v[2];
-#define MSC_LAUNCH(ND_, L_) central_diff_kernel<ND_, L_><<<grid, 256, 0, stream>>>(f, out, X, Y, Z)
+#define MSC_LAUNCH(ND_, L_) (count_launch(), central_diff_kernel<ND_, L_><<<grid, 256, 0, stream>>>(f, out, X, Y, Z))
   if (nd == 3) {
     if (layout == 0) MSC_LAUNCH(3, 0);
     else if (layout == 1) MSC_LAUNCH(3, 1);

@@ -584,6 +584,7 @@ __global__ void clean_resolve_kernel(const int32_t* __restrict__ lab, const VolD
 cudaError_t launch_integrate_pass1(const float4* G, const VolDims& V, const IntegParams& P, const SpreadOrder& S,
                                    int32_t* lab, uint8_t* lvl, int num_sms, cudaStream_t stream) {
   const int64_t N = V.X * V.Y * V.Z;
+  ::msc::count_launch();
   init_levels_kernel<<<num_sms * 8, 256, 0, stream>>>(lab, lvl, N);
   for (int L = 0; L < S.nlev; L++) {
     const int64_t count = S.offset[L + 1] - S.offset[L];
@@ -591,6 +592,7 @@ cudaError_t launch_integrate_pass1(const float4* G, const VolDims& V, const Inte
     Adv32 A{G, V, P, lab, lvl, L + 1, nullptr};
     const int64_t blocks = (count + 127) / 128;
     const int grid = (int)(blocks < num_sms * 16 ? blocks : num_sms * 16);
+    ::msc::count_launch();
     integrate_level_kernel<<<grid, 128, 0, stream>>>(A, S.start[L], S.stride[L], count, lab, lvl);
   }
   return cudaGetLastError();
@@ -598,6 +600,7 @@ cudaError_t launch_integrate_pass1(const float4* G, const VolDims& V, const Inte
 
 cudaError_t launch_boundary_set(const int32_t* lab, const uint8_t* state, const VolDims& V, int64_t* list, int* n,
                                 uint32_t* queued, int num_sms, cudaStream_t stream) {
+  ::msc::count_launch();
   boundary_set_kernel<<<num_sms * 8, 256, 0, stream>>>(lab, state, V, list, n, queued);
   return cudaGetLastError();
 }
@@ -608,6 +611,7 @@ cudaError_t launch_fixup(const double* G, const VolDims& V, const IntegParams& P
   if (n <= 0) return cudaSuccess;
   Adv64 A{G, V, P, state};
   const int blocks = (n + 127) / 128;
+  ::msc::count_launch();
   fixup_kernel<<<blocks < num_sms * 16 ? blocks : num_sms * 16, 128, 0, stream>>>(A, lab, lab0, state, list, n, next,
                                                                                   n_next, queued);
   return cudaGetLastError();
@@ -619,6 +623,7 @@ cudaError_t launch_fixup32(const float4* G, const VolDims& V, const IntegParams&
   if (n <= 0) return cudaSuccess;
   Adv32 A{G, V, P, lab, nullptr, 0, state};
   const int blocks = (n + 127) / 128;
+  ::msc::count_launch();
   fixup32_kernel<<<blocks < num_sms * 16 ? blocks : num_sms * 16, 128, 0, stream>>>(A, lab, lab0, state, list, n, next,
                                                                                     n_next, queued, amb, n_amb,
                                                                                     amb_mode);
@@ -629,11 +634,16 @@ cudaError_t launch_clean(const int32_t* lab, const float* f, const VolDims& V, i
                          int32_t* out, int num_sms, cudaStream_t stream) {
   const int64_t N = V.X * V.Y * V.Z;
   const int grid = num_sms * 8;
+  ::msc::count_launch();
   uf_init_kernel<<<grid, 256, 0, stream>>>(parent, N);
+  ::msc::count_launch();
   uf_hook_kernel<<<grid, 256, 0, stream>>>(lab, f, V, dir, parent);
   // roots into `target`; from there on `target` holds the roots and `parent` the merge targets
+  ::msc::count_launch();
   uf_roots_kernel<<<grid, 256, 0, stream>>>(parent, target, N);
+  ::msc::count_launch();
   clean_target_kernel<<<grid, 256, 0, stream>>>(lab, f, V, dir, target, parent);
+  ::msc::count_launch();
   clean_resolve_kernel<<<grid, 256, 0, stream>>>(lab, V, target, parent, out);
   return cudaGetLastError();
 }

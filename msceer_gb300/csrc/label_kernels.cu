@@ -379,6 +379,7 @@ cudaError_t launch_terminal_pass(const float* f, int32_t* lab, const VolDims& V,
   const size_t sm = VB::smem_bytes() + 16;
   cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
   if (e != cudaSuccess) return e;
+  ::msc::count_launch();
   k<<<grid, kVBS, sm, stream>>>(f, lab, V, dir, dirty_in, dirty_out, changed, err);
   return cudaGetLastError();
 }
@@ -386,6 +387,7 @@ cudaError_t launch_terminal_pass(const float* f, int32_t* lab, const VolDims& V,
 cudaError_t launch_find_critical(const uint8_t* g, const VolDims& V, int dir, int32_t* ext_id_of_key,
                                  int64_t* ext_cells, int* n_ext, int64_t* saddles, int* n_sad, int num_sms,
                                  cudaStream_t stream) {
+  ::msc::count_launch();
   find_critical_kernel<<<num_sms * 8, 256, 0, stream>>>(g, V, dir, ext_id_of_key, ext_cells, n_ext, saddles, n_sad);
   return cudaGetLastError();
 }
@@ -395,6 +397,7 @@ cudaError_t launch_trace_arcs(const uint8_t* g, const float* f, const VolDims& V
                               int* err, int num_sms, cudaStream_t stream) {
   if (n_sad <= 0) return cudaSuccess;
   const int blocks = (n_sad + 255) / 256;
+  ::msc::count_launch();
   trace_arcs_kernel<<<blocks < num_sms * 8 ? blocks : num_sms * 8, 256, 0, stream>>>(
       g, f, V, dir, saddles, n_sad, ext_id_of_key, threshold, arcs, n_arcs, err);
   return cudaGetLastError();
@@ -404,6 +407,7 @@ cudaError_t launch_extremum_info(const float* f, const VolDims& V, int dir, cons
                                  int64_t* hv, float* fval, int64_t* seed, int num_sms, cudaStream_t stream) {
   if (n_ext <= 0) return cudaSuccess;
   const int blocks = (n_ext + 255) / 256;
+  ::msc::count_launch();
   extremum_info_kernel<<<blocks < num_sms * 8 ? blocks : num_sms * 8, 256, 0, stream>>>(f, V, dir, ext_cells, n_ext,
                                                                                          hv, fval, seed);
   return cudaGetLastError();
@@ -414,7 +418,9 @@ cudaError_t launch_group_seeds(const int32_t* rep, const int64_t* seed, int n_ex
   if (n_ext <= 0) return cudaSuccess;
   const int blocks = (n_ext + 255) / 256;
   const int grid = blocks < num_sms * 8 ? blocks : num_sms * 8;
+  ::msc::count_launch();
   group_name_kernel<<<grid, 256, 0, stream>>>(rep, seed, n_ext, name);
+  ::msc::count_launch();
   place_seeds_kernel<<<grid, 256, 0, stream>>>(rep, seed, n_ext, name, lab, state);
   return cudaGetLastError();
 }

@@ -17,9 +17,10 @@
 // with the marked items, runs the value-2 walk to its local fixpoint, then the
 // value-1 walk, and writes back the tile.  Marks in the halo stay local.  Two ways
 // finish the closure across tile borders:
-//   single pass (default)  one tile pass saves every tile's final box; a check kernel
-//       lowers the cells some neighbour's saved halo holds lower and queues the
-//       lowered items; a walk kernel finishes their walks in global memory.
+//   single pass (default)  one tile pass saves the halo cells every tile lowered; a
+//       check kernel lowers those cells in global memory where the owner holds them
+//       higher and queues the lowered items; a walk kernel finishes their walks in
+//       global memory.
 //   multi pass (fallback, and the allocation-free entry)  repeated tile passes; later
 //       passes revisit only tiles whose halo changed (a neighbour wrote a cell within
 //       2 cells of the shared border) and seed only from the halo, because everything
@@ -50,6 +51,43 @@ __device__ __forceinline__ void lcoords(int i, int& lx, int& ly, int& lz) {
   lx = i % T::LX;
   ly = (i / T::LX) % T::LY;
   lz = i / (T::LX * T::LY);
+}
+
+// k-th halo cell of the box -> box index (z slabs, then y rows, then x columns)
+template <class T, int ND>
+__device__ __forceinline__ int halo_cell(int h) {
+  constexpr int H = T::H, LX = T::LX, LY = T::LY, LZ = T::LZ;
+  int lz = 0;
+  if (ND == 3) {
+    constexpr int SLAB = 2 * H * LX * LY;  // z < H and z >= LZ - H
+    if (h < SLAB) {
+      const int s = h / (LX * LY), r = h % (LX * LY);
+      lz = s < H ? s : LZ - 2 * H + s;
+      return r + LX * LY * lz;
+    }
+    h -= SLAB;
+  }
+  constexpr int P = 2 * H * LX + 2 * H * (LY - 2 * H);  // halo cells of one inner plane
+  lz = (ND == 3 ? H : 0) + h / P;
+  int r = h % P;
+  int lx, ly;
+  if (r < 2 * H * LX) {
+    const int s = r / LX;
+    ly = s < H ? s : LY - 2 * H + s;
+    lx = r % LX;
+  } else {
+    r -= 2 * H * LX;
+    const int s = r / (LY - 2 * H);
+    lx = s < H ? s : LX - 2 * H + s;
+    ly = H + r % (LY - 2 * H);
+  }
+  return lx + LX * (ly + LY * lz);
+}
+
+template <class T, int ND>
+__host__ __device__ constexpr int halo_count() {
+  return (ND == 3 ? 2 * T::H * T::LX * T::LY : 0) +
+         (ND == 3 ? (T::LZ - 2 * T::H) : 1) * (2 * T::H * T::LX + 2 * T::H * (T::LY - 2 * T::H));
 }
 
 // Queue append for the lanes of a warp that are converged here: one shared-memory
@@ -390,7 +428,7 @@ struct LdirWalk2 {
     const uint8_t bt = sg[t];
     const unsigned code = (bt >> 2) & 7u;
     if (!(bt & 1u) || code == 7u) return -1;  // unassigned or critical
-    if (r2) m2[t] = 1;
+    if (r2) m2[t] |= 1u;
     else if ((bt >> 5) != 1u) sg[t] = (uint8_t)((bt & 0x1Fu) | (1u << 5));
     const int pc = map3(dec_map, (int)code);
     const int pa = pc >> 1, psg = (pc & 1) ? -1 : 1;
@@ -404,16 +442,16 @@ struct LdirWalk2 {
     if (r2) {
       const int pdim = (lp[0] & 1) + (lp[1] & 1) + (ND == 3 ? (lp[2] & 1) : 0);
       if (pdim != 1) {  // a hex: the value-2 path ends here
-        m2[tp] = 1;
+        m2[tp] |= 1u;
         return -1;
       }
-      if ((bp >> 5) == 2u || m2[tp]) return -1;  // a root, or marked already
+      if ((bp >> 5) == 2u || (m2[tp] & 1u)) return -1;  // a root, or marked already
     } else {
       if ((bp >> 5) == 1u) return -1;
     }
     const uint32_t bit = 1u << (tp & 31);
     if (atomicOr(&vis[tp >> 5], bit) & bit) return -1;
-    if (r2) m2[tp] = 1;
+    if (r2) m2[tp] |= 1u;
     else sg[tp] = (uint8_t)((bp & 0x1Fu) | (1u << 5));
     return tp;
   }
@@ -515,7 +553,7 @@ __global__ void __launch_bounds__(BS) ldir_tile_kernel(const LdirBatch B, uint8_
         int dim = 0;
         if (valid) {
           sg[k] = v[u];
-          m2[k] = 0;
+          m2[k] = (uint8_t)(v[u] & 0xE0u);  // staged ldir above the value-2 mark bit
           const int lx = k % T::LX, row = k / T::LX;
           const int ly = row % T::LY, lz = row / T::LY;
           dim = (lx & 1) + (ly & 1) + (ND == 3 ? (lz & 1) : 0);
@@ -545,7 +583,7 @@ __global__ void __launch_bounds__(BS) ldir_tile_kernel(const LdirBatch B, uint8_
     // fold the value-2 marks into the bytes
     for (int k = tid; k < NL; k += BS) {
       const uint8_t b = sg[k];
-      if (m2[k] && (b >> 5) == 3u) sg[k] = (uint8_t)((b & 0x1Fu) | (2u << 5));
+      if ((m2[k] & 1u) && (b >> 5) == 3u) sg[k] = (uint8_t)((b & 0x1Fu) | (2u << 5));
     }
     __syncthreads();
 
@@ -558,47 +596,16 @@ __global__ void __launch_bounds__(BS) ldir_tile_kernel(const LdirBatch B, uint8_
       if (gx < dX && gy < dY && gz < dZ)
         g[gx + gy * D.cs[1] + gz * D.cs[2]] = sg[(ix + T::H) + T::LX * ((iy + T::H) + T::LY * (iz + (ND == 3 ? T::H : 0)))];
     }
-    uint8_t* sv = saved + flat * (int64_t)NL;
-    for (int k = tid; k < NL; k += BS) sv[k] = sg[k];
+    // save the halo cells this tile lowered (0 for the rest), in halo order
+    constexpr int NH = halo_count<T, ND>();
+    uint8_t* sv = saved + flat * (int64_t)NH;
+    for (int h = tid; h < NH; h += BS) {
+      const int k = halo_cell<T, ND>(h);
+      const uint8_t b = sg[k];
+      sv[h] = ((unsigned)(b >> 5) < (unsigned)(m2[k] >> 5)) ? b : (uint8_t)0;
+    }
     __syncthreads();
   }
-}
-
-// k-th halo cell of the box -> box index (z slabs, then y rows, then x columns)
-template <class T, int ND>
-__device__ __forceinline__ int halo_cell(int h) {
-  constexpr int H = T::H, LX = T::LX, LY = T::LY, LZ = T::LZ;
-  int lz = 0;
-  if (ND == 3) {
-    constexpr int SLAB = 2 * H * LX * LY;  // z < H and z >= LZ - H
-    if (h < SLAB) {
-      const int s = h / (LX * LY), r = h % (LX * LY);
-      lz = s < H ? s : LZ - 2 * H + s;
-      return r + LX * LY * lz;
-    }
-    h -= SLAB;
-  }
-  constexpr int P = 2 * H * LX + 2 * H * (LY - 2 * H);  // halo cells of one inner plane
-  lz = (ND == 3 ? H : 0) + h / P;
-  int r = h % P;
-  int lx, ly;
-  if (r < 2 * H * LX) {
-    const int s = r / LX;
-    ly = s < H ? s : LY - 2 * H + s;
-    lx = r % LX;
-  } else {
-    r -= 2 * H * LX;
-    const int s = r / (LY - 2 * H);
-    lx = s < H ? s : LX - 2 * H + s;
-    ly = H + r % (LY - 2 * H);
-  }
-  return lx + LX * (ly + LY * lz);
-}
-
-template <class T, int ND>
-__host__ __device__ constexpr int halo_count() {
-  return (ND == 3 ? 2 * T::H * T::LX * T::LY : 0) +
-         (ND == 3 ? (T::LZ - 2 * T::H) : 1) * (2 * T::H * T::LX + 2 * T::H * (T::LY - 2 * T::H));
 }
 
 __device__ __forceinline__ void push_item(int64_t* q, int* n, int cap, int* err, int64_t c) {
@@ -621,10 +628,10 @@ __global__ void ldir_check_kernel(const LdirBatch B, const uint8_t* __restrict__
   constexpr int NH = halo_count<T, ND>();
   const int64_t total = B.total_tiles * NH;
   for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
+    const uint8_t s = saved[e];
+    if (!(s & 1u)) continue;  // not lowered by its tile
     const int64_t flat = e / NH;
     const int b = halo_cell<T, ND>((int)(e % NH));
-    const uint8_t s = saved[flat * T::NL + b];
-    if (!(s & 1u)) continue;  // outside the complex, or nothing there
     const int vi = batch_volume(B, flat);
     const LdirVol& vol = B.v[vi];
     const GradDims& D = vol.D;
@@ -717,7 +724,7 @@ int64_t ldir_num_tiles(int nd, const GradDims& D) {
   return ((D.d[0] + kTX2 - 1) / kTX2) * ((D.d[1] + kTY2 - 1) / kTY2);
 }
 
-int64_t ldir_box_bytes(int nd) { return nd == 3 ? Tile3::NL : Tile2::NL; }
+int64_t ldir_halo_bytes(int nd) { return nd == 3 ? halo_count<Tile3, 3>() : halo_count<Tile2, 2>(); }
 
 cudaError_t make_ldir_batch(int nd, int n, uint8_t* const* g, const GradDims* D, LdirBatch* B) {
   if (n < 1 || n > kMaxBatch || (nd == 2 && n != 1)) return cudaErrorInvalidValue;
@@ -742,12 +749,14 @@ cudaError_t launch_ldir_tile(int nd, const LdirBatch& B, uint8_t* saved, int* er
     const size_t sm = Tile3::tile_smem_bytes();
     cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
     if (e != cudaSuccess) return e;
+    ::msc::count_launch();
     k<<<grid, kBS3, sm, stream>>>(B, saved, err);
   } else {
     auto k = ldir_tile_kernel<2, kTX2, kTY2, 1, kBS2>;
     const size_t sm = Tile2::tile_smem_bytes();
     cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
     if (e != cudaSuccess) return e;
+    ::msc::count_launch();
     k<<<grid, kBS2, sm, stream>>>(B, saved, err);
   }
   return cudaGetLastError();
@@ -755,10 +764,13 @@ cudaError_t launch_ldir_tile(int nd, const LdirBatch& B, uint8_t* saved, int* er
 
 cudaError_t launch_ldir_check(int nd, const LdirBatch& B, const uint8_t* saved, int64_t* queue, int* n_queue, int cap,
                               int* lock, int* err, int num_sms, cudaStream_t stream) {
-  if (nd == 3)
+  if (nd == 3) {
+    ::msc::count_launch();
     ldir_check_kernel<3, kTX3, kTY3, kTZ3><<<num_sms * 8, 256, 0, stream>>>(B, saved, queue, n_queue, cap, lock, err);
-  else
+  } else {
+    ::msc::count_launch();
     ldir_check_kernel<2, kTX2, kTY2, 1><<<num_sms * 8, 256, 0, stream>>>(B, saved, queue, n_queue, cap, lock, err);
+  }
   return cudaGetLastError();
 }
 
@@ -767,10 +779,13 @@ cudaError_t launch_ldir_walk(int nd, const LdirBatch& B, const int64_t* qin, int
   if (n_in <= 0) return cudaSuccess;
   const int blocks = (n_in + 127) / 128;
   const int grid = blocks < num_sms * 16 ? blocks : num_sms * 16;
-  if (nd == 3)
+  if (nd == 3) {
+    ::msc::count_launch();
     ldir_walk_kernel<3><<<grid, 128, 0, stream>>>(B, qin, n_in, qout, n_out, cap, lock, err);
-  else
+  } else {
+    ::msc::count_launch();
     ldir_walk_kernel<2><<<grid, 128, 0, stream>>>(B, qin, n_in, qout, n_out, cap, lock, err);
+  }
   return cudaGetLastError();
 }
 
@@ -785,12 +800,14 @@ cudaError_t launch_ldir_pass(int nd, uint8_t* g, const GradDims& D, const uint8_
     const size_t sm = Tile3::smem_bytes();
     cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
     if (e != cudaSuccess) return e;
+    ::msc::count_launch();
     k<<<grid, kBS3, sm, stream>>>(g, D, dirty_in, dirty_out, changed, err);
   } else {
     auto k = ldir_pass_kernel<2, kTX2, kTY2, 1, kBS2>;
     const size_t sm = Tile2::smem_bytes();
     cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
     if (e != cudaSuccess) return e;
+    ::msc::count_launch();
     k<<<grid, kBS2, sm, stream>>>(g, D, dirty_in, dirty_out, changed, err);
   }
   return cudaGetLastError();

@@ -94,10 +94,13 @@ cudaError_t launch_lstar(int nd, const float* f, uint8_t* g, const GradDims& D, 
   const dim3 grid((unsigned)((D.v[0] + 31) / 32), (unsigned)((D.v[1] + BS / 32 - 1) / (BS / 32)),
                   (unsigned)(D.v[2] < 65535 ? D.v[2] : 65535));
   if (grid.y > 65535u) return cudaErrorInvalidValue;
-  if (nd == 3)
+  if (nd == 3) {
+    ::msc::count_launch();
     lstar_kernel<3, BS><<<grid, BS, 0, stream>>>(f, g, D, err);
-  else
+  } else {
+    ::msc::count_launch();
     lstar_kernel<2, BS><<<grid, BS, 0, stream>>>(f, g, D, err);
+  }
   return cudaGetLastError();
 }
 
@@ -124,6 +127,7 @@ cudaError_t launch_lstar_batch(const LstarBatch& B, int* err, int num_sms, cudaS
   const int64_t cap = (int64_t)num_sms * 64;
   const int grid = (int)(B.total_blocks < cap ? B.total_blocks : cap);
   if (grid <= 0) return cudaSuccess;
+  ::msc::count_launch();
   lstar_batch_kernel<kLstarBS><<<grid, kLstarBS, 0, stream>>>(B, err);
   return cudaGetLastError();
 }

@@ -6,6 +6,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cstdlib>
 
 #include <cstdio>
@@ -158,7 +159,7 @@ int ldir_passes(int nd, uint8_t* g, const msc::GradDims& D, cudaStream_t stream,
 // state is a valid start).
 int ldir_batch_impl(int nd, const msc::LdirBatch& B, cudaStream_t stream, Scratch& s, int* passes_out) {
   const int64_t ntiles = B.total_tiles;
-  const int64_t box = msc::ldir_box_bytes(nd);
+  const int64_t box = msc::ldir_halo_bytes(nd);
   const int sms = num_sms();
   int cap = (int)std::min<int64_t>(std::max<int64_t>(ntiles * 256, 1 << 16), (int64_t)1 << 30);
   // MSC_LDIR_QUEUE_CAP lowers the frontier capacity (tests of the multi-pass fallback)
@@ -334,6 +335,9 @@ int grad_batch_impl(int n, const float* const* f, const int64_t* dims, uint8_t* 
 namespace msc {
 // Records the calling thread's error text for msc_last_error_string().
 int set_last_error(int code, const char* msg) { return fail(code, msg); }
+
+std::atomic<long long> g_launches{0};
+void count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
 }  // namespace msc
 
 extern "C" {
@@ -343,6 +347,8 @@ int msc_version(void) { return 100; }
 const char* msc_last_error_string(void) { return g_last_error.c_str(); }
 
 int msc_last_ldir_passes(void) { return g_last_passes; }
+
+int64_t msc_kernel_launches(void) { return (int64_t)msc::g_launches.load(std::memory_order_relaxed); }
 
 int64_t msc_num_cells_3d(const int64_t dims[3]) {
   msc::GradDims D;

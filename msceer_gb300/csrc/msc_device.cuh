@@ -12,6 +12,9 @@
 
 namespace msc {
 
+// Process-wide count of the library's kernel launches (msc_kernel_launches()).
+void count_launch();
+
 enum : int {
   kErrNone = 0,
   kErrNaN = 1 << 0,          // input contains NaN (outside the order's contract)
@@ -61,7 +64,7 @@ struct LstarBatch {
 cudaError_t make_lstar_batch(int n, const float* const* f, uint8_t* const* g, const GradDims* D, LstarBatch* B);
 cudaError_t launch_lstar_batch(const LstarBatch& B, int* err, int num_sms, cudaStream_t stream);
 int64_t ldir_num_tiles(int nd, const GradDims& D);
-int64_t ldir_box_bytes(int nd);
+int64_t ldir_halo_bytes(int nd);
 struct LdirVol {
   uint8_t* g;
   GradDims D;

@@ -248,6 +248,7 @@ int prepare_direction(LabelCtx& c, DirLabels& d, int32_t* stage_terminal) {
   LCUDA(c.pool.get(&d.lab, N), "alloc");
   LCUDA(c.pool.get(&d.state, N), "alloc");
   LCUDA(cudaMemsetAsync(c.counters, 0, 3 * sizeof(int), st), "memset");
+  ::msc::count_launch();
   fill_i32_kernel<<<c.grid, 256, 0, st>>>(c.key, N, -1);
   LCUDA(msc::launch_find_critical(c.grad, V, dir, c.key, c.ext_cells, c.counters, c.saddles, c.counters + 1, c.sms, st),
         "critical");
@@ -268,7 +269,10 @@ int prepare_direction(LabelCtx& c, DirLabels& d, int32_t* stage_terminal) {
         "trace arcs");
   int n_arcs = 0;
   if (int rc = read_int(c.counters + 2, &n_arcs, st)) return rc;
-  if (n_ext > 0) iota_kernel<<<(n_ext + 255) / 256, 256, 0, st>>>(rep, n_ext);
+  if (n_ext > 0) {
+    ::msc::count_launch();
+    iota_kernel<<<(n_ext + 255) / 256, 256, 0, st>>>(rep, n_ext);
+  }
   if (n_arcs > 0) {
     // the few arcs that can merge: exact priority-queue simplification on the host
     std::vector<msc::Arc> ha(n_arcs);
@@ -284,7 +288,9 @@ int prepare_direction(LabelCtx& c, DirLabels& d, int32_t* stage_terminal) {
     LCUDA(cudaMemcpyAsync(rep, hrep.data(), n_ext * sizeof(int32_t), cudaMemcpyHostToDevice, st), "write rep");
     LCUDA(cudaStreamSynchronize(st), "sync");
   }
+  ::msc::count_launch();
   fill_i32_kernel<<<c.grid, 256, 0, st>>>(d.lab, N, -1);
+  ::msc::count_launch();
   fill_i32_kernel<<<(n_ext + 256) / 256, 256, 0, st>>>(name, n_ext + 1, INT_MAX);
   LCUDA(cudaMemsetAsync(d.state, 0, (size_t)N, st), "memset");
   LCUDA(msc::launch_group_seeds(rep, d.seed, n_ext, name, d.lab, d.state, c.sms, st), "seeds");
@@ -304,7 +310,11 @@ int prepare_direction(LabelCtx& c, DirLabels& d, int32_t* stage_terminal) {
     din = dout;
     dout = (dout == c.tiles) ? c.tiles + c.ntiles : c.tiles;
   }
-  if (stage_terminal) snapshot_kernel<<<c.grid, 256, 0, st>>>(d.lab, stage_terminal, N);
+  if (stage_terminal) {
+    ::msc::count_launch();
+    snapshot_kernel<<<c.grid, 256, 0, st>>>(d.lab, stage_terminal, N);
+  }
+  ::msc::count_launch();
   terminal_state_kernel<<<c.grid, 256, 0, st>>>(d.lab, d.state, N);
   return MSC_OK;
 }
@@ -318,7 +328,10 @@ msc::IntegParams integ_params(const msc_integ_params* p, int dir) {
 int first_pass(LabelCtx& c, DirLabels& d) {
   const int64_t N = c.N;
   cudaStream_t st = c.st;
-  if (d.n_ext > 0) zero_seed_grad_kernel<<<(d.n_ext + 255) / 256, 256, 0, st>>>(d.seed, d.n_ext, c.g32, c.g64);
+  if (d.n_ext > 0) {
+    ::msc::count_launch();
+    zero_seed_grad_kernel<<<(d.n_ext + 255) / 256, 256, 0, st>>>(d.seed, d.n_ext, c.g32, c.g64);
+  }
   const msc::IntegParams P = integ_params(c.p, d.dir);
   msc::SpreadOrder S{};
   S.nlev = 0;
@@ -383,7 +396,10 @@ int finish_direction(LabelCtx& c, DirLabels& d, int32_t* out, int32_t* stage_int
     if (int rc = read_int(c.counters + 6, &n_list, st)) return rc;
     std::swap(cur, nxt);
   }
-  if (stage_integrated) snapshot_kernel<<<c.grid, 256, 0, st>>>(d.lab, stage_integrated, N);
+  if (stage_integrated) {
+    ::msc::count_launch();
+    snapshot_kernel<<<c.grid, 256, 0, st>>>(d.lab, stage_integrated, N);
+  }
   if (!out) return MSC_OK;
 
   // isolated-region cleaner

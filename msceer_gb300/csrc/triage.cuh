@@ -9,6 +9,8 @@
 
 namespace msc {
 
+void count_launch();  // msc_capi.cu
+
 struct ConvDims {
   int64_t X, Y, Z, N;  // vertices per axis, N = X*Y*Z
 };

@@ -207,18 +207,21 @@ cudaError_t launch_conv3_tc(int epi, const CUtensorMap& in_map, const uint8_t* w
     case kEpiReluBf16:
       e = cudaFuncSetAttribute(conv3_tc_kernel<kEpiReluBf16>, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemConv);
       if (e != cudaSuccess) return e;
+      ::msc::count_launch();
       conv3_tc_kernel<kEpiReluBf16><<<grid, 128, kSmemConv, st>>>(in_map, wblob, bias, D, out_act, out_logits,
                                                                    mask_act, err);
       break;
     case kEpiLogits:
       e = cudaFuncSetAttribute(conv3_tc_kernel<kEpiLogits>, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemConv);
       if (e != cudaSuccess) return e;
+      ::msc::count_launch();
       conv3_tc_kernel<kEpiLogits><<<grid, 128, kSmemConv, st>>>(in_map, wblob, bias, D, out_act, out_logits, mask_act,
                                                                  err);
       break;
     default:
       e = cudaFuncSetAttribute(conv3_tc_kernel<kEpiMaskBf16>, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemConv);
       if (e != cudaSuccess) return e;
+      ::msc::count_launch();
       conv3_tc_kernel<kEpiMaskBf16><<<grid, 128, kSmemConv, st>>>(in_map, wblob, bias, D, out_act, out_logits,
                                                                    mask_act, err);
       break;

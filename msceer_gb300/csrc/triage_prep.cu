@@ -351,7 +351,9 @@ cudaError_t launch_features(const float* f, const float4* g, const int32_t* lab,
   const int64_t N = V.X * V.Y * V.Z;
   cudaError_t e = cudaMemsetAsync(sums, 0, 3 * sizeof(double), st);
   if (e != cudaSuccess) return e;
+  ::msc::count_launch();
   feature_stats_kernel<<<num_sms * 4, 256, 0, st>>>(f, g, N, sums);
+  ::msc::count_launch();
   features_kernel<<<num_sms * 8, 256, 0, st>>>(f, g, lab, state, V, dir, sums, out);
   return cudaGetLastError();
 }
@@ -360,6 +362,7 @@ cudaError_t launch_triage_apply(const float* logits, float logit_threshold, uint
                                 float audit_frac, uint64_t audit_seed, unsigned long long* counts, int num_sms,
                                 cudaStream_t st) {
   const double q = audit_frac <= 0.f ? 0.0 : (audit_frac >= 1.f ? 4294967295.0 : (double)audit_frac * 4294967296.0);
+  ::msc::count_launch();
   triage_apply_kernel<<<num_sms * 8, 256, 0, st>>>(logits, logit_threshold, state, flags, N, (uint32_t)q, audit_seed,
                                                    counts);
   return cudaGetLastError();
@@ -367,29 +370,34 @@ cudaError_t launch_triage_apply(const float* logits, float logit_threshold, uint
 
 cudaError_t launch_audit_count(const int32_t* lab, const int32_t* first, const uint8_t* flags, int64_t N,
                                unsigned long long* count, int num_sms, cudaStream_t st) {
+  ::msc::count_launch();
   audit_count_kernel<<<num_sms * 8, 256, 0, st>>>(lab, first, flags, N, count);
   return cudaGetLastError();
 }
 
 cudaError_t launch_change_targets(const int32_t* lab, const int32_t* first, int64_t N, uint8_t* targets, int num_sms,
                                   cudaStream_t st) {
+  ::msc::count_launch();
   change_targets_kernel<<<num_sms * 8, 256, 0, st>>>(lab, first, N, targets);
   return cudaGetLastError();
 }
 
 cudaError_t launch_pack_weights(const float* params, uint8_t* blobs, cudaStream_t st) {
+  ::msc::count_launch();
   pack_weights_kernel<<<(5 * 27 * 256 + 255) / 256, 256, 0, st>>>(params, blobs);
   return cudaGetLastError();
 }
 
 cudaError_t launch_bce_loss(const float* logits, const uint8_t* target, const ConvDims& D, float pos_weight,
                             float scale, __nv_bfloat16* dY, double* loss, int num_sms, cudaStream_t st) {
+  ::msc::count_launch();
   bce_loss_kernel<<<num_sms * 8, 256, 0, st>>>(logits, target, D, pos_weight, scale, dY, loss);
   return cudaGetLastError();
 }
 
 cudaError_t launch_conv_wgrad(const __nv_bfloat16* X, const __nv_bfloat16* dY, const ConvDims& D, float* dW,
                               float* db, int num_sms, cudaStream_t st) {
+  ::msc::count_launch();
   conv_wgrad_kernel<<<num_sms * 4, 128, 0, st>>>(X, dY, D, dW, db);
   return cudaGetLastError();
 }
@@ -398,6 +406,7 @@ cudaError_t launch_adam(float* p, const float* g, float* m, float* v, int n, flo
                         cudaStream_t st) {
   const float b1 = 0.9f, b2 = 0.999f;
   const float bc1 = 1.f - powf(b1, (float)step), bc2 = 1.f - powf(b2, (float)step);
+  ::msc::count_launch();
   adam_kernel<<<(n + 255) / 256, 256, 0, st>>>(p, g, m, v, n, lr, b1, b2, 1e-8f, bc1, bc2, mask);
   return cudaGetLastError();
 }
