@@ -11,6 +11,7 @@ from .api import (  # noqa: F401
     TopologicalRegularGrid3D,
     ascending_manifold_dims,
     integrated_labels,
+    integrated_labels_batch,
     lower_star_grad,
     lower_star_grad_batch,
     lower_star_pairs,

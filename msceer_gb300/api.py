@@ -191,6 +191,22 @@ def integrated_labels(f, grad, error_threshold=1e-4, gradient_threshold=None, it
     return out
 
 
+def integrated_labels_batch(volumes, grads, threads: int = 4, **kwargs):
+    """integrated_labels of many volumes, `threads` at a time on their own CUDA streams
+    (each call synchronises only its own stream, so the volumes overlap on the GPU)."""
+    import concurrent.futures as cf
+
+    import torch
+
+    def one(i):
+        s = torch.cuda.Stream(device=volumes[i].device)
+        with torch.cuda.stream(s):
+            return integrated_labels(volumes[i], grads[i], **kwargs)
+
+    with cf.ThreadPoolExecutor(max_workers=max(1, threads)) as ex:
+        return list(ex.map(one, range(len(volumes))))
+
+
 class TopologicalRegularGrid3D:
     """Cell-complex index algebra of a non-periodic X x Y x Z vertex grid."""
 

@@ -613,9 +613,12 @@ __device__ __forceinline__ void push_item(int64_t* q, int* n, int cap, int* err,
   if (slot < cap) q[slot] = c; else atomicOr(err, kErrLocalQueue);
 }
 
-// frontier entries carry their volume in the top bits
-constexpr int kVolShift = 58;
+// frontier entries carry their volume above the cell id (bits 57-62, so entries stay
+// non-negative for every volume index below kMaxBatch = 64)
+constexpr int kVolShift = 57;
 constexpr int64_t kCellMask = ((int64_t)1 << kVolShift) - 1;
+static_assert(kMaxBatch <= 64, "six volume bits");
+__device__ __forceinline__ int entry_volume(int64_t e) { return (int)((uint64_t)e >> kVolShift); }
 
 __device__ __forceinline__ GradView volume_view(const LdirVol& v, int* lock, int* err) {
   return GradView{v.g, reinterpret_cast<uintptr_t>(v.g), reinterpret_cast<uintptr_t>(v.g + v.D.ncells), lock, err};
@@ -626,28 +629,37 @@ __global__ void ldir_check_kernel(const LdirBatch B, const uint8_t* __restrict__
                                   int* __restrict__ n_queue, int cap, int* lock, int* err) {
   using T = LdirTile<ND, TX, TY, TZ>;
   constexpr int NH = halo_count<T, ND>();
+  static_assert(NH % 16 == 0, "halo records are read 16 bytes at a time");
   const int64_t total = B.total_tiles * NH;
-  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
-    const uint8_t s = saved[e];
-    if (!(s & 1u)) continue;  // not lowered by its tile
-    const int64_t flat = e / NH;
-    const int b = halo_cell<T, ND>((int)(e % NH));
-    const int vi = batch_volume(B, flat);
-    const LdirVol& vol = B.v[vi];
-    const GradDims& D = vol.D;
-    const int64_t ntx = (D.d[0] + TX - 1) / TX, nty = (D.d[1] + TY - 1) / TY;
-    const int64_t tile = flat - vol.tile0;
-    const int64_t tx = tile % ntx, ty = (tile / ntx) % nty, tz = (ND == 3) ? tile / (ntx * nty) : 0;
-    const int lx = b % T::LX, ly = (b / T::LX) % T::LY, lz = b / (T::LX * T::LY);
-    const int64_t gx = tx * TX - T::H + lx, gy = ty * TY - T::H + ly, gz = (ND == 3) ? tz * TZ - T::H + lz : 0;
-    const int64_t c = gx + gy * D.cs[1] + gz * D.cs[2];
-    const unsigned v = s >> 5;
-    if ((unsigned)(vol.g[c] >> 5) <= v) continue;
-    const GradView G = volume_view(vol, lock, err);
-    if (!lower_ldir(G, c, v)) continue;
-    const int dim = (int)((gx & 1) + (gy & 1) + (gz & 1));
-    if ((dim == 1 && v == 2u) || (dim == 2 && v == 1u))
-      push_item(queue, n_queue, cap, err, ((int64_t)vi << kVolShift) | c);
+  // 16 saved bytes per step: almost all are zero (not lowered by their tile)
+  for (int64_t e0 = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) * 16; e0 < total;
+       e0 += (int64_t)gridDim.x * blockDim.x * 16) {
+    const uint4 q = *reinterpret_cast<const uint4*>(saved + e0);
+    if (!((q.x | q.y | q.z | q.w) & 0x01010101u)) continue;
+#pragma unroll 1
+    for (int j = 0; j < 16; j++) {
+      const int64_t e = e0 + j;
+      const uint8_t s = saved[e];
+      if (!(s & 1u)) continue;  // not lowered by its tile
+      const int64_t flat = e / NH;
+      const int b = halo_cell<T, ND>((int)(e % NH));
+      const int vi = batch_volume(B, flat);
+      const LdirVol& vol = B.v[vi];
+      const GradDims& D = vol.D;
+      const int64_t ntx = (D.d[0] + TX - 1) / TX, nty = (D.d[1] + TY - 1) / TY;
+      const int64_t tile = flat - vol.tile0;
+      const int64_t tx = tile % ntx, ty = (tile / ntx) % nty, tz = (ND == 3) ? tile / (ntx * nty) : 0;
+      const int lx = b % T::LX, ly = (b / T::LX) % T::LY, lz = b / (T::LX * T::LY);
+      const int64_t gx = tx * TX - T::H + lx, gy = ty * TY - T::H + ly, gz = (ND == 3) ? tz * TZ - T::H + lz : 0;
+      const int64_t c = gx + gy * D.cs[1] + gz * D.cs[2];
+      const unsigned v = s >> 5;
+      if ((unsigned)(vol.g[c] >> 5) <= v) continue;
+      const GradView G = volume_view(vol, lock, err);
+      if (!lower_ldir(G, c, v)) continue;
+      const int dim = (int)((gx & 1) + (gy & 1) + (gz & 1));
+      if ((dim == 1 && v == 2u) || (dim == 2 && v == 1u))
+        push_item(queue, n_queue, cap, err, ((int64_t)vi << kVolShift) | c);
+    }
   }
 }
 
@@ -661,7 +673,11 @@ __global__ void __launch_bounds__(128) ldir_walk_kernel(const LdirBatch B, const
   int64_t stack[SD];
   for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n_in; k += gridDim.x * blockDim.x) {
     const int64_t entry = qin[k];
-    const int vi = (int)(entry >> kVolShift);
+    const int vi = entry_volume(entry);
+    if (vi >= B.n) {  // not an entry this launch wrote
+      atomicOr(err, kErrPassLimit);
+      continue;
+    }
     const LdirVol& vol = B.v[vi];
     const GradDims& D = vol.D;
     const GradView G = volume_view(vol, lock, err);

@@ -223,3 +223,15 @@ def test_batch_of_uneven_volumes_equals_single_calls(gpu):
     got = lower_star_grad_batch(vols)
     for v, g in zip(vols, got):
         assert torch.equal(g, lower_star_grad(v))
+
+
+def test_batch_of_48_volumes(gpu):
+    """Volume indices of 32 and above (the frontier entries carry the index in their top bits)."""
+    import torch
+    from msceer_gb300 import lower_star_grad, lower_star_grad_batch
+    rng = np.random.default_rng(22)
+    shapes = [tuple(int(v) for v in rng.integers(16, 48, size=3)) for _ in range(48)]
+    vols = [torch.from_numpy(fields.power_law_field(s, seed=100 + i)).to(gpu) for i, s in enumerate(shapes)]
+    got = lower_star_grad_batch(vols)
+    for v, g in zip(vols, got):
+        assert torch.equal(g, lower_star_grad(v))

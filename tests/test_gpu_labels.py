@@ -54,3 +54,17 @@ def test_labels_vs_oracle(gpu, oracle, name, precision):
     for k in ("asc", "dsc"):
         labs = np.unique(got[k])
         assert (labs >= -1).all()
+
+
+def test_batch_labels_on_concurrent_streams_equal_sequential(gpu):
+    import torch
+    from msceer_gb300 import integrated_labels, integrated_labels_batch, lower_star_grad_batch
+    shapes = [(30, 26, 22), (40, 20, 33), (24, 36, 28), (18, 18, 50)]
+    vols = [torch.from_numpy(fields.power_law_field(s, seed=40 + i)).to(gpu) for i, s in enumerate(shapes)]
+    grads = lower_star_grad_batch(vols)
+    torch.cuda.synchronize()
+    got = integrated_labels_batch(vols, grads, threads=3)
+    for v, g, r in zip(vols, grads, got):
+        want = integrated_labels(v, g)
+        for k in ("asc", "dsc"):
+            assert torch.equal(r[k], want[k])
