@@ -82,7 +82,10 @@ int msc_lower_star_grad_2d(const float* f, const int64_t dims[2], uint8_t* grad_
  * which runs one process per volume): f[i], grad[i] are device buffers of volume i
  * with dims[3*i..3*i+2]; every .grad equals msc_lower_star_grad_3d's.  Up to 64
  * volumes share each kernel launch (a flat grid over all their blocks / tiles, the
- * volume table passed in the launch parameters).  Synchronises `stream` at the end. */
+ * volume table passed in the launch parameters) and run as one CUDA graph, kept and
+ * replayed while the same buffers come back; the launch shapes are tuned by timing on
+ * the first batch of a size class.  Larger batches run in chunks of 64 without a
+ * graph.  Synchronises `stream` at the end. */
 int msc_lower_star_grad_batch_3d(int n, const float* const* f, const int64_t* dims, uint8_t* const* grad,
                                  msc_stream_t stream);
 

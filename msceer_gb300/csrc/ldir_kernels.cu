@@ -665,12 +665,17 @@ __global__ void ldir_check_kernel(const LdirBatch B, const uint8_t* __restrict__
 
 // Finish the walks of queued items in global memory, depth first with a short
 // per-thread stack; what does not fit goes to the next round's queue.
+// n_in_dev (when set): the queue length lives in device memory (graph-captured rounds)
 template <int ND>
 __global__ void __launch_bounds__(128) ldir_walk_kernel(const LdirBatch B, const int64_t* __restrict__ qin, int n_in,
-                                                        int64_t* __restrict__ qout, int* __restrict__ n_out, int cap,
-                                                        int* lock, int* err) {
+                                                        const int* __restrict__ n_in_dev, int64_t* __restrict__ qout,
+                                                        int* __restrict__ n_out, int cap, int* lock, int* err) {
   constexpr int SD = 24;
   int64_t stack[SD];
+  if (n_in_dev) {
+    n_in = *n_in_dev;
+    if (n_in > cap) n_in = 0;  // overflowed: the host finishes with tile passes
+  }
   for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n_in; k += gridDim.x * blockDim.x) {
     const int64_t entry = qin[k];
     const int vi = entry_volume(entry);
@@ -756,8 +761,9 @@ cudaError_t make_ldir_batch(int nd, int n, uint8_t* const* g, const GradDims* D,
   return cudaSuccess;
 }
 
-cudaError_t launch_ldir_tile(int nd, const LdirBatch& B, uint8_t* saved, int* err, int num_sms, cudaStream_t stream) {
-  const int64_t cap = (int64_t)num_sms * 4;
+cudaError_t launch_ldir_tile(int nd, const LdirBatch& B, uint8_t* saved, int* err, int num_sms, cudaStream_t stream,
+                             int ctas_per_sm) {
+  const int64_t cap = (int64_t)num_sms * ctas_per_sm;
   const int grid = (int)(B.total_tiles < cap ? B.total_tiles : cap);
   if (grid <= 0) return cudaSuccess;
   if (nd == 3) {
@@ -797,11 +803,18 @@ cudaError_t launch_ldir_walk(int nd, const LdirBatch& B, const int64_t* qin, int
   const int grid = blocks < num_sms * 16 ? blocks : num_sms * 16;
   if (nd == 3) {
     ::msc::count_launch();
-    ldir_walk_kernel<3><<<grid, 128, 0, stream>>>(B, qin, n_in, qout, n_out, cap, lock, err);
+    ldir_walk_kernel<3><<<grid, 128, 0, stream>>>(B, qin, n_in, nullptr, qout, n_out, cap, lock, err);
   } else {
     ::msc::count_launch();
-    ldir_walk_kernel<2><<<grid, 128, 0, stream>>>(B, qin, n_in, qout, n_out, cap, lock, err);
+    ldir_walk_kernel<2><<<grid, 128, 0, stream>>>(B, qin, n_in, nullptr, qout, n_out, cap, lock, err);
   }
+  return cudaGetLastError();
+}
+
+cudaError_t launch_ldir_walk_dev(const LdirBatch& B, const int64_t* qin, const int* n_in_dev, int64_t* qout, int* n_out,
+                                 int cap, int* lock, int* err, int num_sms, cudaStream_t stream) {
+  ::msc::count_launch();
+  ldir_walk_kernel<3><<<num_sms * 16, 128, 0, stream>>>(B, qin, 0, n_in_dev, qout, n_out, cap, lock, err);
   return cudaGetLastError();
 }
 

@@ -123,8 +123,8 @@ cudaError_t make_lstar_batch(int n, const float* const* f, uint8_t* const* g, co
   return cudaSuccess;
 }
 
-cudaError_t launch_lstar_batch(const LstarBatch& B, int* err, int num_sms, cudaStream_t stream) {
-  const int64_t cap = (int64_t)num_sms * 64;
+cudaError_t launch_lstar_batch(const LstarBatch& B, int* err, int num_sms, cudaStream_t stream, int blocks_per_sm) {
+  const int64_t cap = (int64_t)num_sms * blocks_per_sm;
   const int grid = (int)(B.total_blocks < cap ? B.total_blocks : cap);
   if (grid <= 0) return cudaSuccess;
   ::msc::count_launch();

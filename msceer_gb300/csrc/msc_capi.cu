@@ -7,6 +7,8 @@
 
 #include <algorithm>
 #include <atomic>
+#include <mutex>
+#include <map>
 #include <cstdlib>
 
 #include <cstdio>
@@ -157,16 +159,22 @@ int ldir_passes(int nd, uint8_t* g, const msc::GradDims& D, cudaStream_t stream,
 // lowered.  Should a frontier queue overflow, the multi-pass form finishes the
 // closure from wherever it stands (the closure is monotone, so any intermediate
 // state is a valid start).
-int ldir_batch_impl(int nd, const msc::LdirBatch& B, cudaStream_t stream, Scratch& s, int* passes_out) {
-  const int64_t ntiles = B.total_tiles;
-  const int64_t box = msc::ldir_halo_bytes(nd);
-  const int sms = num_sms();
+// Frontier queue capacity for `ntiles` tiles; MSC_LDIR_QUEUE_CAP lowers it (tests of
+// the multi-pass fallback).
+int frontier_cap(int64_t ntiles) {
   int cap = (int)std::min<int64_t>(std::max<int64_t>(ntiles * 256, 1 << 16), (int64_t)1 << 30);
-  // MSC_LDIR_QUEUE_CAP lowers the frontier capacity (tests of the multi-pass fallback)
   if (const char* e = std::getenv("MSC_LDIR_QUEUE_CAP")) {
     const long v = std::strtol(e, nullptr, 10);
     if (v > 0 && v < cap) cap = (int)v;
   }
+  return cap;
+}
+
+int ldir_batch_impl(int nd, const msc::LdirBatch& B, cudaStream_t stream, Scratch& s, int* passes_out) {
+  const int64_t ntiles = B.total_tiles;
+  const int64_t box = msc::ldir_halo_bytes(nd);
+  const int sms = num_sms();
+  const int cap = frontier_cap(ntiles);
   uint8_t* saved = nullptr;
   int64_t* queues = nullptr;
   int* ctr = nullptr;  // [0] queue a [1] queue b [2] lock [3] frontier overflow / CAS limit
@@ -300,6 +308,197 @@ int host_impl(int nd, const float* fh, const int64_t* dims, uint8_t* gh) {
   return MSC_OK;
 }
 
+// ---- batches of up to kMaxBatch volumes as one CUDA graph -------------------------------------
+//
+// The .grad of a batch is one graph: K1 over all volumes, the ldir tile pass, the halo
+// check and kGraphRounds frontier-walk rounds whose queue lengths stay on the device.
+// After a replay the host reads the counters once; a frontier left over after the
+// captured rounds is walked on, an overflow falls back to tile passes.  The launch
+// shapes (K1 blocks per SM, ldir tiles per SM) are picked by timing the candidates on
+// the first batch of a size class; the instantiated graph is kept and replayed while
+// the same buffers come back.
+
+constexpr int kGraphRounds = 3;
+constexpr int kGraphKernels = 3 + kGraphRounds;  // K1, tile, check, walk rounds
+
+struct BatchGraph {
+  int dev = -1;
+  std::vector<const float*> f;
+  std::vector<uint8_t*> g;
+  std::vector<int64_t> dims;
+  int bps = 64, cps = 4;
+  cudaGraphExec_t exec = nullptr;
+  uint8_t* saved = nullptr;
+  int64_t* queues = nullptr;
+  int* ctr = nullptr;    // [0] [1] queue lengths, [2] lock, [3] overflow / CAS limit
+  int* words = nullptr;  // kernel status words
+  int cap = 0;
+  void release() {
+    if (exec) cudaGraphExecDestroy(exec);
+    exec = nullptr;
+    for (void* q : {(void*)saved, (void*)queues, (void*)ctr, (void*)words})
+      if (q) cudaFree(q);
+    saved = nullptr;
+    queues = nullptr;
+    ctr = nullptr;
+    words = nullptr;
+  }
+  ~BatchGraph() { release(); }
+};
+thread_local BatchGraph t_bgraph;
+std::mutex g_tune_mu;
+std::map<int, std::pair<int, int>> g_tuned;  // size class -> (K1 blocks per SM, ldir tiles per SM)
+
+int capture_batch_graph(BatchGraph& G, const msc::LstarBatch& LB, const msc::LdirBatch& B, int bps, int cps,
+                        cudaGraphExec_t* out) {
+  const int sms = num_sms();
+  cudaStream_t cs = nullptr;
+  MSC_CUDA(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking), "cudaStreamCreate");
+  struct Destroy {
+    cudaStream_t s;
+    ~Destroy() { cudaStreamDestroy(s); }
+  } ds{cs};
+  const long long counted = msc::launches_so_far();  // captured launches do not run now
+  MSC_CUDA(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal), "cudaStreamBeginCapture");
+  cudaError_t e = cudaMemsetAsync(G.words, 0, 2 * sizeof(int), cs);
+  if (e == cudaSuccess) e = cudaMemsetAsync(G.ctr, 0, 4 * sizeof(int), cs);
+  if (e == cudaSuccess) e = msc::launch_lstar_batch(LB, G.words, sms, cs, bps);
+  if (e == cudaSuccess) e = msc::launch_ldir_tile(3, B, G.saved, G.words, sms, cs, cps);
+  if (e == cudaSuccess) e = msc::launch_ldir_check(3, B, G.saved, G.queues, G.ctr, G.cap, G.ctr + 2, G.ctr + 3, sms, cs);
+  for (int r = 0; r < kGraphRounds && e == cudaSuccess; r++) {
+    int* n_in = G.ctr + (r % 2);
+    int* n_out = G.ctr + ((r + 1) % 2);
+    e = cudaMemsetAsync(n_out, 0, sizeof(int), cs);
+    if (e == cudaSuccess)
+      e = msc::launch_ldir_walk_dev(B, G.queues + (size_t)(r % 2) * G.cap, n_in,
+                                    G.queues + (size_t)((r + 1) % 2) * G.cap, n_out, G.cap, G.ctr + 2, G.ctr + 3, sms,
+                                    cs);
+  }
+  cudaGraph_t graph = nullptr;
+  const cudaError_t ec = cudaStreamEndCapture(cs, &graph);
+  msc::add_launches(counted - msc::launches_so_far());
+  if (e == cudaSuccess) e = ec;
+  if (e == cudaSuccess) e = cudaGraphInstantiate(out, graph, 0);
+  if (graph) cudaGraphDestroy(graph);
+  MSC_CUDA(e, "batch graph capture");
+  return MSC_OK;
+}
+
+// Finishes what the captured rounds left: more walk rounds, or tile passes on overflow.
+int finish_batch(BatchGraph& G, const msc::LdirBatch& B, cudaStream_t stream, int* launches) {
+  const int sms = num_sms();
+  int h[4];
+  MSC_CUDA(cudaMemcpyAsync(h, G.ctr, 4 * sizeof(int), cudaMemcpyDeviceToHost, stream), "read counters");
+  MSC_CUDA(cudaStreamSynchronize(stream), "cudaStreamSynchronize");
+  int cur = kGraphRounds % 2;
+  int n = h[cur];
+  bool overflow = h[3] != 0 || h[0] > G.cap || h[1] > G.cap;
+  for (int round = 0; !overflow && n > 0; round++) {
+    if (round > 4096) return fail(MSC_ERR_ITER_LIMIT, "ldir frontier walk did not converge");
+    int* n_out = G.ctr + (1 - cur);
+    MSC_CUDA(cudaMemsetAsync(n_out, 0, sizeof(int), stream), "reset queue");
+    MSC_CUDA(msc::launch_ldir_walk(3, B, G.queues + (size_t)cur * G.cap, n, G.queues + (size_t)(1 - cur) * G.cap, n_out,
+                                   G.cap, G.ctr + 2, G.ctr + 3, sms, stream),
+             "ldir walk kernel launch");
+    (*launches)++;
+    MSC_CUDA(cudaMemcpyAsync(h, G.ctr, 4 * sizeof(int), cudaMemcpyDeviceToHost, stream), "read counters");
+    MSC_CUDA(cudaStreamSynchronize(stream), "cudaStreamSynchronize");
+    cur = 1 - cur;
+    n = h[cur];
+    overflow = h[3] != 0 || n > G.cap;
+  }
+  if (overflow) {
+    Scratch s;
+    if (int rc = alloc_scratch(s, stream)) return rc;
+    for (int i = 0; i < B.n; i++)
+      if (int rc = ldir_passes(3, B.v[i].g, B.v[i].D, stream, s, launches)) return rc;
+    if (int rc = check_errors(s, stream)) return rc;
+  }
+  return MSC_OK;
+}
+
+int grad_batch_graph_impl(int n, const float* const* f, const int64_t* dims, uint8_t* const* g,
+                          const std::vector<msc::GradDims>& D, cudaStream_t stream) {
+  int dev = 0;
+  MSC_CUDA(cudaGetDevice(&dev), "cudaGetDevice");
+  BatchGraph& G = t_bgraph;
+  msc::LstarBatch LB;
+  msc::LdirBatch B;
+  MSC_CUDA(msc::make_lstar_batch(n, f, g, D.data(), &LB), "lower-star batch (plane too large)");
+  MSC_CUDA(msc::make_ldir_batch(3, n, g, D.data(), &B), "ldir batch");
+  const int cap = frontier_cap(B.total_tiles);
+  const bool same = G.exec && G.dev == dev && G.cap == cap && (int)G.f.size() == n &&
+                    std::equal(G.f.begin(), G.f.end(), f) && std::equal(G.g.begin(), G.g.end(), g) &&
+                    std::equal(G.dims.begin(), G.dims.end(), dims);
+  if (!same) {
+    G.release();
+    G.dev = dev;
+    G.f.assign(f, f + n);
+    G.g.assign(g, g + n);
+    G.dims.assign(dims, dims + 3 * n);
+    G.cap = cap;
+    MSC_CUDA(cudaMalloc((void**)&G.saved, (size_t)B.total_tiles * msc::ldir_halo_bytes(3)), "cudaMalloc(saved halos)");
+    MSC_CUDA(cudaMalloc((void**)&G.queues, (size_t)G.cap * 2 * sizeof(int64_t)), "cudaMalloc(queues)");
+    MSC_CUDA(cudaMalloc((void**)&G.ctr, 4 * sizeof(int)), "cudaMalloc(counters)");
+    MSC_CUDA(cudaMalloc((void**)&G.words, 2 * sizeof(int)), "cudaMalloc(status)");
+    // launch shapes: tuned once per size class (log2 of the tile count)
+    int cls = 0;
+    for (int64_t t = B.total_tiles; t > 1; t >>= 1) cls++;
+    std::pair<int, int> best{64, 4};
+    bool tuned = false;
+    {
+      std::lock_guard<std::mutex> lk(g_tune_mu);
+      auto it = g_tuned.find(cls);
+      if (it != g_tuned.end()) {
+        best = it->second;
+        tuned = true;
+      }
+    }
+    if (!tuned && B.total_tiles >= 256) {
+      float best_ms = 1e30f;
+      cudaEvent_t e0, e1;
+      MSC_CUDA(cudaEventCreate(&e0), "cudaEventCreate");
+      MSC_CUDA(cudaEventCreate(&e1), "cudaEventCreate");
+      for (int bps : {32, 64, 128})
+        for (int cps : {2, 4}) {
+          cudaGraphExec_t ex = nullptr;
+          if (int rc = capture_batch_graph(G, LB, B, bps, cps, &ex)) return rc;
+          cudaGraphLaunch(ex, stream);
+          cudaEventRecord(e0, stream);
+          cudaGraphLaunch(ex, stream);
+          cudaEventRecord(e1, stream);
+          msc::add_launches(2 * kGraphKernels);
+          MSC_CUDA(cudaEventSynchronize(e1), "autotune");
+          float ms = 0.f;
+          cudaEventElapsedTime(&ms, e0, e1);
+          cudaGraphExecDestroy(ex);
+          if (ms < best_ms) {
+            best_ms = ms;
+            best = {bps, cps};
+          }
+        }
+      cudaEventDestroy(e0);
+      cudaEventDestroy(e1);
+      std::lock_guard<std::mutex> lk(g_tune_mu);
+      g_tuned[cls] = best;
+    }
+    G.bps = best.first;
+    G.cps = best.second;
+    if (int rc = capture_batch_graph(G, LB, B, G.bps, G.cps, &G.exec)) return rc;
+  }
+  MSC_CUDA(cudaGraphLaunch(G.exec, stream), "cudaGraphLaunch");
+  msc::add_launches(kGraphKernels);
+  int launches = kGraphKernels;
+  if (int rc = finish_batch(G, B, stream, &launches)) return rc;
+  g_last_passes = launches;
+  int err = 0;
+  MSC_CUDA(cudaMemcpyAsync(&err, G.words, sizeof(int), cudaMemcpyDeviceToHost, stream), "read status");
+  MSC_CUDA(cudaStreamSynchronize(stream), "cudaStreamSynchronize");
+  if (err & msc::kErrNaN) return fail(MSC_ERR_NAN_INPUT, "input contains NaN");
+  if (err & msc::kErrLocalQueue) return fail(MSC_ERR_QUEUE_OVERFLOW, "ldir tile queue overflow");
+  return MSC_OK;
+}
+
 // Many 3D volumes: one K1 launch and one ldir tile / check / walk sequence per chunk
 // of up to kMaxBatch volumes.
 int grad_batch_impl(int n, const float* const* f, const int64_t* dims, uint8_t* const* g, cudaStream_t stream) {
@@ -311,6 +510,7 @@ int grad_batch_impl(int n, const float* const* f, const int64_t* dims, uint8_t* 
     if (!make_dims(3, dims + 3 * i, &D[i])) return fail(MSC_ERR_BAD_DIMS, "invalid dims of volume " + std::to_string(i));
     if (!f[i] || !g[i]) return fail(MSC_ERR_NULL_POINTER, "null buffer of volume " + std::to_string(i));
   }
+  if (n <= msc::kMaxBatch) return grad_batch_graph_impl(n, f, dims, g, D, stream);
   Scratch s;
   if (int rc = alloc_scratch(s, stream)) return rc;
   const int sms = num_sms();
@@ -338,6 +538,8 @@ int set_last_error(int code, const char* msg) { return fail(code, msg); }
 
 std::atomic<long long> g_launches{0};
 void count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+void add_launches(long long n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
+long long launches_so_far() { return g_launches.load(std::memory_order_relaxed); }
 }  // namespace msc
 
 extern "C" {

@@ -14,6 +14,8 @@ namespace msc {
 
 // Process-wide count of the library's kernel launches (msc_kernel_launches()).
 void count_launch();
+void add_launches(long long n);
+long long launches_so_far();
 
 enum : int {
   kErrNone = 0,
@@ -62,7 +64,8 @@ struct LstarBatch {
   LstarVol v[kMaxBatch];
 };
 cudaError_t make_lstar_batch(int n, const float* const* f, uint8_t* const* g, const GradDims* D, LstarBatch* B);
-cudaError_t launch_lstar_batch(const LstarBatch& B, int* err, int num_sms, cudaStream_t stream);
+cudaError_t launch_lstar_batch(const LstarBatch& B, int* err, int num_sms, cudaStream_t stream,
+                               int blocks_per_sm = 64);
 int64_t ldir_num_tiles(int nd, const GradDims& D);
 int64_t ldir_halo_bytes(int nd);
 struct LdirVol {
@@ -76,7 +79,11 @@ struct LdirBatch {
   LdirVol v[kMaxBatch];
 };
 cudaError_t make_ldir_batch(int nd, int n, uint8_t* const* g, const GradDims* D, LdirBatch* B);
-cudaError_t launch_ldir_tile(int nd, const LdirBatch& B, uint8_t* saved, int* err, int num_sms, cudaStream_t stream);
+cudaError_t launch_ldir_tile(int nd, const LdirBatch& B, uint8_t* saved, int* err, int num_sms, cudaStream_t stream,
+                             int ctas_per_sm = 4);
+// one walk round whose input length is read from device memory (for graph capture)
+cudaError_t launch_ldir_walk_dev(const LdirBatch& B, const int64_t* qin, const int* n_in_dev, int64_t* qout, int* n_out,
+                                 int cap, int* lock, int* err, int num_sms, cudaStream_t stream);
 cudaError_t launch_ldir_check(int nd, const LdirBatch& B, const uint8_t* saved, int64_t* queue, int* n_queue, int cap,
                               int* lock, int* err, int num_sms, cudaStream_t stream);
 cudaError_t launch_ldir_walk(int nd, const LdirBatch& B, const int64_t* qin, int n_in, int64_t* qout, int* n_out,

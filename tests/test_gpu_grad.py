@@ -235,3 +235,30 @@ def test_batch_of_48_volumes(gpu):
     got = lower_star_grad_batch(vols)
     for v, g in zip(vols, got):
         assert torch.equal(g, lower_star_grad(v))
+
+
+def test_batch_graph_replay_sees_new_values(gpu):
+    """The batch graph is kept while the same buffers come back: a replay after the
+    volumes changed in place gives the .grad of the new values."""
+    import torch
+    from msceer_gb300 import lower_star_grad, lower_star_grad_batch
+    shapes = [(40, 36, 33), (17, 64, 50), (64, 64, 64), (5, 9, 70)]
+    vols = [torch.from_numpy(fields.power_law_field(s, seed=200 + i)).to(gpu) for i, s in enumerate(shapes)]
+    outs = lower_star_grad_batch(vols)
+    for v, g in zip(vols, outs):
+        assert torch.equal(g, lower_star_grad(v))
+    for v in vols:
+        v.mul_(-1.0)
+    again = lower_star_grad_batch(vols, outs)
+    for v, g in zip(vols, again):
+        assert torch.equal(g, lower_star_grad(v))
+
+
+def test_batch_graph_overflow_falls_back_to_passes(gpu, oracle, monkeypatch):
+    monkeypatch.setenv("MSC_LDIR_QUEUE_CAP", "8")
+    import torch
+    from msceer_gb300 import lower_star_grad_batch
+    fs = [fields.power_law_field(s, seed=300 + i) for i, s in enumerate([(70, 66, 60), (33, 80, 41)])]
+    got = lower_star_grad_batch([torch.from_numpy(f).to(gpu) for f in fs])
+    for f, g in zip(fs, got):
+        assert np.array_equal(g.cpu().numpy(), oracle.grad(f))
