@@ -36,9 +36,10 @@ __device__ __forceinline__ F3 lerp3(F3 a, F3 b, float t) {
   const float u = 1.f - t;
   return {a.x * u + b.x * t, a.y * u + b.y * t, a.z * u + b.z * t};
 }
-__device__ __forceinline__ float clampf_ext(float v, int64_t n) {
+// clamp into [0, n - 1] given fn = (float)n
+__device__ __forceinline__ float clampf_ext(float v, float fn) {
   if (v < 0.f) v = 0.f;
-  if (v >= (float)n) v = (float)n - 1.f;
+  if (v >= fn) v = fn - 1.f;
   return v;
 }
 
@@ -50,6 +51,24 @@ struct Adv32 {
   const uint8_t* lvl;    // ... in an earlier level of the spread order (level array, when set)
   int level;
   const uint8_t* state;  // fix-up stop (when set): nearest vertex certain terminal
+  // Converted once on the host: (float)P.max_step, (float)P.step_mult, the extents
+  // (float)V.X .. and (float)(V.X - 2) ..  (a double-to-float or 64-bit integer
+  // conversion per iteration would run on the slow FP64 pipe)
+  float ms = 0.f, sgn = 0.f;
+  float ext[3] = {0.f, 0.f, 0.f}, ext2[3] = {0.f, 0.f, 0.f};
+
+  static Adv32 make(const float4* G, const VolDims& V, const IntegParams& P, const int32_t* lab, const uint8_t* lvl,
+                    int level, const uint8_t* state) {
+    Adv32 A{G, V, P, lab, lvl, level, state};
+    A.ms = (float)P.max_step;
+    A.sgn = (float)P.step_mult;
+    const int64_t e[3] = {V.X, V.Y, V.Z};
+    for (int a = 0; a < 3; a++) {
+      A.ext[a] = (float)e[a];
+      A.ext2[a] = (float)(e[a] - 2);
+    }
+    return A;
+  }
 
   __device__ __forceinline__ F3 corner(int64_t x, int64_t y, int64_t z) const {
     const float4 g = __ldg(G + vid(V, x, y, z));
@@ -70,81 +89,91 @@ struct Adv32 {
 #pragma unroll
     for (int n = 0; n < 8; n++) c[n] = corner(vv[0][n & 1], vv[1][(n >> 1) & 1], vv[2][n >> 2]);
   }
-  __device__ __forceinline__ static F3 trilin(F3 s, const int64_t b[3], const F3 c[8]) {
-    const float fx = s.x - (float)b[0], fy = s.y - (float)b[1], fz = s.z - (float)b[2];
+  // bf: the base corner as floats
+  __device__ __forceinline__ static F3 trilin(F3 s, const float bf[3], const F3 c[8]) {
+    const float fx = s.x - bf[0], fy = s.y - bf[1], fz = s.z - bf[2];
     const F3 x0 = lerp3(c[0], c[1], fx), x1 = lerp3(c[2], c[3], fx), x2 = lerp3(c[4], c[5], fx), x3 = lerp3(c[6], c[7], fx);
     return lerp3(lerp3(x0, x1, fy), lerp3(x2, x3, fy), fz);
   }
   // Vec3l(p + 0.5), clamped into the grid (the reference clamps only near the
   // boundary, where its own points can leave it; elsewhere clamping changes nothing)
   __device__ __forceinline__ int64_t nearest(F3 p, bool) const {
-    return vid(V, (int64_t)clampf_ext(p.x + 0.5f, V.X), (int64_t)clampf_ext(p.y + 0.5f, V.Y),
-               (int64_t)clampf_ext(p.z + 0.5f, V.Z));
+    return vid(V, (int)clampf_ext(p.x + 0.5f, ext[0]), (int)clampf_ext(p.y + 0.5f, ext[1]),
+               (int)clampf_ext(p.z + 0.5f, ext[2]));
   }
-  // gm_end: the gradient magnitude at a low-gradient stop
-  __device__ int advect(F3& cur, int& iters, bool nearb, float& gm_end) const {
-    F3 c[8];
-    F3 old = cur;
+  // AdvectThroughVoxel{NoCheck,NearBoundary} split in two, so that a lane can run its
+  // streamline one iteration at a time.  enter(): the voxel's base corner, its eight
+  // corner gradients and the gradient at `cur`; false when there is no direction to
+  // follow (LOW_GRADIENT).  The caller then sets old = cur.
+  __device__ __forceinline__ bool enter(const F3& cur, bool nearb, float bf[3], F3 c[8], F3& g, float& gm,
+                                        float& step, float& gm_end) const {
     int64_t b[3];
     if (nearb) {
-      b[0] = (int64_t)clampf_ext(cur.x, V.X);
-      b[1] = (int64_t)clampf_ext(cur.y, V.Y);
-      b[2] = (int64_t)clampf_ext(cur.z, V.Z);
+      b[0] = (int)clampf_ext(cur.x, ext[0]);
+      b[1] = (int)clampf_ext(cur.y, ext[1]);
+      b[2] = (int)clampf_ext(cur.z, ext[2]);
     } else {
-      b[0] = (int64_t)fminf(fmaxf(cur.x, 0.f), (float)(V.X - 2));
-      b[1] = (int64_t)fminf(fmaxf(cur.y, 0.f), (float)(V.Y - 2));
-      b[2] = (int64_t)fminf(fmaxf(cur.z, 0.f), (float)(V.Z - 2));
+      b[0] = (int)fminf(fmaxf(cur.x, 0.f), ext2[0]);
+      b[1] = (int)fminf(fmaxf(cur.y, 0.f), ext2[1]);
+      b[2] = (int)fminf(fmaxf(cur.z, 0.f), ext2[2]);
     }
     surround(b, nearb, c);
-    F3 g = trilin(cur, b, c);
-    float gm = sqrtf(g.x * g.x + g.y * g.y + g.z * g.z);
+    bf[0] = (float)(int)b[0];
+    bf[1] = (float)(int)b[1];
+    bf[2] = (float)(int)b[2];
+    g = trilin(cur, bf, c);
+    gm = sqrtf(g.x * g.x + g.y * g.y + g.z * g.z);
     gm_end = 0.f;
-    if (!(gm > 0.f) || !isfinite(gm)) return EV_LOW_GRADIENT;  // no direction to follow
-    const float ms = (float)P.max_step;
-    float step = ms / gm;
-    while (iters-- > 0) {
-      if (!(old.x == cur.x && old.y == cur.y && old.z == cur.z)) {
-        if ((int)cur.x != (int)old.x || (int)cur.y != (int)old.y || (int)cur.z != (int)old.z) return EV_OUT_OF_VOXEL;
-        g = trilin(cur, b, c);
-        gm = sqrtf(g.x * g.x + g.y * g.y + g.z * g.z);
-        if (!(gm > 0.f) || !isfinite(gm)) return EV_LOW_GRADIENT;
-        if (gm * step > ms) step = ms / gm;
-        old = cur;
-      }
-      if (gm < P.gthresh) {
-        gm_end = gm;
-        return EV_LOW_GRADIENT;
-      }
-      const float sm = (float)P.step_mult * step;
-      const F3 e1 = {g.x * sm, g.y * sm, g.z * sm};
-      const float hs = sm * 0.5f;
-      const F3 hd = {g.x * hs, g.y * hs, g.z * hs};
-      const F3 hg = trilin({cur.x + hd.x, cur.y + hd.y, cur.z + hd.z}, b, c);
-      const F3 e2 = {hg.x * hs + hd.x, hg.y * hs + hd.y, hg.z * hs + hd.z};
-      const float dx = e2.x - e1.x, dy = e2.y - e1.y, dz = e2.z - e1.z;
-      if (dx * dx + dy * dy + dz * dz < P.ethresh) {
-        F3 np = {cur.x + e2.x, cur.y + e2.y, cur.z + e2.z};
-        if (nearb) {
-          np.x = clampf_ext(np.x, V.X);
-          np.y = clampf_ext(np.y, V.Y);
-          np.z = clampf_ext(np.z, V.Z);
-        }
-        cur = np;
-        step = fminf(step * 1.8f, ms / gm);
-        const int64_t nv = nearest(cur, nearb);
-        if (state) {
-          const uint8_t st = state[nv];
-          if (st == kStSeed || st == kStTerminal) return EV_HIT_PREASSIGNED;
-        } else if (lvl) {
-          if (lvl[nv] < level) return EV_HIT_PREASSIGNED;
-        } else if (lab[nv] != -1) {
-          return EV_HIT_PREASSIGNED;
-        }
-      } else {
-        step = step * 0.5f;
-      }
+    if (!(gm > 0.f) || !isfinite(gm)) return false;
+    step = ms / gm;
+    return true;
+  }
+  // One iteration of the advection loop (one `iters` decrement); EV_NONE to go on.
+  // gm_end: the gradient magnitude at a low-gradient stop (0 where there was none).
+  __device__ __forceinline__ int trip(F3& cur, F3& old, int& iters, bool nearb, const float b[3], const F3 c[8],
+                                      F3& g, float& gm, float& step, float& gm_end) const {
+    if (!(iters-- > 0)) return EV_OVER_MAX_ITERATIONS;
+    if (!(old.x == cur.x && old.y == cur.y && old.z == cur.z)) {
+      if ((int)cur.x != (int)old.x || (int)cur.y != (int)old.y || (int)cur.z != (int)old.z) return EV_OUT_OF_VOXEL;
+      g = trilin(cur, b, c);
+      gm = sqrtf(g.x * g.x + g.y * g.y + g.z * g.z);
+      if (!(gm > 0.f) || !isfinite(gm)) return EV_LOW_GRADIENT;
+      if (gm * step > ms) step = ms / gm;
+      old = cur;
     }
-    return EV_OVER_MAX_ITERATIONS;
+    if (gm < P.gthresh) {
+      gm_end = gm;
+      return EV_LOW_GRADIENT;
+    }
+    const float sm = sgn * step;
+    const F3 e1 = {g.x * sm, g.y * sm, g.z * sm};
+    const float hs = sm * 0.5f;
+    const F3 hd = {g.x * hs, g.y * hs, g.z * hs};
+    const F3 hg = trilin({cur.x + hd.x, cur.y + hd.y, cur.z + hd.z}, b, c);
+    const F3 e2 = {hg.x * hs + hd.x, hg.y * hs + hd.y, hg.z * hs + hd.z};
+    const float dx = e2.x - e1.x, dy = e2.y - e1.y, dz = e2.z - e1.z;
+    if (dx * dx + dy * dy + dz * dz < P.ethresh) {
+      F3 np = {cur.x + e2.x, cur.y + e2.y, cur.z + e2.z};
+      if (nearb) {
+        np.x = clampf_ext(np.x, ext[0]);
+        np.y = clampf_ext(np.y, ext[1]);
+        np.z = clampf_ext(np.z, ext[2]);
+      }
+      cur = np;
+      step = fminf(step * 1.8f, ms / gm);
+      const int64_t nv = nearest(cur, nearb);
+      if (state) {
+        const uint8_t st = state[nv];
+        if (st == kStSeed || st == kStTerminal) return EV_HIT_PREASSIGNED;
+      } else if (lvl) {
+        if (lvl[nv] < level) return EV_HIT_PREASSIGNED;
+      } else if (lab[nv] != -1) {
+        return EV_HIT_PREASSIGNED;
+      }
+    } else {
+      step = step * 0.5f;
+    }
+    return EV_NONE;
   }
 };
 
@@ -159,45 +188,107 @@ __device__ __forceinline__ int dist_to_boundary(const VolDims& V, int64_t x, int
 
 
 constexpr int kPathCap = 48;
+constexpr unsigned kFullMask = 0xffffffffu;
+
+// Streamlines differ in length by orders of magnitude (most end within a few dozen
+// iterations, a few run to the iteration limit circling a sink on a boundary face), so
+// a warp that integrated 32 fixed streamlines would idle most of its lanes behind the
+// longest one.  Instead every lane runs its streamline one iteration per turn of the
+// warp's loop and takes the next work item as soon as its own streamline ends; the
+// items are handed out by one warp-aggregated atomicAdd per turn.
+enum : int { kLaneIdle = 0, kLaneEnter, kLaneStep, kLaneEnd, kLaneDone };
+// resident CTAs of 128 threads per SM for the lane-refilling kernels
+constexpr int kLaneCtasPerSm = 16;
+
+// Claims a work item for every lane of the warp that asks for one (`want`); returns
+// the item of the calling lane (meaningless where it did not ask).
+__device__ __forceinline__ unsigned long long claim_item(bool want, unsigned long long* work) {
+  const unsigned ask = __ballot_sync(kFullMask, want);
+  if (!ask) return 0;
+  const int lane = threadIdx.x & 31;
+  const int leader = __ffs(ask) - 1;
+  unsigned long long base = 0;
+  if (lane == leader) base = atomicAdd(work, (unsigned long long)__popc(ask));
+  base = __shfl_sync(kFullMask, base, leader);
+  return base + (unsigned long long)__popc(ask & ((1u << lane) - 1u));
+}
 
 // One level of the spread order.  Streamlines of a level see only the labels of
 // earlier levels (lvl[v] < level; terminals are level 0, unlabelled vertices 255),
 // so a level's outcome does not depend on thread timing; where several streamlines
 // of the level pass the same unlabelled vertex, the smallest label wins (unsigned
 // atomicMin: a region's id < "reached no region" < unlabelled).  Level by level the
-// pass is therefore deterministic.
+// pass is therefore deterministic.  `work` counts the level's claimed items (zero at
+// launch).
 __global__ void __launch_bounds__(128) integrate_level_kernel(const Adv32 A, int64_t start, int64_t stride, int64_t count,
-                                                              int32_t* __restrict__ lab, uint8_t* __restrict__ lvl) {
+                                                              int32_t* __restrict__ lab, uint8_t* __restrict__ lvl,
+                                                              unsigned long long* __restrict__ work) {
   const VolDims& V = A.V;
   const int level = A.level;
   int path[kPathCap];
-  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < count; t += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t i = start + t * stride;
-    if (lvl[i] < level) continue;  // labelled already
-    int64_t x = i % V.X, y = (i / V.X) % V.Y, z = i / (V.X * V.Y);
-    F3 cur = {(float)x, (float)y, (float)z};
-    int iters = A.P.iteration_limit;
-    int np = 0;
-    path[np++] = (int)i;
-    int64_t end = i;
-    float gm_end;
-    while (true) {
-      const bool nb = dist_to_boundary(V, x, y, z) <= 1;
-      const int ev = A.advect(cur, iters, nb, gm_end);
-      end = A.nearest(cur, nb);
-      x = end % V.X;
-      y = (end / V.X) % V.Y;
-      z = end / (V.X * V.Y);
-      if (np < kPathCap) path[np++] = (int)end;
-      if (ev != EV_OUT_OF_VOXEL) break;
+  int np = 0;
+  int64_t end = 0;
+  int phase = kLaneIdle;
+  int64_t x = 0, y = 0, z = 0;
+  F3 cur = {0.f, 0.f, 0.f}, old = cur, g = cur;
+  float gm = 0.f, step = 0.f, gm_end = 0.f;
+  int iters = 0;
+  bool nb = false;
+  float b[3] = {0.f, 0.f, 0.f};
+  F3 c[8];
+  while (true) {
+    const unsigned long long t = claim_item(phase == kLaneIdle, work);
+    if (phase == kLaneIdle) {
+      if (t >= (unsigned long long)count) {
+        phase = kLaneDone;
+      } else {
+        const int64_t i = start + (int64_t)t * stride;
+        if (lvl[i] >= level) {  // else labelled already: ask again next turn
+          x = i % V.X;
+          y = (i / V.X) % V.Y;
+          z = i / (V.X * V.Y);
+          cur = {(float)x, (float)y, (float)z};
+          iters = A.P.iteration_limit;
+          np = 0;
+          path[np++] = (int)i;
+          phase = kLaneEnter;
+        }
+      }
     }
-    int32_t dest = lvl[end] < level ? lab[end] : -1;
-    if (dest == -1) dest = kLabelNone;  // reached no region: assigned to nothing
-    for (int k = 0; k < np; k++) {
-      const int p = path[k];
-      if (lvl[p] < level) continue;  // labelled in an earlier level: keep
-      atomicMin(reinterpret_cast<unsigned int*>(&lab[p]), (unsigned int)dest);
-      lvl[p] = (uint8_t)level;
+    if (__all_sync(kFullMask, phase == kLaneDone)) break;
+    if (phase == kLaneEnter) {
+      nb = dist_to_boundary(V, x, y, z) <= 1;
+      if (A.enter(cur, nb, b, c, g, gm, step, gm_end)) {
+        old = cur;
+        phase = kLaneStep;
+      } else {
+        phase = kLaneEnd;
+      }
+    }
+    if (phase == kLaneStep) {
+      const int ev = A.trip(cur, old, iters, nb, b, c, g, gm, step, gm_end);
+      if (ev != EV_NONE) {
+        end = A.nearest(cur, nb);
+        x = end % V.X;
+        y = (end / V.X) % V.Y;
+        z = end / (V.X * V.Y);
+        if (np < kPathCap) path[np++] = (int)end;
+        phase = ev == EV_OUT_OF_VOXEL ? kLaneEnter : kLaneEnd;
+      }
+    } else if (phase == kLaneEnd) {  // ended at its voxel entry
+      end = A.nearest(cur, nb);
+      if (np < kPathCap) path[np++] = (int)end;
+    }
+    if (phase == kLaneEnd) {
+      int32_t dest = lvl[end] < level ? lab[end] : -1;
+      if (dest == -1) dest = kLabelNone;  // reached no region: assigned to nothing
+      for (int k = 0; k < np; k++) {
+        const int p = path[k];
+        if (lvl[p] < level) continue;  // labelled in an earlier level: keep
+        atomicMin(reinterpret_cast<unsigned int*>(&lab[p]), (unsigned int)dest);
+        lvl[p] = (uint8_t)level;
+      }
+      phase = kLaneIdle;
     }
   }
 }
@@ -251,8 +342,9 @@ struct Adv64 {
 #pragma unroll
     for (int n = 0; n < 8; n++) c[n] = corner(vv[0][n & 1], vv[1][(n >> 1) & 1], vv[2][n >> 2]);
   }
-  __device__ __forceinline__ static D3 trilin(D3 s, const int64_t b[3], const D3 c[8]) {
-    const double fx = ds(s.x, (double)b[0]), fy = ds(s.y, (double)b[1]), fz = ds(s.z, (double)b[2]);
+  // bf: the base corner as doubles
+  __device__ __forceinline__ static D3 trilin(D3 s, const double bf[3], const D3 c[8]) {
+    const double fx = ds(s.x, bf[0]), fy = ds(s.y, bf[1]), fz = ds(s.z, bf[2]);
     const D3 x0 = dlerp(c[0], c[1], fx), x1 = dlerp(c[2], c[3], fx), x2 = dlerp(c[4], c[5], fx), x3 = dlerp(c[6], c[7], fx);
     return dlerp(dlerp(x0, x1, fy), dlerp(x2, x3, fy), fz);
   }
@@ -260,9 +352,9 @@ struct Adv64 {
     return vid(V, (int64_t)clampd_ext(da(p.x, 0.5), V.X), (int64_t)clampd_ext(da(p.y, 0.5), V.Y),
                (int64_t)clampd_ext(da(p.z, 0.5), V.Z));
   }
-  __device__ int advect(D3& cur, int& iters, bool nearb) const {
-    D3 c[8];
-    D3 old = cur;
+  // The FP32 advector's enter / trip in the reference's FP64 arithmetic.
+  __device__ __forceinline__ bool enter(const D3& cur, bool nearb, double bf[3], D3 c[8], D3& g, float& gm,
+                                        float& step) const {
     int64_t b[3];
     if (nearb) {
       b[0] = (int64_t)clampd_ext(cur.x, V.X);
@@ -274,48 +366,54 @@ struct Adv64 {
       b[2] = (int64_t)fmin(fmax(cur.z, 0.0), (double)(V.Z - 2));
     }
     surround(b, nearb, c);
-    D3 g = trilin(cur, b, c);
-    float gm = __double2float_rn(__dsqrt_rn(magsq(g)));
-    if (!(gm > 0.f) || !isfinite(gm)) return EV_LOW_GRADIENT;  // no direction to follow
-    float step = __double2float_rn(__ddiv_rn(P.max_step, (double)gm));
-    while (iters-- > 0) {
-      if (!(old.x == cur.x && old.y == cur.y && old.z == cur.z)) {
-        if ((int)cur.x != (int)old.x || (int)cur.y != (int)old.y || (int)cur.z != (int)old.z) return EV_OUT_OF_VOXEL;
-        g = trilin(cur, b, c);
-        gm = __double2float_rn(__dsqrt_rn(magsq(g)));
-        if (!(gm > 0.f) || !isfinite(gm)) return EV_LOW_GRADIENT;
-        if ((double)__fmul_rn(gm, step) > P.max_step) step = __double2float_rn(__ddiv_rn(P.max_step, (double)gm));
-        old = cur;
-      }
-      if (gm < P.gthresh) return EV_LOW_GRADIENT;
-      // full step: Vec3d * float multiplies in float (gi_vectors.h:250)
-      const float sm = __fmul_rn((float)P.step_mult, step);
-      const D3 e1 = {(double)__fmul_rn(__double2float_rn(g.x), sm), (double)__fmul_rn(__double2float_rn(g.y), sm),
-                     (double)__fmul_rn(__double2float_rn(g.z), sm)};
-      const double hs = dm((double)step, (double)P.step_mult * 0.5);
-      const D3 hd = {dm(g.x, hs), dm(g.y, hs), dm(g.z, hs)};
-      const D3 hg = trilin({da(cur.x, hd.x), da(cur.y, hd.y), da(cur.z, hd.z)}, b, c);
-      const D3 e2 = {da(dm(hg.x, hs), hd.x), da(dm(hg.y, hs), hd.y), da(dm(hg.z, hs), hd.z)};
-      const D3 df = {ds(e2.x, e1.x), ds(e2.y, e1.y), ds(e2.z, e1.z)};
-      const float err = __double2float_rn(magsq(df));
-      if (err < P.ethresh) {
-        D3 np = {da(cur.x, e2.x), da(cur.y, e2.y), da(cur.z, e2.z)};
-        if (nearb) {
-          np.x = clampd_ext(np.x, V.X);
-          np.y = clampd_ext(np.y, V.Y);
-          np.z = clampd_ext(np.z, V.Z);
-        }
-        cur = np;
-        const float a = __double2float_rn(dm((double)step, 1.8));
-        const float bb = __double2float_rn(__ddiv_rn(P.max_step, (double)gm));
-        step = a < bb ? a : bb;
-        const uint8_t st = state[nearest(cur, nearb)];
-        if (st == kStSeed || st == kStTerminal) return EV_HIT_PREASSIGNED;
-      } else {
-        step = __double2float_rn(dm((double)step, 0.5));
-      }
+    bf[0] = (double)b[0];
+    bf[1] = (double)b[1];
+    bf[2] = (double)b[2];
+    g = trilin(cur, bf, c);
+    gm = __double2float_rn(__dsqrt_rn(magsq(g)));
+    if (!(gm > 0.f) || !isfinite(gm)) return false;  // no direction to follow
+    step = __double2float_rn(__ddiv_rn(P.max_step, (double)gm));
+    return true;
+  }
+  __device__ __forceinline__ int trip(D3& cur, D3& old, int& iters, bool nearb, const double bf[3], const D3 c[8],
+                                      D3& g, float& gm, float& step) const {
+    if (!(iters-- > 0)) return EV_OVER_MAX_ITERATIONS;
+    if (!(old.x == cur.x && old.y == cur.y && old.z == cur.z)) {
+      if ((int)cur.x != (int)old.x || (int)cur.y != (int)old.y || (int)cur.z != (int)old.z) return EV_OUT_OF_VOXEL;
+      g = trilin(cur, bf, c);
+      gm = __double2float_rn(__dsqrt_rn(magsq(g)));
+      if (!(gm > 0.f) || !isfinite(gm)) return EV_LOW_GRADIENT;
+      if ((double)__fmul_rn(gm, step) > P.max_step) step = __double2float_rn(__ddiv_rn(P.max_step, (double)gm));
+      old = cur;
     }
-    return EV_OVER_MAX_ITERATIONS;
+    if (gm < P.gthresh) return EV_LOW_GRADIENT;
+    // full step: Vec3d * float multiplies in float (gi_vectors.h:250)
+    const float sm = __fmul_rn((float)P.step_mult, step);
+    const D3 e1 = {(double)__fmul_rn(__double2float_rn(g.x), sm), (double)__fmul_rn(__double2float_rn(g.y), sm),
+                   (double)__fmul_rn(__double2float_rn(g.z), sm)};
+    const double hs = dm((double)step, (double)P.step_mult * 0.5);
+    const D3 hd = {dm(g.x, hs), dm(g.y, hs), dm(g.z, hs)};
+    const D3 hg = trilin({da(cur.x, hd.x), da(cur.y, hd.y), da(cur.z, hd.z)}, bf, c);
+    const D3 e2 = {da(dm(hg.x, hs), hd.x), da(dm(hg.y, hs), hd.y), da(dm(hg.z, hs), hd.z)};
+    const D3 df = {ds(e2.x, e1.x), ds(e2.y, e1.y), ds(e2.z, e1.z)};
+    const float err = __double2float_rn(magsq(df));
+    if (err < P.ethresh) {
+      D3 np = {da(cur.x, e2.x), da(cur.y, e2.y), da(cur.z, e2.z)};
+      if (nearb) {
+        np.x = clampd_ext(np.x, V.X);
+        np.y = clampd_ext(np.y, V.Y);
+        np.z = clampd_ext(np.z, V.Z);
+      }
+      cur = np;
+      const float a = __double2float_rn(dm((double)step, 1.8));
+      const float bb = __double2float_rn(__ddiv_rn(P.max_step, (double)gm));
+      step = a < bb ? a : bb;
+      const uint8_t st = state[nearest(cur, nearb)];
+      if (st == kStSeed || st == kStTerminal) return EV_HIT_PREASSIGNED;
+    } else {
+      step = __double2float_rn(dm((double)step, 0.5));
+    }
+    return EV_NONE;
   }
 };
 
@@ -348,35 +446,68 @@ __global__ void boundary_set_kernel(const int32_t* __restrict__ lab, const uint8
 __global__ void __launch_bounds__(128) fixup_kernel(const Adv64 A, int32_t* __restrict__ lab,
                                                     const int32_t* __restrict__ lab0, uint8_t* __restrict__ state,
                                                     const int64_t* __restrict__ list, int n, int64_t* __restrict__ next,
-                                                    int* __restrict__ n_next, uint32_t* __restrict__ queued) {
+                                                    int* __restrict__ n_next, uint32_t* __restrict__ queued,
+                                                    unsigned long long* __restrict__ work) {
   const VolDims& V = A.V;
-  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
-    const int64_t v = list[k];
-    atomicAnd(&queued[v >> 5], ~(1u << (v & 31)));
-    const int32_t init = lab[v];
-    int64_t x = v % V.X, y = (v / V.X) % V.Y, z = v / (V.X * V.Y);
-    D3 cur = {(double)x, (double)y, (double)z};
-    int iters = A.P.iteration_limit;
-    int64_t end = v;
-    while (true) {
-      const bool nb = dist_to_boundary(V, x, y, z) <= 1;
-      const int ev = A.advect(cur, iters, nb);
-      end = A.nearest(cur, nb);
-      x = end % V.X;
-      y = (end / V.X) % V.Y;
-      z = end / (V.X * V.Y);
-      if (ev != EV_OUT_OF_VOXEL) break;
+  int phase = kLaneIdle;
+  int64_t v = 0, x = 0, y = 0, z = 0;
+  int32_t init = 0;
+  D3 cur = {0.0, 0.0, 0.0}, old = cur, g = cur;
+  float gm = 0.f, step = 0.f;
+  int iters = 0;
+  bool nb = false;
+  double b[3] = {0.0, 0.0, 0.0};
+  D3 c[8];
+  while (true) {
+    const unsigned long long k = claim_item(phase == kLaneIdle, work);
+    if (phase == kLaneIdle) {
+      if (k >= (unsigned long long)n) {
+        phase = kLaneDone;
+      } else {
+        v = list[k];
+        atomicAnd(&queued[v >> 5], ~(1u << (v & 31)));
+        init = lab[v];
+        x = v % V.X;
+        y = (v / V.X) % V.Y;
+        z = v / (V.X * V.Y);
+        cur = {(double)x, (double)y, (double)z};
+        iters = A.P.iteration_limit;
+        phase = kLaneEnter;
+      }
     }
+    if (__all_sync(kFullMask, phase == kLaneDone)) break;
+    if (phase == kLaneEnter) {
+      nb = dist_to_boundary(V, x, y, z) <= 1;
+      if (A.enter(cur, nb, b, c, g, gm, step)) {
+        old = cur;
+        phase = kLaneStep;
+      } else {
+        phase = kLaneEnd;
+      }
+    }
+    if (phase == kLaneStep) {
+      const int ev = A.trip(cur, old, iters, nb, b, c, g, gm, step);
+      if (ev == EV_OUT_OF_VOXEL) {
+        const int64_t e = A.nearest(cur, nb);
+        x = e % V.X;
+        y = (e / V.X) % V.Y;
+        z = e / (V.X * V.Y);
+        phase = kLaneEnter;
+      } else if (ev != EV_NONE) {
+        phase = kLaneEnd;
+      }
+    }
+    if (phase != kLaneEnd) continue;
+    phase = kLaneIdle;
+    const int64_t end = A.nearest(cur, nb);
     int32_t nl = lab0[end];
     if (nl == -1) nl = kLabelNone;
     lab[v] = nl;
     state[v] = kStNonterminal;
     if (nl == init) continue;
-    x = v % V.X;
-    y = (v / V.X) % V.Y;
-    z = v / (V.X * V.Y);
-    const int64_t nbr[6] = {x < V.X - 1 ? v + 1 : -1, x > 0 ? v - 1 : -1, y < V.Y - 1 ? v + V.X : -1,
-                            y > 0 ? v - V.X : -1, z < V.Z - 1 ? v + V.X * V.Y : -1, z > 0 ? v - V.X * V.Y : -1};
+    const int64_t vx = v % V.X, vy = (v / V.X) % V.Y, vz = v / (V.X * V.Y);
+    const int64_t nbr[6] = {vx < V.X - 1 ? v + 1 : -1, vx > 0 ? v - 1 : -1, vy < V.Y - 1 ? v + V.X : -1,
+                            vy > 0 ? v - V.X : -1, vz < V.Z - 1 ? v + V.X * V.Y : -1, vz > 0 ? v - V.X * V.Y : -1};
 #pragma unroll
     for (int j = 0; j < 6; j++) {
       const int64_t u = nbr[j];
@@ -402,26 +533,63 @@ __global__ void __launch_bounds__(128) fixup32_kernel(const Adv32 A, int32_t* __
                                                       const int64_t* __restrict__ list, int n,
                                                       int64_t* __restrict__ next, int* __restrict__ n_next,
                                                       uint32_t* __restrict__ queued, int64_t* __restrict__ amb,
-                                                      int* __restrict__ n_amb, int amb_mode) {
+                                                      int* __restrict__ n_amb, int amb_mode,
+                                                      unsigned long long* __restrict__ work) {
   const VolDims& V = A.V;
-  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
-    const int64_t v = list[k];
-    const int32_t init = lab[v];
-    int64_t x = v % V.X, y = (v / V.X) % V.Y, z = v / (V.X * V.Y);
-    F3 cur = {(float)x, (float)y, (float)z};
-    int iters = A.P.iteration_limit;
-    int64_t end = v;
-    int ev;
-    float gm_end = 0.f;
-    while (true) {
-      const bool nb = dist_to_boundary(V, x, y, z) <= 1;
-      ev = A.advect(cur, iters, nb, gm_end);
-      end = A.nearest(cur, nb);
-      x = end % V.X;
-      y = (end / V.X) % V.Y;
-      z = end / (V.X * V.Y);
-      if (ev != EV_OUT_OF_VOXEL) break;
+  int phase = kLaneIdle;
+  int64_t v = 0, x = 0, y = 0, z = 0;
+  int32_t init = 0;
+  F3 cur = {0.f, 0.f, 0.f}, old = cur, g = cur;
+  float gm = 0.f, step = 0.f, gm_end = 0.f;
+  int iters = 0, ev = EV_NONE;
+  bool nb = false;
+  float b[3] = {0.f, 0.f, 0.f};
+  F3 c[8];
+  while (true) {
+    const unsigned long long k = claim_item(phase == kLaneIdle, work);
+    if (phase == kLaneIdle) {
+      if (k >= (unsigned long long)n) {
+        phase = kLaneDone;
+      } else {
+        v = list[k];
+        init = lab[v];
+        x = v % V.X;
+        y = (v / V.X) % V.Y;
+        z = v / (V.X * V.Y);
+        cur = {(float)x, (float)y, (float)z};
+        iters = A.P.iteration_limit;
+        phase = kLaneEnter;
+      }
     }
+    if (__all_sync(kFullMask, phase == kLaneDone)) break;
+    if (phase == kLaneEnter) {
+      nb = dist_to_boundary(V, x, y, z) <= 1;
+      if (A.enter(cur, nb, b, c, g, gm, step, gm_end)) {
+        old = cur;
+        phase = kLaneStep;
+      } else {
+        ev = EV_LOW_GRADIENT;
+        phase = kLaneEnd;
+      }
+    }
+    if (phase == kLaneStep) {
+      ev = A.trip(cur, old, iters, nb, b, c, g, gm, step, gm_end);
+      if (ev == EV_OUT_OF_VOXEL) {
+        const int64_t e = A.nearest(cur, nb);
+        x = e % V.X;
+        y = (e / V.X) % V.Y;
+        z = e / (V.X * V.Y);
+        phase = kLaneEnter;
+      } else if (ev != EV_NONE) {
+        phase = kLaneEnd;
+      }
+    }
+    if (phase != kLaneEnd) continue;
+    phase = kLaneIdle;
+    const int64_t end = A.nearest(cur, nb);
+    x = end % V.X;
+    y = (end / V.X) % V.Y;
+    z = end / (V.X * V.Y);
     // a low-gradient stop whose FP32 magnitude lies within 2^-8 (relative) of the
     // threshold: FP32 rounding could have taken the other side of the stop test.  A
     // streamline that decelerates into an extremum crosses the threshold well inside
@@ -446,13 +614,12 @@ __global__ void __launch_bounds__(128) fixup32_kernel(const Adv32 A, int32_t* __
         if ((st == kStSeed || st == kStTerminal) && lab0[u] != le) ambiguous = true;
       }
     } else if (!ambiguous && ev == EV_HIT_PREASSIGNED) {
-      const int64_t b[3] = {(int64_t)fminf(fmaxf(cur.x, 0.f), (float)(V.X - 2)),
-                            (int64_t)fminf(fmaxf(cur.y, 0.f), (float)(V.Y - 2)),
-                            (int64_t)fminf(fmaxf(cur.z, 0.f), (float)(V.Z - 2))};
+      const int64_t bb[3] = {(int)fminf(fmaxf(cur.x, 0.f), A.ext2[0]), (int)fminf(fmaxf(cur.y, 0.f), A.ext2[1]),
+                             (int)fminf(fmaxf(cur.z, 0.f), A.ext2[2])};
       int32_t seen = kLabelNone;
 #pragma unroll
-      for (int c = 0; c < 8; c++) {
-        const int64_t u = vid(V, b[0] + (c & 1), b[1] + ((c >> 1) & 1), b[2] + (c >> 2));
+      for (int q = 0; q < 8; q++) {
+        const int64_t u = vid(V, bb[0] + (q & 1), bb[1] + ((q >> 1) & 1), bb[2] + (q >> 2));
         const uint8_t st = state[u];
         if (st != kStSeed && st != kStTerminal) continue;
         const int32_t l = lab0[u];
@@ -470,11 +637,9 @@ __global__ void __launch_bounds__(128) fixup32_kernel(const Adv32 A, int32_t* __
     lab[v] = nl;
     state[v] = kStNonterminal;
     if (nl == init) continue;
-    x = v % V.X;
-    y = (v / V.X) % V.Y;
-    z = v / (V.X * V.Y);
-    const int64_t nbr[6] = {x < V.X - 1 ? v + 1 : -1, x > 0 ? v - 1 : -1, y < V.Y - 1 ? v + V.X : -1,
-                            y > 0 ? v - V.X : -1, z < V.Z - 1 ? v + V.X * V.Y : -1, z > 0 ? v - V.X * V.Y : -1};
+    const int64_t vx = v % V.X, vy = (v / V.X) % V.Y, vz = v / (V.X * V.Y);
+    const int64_t nbr[6] = {vx < V.X - 1 ? v + 1 : -1, vx > 0 ? v - 1 : -1, vy < V.Y - 1 ? v + V.X : -1,
+                            vy > 0 ? v - V.X : -1, vz < V.Z - 1 ? v + V.X * V.Y : -1, vz > 0 ? v - V.X * V.Y : -1};
 #pragma unroll
     for (int j = 0; j < 6; j++) {
       const int64_t u = nbr[j];
@@ -582,18 +747,20 @@ __global__ void clean_resolve_kernel(const int32_t* __restrict__ lab, const VolD
 // ---- launchers ---------------------------------------------------------------------------
 
 cudaError_t launch_integrate_pass1(const float4* G, const VolDims& V, const IntegParams& P, const SpreadOrder& S,
-                                   int32_t* lab, uint8_t* lvl, int num_sms, cudaStream_t stream) {
+                                   int32_t* lab, uint8_t* lvl, unsigned long long* work, int num_sms,
+                                   cudaStream_t stream) {
   const int64_t N = V.X * V.Y * V.Z;
+  if (cudaError_t e = cudaMemsetAsync(work, 0, sizeof(unsigned long long) * 48, stream)) return e;
   ::msc::count_launch();
   init_levels_kernel<<<num_sms * 8, 256, 0, stream>>>(lab, lvl, N);
   for (int L = 0; L < S.nlev; L++) {
     const int64_t count = S.offset[L + 1] - S.offset[L];
     if (count <= 0) continue;
-    Adv32 A{G, V, P, lab, lvl, L + 1, nullptr};
+    const Adv32 A = Adv32::make(G, V, P, lab, lvl, L + 1, nullptr);
     const int64_t blocks = (count + 127) / 128;
-    const int grid = (int)(blocks < num_sms * 16 ? blocks : num_sms * 16);
+    const int grid = (int)(blocks < num_sms * kLaneCtasPerSm ? blocks : num_sms * kLaneCtasPerSm);
     ::msc::count_launch();
-    integrate_level_kernel<<<grid, 128, 0, stream>>>(A, S.start[L], S.stride[L], count, lab, lvl);
+    integrate_level_kernel<<<grid, 128, 0, stream>>>(A, S.start[L], S.stride[L], count, lab, lvl, work + L);
   }
   return cudaGetLastError();
 }
@@ -607,26 +774,28 @@ cudaError_t launch_boundary_set(const int32_t* lab, const uint8_t* state, const 
 
 cudaError_t launch_fixup(const double* G, const VolDims& V, const IntegParams& P, int32_t* lab, const int32_t* lab0,
                          uint8_t* state, const int64_t* list, int n, int64_t* next, int* n_next, uint32_t* queued,
-                         int num_sms, cudaStream_t stream) {
+                         unsigned long long* work, int num_sms, cudaStream_t stream) {
   if (n <= 0) return cudaSuccess;
   Adv64 A{G, V, P, state};
   const int blocks = (n + 127) / 128;
+  if (cudaError_t e = cudaMemsetAsync(work, 0, sizeof(unsigned long long), stream)) return e;
   ::msc::count_launch();
-  fixup_kernel<<<blocks < num_sms * 16 ? blocks : num_sms * 16, 128, 0, stream>>>(A, lab, lab0, state, list, n, next,
-                                                                                  n_next, queued);
+  fixup_kernel<<<blocks < num_sms * kLaneCtasPerSm ? blocks : num_sms * kLaneCtasPerSm, 128, 0, stream>>>(
+      A, lab, lab0, state, list, n, next, n_next, queued, work);
   return cudaGetLastError();
 }
 
 cudaError_t launch_fixup32(const float4* G, const VolDims& V, const IntegParams& P, int32_t* lab, const int32_t* lab0,
                            uint8_t* state, const int64_t* list, int n, int64_t* next, int* n_next, uint32_t* queued,
-                           int64_t* amb, int* n_amb, int amb_mode, int num_sms, cudaStream_t stream) {
+                           int64_t* amb, int* n_amb, int amb_mode, unsigned long long* work, int num_sms,
+                           cudaStream_t stream) {
   if (n <= 0) return cudaSuccess;
-  Adv32 A{G, V, P, lab, nullptr, 0, state};
+  const Adv32 A = Adv32::make(G, V, P, lab, nullptr, 0, state);
   const int blocks = (n + 127) / 128;
+  if (cudaError_t e = cudaMemsetAsync(work, 0, sizeof(unsigned long long), stream)) return e;
   ::msc::count_launch();
-  fixup32_kernel<<<blocks < num_sms * 16 ? blocks : num_sms * 16, 128, 0, stream>>>(A, lab, lab0, state, list, n, next,
-                                                                                    n_next, queued, amb, n_amb,
-                                                                                    amb_mode);
+  fixup32_kernel<<<blocks < num_sms * kLaneCtasPerSm ? blocks : num_sms * kLaneCtasPerSm, 128, 0, stream>>>(
+      A, lab, lab0, state, list, n, next, n_next, queued, amb, n_amb, amb_mode, work);
   return cudaGetLastError();
 }
 

@@ -183,6 +183,7 @@ struct LabelCtx {
   uint32_t* queued = nullptr;
   uint8_t* tiles = nullptr;
   int* counters = nullptr;  // [0] n_ext [1] n_sad [2] n_arcs [3] changed [4] err [5] n_list [6] n_next [7] n_amb
+  unsigned long long* work = nullptr;  // claimed work items of the integration kernels (48)
   explicit LabelCtx(cudaStream_t s) : st(s), pool(s) {}
 };
 
@@ -223,6 +224,7 @@ int setup_ctx(LabelCtx& c, const float* f, const uint8_t* grad, const int64_t* d
   LCUDA(c.pool.get(&c.queued, N / 32 + 1), "alloc");
   LCUDA(c.pool.get(&c.tiles, 2 * c.ntiles), "alloc");
   LCUDA(c.pool.get(&c.counters, 8), "alloc");
+  LCUDA(c.pool.get(&c.work, 48), "alloc");
   LCUDA(cudaMemsetAsync(c.counters, 0, 8 * sizeof(int), c.st), "memset");
   msc::GradDims GD{};
   for (int a = 0; a < 3; a++) {
@@ -346,7 +348,7 @@ int first_pass(LabelCtx& c, DirLabels& d) {
   }
   uint8_t* lvl;
   LCUDA(c.pool.get(&lvl, N), "alloc");
-  LCUDA(msc::launch_integrate_pass1(c.g32, c.V, P, S, d.lab, lvl, c.sms, st), "integrate");
+  LCUDA(msc::launch_integrate_pass1(c.g32, c.V, P, S, d.lab, lvl, c.work, c.sms, st), "integrate");
   return MSC_OK;
 }
 
@@ -379,17 +381,18 @@ int finish_direction(LabelCtx& c, DirLabels& d, int32_t* out, int32_t* stage_int
     if (waves > N) return fail(MSC_ERR_ITER_LIMIT, "fix-up did not converge");
     LCUDA(cudaMemsetAsync(c.counters + 6, 0, 2 * sizeof(int), st), "memset");
     if (p->precision == 1) {
-      LCUDA(msc::launch_fixup(c.g64, V, P, d.lab, lab0, d.state, cur, n_list, nxt, c.counters + 6, c.queued, sms, st),
+      LCUDA(msc::launch_fixup(c.g64, V, P, d.lab, lab0, d.state, cur, n_list, nxt, c.counters + 6, c.queued, c.work,
+                              sms, st),
             "fix-up");
     } else {
       LCUDA(msc::launch_fixup32(c.g32, V, P, d.lab, lab0, d.state, cur, n_list, nxt, c.counters + 6, c.queued, c.amb,
-                                c.counters + 7, p->precision == 2 ? 2 : 0, sms, st),
+                                c.counters + 7, p->precision == 2 ? 2 : 0, c.work, sms, st),
             "fix-up");
       int n_amb = 0;
       if (int rc = read_int(c.counters + 7, &n_amb, st)) return rc;
       stats[1] += n_amb;
-      LCUDA(msc::launch_fixup(c.g64, V, P, d.lab, lab0, d.state, c.amb, n_amb, nxt, c.counters + 6, c.queued, sms,
-                              st),
+      LCUDA(msc::launch_fixup(c.g64, V, P, d.lab, lab0, d.state, c.amb, n_amb, nxt, c.counters + 6, c.queued, c.work,
+                              sms, st),
             "fix-up");
     }
     stats[0] += n_list;
