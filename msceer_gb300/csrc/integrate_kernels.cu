@@ -18,6 +18,8 @@
 //   components' first vertices in the walk order; every component that does not hold
 //   its region's extremum joins the component of its first earlier neighbour from
 //   another region; chains resolve by pointer jumping.
+#include <cstdlib>
+
 #include "label_common.cuh"
 
 namespace msc {
@@ -97,9 +99,15 @@ struct Adv32 {
   }
   // Vec3l(p + 0.5), clamped into the grid (the reference clamps only near the
   // boundary, where its own points can leave it; elsewhere clamping changes nothing)
+  __device__ __forceinline__ void nearest3(F3 p, int& ix, int& iy, int& iz) const {
+    ix = (int)clampf_ext(p.x + 0.5f, ext[0]);
+    iy = (int)clampf_ext(p.y + 0.5f, ext[1]);
+    iz = (int)clampf_ext(p.z + 0.5f, ext[2]);
+  }
   __device__ __forceinline__ int64_t nearest(F3 p, bool) const {
-    return vid(V, (int)clampf_ext(p.x + 0.5f, ext[0]), (int)clampf_ext(p.y + 0.5f, ext[1]),
-               (int)clampf_ext(p.z + 0.5f, ext[2]));
+    int ix, iy, iz;
+    nearest3(p, ix, iy, iz);
+    return vid(V, ix, iy, iz);
   }
   // AdvectThroughVoxel{NoCheck,NearBoundary} split in two, so that a lane can run its
   // streamline one iteration at a time.  enter(): the voxel's base corner, its eight
@@ -187,6 +195,21 @@ __device__ __forceinline__ int dist_to_boundary(const VolDims& V, int64_t x, int
 }
 
 
+// Vertex coordinates of index v; 32-bit division while the grid's indices fit 32 bits.
+__device__ __forceinline__ void split_index(const VolDims& V, int64_t v, int& x, int& y, int& z) {
+  if (V.X * V.Y * V.Z <= (int64_t)0xFFFFFFFF) {
+    const uint32_t u = (uint32_t)v, X = (uint32_t)V.X, Y = (uint32_t)V.Y;
+    const uint32_t r = u / X;
+    x = (int)(u - r * X);
+    y = (int)(r % Y);
+    z = (int)(r / Y);
+  } else {
+    x = (int)(v % V.X);
+    y = (int)((v / V.X) % V.Y);
+    z = (int)(v / (V.X * V.Y));
+  }
+}
+
 constexpr int kPathCap = 48;
 constexpr unsigned kFullMask = 0xffffffffu;
 
@@ -220,6 +243,7 @@ __device__ __forceinline__ unsigned long long claim_item(bool want, unsigned lon
 // atomicMin: a region's id < "reached no region" < unlabelled).  Level by level the
 // pass is therefore deterministic.  `work` counts the level's claimed items (zero at
 // launch).
+template <int K>
 __global__ void __launch_bounds__(128) integrate_level_kernel(const Adv32 A, int64_t start, int64_t stride, int64_t count,
                                                               int32_t* __restrict__ lab, uint8_t* __restrict__ lvl,
                                                               unsigned long long* __restrict__ work) {
@@ -229,7 +253,7 @@ __global__ void __launch_bounds__(128) integrate_level_kernel(const Adv32 A, int
   int np = 0;
   int64_t end = 0;
   int phase = kLaneIdle;
-  int64_t x = 0, y = 0, z = 0;
+  int x = 0, y = 0, z = 0;
   F3 cur = {0.f, 0.f, 0.f}, old = cur, g = cur;
   float gm = 0.f, step = 0.f, gm_end = 0.f;
   int iters = 0;
@@ -244,9 +268,7 @@ __global__ void __launch_bounds__(128) integrate_level_kernel(const Adv32 A, int
       } else {
         const int64_t i = start + (int64_t)t * stride;
         if (lvl[i] >= level) {  // else labelled already: ask again next turn
-          x = i % V.X;
-          y = (i / V.X) % V.Y;
-          z = i / (V.X * V.Y);
+          split_index(V, i, x, y, z);
           cur = {(float)x, (float)y, (float)z};
           iters = A.P.iteration_limit;
           np = 0;
@@ -262,22 +284,22 @@ __global__ void __launch_bounds__(128) integrate_level_kernel(const Adv32 A, int
         old = cur;
         phase = kLaneStep;
       } else {
+        A.nearest3(cur, x, y, z);  // ended at its voxel entry
+        end = vid(V, x, y, z);
+        if (np < kPathCap) path[np++] = (int)end;
         phase = kLaneEnd;
       }
     }
     if (phase == kLaneStep) {
-      const int ev = A.trip(cur, old, iters, nb, b, c, g, gm, step, gm_end);
-      if (ev != EV_NONE) {
-        end = A.nearest(cur, nb);
-        x = end % V.X;
-        y = (end / V.X) % V.Y;
-        z = end / (V.X * V.Y);
+      for (int r = 0; r < K; r++) {
+        const int ev = A.trip(cur, old, iters, nb, b, c, g, gm, step, gm_end);
+        if (ev == EV_NONE) continue;
+        A.nearest3(cur, x, y, z);
+        end = vid(V, x, y, z);
         if (np < kPathCap) path[np++] = (int)end;
         phase = ev == EV_OUT_OF_VOXEL ? kLaneEnter : kLaneEnd;
+        break;
       }
-    } else if (phase == kLaneEnd) {  // ended at its voxel entry
-      end = A.nearest(cur, nb);
-      if (np < kPathCap) path[np++] = (int)end;
     }
     if (phase == kLaneEnd) {
       int32_t dest = lvl[end] < level ? lab[end] : -1;
@@ -348,9 +370,15 @@ struct Adv64 {
     const D3 x0 = dlerp(c[0], c[1], fx), x1 = dlerp(c[2], c[3], fx), x2 = dlerp(c[4], c[5], fx), x3 = dlerp(c[6], c[7], fx);
     return dlerp(dlerp(x0, x1, fy), dlerp(x2, x3, fy), fz);
   }
+  __device__ __forceinline__ void nearest3(D3 p, int& ix, int& iy, int& iz) const {
+    ix = (int)(int64_t)clampd_ext(da(p.x, 0.5), V.X);
+    iy = (int)(int64_t)clampd_ext(da(p.y, 0.5), V.Y);
+    iz = (int)(int64_t)clampd_ext(da(p.z, 0.5), V.Z);
+  }
   __device__ __forceinline__ int64_t nearest(D3 p, bool) const {
-    return vid(V, (int64_t)clampd_ext(da(p.x, 0.5), V.X), (int64_t)clampd_ext(da(p.y, 0.5), V.Y),
-               (int64_t)clampd_ext(da(p.z, 0.5), V.Z));
+    int ix, iy, iz;
+    nearest3(p, ix, iy, iz);
+    return vid(V, ix, iy, iz);
   }
   // The FP32 advector's enter / trip in the reference's FP64 arithmetic.
   __device__ __forceinline__ bool enter(const D3& cur, bool nearb, double bf[3], D3 c[8], D3& g, float& gm,
@@ -443,6 +471,7 @@ __global__ void boundary_set_kernel(const int32_t* __restrict__ lab, const uint8
 // certain terminal that is the region's label (never changed), and at any other
 // ending (low gradient, iteration limit) it is a value no concurrent re-decision can
 // be rewriting, so every wave's outcome is independent of thread timing.
+template <int K>
 __global__ void __launch_bounds__(128) fixup_kernel(const Adv64 A, int32_t* __restrict__ lab,
                                                     const int32_t* __restrict__ lab0, uint8_t* __restrict__ state,
                                                     const int64_t* __restrict__ list, int n, int64_t* __restrict__ next,
@@ -450,7 +479,8 @@ __global__ void __launch_bounds__(128) fixup_kernel(const Adv64 A, int32_t* __re
                                                     unsigned long long* __restrict__ work) {
   const VolDims& V = A.V;
   int phase = kLaneIdle;
-  int64_t v = 0, x = 0, y = 0, z = 0;
+  int64_t v = 0;
+  int x = 0, y = 0, z = 0;
   int32_t init = 0;
   D3 cur = {0.0, 0.0, 0.0}, old = cur, g = cur;
   float gm = 0.f, step = 0.f;
@@ -467,9 +497,7 @@ __global__ void __launch_bounds__(128) fixup_kernel(const Adv64 A, int32_t* __re
         v = list[k];
         atomicAnd(&queued[v >> 5], ~(1u << (v & 31)));
         init = lab[v];
-        x = v % V.X;
-        y = (v / V.X) % V.Y;
-        z = v / (V.X * V.Y);
+        split_index(V, v, x, y, z);
         cur = {(double)x, (double)y, (double)z};
         iters = A.P.iteration_limit;
         phase = kLaneEnter;
@@ -482,30 +510,29 @@ __global__ void __launch_bounds__(128) fixup_kernel(const Adv64 A, int32_t* __re
         old = cur;
         phase = kLaneStep;
       } else {
+        A.nearest3(cur, x, y, z);
         phase = kLaneEnd;
       }
     }
     if (phase == kLaneStep) {
-      const int ev = A.trip(cur, old, iters, nb, b, c, g, gm, step);
-      if (ev == EV_OUT_OF_VOXEL) {
-        const int64_t e = A.nearest(cur, nb);
-        x = e % V.X;
-        y = (e / V.X) % V.Y;
-        z = e / (V.X * V.Y);
-        phase = kLaneEnter;
-      } else if (ev != EV_NONE) {
-        phase = kLaneEnd;
+      for (int r = 0; r < K; r++) {
+        const int ev = A.trip(cur, old, iters, nb, b, c, g, gm, step);
+        if (ev == EV_NONE) continue;
+        A.nearest3(cur, x, y, z);
+        phase = ev == EV_OUT_OF_VOXEL ? kLaneEnter : kLaneEnd;
+        break;
       }
     }
     if (phase != kLaneEnd) continue;
     phase = kLaneIdle;
-    const int64_t end = A.nearest(cur, nb);
+    const int64_t end = vid(V, x, y, z);
     int32_t nl = lab0[end];
     if (nl == -1) nl = kLabelNone;
     lab[v] = nl;
     state[v] = kStNonterminal;
     if (nl == init) continue;
-    const int64_t vx = v % V.X, vy = (v / V.X) % V.Y, vz = v / (V.X * V.Y);
+    int vx, vy, vz;
+    split_index(V, v, vx, vy, vz);
     const int64_t nbr[6] = {vx < V.X - 1 ? v + 1 : -1, vx > 0 ? v - 1 : -1, vy < V.Y - 1 ? v + V.X : -1,
                             vy > 0 ? v - V.X : -1, vz < V.Z - 1 ? v + V.X * V.Y : -1, vz > 0 ? v - V.X * V.Y : -1};
 #pragma unroll
@@ -528,6 +555,7 @@ __global__ void __launch_bounds__(128) fixup_kernel(const Adv64 A, int32_t* __re
 //     different certain region (FP32 rounding may have picked the wrong side);
 //   amb_mode 2: its final voxel touches two different certain regions (any ending
 //     within half a voxel of a basin boundary).
+template <int K>
 __global__ void __launch_bounds__(128) fixup32_kernel(const Adv32 A, int32_t* __restrict__ lab,
                                                       const int32_t* __restrict__ lab0, uint8_t* __restrict__ state,
                                                       const int64_t* __restrict__ list, int n,
@@ -537,7 +565,8 @@ __global__ void __launch_bounds__(128) fixup32_kernel(const Adv32 A, int32_t* __
                                                       unsigned long long* __restrict__ work) {
   const VolDims& V = A.V;
   int phase = kLaneIdle;
-  int64_t v = 0, x = 0, y = 0, z = 0;
+  int64_t v = 0;
+  int x = 0, y = 0, z = 0;
   int32_t init = 0;
   F3 cur = {0.f, 0.f, 0.f}, old = cur, g = cur;
   float gm = 0.f, step = 0.f, gm_end = 0.f;
@@ -553,9 +582,7 @@ __global__ void __launch_bounds__(128) fixup32_kernel(const Adv32 A, int32_t* __
       } else {
         v = list[k];
         init = lab[v];
-        x = v % V.X;
-        y = (v / V.X) % V.Y;
-        z = v / (V.X * V.Y);
+        split_index(V, v, x, y, z);
         cur = {(float)x, (float)y, (float)z};
         iters = A.P.iteration_limit;
         phase = kLaneEnter;
@@ -569,27 +596,22 @@ __global__ void __launch_bounds__(128) fixup32_kernel(const Adv32 A, int32_t* __
         phase = kLaneStep;
       } else {
         ev = EV_LOW_GRADIENT;
+        A.nearest3(cur, x, y, z);
         phase = kLaneEnd;
       }
     }
     if (phase == kLaneStep) {
-      ev = A.trip(cur, old, iters, nb, b, c, g, gm, step, gm_end);
-      if (ev == EV_OUT_OF_VOXEL) {
-        const int64_t e = A.nearest(cur, nb);
-        x = e % V.X;
-        y = (e / V.X) % V.Y;
-        z = e / (V.X * V.Y);
-        phase = kLaneEnter;
-      } else if (ev != EV_NONE) {
-        phase = kLaneEnd;
+      for (int r = 0; r < K; r++) {
+        ev = A.trip(cur, old, iters, nb, b, c, g, gm, step, gm_end);
+        if (ev == EV_NONE) continue;
+        A.nearest3(cur, x, y, z);
+        phase = ev == EV_OUT_OF_VOXEL ? kLaneEnter : kLaneEnd;
+        break;
       }
     }
     if (phase != kLaneEnd) continue;
     phase = kLaneIdle;
-    const int64_t end = A.nearest(cur, nb);
-    x = end % V.X;
-    y = (end / V.X) % V.Y;
-    z = end / (V.X * V.Y);
+    const int64_t end = vid(V, x, y, z);
     // a low-gradient stop whose FP32 magnitude lies within 2^-8 (relative) of the
     // threshold: FP32 rounding could have taken the other side of the stop test.  A
     // streamline that decelerates into an extremum crosses the threshold well inside
@@ -637,7 +659,8 @@ __global__ void __launch_bounds__(128) fixup32_kernel(const Adv32 A, int32_t* __
     lab[v] = nl;
     state[v] = kStNonterminal;
     if (nl == init) continue;
-    const int64_t vx = v % V.X, vy = (v / V.X) % V.Y, vz = v / (V.X * V.Y);
+    int vx, vy, vz;
+    split_index(V, v, vx, vy, vz);
     const int64_t nbr[6] = {vx < V.X - 1 ? v + 1 : -1, vx > 0 ? v - 1 : -1, vy < V.Y - 1 ? v + V.X : -1,
                             vy > 0 ? v - V.X : -1, vz < V.Z - 1 ? v + V.X * V.Y : -1, vz > 0 ? v - V.X * V.Y : -1};
 #pragma unroll
@@ -746,6 +769,18 @@ __global__ void clean_resolve_kernel(const int32_t* __restrict__ lab, const VolD
 
 // ---- launchers ---------------------------------------------------------------------------
 
+// Stepping iterations per turn of the lane-refilling loops: more amortise the turn's
+// hand-out and voxel-entry work, fewer leave less idle time after a lane's event.
+// MSC_TRIPS_PER_TURN (1, 2, 4 or 8) overrides the default for tuning.
+int trips_per_turn() {
+  static const int k = [] {
+    const char* e = std::getenv("MSC_TRIPS_PER_TURN");
+    const int v = e ? std::atoi(e) : 4;
+    return (v == 1 || v == 2 || v == 8) ? v : 4;
+  }();
+  return k;
+}
+
 cudaError_t launch_integrate_pass1(const float4* G, const VolDims& V, const IntegParams& P, const SpreadOrder& S,
                                    int32_t* lab, uint8_t* lvl, unsigned long long* work, int num_sms,
                                    cudaStream_t stream) {
@@ -760,7 +795,19 @@ cudaError_t launch_integrate_pass1(const float4* G, const VolDims& V, const Inte
     const int64_t blocks = (count + 127) / 128;
     const int grid = (int)(blocks < num_sms * kLaneCtasPerSm ? blocks : num_sms * kLaneCtasPerSm);
     ::msc::count_launch();
-    integrate_level_kernel<<<grid, 128, 0, stream>>>(A, S.start[L], S.stride[L], count, lab, lvl, work + L);
+    switch (trips_per_turn()) {
+      case 1:
+        integrate_level_kernel<1><<<grid, 128, 0, stream>>>(A, S.start[L], S.stride[L], count, lab, lvl, work + L);
+        break;
+      case 2:
+        integrate_level_kernel<2><<<grid, 128, 0, stream>>>(A, S.start[L], S.stride[L], count, lab, lvl, work + L);
+        break;
+      case 8:
+        integrate_level_kernel<8><<<grid, 128, 0, stream>>>(A, S.start[L], S.stride[L], count, lab, lvl, work + L);
+        break;
+      default:
+        integrate_level_kernel<4><<<grid, 128, 0, stream>>>(A, S.start[L], S.stride[L], count, lab, lvl, work + L);
+    }
   }
   return cudaGetLastError();
 }
@@ -780,7 +827,7 @@ cudaError_t launch_fixup(const double* G, const VolDims& V, const IntegParams& P
   const int blocks = (n + 127) / 128;
   if (cudaError_t e = cudaMemsetAsync(work, 0, sizeof(unsigned long long), stream)) return e;
   ::msc::count_launch();
-  fixup_kernel<<<blocks < num_sms * kLaneCtasPerSm ? blocks : num_sms * kLaneCtasPerSm, 128, 0, stream>>>(
+  fixup_kernel<2><<<blocks < num_sms * kLaneCtasPerSm ? blocks : num_sms * kLaneCtasPerSm, 128, 0, stream>>>(
       A, lab, lab0, state, list, n, next, n_next, queued, work);
   return cudaGetLastError();
 }
@@ -794,8 +841,24 @@ cudaError_t launch_fixup32(const float4* G, const VolDims& V, const IntegParams&
   const int blocks = (n + 127) / 128;
   if (cudaError_t e = cudaMemsetAsync(work, 0, sizeof(unsigned long long), stream)) return e;
   ::msc::count_launch();
-  fixup32_kernel<<<blocks < num_sms * kLaneCtasPerSm ? blocks : num_sms * kLaneCtasPerSm, 128, 0, stream>>>(
-      A, lab, lab0, state, list, n, next, n_next, queued, amb, n_amb, amb_mode, work);
+  const int grid = blocks < num_sms * kLaneCtasPerSm ? blocks : num_sms * kLaneCtasPerSm;
+  switch (trips_per_turn()) {
+    case 1:
+      fixup32_kernel<1><<<grid, 128, 0, stream>>>(A, lab, lab0, state, list, n, next, n_next, queued, amb,
+                                                     n_amb, amb_mode, work);
+      break;
+    case 2:
+      fixup32_kernel<2><<<grid, 128, 0, stream>>>(A, lab, lab0, state, list, n, next, n_next, queued, amb,
+                                                     n_amb, amb_mode, work);
+      break;
+    case 8:
+      fixup32_kernel<8><<<grid, 128, 0, stream>>>(A, lab, lab0, state, list, n, next, n_next, queued, amb,
+                                                     n_amb, amb_mode, work);
+      break;
+    default:
+      fixup32_kernel<4><<<grid, 128, 0, stream>>>(A, lab, lab0, state, list, n, next, n_next, queued, amb,
+                                                     n_amb, amb_mode, work);
+  }
   return cudaGetLastError();
 }
 
