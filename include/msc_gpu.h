@@ -159,6 +159,10 @@ const char* msc_labels_last_error_string(void);
 /* Work counts of the last labeling call on the calling thread: boundary
  * re-decisions (ascending), of which in FP64, then the same for descending. */
 void msc_labels_last_stats(int64_t out[4]);
+/* Advection iterations (adaptive Euler step attempts) of the last labeling call on
+ * the calling thread: first pass, FP32 boundary re-decisions, FP64 re-decisions;
+ * ascending, then descending. */
+void msc_labels_last_iterations(int64_t out[6]);
 
 /* Stage 2 for callers that may not allocate device memory: the same result as
  * msc_ascending_manifold_dims_3d, with the pass scratch (tile flags, status words)

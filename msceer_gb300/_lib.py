@@ -45,6 +45,7 @@ SIGNATURES = {
     "msc_kernel_launches": (ctypes.c_int64, []),
     "msc_labels_last_error_string": (ctypes.c_char_p, []),
     "msc_labels_last_stats": (None, [_I64P]),
+    "msc_labels_last_iterations": (None, [_I64P]),
     "msc_triage_last_error_string": (ctypes.c_char_p, []),
     "msc_triage_features_3d": (ctypes.c_int, [_VP, _VP, _I64P, _VP, _VP, _VP, _VP]),  # f grad dims p feat tgt st
     "msc_triage_forward_3d": (ctypes.c_int, [_VP, _I64P, _VP, _VP, _VP, _VP, _VP]),

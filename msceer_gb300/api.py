@@ -179,8 +179,12 @@ def integrated_labels(f, grad, error_threshold=1e-4, gradient_threshold=None, it
     _lib.check(rc, "msc_integrated_labels_3d")
     stats = (ctypes.c_int64 * 4)()
     lib.msc_labels_last_stats(stats)
+    it = (ctypes.c_int64 * 6)()
+    lib.msc_labels_last_iterations(it)
     out = {"stats": {"asc_redecided": stats[0], "asc_fp64": stats[1], "dsc_redecided": stats[2],
-                     "dsc_fp64": stats[3]}}
+                     "dsc_fp64": stats[3]},
+           "iterations": {f"{d}_{k}": it[3 * i + j] for i, d in enumerate(("asc", "dsc"))
+                          for j, k in enumerate(("first_pass", "fp32", "fp64"))}}
     if asc is not None:
         out["asc"] = asc
     if dsc is not None:

@@ -236,6 +236,13 @@ __device__ __forceinline__ unsigned long long claim_item(bool want, unsigned lon
   return base + (unsigned long long)__popc(ask & ((1u << lane) - 1u));
 }
 
+// Adds the warp's trip counts to *trips (one atomic per warp; every lane calls it).
+__device__ __forceinline__ void add_trips(unsigned long long n, unsigned long long* trips) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) n += __shfl_down_sync(kFullMask, n, o);
+  if ((threadIdx.x & 31) == 0 && n) atomicAdd(trips, n);
+}
+
 // One level of the spread order.  Streamlines of a level see only the labels of
 // earlier levels (lvl[v] < level; terminals are level 0, unlabelled vertices 255),
 // so a level's outcome does not depend on thread timing; where several streamlines
@@ -246,13 +253,15 @@ __device__ __forceinline__ unsigned long long claim_item(bool want, unsigned lon
 template <int K>
 __global__ void __launch_bounds__(128) integrate_level_kernel(const Adv32 A, int64_t start, int64_t stride, int64_t count,
                                                               int32_t* __restrict__ lab, uint8_t* __restrict__ lvl,
-                                                              unsigned long long* __restrict__ work) {
+                                                              unsigned long long* __restrict__ work,
+                                                              unsigned long long* __restrict__ trips) {
   const VolDims& V = A.V;
   const int level = A.level;
   int path[kPathCap];
   int np = 0;
   int64_t end = 0;
   int phase = kLaneIdle;
+  unsigned long long ntrips = 0;
   int x = 0, y = 0, z = 0;
   F3 cur = {0.f, 0.f, 0.f}, old = cur, g = cur;
   float gm = 0.f, step = 0.f, gm_end = 0.f;
@@ -277,7 +286,10 @@ __global__ void __launch_bounds__(128) integrate_level_kernel(const Adv32 A, int
         }
       }
     }
-    if (__all_sync(kFullMask, phase == kLaneDone)) break;
+    if (__all_sync(kFullMask, phase == kLaneDone)) {
+      add_trips(ntrips, trips);
+      break;
+    }
     if (phase == kLaneEnter) {
       nb = dist_to_boundary(V, x, y, z) <= 1;
       if (A.enter(cur, nb, b, c, g, gm, step, gm_end)) {
@@ -292,6 +304,7 @@ __global__ void __launch_bounds__(128) integrate_level_kernel(const Adv32 A, int
     }
     if (phase == kLaneStep) {
       for (int r = 0; r < K; r++) {
+        ntrips++;
         const int ev = A.trip(cur, old, iters, nb, b, c, g, gm, step, gm_end);
         if (ev == EV_NONE) continue;
         A.nearest3(cur, x, y, z);
@@ -476,9 +489,11 @@ __global__ void __launch_bounds__(128) fixup_kernel(const Adv64 A, int32_t* __re
                                                     const int32_t* __restrict__ lab0, uint8_t* __restrict__ state,
                                                     const int64_t* __restrict__ list, int n, int64_t* __restrict__ next,
                                                     int* __restrict__ n_next, uint32_t* __restrict__ queued,
-                                                    unsigned long long* __restrict__ work) {
+                                                    unsigned long long* __restrict__ work,
+                                                    unsigned long long* __restrict__ trips) {
   const VolDims& V = A.V;
   int phase = kLaneIdle;
+  unsigned long long ntrips = 0;
   int64_t v = 0;
   int x = 0, y = 0, z = 0;
   int32_t init = 0;
@@ -503,7 +518,10 @@ __global__ void __launch_bounds__(128) fixup_kernel(const Adv64 A, int32_t* __re
         phase = kLaneEnter;
       }
     }
-    if (__all_sync(kFullMask, phase == kLaneDone)) break;
+    if (__all_sync(kFullMask, phase == kLaneDone)) {
+      add_trips(ntrips, trips);
+      break;
+    }
     if (phase == kLaneEnter) {
       nb = dist_to_boundary(V, x, y, z) <= 1;
       if (A.enter(cur, nb, b, c, g, gm, step)) {
@@ -516,6 +534,7 @@ __global__ void __launch_bounds__(128) fixup_kernel(const Adv64 A, int32_t* __re
     }
     if (phase == kLaneStep) {
       for (int r = 0; r < K; r++) {
+        ntrips++;
         const int ev = A.trip(cur, old, iters, nb, b, c, g, gm, step);
         if (ev == EV_NONE) continue;
         A.nearest3(cur, x, y, z);
@@ -562,9 +581,11 @@ __global__ void __launch_bounds__(128) fixup32_kernel(const Adv32 A, int32_t* __
                                                       int64_t* __restrict__ next, int* __restrict__ n_next,
                                                       uint32_t* __restrict__ queued, int64_t* __restrict__ amb,
                                                       int* __restrict__ n_amb, int amb_mode,
-                                                      unsigned long long* __restrict__ work) {
+                                                      unsigned long long* __restrict__ work,
+                                                      unsigned long long* __restrict__ trips) {
   const VolDims& V = A.V;
   int phase = kLaneIdle;
+  unsigned long long ntrips = 0;
   int64_t v = 0;
   int x = 0, y = 0, z = 0;
   int32_t init = 0;
@@ -588,7 +609,10 @@ __global__ void __launch_bounds__(128) fixup32_kernel(const Adv32 A, int32_t* __
         phase = kLaneEnter;
       }
     }
-    if (__all_sync(kFullMask, phase == kLaneDone)) break;
+    if (__all_sync(kFullMask, phase == kLaneDone)) {
+      add_trips(ntrips, trips);
+      break;
+    }
     if (phase == kLaneEnter) {
       nb = dist_to_boundary(V, x, y, z) <= 1;
       if (A.enter(cur, nb, b, c, g, gm, step, gm_end)) {
@@ -602,6 +626,7 @@ __global__ void __launch_bounds__(128) fixup32_kernel(const Adv32 A, int32_t* __
     }
     if (phase == kLaneStep) {
       for (int r = 0; r < K; r++) {
+        ntrips++;
         ev = A.trip(cur, old, iters, nb, b, c, g, gm, step, gm_end);
         if (ev == EV_NONE) continue;
         A.nearest3(cur, x, y, z);
@@ -782,8 +807,8 @@ int trips_per_turn() {
 }
 
 cudaError_t launch_integrate_pass1(const float4* G, const VolDims& V, const IntegParams& P, const SpreadOrder& S,
-                                   int32_t* lab, uint8_t* lvl, unsigned long long* work, int num_sms,
-                                   cudaStream_t stream) {
+                                   int32_t* lab, uint8_t* lvl, unsigned long long* work, unsigned long long* trips,
+                                   int num_sms, cudaStream_t stream) {
   const int64_t N = V.X * V.Y * V.Z;
   if (cudaError_t e = cudaMemsetAsync(work, 0, sizeof(unsigned long long) * 48, stream)) return e;
   ::msc::count_launch();
@@ -797,16 +822,16 @@ cudaError_t launch_integrate_pass1(const float4* G, const VolDims& V, const Inte
     ::msc::count_launch();
     switch (trips_per_turn()) {
       case 1:
-        integrate_level_kernel<1><<<grid, 128, 0, stream>>>(A, S.start[L], S.stride[L], count, lab, lvl, work + L);
+        integrate_level_kernel<1><<<grid, 128, 0, stream>>>(A, S.start[L], S.stride[L], count, lab, lvl, work + L, trips);
         break;
       case 2:
-        integrate_level_kernel<2><<<grid, 128, 0, stream>>>(A, S.start[L], S.stride[L], count, lab, lvl, work + L);
+        integrate_level_kernel<2><<<grid, 128, 0, stream>>>(A, S.start[L], S.stride[L], count, lab, lvl, work + L, trips);
         break;
       case 8:
-        integrate_level_kernel<8><<<grid, 128, 0, stream>>>(A, S.start[L], S.stride[L], count, lab, lvl, work + L);
+        integrate_level_kernel<8><<<grid, 128, 0, stream>>>(A, S.start[L], S.stride[L], count, lab, lvl, work + L, trips);
         break;
       default:
-        integrate_level_kernel<4><<<grid, 128, 0, stream>>>(A, S.start[L], S.stride[L], count, lab, lvl, work + L);
+        integrate_level_kernel<4><<<grid, 128, 0, stream>>>(A, S.start[L], S.stride[L], count, lab, lvl, work + L, trips);
     }
   }
   return cudaGetLastError();
@@ -821,21 +846,21 @@ cudaError_t launch_boundary_set(const int32_t* lab, const uint8_t* state, const 
 
 cudaError_t launch_fixup(const double* G, const VolDims& V, const IntegParams& P, int32_t* lab, const int32_t* lab0,
                          uint8_t* state, const int64_t* list, int n, int64_t* next, int* n_next, uint32_t* queued,
-                         unsigned long long* work, int num_sms, cudaStream_t stream) {
+                         unsigned long long* work, unsigned long long* trips, int num_sms, cudaStream_t stream) {
   if (n <= 0) return cudaSuccess;
   Adv64 A{G, V, P, state};
   const int blocks = (n + 127) / 128;
   if (cudaError_t e = cudaMemsetAsync(work, 0, sizeof(unsigned long long), stream)) return e;
   ::msc::count_launch();
   fixup_kernel<2><<<blocks < num_sms * kLaneCtasPerSm ? blocks : num_sms * kLaneCtasPerSm, 128, 0, stream>>>(
-      A, lab, lab0, state, list, n, next, n_next, queued, work);
+      A, lab, lab0, state, list, n, next, n_next, queued, work, trips);
   return cudaGetLastError();
 }
 
 cudaError_t launch_fixup32(const float4* G, const VolDims& V, const IntegParams& P, int32_t* lab, const int32_t* lab0,
                            uint8_t* state, const int64_t* list, int n, int64_t* next, int* n_next, uint32_t* queued,
-                           int64_t* amb, int* n_amb, int amb_mode, unsigned long long* work, int num_sms,
-                           cudaStream_t stream) {
+                           int64_t* amb, int* n_amb, int amb_mode, unsigned long long* work,
+                           unsigned long long* trips, int num_sms, cudaStream_t stream) {
   if (n <= 0) return cudaSuccess;
   const Adv32 A = Adv32::make(G, V, P, lab, nullptr, 0, state);
   const int blocks = (n + 127) / 128;
@@ -845,19 +870,19 @@ cudaError_t launch_fixup32(const float4* G, const VolDims& V, const IntegParams&
   switch (trips_per_turn()) {
     case 1:
       fixup32_kernel<1><<<grid, 128, 0, stream>>>(A, lab, lab0, state, list, n, next, n_next, queued, amb,
-                                                     n_amb, amb_mode, work);
+                                                     n_amb, amb_mode, work, trips);
       break;
     case 2:
       fixup32_kernel<2><<<grid, 128, 0, stream>>>(A, lab, lab0, state, list, n, next, n_next, queued, amb,
-                                                     n_amb, amb_mode, work);
+                                                     n_amb, amb_mode, work, trips);
       break;
     case 8:
       fixup32_kernel<8><<<grid, 128, 0, stream>>>(A, lab, lab0, state, list, n, next, n_next, queued, amb,
-                                                     n_amb, amb_mode, work);
+                                                     n_amb, amb_mode, work, trips);
       break;
     default:
       fixup32_kernel<4><<<grid, 128, 0, stream>>>(A, lab, lab0, state, list, n, next, n_next, queued, amb,
-                                                     n_amb, amb_mode, work);
+                                                     n_amb, amb_mode, work, trips);
   }
   return cudaGetLastError();
 }

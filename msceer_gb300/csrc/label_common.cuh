@@ -103,20 +103,21 @@ struct SpreadOrder {
   int64_t start[48], stride[48], offset[49];
 };
 
-// `work`: 48 device counters (the levels' claimed items), zeroed here
+// `work`: 48 device counters (the levels' claimed items), zeroed here.  `trips`
+// (here and below): a device counter the kernels add their advection iterations to.
 cudaError_t launch_integrate_pass1(const float4* G, const VolDims& V, const IntegParams& P, const SpreadOrder& S,
-                                   int32_t* lab, uint8_t* lvl, unsigned long long* work, int num_sms,
-                                   cudaStream_t stream);
+                                   int32_t* lab, uint8_t* lvl, unsigned long long* work, unsigned long long* trips,
+                                   int num_sms, cudaStream_t stream);
 cudaError_t launch_boundary_set(const int32_t* lab, const uint8_t* state, const VolDims& V, int64_t* list, int* n,
                                 uint32_t* queued, int num_sms, cudaStream_t stream);
 // `work`: a device counter of claimed items, zeroed by the launchers
 cudaError_t launch_fixup(const double* G, const VolDims& V, const IntegParams& P, int32_t* lab, const int32_t* lab0,
                          uint8_t* state, const int64_t* list, int n, int64_t* next, int* n_next, uint32_t* queued,
-                         unsigned long long* work, int num_sms, cudaStream_t stream);
+                         unsigned long long* work, unsigned long long* trips, int num_sms, cudaStream_t stream);
 cudaError_t launch_fixup32(const float4* G, const VolDims& V, const IntegParams& P, int32_t* lab, const int32_t* lab0,
                            uint8_t* state, const int64_t* list, int n, int64_t* next, int* n_next, uint32_t* queued,
-                           int64_t* amb, int* n_amb, int amb_mode, unsigned long long* work, int num_sms,
-                           cudaStream_t stream);
+                           int64_t* amb, int* n_amb, int amb_mode, unsigned long long* work,
+                           unsigned long long* trips, int num_sms, cudaStream_t stream);
 cudaError_t launch_clean(const int32_t* lab, const float* f, const VolDims& V, int dir, int64_t* parent, int64_t* target,
                          int32_t* out, int num_sms, cudaStream_t stream);
 

@@ -22,6 +22,7 @@ namespace {
 thread_local std::string t_err;
 // per direction (asc, dsc): fix-up re-decisions, of which in FP64
 thread_local int64_t t_stats[4];
+thread_local int64_t t_trips[6];
 
 int fail(int code, const std::string& m) {
   t_err = m;
@@ -183,13 +184,14 @@ struct LabelCtx {
   uint32_t* queued = nullptr;
   uint8_t* tiles = nullptr;
   int* counters = nullptr;  // [0] n_ext [1] n_sad [2] n_arcs [3] changed [4] err [5] n_list [6] n_next [7] n_amb
-  unsigned long long* work = nullptr;  // claimed work items of the integration kernels (48)
+  unsigned long long* work = nullptr;  // [0, 48) claimed work items, [48, 51) advection iterations
   explicit LabelCtx(cudaStream_t s) : st(s), pool(s) {}
 };
 
 // One direction's labels between the phases.
 struct DirLabels {
   int dir = -1;
+  int64_t trips[3] = {0, 0, 0};  // advection iterations: first pass, FP32 fix-up, FP64 re-decisions
   int32_t* lab = nullptr;
   uint8_t* state = nullptr;
   int64_t* seed = nullptr;
@@ -224,7 +226,7 @@ int setup_ctx(LabelCtx& c, const float* f, const uint8_t* grad, const int64_t* d
   LCUDA(c.pool.get(&c.queued, N / 32 + 1), "alloc");
   LCUDA(c.pool.get(&c.tiles, 2 * c.ntiles), "alloc");
   LCUDA(c.pool.get(&c.counters, 8), "alloc");
-  LCUDA(c.pool.get(&c.work, 48), "alloc");
+  LCUDA(c.pool.get(&c.work, 64), "alloc");
   LCUDA(cudaMemsetAsync(c.counters, 0, 8 * sizeof(int), c.st), "memset");
   msc::GradDims GD{};
   for (int a = 0; a < 3; a++) {
@@ -348,7 +350,8 @@ int first_pass(LabelCtx& c, DirLabels& d) {
   }
   uint8_t* lvl;
   LCUDA(c.pool.get(&lvl, N), "alloc");
-  LCUDA(msc::launch_integrate_pass1(c.g32, c.V, P, S, d.lab, lvl, c.work, c.sms, st), "integrate");
+  LCUDA(cudaMemsetAsync(c.work + 48, 0, 3 * sizeof(unsigned long long), st), "memset");
+  LCUDA(msc::launch_integrate_pass1(c.g32, c.V, P, S, d.lab, lvl, c.work, c.work + 48, c.sms, st), "integrate");
   return MSC_OK;
 }
 
@@ -382,22 +385,28 @@ int finish_direction(LabelCtx& c, DirLabels& d, int32_t* out, int32_t* stage_int
     LCUDA(cudaMemsetAsync(c.counters + 6, 0, 2 * sizeof(int), st), "memset");
     if (p->precision == 1) {
       LCUDA(msc::launch_fixup(c.g64, V, P, d.lab, lab0, d.state, cur, n_list, nxt, c.counters + 6, c.queued, c.work,
-                              sms, st),
+                              c.work + 50, sms, st),
             "fix-up");
     } else {
       LCUDA(msc::launch_fixup32(c.g32, V, P, d.lab, lab0, d.state, cur, n_list, nxt, c.counters + 6, c.queued, c.amb,
-                                c.counters + 7, p->precision == 2 ? 2 : 0, c.work, sms, st),
+                                c.counters + 7, p->precision == 2 ? 2 : 0, c.work, c.work + 49, sms, st),
             "fix-up");
       int n_amb = 0;
       if (int rc = read_int(c.counters + 7, &n_amb, st)) return rc;
       stats[1] += n_amb;
       LCUDA(msc::launch_fixup(c.g64, V, P, d.lab, lab0, d.state, c.amb, n_amb, nxt, c.counters + 6, c.queued, c.work,
-                              sms, st),
+                              c.work + 50, sms, st),
             "fix-up");
     }
     stats[0] += n_list;
     if (int rc = read_int(c.counters + 6, &n_list, st)) return rc;
     std::swap(cur, nxt);
+  }
+  {
+    unsigned long long h[3];
+    LCUDA(cudaMemcpyAsync(h, c.work + 48, sizeof(h), cudaMemcpyDeviceToHost, st), "read iterations");
+    LCUDA(cudaStreamSynchronize(st), "cudaStreamSynchronize");
+    for (int k = 0; k < 3; k++) d.trips[k] = (int64_t)h[k];
   }
   if (stage_integrated) {
     ::msc::count_launch();
@@ -432,6 +441,7 @@ int labels_impl(const float* f, const uint8_t* grad, const int64_t* dims, const 
   LabelCtx c(st);
   if (int rc = setup_ctx(c, f, grad, dims, p)) return rc;
   for (int k = 0; k < 4; k++) t_stats[k] = 0;
+  for (int k = 0; k < 6; k++) t_trips[k] = 0;
   for (int pass = 0; pass < 2; pass++) {
     int32_t* out = pass == 0 ? out_asc : out_dsc;
     if (!out) continue;
@@ -440,6 +450,7 @@ int labels_impl(const float* f, const uint8_t* grad, const int64_t* dims, const 
     if (int rc = prepare_direction(c, d, stages ? stages + (2 * pass) * c.N : nullptr)) return rc;
     if (int rc = integrate_direction(c, d, out, stages ? stages + (2 * pass + 1) * c.N : nullptr, t_stats + 2 * pass))
       return rc;
+    for (int k = 0; k < 3; k++) t_trips[3 * pass + k] = d.trips[k];
   }
   return finish_errors(c);
 }
@@ -504,6 +515,7 @@ int triage_labels_impl(const float* f, const uint8_t* grad, const int64_t* dims,
   const float thr[2] = {tp->logit_threshold_asc, tp->logit_threshold_dsc};
   int32_t* outs[2] = {out_asc, out_dsc};
   int64_t fix[4] = {0, 0, 0, 0};
+  for (int k = 0; k < 6; k++) t_trips[k] = 0;
   for (int k = 0; k < 2; k++) {
     DirLabels d;
     d.dir = k == 0 ? -1 : 1;
@@ -516,6 +528,7 @@ int triage_labels_impl(const float* f, const uint8_t* grad, const int64_t* dims,
                                    counts + 3 * k, c.sms, st),
           "triage apply");
     if (int rc = finish_direction(c, d, outs[k], nullptr, fix + 2 * k)) return rc;
+    for (int q = 0; q < 3; q++) t_trips[3 * k + q] = d.trips[q];
     LCUDA(msc::launch_audit_count(d.lab, first, flags, N, counts + 3 * k + 2, c.sms, st), "audit");
   }
   for (int k = 0; k < 4; k++) t_stats[k] = fix[k];
@@ -597,6 +610,11 @@ const char* msc_labels_last_error_string(void) { return t_err.c_str(); }
 void msc_labels_last_stats(int64_t out[4]) {
   if (out)
     for (int k = 0; k < 4; k++) out[k] = t_stats[k];
+}
+
+void msc_labels_last_iterations(int64_t out[6]) {
+  if (out)
+    for (int k = 0; k < 6; k++) out[k] = t_trips[k];
 }
 
 int msc_integrated_labels_3d(const float* f, const uint8_t* grad, const int64_t dims[3], const msc_integ_params* params,

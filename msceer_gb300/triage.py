@@ -231,4 +231,8 @@ def triage_labels(f, grad, net: TriageNet, error_threshold=1e-4, gradient_thresh
     _check(rc, "msc_triage_labels_3d")
     names = ("flagged", "audited", "audit_changed", "redecided")
     st = {f"{d}_{k}": int(stats[4 * i + j]) for i, d in enumerate(("asc", "dsc")) for j, k in enumerate(names)}
-    return {"asc": asc, "dsc": dsc, "stats": st}
+    it = (ctypes.c_int64 * 6)()
+    _lib.load().msc_labels_last_iterations(it)
+    iters = {f"{d}_{k}": int(it[3 * i + j]) for i, d in enumerate(("asc", "dsc"))
+             for j, k in enumerate(("first_pass", "fp32", "fp64"))}
+    return {"asc": asc, "dsc": dsc, "stats": st, "iterations": iters}
