@@ -233,6 +233,6 @@ def triage_labels(f, grad, net: TriageNet, error_threshold=1e-4, gradient_thresh
     st = {f"{d}_{k}": int(stats[4 * i + j]) for i, d in enumerate(("asc", "dsc")) for j, k in enumerate(names)}
     it = (ctypes.c_int64 * 6)()
     _lib.load().msc_labels_last_iterations(it)
-    iters = {f"{d}_{k}": int(it[3 * i + j]) for i, d in enumerate(("asc", "dsc"))
-             for j, k in enumerate(("first_pass", "fp32", "fp64"))}
-    return {"asc": asc, "dsc": dsc, "stats": st, "iterations": iters}
+    st.update({f"{d}_iterations_{k}": int(it[3 * i + j]) for i, d in enumerate(("asc", "dsc"))
+               for j, k in enumerate(("first_pass", "fp32", "fp64"))})
+    return {"asc": asc, "dsc": dsc, "stats": st}
