@@ -148,8 +148,8 @@ def integrated_labels(f, grad, error_threshold=1e-4, gradient_threshold=None, it
     boundary vertices in FP32 and the ambiguous ones in FP64; 1 re-decides all of them
     in FP64.  Returns a dict with "asc" and/or "dsc" int32 tensors (a label is the
     vertex id of the region's extremum, -1 none), "stats" (boundary re-decisions and
-    FP64 ones per direction, and the advection iterations of each stage) and, with ``stages``, the terminal / integrated labels of
-    each direction."""
+    FP64 ones per direction, and the advection iterations of each stage) and, with
+    ``stages``, the terminal / integrated labels of each direction."""
     import torch
 
     if not (f.is_cuda and grad.is_cuda):
@@ -181,10 +181,10 @@ def integrated_labels(f, grad, error_threshold=1e-4, gradient_threshold=None, it
     lib.msc_labels_last_stats(stats)
     it = (ctypes.c_int64 * 6)()
     lib.msc_labels_last_iterations(it)
-    st = {"asc_redecided": stats[0], "asc_fp64": stats[1], "dsc_redecided": stats[2], "dsc_fp64": stats[3]}
-    st.update({f"{d}_iterations_{k}": it[3 * i + j] for i, d in enumerate(("asc", "dsc"))
+    sd = {"asc_redecided": stats[0], "asc_fp64": stats[1], "dsc_redecided": stats[2], "dsc_fp64": stats[3]}
+    sd.update({f"{d}_iterations_{k}": it[3 * i + j] for i, d in enumerate(("asc", "dsc"))
                for j, k in enumerate(("first_pass", "fp32", "fp64"))})
-    out = {"stats": st}
+    out = {"stats": sd}
     if asc is not None:
         out["asc"] = asc
     if dsc is not None:
