@@ -343,6 +343,24 @@ def run_ours(args, ws, rank, local):
                                 "speedup_vs_plain": ms_plain / ms}
         if net is not None:
             line_extra["labels"]["thresholds"] = [net.threshold_asc, net.threshold_dsc]
+        # the labeling's kernels are FP32 issue-bound streamline integrations: their
+        # roofline is the FP32 rate.  Operations per advection iteration: two trilinear
+        # interpolations of the 3-vector gradient (73 each) plus step control (~37).
+        st = res["stats"]
+        it32 = sum(st.get(f"{d}_iterations_{k}", 0) for d in ("asc", "dsc") for k in ("first_pass", "fp32"))
+        it64 = sum(st.get(f"{d}_iterations_fp64", 0) for d in ("asc", "dsc"))
+        labels_ms = max(ms - t_grad, 1e-9)
+        sms = torch.cuda.get_device_properties(dev).multi_processor_count
+        fp32_peak = FP32_LANES_PER_SM * sms * 2 * SM_MAX_MHZ * 1e6 / 1e12
+        achieved = it32 * FLOP_PER_ITERATION / (labels_ms * 1e-3) / 1e12
+        line_extra["integration"] = {
+            "kernels": "integrate_level_kernel + fixup32_kernel (FP32), fixup_kernel (FP64 re-decisions)",
+            "bound": "fp32 issue", "iterations_fp32": it32, "iterations_fp64": it64,
+            "flop_per_iteration": FLOP_PER_ITERATION, "labels_ms": labels_ms,
+            "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s", "frac": achieved / fp32_peak,
+            "peak_kind": f"nominal FP32 ({sms} SMs x {FP32_LANES_PER_SM} lanes x FMA at {SM_MAX_MHZ} MHz)",
+            "scope": "all FP32 advection iterations of the step over the whole labeling time (every labeling "
+                     "kernel included, so a lower bound for the integration kernels)"}
 
     # end to end through the C ABI host entry, pinned host buffers
     e2e_reps = max(1, min(args.steps, 3))
@@ -454,6 +472,9 @@ def run_ours(args, ws, rank, local):
 # dram__bytes_read.sum + dram__bytes_write.sum per launch from the committed ncu
 # summaries under profiles/ (None until captured)
 TRAFFIC_PER_LAUNCH: dict = {}
+FLOP_PER_ITERATION = 183
+FP32_LANES_PER_SM = 128
+SM_MAX_MHZ = 2070
 
 
 def main():
