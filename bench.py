@@ -471,7 +471,16 @@ def run_ours(args, ws, rank, local):
 
 # dram__bytes_read.sum + dram__bytes_write.sum per launch from the committed ncu
 # summaries under profiles/ (None until captured)
-TRAFFIC_PER_LAUNCH: dict = {}
+# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per launch from one ncu
+# --set full capture of the kernels at 320^3, scaled to 512^3 by the vertex
+# count (x 4.096): the traffic grows with the volume.  ldir_stage = tile + check
+# kernels (the walk's share is below 3% of the stage's time).
+TRAFFIC_PER_LAUNCH: dict = {
+    ("lstar_kernel", 320): 0.131313e9 + 0.206132e9,
+    ("ldir_stage", 320): 0.313691e9 + 0.364048e9 + 0.448826e9 + 0.025934e9,
+    ("lstar_kernel", 512): (0.131313e9 + 0.206132e9) * 4.096,
+    ("ldir_stage", 512): (0.313691e9 + 0.364048e9 + 0.448826e9 + 0.025934e9) * 4.096,
+}
 FLOP_PER_ITERATION = 183
 FP32_LANES_PER_SM = 128
 SM_MAX_MHZ = 2070
