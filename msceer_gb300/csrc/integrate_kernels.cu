@@ -49,8 +49,8 @@ struct Adv32 {
   const float4* G;
   VolDims V;
   IntegParams P;
-  const int32_t* lab;     // pass-1 stop: nearest vertex labelled (assigned or terminal) ...
-  const uint8_t* lvl;    // ... in an earlier level of the spread order (level array, when set)
+  const int32_t* lab;
+  const uint8_t* lvl;    // pass-1 stop (when set): nearest vertex labelled in an earlier level
   int level;
   const uint8_t* state;  // fix-up stop (when set): nearest vertex certain terminal
   // Converted once on the host: (float)P.max_step, (float)P.step_mult, the extents
@@ -152,7 +152,7 @@ struct Adv32 {
   // One iteration of the advection loop (one `iters` decrement); EV_NONE to go on.
   // gm_end: the gradient magnitude at a low-gradient stop (0 where there was none).
   __device__ __forceinline__ int trip(F3& cur, F3& old, int& iters, bool nearb, const float b[3], const F3 c[8],
-                                      F3& g, float& gm, float& step, float& gm_end) const {
+                                      F3& g, float& gm, float& step, float& gm_end, int64_t& last_nv) const {
     if (!(iters-- > 0)) return EV_OVER_MAX_ITERATIONS;
     if (!(old.x == cur.x && old.y == cur.y && old.z == cur.z)) {
       if ((int)cur.x != (int)old.x || (int)cur.y != (int)old.y || (int)cur.z != (int)old.z) return EV_OUT_OF_VOXEL;
@@ -182,14 +182,18 @@ struct Adv32 {
       }
       cur = np;
       step = fminf(step * 1.8f, ms / gm);
+      // the stop test reads memory only when the nearest vertex changed: what it reads
+      // (certain terminals in the fix-up, earlier levels in the first pass) does not
+      // change while the kernel runs, and a vertex it passed once does not stop it later
       const int64_t nv = nearest(cur, nearb);
-      if (state) {
-        const uint8_t st = state[nv];
-        if (st == kStSeed || st == kStTerminal) return EV_HIT_PREASSIGNED;
-      } else if (lvl) {
-        if (lvl[nv] < level) return EV_HIT_PREASSIGNED;
-      } else if (lab[nv] != -1) {
-        return EV_HIT_PREASSIGNED;
+      if (nv != last_nv) {
+        if (state) {
+          const uint8_t st = state[nv];
+          if (st == kStSeed || st == kStTerminal) return EV_HIT_PREASSIGNED;
+        } else if (lvl[nv] < level) {
+          return EV_HIT_PREASSIGNED;
+        }
+        last_nv = nv;
       }
     } else {
       step = step * 0.5f;
@@ -264,7 +268,7 @@ __device__ __forceinline__ void add_trips(unsigned long long n, unsigned long lo
 // pass is therefore deterministic.  `work` counts the level's claimed items (zero at
 // launch).
 template <int K>
-__global__ void __launch_bounds__(128) integrate_level_kernel(const Adv32 A, int64_t start, int64_t stride, int64_t count,
+__global__ void __launch_bounds__(128, 6) integrate_level_kernel(const Adv32 A, int64_t start, int64_t stride, int64_t count,
                                                               int32_t* __restrict__ lab, uint8_t* __restrict__ lvl,
                                                               unsigned long long* __restrict__ work,
                                                               unsigned long long* __restrict__ trips) {
@@ -284,6 +288,7 @@ __global__ void __launch_bounds__(128) integrate_level_kernel(const Adv32 A, int
   F3 c[8];
   F3 anchor = cur;  // trapped-streamline test
   int t_iters = 0, t_n = 0;
+  int64_t last_nv = -1;  // nearest vertex the stop test last passed
   while (true) {
     const unsigned long long t = claim_item(phase == kLaneIdle, work);
     if (phase == kLaneIdle) {
@@ -298,6 +303,7 @@ __global__ void __launch_bounds__(128) integrate_level_kernel(const Adv32 A, int
           anchor = cur;
           t_iters = iters;
           t_n = 0;
+          last_nv = -1;
           np = 0;
           path[np++] = (int)i;
           phase = kLaneEnter;
@@ -308,29 +314,31 @@ __global__ void __launch_bounds__(128) integrate_level_kernel(const Adv32 A, int
       add_trips(ntrips, trips);
       break;
     }
-    if (phase == kLaneEnter) {
-      nb = dist_to_boundary(V, x, y, z) <= 1;
-      if (A.enter(cur, nb, b, c, g, gm, step, gm_end)) {
-        old = cur;
-        phase = kLaneStep;
-      } else {
-        A.nearest3(cur, x, y, z);  // ended at its voxel entry
-        end = vid(V, x, y, z);
-        if (np < kPathCap) path[np++] = (int)end;
-        phase = kLaneEnd;
+    // K steps; a lane that leaves its voxel enters the next one within the same turn,
+    // a lane whose streamline ended waits for the turn's end
+    for (int r = 0; r < K; r++) {
+      if (phase == kLaneEnter) {
+        nb = dist_to_boundary(V, x, y, z) <= 1;
+        if (A.enter(cur, nb, b, c, g, gm, step, gm_end)) {
+          old = cur;
+          phase = kLaneStep;
+        } else {
+          A.nearest3(cur, x, y, z);  // ended at its voxel entry
+          end = vid(V, x, y, z);
+          if (np < kPathCap) path[np++] = (int)end;
+          phase = kLaneEnd;
+        }
       }
+      if (phase != kLaneStep) continue;
+      ntrips++;
+      const int ev = A.trip(cur, old, iters, nb, b, c, g, gm, step, gm_end, last_nv);
+      if (ev == EV_NONE) continue;
+      A.nearest3(cur, x, y, z);
+      end = vid(V, x, y, z);
+      if (np < kPathCap) path[np++] = (int)end;
+      phase = ev == EV_OUT_OF_VOXEL ? kLaneEnter : kLaneEnd;
     }
-    if (phase == kLaneStep) {
-      for (int r = 0; r < K; r++) {
-        ntrips++;
-        const int ev = A.trip(cur, old, iters, nb, b, c, g, gm, step, gm_end);
-        if (ev == EV_NONE) continue;
-        A.nearest3(cur, x, y, z);
-        end = vid(V, x, y, z);
-        if (np < kPathCap) path[np++] = (int)end;
-        phase = ev == EV_OUT_OF_VOXEL ? kLaneEnter : kLaneEnd;
-        break;
-      }
+    {
       if (phase == kLaneStep && A.P.trap_window > 0 && t_iters - iters >= A.P.trap_window) {
         t_iters = iters;
         if (A.trapped(cur, anchor, t_n)) {  // ends where the iteration limit would have
@@ -549,25 +557,23 @@ __global__ void __launch_bounds__(128) fixup_kernel(const Adv64 A, int32_t* __re
       add_trips(ntrips, trips);
       break;
     }
-    if (phase == kLaneEnter) {
-      nb = dist_to_boundary(V, x, y, z) <= 1;
-      if (A.enter(cur, nb, b, c, g, gm, step)) {
-        old = cur;
-        phase = kLaneStep;
-      } else {
-        A.nearest3(cur, x, y, z);
-        phase = kLaneEnd;
+    for (int r = 0; r < K; r++) {
+      if (phase == kLaneEnter) {
+        nb = dist_to_boundary(V, x, y, z) <= 1;
+        if (A.enter(cur, nb, b, c, g, gm, step)) {
+          old = cur;
+          phase = kLaneStep;
+        } else {
+          A.nearest3(cur, x, y, z);
+          phase = kLaneEnd;
+        }
       }
-    }
-    if (phase == kLaneStep) {
-      for (int r = 0; r < K; r++) {
-        ntrips++;
-        const int ev = A.trip(cur, old, iters, nb, b, c, g, gm, step);
-        if (ev == EV_NONE) continue;
-        A.nearest3(cur, x, y, z);
-        phase = ev == EV_OUT_OF_VOXEL ? kLaneEnter : kLaneEnd;
-        break;
-      }
+      if (phase != kLaneStep) continue;
+      ntrips++;
+      const int ev = A.trip(cur, old, iters, nb, b, c, g, gm, step);
+      if (ev == EV_NONE) continue;
+      A.nearest3(cur, x, y, z);
+      phase = ev == EV_OUT_OF_VOXEL ? kLaneEnter : kLaneEnd;
     }
     if (phase != kLaneEnd) continue;
     phase = kLaneIdle;
@@ -602,7 +608,7 @@ __global__ void __launch_bounds__(128) fixup_kernel(const Adv64 A, int32_t* __re
 //   amb_mode 2: its final voxel touches two different certain regions (any ending
 //     within half a voxel of a basin boundary).
 template <int K>
-__global__ void __launch_bounds__(128) fixup32_kernel(const Adv32 A, int32_t* __restrict__ lab,
+__global__ void __launch_bounds__(128, 6) fixup32_kernel(const Adv32 A, int32_t* __restrict__ lab,
                                                       const int32_t* __restrict__ lab0, uint8_t* __restrict__ state,
                                                       const int64_t* __restrict__ list, int n,
                                                       int64_t* __restrict__ next, int* __restrict__ n_next,
@@ -624,6 +630,7 @@ __global__ void __launch_bounds__(128) fixup32_kernel(const Adv32 A, int32_t* __
   F3 c[8];
   F3 anchor = cur;  // trapped-streamline test
   int t_iters = 0, t_n = 0;
+  int64_t last_nv = -1;  // nearest vertex the stop test last passed
   while (true) {
     const unsigned long long k = claim_item(phase == kLaneIdle, work);
     if (phase == kLaneIdle) {
@@ -638,6 +645,7 @@ __global__ void __launch_bounds__(128) fixup32_kernel(const Adv32 A, int32_t* __
         anchor = cur;
         t_iters = iters;
         t_n = 0;
+        last_nv = -1;
         phase = kLaneEnter;
       }
     }
@@ -645,26 +653,26 @@ __global__ void __launch_bounds__(128) fixup32_kernel(const Adv32 A, int32_t* __
       add_trips(ntrips, trips);
       break;
     }
-    if (phase == kLaneEnter) {
-      nb = dist_to_boundary(V, x, y, z) <= 1;
-      if (A.enter(cur, nb, b, c, g, gm, step, gm_end)) {
-        old = cur;
-        phase = kLaneStep;
-      } else {
-        ev = EV_LOW_GRADIENT;
-        A.nearest3(cur, x, y, z);
-        phase = kLaneEnd;
+    for (int r = 0; r < K; r++) {
+      if (phase == kLaneEnter) {
+        nb = dist_to_boundary(V, x, y, z) <= 1;
+        if (A.enter(cur, nb, b, c, g, gm, step, gm_end)) {
+          old = cur;
+          phase = kLaneStep;
+        } else {
+          ev = EV_LOW_GRADIENT;
+          A.nearest3(cur, x, y, z);
+          phase = kLaneEnd;
+        }
       }
+      if (phase != kLaneStep) continue;
+      ntrips++;
+      ev = A.trip(cur, old, iters, nb, b, c, g, gm, step, gm_end, last_nv);
+      if (ev == EV_NONE) continue;
+      A.nearest3(cur, x, y, z);
+      phase = ev == EV_OUT_OF_VOXEL ? kLaneEnter : kLaneEnd;
     }
-    if (phase == kLaneStep) {
-      for (int r = 0; r < K; r++) {
-        ntrips++;
-        ev = A.trip(cur, old, iters, nb, b, c, g, gm, step, gm_end);
-        if (ev == EV_NONE) continue;
-        A.nearest3(cur, x, y, z);
-        phase = ev == EV_OUT_OF_VOXEL ? kLaneEnter : kLaneEnd;
-        break;
-      }
+    {
       if (phase == kLaneStep && A.P.trap_window > 0 && t_iters - iters >= A.P.trap_window) {
         t_iters = iters;
         if (A.trapped(cur, anchor, t_n)) {  // ends where the iteration limit would have

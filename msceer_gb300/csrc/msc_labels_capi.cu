@@ -413,16 +413,18 @@ int finish_direction(LabelCtx& c, DirLabels& d, int32_t* out, int32_t* stage_int
                                 c.counters + 7, p->precision == 2 ? 2 : 0, c.work, c.work + 49, sms, st),
             "fix-up");
       stats[0] += n_list;
-      if (int rc = read_int(c.counters + 7, &n_amb, st)) return rc;
     } else {
       stats[1] += n_amb;
       LCUDA(msc::launch_fixup(c.g64, V, P, d.lab, lab0, d.state, c.amb, n_amb, nxt, c.counters + 6, c.queued, c.work,
                               c.work + 50, sms, st),
             "fix-up");
       LCUDA(cudaMemsetAsync(c.counters + 7, 0, sizeof(int), st), "memset");
-      n_amb = 0;
     }
-    if (int rc = read_int(c.counters + 6, &n_list, st)) return rc;
+    int h[2];  // next wave's length, ambiguous streamlines waiting
+    LCUDA(cudaMemcpyAsync(h, c.counters + 6, sizeof(h), cudaMemcpyDeviceToHost, st), "read counters");
+    LCUDA(cudaStreamSynchronize(st), "cudaStreamSynchronize");
+    n_list = h[0];
+    n_amb = h[1];
     std::swap(cur, nxt);
   }
   {
