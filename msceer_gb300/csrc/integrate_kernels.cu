@@ -228,6 +228,7 @@ __device__ __forceinline__ void split_index(const VolDims& V, int64_t v, int& x,
 }
 
 constexpr int kPathCap = 48;
+constexpr int kMaxDraws = 4;  // first pass: hand-out rounds per turn for lanes that drew labelled vertices
 constexpr unsigned kFullMask = 0xffffffffu;
 
 // Streamlines differ in length by orders of magnitude (most end within a few dozen
@@ -290,25 +291,30 @@ __global__ void __launch_bounds__(128, 6) integrate_level_kernel(const Adv32 A, 
   int t_iters = 0, t_n = 0;
   int64_t last_nv = -1;  // nearest vertex the stop test last passed
   while (true) {
-    const unsigned long long t = claim_item(phase == kLaneIdle, work);
-    if (phase == kLaneIdle) {
-      if (t >= (unsigned long long)count) {
-        phase = kLaneDone;
-      } else {
-        const int64_t i = start + (int64_t)t * stride;
-        if (lvl[i] >= level) {  // else labelled already: ask again next turn
-          split_index(V, i, x, y, z);
-          cur = {(float)x, (float)y, (float)z};
-          iters = A.P.iteration_limit;
-          anchor = cur;
-          t_iters = iters;
-          t_n = 0;
-          last_nv = -1;
-          np = 0;
-          path[np++] = (int)i;
-          phase = kLaneEnter;
+    // most items of the late levels were labelled by earlier paths: a lane that drew
+    // one draws again at once (a few rounds) instead of idling through the turn
+    for (int draw = 0; draw < kMaxDraws; draw++) {
+      const unsigned long long t = claim_item(phase == kLaneIdle, work);
+      if (phase == kLaneIdle) {
+        if (t >= (unsigned long long)count) {
+          phase = kLaneDone;
+        } else {
+          const int64_t i = start + (int64_t)t * stride;
+          if (lvl[i] >= level) {  // else labelled already
+            split_index(V, i, x, y, z);
+            cur = {(float)x, (float)y, (float)z};
+            iters = A.P.iteration_limit;
+            anchor = cur;
+            t_iters = iters;
+            t_n = 0;
+            last_nv = -1;
+            np = 0;
+            path[np++] = (int)i;
+            phase = kLaneEnter;
+          }
         }
       }
+      if (!__any_sync(kFullMask, phase == kLaneIdle)) break;
     }
     if (__all_sync(kFullMask, phase == kLaneDone)) {
       add_trips(ntrips, trips);
