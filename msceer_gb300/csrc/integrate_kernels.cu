@@ -261,7 +261,9 @@ __device__ __forceinline__ void add_trips(unsigned long long n, unsigned long lo
   if ((threadIdx.x & 31) == 0 && n) atomicAdd(trips, n);
 }
 
-// One level of the spread order.  Streamlines of a level see only the labels of
+// One level of the spread order (or a group of consecutive small levels, [L0, L1),
+// which then act as one level: each of those launches would wait for its slowest
+// streamline while the GPU idles).  Streamlines of a level see only the labels of
 // earlier levels (lvl[v] < level; terminals are level 0, unlabelled vertices 255),
 // so a level's outcome does not depend on thread timing; where several streamlines
 // of the level pass the same unlabelled vertex, the smallest label wins (unsigned
@@ -269,12 +271,13 @@ __device__ __forceinline__ void add_trips(unsigned long long n, unsigned long lo
 // pass is therefore deterministic.  `work` counts the level's claimed items (zero at
 // launch).
 template <int K>
-__global__ void __launch_bounds__(128, 6) integrate_level_kernel(const Adv32 A, int64_t start, int64_t stride, int64_t count,
+__global__ void __launch_bounds__(128, 6) integrate_level_kernel(const Adv32 A, const SpreadOrder S, int L0, int L1,
                                                               int32_t* __restrict__ lab, uint8_t* __restrict__ lvl,
                                                               unsigned long long* __restrict__ work,
                                                               unsigned long long* __restrict__ trips) {
   const VolDims& V = A.V;
   const int level = A.level;
+  const int64_t count = S.offset[L1] - S.offset[L0];
   int path[kPathCap];
   int np = 0;
   int64_t end = 0;
@@ -299,7 +302,10 @@ __global__ void __launch_bounds__(128, 6) integrate_level_kernel(const Adv32 A, 
         if (t >= (unsigned long long)count) {
           phase = kLaneDone;
         } else {
-          const int64_t i = start + (int64_t)t * stride;
+          const int64_t u = S.offset[L0] + (int64_t)t;
+          int L = L0;
+          while (L + 1 < L1 && S.offset[L + 1] <= u) L++;
+          const int64_t i = S.start[L] + (u - S.offset[L]) * S.stride[L];
           if (lvl[i] >= level) {  // else labelled already
             split_index(V, i, x, y, z);
             cur = {(float)x, (float)y, (float)z};
@@ -434,6 +440,17 @@ struct Adv64 {
     nearest3(p, ix, iy, iz);
     return vid(V, ix, iy, iz);
   }
+  // The FP32 advector's trapped-streamline test on FP64 positions.
+  __device__ __forceinline__ bool trapped(const D3& cur, D3& anchor, int& n) const {
+    const double d = fmax(fabs(cur.x - anchor.x), fmax(fabs(cur.y - anchor.y), fabs(cur.z - anchor.z)));
+    const double rx = (cur.x + 0.5) - floor(cur.x + 0.5);
+    const double ry = (cur.y + 0.5) - floor(cur.y + 0.5);
+    const double rz = (cur.z + 0.5) - floor(cur.z + 0.5);
+    const double mg = fmin(fmin(fmin(rx, 1.0 - rx), fmin(ry, 1.0 - ry)), fmin(rz, 1.0 - rz));
+    n = (d < (double)P.trap_radius && mg > (double)P.trap_margin) ? n + 1 : 0;
+    anchor = cur;
+    return n >= 2;
+  }
   // The FP32 advector's enter / trip in the reference's FP64 arithmetic.
   __device__ __forceinline__ bool enter(const D3& cur, bool nearb, double bf[3], D3 c[8], D3& g, float& gm,
                                         float& step) const {
@@ -544,6 +561,8 @@ __global__ void __launch_bounds__(128) fixup_kernel(const Adv64 A, int32_t* __re
   bool nb = false;
   double b[3] = {0.0, 0.0, 0.0};
   D3 c[8];
+  D3 anchor = cur;  // trapped-streamline test (off in the all-FP64 mode)
+  int t_iters = 0, t_n = 0;
   while (true) {
     const unsigned long long k = claim_item(phase == kLaneIdle, work);
     if (phase == kLaneIdle) {
@@ -556,6 +575,9 @@ __global__ void __launch_bounds__(128) fixup_kernel(const Adv64 A, int32_t* __re
         split_index(V, v, x, y, z);
         cur = {(double)x, (double)y, (double)z};
         iters = A.P.iteration_limit;
+        anchor = cur;
+        t_iters = iters;
+        t_n = 0;
         phase = kLaneEnter;
       }
     }
@@ -580,6 +602,13 @@ __global__ void __launch_bounds__(128) fixup_kernel(const Adv64 A, int32_t* __re
       if (ev == EV_NONE) continue;
       A.nearest3(cur, x, y, z);
       phase = ev == EV_OUT_OF_VOXEL ? kLaneEnter : kLaneEnd;
+    }
+    if (phase == kLaneStep && A.P.trap_window > 0 && t_iters - iters >= A.P.trap_window) {
+      t_iters = iters;
+      if (A.trapped(cur, anchor, t_n)) {  // ends where the iteration limit would have
+        A.nearest3(cur, x, y, z);
+        phase = kLaneEnd;
+      }
     }
     if (phase != kLaneEnd) continue;
     phase = kLaneIdle;
@@ -868,25 +897,33 @@ cudaError_t launch_integrate_pass1(const float4* G, const VolDims& V, const Inte
   if (cudaError_t e = cudaMemsetAsync(work, 0, sizeof(unsigned long long) * 48, stream)) return e;
   ::msc::count_launch();
   init_levels_kernel<<<num_sms * 8, 256, 0, stream>>>(lab, lvl, N);
-  for (int L = 0; L < S.nlev; L++) {
-    const int64_t count = S.offset[L + 1] - S.offset[L];
+  // the levels up to a total of max(2^16, N/512) items form the first group
+  const int64_t small = N / 512 > 65536 ? N / 512 : 65536;
+  int stamp = 0;
+  for (int L0 = 0; L0 < S.nlev;) {
+    int L1 = L0 + 1;
+    while (L1 < S.nlev && S.offset[L1 + 1] - S.offset[L0] <= small) L1++;
+    const int64_t count = S.offset[L1] - S.offset[L0];
+    const int g0 = L0;
+    L0 = L1;
     if (count <= 0) continue;
-    const Adv32 A = Adv32::make(G, V, P, lab, lvl, L + 1, nullptr);
+    const Adv32 A = Adv32::make(G, V, P, lab, lvl, ++stamp, nullptr);
     const int64_t blocks = (count + 127) / 128;
     const int grid = (int)(blocks < num_sms * kLaneCtasPerSm ? blocks : num_sms * kLaneCtasPerSm);
+    unsigned long long* w = work + (stamp - 1);
     ::msc::count_launch();
     switch (trips_per_turn()) {
       case 16:
-        integrate_level_kernel<16><<<grid, 128, 0, stream>>>(A, S.start[L], S.stride[L], count, lab, lvl, work + L, trips);
+        integrate_level_kernel<16><<<grid, 128, 0, stream>>>(A, S, g0, L1, lab, lvl, w, trips);
         break;
       case 2:
-        integrate_level_kernel<2><<<grid, 128, 0, stream>>>(A, S.start[L], S.stride[L], count, lab, lvl, work + L, trips);
+        integrate_level_kernel<2><<<grid, 128, 0, stream>>>(A, S, g0, L1, lab, lvl, w, trips);
         break;
       case 4:
-        integrate_level_kernel<4><<<grid, 128, 0, stream>>>(A, S.start[L], S.stride[L], count, lab, lvl, work + L, trips);
+        integrate_level_kernel<4><<<grid, 128, 0, stream>>>(A, S, g0, L1, lab, lvl, w, trips);
         break;
       default:
-        integrate_level_kernel<8><<<grid, 128, 0, stream>>>(A, S.start[L], S.stride[L], count, lab, lvl, work + L, trips);
+        integrate_level_kernel<8><<<grid, 128, 0, stream>>>(A, S, g0, L1, lab, lvl, w, trips);
     }
   }
   return cudaGetLastError();

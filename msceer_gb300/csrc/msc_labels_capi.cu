@@ -326,7 +326,7 @@ int prepare_direction(LabelCtx& c, DirLabels& d, int32_t* stage_terminal) {
 // Streamlines that orbit a sink of the interpolated gradient without reaching the
 // stop threshold run to the iteration limit and end at their nearest vertex (on k^-3
 // fields ~4% of the descending boundary re-decisions, ~3/4 of all their iterations).
-// Outside the all-FP64 mode the FP32 kernels end such a streamline once it has
+// Outside the all-FP64 mode the integration kernels end such a streamline once it has
 // stayed within 0.02 voxel for two windows of 128 iterations, 0.05 voxel or more
 // inside its nearest vertex's cell: the same nearest vertex, hence the same label,
 // unless the orbit would later escape (measured with the FP64 oracle on k^-3 and
