@@ -897,8 +897,9 @@ cudaError_t launch_integrate_pass1(const float4* G, const VolDims& V, const Inte
   if (cudaError_t e = cudaMemsetAsync(work, 0, sizeof(unsigned long long) * 48, stream)) return e;
   ::msc::count_launch();
   init_levels_kernel<<<num_sms * 8, 256, 0, stream>>>(lab, lvl, N);
-  // the levels up to a total of max(2^16, N/512) items form the first group
-  const int64_t small = N / 512 > 65536 ? N / 512 : 65536;
+  // the levels up to a total of N/512 items form the first group (a fraction of the
+  // volume small enough that their mutual path compression does not matter)
+  const int64_t small = N / 512;
   int stamp = 0;
   for (int L0 = 0; L0 < S.nlev;) {
     int L1 = L0 + 1;
