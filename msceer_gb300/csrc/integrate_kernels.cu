@@ -362,13 +362,26 @@ __global__ void __launch_bounds__(128, 6) integrate_level_kernel(const Adv32 A, 
       }
     }
     if (phase == kLaneEnd) {
-      int32_t dest = lvl[end] < level ? lab[end] : -1;
+      const uint8_t le = lvl[end];
+      const int32_t lb = lab[end];
+      int32_t dest = le < level ? lb : -1;
       if (dest == -1) dest = kLabelNone;  // reached no region: assigned to nothing
-      for (int k = 0; k < np; k++) {
-        const int p = path[k];
-        if (lvl[p] < level) continue;  // labelled in an earlier level: keep
-        atomicMin(reinterpret_cast<unsigned int*>(&lab[p]), (unsigned int)dest);
-        lvl[p] = (uint8_t)level;
+      // the path's level bytes are read eight at a time, so that one lane's write-back
+      // waits for a memory round trip per eight vertices rather than per vertex
+      for (int k0 = 0; k0 < np; k0 += 8) {
+        int pk[8];
+        uint8_t lk[8];
+#pragma unroll
+        for (int j = 0; j < 8; j++) {
+          pk[j] = k0 + j < np ? path[k0 + j] : -1;
+          lk[j] = pk[j] >= 0 ? lvl[pk[j]] : 0;
+        }
+#pragma unroll
+        for (int j = 0; j < 8; j++) {
+          if (pk[j] < 0 || lk[j] < level) continue;  // labelled in an earlier level: keep
+          atomicMin(reinterpret_cast<unsigned int*>(&lab[pk[j]]), (unsigned int)dest);
+          lvl[pk[j]] = (uint8_t)level;
+        }
       }
       phase = kLaneIdle;
     }
@@ -720,6 +733,7 @@ __global__ void __launch_bounds__(128, 6) fixup32_kernel(const Adv32 A, int32_t*
     if (phase != kLaneEnd) continue;
     phase = kLaneIdle;
     const int64_t end = vid(V, x, y, z);
+    const int32_t lend = lab0[end];
     // a low-gradient stop whose FP32 magnitude lies within 2^-8 (relative) of the
     // threshold: FP32 rounding could have taken the other side of the stop test.  A
     // streamline that decelerates into an extremum crosses the threshold well inside
@@ -729,7 +743,7 @@ __global__ void __launch_bounds__(128, 6) fixup32_kernel(const Adv32 A, int32_t*
       const float pc[3] = {cur.x, cur.y, cur.z};
       const int64_t ext[3] = {V.X, V.Y, V.Z};
       const int64_t ev3[3] = {x, y, z};
-      const int32_t le = lab0[end];
+      const int32_t le = lend;
 #pragma unroll
       for (int a = 0; a < 3; a++) {
         const float q = pc[a] + 0.5f;
@@ -762,7 +776,7 @@ __global__ void __launch_bounds__(128, 6) fixup32_kernel(const Adv32 A, int32_t*
       continue;
     }
     atomicAnd(&queued[v >> 5], ~(1u << (v & 31)));
-    int32_t nl = lab0[end];
+    int32_t nl = lend;
     if (nl == -1) nl = kLabelNone;
     lab[v] = nl;
     state[v] = kStNonterminal;
@@ -771,10 +785,18 @@ __global__ void __launch_bounds__(128, 6) fixup32_kernel(const Adv32 A, int32_t*
     split_index(V, v, vx, vy, vz);
     const int64_t nbr[6] = {vx < V.X - 1 ? v + 1 : -1, vx > 0 ? v - 1 : -1, vy < V.Y - 1 ? v + V.X : -1,
                             vy > 0 ? v - V.X : -1, vz < V.Z - 1 ? v + V.X * V.Y : -1, vz > 0 ? v - V.X * V.Y : -1};
+    // the six neighbours' bytes and labels are read together (one memory round trip)
+    uint8_t su[6];
+    int32_t lu[6];
+#pragma unroll
+    for (int j = 0; j < 6; j++) {
+      su[j] = nbr[j] >= 0 ? state[nbr[j]] : (uint8_t)kStNonterminal;
+      lu[j] = nbr[j] >= 0 ? lab[nbr[j]] : nl;
+    }
 #pragma unroll
     for (int j = 0; j < 6; j++) {
       const int64_t u = nbr[j];
-      if (u < 0 || state[u] != kStUnassigned || lab[u] == nl) continue;
+      if (su[j] != kStUnassigned || lu[j] == nl) continue;
       const uint32_t bit = 1u << (u & 31);
       if (atomicOr(&queued[u >> 5], bit) & bit) continue;
       next[atomicAdd(n_next, 1)] = u;
