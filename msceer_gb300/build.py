@@ -71,7 +71,7 @@ def build_library(verbose: bool = False, force: bool = False) -> Path:
             list(ex.map(lambda c: _run(c, verbose), jobs))
     if force or jobs or _stale(LIB, objs):
         tmp = LIB.with_suffix(".so.tmp")
-        _run([nvcc, *GENCODE, "-shared", "-o", tmp, *objs, "-lcudart"], verbose)
+        _run([nvcc, *GENCODE, "-shared", "-o", tmp, *objs, "-lcudart", "-lpthread"], verbose)
         os.replace(tmp, LIB)
     return LIB
 

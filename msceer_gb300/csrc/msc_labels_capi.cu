@@ -6,7 +6,10 @@
 #include <climits>
 #include <cmath>
 #include <cstring>
+#include <condition_variable>
+#include <mutex>
 #include <queue>
+#include <thread>
 #include <string>
 #include <utility>
 #include <vector>
@@ -460,9 +463,84 @@ int finish_errors(LabelCtx& c) {
   return MSC_OK;
 }
 
+int labels_concurrent(const float* f, const uint8_t* grad, const int64_t* dims, const msc_integ_params* p,
+                      int32_t* out_asc, int32_t* out_dsc, int32_t* stages, cudaStream_t st);
+
+// The descending direction of a two-direction call on its own stream and host thread,
+// concurrently with the ascending one: the two share nothing but the inputs, so their
+// kernels fill each other's idle time (launch tails, host synchronisation, the FP64
+// re-decisions).  The reference integrates the descending labels on the gradient the
+// ascending pass zeroed at the minima' seeds; this job has its own gradient copy and
+// zeroes those seeds too once the ascending job has found them (`asc_seeds`).
+struct SeedHandoff {
+  std::mutex mu;
+  std::condition_variable cv;
+  bool ready = false;
+  const int64_t* seed = nullptr;  // device, on the ascending job's stream
+  int n = -1;                     // -1: the ascending job failed before its seeds
+  cudaEvent_t done = nullptr;     // recorded on the ascending stream after the seeds
+  void publish(const int64_t* s, int k, cudaEvent_t e) {
+    std::lock_guard<std::mutex> lk(mu);
+    seed = s;
+    n = k;
+    done = e;
+    ready = true;
+    cv.notify_all();
+  }
+};
+
+struct DscJob {
+  int rc = MSC_OK;
+  std::string err;
+  int64_t stats[2] = {0, 0};
+  int64_t trips[3] = {0, 0, 0};
+};
+
+void run_dsc_job(int dev, cudaEvent_t inputs_ready, const float* f, const uint8_t* grad, const int64_t* dims,
+                 const msc_integ_params* p, int32_t* out, int32_t* stages, SeedHandoff* asc, DscJob* job) {
+  auto body = [&]() -> int {
+    LCUDA(cudaSetDevice(dev), "cudaSetDevice");
+    cudaStream_t sb = nullptr;
+    LCUDA(cudaStreamCreateWithFlags(&sb, cudaStreamNonBlocking), "cudaStreamCreate");
+    struct Destroy {
+      cudaStream_t s;
+      ~Destroy() {
+        cudaStreamSynchronize(s);
+        cudaStreamDestroy(s);
+      }
+    } ds{sb};
+    LCUDA(cudaStreamWaitEvent(sb, inputs_ready, 0), "cudaStreamWaitEvent");
+    int rc = MSC_OK;
+    {
+      LabelCtx c(sb);
+      if ((rc = setup_ctx(c, f, grad, dims, p))) return rc;
+      DirLabels d;
+      d.dir = 1;
+      if ((rc = prepare_direction(c, d, stages ? stages + 2 * c.N : nullptr))) return rc;
+      {
+        std::unique_lock<std::mutex> lk(asc->mu);
+        asc->cv.wait(lk, [&] { return asc->ready; });
+      }
+      if (asc->n < 0) return fail(MSC_ERR_CUDA, "ascending labels failed");
+      if (asc->n > 0) {
+        LCUDA(cudaStreamWaitEvent(sb, asc->done, 0), "cudaStreamWaitEvent");
+        ::msc::count_launch();
+        zero_seed_grad_kernel<<<(asc->n + 255) / 256, 256, 0, sb>>>(asc->seed, asc->n, c.g32, c.g64);
+      }
+      if ((rc = integrate_direction(c, d, out, stages ? stages + 3 * c.N : nullptr, job->stats))) return rc;
+      for (int k = 0; k < 3; k++) job->trips[k] = d.trips[k];
+      rc = finish_errors(c);
+    }
+    return rc;
+  };
+  job->rc = body();
+  if (job->rc != MSC_OK) job->err = t_err;
+}
+
 int labels_impl(const float* f, const uint8_t* grad, const int64_t* dims, const msc_integ_params* p, int32_t* out_asc,
                 int32_t* out_dsc, int32_t* stages, cudaStream_t st) {
   if (!out_asc && !out_dsc) return fail(MSC_ERR_NULL_POINTER, "null argument");
+  if (out_asc && out_dsc) return labels_concurrent(f, grad, dims, p, out_asc, out_dsc, stages, st);
   LabelCtx c(st);
   if (int rc = setup_ctx(c, f, grad, dims, p)) return rc;
   for (int k = 0; k < 4; k++) t_stats[k] = 0;
@@ -478,6 +556,60 @@ int labels_impl(const float* f, const uint8_t* grad, const int64_t* dims, const 
     for (int k = 0; k < 3; k++) t_trips[3 * pass + k] = d.trips[k];
   }
   return finish_errors(c);
+}
+
+// Both directions: the ascending one on the caller's stream and thread, the
+// descending one concurrently (run_dsc_job).
+int labels_concurrent(const float* f, const uint8_t* grad, const int64_t* dims, const msc_integ_params* p,
+                      int32_t* out_asc, int32_t* out_dsc, int32_t* stages, cudaStream_t st) {
+  for (int k = 0; k < 4; k++) t_stats[k] = 0;
+  for (int k = 0; k < 6; k++) t_trips[k] = 0;
+  int dev = 0;
+  LCUDA(cudaGetDevice(&dev), "cudaGetDevice");
+  cudaEvent_t inputs_ready = nullptr, seeds_done = nullptr;
+  LCUDA(cudaEventCreateWithFlags(&inputs_ready, cudaEventDisableTiming), "cudaEventCreate");
+  LCUDA(cudaEventCreateWithFlags(&seeds_done, cudaEventDisableTiming), "cudaEventCreate");
+  struct Events {
+    cudaEvent_t a, b;
+    ~Events() {
+      cudaEventDestroy(a);
+      cudaEventDestroy(b);
+    }
+  } evs{inputs_ready, seeds_done};
+  LCUDA(cudaEventRecord(inputs_ready, st), "cudaEventRecord");
+  SeedHandoff handoff;
+  DscJob job;
+  std::thread worker;
+  try {
+    worker = std::thread(run_dsc_job, dev, inputs_ready, f, grad, dims, p, out_dsc, stages, &handoff, &job);
+  } catch (...) {
+    return fail(MSC_ERR_CUDA, "could not start the descending labels' host thread");
+  }
+  int rc = MSC_OK;
+  {
+    LabelCtx c(st);
+    DirLabels d;
+    d.dir = -1;
+    rc = setup_ctx(c, f, grad, dims, p);
+    if (rc == MSC_OK) rc = prepare_direction(c, d, stages);
+    if (rc == MSC_OK) {
+      // the minima' seeds: run_dsc_job zeroes them in its gradient copy
+      const cudaError_t e = cudaEventRecord(seeds_done, st);
+      if (e != cudaSuccess) rc = fail(MSC_ERR_CUDA, std::string("cudaEventRecord: ") + cudaGetErrorString(e));
+    }
+    handoff.publish(d.seed, rc == MSC_OK ? d.n_ext : -1, seeds_done);
+    if (rc == MSC_OK) rc = integrate_direction(c, d, out_asc, stages ? stages + c.N : nullptr, t_stats);
+    for (int k = 0; k < 3; k++) t_trips[k] = d.trips[k];
+    if (rc == MSC_OK) rc = finish_errors(c);
+    // the descending job reads d.seed from this context's pool: wait for it first
+    worker.join();
+  }
+  if (rc != MSC_OK) return rc;
+  if (job.rc != MSC_OK) return fail(job.rc, job.err);
+  t_stats[2] = job.stats[0];
+  t_stats[3] = job.stats[1];
+  for (int k = 0; k < 3; k++) t_trips[3 + k] = job.trips[k];
+  return MSC_OK;
 }
 
 // Network features of one direction from its first-pass labels (triage_prep.cu).
