@@ -464,7 +464,10 @@ int finish_errors(LabelCtx& c) {
 }
 
 int labels_concurrent(const float* f, const uint8_t* grad, const int64_t* dims, const msc_integ_params* p,
-                      int32_t* out_asc, int32_t* out_dsc, int32_t* stages, cudaStream_t st);
+                      const msc_triage_params* tp, int32_t* out_asc, int32_t* out_dsc, int32_t* stages,
+                      int64_t* tstats, cudaStream_t st);
+int direction_rest(LabelCtx& c, DirLabels& d, int k, const msc_triage_params* tp, int32_t* out,
+                   int32_t* stage_integrated, int64_t fix[2], int64_t counts_out[3]);
 
 // The descending direction of a two-direction call on its own stream and host thread,
 // concurrently with the ascending one: the two share nothing but the inputs, so their
@@ -494,10 +497,12 @@ struct DscJob {
   std::string err;
   int64_t stats[2] = {0, 0};
   int64_t trips[3] = {0, 0, 0};
+  int64_t counts[3] = {0, 0, 0};  // triage: flagged, audited, audited the fix-up changed
 };
 
 void run_dsc_job(int dev, cudaEvent_t inputs_ready, const float* f, const uint8_t* grad, const int64_t* dims,
-                 const msc_integ_params* p, int32_t* out, int32_t* stages, SeedHandoff* asc, DscJob* job) {
+                 const msc_integ_params* p, const msc_triage_params* tp, int32_t* out, int32_t* stages,
+                 SeedHandoff* asc, DscJob* job) {
   auto body = [&]() -> int {
     LCUDA(cudaSetDevice(dev), "cudaSetDevice");
     cudaStream_t sb = nullptr;
@@ -527,7 +532,8 @@ void run_dsc_job(int dev, cudaEvent_t inputs_ready, const float* f, const uint8_
         ::msc::count_launch();
         zero_seed_grad_kernel<<<(asc->n + 255) / 256, 256, 0, sb>>>(asc->seed, asc->n, c.g32, c.g64);
       }
-      if ((rc = integrate_direction(c, d, out, stages ? stages + 3 * c.N : nullptr, job->stats))) return rc;
+      if ((rc = direction_rest(c, d, 1, tp, out, stages ? stages + 3 * c.N : nullptr, job->stats, job->counts)))
+        return rc;
       for (int k = 0; k < 3; k++) job->trips[k] = d.trips[k];
       rc = finish_errors(c);
     }
@@ -540,7 +546,7 @@ void run_dsc_job(int dev, cudaEvent_t inputs_ready, const float* f, const uint8_
 int labels_impl(const float* f, const uint8_t* grad, const int64_t* dims, const msc_integ_params* p, int32_t* out_asc,
                 int32_t* out_dsc, int32_t* stages, cudaStream_t st) {
   if (!out_asc && !out_dsc) return fail(MSC_ERR_NULL_POINTER, "null argument");
-  if (out_asc && out_dsc) return labels_concurrent(f, grad, dims, p, out_asc, out_dsc, stages, st);
+  if (out_asc && out_dsc) return labels_concurrent(f, grad, dims, p, nullptr, out_asc, out_dsc, stages, nullptr, st);
   LabelCtx c(st);
   if (int rc = setup_ctx(c, f, grad, dims, p)) return rc;
   for (int k = 0; k < 4; k++) t_stats[k] = 0;
@@ -561,7 +567,8 @@ int labels_impl(const float* f, const uint8_t* grad, const int64_t* dims, const 
 // Both directions: the ascending one on the caller's stream and thread, the
 // descending one concurrently (run_dsc_job).
 int labels_concurrent(const float* f, const uint8_t* grad, const int64_t* dims, const msc_integ_params* p,
-                      int32_t* out_asc, int32_t* out_dsc, int32_t* stages, cudaStream_t st) {
+                      const msc_triage_params* tp, int32_t* out_asc, int32_t* out_dsc, int32_t* stages,
+                      int64_t* tstats, cudaStream_t st) {
   for (int k = 0; k < 4; k++) t_stats[k] = 0;
   for (int k = 0; k < 6; k++) t_trips[k] = 0;
   int dev = 0;
@@ -581,11 +588,12 @@ int labels_concurrent(const float* f, const uint8_t* grad, const int64_t* dims, 
   DscJob job;
   std::thread worker;
   try {
-    worker = std::thread(run_dsc_job, dev, inputs_ready, f, grad, dims, p, out_dsc, stages, &handoff, &job);
+    worker = std::thread(run_dsc_job, dev, inputs_ready, f, grad, dims, p, tp, out_dsc, stages, &handoff, &job);
   } catch (...) {
     return fail(MSC_ERR_CUDA, "could not start the descending labels' host thread");
   }
   int rc = MSC_OK;
+  int64_t counts[3] = {0, 0, 0};
   {
     LabelCtx c(st);
     DirLabels d;
@@ -598,7 +606,7 @@ int labels_concurrent(const float* f, const uint8_t* grad, const int64_t* dims, 
       if (e != cudaSuccess) rc = fail(MSC_ERR_CUDA, std::string("cudaEventRecord: ") + cudaGetErrorString(e));
     }
     handoff.publish(d.seed, rc == MSC_OK ? d.n_ext : -1, seeds_done);
-    if (rc == MSC_OK) rc = integrate_direction(c, d, out_asc, stages ? stages + c.N : nullptr, t_stats);
+    if (rc == MSC_OK) rc = direction_rest(c, d, 0, tp, out_asc, stages ? stages + c.N : nullptr, t_stats, counts);
     for (int k = 0; k < 3; k++) t_trips[k] = d.trips[k];
     if (rc == MSC_OK) rc = finish_errors(c);
     // the descending job reads d.seed from this context's pool: wait for it first
@@ -609,6 +617,14 @@ int labels_concurrent(const float* f, const uint8_t* grad, const int64_t* dims, 
   t_stats[2] = job.stats[0];
   t_stats[3] = job.stats[1];
   for (int k = 0; k < 3; k++) t_trips[3 + k] = job.trips[k];
+  if (tstats) {
+    for (int k = 0; k < 3; k++) {
+      tstats[k] = counts[k];
+      tstats[4 + k] = job.counts[k];
+    }
+    tstats[3] = t_stats[0];
+    tstats[7] = t_stats[2];
+  }
   return MSC_OK;
 }
 
@@ -647,18 +663,21 @@ int triage_features_impl(const float* f, const uint8_t* grad, const int64_t* dim
   return finish_errors(c);
 }
 
-int triage_labels_impl(const float* f, const uint8_t* grad, const int64_t* dims, const msc_integ_params* p,
-                       const msc_triage_params* tp, int32_t* out_asc, int32_t* out_dsc, int64_t* stats,
-                       cudaStream_t st) {
-  if (!out_asc || !out_dsc || !tp || !tp->weights) return fail(MSC_ERR_NULL_POINTER, "null argument");
-  LabelCtx c(st);
-  if (int rc = setup_ctx(c, f, grad, dims, p)) return rc;
+// After prepare_direction: the plain rest of one direction (first pass, fix-up,
+// cleaner) or, with `tp`, the triaged one -- first pass, network features and
+// inference, the flagged vertices plus the audit into the fix-up, the audit count.
+// k: 0 ascending, 1 descending; counts_out (triage): flagged, audited, audited the
+// fix-up changed.
+int direction_rest(LabelCtx& c, DirLabels& d, int k, const msc_triage_params* tp, int32_t* out,
+                   int32_t* stage_integrated, int64_t fix[2], int64_t counts_out[3]) {
+  if (!tp) return integrate_direction(c, d, out, stage_integrated, fix);
+  cudaStream_t st = c.st;
   const int64_t N = c.N;
   uint8_t *blobs, *flags;
   __nv_bfloat16 *feat, *act1, *act2;
   float* logits;
   int32_t* first;
-  unsigned long long* counts;  // per direction: flagged, audited, audited the fix-up changed
+  unsigned long long* counts;
   LCUDA(c.pool.get(&blobs, msc::kTriageBlobBytes), "alloc");
   LCUDA(c.pool.get(&feat, 16 * N), "alloc");
   LCUDA(c.pool.get(&act1, 16 * N), "alloc");
@@ -666,41 +685,36 @@ int triage_labels_impl(const float* f, const uint8_t* grad, const int64_t* dims,
   LCUDA(c.pool.get(&logits, 2 * N), "alloc");
   LCUDA(c.pool.get(&flags, N), "alloc");
   LCUDA(c.pool.get(&first, N), "alloc");
-  LCUDA(c.pool.get(&counts, 6), "alloc");
-  LCUDA(cudaMemsetAsync(counts, 0, 6 * sizeof(unsigned long long), st), "memset");
+  LCUDA(c.pool.get(&counts, 3), "alloc");
+  LCUDA(cudaMemsetAsync(counts, 0, 3 * sizeof(unsigned long long), st), "memset");
   const msc::ConvDims D{c.V.X, c.V.Y, c.V.Z, N};
-  const float thr[2] = {tp->logit_threshold_asc, tp->logit_threshold_dsc};
-  int32_t* outs[2] = {out_asc, out_dsc};
-  int64_t fix[4] = {0, 0, 0, 0};
-  for (int k = 0; k < 6; k++) t_trips[k] = 0;
-  for (int k = 0; k < 2; k++) {
-    DirLabels d;
-    d.dir = k == 0 ? -1 : 1;
-    if (int rc = prepare_direction(c, d, nullptr)) return rc;
-    if (int rc = first_pass(c, d)) return rc;
-    if (int rc = direction_features(c, d, feat)) return rc;
-    LCUDA(msc::triage_forward(feat, D, tp->weights, blobs, act1, act2, logits, c.counters + 4, st), "triage forward");
-    LCUDA(cudaMemcpyAsync(first, d.lab, N * sizeof(int32_t), cudaMemcpyDeviceToDevice, st), "copy");
-    LCUDA(msc::launch_triage_apply(logits, thr[k], d.state, flags, N, tp->audit_fraction, tp->audit_seed + (uint64_t)k,
-                                   counts + 3 * k, c.sms, st),
-          "triage apply");
-    if (int rc = finish_direction(c, d, outs[k], nullptr, fix + 2 * k)) return rc;
-    for (int q = 0; q < 3; q++) t_trips[3 * k + q] = d.trips[q];
-    LCUDA(msc::launch_audit_count(d.lab, first, flags, N, counts + 3 * k + 2, c.sms, st), "audit");
-  }
-  for (int k = 0; k < 4; k++) t_stats[k] = fix[k];
-  if (stats) {
-    unsigned long long h[6];
-    LCUDA(cudaMemcpyAsync(h, counts, sizeof(h), cudaMemcpyDeviceToHost, st), "read counts");
-    LCUDA(cudaStreamSynchronize(st), "sync");
-    for (int k = 0; k < 2; k++) {
-      stats[4 * k + 0] = (int64_t)h[3 * k];
-      stats[4 * k + 1] = (int64_t)h[3 * k + 1];
-      stats[4 * k + 2] = (int64_t)h[3 * k + 2];
-      stats[4 * k + 3] = fix[2 * k];
-    }
-  }
-  return finish_errors(c);
+  const float thr = k == 0 ? tp->logit_threshold_asc : tp->logit_threshold_dsc;
+  if (int rc = first_pass(c, d)) return rc;
+  if (int rc = direction_features(c, d, feat)) return rc;
+  LCUDA(msc::triage_forward(feat, D, tp->weights, blobs, act1, act2, logits, c.counters + 4, st), "triage forward");
+  LCUDA(cudaMemcpyAsync(first, d.lab, N * sizeof(int32_t), cudaMemcpyDeviceToDevice, st), "copy");
+  LCUDA(msc::launch_triage_apply(logits, thr, d.state, flags, N, tp->audit_fraction, tp->audit_seed + (uint64_t)k,
+                                 counts, c.sms, st),
+        "triage apply");
+  if (int rc = finish_direction(c, d, out, nullptr, fix)) return rc;
+  LCUDA(msc::launch_audit_count(d.lab, first, flags, N, counts + 2, c.sms, st), "audit");
+  unsigned long long h[3];
+  LCUDA(cudaMemcpyAsync(h, counts, sizeof(h), cudaMemcpyDeviceToHost, st), "read counts");
+  LCUDA(cudaStreamSynchronize(st), "sync");
+  for (int q = 0; q < 3; q++) counts_out[q] = (int64_t)h[q];
+  return MSC_OK;
+}
+
+// Both directions with triage, concurrently (labels_concurrent).
+int triage_labels_impl(const float* f, const uint8_t* grad, const int64_t* dims, const msc_integ_params* p,
+                       const msc_triage_params* tp, int32_t* out_asc, int32_t* out_dsc, int64_t* stats,
+                       cudaStream_t st) {
+  if (!out_asc || !out_dsc || !tp || !tp->weights) return fail(MSC_ERR_NULL_POINTER, "null argument");
+  int64_t tstats[8];
+  if (int rc = labels_concurrent(f, grad, dims, p, tp, out_asc, out_dsc, nullptr, tstats, st)) return rc;
+  if (stats)
+    for (int k = 0; k < 8; k++) stats[k] = tstats[k];
+  return MSC_OK;
 }
 
 // Per-thread device staging of the host-buffer entry, kept between calls.
