@@ -72,9 +72,10 @@ struct Adv32 {
     return A;
   }
 
-  // the eight corner gradients of the voxel with base corner b: the index offsets of
-  // the two planes along each axis are formed once (clamped into the grid near its
-  // faces), each corner is then two additions away
+  __device__ __forceinline__ F3 corner(int64_t x, int64_t y, int64_t z) const {
+    const float4 g = __ldg(G + vid(V, x, y, z));
+    return {g.x, g.y, g.z};
+  }
   __device__ __forceinline__ void surround(const int64_t b[3], bool clamp, F3 c[8]) const {
     int64_t vv[3][2];
     const int64_t ext[3] = {V.X, V.Y, V.Z};
@@ -87,13 +88,8 @@ struct Adv32 {
         if (b[a] >= ext[a] - 1) vv[a][0] = vv[a][1] = ext[a] - 1;
       }
     }
-    const int64_t sy = V.X, sz = V.X * V.Y;
-    const int64_t oy[2] = {vv[1][0] * sy, vv[1][1] * sy}, oz[2] = {vv[2][0] * sz, vv[2][1] * sz};
 #pragma unroll
-    for (int n = 0; n < 8; n++) {
-      const float4 g = __ldg(G + (vv[0][n & 1] + oy[(n >> 1) & 1] + oz[n >> 2]));
-      c[n] = {g.x, g.y, g.z};
-    }
+    for (int n = 0; n < 8; n++) c[n] = corner(vv[0][n & 1], vv[1][(n >> 1) & 1], vv[2][n >> 2]);
   }
   // bf: the base corner as floats
   __device__ __forceinline__ static F3 trilin(F3 s, const float bf[3], const F3 c[8]) {
@@ -127,11 +123,11 @@ struct Adv32 {
     return n >= 2;
   }
   // AdvectThroughVoxel{NoCheck,NearBoundary} split in two, so that a lane can run its
-  // streamline one iteration at a time.  enter(): the voxel's base corner and its
-  // eight corner gradients; the gradient at `cur` and the first step follow in the
-  // next trip() (`fresh`), in the branch every lane takes after it moved, so that a
-  // lane entering a voxel adds only its loads to the warp's work.
-  __device__ __forceinline__ void enter(const F3& cur, bool nearb, float bf[3], F3 c[8]) const {
+  // streamline one iteration at a time.  enter(): the voxel's base corner, its eight
+  // corner gradients and the gradient at `cur`; false when there is no direction to
+  // follow (LOW_GRADIENT).  The caller then sets old = cur.
+  __device__ __forceinline__ bool enter(const F3& cur, bool nearb, float bf[3], F3 c[8], F3& g, float& gm,
+                                        float& step, float& gm_end) const {
     int64_t b[3];
     if (nearb) {
       b[0] = (int)clampf_ext(cur.x, ext[0]);
@@ -146,27 +142,25 @@ struct Adv32 {
     bf[0] = (float)(int)b[0];
     bf[1] = (float)(int)b[1];
     bf[2] = (float)(int)b[2];
+    g = trilin(cur, bf, c);
+    gm = sqrtf(g.x * g.x + g.y * g.y + g.z * g.z);
+    gm_end = 0.f;
+    if (!(gm > 0.f) || !isfinite(gm)) return false;
+    step = ms / gm;
+    return true;
   }
   // One iteration of the advection loop (one `iters` decrement); EV_NONE to go on.
   // gm_end: the gradient magnitude at a low-gradient stop (0 where there was none).
-  // `fresh`: the first trip in a voxel (after enter()): the gradient at `cur`, a stop
-  // where it has no direction, the first step ms / |g| -- the reference's voxel entry
-  // -- then the iteration.  The iteration count is tested first, so a streamline that
-  // enters a voxel with no iterations left ends as over the limit where the reference
-  // would report a low gradient for a zero gradient there; both end at the same vertex.
-  __device__ __forceinline__ int trip(F3& cur, F3& old, bool& fresh, int& iters, bool nearb, const float b[3],
-                                      const F3 c[8], F3& g, float& gm, float& step, float& gm_end,
-                                      int64_t& last_nv) const {
+  __device__ __forceinline__ int trip(F3& cur, F3& old, int& iters, bool nearb, const float b[3], const F3 c[8],
+                                      F3& g, float& gm, float& step, float& gm_end, int64_t& last_nv) const {
     if (!(iters-- > 0)) return EV_OVER_MAX_ITERATIONS;
-    if (fresh || !(old.x == cur.x && old.y == cur.y && old.z == cur.z)) {
-      if (!fresh && ((int)cur.x != (int)old.x || (int)cur.y != (int)old.y || (int)cur.z != (int)old.z))
-        return EV_OUT_OF_VOXEL;
+    if (!(old.x == cur.x && old.y == cur.y && old.z == cur.z)) {
+      if ((int)cur.x != (int)old.x || (int)cur.y != (int)old.y || (int)cur.z != (int)old.z) return EV_OUT_OF_VOXEL;
       g = trilin(cur, b, c);
       gm = sqrtf(g.x * g.x + g.y * g.y + g.z * g.z);
       if (!(gm > 0.f) || !isfinite(gm)) return EV_LOW_GRADIENT;
-      if (fresh || gm * step > ms) step = ms / gm;
+      if (gm * step > ms) step = ms / gm;
       old = cur;
-      fresh = false;
     }
     if (gm < P.gthresh) {
       gm_end = gm;
@@ -299,7 +293,6 @@ __global__ void __launch_bounds__(128, 6) integrate_level_kernel(const Adv32 A, 
   F3 anchor = cur;  // trapped-streamline test
   int t_iters = 0, t_n = 0;
   int64_t last_nv = -1;  // nearest vertex the stop test last passed
-  bool fresh = false;    // the next trip is the first in its voxel
   while (true) {
     // most items of the late levels were labelled by earlier paths: a lane that drew
     // one draws again at once (a few rounds) instead of idling through the turn
@@ -338,14 +331,19 @@ __global__ void __launch_bounds__(128, 6) integrate_level_kernel(const Adv32 A, 
     for (int r = 0; r < K; r++) {
       if (phase == kLaneEnter) {
         nb = dist_to_boundary(V, x, y, z) <= 1;
-        A.enter(cur, nb, b, c);
-        fresh = true;
-        gm_end = 0.f;
-        phase = kLaneStep;
+        if (A.enter(cur, nb, b, c, g, gm, step, gm_end)) {
+          old = cur;
+          phase = kLaneStep;
+        } else {
+          A.nearest3(cur, x, y, z);  // ended at its voxel entry
+          end = vid(V, x, y, z);
+          if (np < kPathCap) path[np++] = (int)end;
+          phase = kLaneEnd;
+        }
       }
       if (phase != kLaneStep) continue;
       ntrips++;
-      const int ev = A.trip(cur, old, fresh, iters, nb, b, c, g, gm, step, gm_end, last_nv);
+      const int ev = A.trip(cur, old, iters, nb, b, c, g, gm, step, gm_end, last_nv);
       if (ev == EV_NONE) continue;
       A.nearest3(cur, x, y, z);
       end = vid(V, x, y, z);
@@ -681,7 +679,6 @@ __global__ void __launch_bounds__(128, 6) fixup32_kernel(const Adv32 A, int32_t*
   F3 anchor = cur;  // trapped-streamline test
   int t_iters = 0, t_n = 0;
   int64_t last_nv = -1;  // nearest vertex the stop test last passed
-  bool fresh = false;    // the next trip is the first in its voxel
   while (true) {
     const unsigned long long k = claim_item(phase == kLaneIdle, work);
     if (phase == kLaneIdle) {
@@ -707,14 +704,18 @@ __global__ void __launch_bounds__(128, 6) fixup32_kernel(const Adv32 A, int32_t*
     for (int r = 0; r < K; r++) {
       if (phase == kLaneEnter) {
         nb = dist_to_boundary(V, x, y, z) <= 1;
-        A.enter(cur, nb, b, c);
-        fresh = true;
-        gm_end = 0.f;
-        phase = kLaneStep;
+        if (A.enter(cur, nb, b, c, g, gm, step, gm_end)) {
+          old = cur;
+          phase = kLaneStep;
+        } else {
+          ev = EV_LOW_GRADIENT;
+          A.nearest3(cur, x, y, z);
+          phase = kLaneEnd;
+        }
       }
       if (phase != kLaneStep) continue;
       ntrips++;
-      ev = A.trip(cur, old, fresh, iters, nb, b, c, g, gm, step, gm_end, last_nv);
+      ev = A.trip(cur, old, iters, nb, b, c, g, gm, step, gm_end, last_nv);
       if (ev == EV_NONE) continue;
       A.nearest3(cur, x, y, z);
       phase = ev == EV_OUT_OF_VOXEL ? kLaneEnter : kLaneEnd;
