@@ -967,7 +967,11 @@ cudaError_t launch_fixup(const double* G, const VolDims& V, const IntegParams& P
   const int blocks = (n + 127) / 128;
   if (cudaError_t e = cudaMemsetAsync(work, 0, sizeof(unsigned long long), stream)) return e;
   ::msc::count_launch();
-  fixup_kernel<2><<<blocks < num_sms * kLaneCtasPerSm ? blocks : num_sms * kLaneCtasPerSm, 128, 0, stream>>>(
+  // one CTA per SM: the FP64 re-decisions are few (~0.1% of the re-decisions), and with
+  // more lanes than a few items each, most warps would run nearly empty through their
+  // longest streamline while the FP64 pipe executes every warp instruction in full
+  // (512^3 labels: 1.10 s with 16 CTAs per SM, 1.07 s with one)
+  fixup_kernel<2><<<blocks < num_sms ? blocks : num_sms, 128, 0, stream>>>(
       A, lab, lab0, state, list, n, next, n_next, queued, work, trips);
   return cudaGetLastError();
 }
