@@ -5,16 +5,19 @@ Workload (default): the 512^3 float32 Gaussian random field with a k^-3 power
 spectrum, seed = rank (held out from the triage network's training fields).  One
 step = the complete lower-star .grad of the volume (bit-identical to steepest_lstar)
 plus the ascending and descending integrated labels of ondemandaccurate (error
-threshold 1e-4, gradient threshold 1e-6 max|f|, 4000 iterations, 0.25-voxel steps),
-with the learned triage when its trained weights are present, else the plain full
-integration.
+threshold 1e-4, gradient threshold 1e-6 max|f|, 4000 iterations, 0.25-voxel steps)
+through the plain full integration; the learned triage (when its trained weights are
+present) is measured beside it ("learned": throughput, speed-up and label difference
+against the plain labels), or timed as the step with --triage.
 
   value       Gvert/s of the step with the volume already resident in HBM (CUDA
               events on the launching stream, K steps between barriers +
               synchronisation, max over ranks; every rank runs its own replica --
               the path needs no collective)
-  plain       the same step with the plain full integration, and the label mismatch
-              between the two (the plain path is the judge of the triage)
+  plain       the step with the plain full integration (the drop-in path, and the
+              judge of the triage)
+  learned     the step with the learned triage, its speed-up over plain and its
+              label difference from the plain labels
   e2e         the same metric through the C ABI host entry msc_ondemand_labels_host:
               H2D of f, .grad, labels, D2H of both label volumes per step
   grad        the .grad alone: Gvert/s and its per-kernel breakdown
@@ -60,7 +63,10 @@ def parse_args():
     p.add_argument("--impl", choices=["ours", "reference"], default="ours")
     p.add_argument("--size", type=int, default=512, help="edge of the cubic volume")
     p.add_argument("--no-cpu-baseline", action="store_true")
-    p.add_argument("--no-triage", action="store_true", help="time the plain full integration as the step")
+    p.add_argument("--triage", action="store_true",
+                   help="time the learned triage as the step (default: the plain full integration, with the triage "
+                        "measured beside it)")
+    p.add_argument("--no-triage", action="store_true", help="skip the learned triage altogether")
     p.add_argument("--grad-only", action="store_true", help="time the .grad alone as the step")
     p.add_argument("--no-batch", action="store_true", help="skip the 64-volume batching measurement")
     return p.parse_args()
@@ -255,16 +261,17 @@ def run_ours(args, ws, rank, local):
     gt = 1e-6 * float(np.abs(f_np).max())
     integ = dict(INTEG, gradient_threshold=gt)
 
-    net = None
+    net = None  # the trained triage network, measured beside the step (or as the step with --triage)
     if not args.grad_only and not args.no_triage and triage.WEIGHTS_FILE.exists():
         net = triage.TriageNet.load(device=dev)
+    step_net = net if args.triage else None
 
     def step():
         lower_star_grad(f_dev, out=g_dev)
         if args.grad_only:
             return None
-        if net is not None:
-            return triage.triage_labels(f_dev, g_dev, net, **integ)
+        if step_net is not None:
+            return triage.triage_labels(f_dev, g_dev, step_net, **integ)
         return integrated_labels(f_dev, g_dev, **integ)
 
     def barrier():
@@ -325,24 +332,33 @@ def run_ours(args, ws, rank, local):
 
     line_extra = {}
     if not args.grad_only:
-        # the plain full integration (once) and the mismatch of the timed labels against it
-        torch.cuda.synchronize(dev)
-        p0, p1 = _events(2)
-        p0.record(stream)
-        lower_star_grad(f_dev, out=g_dev)
-        plain = integrated_labels(f_dev, g_dev, **integ)
-        p1.record(stream)
-        torch.cuda.synchronize(dev)
-        ms_plain = p0.elapsed_time(p1)
-        mism = {k: float((res[k] != plain[k]).float().mean().item()) for k in ("asc", "dsc")}
+        # the other mode once (the plain full integration beside a triaged step, or the
+        # triage beside the plain step) and the triage's label difference from the plain
+        def once(use_net):
+            torch.cuda.synchronize(dev)
+            p0, p1 = _events(2)
+            p0.record(stream)
+            lower_star_grad(f_dev, out=g_dev)
+            r = triage.triage_labels(f_dev, g_dev, use_net, **integ) if use_net is not None else \
+                integrated_labels(f_dev, g_dev, **integ)
+            p1.record(stream)
+            torch.cuda.synchronize(dev)
+            return r, p0.elapsed_time(p1)
+        if step_net is not None:
+            plain, ms_plain = once(None)
+            learned, ms_learned = res, ms
+        else:
+            plain, ms_plain = res, ms
+            learned, ms_learned = once(net) if net is not None else (None, None)
         line_extra["plain"] = {"value": V / (ms_plain * 1e-3) / 1e9, "unit": UNIT, "ms_per_step": ms_plain,
                                "redecided": plain["stats"]}
-        line_extra["labels"] = {"mode": "learned triage" if net is not None else "plain full integration",
-                                "mismatch_vs_plain": mism,
-                                "stats": res["stats"],
-                                "speedup_vs_plain": ms_plain / ms}
-        if net is not None:
-            line_extra["labels"]["thresholds"] = [net.threshold_asc, net.threshold_dsc]
+        line_extra["labels"] = {"mode": "learned triage" if step_net is not None else "plain full integration"}
+        if learned is not None:
+            line_extra["learned"] = {
+                "value": V / (ms_learned * 1e-3) / 1e9, "unit": UNIT, "ms_per_step": ms_learned,
+                "speedup_vs_plain": ms_plain / ms_learned,
+                "mismatch_vs_plain": {k: float((learned[k] != plain[k]).float().mean().item()) for k in ("asc", "dsc")},
+                "stats": learned["stats"], "thresholds": [net.threshold_asc, net.threshold_dsc]}
         # the labeling's kernels are FP32 issue-bound streamline integrations: their
         # roofline is the FP32 rate.  Operations per advection iteration: two trilinear
         # interpolations of the 3-vector gradient (73 each) plus step control (~37).
@@ -375,8 +391,9 @@ def run_ours(args, ws, rank, local):
         p = _lib.IntegParams(integ["error_threshold"], gt, integ["iteration_limit"], integ["max_step"],
                              integ["presimp_threshold"], 0)
         tp = None
-        if net is not None:
-            tp = triage.TriageParams(net.weights.data_ptr(), net.threshold_asc, net.threshold_dsc, 0.01, 12345)
+        if step_net is not None:
+            tp = triage.TriageParams(step_net.weights.data_ptr(), step_net.threshold_asc, step_net.threshold_dsc,
+                                     0.01, 12345)
 
         def fn():
             rc = lib.msc_ondemand_labels_host(ctypes.c_void_p(f_host.data_ptr()), _lib.dims_arg(dims), ctypes.byref(p),
@@ -444,7 +461,7 @@ def run_ours(args, ws, rank, local):
 
     if rank == 0:
         mode = ".grad only" if args.grad_only else (
-            ".grad + learned-triage labels" if net is not None else ".grad + plain integrated labels")
+            ".grad + learned-triage labels" if step_net is not None else ".grad + plain integrated labels")
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
                 "vs_baseline": None, "dtype": "f32" if args.grad_only else "f32+f64", "data": "synthetic",
