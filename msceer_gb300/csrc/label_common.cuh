@@ -97,8 +97,9 @@ struct IntegParams {
   // Trapped-streamline cut-off (0 = off): every trap_window iterations the position
   // is compared with the one trap_window iterations before; a streamline that moved
   // less than trap_radius (voxels, max norm) two checks in a row ends there -- in the
-  // fix-up, when it is within trap_margin of a plane where its nearest vertex changes,
-  // only if the vertices on the sides it may settle on carry the same label.
+  // FP64 re-decisions, when it is within trap_margin of a plane where its nearest
+  // vertex changes, only if the vertices on the sides it may settle on carry the same
+  // label.
   int trap_window = 0;
   float trap_radius = 0.f, trap_margin = 0.f;
 };

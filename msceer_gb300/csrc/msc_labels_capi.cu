@@ -331,10 +331,10 @@ int prepare_direction(LabelCtx& c, DirLabels& d, int32_t* stage_terminal) {
 // fields ~2% of the descending boundary re-decisions and 3/4 of their iterations; many
 // such sinks lie on a plane where the nearest vertex changes).  Outside the all-FP64
 // mode the integration kernels end such a streamline once it has stayed within 0.02
-// voxel for two windows of 128 iterations; within 0.05 voxel of a nearest-vertex plane
-// only if the vertices on both sides carry the same decision label.  Measured with the
-// FP64 oracle (the same test added to its integrator) on k^-3 and Gaussian-sum fields at
-// 64^3 and 96^3: at most 2e-5 of the labels change, the oracle itself runs 2x faster.
+// voxel for two windows of 128 iterations (the FP64 re-decisions, within 0.05 voxel of
+// a nearest-vertex plane, only if the vertices on both sides carry the same decision
+// label).  Measured with the FP64 oracle (the same test added to its integrator) on
+// k^-3 and Gaussian-sum fields at 64^3 and 96^3: at most 2e-5 of the labels change.
 msc::IntegParams integ_params(const msc_integ_params* p, int dir) {
   msc::IntegParams P{p->error_threshold, p->gradient_threshold, p->iteration_limit, (double)p->max_step, dir};
   if (p->precision != 1) {
