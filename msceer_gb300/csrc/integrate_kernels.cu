@@ -300,10 +300,7 @@ template <int K>
 __global__ void __launch_bounds__(128, 6) integrate_level_kernel(const Adv32 A, const SpreadOrder S, int L0, int L1,
                                                               int32_t* __restrict__ lab, uint8_t* __restrict__ lvl,
                                                               unsigned long long* __restrict__ work,
-                                                              unsigned long long* __restrict__ trips,
-                                                              int2* __restrict__ pairs,
-                                                              unsigned long long* __restrict__ npairs,
-                                                              unsigned long long cap) {
+                                                              unsigned long long* __restrict__ trips) {
   const VolDims& V = A.V;
   const int level = A.level;
   const int64_t count = S.offset[L1] - S.offset[L0];
@@ -391,45 +388,29 @@ __global__ void __launch_bounds__(128, 6) integrate_level_kernel(const Adv32 A, 
       }
     }
     if (phase == kLaneEnd) {
-      // the path's labels are applied after the level (apply_paths_kernel): no
-      // streamline of the level reads them, and a lane that waited here for the path's
-      // level bytes would hold its warp
-      const unsigned long long slot = atomicAdd(npairs, (unsigned long long)np);
-      if (slot + (unsigned long long)np <= cap) {
-        for (int k = 0; k < np; k++) pairs[slot + k] = make_int2(path[k], (int)end);
-      } else {  // the pair buffer is full: write back here
-        const uint8_t le = lvl[end];
-        const int32_t lb = lab[end];
-        int32_t dest = le < level ? lb : -1;
-        if (dest == -1) dest = kLabelNone;  // reached no region: assigned to nothing
-        for (int k = 0; k < np; k++) {
-          const int p = path[k];
-          if (lvl[p] < level) continue;  // labelled in an earlier level: keep
-          atomicMin(reinterpret_cast<unsigned int*>(&lab[p]), (unsigned int)dest);
-          lvl[p] = (uint8_t)level;
+      const uint8_t le = lvl[end];
+      const int32_t lb = lab[end];
+      int32_t dest = le < level ? lb : -1;
+      if (dest == -1) dest = kLabelNone;  // reached no region: assigned to nothing
+      // the path's level bytes are read eight at a time, so that one lane's write-back
+      // waits for a memory round trip per eight vertices rather than per vertex
+      for (int k0 = 0; k0 < np; k0 += 8) {
+        int pk[8];
+        uint8_t lk[8];
+#pragma unroll
+        for (int j = 0; j < 8; j++) {
+          pk[j] = k0 + j < np ? path[k0 + j] : -1;
+          lk[j] = pk[j] >= 0 ? lvl[pk[j]] : 0;
+        }
+#pragma unroll
+        for (int j = 0; j < 8; j++) {
+          if (pk[j] < 0 || lk[j] < level) continue;  // labelled in an earlier level: keep
+          atomicMin(reinterpret_cast<unsigned int*>(&lab[pk[j]]), (unsigned int)dest);
+          lvl[pk[j]] = (uint8_t)level;
         }
       }
       phase = kLaneIdle;
     }
-  }
-}
-
-// The level's path labels: every recorded (path vertex, streamline end) pair.  The
-// end's label counts only if it was labelled in an earlier level (else the streamline
-// reached no region); vertices labelled in an earlier level keep theirs, the rest take
-// the smallest label any of the level's paths through them brings.
-__global__ void apply_paths_kernel(const int2* __restrict__ pairs, const unsigned long long* __restrict__ npairs,
-                                   unsigned long long cap, int32_t* __restrict__ lab, uint8_t* __restrict__ lvl,
-                                   int level) {
-  const unsigned long long n = *npairs < cap ? *npairs : cap;
-  for (unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; i < n;
-       i += (unsigned long long)gridDim.x * blockDim.x) {
-    const int2 pe = pairs[i];
-    if (lvl[pe.x] < level) continue;
-    int32_t dest = lvl[pe.y] < level ? lab[pe.y] : -1;
-    if (dest == -1) dest = kLabelNone;
-    atomicMin(reinterpret_cast<unsigned int*>(&lab[pe.x]), (unsigned int)dest);
-    lvl[pe.x] = (uint8_t)level;
   }
 }
 
@@ -981,8 +962,7 @@ int trips_per_turn() {
 
 cudaError_t launch_integrate_pass1(const float4* G, const VolDims& V, const IntegParams& P, const SpreadOrder& S,
                                    int32_t* lab, uint8_t* lvl, unsigned long long* work, unsigned long long* trips,
-                                   int2* pairs, unsigned long long* npairs, unsigned long long cap, int num_sms,
-                                   cudaStream_t stream) {
+                                   int num_sms, cudaStream_t stream) {
   const int64_t N = V.X * V.Y * V.Z;
   if (cudaError_t e = cudaMemsetAsync(work, 0, sizeof(unsigned long long) * 48, stream)) return e;
   ::msc::count_launch();
@@ -1002,27 +982,20 @@ cudaError_t launch_integrate_pass1(const float4* G, const VolDims& V, const Inte
     const int64_t blocks = (count + 127) / 128;
     const int grid = (int)(blocks < num_sms * kLaneCtasPerSm ? blocks : num_sms * kLaneCtasPerSm);
     unsigned long long* w = work + (stamp - 1);
-    if (cudaError_t e = cudaMemsetAsync(npairs, 0, sizeof(unsigned long long), stream)) return e;
     ::msc::count_launch();
     switch (trips_per_turn()) {
       case 16:
-        integrate_level_kernel<16><<<grid, 128, 0, stream>>>(A, S, g0, L1, lab, lvl, w, trips, pairs, npairs,
-                                                             cap);
+        integrate_level_kernel<16><<<grid, 128, 0, stream>>>(A, S, g0, L1, lab, lvl, w, trips);
         break;
       case 2:
-        integrate_level_kernel<2><<<grid, 128, 0, stream>>>(A, S, g0, L1, lab, lvl, w, trips, pairs, npairs,
-                                                             cap);
+        integrate_level_kernel<2><<<grid, 128, 0, stream>>>(A, S, g0, L1, lab, lvl, w, trips);
         break;
       case 4:
-        integrate_level_kernel<4><<<grid, 128, 0, stream>>>(A, S, g0, L1, lab, lvl, w, trips, pairs, npairs,
-                                                             cap);
+        integrate_level_kernel<4><<<grid, 128, 0, stream>>>(A, S, g0, L1, lab, lvl, w, trips);
         break;
       default:
-        integrate_level_kernel<8><<<grid, 128, 0, stream>>>(A, S, g0, L1, lab, lvl, w, trips, pairs, npairs,
-                                                             cap);
+        integrate_level_kernel<8><<<grid, 128, 0, stream>>>(A, S, g0, L1, lab, lvl, w, trips);
     }
-    ::msc::count_launch();
-    apply_paths_kernel<<<num_sms * 8, 256, 0, stream>>>(pairs, npairs, cap, lab, lvl, stamp);
   }
   return cudaGetLastError();
 }

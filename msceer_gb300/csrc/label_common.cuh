@@ -113,12 +113,9 @@ struct SpreadOrder {
 
 // `work`: 48 device counters (the levels' claimed items), zeroed here.  `trips`
 // (here and below): a device counter the kernels add their advection iterations to.
-// `pairs`: room for `cap` (path vertex, streamline end) pairs of one level, `npairs`
-// their device counter (the label write-back runs after each level).
 cudaError_t launch_integrate_pass1(const float4* G, const VolDims& V, const IntegParams& P, const SpreadOrder& S,
                                    int32_t* lab, uint8_t* lvl, unsigned long long* work, unsigned long long* trips,
-                                   int2* pairs, unsigned long long* npairs, unsigned long long cap, int num_sms,
-                                   cudaStream_t stream);
+                                   int num_sms, cudaStream_t stream);
 cudaError_t launch_boundary_set(const int32_t* lab, const uint8_t* state, const VolDims& V, int64_t* list, int* n,
                                 uint32_t* queued, int num_sms, cudaStream_t stream);
 // `work`: a device counter of claimed items, zeroed by the launchers

@@ -367,14 +367,9 @@ int first_pass(LabelCtx& c, DirLabels& d) {
     S.nlev++;
   }
   uint8_t* lvl;
-  int2* pairs;  // a level's (path vertex, end) pairs: 4 per vertex of the volume
-  const unsigned long long cap = 4ull * (unsigned long long)N;
   LCUDA(c.pool.get(&lvl, N), "alloc");
-  LCUDA(c.pool.get(&pairs, cap), "alloc");
   LCUDA(cudaMemsetAsync(c.work + 48, 0, 3 * sizeof(unsigned long long), st), "memset");
-  LCUDA(msc::launch_integrate_pass1(c.g32, c.V, P, S, d.lab, lvl, c.work, c.work + 48, pairs, c.work + 52, cap, c.sms,
-                                    st),
-        "integrate");
+  LCUDA(msc::launch_integrate_pass1(c.g32, c.V, P, S, d.lab, lvl, c.work, c.work + 48, c.sms, st), "integrate");
   return MSC_OK;
 }
 
