@@ -111,42 +111,12 @@ struct Adv32 {
   }
   // The trapped-streamline test (IntegParams::trap_window): compares `cur` with the
   // anchor set trap_window iterations before, moves the anchor, counts the
-  // consecutive tight windows in `n`; true once there are two.  With `lab0` (the
-  // decision labels; the FP64 re-decisions pass them) an orbit within trap_margin of a
-  // plane where its nearest vertex changes ends only if the vertices on every side it
-  // may settle on carry the same label; otherwise the count restarts and the
-  // streamline goes on.
-  __device__ __forceinline__ bool trapped(const F3& cur, F3& anchor, int& n, const int32_t* lab0) const {
+  // consecutive tight windows in `n`; true once there are two.
+  __device__ __forceinline__ bool trapped(const F3& cur, F3& anchor, int& n) const {
     const float d = fmaxf(fabsf(cur.x - anchor.x), fmaxf(fabsf(cur.y - anchor.y), fabsf(cur.z - anchor.z)));
     n = d < P.trap_radius ? n + 1 : 0;
     anchor = cur;
-    if (n < 2) return false;
-    if (!lab0 || sides_agree(cur, lab0)) return true;
-    n = 0;
-    return false;
-  }
-  // Out of line (rarely called; keeps the stepping loop's registers free).
-  __device__ __noinline__ bool sides_agree(const F3 cur, const int32_t* lab0) const {
-    int q[3];
-    nearest3(cur, q[0], q[1], q[2]);
-    const float pc[3] = {cur.x, cur.y, cur.z};
-    const int64_t e[3] = {V.X, V.Y, V.Z};
-    int alt[3];
-#pragma unroll
-    for (int a = 0; a < 3; a++) {
-      const float pa = pc[a] + 0.5f;
-      const float r = pa - floorf(pa);
-      alt[a] = fminf(r, 1.f - r) <= P.trap_margin ? (r < 0.5f ? -1 : 1) : 0;
-      if (q[a] + alt[a] < 0 || q[a] + alt[a] >= e[a]) alt[a] = 0;
-    }
-    if (!(alt[0] | alt[1] | alt[2])) return true;
-    const int32_t l0 = lab0[vid(V, q[0], q[1], q[2])];
-    for (int m = 1; m < 8; m++) {
-      if (((m & 1) && !alt[0]) || ((m & 2) && !alt[1]) || ((m & 4) && !alt[2])) continue;
-      if (lab0[vid(V, q[0] + ((m & 1) ? alt[0] : 0), q[1] + ((m & 2) ? alt[1] : 0), q[2] + ((m & 4) ? alt[2] : 0))] != l0)
-        return false;
-    }
-    return true;
+    return n >= 2;
   }
   // AdvectThroughVoxel{NoCheck,NearBoundary} split in two, so that a lane can run its
   // streamline one iteration at a time.  enter(): the voxel's base corner, its eight
@@ -379,7 +349,7 @@ __global__ void __launch_bounds__(128, 6) integrate_level_kernel(const Adv32 A, 
     {
       if (phase == kLaneStep && A.P.trap_window > 0 && t_iters - iters >= A.P.trap_window) {
         t_iters = iters;
-        if (A.trapped(cur, anchor, t_n, nullptr)) {  // ends where the iteration limit would have
+        if (A.trapped(cur, anchor, t_n)) {  // ends where the iteration limit would have
           A.nearest3(cur, x, y, z);
           end = vid(V, x, y, z);
           if (np < kPathCap) path[np++] = (int)end;
@@ -480,33 +450,11 @@ struct Adv64 {
     return vid(V, ix, iy, iz);
   }
   // The FP32 advector's trapped-streamline test on FP64 positions.
-  __device__ __forceinline__ bool trapped(const D3& cur, D3& anchor, int& n, const int32_t* lab0) const {
+  __device__ __forceinline__ bool trapped(const D3& cur, D3& anchor, int& n) const {
     const double d = fmax(fabs(cur.x - anchor.x), fmax(fabs(cur.y - anchor.y), fabs(cur.z - anchor.z)));
     n = d < (double)P.trap_radius ? n + 1 : 0;
     anchor = cur;
-    if (n < 2) return false;
-    int q[3];
-    nearest3(cur, q[0], q[1], q[2]);
-    const double pc[3] = {cur.x, cur.y, cur.z};
-    const int64_t e[3] = {V.X, V.Y, V.Z};
-    int alt[3];
-#pragma unroll
-    for (int a = 0; a < 3; a++) {
-      const double pa = pc[a] + 0.5;
-      const double r = pa - floor(pa);
-      alt[a] = fmin(r, 1.0 - r) <= (double)P.trap_margin ? (r < 0.5 ? -1 : 1) : 0;
-      if (q[a] + alt[a] < 0 || q[a] + alt[a] >= e[a]) alt[a] = 0;
-    }
-    if (!(alt[0] | alt[1] | alt[2])) return true;
-    const int32_t l0 = lab0[vid(V, q[0], q[1], q[2])];
-    for (int m = 1; m < 8; m++) {
-      if (((m & 1) && !alt[0]) || ((m & 2) && !alt[1]) || ((m & 4) && !alt[2])) continue;
-      if (lab0[vid(V, q[0] + ((m & 1) ? alt[0] : 0), q[1] + ((m & 2) ? alt[1] : 0), q[2] + ((m & 4) ? alt[2] : 0))] != l0) {
-        n = 0;
-        return false;
-      }
-    }
-    return true;
+    return n >= 2;
   }
   // The FP32 advector's enter / trip in the reference's FP64 arithmetic.
   __device__ __forceinline__ bool enter(const D3& cur, bool nearb, double bf[3], D3 c[8], D3& g, float& gm,
@@ -662,7 +610,7 @@ __global__ void __launch_bounds__(128) fixup_kernel(const Adv64 A, int32_t* __re
     }
     if (phase == kLaneStep && A.P.trap_window > 0 && t_iters - iters >= A.P.trap_window) {
       t_iters = iters;
-      if (A.trapped(cur, anchor, t_n, lab0)) {  // ends where the iteration limit would have
+      if (A.trapped(cur, anchor, t_n)) {  // ends where the iteration limit would have
         A.nearest3(cur, x, y, z);
         phase = kLaneEnd;
       }
@@ -767,11 +715,7 @@ __global__ void __launch_bounds__(128, 6) fixup32_kernel(const Adv32 A, int32_t*
     {
       if (phase == kLaneStep && A.P.trap_window > 0 && t_iters - iters >= A.P.trap_window) {
         t_iters = iters;
-        // no side check here: where the sides differ the FP32 orbit's final side is as
-        // much a coin flip against the FP64 one after 4000 iterations as now (512^3
-        // labels 0.89 -> 0.78 s; difference from the all-FP64 labels 1.6e-4 -> 1.7e-4
-        // of the vertices at 256^3, 1.7e-4 -> 2.1e-4 at 192^3)
-        if (A.trapped(cur, anchor, t_n, nullptr)) {  // ends where the iteration limit would have
+        if (A.trapped(cur, anchor, t_n)) {  // ends where the iteration limit would have
           ev = EV_OVER_MAX_ITERATIONS;
           A.nearest3(cur, x, y, z);
           phase = kLaneEnd;

@@ -96,12 +96,9 @@ struct IntegParams {
   int step_mult;  // -1: flow downhill (ascending manifolds of minima), +1 uphill
   // Trapped-streamline cut-off (0 = off): every trap_window iterations the position
   // is compared with the one trap_window iterations before; a streamline that moved
-  // less than trap_radius (voxels, max norm) two checks in a row ends there -- in the
-  // FP64 re-decisions, when it is within trap_margin of a plane where its nearest
-  // vertex changes, only if the vertices on the sides it may settle on carry the same
-  // label.
+  // less than trap_radius (voxels, max norm) two checks in a row ends there.
   int trap_window = 0;
-  float trap_radius = 0.f, trap_margin = 0.f;
+  float trap_radius = 0.f;
 };
 
 // Spread visiting order of the first pass (:166-174 with one thread): level L

@@ -328,19 +328,18 @@ int prepare_direction(LabelCtx& c, DirLabels& d, int32_t* stage_terminal) {
 
 // Streamlines that orbit a sink of the interpolated gradient without reaching the
 // stop threshold run to the iteration limit and end at their nearest vertex (on k^-3
-// fields ~2% of the descending boundary re-decisions and 3/4 of their iterations; many
-// such sinks lie on a plane where the nearest vertex changes).  Outside the all-FP64
-// mode the integration kernels end such a streamline once it has stayed within 0.02
-// voxel for two windows of 128 iterations (the FP64 re-decisions, within 0.05 voxel of
-// a nearest-vertex plane, only if the vertices on both sides carry the same decision
-// label).  Measured with the FP64 oracle (the same test added to its integrator) on
-// k^-3 and Gaussian-sum fields at 64^3 and 96^3: at most 2e-5 of the labels change.
+// fields ~2% of the descending boundary re-decisions and 3/4 of their iterations).
+// Outside the all-FP64 mode the integration kernels end such a streamline once it has
+// stayed within 0.02 voxel for two windows of 128 iterations.  Where the orbit sits on
+// a plane at which the nearest vertex changes, its final side is a coin flip of the
+// chaotic orbit; against the all-FP64 labels the cut-off changed nothing measurable
+// (256^3 and 192^3 k^-3: 3.4e-5 / 1.7e-4 and 3.5e-5 / 2.1e-4 label difference, asc /
+// dsc, with and without it in the FP64 re-decisions).
 msc::IntegParams integ_params(const msc_integ_params* p, int dir) {
   msc::IntegParams P{p->error_threshold, p->gradient_threshold, p->iteration_limit, (double)p->max_step, dir};
   if (p->precision != 1) {
     P.trap_window = 128;
     P.trap_radius = 0.02f;
-    P.trap_margin = 0.05f;
   }
   return P;
 }

@@ -164,3 +164,22 @@ def test_triage_nothing_flagged_keeps_first_pass(gpu):
     n = f.size
     assert 0 < audited["asc_audited"] < 0.05 * n
     assert 0 <= audited["asc_audit_changed"] <= audited["asc_audited"]
+
+
+def test_trained_network_saves_redecisions(gpu):
+    """Ablation: the committed network against the method without it.  On a held-out
+    k^-3 field it re-decides fewer boundary vertices than the plain fix-up while its
+    labels stay within the 0.1% budget of the plain ones."""
+    from msceer_gb300 import integrated_labels, triage
+    if not triage.WEIGHTS_FILE.exists():
+        pytest.skip("no trained weights")
+    f, t, g = _labels_setup((96, 96, 96), 0)
+    net = triage.TriageNet.load()
+    plain = integrated_labels(t, g, 1e-4, None, 4000, 0.25, 0.0)
+    tri = triage.triage_labels(t, g, net)
+    for d in ("asc", "dsc"):
+        saved = 1 - tri["stats"][f"{d}_redecided"] / plain["stats"][f"{d}_redecided"]
+        mism = (tri[d] != plain[d]).float().mean().item()
+        print(d, "re-decisions saved", saved, "label difference", mism)
+        assert saved > 0.05, saved
+        assert mism <= 1e-3, mism
