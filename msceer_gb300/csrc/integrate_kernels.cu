@@ -525,20 +525,31 @@ struct Adv64 {
 __global__ void boundary_set_kernel(const int32_t* __restrict__ lab, const uint8_t* __restrict__ state, const VolDims V,
                                     int64_t* __restrict__ list, int* __restrict__ n, uint32_t* __restrict__ queued) {
   const int64_t N = V.X * V.Y * V.Z;
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < N; i += (int64_t)gridDim.x * blockDim.x) {
-    if (state[i] != kStUnassigned) continue;
-    const int64_t x = i % V.X, y = (i / V.X) % V.Y, z = i / (V.X * V.Y);
-    const int32_t l = lab[i];
+  const int lane = threadIdx.x & 31;
+  // a warp covers 32 consecutive vertices starting at a multiple of 32 (block size and
+  // grid stride are multiples of 32), i.e. exactly one word of `queued`
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i - lane < N; i += (int64_t)gridDim.x * blockDim.x) {
     bool diff = false;
-    if (x < V.X - 1) diff |= lab[i + 1] != l;
-    if (x > 0) diff |= lab[i - 1] != l;
-    if (y < V.Y - 1) diff |= lab[i + V.X] != l;
-    if (y > 0) diff |= lab[i - V.X] != l;
-    if (z < V.Z - 1) diff |= lab[i + V.X * V.Y] != l;
-    if (z > 0) diff |= lab[i - V.X * V.Y] != l;
-    if (!diff) continue;
-    atomicOr(&queued[i >> 5], 1u << (i & 31));
-    list[atomicAdd(n, 1)] = i;
+    if (i < N && state[i] == kStUnassigned) {
+      int x, y, z;
+      split_index(V, i, x, y, z);
+      const int32_t l = lab[i];
+      if (x < V.X - 1) diff |= lab[i + 1] != l;
+      if (x > 0) diff |= lab[i - 1] != l;
+      if (y < V.Y - 1) diff |= lab[i + V.X] != l;
+      if (y > 0) diff |= lab[i - V.X] != l;
+      if (z < V.Z - 1) diff |= lab[i + V.X * V.Y] != l;
+      if (z > 0) diff |= lab[i - V.X * V.Y] != l;
+    }
+    const unsigned m = __ballot_sync(kFullMask, diff);  // (the loop bound is warp-uniform)
+    if (!m) continue;
+    int base = 0;
+    if (lane == 0) {
+      atomicOr(&queued[i >> 5], m);
+      base = atomicAdd(n, __popc(m));
+    }
+    base = __shfl_sync(kFullMask, base, 0);
+    if (diff) list[base + __popc(m & ((1u << lane) - 1u))] = i;
   }
 }
 
@@ -548,7 +559,7 @@ __global__ void boundary_set_kernel(const int32_t* __restrict__ lab, const uint8
 // ending (low gradient, iteration limit) it is a value no concurrent re-decision can
 // be rewriting, so every wave's outcome is independent of thread timing.
 template <int K>
-__global__ void __launch_bounds__(128) fixup_kernel(const Adv64 A, int32_t* __restrict__ lab,
+__global__ void __launch_bounds__(32) fixup_kernel(const Adv64 A, int32_t* __restrict__ lab,
                                                     const int32_t* __restrict__ lab0, uint8_t* __restrict__ state,
                                                     const int64_t* __restrict__ list, int n, int64_t* __restrict__ next,
                                                     int* __restrict__ n_next, uint32_t* __restrict__ queued,
@@ -956,14 +967,15 @@ cudaError_t launch_fixup(const double* G, const VolDims& V, const IntegParams& P
                          unsigned long long* work, unsigned long long* trips, int num_sms, cudaStream_t stream) {
   if (n <= 0) return cudaSuccess;
   Adv64 A{G, V, P, state};
-  const int blocks = (n + 127) / 128;
+  const int blocks = (n + 31) / 32;
   if (cudaError_t e = cudaMemsetAsync(work, 0, sizeof(unsigned long long), stream)) return e;
   ::msc::count_launch();
-  // one CTA per SM: the FP64 re-decisions are few (~0.1% of the re-decisions), and with
-  // more lanes than a few items each, most warps would run nearly empty through their
-  // longest streamline while the FP64 pipe executes every warp instruction in full
-  // (512^3 labels: 1.10 s with 16 CTAs per SM, 1.07 s with one)
-  fixup_kernel<2><<<blocks < num_sms ? blocks : num_sms, 128, 0, stream>>>(
+  // one-warp CTAs, at most four per SM: the FP64 re-decisions are few (~0.1% of the
+  // re-decisions) and bound by each SM's FP64 pipe, which executes every warp
+  // instruction in full however few lanes are active -- so a small wave is spread over
+  // as many SMs as it has warps, and a large one keeps a few items per lane (512^3
+  // labels: 1.10 s with 16 CTAs of 128 per SM, 1.07 s with one)
+  fixup_kernel<2><<<blocks < num_sms * 4 ? blocks : num_sms * 4, 32, 0, stream>>>(
       A, lab, lab0, state, list, n, next, n_next, queued, work, trips);
   return cudaGetLastError();
 }

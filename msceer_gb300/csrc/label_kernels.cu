@@ -31,20 +31,41 @@ __global__ void find_critical_kernel(const uint8_t* __restrict__ g, const VolDim
                                      int* __restrict__ n_ext, int64_t* __restrict__ saddles, int* __restrict__ n_sad) {
   const int ext_dim = dir < 0 ? 0 : 3, sad_dim = dir < 0 ? 1 : 2;
   const int64_t nc = V.dX * V.dY * V.dZ;
+  const int lane = threadIdx.x & 31;
   for (int64_t id = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; id < nc; id += (int64_t)gridDim.x * blockDim.x) {
     const uint8_t b = g[id];
-    if (((b >> 2) & 7) != 7) continue;
-    int64_t k[3];
-    cell_coords(V, id, k);
-    const int d = (int)((k[0] & 1) + (k[1] & 1) + (k[2] & 1));
-    if (d == ext_dim) {
-      const int slot = atomicAdd(n_ext, 1);
-      ext_cells[slot] = id;
-      ext_id_of_key[(k[0] >> 1) + (k[1] >> 1) * V.X + (k[2] >> 1) * V.X * V.Y] = slot;
-    } else if (d == sad_dim) {
+    int kind = 0;  // 1: extremum, 2: saddle of this direction
+    int64_t k[3] = {0, 0, 0};
+    if (((b >> 2) & 7) == 7) {
+      cell_coords(V, id, k);
+      const int d = (int)((k[0] & 1) + (k[1] & 1) + (k[2] & 1));
+      if (d == ext_dim) kind = 1;
       // trace_up_2saddle skips 2-saddles on the boundary (gi_extrema_region_builder.h:315-318)
-      if (dir > 0 && boundary_value(V, k) != 0) continue;
-      saddles[atomicAdd(n_sad, 1)] = id;
+      else if (d == sad_dim && !(dir > 0 && boundary_value(V, k) != 0)) kind = 2;
+    }
+    // one atomic per warp and kind: millions of critical cells would otherwise
+    // serialise on the two counters
+    const unsigned act = __activemask();
+    const unsigned lt = (1u << lane) - 1u;
+    const unsigned me = __ballot_sync(act, kind == 1);
+    if (me) {
+      const int leader = __ffs(me) - 1;
+      int base = 0;
+      if (lane == leader) base = atomicAdd(n_ext, __popc(me));
+      base = __shfl_sync(act, base, leader);
+      if (kind == 1) {
+        const int slot = base + __popc(me & lt);
+        ext_cells[slot] = id;
+        ext_id_of_key[(k[0] >> 1) + (k[1] >> 1) * V.X + (k[2] >> 1) * V.X * V.Y] = slot;
+      }
+    }
+    const unsigned ms = __ballot_sync(act, kind == 2);
+    if (ms) {
+      const int leader = __ffs(ms) - 1;
+      int base = 0;
+      if (lane == leader) base = atomicAdd(n_sad, __popc(ms));
+      base = __shfl_sync(act, base, leader);
+      if (kind == 2) saddles[base + __popc(ms & lt)] = id;
     }
   }
 }
