@@ -79,6 +79,21 @@ def dist_setup():
     return ws, rank, local
 
 
+def max_over_ranks(x: float, pg, device) -> float:
+    """The largest value of x over the ranks (the slowest replica's time)."""
+    if pg is None:
+        return x
+    import torch
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    pg.all_reduce(t, op=pg.ReduceOp.MAX)
+    return float(t.item())
+
+
+def aggregate_gvps(ws: int, vertices_per_rank: int, seconds: float) -> float:
+    """Whole-job Gvert/s: every rank processes its own volume in `seconds` (the max over ranks)."""
+    return ws * vertices_per_rank / seconds / 1e9
+
+
 def load_peaks():
     p = ROOT / "MEASURED_PEAKS.json"
     if p.exists():
@@ -298,13 +313,9 @@ def run_ours(args, ws, rank, local):
         e1.record(stream)
         barrier()
         launches = lib.msc_kernel_launches() - l0
-    ms = e0.elapsed_time(e1) / args.steps
+    ms = max_over_ranks(e0.elapsed_time(e1) / args.steps, pg, dev)
     clocks = clk.summary()
-    if pg is not None:
-        t = torch.tensor([ms], device=dev)
-        pg.all_reduce(t, op=pg.ReduceOp.MAX)
-        ms = float(t.item())
-    value = ws * V / (ms * 1e-3) / 1e9
+    value = aggregate_gvps(ws, V, ms * 1e-3)
 
     # the .grad alone and its stages, on the launching stream
     reps = max(3, min(args.steps, 10))
@@ -406,12 +417,8 @@ def run_ours(args, ws, rank, local):
     t0 = time.perf_counter()
     for _ in range(e2e_reps):
         fn()
-    t_e2e = (time.perf_counter() - t0) / e2e_reps
-    if pg is not None:
-        t = torch.tensor([t_e2e], device=dev)
-        pg.all_reduce(t, op=pg.ReduceOp.MAX)
-        t_e2e = float(t.item())
-    e2e = ws * V / t_e2e / 1e9
+    t_e2e = max_over_ranks((time.perf_counter() - t0) / e2e_reps, pg, dev)
+    e2e = aggregate_gvps(ws, V, t_e2e)
 
     # batching: 64 volumes with edge lengths log-uniform in [32, 256] per axis (k^-3 fields,
     # seeds 0..63): the .grad of all of them in shared launches vs one call per volume
