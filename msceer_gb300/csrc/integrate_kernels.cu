@@ -224,7 +224,6 @@ __device__ __forceinline__ void split_index(const VolDims& V, int64_t v, int& x,
 }
 
 constexpr int kPathCap = 48;
-constexpr int kMaxDraws = 4;  // first pass: hand-out rounds per turn for lanes that drew labelled vertices
 constexpr unsigned kFullMask = 0xffffffffu;
 
 // Streamlines differ in length by orders of magnitude (most end within a few dozen
@@ -266,14 +265,42 @@ __device__ __forceinline__ void add_trips(unsigned long long n, unsigned long lo
 // atomicMin: a region's id < "reached no region" < unlabelled).  Level by level the
 // pass is therefore deterministic.  `work` counts the level's claimed items (zero at
 // launch).
+// The vertices of levels [L0, L1) not labelled in an earlier level, compacted into
+// `items` (their order does not matter: a level's outcome does not depend on it).
+// Checking here, before the level runs, skips exactly the vertices the level's
+// streamlines would skip: those stamped below `level`.
+__global__ void compact_level_kernel(const SpreadOrder S, int L0, int L1, const uint8_t* __restrict__ lvl, int level,
+                                     int32_t* __restrict__ items, unsigned long long* __restrict__ n_items) {
+  const int64_t count = S.offset[L1] - S.offset[L0];
+  const int lane = threadIdx.x & 31;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t - lane < count;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    int64_t i = -1;
+    if (t < count) {
+      const int64_t u = S.offset[L0] + t;
+      int L = L0;
+      while (L + 1 < L1 && S.offset[L + 1] <= u) L++;
+      i = S.start[L] + (u - S.offset[L]) * S.stride[L];
+      if (lvl[i] < level) i = -1;
+    }
+    const unsigned m = __ballot_sync(kFullMask, i >= 0);  // (the loop bound is warp-uniform)
+    if (!m) continue;
+    unsigned long long base = 0;
+    if (lane == 0) base = atomicAdd(n_items, (unsigned long long)__popc(m));
+    base = __shfl_sync(kFullMask, base, 0);
+    if (i >= 0) items[base + __popc(m & ((1u << lane) - 1u))] = (int32_t)i;
+  }
+}
+
 template <int K>
-__global__ void __launch_bounds__(128, 6) integrate_level_kernel(const Adv32 A, const SpreadOrder S, int L0, int L1,
+__global__ void __launch_bounds__(128, 6) integrate_level_kernel(const Adv32 A, const int32_t* __restrict__ items,
+                                                              const unsigned long long* __restrict__ n_items,
                                                               int32_t* __restrict__ lab, uint8_t* __restrict__ lvl,
                                                               unsigned long long* __restrict__ work,
                                                               unsigned long long* __restrict__ trips) {
   const VolDims& V = A.V;
   const int level = A.level;
-  const int64_t count = S.offset[L1] - S.offset[L0];
+  const unsigned long long count = *n_items;
   int path[kPathCap];
   int np = 0;
   int64_t end = 0;
@@ -290,33 +317,25 @@ __global__ void __launch_bounds__(128, 6) integrate_level_kernel(const Adv32 A, 
   int t_iters = 0, t_n = 0;
   int64_t last_nv = -1;  // nearest vertex the stop test last passed
   while (true) {
-    // most items of the late levels were labelled by earlier paths: a lane that drew
-    // one draws again at once (a few rounds) instead of idling through the turn
-    for (int draw = 0; draw < kMaxDraws; draw++) {
+    {
       const unsigned long long t = claim_item(phase == kLaneIdle, work);
       if (phase == kLaneIdle) {
-        if (t >= (unsigned long long)count) {
+        if (t >= count) {
           phase = kLaneDone;
         } else {
-          const int64_t u = S.offset[L0] + (int64_t)t;
-          int L = L0;
-          while (L + 1 < L1 && S.offset[L + 1] <= u) L++;
-          const int64_t i = S.start[L] + (u - S.offset[L]) * S.stride[L];
-          if (lvl[i] >= level) {  // else labelled already
-            split_index(V, i, x, y, z);
-            cur = {(float)x, (float)y, (float)z};
-            iters = A.P.iteration_limit;
-            anchor = cur;
-            t_iters = iters;
-            t_n = 0;
-            last_nv = -1;
-            np = 0;
-            path[np++] = (int)i;
-            phase = kLaneEnter;
-          }
+          const int64_t i = items[t];
+          split_index(V, i, x, y, z);
+          cur = {(float)x, (float)y, (float)z};
+          iters = A.P.iteration_limit;
+          anchor = cur;
+          t_iters = iters;
+          t_n = 0;
+          last_nv = -1;
+          np = 0;
+          path[np++] = (int)i;
+          phase = kLaneEnter;
         }
       }
-      if (!__any_sync(kFullMask, phase == kLaneIdle)) break;
     }
     if (__all_sync(kFullMask, phase == kLaneDone)) {
       add_trips(ntrips, trips);
@@ -917,7 +936,7 @@ int trips_per_turn() {
 
 cudaError_t launch_integrate_pass1(const float4* G, const VolDims& V, const IntegParams& P, const SpreadOrder& S,
                                    int32_t* lab, uint8_t* lvl, unsigned long long* work, unsigned long long* trips,
-                                   int num_sms, cudaStream_t stream) {
+                                   int32_t* items, unsigned long long* n_items, int num_sms, cudaStream_t stream) {
   const int64_t N = V.X * V.Y * V.Z;
   if (cudaError_t e = cudaMemsetAsync(work, 0, sizeof(unsigned long long) * 48, stream)) return e;
   ::msc::count_launch();
@@ -937,19 +956,22 @@ cudaError_t launch_integrate_pass1(const float4* G, const VolDims& V, const Inte
     const int64_t blocks = (count + 127) / 128;
     const int grid = (int)(blocks < num_sms * kLaneCtasPerSm ? blocks : num_sms * kLaneCtasPerSm);
     unsigned long long* w = work + (stamp - 1);
+    if (cudaError_t e = cudaMemsetAsync(n_items, 0, sizeof(unsigned long long), stream)) return e;
+    ::msc::count_launch();
+    compact_level_kernel<<<grid, 128, 0, stream>>>(S, g0, L1, lvl, stamp, items, n_items);
     ::msc::count_launch();
     switch (trips_per_turn()) {
       case 16:
-        integrate_level_kernel<16><<<grid, 128, 0, stream>>>(A, S, g0, L1, lab, lvl, w, trips);
+        integrate_level_kernel<16><<<grid, 128, 0, stream>>>(A, items, n_items, lab, lvl, w, trips);
         break;
       case 2:
-        integrate_level_kernel<2><<<grid, 128, 0, stream>>>(A, S, g0, L1, lab, lvl, w, trips);
+        integrate_level_kernel<2><<<grid, 128, 0, stream>>>(A, items, n_items, lab, lvl, w, trips);
         break;
       case 4:
-        integrate_level_kernel<4><<<grid, 128, 0, stream>>>(A, S, g0, L1, lab, lvl, w, trips);
+        integrate_level_kernel<4><<<grid, 128, 0, stream>>>(A, items, n_items, lab, lvl, w, trips);
         break;
       default:
-        integrate_level_kernel<8><<<grid, 128, 0, stream>>>(A, S, g0, L1, lab, lvl, w, trips);
+        integrate_level_kernel<8><<<grid, 128, 0, stream>>>(A, items, n_items, lab, lvl, w, trips);
     }
   }
   return cudaGetLastError();

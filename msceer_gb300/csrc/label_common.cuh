@@ -110,9 +110,10 @@ struct SpreadOrder {
 
 // `work`: 48 device counters (the levels' claimed items), zeroed here.  `trips`
 // (here and below): a device counter the kernels add their advection iterations to.
+// `items`: scratch for the largest level's vertices, `n_items` a device counter.
 cudaError_t launch_integrate_pass1(const float4* G, const VolDims& V, const IntegParams& P, const SpreadOrder& S,
                                    int32_t* lab, uint8_t* lvl, unsigned long long* work, unsigned long long* trips,
-                                   int num_sms, cudaStream_t stream);
+                                   int32_t* items, unsigned long long* n_items, int num_sms, cudaStream_t stream);
 cudaError_t launch_boundary_set(const int32_t* lab, const uint8_t* state, const VolDims& V, int64_t* list, int* n,
                                 uint32_t* queued, int num_sms, cudaStream_t stream);
 // `work`: a device counter of claimed items, zeroed by the launchers

@@ -368,7 +368,10 @@ int first_pass(LabelCtx& c, DirLabels& d) {
   uint8_t* lvl;
   LCUDA(c.pool.get(&lvl, N), "alloc");
   LCUDA(cudaMemsetAsync(c.work + 48, 0, 3 * sizeof(unsigned long long), st), "memset");
-  LCUDA(msc::launch_integrate_pass1(c.g32, c.V, P, S, d.lab, lvl, c.work, c.work + 48, c.sms, st), "integrate");
+  // the fix-up's list buffer (N int64) holds a level's vertices (at most N) meanwhile
+  LCUDA(msc::launch_integrate_pass1(c.g32, c.V, P, S, d.lab, lvl, c.work, c.work + 48,
+                                    reinterpret_cast<int32_t*>(c.list_a), c.work + 52, c.sms, st),
+        "integrate");
   return MSC_OK;
 }
 
