@@ -46,6 +46,7 @@ SIGNATURES = {
     "msc_labels_last_error_string": (ctypes.c_char_p, []),
     "msc_labels_last_stats": (None, [_I64P]),
     "msc_labels_last_iterations": (None, [_I64P]),
+    "msc_trim_scratch": (None, []),
     "msc_triage_last_error_string": (ctypes.c_char_p, []),
     "msc_triage_features_3d": (ctypes.c_int, [_VP, _VP, _I64P, _VP, _VP, _VP, _VP]),  # f grad dims p feat tgt st
     "msc_triage_forward_3d": (ctypes.c_int, [_VP, _I64P, _VP, _VP, _VP, _VP, _VP]),
