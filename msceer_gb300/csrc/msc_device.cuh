@@ -13,6 +13,10 @@
 namespace msc {
 
 // Process-wide count of the library's kernel launches (msc_kernel_launches()).
+// The library's device scratch comes from a memory pool of its own per device that keeps
+// its memory between calls (msc_trim_scratch hands the unused part back).
+cudaError_t scratch_pool(cudaMemPool_t* out);
+cudaError_t scratch_alloc(void** p, size_t bytes, cudaStream_t stream);
 void count_launch();
 void add_launches(long long n);
 long long launches_so_far();

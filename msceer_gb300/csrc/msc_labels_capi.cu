@@ -145,41 +145,13 @@ void host_merge(int dir, float threshold, std::vector<msc::Arc>& arcs, const std
   for (int i = 0; i < n; i++) rep[i] = find(i);
 }
 
-// The labeling's scratch comes from a memory pool of the library's own per device that
-// keeps its memory between calls (msc_trim_scratch hands it back): a 512^3 call uses
-// ~18 GB per direction, and mapping that afresh on every call cost ~0.09 s of 0.72 s.
-std::mutex g_pool_mu;
-std::map<int, cudaMemPool_t> g_pools;
-
-cudaError_t scratch_pool(cudaMemPool_t* out) {
-  int dev = 0;
-  if (cudaError_t e = cudaGetDevice(&dev)) return e;
-  std::lock_guard<std::mutex> lk(g_pool_mu);
-  auto it = g_pools.find(dev);
-  if (it != g_pools.end()) {
-    *out = it->second;
-    return cudaSuccess;
-  }
-  cudaMemPoolProps props = {};
-  props.allocType = cudaMemAllocationTypePinned;
-  props.location.type = cudaMemLocationTypeDevice;
-  props.location.id = dev;
-  cudaMemPool_t pool = nullptr;
-  if (cudaError_t e = cudaMemPoolCreate(&pool, &props)) return e;
-  uint64_t keep = ~0ull;
-  if (cudaError_t e = cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep)) return e;
-  g_pools[dev] = pool;
-  *out = pool;
-  return cudaSuccess;
-}
-
 // Device scratch of one call, freed in stream order into the scratch pool.
 struct Pool {
   cudaStream_t st;
   cudaMemPool_t mp = nullptr;
   cudaError_t init_err;
   std::vector<void*> ptrs;
-  explicit Pool(cudaStream_t s) : st(s) { init_err = scratch_pool(&mp); }
+  explicit Pool(cudaStream_t s) : st(s) { init_err = msc::scratch_pool(&mp); }
   ~Pool() {
     for (void* p : ptrs) cudaFreeAsync(p, st);
   }
@@ -816,11 +788,6 @@ const char* msc_labels_last_error_string(void) { return t_err.c_str(); }
 void msc_labels_last_stats(int64_t out[4]) {
   if (out)
     for (int k = 0; k < 4; k++) out[k] = t_stats[k];
-}
-
-void msc_trim_scratch(void) {
-  std::lock_guard<std::mutex> lk(g_pool_mu);
-  for (auto& kv : g_pools) cudaMemPoolTrimTo(kv.second, 0);
 }
 
 void msc_labels_last_iterations(int64_t out[6]) {
