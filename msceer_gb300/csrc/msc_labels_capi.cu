@@ -334,15 +334,15 @@ int prepare_direction(LabelCtx& c, DirLabels& d, int32_t* stage_terminal) {
 // stop threshold run to the iteration limit and end at their nearest vertex (on k^-3
 // fields ~2% of the descending boundary re-decisions and 3/4 of their iterations).
 // Outside the all-FP64 mode the integration kernels end such a streamline once it has
-// stayed within 0.02 voxel for two windows of 128 iterations.  Where the orbit sits on
-// a plane at which the nearest vertex changes, its final side is a coin flip of the
-// chaotic orbit; against the all-FP64 labels the cut-off changed nothing measurable
-// (256^3 and 192^3 k^-3: 3.4e-5 / 1.7e-4 and 3.5e-5 / 2.1e-4 label difference, asc /
-// dsc, with and without it in the FP64 re-decisions).
+// stayed within 0.02 voxel for two windows of 64 iterations.  Where the orbit sits on a
+// plane at which the nearest vertex changes, its final side is a coin flip of the
+// chaotic orbit.  Against the all-FP64 labels (k^-3, asc / dsc): 3.6e-5 / 2.0e-4 of the
+// vertices differ at 256^3, 3.8e-5 / 2.6e-4 at 192^3 (windows of 128: 3.4e-5 / 1.7e-4
+// and 3.5e-5 / 2.1e-4, at 10% more time for the 512^3 labels).
 msc::IntegParams integ_params(const msc_integ_params* p, int dir) {
   msc::IntegParams P{p->error_threshold, p->gradient_threshold, p->iteration_limit, (double)p->max_step, dir};
   if (p->precision != 1) {
-    P.trap_window = 128;
+    P.trap_window = 64;
     P.trap_radius = 0.02f;
   }
   return P;
