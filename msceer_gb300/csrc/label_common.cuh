@@ -34,6 +34,14 @@ enum : uint8_t {
 constexpr int32_t kLabelNone = -2;
 
 __host__ __device__ inline void cell_coords(const VolDims& V, int64_t id, int64_t k[3]) {
+  if ((uint64_t)id <= 0xFFFFFFFFull) {  // 32-bit divisions (a 64-bit one is a long sequence)
+    const uint32_t u = (uint32_t)id, dx = (uint32_t)V.dX, dy = (uint32_t)V.dY;
+    const uint32_t q = u / dx;
+    k[0] = u - q * dx;
+    k[1] = q % dy;
+    k[2] = q / dy;
+    return;
+  }
   k[0] = id % V.dX;
   k[1] = (id / V.dX) % V.dY;
   k[2] = id / (V.dX * V.dY);

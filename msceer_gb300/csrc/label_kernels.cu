@@ -26,46 +26,76 @@ namespace msc {
 
 // Every critical cell of the extremum / saddle dimension of the walk.  Extremum ids
 // are keyed by a vertex: the minimum itself, or the hex's lowest corner.
+// Warp-wide exclusive prefix sum of v; `total` receives the warp's sum.
+__device__ __forceinline__ int warp_exclusive_sum(int v, int& total) {
+  const int lane = threadIdx.x & 31;
+  int x = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += y;
+  }
+  total = __shfl_sync(0xffffffffu, x, 31);
+  return x - v;
+}
+
+// Every thread scans 16 consecutive cells (one 16-byte load where the array allows);
+// the critical cells of this direction are appended with one atomic per warp and kind.
 __global__ void find_critical_kernel(const uint8_t* __restrict__ g, const VolDims V, int dir,
                                      int32_t* __restrict__ ext_id_of_key, int64_t* __restrict__ ext_cells,
                                      int* __restrict__ n_ext, int64_t* __restrict__ saddles, int* __restrict__ n_sad) {
   const int ext_dim = dir < 0 ? 0 : 3, sad_dim = dir < 0 ? 1 : 2;
   const int64_t nc = V.dX * V.dY * V.dZ;
+  const int64_t nchunks = (nc + 15) / 16;
+  const bool vec = (reinterpret_cast<uintptr_t>(g) & 15u) == 0;
   const int lane = threadIdx.x & 31;
-  for (int64_t id = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; id < nc; id += (int64_t)gridDim.x * blockDim.x) {
-    const uint8_t b = g[id];
-    int kind = 0;  // 1: extremum, 2: saddle of this direction
-    int64_t k[3] = {0, 0, 0};
-    if (((b >> 2) & 7) == 7) {
-      cell_coords(V, id, k);
+  for (int64_t ch = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; ch - lane < nchunks;
+       ch += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t c0 = ch * 16;
+    uint8_t bytes[16];
+    if (ch < nchunks && vec && c0 + 16 <= nc) {
+      const uint4 w = *reinterpret_cast<const uint4*>(g + c0);
+      const uint32_t ws[4] = {w.x, w.y, w.z, w.w};
+#pragma unroll
+      for (int j = 0; j < 16; j++) bytes[j] = (uint8_t)(ws[j >> 2] >> (8 * (j & 3)));
+    } else {
+#pragma unroll
+      for (int j = 0; j < 16; j++) bytes[j] = (ch < nchunks && c0 + j < nc) ? g[c0 + j] : (uint8_t)0;
+    }
+    uint32_t ext_mask = 0, sad_mask = 0;
+#pragma unroll
+    for (int j = 0; j < 16; j++) {
+      if (((bytes[j] >> 2) & 7) != 7) continue;
+      int64_t k[3];
+      cell_coords(V, c0 + j, k);
       const int d = (int)((k[0] & 1) + (k[1] & 1) + (k[2] & 1));
-      if (d == ext_dim) kind = 1;
+      if (d == ext_dim) ext_mask |= 1u << j;
       // trace_up_2saddle skips 2-saddles on the boundary (gi_extrema_region_builder.h:315-318)
-      else if (d == sad_dim && !(dir > 0 && boundary_value(V, k) != 0)) kind = 2;
+      else if (d == sad_dim && !(dir > 0 && boundary_value(V, k) != 0)) sad_mask |= 1u << j;
     }
-    // one atomic per warp and kind: millions of critical cells would otherwise
-    // serialise on the two counters
-    const unsigned act = __activemask();
-    const unsigned lt = (1u << lane) - 1u;
-    const unsigned me = __ballot_sync(act, kind == 1);
-    if (me) {
-      const int leader = __ffs(me) - 1;
-      int base = 0;
-      if (lane == leader) base = atomicAdd(n_ext, __popc(me));
-      base = __shfl_sync(act, base, leader);
-      if (kind == 1) {
-        const int slot = base + __popc(me & lt);
-        ext_cells[slot] = id;
-        ext_id_of_key[(k[0] >> 1) + (k[1] >> 1) * V.X + (k[2] >> 1) * V.X * V.Y] = slot;
-      }
+    int ne = 0, ns = 0;
+    const int oe = warp_exclusive_sum(__popc(ext_mask), ne);
+    const int os = warp_exclusive_sum(__popc(sad_mask), ns);
+    int be = 0, bs = 0;
+    if (lane == 0) {
+      if (ne) be = atomicAdd(n_ext, ne);
+      if (ns) bs = atomicAdd(n_sad, ns);
     }
-    const unsigned ms = __ballot_sync(act, kind == 2);
-    if (ms) {
-      const int leader = __ffs(ms) - 1;
-      int base = 0;
-      if (lane == leader) base = atomicAdd(n_sad, __popc(ms));
-      base = __shfl_sync(act, base, leader);
-      if (kind == 2) saddles[base + __popc(ms & lt)] = id;
+    be = __shfl_sync(0xffffffffu, be, 0) + oe;
+    bs = __shfl_sync(0xffffffffu, bs, 0) + os;
+    while (ext_mask) {
+      const int j = __ffs(ext_mask) - 1;
+      ext_mask &= ext_mask - 1;
+      int64_t k[3];
+      cell_coords(V, c0 + j, k);
+      ext_cells[be] = c0 + j;
+      ext_id_of_key[(k[0] >> 1) + (k[1] >> 1) * V.X + (k[2] >> 1) * V.X * V.Y] = be;
+      be++;
+    }
+    while (sad_mask) {
+      const int j = __ffs(sad_mask) - 1;
+      sad_mask &= sad_mask - 1;
+      saddles[bs++] = c0 + j;
     }
   }
 }
