@@ -208,6 +208,9 @@ __global__ void place_seeds_kernel(const int32_t* __restrict__ rep, const int64_
 
 // ---- K5b: certain terminal regions --------------------------------------------------
 
+constexpr uint16_t kQueueEmpty = 0xFFFF;          // an unfilled slot of a shared-memory queue
+constexpr uint32_t kQueueSpinLimit = 1u << 24;    // bound of a wait for a slot (~0.5 s)
+
 template <int TX, int TY, int TZ>
 struct VBox {
   static constexpr int H = 2;
@@ -262,7 +265,7 @@ struct TerminalWalk {
       if (!inside(wx + nx[k], wy + ny[k], wz + nz[k])) continue;
       const int u = w + nx[k] + ny[k] * B::LX + nz[k] * B::LX * B::LY;
       if (!before(u, w)) continue;
-      const int32_t lu = sl[u];
+      const int32_t lu = reinterpret_cast<volatile int32_t*>(sl)[u];
       if (lu < 0) return -1;
       if (!has) { lab = lu; has = true; }
       else if (lu != lab) return -1;
@@ -280,18 +283,20 @@ struct TerminalWalk {
       if (wx < 1 || wx >= B::LX - 1 || wy < 1 || wy >= B::LY - 1 || wz < 1 || wz >= B::LZ - 1) continue;
       if (!inside(wx, wy, wz)) continue;
       const int w = v + nx[k] + ny[k] * B::LX + nz[k] * B::LX * B::LY;
-      if (sl[w] != -1 || !before(v, w)) continue;
+      if (reinterpret_cast<volatile int32_t*>(sl)[w] != -1 || !before(v, w)) continue;
       const int32_t l = inspect(w, wx, wy, wz);
       if (l < 0) continue;
       const uint32_t bit = 1u << (w & 31);
       if (atomicOr(&vis[w >> 5], bit) & bit) continue;
-      sl[w] = l;
+      reinterpret_cast<volatile int32_t*>(sl)[w] = l;
+      __threadfence_block();  // the label before the vertex is handed to another thread
       atomicOr(&dirty[w >> 5], bit);
       if (next < 0) {
         next = w;
       } else {
         const int slot = atomicAdd(qtail, 1);
-        if (slot < B::NL) sq[slot] = (uint16_t)w; else atomicOr(err, kErrLocalQueue);
+        if (slot < B::NL) reinterpret_cast<volatile uint16_t*>(sq)[slot] = (uint16_t)w;
+        else atomicOr(err, kErrLocalQueue);
       }
     }
     return next;
@@ -310,10 +315,13 @@ __global__ void __launch_bounds__(BS) terminal_pass_kernel(const float* __restri
   extern __shared__ __align__(16) unsigned char s_dyn[];
   float* sf = reinterpret_cast<float*>(s_dyn);
   int32_t* sl = reinterpret_cast<int32_t*>(s_dyn + (size_t)NL * 4);
+  // queue: NL pushes at most (a vertex is labelled once) plus one pending claim per thread
+  constexpr int QCAP = NL + BS;
   uint16_t* sq = reinterpret_cast<uint16_t*>(s_dyn + (size_t)NL * 8);
-  uint32_t* s_vis = reinterpret_cast<uint32_t*>(s_dyn + (size_t)NL * 10 + ((NL * 10) % 4 ? 4 - (NL * 10) % 4 : 0));
+  constexpr size_t VOFF = (size_t)NL * 8 + (size_t)QCAP * 2;
+  uint32_t* s_vis = reinterpret_cast<uint32_t*>(s_dyn + VOFF + (VOFF % 4 ? 4 - VOFF % 4 : 0));
   uint32_t* s_dirty = s_vis + B::NW;
-  __shared__ int s_qtail, s_border;
+  __shared__ int s_qtail, s_border, s_head, s_done;
 
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   constexpr int NWARPS = BS / 32;
@@ -349,11 +357,14 @@ __global__ void __launch_bounds__(BS) terminal_pass_kernel(const float* __restri
     if (tid == 0) {
       s_qtail = 0;
       s_border = 0;
+      s_head = 0;
+      s_done = 0;
     }
     for (int w = tid; w < B::NW; w += BS) {
       s_vis[w] = 0;
       s_dirty[w] = 0;
     }
+    for (int k = tid; k < QCAP; k += BS) sq[k] = kQueueEmpty;
     __syncthreads();
     for (int row = warp; row < B::LY * B::LZ; row += NWARPS) {
       const int ly = row % B::LY, lz = row / B::LY;
@@ -374,19 +385,40 @@ __global__ void __launch_bounds__(BS) terminal_pass_kernel(const float* __restri
       }
     }
     __syncthreads();
-    int lo = 0, hi = s_qtail;
-#pragma unroll 1
-    while (lo < hi) {
-      for (int k = lo + tid; k < hi; k += BS) {
-        int it = sq[k];
-        while (it >= 0) it = W.step(it);
+    // The walk's fixpoint does not depend on the order, so instead of breadth-first
+    // levels separated by barriers (threads idled at each barrier behind the longest
+    // chain) every thread claims the next queue slot as soon as its chain ends.  Slots
+    // are filled in the order they are reserved (s_qtail); a thread whose slot is not
+    // filled yet waits, and all stop once every reserved item is done (s_done ==
+    // s_qtail) with their slots beyond the last one: an item counts as done only after
+    // its chain has reserved whatever it pushes, so no work is in flight then.
+    {
+      int h = atomicAdd(&s_head, 1);
+      volatile uint16_t* vq = sq;
+      volatile int* vdone = &s_done;
+      volatile int* vtail = &s_qtail;
+      for (uint32_t spin = 0;; spin++) {
+        const uint16_t it = h < QCAP ? (uint16_t)vq[h] : (uint16_t)kQueueEmpty;
+        if (it != kQueueEmpty) {
+          int cur = it;
+          while (cur >= 0) cur = W.step(cur);
+          __threadfence_block();
+          atomicAdd(&s_done, 1);
+          h = atomicAdd(&s_head, 1);
+          spin = 0;
+          continue;
+        }
+        const int d = *vdone;
+        const int t = *vtail;
+        if (d == t && h >= t) break;
+        if (spin > kQueueSpinLimit) {  // cannot happen by construction: report, stop
+          atomicOr(err, kErrIterLimit);
+          break;
+        }
+        __nanosleep(32);
       }
-      __syncthreads();
-      const int nhi = s_qtail;
-      __syncthreads();
-      lo = hi;
-      hi = nhi;
     }
+    __syncthreads();
     for (int w = tid; w < B::NW; w += BS) {
       uint32_t m = s_dirty[w];
       while (m) {
@@ -427,7 +459,7 @@ cudaError_t launch_terminal_pass(const float* f, int32_t* lab, const VolDims& V,
   const int grid = (int)(nt < cap ? nt : cap);
   if (grid <= 0) return cudaSuccess;
   auto k = terminal_pass_kernel<kVTX, kVTY, kVTZ, kVBS>;
-  const size_t sm = VB::smem_bytes() + 16;
+  const size_t sm = VB::smem_bytes() + (size_t)kVBS * 2 + 16;
   cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
   if (e != cudaSuccess) return e;
   ::msc::count_launch();
