@@ -41,8 +41,12 @@ struct LdirTile {
   static constexpr int NW = (NL + 31) / 32;
   // dynamic shared memory of the pass kernel: queue (u16) | bytes | visited bits | changed bits
   static constexpr size_t smem_bytes() { return (size_t)NL * 2 + ((NL + 3) / 4) * 4 + (size_t)NW * 8; }
-  // of the tile kernel: queue (u16) | bytes | value-2 marks | visited bits
-  static constexpr size_t tile_smem_bytes() { return (size_t)NL * 2 + ((NL + 3) / 4) * 8 + (size_t)NW * 4; }
+  // of the tile kernel: queue (u16; NL items at most plus one pending claim per thread,
+  // QX >= the block size) | bytes | value-2 marks | visited bits
+  static constexpr int QX = 1024;
+  static constexpr size_t tile_smem_bytes() {
+    return (size_t)(NL + QX) * 2 + ((NL + 3) / 4) * 8 + (size_t)NW * 4;
+  }
 };
 
 // local index -> local coords
@@ -104,6 +108,24 @@ __device__ __forceinline__ void warp_push(uint16_t* sq, int* qtail, int cap, int
   if (want) {
     const int slot = base + __popc(m & ((1u << lane) - 1u));
     if (slot < cap) sq[slot] = (uint16_t)item; else atomicOr(err, kErrLocalQueue);
+  }
+}
+
+// warp_push for a queue that other threads read while it grows (the tile kernel's
+// barrier-free walk): the item is stored through a volatile pointer.
+__device__ __forceinline__ void warp_push_live(uint16_t* sq, int* qtail, int cap, int* err, bool want, int item) {
+  const unsigned act = __activemask();
+  const unsigned m = __ballot_sync(act, want);
+  if (!m) return;
+  const int lane = threadIdx.x & 31;
+  const int leader = __ffs(m) - 1;
+  int base = 0;
+  if (lane == leader) base = atomicAdd(qtail, __popc(m));
+  base = __shfl_sync(act, base, leader);
+  if (want) {
+    const int slot = base + __popc(m & ((1u << lane) - 1u));
+    if (slot < cap) reinterpret_cast<volatile uint16_t*>(sq)[slot] = (uint16_t)item;
+    else atomicOr(err, kErrLocalQueue);
   }
 }
 
@@ -466,11 +488,14 @@ struct LdirWalk2 {
       for (int s = 0; s < 2; s++) {
         // cofacets only along even axes, +axis first
         const int nx = (l[a] & 1) ? -1 : visit(i, l, a, s == 0 ? 1 : -1, r2);
-        warp_push(sq, qtail, T::NL, err, nx >= 0, nx);
+        warp_push_live(sq, qtail, T::NL, err, nx >= 0, nx);
       }
     }
   }
 };
+
+constexpr uint16_t kTileQueueEmpty = 0xFFFF;        // an unfilled slot (NL < 65535)
+constexpr uint32_t kTileQueueSpinLimit = 1u << 24;  // bound of a wait for a slot (~0.5 s)
 
 __device__ __forceinline__ int batch_volume(const LdirBatch& B, int64_t flat_tile) {
   int lo = 0, hi = B.n - 1;
@@ -489,11 +514,13 @@ __global__ void __launch_bounds__(BS) ldir_tile_kernel(const LdirBatch B, uint8_
   static_assert(NL < 65536, "local ids are 16-bit");
   extern __shared__ __align__(16) unsigned char s_dyn[];
   // queue (u16) | .grad bytes | value-2 marks | visited bits
+  constexpr int QCAP = NL + T::QX;
+  static_assert(BS <= T::QX, "one pending queue claim per thread");
   uint16_t* sq = reinterpret_cast<uint16_t*>(s_dyn);
-  uint8_t* sg = s_dyn + (size_t)NL * 2;
+  uint8_t* sg = s_dyn + (size_t)QCAP * 2;
   uint8_t* m2 = sg + ((NL + 3) / 4) * 4;
   uint32_t* s_vis = reinterpret_cast<uint32_t*>(m2 + ((NL + 3) / 4) * 4);
-  __shared__ int s_qtail;
+  __shared__ int s_qtail, s_head, s_done;
 
   const int tid = threadIdx.x;
 
@@ -523,8 +550,13 @@ __global__ void __launch_bounds__(BS) ldir_tile_kernel(const LdirBatch B, uint8_
       const int64_t hi = dd[a] - o[a];
       W.lmax[a] = (int)(hi < LE[a] ? hi : LE[a]);
     }
-    if (tid == 0) s_qtail = 0;
+    if (tid == 0) {
+      s_qtail = 0;
+      s_head = 0;
+      s_done = 0;
+    }
     for (int w = tid; w < T::NW; w += BS) s_vis[w] = 0;
+    for (int k = tid; k < QCAP; k += BS) sq[k] = kTileQueueEmpty;
     __syncthreads();
 
     // stage the box (cells outside the complex read as 0 = unassigned), many loads in
@@ -565,19 +597,35 @@ __global__ void __launch_bounds__(BS) ldir_tile_kernel(const LdirBatch B, uint8_
     }
     __syncthreads();
 
-    // both closures, level by level
-    int lo = 0, hi = s_qtail;
-#pragma unroll 1
-    while (lo < hi) {
-      for (int k0 = lo; k0 < hi; k0 += BS) {
-        const int k = k0 + tid;
-        if (k < hi) W.step(sq[k]);
+    // both closures; the fixpoint does not depend on the order, so rather than BFS
+    // levels separated by barriers every thread takes the next queue slot as soon as
+    // its item is walked.  A slot below s_qtail is filled by its producer; a thread
+    // whose slot is beyond every reserved one stops once every reserved item is done
+    // (an item counts as done only after its pushes were reserved).
+    {
+      int h = atomicAdd(&s_head, 1);
+      volatile uint16_t* vq = sq;
+      volatile int* vdone = &s_done;
+      volatile int* vtail = &s_qtail;
+      for (uint32_t spin = 0;; spin++) {
+        const uint16_t it = h < QCAP ? (uint16_t)vq[h] : (uint16_t)kTileQueueEmpty;
+        if (it != kTileQueueEmpty) {
+          W.step(it);
+          __threadfence_block();
+          atomicAdd(&s_done, 1);
+          h = atomicAdd(&s_head, 1);
+          spin = 0;
+          continue;
+        }
+        const int d = *vdone;
+        const int t = *vtail;
+        if (d == t && h >= t) break;
+        if (spin > kTileQueueSpinLimit) {  // cannot happen by construction: report, stop
+          atomicOr(err, kErrPassLimit);
+          break;
+        }
+        __nanosleep(32);
       }
-      __syncthreads();
-      const int nhi = s_qtail;
-      __syncthreads();
-      lo = hi;
-      hi = nhi;
     }
 
     // fold the value-2 marks into the bytes
