@@ -314,14 +314,13 @@ MSC_HD uint8_t cell_byte(const State& st, int p, uint32_t Bany, uint32_t enc_map
   return (uint8_t)(1 | (flag << 1) | (code << 2) | (ldir << 5));
 }
 
-// One vertex, end to end: gather its 3^ND neighbourhood through `load(p)`, write the
-// values to the column `col` (stride `cs`), build the lower star, expand every
-// boundary class and emit each owned cell's byte through `store(p, byte)`.
-// `interior`: the vertex is at least one vertex away from every face (no bounds
-// checks, a single boundary class).  Returns true if a NaN was seen.
-template <int ND, class Load, class Store>
-MSC_HD bool process_vertex(int64_t x, int64_t y, int64_t z, int64_t X, int64_t Y, int64_t Z, bool interior,
-                           const Load& load, uint64_t* col, int cs, uint32_t enc_map, const Store& store) {
+// First half of one vertex's work: gather its 3^ND neighbourhood through `load(p)`,
+// write the cells' lowest-vertex keys to the column `col` (stride `cs`) and return the
+// lower-star mask.  `interior`: the vertex is at least one vertex away from every face
+// (no bounds checks).  `nan` is set if a NaN was seen.
+template <int ND, class Load>
+MSC_HD uint32_t lower_star_keys(int64_t x, int64_t y, int64_t z, int64_t X, int64_t Y, int64_t Z, bool interior,
+                                const Load& load, uint64_t* col, int cs, bool& nan) {
   using N = Nb<ND>;
   constexpr int NPOS = N::NPOS;
   constexpr int C = N::CENTER;
@@ -330,7 +329,7 @@ MSC_HD bool process_vertex(int64_t x, int64_t y, int64_t z, int64_t X, int64_t Y
   uint64_t k[NPOS];  // vertex keys, folded below into the cells' lowest-vertex keys
   k[C] = order_key(fc, C);
   uint32_t lower = 0;
-  bool nan = (fc != fc);
+  nan = (fc != fc);
   if (interior) {
 #pragma unroll
     for (int p = 0; p < NPOS; p++) {
@@ -375,13 +374,23 @@ MSC_HD bool process_vertex(int64_t x, int64_t y, int64_t z, int64_t X, int64_t Y
   }
 #pragma unroll
   for (int p = 0; p < NPOS; p++) col[p * cs] = k[p];
-  const uint32_t L = lower_star_mask<ND>(lower);
+  return lower_star_mask<ND>(lower);
+}
+
+// Second half: expand every boundary class of the lower star L (keys in `col`) and
+// emit each owned cell's byte through `store(p, byte)`.  bx/by/bz: the vertex lies on
+// the first or last plane of that axis (ignored for an interior vertex).
+template <int ND, class Store>
+MSC_HD void expand_and_store(uint32_t L, uint64_t* col, int cs, bool interior, bool bx, bool by, bool bz,
+                             uint32_t enc_map, const Store& store) {
+  using N = Nb<ND>;
+  constexpr int NPOS = N::NPOS;
   LowerStarState<ND, KeyCol> st(KeyCol{col, cs});
   uint32_t Bany = 0;
   if (interior)
     st.expand(L);
   else
-    Bany = run_classes<ND>(st, L, x == 0 || x == X - 1, y == 0 || y == Y - 1, ND == 3 && (z == 0 || z == Z - 1));
+    Bany = run_classes<ND>(st, L, bx, by, ND == 3 && bz);
   // byte bit-planes: assigned | flag | pair code (7 if critical) | ldir, where ldir
   // is 2 / 1 / 0 for critical 1- / 2- / 3-cells and 3 otherwise
   constexpr uint32_t D0 = N::dim_mask(0), D1 = N::dim_mask(1), D2 = N::dim_mask(2);
@@ -411,6 +420,17 @@ MSC_HD bool process_vertex(int64_t x, int64_t y, int64_t z, int64_t X, int64_t Y
                        (((p2 >> p) & 1u) << 4) | (((l0 >> p) & 1u) << 5) | (((l1 >> p) & 1u) << 6);
     store(p, (uint8_t)b);
   }
+}
+
+
+// One vertex, end to end (both halves).  Returns true if a NaN was seen.
+template <int ND, class Load, class Store>
+MSC_HD bool process_vertex(int64_t x, int64_t y, int64_t z, int64_t X, int64_t Y, int64_t Z, bool interior,
+                           const Load& load, uint64_t* col, int cs, uint32_t enc_map, const Store& store) {
+  bool nan = false;
+  const uint32_t L = lower_star_keys<ND>(x, y, z, X, Y, Z, interior, load, col, cs, nan);
+  expand_and_store<ND>(L, col, cs, interior, x == 0 || x == X - 1, y == 0 || y == Y - 1, z == 0 || z == Z - 1,
+                       enc_map, store);
   return nan;
 }
 
