@@ -4,15 +4,18 @@
 // (gi_numeric_integrator_path_compressing.h:75-433) with AdaptiveEulerAdvector3D
 // (gi_adaptive_euler_advector.h:51-305):
 //   pass 1   every unassigned vertex integrates (FP32) until its nearest vertex is
-//            assigned or terminal, runs out of gradient or of iterations; every vertex
-//            it passed takes the destination label (path compression).  One streamline
-//            per thread; the vertices are visited in the reference's spread order so
-//            early paths compress later ones.
+//            labelled in an earlier level of the reference's spread order, runs out
+//            of gradient or of iterations; every vertex it passed takes the
+//            destination label (path compression), level by level.
 //   fix-up   vertices with a differently labelled 6-neighbour re-integrate until a
-//            certain terminal region, in FP64 with the reference's operation order
-//            (explicit _rn intrinsics: no contraction), so that basin boundaries are
-//            decided as the FP64 oracle decides them; changed labels reopen their
-//            neighbours, in waves to a fixpoint.
+//            certain terminal region, in FP32, and those whose FP32 ending is
+//            ambiguous again in FP64 with the reference's operation order (explicit
+//            _rn intrinsics: no contraction); changed labels reopen their neighbours,
+//            in waves to a fixpoint.
+// All integration kernels run persistent warps whose lanes each advance their own
+// streamline a few iterations per turn and take the next one as soon as it ends; a
+// streamline trapped in a tiny orbit ends where the iteration limit would have ended
+// it (outside the all-FP64 mode).
 // IsolatedCCRegionRemoverNEW::ComputeOutput (gi_isolated_region_remover.h:155-192):
 //   same-label 6-connected components by a lock-free union-find whose roots are the
 //   components' first vertices in the walk order; every component that does not hold
@@ -49,7 +52,6 @@ struct Adv32 {
   const float4* G;
   VolDims V;
   IntegParams P;
-  const int32_t* lab;
   const uint8_t* lvl;    // pass-1 stop (when set): nearest vertex labelled in an earlier level
   int level;
   const uint8_t* state;  // fix-up stop (when set): nearest vertex certain terminal
@@ -59,9 +61,9 @@ struct Adv32 {
   float ms = 0.f, sgn = 0.f;
   float ext[3] = {0.f, 0.f, 0.f}, ext2[3] = {0.f, 0.f, 0.f};
 
-  static Adv32 make(const float4* G, const VolDims& V, const IntegParams& P, const int32_t* lab, const uint8_t* lvl,
-                    int level, const uint8_t* state) {
-    Adv32 A{G, V, P, lab, lvl, level, state};
+  static Adv32 make(const float4* G, const VolDims& V, const IntegParams& P, const uint8_t* lvl, int level,
+                    const uint8_t* state) {
+    Adv32 A{G, V, P, lvl, level, state};
     A.ms = (float)P.max_step;
     A.sgn = (float)P.step_mult;
     const int64_t e[3] = {V.X, V.Y, V.Z};
@@ -952,7 +954,7 @@ cudaError_t launch_integrate_pass1(const float4* G, const VolDims& V, const Inte
     const int g0 = L0;
     L0 = L1;
     if (count <= 0) continue;
-    const Adv32 A = Adv32::make(G, V, P, lab, lvl, ++stamp, nullptr);
+    const Adv32 A = Adv32::make(G, V, P, lvl, ++stamp, nullptr);
     const int64_t blocks = (count + 127) / 128;
     const int grid = (int)(blocks < num_sms * kLaneCtasPerSm ? blocks : num_sms * kLaneCtasPerSm);
     unsigned long long* w = work + (stamp - 1);
@@ -1007,7 +1009,7 @@ cudaError_t launch_fixup32(const float4* G, const VolDims& V, const IntegParams&
                            int64_t* amb, int* n_amb, int amb_mode, unsigned long long* work,
                            unsigned long long* trips, int num_sms, cudaStream_t stream) {
   if (n <= 0) return cudaSuccess;
-  const Adv32 A = Adv32::make(G, V, P, lab, nullptr, 0, state);
+  const Adv32 A = Adv32::make(G, V, P, nullptr, 0, state);
   const int blocks = (n + 127) / 128;
   if (cudaError_t e = cudaMemsetAsync(work, 0, sizeof(unsigned long long), stream)) return e;
   ::msc::count_launch();
