@@ -496,14 +496,14 @@ def run_ours(args, ws, rank, local):
 # dram__bytes_read.sum + dram__bytes_write.sum per launch from the committed ncu
 # summaries under profiles/ (None until captured)
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per launch from one ncu
-# --set full capture of the kernels at 320^3, scaled to 512^3 by the vertex
-# count (x 4.096): the traffic grows with the volume.  ldir_stage = tile + check
-# kernels (the walk's share is below 3% of the stage's time).
+# --set full capture of the kernels at 256^3 (f and .grad together 201 MB, above the
+# L2), scaled to 512^3 by the vertex count (x 8): the traffic grows with the volume.
+# ldir_stage = tile + check kernels (the walk's share is below 3% of the stage's time).
 TRAFFIC_PER_LAUNCH: dict = {
-    ("lstar_kernel", 320): 0.131313e9 + 0.206132e9,
-    ("ldir_stage", 320): 0.313691e9 + 0.364048e9 + 0.448826e9 + 0.025934e9,
-    ("lstar_kernel", 512): (0.131313e9 + 0.206132e9) * 4.096,
-    ("ldir_stage", 512): (0.313691e9 + 0.364048e9 + 0.448826e9 + 0.025934e9) * 4.096,
+    ("lstar_kernel", 256): 67.168e6 + 78.372e6,
+    ("ldir_stage", 256): 158.404e6 + 159.985e6 + 224.759e6 + 12.212e6,
+    ("lstar_kernel", 512): (67.168e6 + 78.372e6) * 8,
+    ("ldir_stage", 512): (158.404e6 + 159.985e6 + 224.759e6 + 12.212e6) * 8,
 }
 FLOP_PER_ITERATION = 183
 FP32_LANES_PER_SM = 128
