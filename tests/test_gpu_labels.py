@@ -68,3 +68,20 @@ def test_batch_labels_on_concurrent_streams_equal_sequential(gpu):
         want = integrated_labels(v, g)
         for k in ("asc", "dsc"):
             assert torch.equal(r[k], want[k])
+
+
+def test_scratch_pool_trim_and_reuse(gpu):
+    """The labeling keeps its scratch in a pool between calls; handing the pool's memory
+    back (msc_trim_scratch) and labeling again gives the same labels."""
+    import torch
+    from msceer_gb300 import _lib, integrated_labels, lower_star_grad
+    f = fields.power_law_field((48, 44, 40), seed=9)
+    t = torch.from_numpy(f).to(gpu)
+    g = lower_star_grad(t)
+    a = integrated_labels(t, g, 1e-4, None, 4000, 0.25, 0.0)
+    b = integrated_labels(t, g, 1e-4, None, 4000, 0.25, 0.0)
+    _lib.load().msc_trim_scratch()
+    torch.cuda.synchronize()
+    c = integrated_labels(t, g, 1e-4, None, 4000, 0.25, 0.0)
+    for k in ("asc", "dsc"):
+        assert torch.equal(a[k], b[k]) and torch.equal(a[k], c[k])
