@@ -85,3 +85,16 @@ def test_scratch_pool_trim_and_reuse(gpu):
     c = integrated_labels(t, g, 1e-4, None, 4000, 0.25, 0.0)
     for k in ("asc", "dsc"):
         assert torch.equal(a[k], b[k]) and torch.equal(a[k], c[k])
+
+
+def test_two_direction_call_matches_single_direction_ascending(gpu):
+    """A two-direction call runs the descending labels concurrently on their own stream
+    and gradient copy; its ascending labels equal those of an ascending-only call."""
+    import torch
+    from msceer_gb300 import integrated_labels, lower_star_grad
+    f = fields.power_law_field((56, 48, 40), seed=10)
+    t = torch.from_numpy(f).to(gpu)
+    g = lower_star_grad(t)
+    both = integrated_labels(t, g, 1e-4, None, 4000, 0.25, 0.0)
+    asc = integrated_labels(t, g, 1e-4, None, 4000, 0.25, 0.0, descending=False)
+    assert torch.equal(both["asc"], asc["asc"])
