@@ -48,6 +48,14 @@ __device__ __forceinline__ float clampf_ext(float v, float fn) {
   return v;
 }
 
+// Streamlines differ in length by orders of magnitude (most end within a few dozen
+// iterations, a few run to the iteration limit circling a sink on a boundary face), so
+// a warp that integrated 32 fixed streamlines would idle most of its lanes behind the
+// longest one.  Instead every lane runs its streamline one iteration per turn of the
+// warp's loop and takes the next work item as soon as its own streamline ends; the
+// items are handed out by one warp-aggregated atomicAdd per turn.
+enum : int { kLaneIdle = 0, kLaneEnter, kLaneStep, kLaneEnd, kLaneDone };
+
 struct Adv32 {
   const float4* G;
   VolDims V;
@@ -60,6 +68,8 @@ struct Adv32 {
   // conversion per iteration would run on the slow FP64 pipe)
   float ms = 0.f, sgn = 0.f;
   float ext[3] = {0.f, 0.f, 0.f}, ext2[3] = {0.f, 0.f, 0.f};
+  int64_t XY = 0;    // vertices per z-plane
+  bool i32 = false;  // vertex ids fit 32 bits
 
   static Adv32 make(const float4* G, const VolDims& V, const IntegParams& P, const uint8_t* lvl, int level,
                     const uint8_t* state) {
@@ -71,27 +81,37 @@ struct Adv32 {
       A.ext[a] = (float)e[a];
       A.ext2[a] = (float)(e[a] - 2);
     }
+    A.XY = V.X * V.Y;
+    A.i32 = V.X * V.Y * V.Z <= (int64_t)0xFFFFFFFF;
     return A;
   }
 
-  __device__ __forceinline__ F3 corner(int64_t x, int64_t y, int64_t z) const {
-    const float4 g = __ldg(G + vid(V, x, y, z));
-    return {g.x, g.y, g.z};
+  // Vertex id of (x, y, z) in 32-bit arithmetic while the grid's ids fit 32 bits
+  __device__ __forceinline__ int64_t index(int x, int y, int z) const {
+    if (i32) return (int64_t)((uint32_t)x + (uint32_t)V.X * ((uint32_t)y + (uint32_t)V.Y * (uint32_t)z));
+    return vid(V, x, y, z);
   }
-  __device__ __forceinline__ void surround(const int64_t b[3], bool clamp, F3 c[8]) const {
-    int64_t vv[3][2];
-    const int64_t ext[3] = {V.X, V.Y, V.Z};
+  // The voxel that holds `cur` (clamped into the grid near its boundary): its base
+  // corner as floats and its eight corner gradients.  A voxel clamped onto the grid's
+  // last plane along an axis repeats that plane's corners there.
+  __device__ __forceinline__ void load_voxel(const F3& cur, bool nearb, float bf[3], F3 c[8]) const {
+    const float p[3] = {cur.x, cur.y, cur.z};
+    int b[3];
+    int64_t o[3] = {1, V.X, XY};
+    const int E[3] = {(int)V.X, (int)V.Y, (int)V.Z};
 #pragma unroll
     for (int a = 0; a < 3; a++) {
-      vv[a][0] = b[a];
-      vv[a][1] = b[a] + 1;
-      if (clamp) {
-        if (b[a] < 0) vv[a][0] = 0;
-        if (b[a] >= ext[a] - 1) vv[a][0] = vv[a][1] = ext[a] - 1;
-      }
+      b[a] = nearb ? (int)clampf_ext(p[a], ext[a]) : (int)fminf(fmaxf(p[a], 0.f), ext2[a]);
+      b[a] = max(b[a], 0);
+      if (nearb && b[a] >= E[a] - 1) o[a] = 0;
+      bf[a] = (float)b[a];
     }
+    const float4* q = G + index(b[0], b[1], b[2]);
 #pragma unroll
-    for (int n = 0; n < 8; n++) c[n] = corner(vv[0][n & 1], vv[1][(n >> 1) & 1], vv[2][n >> 2]);
+    for (int n = 0; n < 8; n++) {
+      const float4 v = __ldg(q + ((n & 1) ? o[0] : 0) + ((n & 2) ? o[1] : 0) + ((n & 4) ? o[2] : 0));
+      c[n] = {v.x, v.y, v.z};
+    }
   }
   // bf: the base corner as floats
   __device__ __forceinline__ static F3 trilin(F3 s, const float bf[3], const F3 c[8]) {
@@ -106,10 +126,10 @@ struct Adv32 {
     iy = (int)clampf_ext(p.y + 0.5f, ext[1]);
     iz = (int)clampf_ext(p.z + 0.5f, ext[2]);
   }
-  __device__ __forceinline__ int64_t nearest(F3 p, bool) const {
+  __device__ __forceinline__ int64_t nearest(F3 p) const {
     int ix, iy, iz;
     nearest3(p, ix, iy, iz);
-    return vid(V, ix, iy, iz);
+    return index(ix, iy, iz);
   }
   // The trapped-streamline test (IntegParams::trap_window): compares `cur` with the
   // anchor set trap_window iterations before, moves the anchor, counts the
@@ -120,94 +140,95 @@ struct Adv32 {
     anchor = cur;
     return n >= 2;
   }
-  // AdvectThroughVoxel{NoCheck,NearBoundary} split in two, so that a lane can run its
-  // streamline one iteration at a time.  enter(): the voxel's base corner, its eight
-  // corner gradients and the gradient at `cur`; false when there is no direction to
-  // follow (LOW_GRADIENT).  The caller then sets old = cur.
-  __device__ __forceinline__ bool enter(const F3& cur, bool nearb, float bf[3], F3 c[8], F3& g, float& gm,
-                                        float& step, float& gm_end) const {
-    int64_t b[3];
-    if (nearb) {
-      b[0] = (int)clampf_ext(cur.x, ext[0]);
-      b[1] = (int)clampf_ext(cur.y, ext[1]);
-      b[2] = (int)clampf_ext(cur.z, ext[2]);
-    } else {
-      b[0] = (int)fminf(fmaxf(cur.x, 0.f), ext2[0]);
-      b[1] = (int)fminf(fmaxf(cur.y, 0.f), ext2[1]);
-      b[2] = (int)fminf(fmaxf(cur.z, 0.f), ext2[2]);
-    }
-    surround(b, nearb, c);
-    bf[0] = (float)(int)b[0];
-    bf[1] = (float)(int)b[1];
-    bf[2] = (float)(int)b[2];
-    g = trilin(cur, bf, c);
-    gm = sqrtf(g.x * g.x + g.y * g.y + g.z * g.z);
-    gm_end = 0.f;
-    if (!(gm > 0.f) || !isfinite(gm)) return false;
-    step = ms / gm;
-    return true;
-  }
-  // One iteration of the advection loop (one `iters` decrement); EV_NONE to go on.
-  // gm_end: the gradient magnitude at a low-gradient stop (0 where there was none).
-  __device__ __forceinline__ int trip(F3& cur, F3& old, int& iters, bool nearb, const float b[3], const F3 c[8],
-                                      F3& g, float& gm, float& step, float& gm_end, int64_t& last_nv) const {
-    if (!(iters-- > 0)) return EV_OVER_MAX_ITERATIONS;
-    if (!(old.x == cur.x && old.y == cur.y && old.z == cur.z)) {
-      if ((int)cur.x != (int)old.x || (int)cur.y != (int)old.y || (int)cur.z != (int)old.z) return EV_OUT_OF_VOXEL;
-      g = trilin(cur, b, c);
-      gm = sqrtf(g.x * g.x + g.y * g.y + g.z * g.z);
-      if (!(gm > 0.f) || !isfinite(gm)) return EV_LOW_GRADIENT;
-      if (gm * step > ms) step = ms / gm;
-      old = cur;
-    }
-    if (gm < P.gthresh) {
-      gm_end = gm;
-      return EV_LOW_GRADIENT;
-    }
-    const float sm = sgn * step;
-    const F3 e1 = {g.x * sm, g.y * sm, g.z * sm};
-    const float hs = sm * 0.5f;
-    const F3 hd = {g.x * hs, g.y * hs, g.z * hs};
-    const F3 hg = trilin({cur.x + hd.x, cur.y + hd.y, cur.z + hd.z}, b, c);
-    const F3 e2 = {hg.x * hs + hd.x, hg.y * hs + hd.y, hg.z * hs + hd.z};
-    const float dx = e2.x - e1.x, dy = e2.y - e1.y, dz = e2.z - e1.z;
-    if (dx * dx + dy * dy + dz * dz < P.ethresh) {
-      F3 np = {cur.x + e2.x, cur.y + e2.y, cur.z + e2.z};
-      if (nearb) {
-        np.x = clampf_ext(np.x, ext[0]);
-        np.y = clampf_ext(np.y, ext[1]);
-        np.z = clampf_ext(np.z, ext[2]);
-      }
-      cur = np;
-      step = fminf(step * 1.8f, ms / gm);
-      // the stop test reads memory only when the nearest vertex changed: what it reads
-      // (certain terminals in the fix-up, earlier levels in the first pass) does not
-      // change while the kernel runs, and a vertex it passed once does not stop it later
-      const int64_t nv = nearest(cur, nearb);
-      if (nv != last_nv) {
-        if (state) {
-          const uint8_t st = state[nv];
-          if (st == kStSeed || st == kStTerminal) return EV_HIT_PREASSIGNED;
-        } else if (lvl[nv] < level) {
-          return EV_HIT_PREASSIGNED;
-        }
-        last_nv = nv;
-      }
-    } else {
-      step = step * 0.5f;
-    }
-    return EV_NONE;
-  }
+  // One round of a lane's streamline (phase kLaneEnter or kLaneStep): the loop body of
+  // AdvectThroughVoxel{NoCheck,NearBoundary}, one `iters` decrement, with the entry
+  // into a voxel folded in (x, y, z: the entering lane's nearest vertex).  Written
+  // without branches between its outcomes (moved or not, step accepted or rejected):
+  // every stepping lane of a warp runs the same instructions, so that the warp issues
+  // one iteration's instructions per round rather than one per outcome.  A lane whose
+  // last step was rejected evaluates the gradient at its unchanged position again (the
+  // same value).  slim caches max_step / |g|.  EV_NONE to go on; gm_end: the gradient
+  // magnitude at a low-gradient stop (0 where there was none).
+  __device__ __forceinline__ int advance(int& phase, int x, int y, int z, F3& cur, F3& old, int& iters, bool& nb,
+                                         float b[3], F3 c[8], F3& g, float& gm, float& step, float& slim,
+                                         float& gm_end, int64_t& last_nv, unsigned long long& ntrips) const;
 };
 
-__device__ __forceinline__ int dist_to_boundary(const VolDims& V, int64_t x, int64_t y, int64_t z) {
-  int64_t m = x < V.X - 1 - x ? x : V.X - 1 - x;
-  const int64_t my = y < V.Y - 1 - y ? y : V.Y - 1 - y;
-  const int64_t mz = z < V.Z - 1 - z ? z : V.Z - 1 - z;
-  if (my < m) m = my;
-  if (mz < m) m = mz;
-  return (int)m;
+// Distance of vertex (x, y, z) to the grid's nearest face, in vertices
+__device__ __forceinline__ int dist_to_boundary(const VolDims& V, int x, int y, int z) {
+  const int X = (int)V.X, Y = (int)V.Y, Z = (int)V.Z;
+  return min(min(min(x, X - 1 - x), min(y, Y - 1 - y)), min(z, Z - 1 - z));
 }
+
+__device__ __forceinline__ int Adv32::advance(int& phase, int x, int y, int z, F3& cur, F3& old, int& iters, bool& nb,
+                                              float b[3], F3 c[8], F3& g, float& gm, float& step, float& slim,
+                                              float& gm_end, int64_t& last_nv, unsigned long long& ntrips) const {
+  const bool ent = phase == kLaneEnter;
+  if (ent) {
+    nb = dist_to_boundary(V, x, y, z) <= 1;
+    load_voxel(cur, nb, b, c);
+    gm_end = 0.f;
+    phase = kLaneStep;
+  }
+  const bool moved = !ent && !(old.x == cur.x && old.y == cur.y && old.z == cur.z);
+  const bool left = moved && ((int)cur.x != (int)old.x || (int)cur.y != (int)old.y || (int)cur.z != (int)old.z);
+  const F3 gc = trilin(cur, b, c);
+  const float gmc = sqrtf(gc.x * gc.x + gc.y * gc.y + gc.z * gc.z);
+  const bool bad = !(gmc > 0.f) || !isfinite(gmc);
+  // events before the step, in the reference's order: an entering lane stops on a
+  // vanishing gradient before it takes an iteration; a stepping lane checks the
+  // iteration count, then whether it left its voxel, then the gradient
+  const bool counts = !(ent && bad);
+  ntrips += counts;
+  const bool spent = counts && !(iters > 0);
+  iters -= counts;
+  int ev = spent ? EV_OVER_MAX_ITERATIONS : EV_NONE;
+  if (ent && bad) ev = EV_LOW_GRADIENT;
+  if (!spent && left) ev = EV_OUT_OF_VOXEL;
+  if (!spent && !left && moved && bad) ev = EV_LOW_GRADIENT;
+  if (ev != EV_NONE) return ev;
+  const float sl = ms / gmc;
+  if (ent || gmc * step > ms) step = sl;
+  g = gc;
+  gm = gmc;
+  slim = sl;
+  old = cur;
+  if (gm < P.gthresh) {
+    gm_end = gm;
+    return EV_LOW_GRADIENT;
+  }
+  // the adaptive Euler step: a full step and two half steps, accepted (the step grows)
+  // when they agree within ethresh, otherwise halved
+  const float sm = sgn * step;
+  const F3 e1 = {g.x * sm, g.y * sm, g.z * sm};
+  const float hs = sm * 0.5f;
+  const F3 hd = {g.x * hs, g.y * hs, g.z * hs};
+  const F3 hg = trilin({cur.x + hd.x, cur.y + hd.y, cur.z + hd.z}, b, c);
+  const F3 e2 = {hg.x * hs + hd.x, hg.y * hs + hd.y, hg.z * hs + hd.z};
+  const float dx = e2.x - e1.x, dy = e2.y - e1.y, dz = e2.z - e1.z;
+  const bool acc = dx * dx + dy * dy + dz * dz < P.ethresh;
+  F3 np = {cur.x + e2.x, cur.y + e2.y, cur.z + e2.z};
+  if (nb) {
+    np.x = clampf_ext(np.x, ext[0]);
+    np.y = clampf_ext(np.y, ext[1]);
+    np.z = clampf_ext(np.z, ext[2]);
+  }
+  step = acc ? fminf(step * 1.8f, sl) : step * 0.5f;
+  if (acc) cur = np;
+  // the stop test reads memory only when an accepted step changed the nearest vertex:
+  // what it reads (certain terminals in the fix-up, earlier levels in the first pass)
+  // does not change while the kernel runs, and a vertex it passed once does not stop
+  // the streamline later
+  const int64_t nv = nearest(np);
+  if (acc && nv != last_nv) {
+    const uint8_t st = state ? state[nv] : lvl[nv];
+    const bool hit = state ? (st == kStSeed || st == kStTerminal) : st < level;
+    if (hit) return EV_HIT_PREASSIGNED;
+    last_nv = nv;
+  }
+  return EV_NONE;
+}
+
 
 
 // Vertex coordinates of index v; 32-bit division while the grid's indices fit 32 bits.
@@ -228,13 +249,6 @@ __device__ __forceinline__ void split_index(const VolDims& V, int64_t v, int& x,
 constexpr int kPathCap = 48;
 constexpr unsigned kFullMask = 0xffffffffu;
 
-// Streamlines differ in length by orders of magnitude (most end within a few dozen
-// iterations, a few run to the iteration limit circling a sink on a boundary face), so
-// a warp that integrated 32 fixed streamlines would idle most of its lanes behind the
-// longest one.  Instead every lane runs its streamline one iteration per turn of the
-// warp's loop and takes the next work item as soon as its own streamline ends; the
-// items are handed out by one warp-aggregated atomicAdd per turn.
-enum : int { kLaneIdle = 0, kLaneEnter, kLaneStep, kLaneEnd, kLaneDone };
 // resident CTAs of 128 threads per SM for the lane-refilling kernels
 constexpr int kLaneCtasPerSm = 16;
 
@@ -310,7 +324,7 @@ __global__ void __launch_bounds__(128, 6) integrate_level_kernel(const Adv32 A, 
   unsigned long long ntrips = 0;
   int x = 0, y = 0, z = 0;
   F3 cur = {0.f, 0.f, 0.f}, old = cur, g = cur;
-  float gm = 0.f, step = 0.f, gm_end = 0.f;
+  float gm = 0.f, step = 0.f, slim = 0.f, gm_end = 0.f;
   int iters = 0;
   bool nb = false;
   float b[3] = {0.f, 0.f, 0.f};
@@ -346,21 +360,8 @@ __global__ void __launch_bounds__(128, 6) integrate_level_kernel(const Adv32 A, 
     // K steps; a lane that leaves its voxel enters the next one within the same turn,
     // a lane whose streamline ended waits for the turn's end
     for (int r = 0; r < K; r++) {
-      if (phase == kLaneEnter) {
-        nb = dist_to_boundary(V, x, y, z) <= 1;
-        if (A.enter(cur, nb, b, c, g, gm, step, gm_end)) {
-          old = cur;
-          phase = kLaneStep;
-        } else {
-          A.nearest3(cur, x, y, z);  // ended at its voxel entry
-          end = vid(V, x, y, z);
-          if (np < kPathCap) path[np++] = (int)end;
-          phase = kLaneEnd;
-        }
-      }
-      if (phase != kLaneStep) continue;
-      ntrips++;
-      const int ev = A.trip(cur, old, iters, nb, b, c, g, gm, step, gm_end, last_nv);
+      if (phase != kLaneEnter && phase != kLaneStep) continue;
+      const int ev = A.advance(phase, x, y, z, cur, old, iters, nb, b, c, g, gm, step, slim, gm_end, last_nv, ntrips);
       if (ev == EV_NONE) continue;
       A.nearest3(cur, x, y, z);
       end = vid(V, x, y, z);
@@ -695,7 +696,7 @@ __global__ void __launch_bounds__(128, 6) fixup32_kernel(const Adv32 A, int32_t*
   int x = 0, y = 0, z = 0;
   int32_t init = 0;
   F3 cur = {0.f, 0.f, 0.f}, old = cur, g = cur;
-  float gm = 0.f, step = 0.f, gm_end = 0.f;
+  float gm = 0.f, step = 0.f, slim = 0.f, gm_end = 0.f;
   int iters = 0, ev = EV_NONE;
   bool nb = false;
   float b[3] = {0.f, 0.f, 0.f};
@@ -726,20 +727,8 @@ __global__ void __launch_bounds__(128, 6) fixup32_kernel(const Adv32 A, int32_t*
       break;
     }
     for (int r = 0; r < K; r++) {
-      if (phase == kLaneEnter) {
-        nb = dist_to_boundary(V, x, y, z) <= 1;
-        if (A.enter(cur, nb, b, c, g, gm, step, gm_end)) {
-          old = cur;
-          phase = kLaneStep;
-        } else {
-          ev = EV_LOW_GRADIENT;
-          A.nearest3(cur, x, y, z);
-          phase = kLaneEnd;
-        }
-      }
-      if (phase != kLaneStep) continue;
-      ntrips++;
-      ev = A.trip(cur, old, iters, nb, b, c, g, gm, step, gm_end, last_nv);
+      if (phase != kLaneEnter && phase != kLaneStep) continue;
+      ev = A.advance(phase, x, y, z, cur, old, iters, nb, b, c, g, gm, step, slim, gm_end, last_nv, ntrips);
       if (ev == EV_NONE) continue;
       A.nearest3(cur, x, y, z);
       phase = ev == EV_OUT_OF_VOXEL ? kLaneEnter : kLaneEnd;
