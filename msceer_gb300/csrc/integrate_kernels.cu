@@ -37,10 +37,6 @@ __device__ __forceinline__ int64_t vid(const VolDims& V, int64_t x, int64_t y, i
 struct F3 {
   float x, y, z;
 };
-__device__ __forceinline__ F3 lerp3(F3 a, F3 b, float t) {
-  const float u = 1.f - t;
-  return {a.x * u + b.x * t, a.y * u + b.y * t, a.z * u + b.z * t};
-}
 // clamp into [0, n - 1] given fn = (float)n
 __device__ __forceinline__ float clampf_ext(float v, float fn) {
   if (v < 0.f) v = 0.f;
@@ -92,8 +88,10 @@ struct Adv32 {
     return vid(V, x, y, z);
   }
   // The voxel that holds `cur` (clamped into the grid near its boundary): its base
-  // corner as floats and its eight corner gradients.  A voxel clamped onto the grid's
-  // last plane along an axis repeats that plane's corners there.
+  // corner as floats and its corner gradients, c[n] for the corners n = x + 2y + 4z,
+  // stored for trilin() as c[2k] and c[2k + 1] - c[2k] (the difference along x).  A
+  // voxel clamped onto the grid's last plane along an axis repeats that plane's
+  // corners there.
   __device__ __forceinline__ void load_voxel(const F3& cur, bool nearb, float bf[3], F3 c[8]) const {
     const float p[3] = {cur.x, cur.y, cur.z};
     int b[3];
@@ -112,12 +110,20 @@ struct Adv32 {
       const float4 v = __ldg(q + ((n & 1) ? o[0] : 0) + ((n & 2) ? o[1] : 0) + ((n & 4) ? o[2] : 0));
       c[n] = {v.x, v.y, v.z};
     }
+#pragma unroll
+    for (int n = 1; n < 8; n += 2) c[n] = {c[n].x - c[n - 1].x, c[n].y - c[n - 1].y, c[n].z - c[n - 1].z};
   }
-  // bf: the base corner as floats
+  // Trilinear interpolation of the corner gradients at s (bf: the base corner as
+  // floats; c as load_voxel() stores it), each linear interpolation as a + t (b - a)
+  __device__ __forceinline__ static F3 mix3(F3 a, F3 d, float t) {
+    return {fmaf(t, d.x, a.x), fmaf(t, d.y, a.y), fmaf(t, d.z, a.z)};
+  }
+  __device__ __forceinline__ static F3 sub3(F3 a, F3 b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
   __device__ __forceinline__ static F3 trilin(F3 s, const float bf[3], const F3 c[8]) {
     const float fx = s.x - bf[0], fy = s.y - bf[1], fz = s.z - bf[2];
-    const F3 x0 = lerp3(c[0], c[1], fx), x1 = lerp3(c[2], c[3], fx), x2 = lerp3(c[4], c[5], fx), x3 = lerp3(c[6], c[7], fx);
-    return lerp3(lerp3(x0, x1, fy), lerp3(x2, x3, fy), fz);
+    const F3 x0 = mix3(c[0], c[1], fx), x1 = mix3(c[2], c[3], fx), x2 = mix3(c[4], c[5], fx), x3 = mix3(c[6], c[7], fx);
+    const F3 y0 = mix3(x0, sub3(x1, x0), fy), y1 = mix3(x2, sub3(x3, x2), fy);
+    return mix3(y0, sub3(y1, y0), fz);
   }
   // Vec3l(p + 0.5), clamped into the grid (the reference clamps only near the
   // boundary, where its own points can leave it; elsewhere clamping changes nothing)
