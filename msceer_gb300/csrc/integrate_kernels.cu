@@ -484,9 +484,8 @@ struct Adv64 {
     anchor = cur;
     return n >= 2;
   }
-  // The FP32 advector's enter / trip in the reference's FP64 arithmetic.
-  __device__ __forceinline__ bool enter(const D3& cur, bool nearb, double bf[3], D3 c[8], D3& g, float& gm,
-                                        float& step) const {
+  // The voxel that holds `cur` and its eight corner gradients (as the FP32 advector's)
+  __device__ __forceinline__ void load_voxel(const D3& cur, bool nearb, double bf[3], D3 c[8]) const {
     int64_t b[3];
     if (nearb) {
       b[0] = (int64_t)clampd_ext(cur.x, V.X);
@@ -501,23 +500,37 @@ struct Adv64 {
     bf[0] = (double)b[0];
     bf[1] = (double)b[1];
     bf[2] = (double)b[2];
-    g = trilin(cur, bf, c);
-    gm = __double2float_rn(__dsqrt_rn(magsq(g)));
-    if (!(gm > 0.f) || !isfinite(gm)) return false;  // no direction to follow
-    step = __double2float_rn(__ddiv_rn(P.max_step, (double)gm));
-    return true;
   }
-  __device__ __forceinline__ int trip(D3& cur, D3& old, int& iters, bool nearb, const double bf[3], const D3 c[8],
-                                      D3& g, float& gm, float& step) const {
-    if (!(iters-- > 0)) return EV_OVER_MAX_ITERATIONS;
-    if (!(old.x == cur.x && old.y == cur.y && old.z == cur.z)) {
-      if ((int)cur.x != (int)old.x || (int)cur.y != (int)old.y || (int)cur.z != (int)old.z) return EV_OUT_OF_VOXEL;
-      g = trilin(cur, bf, c);
-      gm = __double2float_rn(__dsqrt_rn(magsq(g)));
-      if (!(gm > 0.f) || !isfinite(gm)) return EV_LOW_GRADIENT;
-      if ((double)__fmul_rn(gm, step) > P.max_step) step = __double2float_rn(__ddiv_rn(P.max_step, (double)gm));
-      old = cur;
+  // The FP32 advector's round (Adv32::advance: one uniform iteration for every stepping
+  // lane, the voxel entry folded in) in the reference's FP64 arithmetic.
+  __device__ __forceinline__ int advance(int& phase, int x, int y, int z, D3& cur, D3& old, int& iters, bool& nb,
+                                         double bf[3], D3 c[8], D3& g, float& gm, float& step,
+                                         unsigned long long& ntrips) const {
+    const bool ent = phase == kLaneEnter;
+    if (ent) {
+      nb = dist_to_boundary(V, x, y, z) <= 1;
+      load_voxel(cur, nb, bf, c);
+      phase = kLaneStep;
     }
+    const bool moved = !ent && !(old.x == cur.x && old.y == cur.y && old.z == cur.z);
+    const bool left = moved && ((int)cur.x != (int)old.x || (int)cur.y != (int)old.y || (int)cur.z != (int)old.z);
+    const D3 gc = trilin(cur, bf, c);
+    const float gmc = __double2float_rn(__dsqrt_rn(magsq(gc)));
+    const bool bad = !(gmc > 0.f) || !isfinite(gmc);  // no direction to follow
+    const bool counts = !(ent && bad);
+    ntrips += counts;
+    const bool spent = counts && !(iters > 0);
+    iters -= counts;
+    int ev = spent ? EV_OVER_MAX_ITERATIONS : EV_NONE;
+    if (ent && bad) ev = EV_LOW_GRADIENT;
+    if (!spent && left) ev = EV_OUT_OF_VOXEL;
+    if (!spent && !left && moved && bad) ev = EV_LOW_GRADIENT;
+    if (ev != EV_NONE) return ev;
+    const float sl = __double2float_rn(__ddiv_rn(P.max_step, (double)gmc));
+    if (ent || (double)__fmul_rn(gmc, step) > P.max_step) step = sl;
+    g = gc;
+    gm = gmc;
+    old = cur;
     if (gm < P.gthresh) return EV_LOW_GRADIENT;
     // full step: Vec3d * float multiplies in float (gi_vectors.h:250)
     const float sm = __fmul_rn((float)P.step_mult, step);
@@ -528,22 +541,19 @@ struct Adv64 {
     const D3 hg = trilin({da(cur.x, hd.x), da(cur.y, hd.y), da(cur.z, hd.z)}, bf, c);
     const D3 e2 = {da(dm(hg.x, hs), hd.x), da(dm(hg.y, hs), hd.y), da(dm(hg.z, hs), hd.z)};
     const D3 df = {ds(e2.x, e1.x), ds(e2.y, e1.y), ds(e2.z, e1.z)};
-    const float err = __double2float_rn(magsq(df));
-    if (err < P.ethresh) {
-      D3 np = {da(cur.x, e2.x), da(cur.y, e2.y), da(cur.z, e2.z)};
-      if (nearb) {
-        np.x = clampd_ext(np.x, V.X);
-        np.y = clampd_ext(np.y, V.Y);
-        np.z = clampd_ext(np.z, V.Z);
-      }
+    const bool acc = __double2float_rn(magsq(df)) < P.ethresh;
+    D3 np = {da(cur.x, e2.x), da(cur.y, e2.y), da(cur.z, e2.z)};
+    if (nb) {
+      np.x = clampd_ext(np.x, V.X);
+      np.y = clampd_ext(np.y, V.Y);
+      np.z = clampd_ext(np.z, V.Z);
+    }
+    const float grown = __double2float_rn(dm((double)step, 1.8));
+    step = acc ? (grown < sl ? grown : sl) : __double2float_rn(dm((double)step, 0.5));
+    if (acc) {
       cur = np;
-      const float a = __double2float_rn(dm((double)step, 1.8));
-      const float bb = __double2float_rn(__ddiv_rn(P.max_step, (double)gm));
-      step = a < bb ? a : bb;
-      const uint8_t st = state[nearest(cur, nearb)];
+      const uint8_t st = state[nearest(cur, nb)];
       if (st == kStSeed || st == kStTerminal) return EV_HIT_PREASSIGNED;
-    } else {
-      step = __double2float_rn(dm((double)step, 0.5));
     }
     return EV_NONE;
   }
@@ -630,19 +640,8 @@ __global__ void __launch_bounds__(32) fixup_kernel(const Adv64 A, int32_t* __res
       break;
     }
     for (int r = 0; r < K; r++) {
-      if (phase == kLaneEnter) {
-        nb = dist_to_boundary(V, x, y, z) <= 1;
-        if (A.enter(cur, nb, b, c, g, gm, step)) {
-          old = cur;
-          phase = kLaneStep;
-        } else {
-          A.nearest3(cur, x, y, z);
-          phase = kLaneEnd;
-        }
-      }
-      if (phase != kLaneStep) continue;
-      ntrips++;
-      const int ev = A.trip(cur, old, iters, nb, b, c, g, gm, step);
+      if (phase != kLaneEnter && phase != kLaneStep) continue;
+      const int ev = A.advance(phase, x, y, z, cur, old, iters, nb, b, c, g, gm, step, ntrips);
       if (ev == EV_NONE) continue;
       A.nearest3(cur, x, y, z);
       phase = ev == EV_OUT_OF_VOXEL ? kLaneEnter : kLaneEnd;
