@@ -920,7 +920,7 @@ __global__ void clean_resolve_kernel(const int32_t* __restrict__ lab, const VolD
 // Stepping iterations per turn of the lane-refilling loops: more amortise the turn's
 // hand-out and voxel-entry work, fewer leave less idle time after a lane's event.
 // MSC_TRIPS_PER_TURN (2, 4, 8 or 16) overrides the default for tuning (512^3 k^-3
-// labels: 1.82 / 1.40 / 1.31 / 1.27 s for 1 / 2 / 4 / 8).
+// labels: 0.48 / 0.46 / 0.45 s for 4 / 8 / 16, within the run-to-run spread of 8 and 16).
 int trips_per_turn() {
   static const int k = [] {
     const char* e = std::getenv("MSC_TRIPS_PER_TURN");
