@@ -21,6 +21,7 @@
 //   components' first vertices in the walk order; every component that does not hold
 //   its region's extremum joins the component of its first earlier neighbour from
 //   another region; chains resolve by pointer jumping.
+#include <cstdio>
 #include <cstdlib>
 
 #include "label_common.cuh"
@@ -920,13 +921,19 @@ __global__ void clean_resolve_kernel(const int32_t* __restrict__ lab, const VolD
 // Stepping iterations per turn of the lane-refilling loops: more amortise the turn's
 // hand-out and voxel-entry work, fewer leave less idle time after a lane's event.
 // MSC_TRIPS_PER_TURN (2, 4, 8 or 16) overrides the default for tuning (512^3 k^-3
-// labels: 0.48 / 0.46 / 0.45 s for 4 / 8 / 16, within the run-to-run spread of 8 and 16).
+// labels, both stages alike: 0.44 / 0.43 / 0.42 s for 4 / 8 / 16).
+// MSC_TRIPS_PER_TURN_PASS1 sets the first pass's apart from the fix-up's.
+static int trips_env(const char* name, int dflt) {
+  const char* e = std::getenv(name);
+  const int v = e ? std::atoi(e) : dflt;
+  return (v == 2 || v == 4 || v == 8 || v == 16) ? v : dflt;
+}
 int trips_per_turn() {
-  static const int k = [] {
-    const char* e = std::getenv("MSC_TRIPS_PER_TURN");
-    const int v = e ? std::atoi(e) : 8;
-    return (v == 2 || v == 4 || v == 16) ? v : 8;
-  }();
+  static const int k = trips_env("MSC_TRIPS_PER_TURN", 16);
+  return k;
+}
+static int trips_per_turn_pass1() {
+  static const int k = trips_env("MSC_TRIPS_PER_TURN_PASS1", trips_per_turn());
   return k;
 }
 
@@ -956,7 +963,7 @@ cudaError_t launch_integrate_pass1(const float4* G, const VolDims& V, const Inte
     ::msc::count_launch();
     compact_level_kernel<<<grid, 128, 0, stream>>>(S, g0, L1, lvl, stamp, items, n_items);
     ::msc::count_launch();
-    switch (trips_per_turn()) {
+    switch (trips_per_turn_pass1()) {
       case 16:
         integrate_level_kernel<16><<<grid, 128, 0, stream>>>(A, items, n_items, lab, lvl, w, trips);
         break;
@@ -969,6 +976,9 @@ cudaError_t launch_integrate_pass1(const float4* G, const VolDims& V, const Inte
       default:
         integrate_level_kernel<8><<<grid, 128, 0, stream>>>(A, items, n_items, lab, lvl, w, trips);
     }
+    char what[64];
+    std::snprintf(what, sizeof(what), "level %d-%d (%lld)", g0, L1 - 1, (long long)count);
+    ::msc::label_trace(stream, P.step_mult, what);
   }
   return cudaGetLastError();
 }

@@ -20,6 +20,9 @@ cudaError_t scratch_alloc(void** p, size_t bytes, cudaStream_t stream);
 void count_launch();
 void add_launches(long long n);
 long long launches_so_far();
+// Labeling phase trace (MSC_LABELS_TRACE=1; msc_labels_capi.cu): a timing event on
+// `st` at a phase boundary of direction `dir` (-1 ascending, 1 descending).
+void label_trace(cudaStream_t st, int dir, const char* what);
 
 enum : int {
   kErrNone = 0,

@@ -3,10 +3,15 @@
 // descending 3-manifold labels (ondemandaccurate.cxx:795-948).
 #include <cuda_runtime.h>
 
+#include <algorithm>
+#include <chrono>
 #include <climits>
 #include <cmath>
+#include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <condition_variable>
+#include <functional>
 #include <map>
 #include <mutex>
 #include <queue>
@@ -41,6 +46,57 @@ int fail(int code, const std::string& m) {
                   std::string(what) + ": " + cudaGetErrorString(e_));                                  \
   } while (0)
 
+// Phase trace (MSC_LABELS_TRACE=1): a timing event per phase boundary of each
+// direction, printed to stderr at the end of the call -- device time of each boundary
+// and host time of its enqueue, both from the call's first mark.
+struct TraceMark {
+  int dir;
+  std::string what;
+  cudaEvent_t ev;
+  std::chrono::steady_clock::time_point host;
+};
+std::mutex g_trace_mu;
+std::vector<TraceMark> g_trace;
+bool trace_on() {
+  static const bool on = [] {
+    const char* e = std::getenv("MSC_LABELS_TRACE");
+    return e && *e && *e != '0';
+  }();
+  return on;
+}
+void trace_mark(cudaStream_t st, int dir, const std::string& what) {
+  if (!trace_on()) return;
+  TraceMark m{dir, what, nullptr, std::chrono::steady_clock::now()};
+  if (cudaEventCreate(&m.ev) != cudaSuccess) return;
+  cudaEventRecord(m.ev, st);
+  std::lock_guard<std::mutex> lk(g_trace_mu);
+  g_trace.push_back(m);
+}
+void trace_dump() {
+  if (!trace_on()) return;
+  std::lock_guard<std::mutex> lk(g_trace_mu);
+  if (g_trace.empty()) return;
+  const cudaEvent_t e0 = g_trace.front().ev;
+  const auto h0 = g_trace.front().host;
+  for (const TraceMark& m : g_trace) {
+    float ms = -1.f;
+    cudaEventSynchronize(m.ev);
+    cudaEventElapsedTime(&ms, e0, m.ev);
+    const double hms = std::chrono::duration<double, std::milli>(m.host - h0).count();
+    std::fprintf(stderr, "[labels] %s %-24s device %9.3f ms  host %9.3f ms\n", m.dir < 0 ? "asc" : "dsc",
+                 m.what.c_str(), ms, hms);
+  }
+  // the first mark's event is every line's base: destroy the events only now
+  for (const TraceMark& m : g_trace) cudaEventDestroy(m.ev);
+  g_trace.clear();
+}
+
+}  // namespace
+
+void msc::label_trace(cudaStream_t st, int dir, const char* what) { trace_mark(st, dir, what); }
+
+namespace {
+
 int sm_count() {
   int dev = 0, n = 0;
   if (cudaGetDevice(&dev) != cudaSuccess) return 148;
@@ -63,6 +119,20 @@ __global__ void terminal_state_kernel(const int32_t* lab, uint8_t* state, int64_
 __global__ void snapshot_kernel(const int32_t* lab, int32_t* out, int64_t n) {
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
     out[i] = lab[i] == msc::kLabelNone ? -1 : lab[i];
+}
+// the extrema that the mergeable arcs touch, gathered for the host merge
+__global__ void gather_extrema_kernel(const int32_t* ids, int m, const int64_t* cells, const int64_t* hv,
+                                      const float* fval, int64_t* oc, int64_t* ohv, float* of) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < m; i += gridDim.x * blockDim.x) {
+    const int32_t e = ids[i];
+    oc[i] = cells[e];
+    ohv[i] = hv[e];
+    of[i] = fval[e];
+  }
+}
+// the host merge's changed representatives: rep[pairs[2k]] = pairs[2k + 1]
+__global__ void scatter_rep_kernel(const int32_t* pairs, int m, int32_t* rep) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < m; i += gridDim.x * blockDim.x) rep[pairs[2 * i]] = pairs[2 * i + 1];
 }
 // SetGradExplicit(seed, 0) (gi_numeric_integrator_path_compressing.h:118-123), both copies
 __global__ void zero_seed_grad_kernel(const int64_t* seed, int n, float4* g32, double* g64) {
@@ -198,6 +268,7 @@ struct LabelCtx {
 // One direction's labels between the phases.
 struct DirLabels {
   int dir = -1;
+  std::function<int()> on_seeds;  // called once the seeds are on the stream (prepare_direction)
   int64_t trips[3] = {0, 0, 0};  // advection iterations: first pass, FP32 fix-up, FP64 re-decisions
   int32_t* lab = nullptr;
   uint8_t* state = nullptr;
@@ -268,6 +339,7 @@ int prepare_direction(LabelCtx& c, DirLabels& d, int32_t* stage_terminal) {
   LCUDA(cudaStreamSynchronize(st), "sync");
   const int n_ext = h[0], n_sad = h[1];
   d.n_ext = n_ext;
+  trace_mark(st, dir, "critical cells");
   LCUDA(c.pool.get(&hv, n_ext + 1), "alloc");
   LCUDA(c.pool.get(&fval, n_ext + 1), "alloc");
   LCUDA(c.pool.get(&d.seed, n_ext + 1), "alloc");
@@ -280,24 +352,66 @@ int prepare_direction(LabelCtx& c, DirLabels& d, int32_t* stage_terminal) {
         "trace arcs");
   int n_arcs = 0;
   if (int rc = read_int(c.counters + 2, &n_arcs, st)) return rc;
+  trace_mark(st, dir, "arcs");
   if (n_ext > 0) {
     ::msc::count_launch();
     iota_kernel<<<(n_ext + 255) / 256, 256, 0, st>>>(rep, n_ext);
   }
   if (n_arcs > 0) {
-    // the few arcs that can merge: exact priority-queue simplification on the host
+    // the few arcs that can merge: exact priority-queue simplification on the host, over
+    // the extrema those arcs touch (the merge reads no other; a merge over all n_ext
+    // extrema copied ~10 M of them at 512^3 for a few hundred arcs)
     std::vector<msc::Arc> ha(n_arcs);
-    std::vector<int64_t> hcells(n_ext), hhv(n_ext);
-    std::vector<float> hf(n_ext);
     LCUDA(cudaMemcpyAsync(ha.data(), arcs, n_arcs * sizeof(msc::Arc), cudaMemcpyDeviceToHost, st), "read arcs");
-    LCUDA(cudaMemcpyAsync(hcells.data(), c.ext_cells, n_ext * sizeof(int64_t), cudaMemcpyDeviceToHost, st), "read");
-    LCUDA(cudaMemcpyAsync(hhv.data(), hv, n_ext * sizeof(int64_t), cudaMemcpyDeviceToHost, st), "read");
-    LCUDA(cudaMemcpyAsync(hf.data(), fval, n_ext * sizeof(float), cudaMemcpyDeviceToHost, st), "read");
+    LCUDA(cudaStreamSynchronize(st), "sync");
+    std::vector<int32_t> ids;
+    ids.reserve(2 * (size_t)n_arcs);
+    for (const msc::Arc& a : ha) {
+      if (a.e1 < 0 || a.e1 >= n_ext || a.e2 < 0 || a.e2 >= n_ext)
+        return fail(MSC_ERR_CUDA, "arc endpoint outside the extremum list");
+      ids.push_back(a.e1);
+      ids.push_back(a.e2);
+    }
+    std::sort(ids.begin(), ids.end());
+    ids.erase(std::unique(ids.begin(), ids.end()), ids.end());
+    const int m = (int)ids.size();
+    for (msc::Arc& a : ha) {
+      a.e1 = (int32_t)(std::lower_bound(ids.begin(), ids.end(), a.e1) - ids.begin());
+      a.e2 = (int32_t)(std::lower_bound(ids.begin(), ids.end(), a.e2) - ids.begin());
+    }
+    int32_t* dids;
+    int64_t *dcells, *dhv;
+    float* dfv;
+    LCUDA(c.pool.get(&dids, 2 * (size_t)m), "alloc");
+    LCUDA(c.pool.get(&dcells, m), "alloc");
+    LCUDA(c.pool.get(&dhv, m), "alloc");
+    LCUDA(c.pool.get(&dfv, m), "alloc");
+    LCUDA(cudaMemcpyAsync(dids, ids.data(), m * sizeof(int32_t), cudaMemcpyHostToDevice, st), "write ids");
+    ::msc::count_launch();
+    gather_extrema_kernel<<<(m + 255) / 256, 256, 0, st>>>(dids, m, c.ext_cells, hv, fval, dcells, dhv, dfv);
+    std::vector<int64_t> hcells(m), hhv(m);
+    std::vector<float> hf(m);
+    LCUDA(cudaMemcpyAsync(hcells.data(), dcells, m * sizeof(int64_t), cudaMemcpyDeviceToHost, st), "read");
+    LCUDA(cudaMemcpyAsync(hhv.data(), dhv, m * sizeof(int64_t), cudaMemcpyDeviceToHost, st), "read");
+    LCUDA(cudaMemcpyAsync(hf.data(), dfv, m * sizeof(float), cudaMemcpyDeviceToHost, st), "read");
     LCUDA(cudaStreamSynchronize(st), "sync");
     std::vector<int32_t> hrep;
     host_merge(dir, c.p->presimp_threshold, ha, hcells, hhv, hf, hrep);
-    LCUDA(cudaMemcpyAsync(rep, hrep.data(), n_ext * sizeof(int32_t), cudaMemcpyHostToDevice, st), "write rep");
-    LCUDA(cudaStreamSynchronize(st), "sync");
+    std::vector<int32_t> pairs;
+    for (int i = 0; i < m; i++)
+      if (hrep[i] != i) {
+        pairs.push_back(ids[i]);
+        pairs.push_back(ids[hrep[i]]);
+      }
+    const int np = (int)pairs.size() / 2;
+    if (np > 0) {
+      // dids holds 2m entries: room for the pairs
+      LCUDA(cudaMemcpyAsync(dids, pairs.data(), 2 * np * sizeof(int32_t), cudaMemcpyHostToDevice, st), "write rep");
+      ::msc::count_launch();
+      scatter_rep_kernel<<<(np + 255) / 256, 256, 0, st>>>(dids, np, rep);
+      LCUDA(cudaStreamSynchronize(st), "sync");
+    }
+    trace_mark(st, dir, "merge " + std::to_string(n_arcs) + " arcs, " + std::to_string(np) + " changed");
   }
   ::msc::count_launch();
   fill_i32_kernel<<<c.grid, 256, 0, st>>>(d.lab, N, -1);
@@ -305,6 +419,9 @@ int prepare_direction(LabelCtx& c, DirLabels& d, int32_t* stage_terminal) {
   fill_i32_kernel<<<(n_ext + 256) / 256, 256, 0, st>>>(name, n_ext + 1, INT_MAX);
   LCUDA(cudaMemsetAsync(d.state, 0, (size_t)N, st), "memset");
   LCUDA(msc::launch_group_seeds(rep, d.seed, n_ext, name, d.lab, d.state, c.sms, st), "seeds");
+  trace_mark(st, dir, "seeds");
+  if (d.on_seeds)
+    if (int rc = d.on_seeds()) return rc;
 
   // certain terminal regions: tile passes to the fixpoint
   const uint8_t* din = nullptr;
@@ -316,7 +433,10 @@ int prepare_direction(LabelCtx& c, DirLabels& d, int32_t* stage_terminal) {
           "regions");
     int changed = 0;
     if (int rc = read_int(c.counters + 3, &changed, st)) return rc;
-    if (!changed) break;
+    if (!changed) {
+      trace_mark(st, dir, "terminal x" + std::to_string(passes + 1));
+      break;
+    }
     if (passes > c.ntiles + 2) return fail(MSC_ERR_ITER_LIMIT, "terminal regions did not converge");
     din = dout;
     dout = (dout == c.tiles) ? c.tiles + c.ntiles : c.tiles;
@@ -373,9 +493,11 @@ int first_pass(LabelCtx& c, DirLabels& d) {
   LCUDA(c.pool.get(&lvl, N), "alloc");
   LCUDA(cudaMemsetAsync(c.work + 48, 0, 3 * sizeof(unsigned long long), st), "memset");
   // the fix-up's list buffer (N int64) holds a level's vertices (at most N) meanwhile
+  trace_mark(st, d.dir, "pass1 start");
   LCUDA(msc::launch_integrate_pass1(c.g32, c.V, P, S, d.lab, lvl, c.work, c.work + 48,
                                     reinterpret_cast<int32_t*>(c.list_a), c.work + 52, c.sms, st),
         "integrate");
+  trace_mark(st, d.dir, "pass1");
   return MSC_OK;
 }
 
@@ -405,6 +527,7 @@ int finish_direction(LabelCtx& c, DirLabels& d, int32_t* out, int32_t* stage_int
   LCUDA(msc::launch_boundary_set(d.lab, d.state, V, c.list_a, c.counters + 5, c.queued, sms, st), "boundary set");
   int n_list = 0;
   if (int rc = read_int(c.counters + 5, &n_list, st)) return rc;
+  trace_mark(st, d.dir, "boundary " + std::to_string(n_list));
   if (p->precision == 3) n_list = 0;  // first pass only
   int64_t* cur = c.list_a;
   int64_t* nxt = c.list_b;
@@ -436,6 +559,7 @@ int finish_direction(LabelCtx& c, DirLabels& d, int32_t* out, int32_t* stage_int
     n_list = h[0];
     n_amb = h[1];
     std::swap(cur, nxt);
+    trace_mark(st, d.dir, "wave " + std::to_string(waves) + " next " + std::to_string(n_list));
   }
   {
     unsigned long long h[3];
@@ -454,6 +578,7 @@ int finish_direction(LabelCtx& c, DirLabels& d, int32_t* out, int32_t* stage_int
   LCUDA(c.pool.get(&parent, N), "alloc");
   LCUDA(c.pool.get(&target, N), "alloc");
   LCUDA(msc::launch_clean(d.lab, c.f, V, d.dir, parent, target, out, sms, st), "clean");
+  trace_mark(st, d.dir, "clean");
   return MSC_OK;
 }
 
@@ -524,8 +649,10 @@ void run_dsc_job(int dev, cudaEvent_t inputs_ready, const float* f, const uint8_
     LCUDA(cudaStreamWaitEvent(sb, inputs_ready, 0), "cudaStreamWaitEvent");
     int rc = MSC_OK;
     {
+      trace_mark(sb, 1, "start");
       LabelCtx c(sb);
       if ((rc = setup_ctx(c, f, grad, dims, p))) return rc;
+      trace_mark(sb, 1, "setup");
       DirLabels d;
       d.dir = 1;
       if ((rc = prepare_direction(c, d, stages ? stages + 2 * c.N : nullptr))) return rc;
@@ -539,6 +666,7 @@ void run_dsc_job(int dev, cudaEvent_t inputs_ready, const float* f, const uint8_
         ::msc::count_launch();
         zero_seed_grad_kernel<<<(asc->n + 255) / 256, 256, 0, sb>>>(asc->seed, asc->n, c.g32, c.g64);
       }
+      trace_mark(sb, 1, "asc seeds zeroed");
       if ((rc = direction_rest(c, d, 1, tp, out, stages ? stages + 3 * c.N : nullptr, job->stats, job->counts)))
         return rc;
       for (int k = 0; k < 3; k++) job->trips[k] = d.trips[k];
@@ -568,7 +696,9 @@ int labels_impl(const float* f, const uint8_t* grad, const int64_t* dims, const 
       return rc;
     for (int k = 0; k < 3; k++) t_trips[3 * pass + k] = d.trips[k];
   }
-  return finish_errors(c);
+  const int rc = finish_errors(c);
+  trace_dump();
+  return rc;
 }
 
 // Both directions: the ascending one on the caller's stream and thread, the
@@ -602,23 +732,30 @@ int labels_concurrent(const float* f, const uint8_t* grad, const int64_t* dims, 
   int rc = MSC_OK;
   int64_t counts[3] = {0, 0, 0};
   {
+    trace_mark(st, -1, "start");
     LabelCtx c(st);
     DirLabels d;
     d.dir = -1;
+    // the minima' seeds go to run_dsc_job (which zeroes them in its gradient copy) as
+    // soon as they exist, before this direction's terminal regions
+    bool published = false;
+    d.on_seeds = [&]() -> int {
+      LCUDA(cudaEventRecord(seeds_done, st), "cudaEventRecord");
+      handoff.publish(d.seed, d.n_ext, seeds_done);
+      published = true;
+      return MSC_OK;
+    };
     rc = setup_ctx(c, f, grad, dims, p);
+    trace_mark(st, -1, "setup");
     if (rc == MSC_OK) rc = prepare_direction(c, d, stages);
-    if (rc == MSC_OK) {
-      // the minima' seeds: run_dsc_job zeroes them in its gradient copy
-      const cudaError_t e = cudaEventRecord(seeds_done, st);
-      if (e != cudaSuccess) rc = fail(MSC_ERR_CUDA, std::string("cudaEventRecord: ") + cudaGetErrorString(e));
-    }
-    handoff.publish(d.seed, rc == MSC_OK ? d.n_ext : -1, seeds_done);
+    if (!published) handoff.publish(nullptr, -1, nullptr);
     if (rc == MSC_OK) rc = direction_rest(c, d, 0, tp, out_asc, stages ? stages + c.N : nullptr, t_stats, counts);
     for (int k = 0; k < 3; k++) t_trips[k] = d.trips[k];
     if (rc == MSC_OK) rc = finish_errors(c);
     // the descending job reads d.seed from this context's pool: wait for it first
     worker.join();
   }
+  trace_dump();
   if (rc != MSC_OK) return rc;
   if (job.rc != MSC_OK) return fail(job.rc, job.err);
   t_stats[2] = job.stats[0];

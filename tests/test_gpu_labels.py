@@ -98,3 +98,28 @@ def test_two_direction_call_matches_single_direction_ascending(gpu):
     both = integrated_labels(t, g, 1e-4, None, 4000, 0.25, 0.0)
     asc = integrated_labels(t, g, 1e-4, None, 4000, 0.25, 0.0, descending=False)
     assert torch.equal(both["asc"], asc["asc"])
+
+
+@pytest.mark.parametrize("name", ["gauss40", "k3_32"])
+def test_labels_with_merge_threshold_vs_oracle(gpu, oracle, name):
+    """A positive presimplification threshold merges extrema along the arcs whose
+    persistence is below it (the host priority-queue merge over the extrema those arcs
+    touch): the terminal regions stay exactly the oracle's."""
+    import torch
+    from msceer_gb300 import integrated_labels, lower_star_grad
+    f = FIELDS[name]()
+    thr = float(0.01 * (f.max() - f.min()))
+    gt = 1e-6 * float(np.abs(f).max())
+    t = torch.from_numpy(f).to(gpu)
+    g = lower_star_grad(t)
+    got = integrated_labels(t, g, 1e-4, gt, 4000, 0.25, thr, stages=True)
+    got.pop("stats")
+    got = {k: v.cpu().numpy() for k, v in got.items()}
+    want = oracle.labels(f, g.cpu().numpy(), 1e-4, gt, 4000, 0.25, thr)
+    plain = oracle.labels(f, g.cpu().numpy(), 1e-4, gt, 4000, 0.25, 0.0)
+    # the threshold merged regions: fewer distinct terminal labels than without it
+    assert len(np.unique(want["asc_terminal"])) < len(np.unique(plain["asc_terminal"]))
+    for k in ("asc_terminal", "dsc_terminal"):
+        assert (got[k] == want[k]).all(), (k, float((got[k] != want[k]).mean()))
+    for k in ("asc", "dsc"):
+        assert float((got[k] != want[k]).mean()) <= TOL_FINAL
