@@ -18,6 +18,7 @@
 // Regions are named by their smallest seed vertex (the extremum's vertex when nothing
 // merged); -1 = outside every region.  The reference numbers regions in unordered_map
 // order, so only the partition is comparable.
+#include <cstdlib>
 #include "label_common.cuh"
 
 namespace msc {
@@ -366,22 +367,46 @@ __global__ void __launch_bounds__(BS) terminal_pass_kernel(const float* __restri
     }
     for (int k = tid; k < QCAP; k += BS) sq[k] = kQueueEmpty;
     __syncthreads();
-    for (int row = warp; row < B::LY * B::LZ; row += NWARPS) {
-      const int ly = row % B::LY, lz = row / B::LY;
-      const bool rin = ly >= W.lmin[1] && ly < W.lmax[1] && lz >= W.lmin[2] && lz < W.lmax[2];
-      const int64_t rbase = W.o[0] + V.X * (W.o[1] + ly) + V.X * V.Y * (W.o[2] + lz);
-      const bool row_halo = ly < B::H || ly >= B::H + TY || lz < B::H || lz >= B::H + TZ;
-      for (int lx = lane; lx < B::LX; lx += 32) {
-        const int i = lx + B::LX * row;
-        const bool in = rin && lx >= W.lmin[0] && lx < W.lmax[0];
-        const float fv = in ? f[rbase + lx] : 0.f;
-        const int32_t l = in ? lab[rbase + lx] : -1;
-        sf[i] = fv;
-        sl[i] = l;
-        if (l < 0) continue;
-        if (!first && !(row_halo || lx < B::H || lx >= B::H + TX)) continue;
-        atomicOr(&s_vis[i >> 5], 1u << (i & 31));
-        sq[atomicAdd(&s_qtail, 1)] = (uint16_t)i;
+    // the box's rows in batches of kRowBatch per warp: every load of a batch is issued
+    // before the first store, so a thread keeps 2 * kRowBatch * XI loads in flight
+    // instead of waiting for one row's before it asks for the next
+    constexpr int NROWS = B::LY * B::LZ, XI = (B::LX + 31) / 32, kRowBatch = 4;
+    for (int r0 = warp; r0 < NROWS; r0 += NWARPS * kRowBatch) {
+      float fv[kRowBatch][XI];
+      int32_t lv[kRowBatch][XI];
+#pragma unroll
+      for (int u = 0; u < kRowBatch; u++) {
+        const int row = r0 + u * NWARPS;
+        const int ly = row % B::LY, lz = row / B::LY;
+        const bool rin = row < NROWS && ly >= W.lmin[1] && ly < W.lmax[1] && lz >= W.lmin[2] && lz < W.lmax[2];
+        const int64_t rbase = W.o[0] + V.X * (W.o[1] + ly) + V.X * V.Y * (W.o[2] + lz);
+#pragma unroll
+        for (int q = 0; q < XI; q++) {
+          const int lx = lane + 32 * q;
+          const bool in = rin && lx < B::LX && lx >= W.lmin[0] && lx < W.lmax[0];
+          fv[u][q] = in ? f[rbase + lx] : 0.f;
+          lv[u][q] = in ? lab[rbase + lx] : -1;
+        }
+      }
+#pragma unroll
+      for (int u = 0; u < kRowBatch; u++) {
+        const int row = r0 + u * NWARPS;
+        if (row >= NROWS) break;  // (warp-uniform)
+        const int ly = row % B::LY, lz = row / B::LY;
+        const bool row_halo = ly < B::H || ly >= B::H + TY || lz < B::H || lz >= B::H + TZ;
+#pragma unroll
+        for (int q = 0; q < XI; q++) {
+          const int lx = lane + 32 * q;
+          if (lx >= B::LX) continue;
+          const int i = lx + B::LX * row;
+          const int32_t l = lv[u][q];
+          sf[i] = fv[u][q];
+          sl[i] = l;
+          if (l < 0) continue;
+          if (!first && !(row_halo || lx < B::H || lx >= B::H + TX)) continue;
+          atomicOr(&s_vis[i >> 5], 1u << (i & 31));
+          sq[atomicAdd(&s_qtail, 1)] = (uint16_t)i;
+        }
       }
     }
     __syncthreads();
@@ -444,7 +469,7 @@ __global__ void __launch_bounds__(BS) terminal_pass_kernel(const float* __restri
 }
 
 namespace {
-constexpr int kVTX = 32, kVTY = 16, kVTZ = 8, kVBS = 256;
+constexpr int kVTX = 32, kVTY = 16, kVTZ = 8, kVBS = 512;
 using VB = VBox<kVTX, kVTY, kVTZ>;
 }  // namespace
 
@@ -458,12 +483,17 @@ cudaError_t launch_terminal_pass(const float* f, int32_t* lab, const VolDims& V,
   const int64_t cap = (int64_t)num_sms * 2;
   const int grid = (int)(nt < cap ? nt : cap);
   if (grid <= 0) return cudaSuccess;
-  auto k = terminal_pass_kernel<kVTX, kVTY, kVTZ, kVBS>;
-  const size_t sm = VB::smem_bytes() + (size_t)kVBS * 2 + 16;
+  // walkers per tile: MSC_TERMINAL_THREADS (256 or 512) overrides the default for tuning
+  static const int bs = [] {
+    const char* e = std::getenv("MSC_TERMINAL_THREADS");
+    return (e && std::atoi(e) == 256) ? 256 : kVBS;
+  }();
+  auto k = bs == 256 ? terminal_pass_kernel<kVTX, kVTY, kVTZ, 256> : terminal_pass_kernel<kVTX, kVTY, kVTZ, kVBS>;
+  const size_t sm = VB::smem_bytes() + (size_t)bs * 2 + 16;
   cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
   if (e != cudaSuccess) return e;
   ::msc::count_launch();
-  k<<<grid, kVBS, sm, stream>>>(f, lab, V, dir, dirty_in, dirty_out, changed, err);
+  k<<<grid, bs, sm, stream>>>(f, lab, V, dir, dirty_in, dirty_out, changed, err);
   return cudaGetLastError();
 }
 
