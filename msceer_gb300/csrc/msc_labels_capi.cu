@@ -238,10 +238,29 @@ struct Pool {
   }
 };
 
-int read_int(const int* d, int* h, cudaStream_t st) {
-  LCUDA(cudaMemcpyAsync(h, d, sizeof(int), cudaMemcpyDeviceToHost, st), "read counter");
-  LCUDA(cudaStreamSynchronize(st), "cudaStreamSynchronize");
-  return MSC_OK;
+// Pinned host words for the counter reads that steer the host loop.  A copy into
+// pageable memory held up the other direction's host thread in its CUDA calls until the
+// copy (and so the kernel before it) had finished; a pinned one does not.  The buffers
+// are reused across calls and never freed (freeing pinned memory synchronises).
+constexpr size_t kPinnedBytes = 256;
+std::mutex g_pin_mu;
+std::vector<void*> g_pin_free;
+void* pinned_get() {
+  {
+    std::lock_guard<std::mutex> lk(g_pin_mu);
+    if (!g_pin_free.empty()) {
+      void* p = g_pin_free.back();
+      g_pin_free.pop_back();
+      return p;
+    }
+  }
+  void* p = nullptr;
+  return cudaMallocHost(&p, kPinnedBytes) == cudaSuccess ? p : nullptr;
+}
+void pinned_put(void* p) {
+  if (!p) return;
+  std::lock_guard<std::mutex> lk(g_pin_mu);
+  g_pin_free.push_back(p);
 }
 
 // Shared state of one labeling call.
@@ -262,13 +281,32 @@ struct LabelCtx {
   uint8_t* tiles = nullptr;
   int* counters = nullptr;  // [0] n_ext [1] n_sad [2] n_arcs [3] changed [4] err [5] n_list [6] n_next [7] n_amb
   unsigned long long* work = nullptr;  // [0, 48) claimed work items, [48, 51) advection iterations
+  void* hpin = nullptr;                // kPinnedBytes of pinned host memory (pinned_get)
   explicit LabelCtx(cudaStream_t s) : st(s), pool(s) {}
+  ~LabelCtx() {
+    cudaStreamSynchronize(st);  // no copy into hpin in flight
+    pinned_put(hpin);
+  }
+  LabelCtx(const LabelCtx&) = delete;
+  LabelCtx& operator=(const LabelCtx&) = delete;
 };
+
+// n values of device memory, read through the context's pinned words
+template <class T>
+int read_dev(LabelCtx& c, const T* d, int n, T* out) {
+  static_assert(sizeof(T) <= 8, "counters");
+  if ((size_t)n * sizeof(T) > kPinnedBytes) return fail(MSC_ERR_CUDA, "counter read too large");
+  LCUDA(cudaMemcpyAsync(c.hpin, d, n * sizeof(T), cudaMemcpyDeviceToHost, c.st), "read counters");
+  LCUDA(cudaStreamSynchronize(c.st), "cudaStreamSynchronize");
+  std::memcpy(out, c.hpin, n * sizeof(T));
+  return MSC_OK;
+}
 
 // One direction's labels between the phases.
 struct DirLabels {
   int dir = -1;
-  std::function<int()> on_seeds;  // called once the seeds are on the stream (prepare_direction)
+  std::function<int()> on_seeds;         // called once the seeds are on the stream (prepare_direction)
+  std::function<int()> before_terminal;  // called before the terminal-region walk (prepare_direction)
   int64_t trips[3] = {0, 0, 0};  // advection iterations: first pass, FP32 fix-up, FP64 re-decisions
   int32_t* lab = nullptr;
   uint8_t* state = nullptr;
@@ -289,6 +327,7 @@ int setup_ctx(LabelCtx& c, const float* f, const uint8_t* grad, const int64_t* d
   c.f = f;
   c.grad = grad;
   c.p = p;
+  if (!c.hpin && !(c.hpin = pinned_get())) return fail(MSC_ERR_OOM, "pinned host words");
   c.sms = sm_count();
   c.grid = c.sms * 8;
   c.ntiles = msc::terminal_num_tiles(c.V);
@@ -335,8 +374,7 @@ int prepare_direction(LabelCtx& c, DirLabels& d, int32_t* stage_terminal) {
   LCUDA(msc::launch_find_critical(c.grad, V, dir, c.key, c.ext_cells, c.counters, c.saddles, c.counters + 1, c.sms, st),
         "critical");
   int h[2];
-  LCUDA(cudaMemcpyAsync(h, c.counters, 2 * sizeof(int), cudaMemcpyDeviceToHost, st), "read");
-  LCUDA(cudaStreamSynchronize(st), "sync");
+  if (int rc = read_dev(c, c.counters, 2, h)) return rc;
   const int n_ext = h[0], n_sad = h[1];
   d.n_ext = n_ext;
   trace_mark(st, dir, "critical cells");
@@ -351,7 +389,7 @@ int prepare_direction(LabelCtx& c, DirLabels& d, int32_t* stage_terminal) {
                                c.counters + 2, c.counters + 4, c.sms, st),
         "trace arcs");
   int n_arcs = 0;
-  if (int rc = read_int(c.counters + 2, &n_arcs, st)) return rc;
+  if (int rc = read_dev(c, c.counters + 2, 1, &n_arcs)) return rc;
   trace_mark(st, dir, "arcs");
   if (n_ext > 0) {
     ::msc::count_launch();
@@ -423,6 +461,8 @@ int prepare_direction(LabelCtx& c, DirLabels& d, int32_t* stage_terminal) {
   if (d.on_seeds)
     if (int rc = d.on_seeds()) return rc;
 
+  if (d.before_terminal)
+    if (int rc = d.before_terminal()) return rc;
   // certain terminal regions: tile passes to the fixpoint
   const uint8_t* din = nullptr;
   uint8_t* dout = c.tiles;
@@ -432,7 +472,7 @@ int prepare_direction(LabelCtx& c, DirLabels& d, int32_t* stage_terminal) {
     LCUDA(msc::launch_terminal_pass(c.f, d.lab, V, dir, din, dout, c.counters + 3, c.counters + 4, c.sms, st),
           "regions");
     int changed = 0;
-    if (int rc = read_int(c.counters + 3, &changed, st)) return rc;
+    if (int rc = read_dev(c, c.counters + 3, 1, &changed)) return rc;
     if (!changed) {
       trace_mark(st, dir, "terminal x" + std::to_string(passes + 1));
       break;
@@ -526,7 +566,7 @@ int finish_direction(LabelCtx& c, DirLabels& d, int32_t* out, int32_t* stage_int
   LCUDA(cudaMemsetAsync(c.counters + 5, 0, 3 * sizeof(int), st), "memset");
   LCUDA(msc::launch_boundary_set(d.lab, d.state, V, c.list_a, c.counters + 5, c.queued, sms, st), "boundary set");
   int n_list = 0;
-  if (int rc = read_int(c.counters + 5, &n_list, st)) return rc;
+  if (int rc = read_dev(c, c.counters + 5, 1, &n_list)) return rc;
   trace_mark(st, d.dir, "boundary " + std::to_string(n_list));
   if (p->precision == 3) n_list = 0;  // first pass only
   int64_t* cur = c.list_a;
@@ -554,8 +594,7 @@ int finish_direction(LabelCtx& c, DirLabels& d, int32_t* out, int32_t* stage_int
       LCUDA(cudaMemsetAsync(c.counters + 7, 0, sizeof(int), st), "memset");
     }
     int h[2];  // next wave's length, ambiguous streamlines waiting
-    LCUDA(cudaMemcpyAsync(h, c.counters + 6, sizeof(h), cudaMemcpyDeviceToHost, st), "read counters");
-    LCUDA(cudaStreamSynchronize(st), "cudaStreamSynchronize");
+    if (int rc = read_dev(c, c.counters + 6, 2, h)) return rc;
     n_list = h[0];
     n_amb = h[1];
     std::swap(cur, nxt);
@@ -563,8 +602,7 @@ int finish_direction(LabelCtx& c, DirLabels& d, int32_t* out, int32_t* stage_int
   }
   {
     unsigned long long h[3];
-    LCUDA(cudaMemcpyAsync(h, c.work + 48, sizeof(h), cudaMemcpyDeviceToHost, st), "read iterations");
-    LCUDA(cudaStreamSynchronize(st), "cudaStreamSynchronize");
+    if (int rc = read_dev(c, c.work + 48, 3, h)) return rc;
     for (int k = 0; k < 3; k++) d.trips[k] = (int64_t)h[k];
   }
   if (stage_integrated) {
@@ -589,7 +627,7 @@ int integrate_direction(LabelCtx& c, DirLabels& d, int32_t* out, int32_t* stage_
 
 int finish_errors(LabelCtx& c) {
   int err = 0;
-  if (int rc = read_int(c.counters + 4, &err, c.st)) return rc;
+  if (int rc = read_dev(c, c.counters + 4, 1, &err)) return rc;
   if (err & msc::kErrLocalQueue) return fail(MSC_ERR_QUEUE_OVERFLOW, "tile queue overflow");
   if (err & msc::kErrIterLimit) return fail(MSC_ERR_ITER_LIMIT, "V-path walk exceeded its bound (invalid gradient?)");
   return MSC_OK;
@@ -655,18 +693,24 @@ void run_dsc_job(int dev, cudaEvent_t inputs_ready, const float* f, const uint8_
       trace_mark(sb, 1, "setup");
       DirLabels d;
       d.dir = 1;
+      // the ascending job's seeds before this direction's terminal-region walk: the walk
+      // holds most of every SM's shared memory, and the ascending merge's small kernels
+      // launched beside it waited for it to end
+      d.before_terminal = [&]() -> int {
+        {
+          std::unique_lock<std::mutex> lk(asc->mu);
+          asc->cv.wait(lk, [&] { return asc->ready; });
+        }
+        if (asc->n < 0) return fail(MSC_ERR_CUDA, "ascending labels failed");
+        if (asc->n > 0) {
+          LCUDA(cudaStreamWaitEvent(sb, asc->done, 0), "cudaStreamWaitEvent");
+          ::msc::count_launch();
+          zero_seed_grad_kernel<<<(asc->n + 255) / 256, 256, 0, sb>>>(asc->seed, asc->n, c.g32, c.g64);
+        }
+        trace_mark(sb, 1, "asc seeds zeroed");
+        return MSC_OK;
+      };
       if ((rc = prepare_direction(c, d, stages ? stages + 2 * c.N : nullptr))) return rc;
-      {
-        std::unique_lock<std::mutex> lk(asc->mu);
-        asc->cv.wait(lk, [&] { return asc->ready; });
-      }
-      if (asc->n < 0) return fail(MSC_ERR_CUDA, "ascending labels failed");
-      if (asc->n > 0) {
-        LCUDA(cudaStreamWaitEvent(sb, asc->done, 0), "cudaStreamWaitEvent");
-        ::msc::count_launch();
-        zero_seed_grad_kernel<<<(asc->n + 255) / 256, 256, 0, sb>>>(asc->seed, asc->n, c.g32, c.g64);
-      }
-      trace_mark(sb, 1, "asc seeds zeroed");
       if ((rc = direction_rest(c, d, 1, tp, out, stages ? stages + 3 * c.N : nullptr, job->stats, job->counts)))
         return rc;
       for (int k = 0; k < 3; k++) job->trips[k] = d.trips[k];
@@ -843,8 +887,7 @@ int direction_rest(LabelCtx& c, DirLabels& d, int k, const msc_triage_params* tp
   if (int rc = finish_direction(c, d, out, nullptr, fix)) return rc;
   LCUDA(msc::launch_audit_count(d.lab, first, flags, N, counts + 2, c.sms, st), "audit");
   unsigned long long h[3];
-  LCUDA(cudaMemcpyAsync(h, counts, sizeof(h), cudaMemcpyDeviceToHost, st), "read counts");
-  LCUDA(cudaStreamSynchronize(st), "sync");
+  if (int rc = read_dev(c, counts, 3, h)) return rc;
   for (int q = 0; q < 3; q++) counts_out[q] = (int64_t)h[q];
   return MSC_OK;
 }
