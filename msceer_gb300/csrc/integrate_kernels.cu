@@ -1003,8 +1003,24 @@ cudaError_t launch_fixup(const double* G, const VolDims& V, const IntegParams& P
   // instruction in full however few lanes are active -- so a small wave is spread over
   // as many SMs as it has warps, and a large one keeps a few items per lane (512^3
   // labels: 1.10 s with 16 CTAs of 128 per SM, 1.07 s with one)
-  fixup_kernel<2><<<blocks < num_sms * 4 ? blocks : num_sms * 4, 32, 0, stream>>>(
-      A, lab, lab0, state, list, n, next, n_next, queued, work, trips);
+  // iterations per turn: MSC_TRIPS_PER_TURN_FP64 (2, 4, 8 or 16) overrides the default
+  // (512^3 k^-3 labels: the same time for 2, 8 and 16 -- the FP64 waves are as long as
+  // their slowest streamline, not bound by the hand-out)
+  static const int k = trips_env("MSC_TRIPS_PER_TURN_FP64", 2);
+  const int grid = blocks < num_sms * 4 ? blocks : num_sms * 4;
+  switch (k) {
+    case 4:
+      fixup_kernel<4><<<grid, 32, 0, stream>>>(A, lab, lab0, state, list, n, next, n_next, queued, work, trips);
+      break;
+    case 16:
+      fixup_kernel<16><<<grid, 32, 0, stream>>>(A, lab, lab0, state, list, n, next, n_next, queued, work, trips);
+      break;
+    case 8:
+      fixup_kernel<8><<<grid, 32, 0, stream>>>(A, lab, lab0, state, list, n, next, n_next, queued, work, trips);
+      break;
+    default:
+      fixup_kernel<2><<<grid, 32, 0, stream>>>(A, lab, lab0, state, list, n, next, n_next, queued, work, trips);
+  }
   return cudaGetLastError();
 }
 

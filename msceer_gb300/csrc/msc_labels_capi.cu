@@ -277,10 +277,13 @@ struct LabelCtx {
   double* g64 = nullptr;
   int32_t* key = nullptr;
   int64_t *ext_cells = nullptr, *saddles = nullptr, *list_a = nullptr, *list_b = nullptr, *amb = nullptr;
+  int64_t *list_c = nullptr, *amb2 = nullptr;  // the FP64 re-decisions' reopened vertices; second ambiguous list
   uint32_t* queued = nullptr;
   uint8_t* tiles = nullptr;
   int* counters = nullptr;  // [0] n_ext [1] n_sad [2] n_arcs [3] changed [4] err [5] n_list [6] n_next [7] n_amb
-  unsigned long long* work = nullptr;  // [0, 48) claimed work items, [48, 51) advection iterations
+                            // [8] FP64 reopened
+  unsigned long long* work = nullptr;  // [0, 48) claimed work items, [48, 51) advection iterations,
+                                       // [52] level items, [56] FP64 claims
   void* hpin = nullptr;                // kPinnedBytes of pinned host memory (pinned_get)
   explicit LabelCtx(cudaStream_t s) : st(s), pool(s) {}
   ~LabelCtx() {
@@ -340,11 +343,13 @@ int setup_ctx(LabelCtx& c, const float* f, const uint8_t* grad, const int64_t* d
   LCUDA(c.pool.get(&c.list_a, N), "alloc");
   LCUDA(c.pool.get(&c.list_b, N), "alloc");
   LCUDA(c.pool.get(&c.amb, N), "alloc");
+  LCUDA(c.pool.get(&c.amb2, N), "alloc");
+  LCUDA(c.pool.get(&c.list_c, N), "alloc");
   LCUDA(c.pool.get(&c.queued, N / 32 + 1), "alloc");
   LCUDA(c.pool.get(&c.tiles, 2 * c.ntiles), "alloc");
-  LCUDA(c.pool.get(&c.counters, 8), "alloc");
+  LCUDA(c.pool.get(&c.counters, 16), "alloc");
   LCUDA(c.pool.get(&c.work, 64), "alloc");
-  LCUDA(cudaMemsetAsync(c.counters, 0, 8 * sizeof(int), c.st), "memset");
+  LCUDA(cudaMemsetAsync(c.counters, 0, 16 * sizeof(int), c.st), "memset");
   msc::GradDims GD{};
   for (int a = 0; a < 3; a++) {
     GD.v[a] = dims[a];
@@ -573,32 +578,88 @@ int finish_direction(LabelCtx& c, DirLabels& d, int32_t* out, int32_t* stage_int
   int64_t* nxt = c.list_b;
   stats[0] = stats[1] = 0;
   int n_amb = 0;  // ambiguous streamlines waiting for FP64 (counters[7] on the device)
-  for (int64_t waves = 0; n_list > 0 || n_amb > 0; waves++) {
-    if (waves > 2 * N + 2) return fail(MSC_ERR_ITER_LIMIT, "fix-up did not converge");
-    LCUDA(cudaMemsetAsync(c.counters + 6, 0, sizeof(int), st), "memset");
-    if (p->precision == 1) {
+  if (p->precision == 1) {
+    // all re-decisions in FP64, wave by wave
+    for (int64_t waves = 0; n_list > 0; waves++) {
+      if (waves > 2 * N + 2) return fail(MSC_ERR_ITER_LIMIT, "fix-up did not converge");
+      LCUDA(cudaMemsetAsync(c.counters + 6, 0, sizeof(int), st), "memset");
       LCUDA(msc::launch_fixup(c.g64, V, P, d.lab, lab0, d.state, cur, n_list, nxt, c.counters + 6, c.queued, c.work,
                               c.work + 50, sms, st),
             "fix-up");
       stats[0] += n_list;
-    } else if (n_list > 0) {
-      LCUDA(msc::launch_fixup32(c.g32, V, P, d.lab, lab0, d.state, cur, n_list, nxt, c.counters + 6, c.queued, c.amb,
-                                c.counters + 7, p->precision == 2 ? 2 : 0, c.work, c.work + 49, sms, st),
-            "fix-up");
-      stats[0] += n_list;
-    } else {
-      stats[1] += n_amb;
-      LCUDA(msc::launch_fixup(c.g64, V, P, d.lab, lab0, d.state, c.amb, n_amb, nxt, c.counters + 6, c.queued, c.work,
-                              c.work + 50, sms, st),
-            "fix-up");
-      LCUDA(cudaMemsetAsync(c.counters + 7, 0, sizeof(int), st), "memset");
+      if (int rc = read_dev(c, c.counters + 6, 1, &n_list)) return rc;
+      std::swap(cur, nxt);
+      trace_mark(st, d.dir, "wave " + std::to_string(waves) + " next " + std::to_string(n_list));
     }
-    int h[2];  // next wave's length, ambiguous streamlines waiting
-    if (int rc = read_dev(c, c.counters + 6, 2, h)) return rc;
-    n_list = h[0];
-    n_amb = h[1];
-    std::swap(cur, nxt);
-    trace_mark(st, d.dir, "wave " + std::to_string(waves) + " next " + std::to_string(n_list));
+  } else {
+    // FP32 waves on `st`; the ambiguous streamlines they collect go through FP64 on a
+    // second stream while the FP32 waves go on (a FP64 wave is as long as its slowest
+    // streamline, ~15 ms at 512^3, and mostly leaves the GPU idle).  The two never share
+    // a list: the FP64 wave reads the ambiguous list the FP32 waves stopped filling
+    // (amb_run), writes the vertices it reopens to list_c, and claims with work[56];
+    // those vertices join the FP32 list when it runs dry.  Decisions read lab0 only and a
+    // vertex's queued bit keeps it in one list at a time, so the closure is the same.
+    cudaStream_t s64 = nullptr;
+    cudaEvent_t ev_in = nullptr, ev_out = nullptr;
+    struct Side {
+      cudaStream_t& s;
+      cudaEvent_t &a, &b;
+      ~Side() {
+        if (s) {
+          cudaStreamSynchronize(s);
+          cudaStreamDestroy(s);
+        }
+        if (a) cudaEventDestroy(a);
+        if (b) cudaEventDestroy(b);
+      }
+    } side{s64, ev_in, ev_out};
+    LCUDA(cudaStreamCreateWithFlags(&s64, cudaStreamNonBlocking), "cudaStreamCreate");
+    LCUDA(cudaEventCreateWithFlags(&ev_in, cudaEventDisableTiming), "cudaEventCreate");
+    LCUDA(cudaEventCreateWithFlags(&ev_out, cudaEventDisableTiming), "cudaEventCreate");
+    int64_t* amb_col = c.amb;   // filled by the FP32 waves (counters[7])
+    int64_t* amb_run = c.amb2;  // read by the FP64 wave in flight
+    bool in_flight = false;
+    for (int64_t waves = 0; n_list > 0 || n_amb > 0 || in_flight; waves++) {
+      if (waves > 2 * N + 2) return fail(MSC_ERR_ITER_LIMIT, "fix-up did not converge");
+      if (!in_flight && n_amb > 0) {
+        std::swap(amb_col, amb_run);
+        const int n_run = n_amb;
+        n_amb = 0;
+        LCUDA(cudaMemsetAsync(c.counters + 7, 0, 2 * sizeof(int), st), "memset");
+        LCUDA(cudaEventRecord(ev_in, st), "cudaEventRecord");
+        LCUDA(cudaStreamWaitEvent(s64, ev_in, 0), "cudaStreamWaitEvent");
+        LCUDA(msc::launch_fixup(c.g64, V, P, d.lab, lab0, d.state, amb_run, n_run, c.list_c, c.counters + 8,
+                                c.queued, c.work + 56, c.work + 50, sms, s64),
+              "fix-up FP64");
+        LCUDA(cudaEventRecord(ev_out, s64), "cudaEventRecord");
+        in_flight = true;
+        stats[1] += n_run;
+        trace_mark(st, d.dir, "fp64 start " + std::to_string(n_run));
+      }
+      if (n_list > 0) {
+        LCUDA(cudaMemsetAsync(c.counters + 6, 0, sizeof(int), st), "memset");
+        LCUDA(msc::launch_fixup32(c.g32, V, P, d.lab, lab0, d.state, cur, n_list, nxt, c.counters + 6, c.queued,
+                                  amb_col, c.counters + 7, p->precision == 2 ? 2 : 0, c.work, c.work + 49, sms, st),
+              "fix-up");
+        stats[0] += n_list;
+        int h[2];  // next wave's length, ambiguous streamlines waiting
+        if (int rc = read_dev(c, c.counters + 6, 2, h)) return rc;
+        n_list = h[0];
+        n_amb = h[1];
+        std::swap(cur, nxt);
+        trace_mark(st, d.dir, "wave " + std::to_string(waves) + " next " + std::to_string(n_list));
+      } else if (in_flight) {
+        // the FP32 waves ran dry: the FP64 wave's reopened vertices are the next list
+        LCUDA(cudaStreamWaitEvent(st, ev_out, 0), "cudaStreamWaitEvent");
+        int n64 = 0;
+        if (int rc = read_dev(c, c.counters + 8, 1, &n64)) return rc;
+        if (n64 > 0)
+          LCUDA(cudaMemcpyAsync(cur, c.list_c, (size_t)n64 * sizeof(int64_t), cudaMemcpyDeviceToDevice, st), "copy");
+        n_list = n64;
+        in_flight = false;
+        trace_mark(st, d.dir, "fp64 done next " + std::to_string(n_list));
+      }
+    }
   }
   {
     unsigned long long h[3];
