@@ -850,7 +850,8 @@ __global__ void uf_hook_kernel(const int32_t* __restrict__ lab, const float* __r
                                int64_t* __restrict__ parent) {
   const int64_t N = V.X * V.Y * V.Z;
   for (int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v < N; v += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t x = v % V.X, y = (v / V.X) % V.Y, z = v / (V.X * V.Y);
+    int x, y, z;
+    split_index(V, v, x, y, z);
     const int64_t nbr[3] = {x < V.X - 1 ? v + 1 : -1, y < V.Y - 1 ? v + V.X : -1, z < V.Z - 1 ? v + V.X * V.Y : -1};
     for (int j = 0; j < 3; j++) {
       const int64_t u = nbr[j];
@@ -888,7 +889,8 @@ __global__ void clean_target_kernel(const int32_t* __restrict__ lab, const float
       target[r] = r;  // only roots are followed; keep the rest defined
       continue;
     }
-    const int64_t x = r % V.X, y = (r / V.X) % V.Y, z = r / (V.X * V.Y);
+    int x, y, z;
+    split_index(V, r, x, y, z);
     const int64_t nbr[6] = {x < V.X - 1 ? r + 1 : -1, x > 0 ? r - 1 : -1, y < V.Y - 1 ? r + V.X : -1,
                             y > 0 ? r - V.X : -1, z < V.Z - 1 ? r + V.X * V.Y : -1, z > 0 ? r - V.X * V.Y : -1};
     int64_t earliest = r;
