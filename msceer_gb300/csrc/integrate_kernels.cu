@@ -316,7 +316,7 @@ __global__ void compact_level_kernel(const SpreadOrder S, int L0, int L1, const 
 }
 
 template <int K>
-__global__ void __launch_bounds__(128, 6) integrate_level_kernel(const Adv32 A, const int32_t* __restrict__ items,
+__global__ void __launch_bounds__(128, 7) integrate_level_kernel(const Adv32 A, const int32_t* __restrict__ items,
                                                               const unsigned long long* __restrict__ n_items,
                                                               int32_t* __restrict__ lab, uint8_t* __restrict__ lvl,
                                                               unsigned long long* __restrict__ work,
@@ -687,7 +687,7 @@ __global__ void __launch_bounds__(32) fixup_kernel(const Adv64 A, int32_t* __res
 //   amb_mode 2: its final voxel touches two different certain regions (any ending
 //     within half a voxel of a basin boundary).
 template <int K>
-__global__ void __launch_bounds__(128, 6) fixup32_kernel(const Adv32 A, int32_t* __restrict__ lab,
+__global__ void __launch_bounds__(128, 7) fixup32_kernel(const Adv32 A, int32_t* __restrict__ lab,
                                                       const int32_t* __restrict__ lab0, uint8_t* __restrict__ state,
                                                       const int64_t* __restrict__ list, int n,
                                                       int64_t* __restrict__ next, int* __restrict__ n_next,
