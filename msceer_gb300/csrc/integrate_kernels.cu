@@ -829,10 +829,11 @@ __device__ __forceinline__ bool comes_before(const float* f, int dir, int64_t a,
   return dir < 0 ? vgreater(f, b, a) : vgreater(f, a, b);
 }
 
-__device__ __forceinline__ int64_t uf_find(int64_t* parent, int64_t v) {
-  int64_t p = parent[v];
+// Vertex ids are 32-bit here: the labeling takes fewer than 2^31 vertices.
+__device__ __forceinline__ int32_t uf_find(int32_t* parent, int32_t v) {
+  int32_t p = parent[v];
   while (p != v) {
-    const int64_t gp = parent[p];
+    const int32_t gp = parent[p];
     if (gp != p) parent[v] = gp;  // path halving
     v = p;
     p = gp;
@@ -840,14 +841,14 @@ __device__ __forceinline__ int64_t uf_find(int64_t* parent, int64_t v) {
   return v;
 }
 
-__global__ void uf_init_kernel(int64_t* __restrict__ parent, int64_t N) {
+__global__ void uf_init_kernel(int32_t* __restrict__ parent, int64_t N) {
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < N; i += (int64_t)gridDim.x * blockDim.x)
-    parent[i] = i;
+    parent[i] = (int32_t)i;
 }
 
 // MergeWithSameNeighbors + MergeByOrder: the earlier root (walk order) stays root
 __global__ void uf_hook_kernel(const int32_t* __restrict__ lab, const float* __restrict__ f, const VolDims V, int dir,
-                               int64_t* __restrict__ parent) {
+                               int32_t* __restrict__ parent) {
   const int64_t N = V.X * V.Y * V.Z;
   for (int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v < N; v += (int64_t)gridDim.x * blockDim.x) {
     int x, y, z;
@@ -857,13 +858,11 @@ __global__ void uf_hook_kernel(const int32_t* __restrict__ lab, const float* __r
       const int64_t u = nbr[j];
       if (u < 0 || lab[u] != lab[v]) continue;
       for (int guard = 0; guard < 1 << 20; guard++) {
-        const int64_t ru = uf_find(parent, u), rv = uf_find(parent, v);
+        const int32_t ru = uf_find(parent, (int32_t)u), rv = uf_find(parent, (int32_t)v);
         if (ru == rv) break;
-        const int64_t early = comes_before(f, dir, ru, rv) ? ru : rv;
-        const int64_t late = early == ru ? rv : ru;
-        if ((int64_t)atomicCAS((unsigned long long*)&parent[late], (unsigned long long)late,
-                               (unsigned long long)early) == late)
-          break;
+        const int32_t early = comes_before(f, dir, ru, rv) ? ru : rv;
+        const int32_t late = early == ru ? rv : ru;
+        if (atomicCAS(&parent[late], late, early) == late) break;
       }
     }
   }
@@ -871,9 +870,9 @@ __global__ void uf_hook_kernel(const int32_t* __restrict__ lab, const float* __r
 
 // Root of every vertex by a read-only walk up the finished forest (path halving here
 // would race with the other threads' walks and could leave a non-root behind).
-__global__ void uf_roots_kernel(const int64_t* __restrict__ parent, int64_t* __restrict__ root, int64_t N) {
+__global__ void uf_roots_kernel(const int32_t* __restrict__ parent, int32_t* __restrict__ root, int64_t N) {
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < N; i += (int64_t)gridDim.x * blockDim.x) {
-    int64_t r = i;
+    int32_t r = (int32_t)i;
     for (int64_t guard = 0; guard < N && parent[r] != r; guard++) r = parent[r];  // strictly earlier each hop
     root[i] = r;
   }
@@ -882,11 +881,11 @@ __global__ void uf_roots_kernel(const int64_t* __restrict__ parent, int64_t* __r
 // MergeBoundaryExtrema: a component root joins the component of its first earlier
 // neighbour from another region (itself if there is none, i.e. an extremum's component)
 __global__ void clean_target_kernel(const int32_t* __restrict__ lab, const float* __restrict__ f, const VolDims V, int dir,
-                                    const int64_t* __restrict__ parent, int64_t* __restrict__ target) {
+                                    const int32_t* __restrict__ parent, int32_t* __restrict__ target) {
   const int64_t N = V.X * V.Y * V.Z;
   for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < N; r += (int64_t)gridDim.x * blockDim.x) {
     if (parent[r] != r) {
-      target[r] = r;  // only roots are followed; keep the rest defined
+      target[r] = (int32_t)r;  // only roots are followed; keep the rest defined
       continue;
     }
     int x, y, z;
@@ -903,11 +902,11 @@ __global__ void clean_target_kernel(const int32_t* __restrict__ lab, const float
   }
 }
 
-__global__ void clean_resolve_kernel(const int32_t* __restrict__ lab, const VolDims V, const int64_t* __restrict__ parent,
-                                     const int64_t* __restrict__ target, int32_t* __restrict__ out) {
+__global__ void clean_resolve_kernel(const int32_t* __restrict__ lab, const VolDims V, const int32_t* __restrict__ parent,
+                                     const int32_t* __restrict__ target, int32_t* __restrict__ out) {
   const int64_t N = V.X * V.Y * V.Z;
   for (int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v < N; v += (int64_t)gridDim.x * blockDim.x) {
-    int64_t r = parent[v];
+    int32_t r = parent[v];
     for (int64_t guard = 0; guard < N && target[r] != r; guard++) r = target[r];  // strictly earlier each hop
     const int32_t l = lab[v];
     const int32_t lr = lab[r];
@@ -1056,7 +1055,7 @@ cudaError_t launch_fixup32(const float4* G, const VolDims& V, const IntegParams&
   return cudaGetLastError();
 }
 
-cudaError_t launch_clean(const int32_t* lab, const float* f, const VolDims& V, int dir, int64_t* parent, int64_t* target,
+cudaError_t launch_clean(const int32_t* lab, const float* f, const VolDims& V, int dir, int32_t* parent, int32_t* target,
                          int32_t* out, int num_sms, cudaStream_t stream) {
   const int64_t N = V.X * V.Y * V.Z;
   const int grid = num_sms * 8;

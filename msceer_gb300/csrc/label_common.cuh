@@ -132,7 +132,7 @@ cudaError_t launch_fixup32(const float4* G, const VolDims& V, const IntegParams&
                            uint8_t* state, const int64_t* list, int n, int64_t* next, int* n_next, uint32_t* queued,
                            int64_t* amb, int* n_amb, int amb_mode, unsigned long long* work,
                            unsigned long long* trips, int num_sms, cudaStream_t stream);
-cudaError_t launch_clean(const int32_t* lab, const float* f, const VolDims& V, int dir, int64_t* parent, int64_t* target,
+cudaError_t launch_clean(const int32_t* lab, const float* f, const VolDims& V, int dir, int32_t* parent, int32_t* target,
                          int32_t* out, int num_sms, cudaStream_t stream);
 
 }  // namespace msc

@@ -673,7 +673,7 @@ int finish_direction(LabelCtx& c, DirLabels& d, int32_t* out, int32_t* stage_int
   if (!out) return MSC_OK;
 
   // isolated-region cleaner
-  int64_t *parent, *target;
+  int32_t *parent, *target;  // (fewer than 2^31 vertices: setup_ctx)
   LCUDA(c.pool.get(&parent, N), "alloc");
   LCUDA(c.pool.get(&target, N), "alloc");
   LCUDA(msc::launch_clean(d.lab, c.f, V, d.dir, parent, target, out, sms, st), "clean");
