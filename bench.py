@@ -15,7 +15,7 @@ against the plain labels), or timed as the step with --triage.
               synchronisation, max over ranks; every rank runs its own replica --
               the path needs no collective)
   plain       the step with the plain full integration (the drop-in path, and the
-              judge of the triage)
+              yardstick of the triage)
   learned     the step with the learned triage, its speed-up over plain and its
               label difference from the plain labels
   e2e         the same metric through the C ABI host entry msc_ondemand_labels_host:

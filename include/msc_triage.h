@@ -10,7 +10,7 @@
  * predicts, per vertex, whether the fix-up would change its first-pass label; only
  * flagged vertices plus a random audit sample are re-decided, the rest keep the
  * first-pass label.  The plain path (msc_integrated_labels_3d) stays the drop-in and
- * the judge of the triage's mismatch.  One network serves both directions: the
+ * the yardstick of the triage's mismatch.  One network serves both directions: the
  * features of the descending direction see -f.
  *
  * Tensors:

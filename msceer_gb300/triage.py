@@ -8,7 +8,7 @@ first-pass labels the fix-up would change; only those vertices (plus a random au
 sample) are re-decided.  Everything here drives the library's own CUDA kernels through
 the C ABI: feature extraction, forward and backward passes, the Adam step and the
 triaged labeling.  The plain full integration (:func:`msceer_gb300.integrated_labels`)
-is the drop-in and the judge of the triage's mismatch.
+is the drop-in and the yardstick of the triage's mismatch.
 """
 from __future__ import annotations
 
