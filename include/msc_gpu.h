@@ -163,7 +163,7 @@ void msc_labels_last_stats(int64_t out[4]);
  * the calling thread: first pass, FP32 boundary re-decisions, FP64 re-decisions;
  * ascending, then descending. */
 void msc_labels_last_iterations(int64_t out[6]);
-/* The labeling keeps its device scratch (about 130 bytes per vertex and direction) in a
+/* The labeling keeps its device scratch (about 135 bytes per vertex and direction) in a
  * memory pool of its own that holds on to the memory between calls; this returns the
  * unused part to the device (call it before the application needs that memory
  * elsewhere).  No counterpart in the reference. */
