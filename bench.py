@@ -505,6 +505,11 @@ TRAFFIC_PER_LAUNCH: dict = {
     ("lstar_kernel", 512): (67.168e6 + 78.372e6) * 8,
     ("ldir_stage", 512): (158.404e6 + 159.985e6 + 224.759e6 + 12.212e6) * 8,
 }
+# FP32 operations of one adaptive-Euler iteration as the reference's advector states
+# it: two trilinear interpolations in the (1 - t) a + t b form (2 x 73), |g| (6), the
+# step clamp (2), the full and two half steps with the error test and the move (29).
+# The kernels execute fewer (each voxel's x-differences are taken once at entry); the
+# count is the algorithmic work, the same for every implementation.
 FLOP_PER_ITERATION = 183
 FP32_LANES_PER_SM = 128
 SM_MAX_MHZ = 2070
