@@ -154,6 +154,17 @@ int msc_integrated_labels_3d(const float* f, const uint8_t* grad, const int64_t 
 int msc_integrated_labels_3d_stages(const float* f, const uint8_t* grad, const int64_t dims[3],
                                     const msc_integ_params* params, int32_t* labels_asc, int32_t* labels_dsc,
                                     int32_t* stages, msc_stream_t stream);
+/* The isolated-region cleaner alone: IsolatedCCRegionRemoverNEW::ComputeOutput
+ * (gi_isolated_region_remover.h:155-192) on caller labels, as ondemandaccurate runs it
+ * after the integration (ondemandaccurate.cxx:866-870, 942-946).  Same-label
+ * 6-connected components; each component whose first vertex (in the order of
+ * `direction`: -1 the ascending labels' IndexCompareLessThan, lowest value first; +1
+ * the descending labels' IndexCompareGreaterThan) has an earlier neighbour joins, in
+ * the reference's vertex order, the component of its earliest neighbour from another
+ * region.  f: device X*Y*Z floats; labels_in / labels_out: device int32 per vertex
+ * (-1 = none; a vertex labelled -1 stays -1).  Blocking. */
+int msc_clean_regions_3d(const float* f, const int32_t* labels_in, const int64_t dims[3], int direction,
+                         int32_t* labels_out, msc_stream_t stream);
 /* Error text of the last failed labeling call on the calling thread. */
 const char* msc_labels_last_error_string(void);
 /* Work counts of the last labeling call on the calling thread: boundary

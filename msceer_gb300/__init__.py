@@ -10,6 +10,7 @@ from .api import (  # noqa: F401
     TopologicalRegularGrid2D,
     TopologicalRegularGrid3D,
     ascending_manifold_dims,
+    clean_regions,
     integrated_labels,
     integrated_labels_batch,
     lower_star_grad,

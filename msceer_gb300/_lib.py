@@ -44,6 +44,7 @@ SIGNATURES = {
     "msc_lower_star_grad_batch_3d": (ctypes.c_int, [ctypes.c_int, _VP, _I64P, _VP, _VP]),
     "msc_kernel_launches": (ctypes.c_int64, []),
     "msc_labels_last_error_string": (ctypes.c_char_p, []),
+    "msc_clean_regions_3d": (ctypes.c_int, [_VP, _VP, _I64P, ctypes.c_int, _VP, _VP]),
     "msc_labels_last_stats": (None, [_I64P]),
     "msc_labels_last_iterations": (None, [_I64P]),
     "msc_trim_scratch": (None, []),
@@ -100,5 +101,6 @@ def dims_arg(dims) -> ctypes.Array:
 def check(rc: int, fn: str) -> None:
     if rc != MSC_OK:
         lib = load()
-        err = lib.msc_labels_last_error_string if "labels" in fn else lib.msc_last_error_string
+        labels = "labels" in fn or "clean" in fn
+        err = lib.msc_labels_last_error_string if labels else lib.msc_last_error_string
         raise MscError(rc, fn, err().decode(errors="replace"))

@@ -195,6 +195,31 @@ def integrated_labels(f, grad, error_threshold=1e-4, gradient_threshold=None, it
     return out
 
 
+def clean_regions(f, labels, direction):
+    """IsolatedCCRegionRemoverNEW on device labels (msc_clean_regions_3d): ``direction``
+    -1 for ascending labels (lowest value first), +1 for descending ones.  ``f``: CUDA
+    float32 (Z, Y, X); ``labels``: CUDA int32 per vertex, -1 = none.  Returns the cleaned
+    labels as a new tensor."""
+    import torch
+
+    if not (f.is_cuda and labels.is_cuda):
+        raise ValueError("clean_regions takes CUDA tensors")
+    f = f.contiguous()
+    labels = labels.contiguous().view(-1)
+    dims = _shape_dims(f.shape)
+    if len(dims) != 3 or labels.numel() != f.numel() or labels.dtype != torch.int32:
+        raise ValueError("clean_regions takes a 3D volume and one int32 label per vertex")
+    out = torch.empty_like(labels)
+    lib = _lib.load()
+    stream = torch.cuda.current_stream(f.device).cuda_stream
+    with torch.cuda.device(f.device):
+        rc = lib.msc_clean_regions_3d(ctypes.c_void_p(f.data_ptr()), ctypes.c_void_p(labels.data_ptr()),
+                                      _lib.dims_arg(dims), int(direction), ctypes.c_void_p(out.data_ptr()),
+                                      ctypes.c_void_p(stream))
+    _lib.check(rc, "msc_clean_regions_3d")
+    return out
+
+
 def integrated_labels_batch(volumes, grads, threads: int = 4, **kwargs):
     """integrated_labels of many volumes, `threads` at a time on their own CUDA streams
     (each call synchronises only its own stream, so the volumes overlap on the GPU)."""

@@ -279,84 +279,232 @@ __device__ __forceinline__ void add_trips(unsigned long long n, unsigned long lo
   if ((threadIdx.x & 31) == 0 && n) atomicAdd(trips, n);
 }
 
-// One level of the spread order (or a group of consecutive small levels, [L0, L1),
-// which then act as one level: each of those launches would wait for its slowest
-// streamline while the GPU idles).  Streamlines of a level see only the labels of
-// earlier levels (lvl[v] < level; terminals are level 0, unlabelled vertices 255),
-// so a level's outcome does not depend on thread timing; where several streamlines
-// of the level pass the same unlabelled vertex, the smallest label wins (unsigned
-// atomicMin: a region's id < "reached no region" < unlabelled).  Level by level the
-// pass is therefore deterministic.  `work` counts the level's claimed items (zero at
-// launch).
-// The vertices of levels [L0, L1) not labelled in an earlier level, compacted into
-// `items` (their order does not matter: a level's outcome does not depend on it).
-// Checking here, before the level runs, skips exactly the vertices the level's
-// streamlines would skip: those stamped below `level`.
-__global__ void compact_level_kernel(const SpreadOrder S, int L0, int L1, const uint8_t* __restrict__ lvl, int level,
-                                     int32_t* __restrict__ items, unsigned long long* __restrict__ n_items) {
-  const int64_t count = S.offset[L1] - S.offset[L0];
-  const int lane = threadIdx.x & 31;
-  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t - lane < count;
-       t += (int64_t)gridDim.x * blockDim.x) {
-    int64_t i = -1;
-    if (t < count) {
-      const int64_t u = S.offset[L0] + t;
-      int L = L0;
-      while (L + 1 < L1 && S.offset[L + 1] <= u) L++;
-      i = S.start[L] + (u - S.offset[L]) * S.stride[L];
-      if (lvl[i] < level) i = -1;
-    }
-    const unsigned m = __ballot_sync(kFullMask, i >= 0);  // (the loop bound is warp-uniform)
-    if (!m) continue;
-    unsigned long long base = 0;
-    if (lane == 0) base = atomicAdd(n_items, (unsigned long long)__popc(m));
-    base = __shfl_sync(kFullMask, base, 0);
-    if (i >= 0) items[base + __popc(m & ((1u << lane) - 1u))] = (int32_t)i;
-  }
+// ---- first pass: speculation, then the reference's sequential outcome ------------------
+//
+// The reference's first pass (:150-240) visits the vertices one at a time in its spread
+// order, and every streamline stops at the first vertex any earlier streamline labelled.
+// Run a whole batch of that order at once and the streamlines no longer see each
+// other's paths: on Gaussian-sum and k^-3 fields that alone moved 0.5-1% of the final
+// labels away from the one-thread reference (the FP32 arithmetic moves ~1e-4).  The
+// sequential outcome is recovered exactly, in parallel:
+//   1. speculate: every streamline of the batch runs, stopping only at vertices
+//      labelled before the batch, and records the sequence of vertices its stop test
+//      passed (and which of them the reference pushes on its path).  The sequential
+//      streamline is a prefix of this one: the advection does not read labels.
+//   2. resolve: a path vertex belongs to the first item (in visiting order) whose
+//      effective path holds it ("claim"); an item is skipped when an earlier one claims
+//      its vertex, and its effective path ends at the first vertex an earlier one
+//      claims ("cut").  Item k's outcome depends only on items < k, so recomputing
+//      claims and cuts from the previous round's cuts reaches the sequential outcome.
+//      After the first round only the claims of vertices between an item's old and new
+//      extent can change; they are recomputed from the vertices' holder lists, and only
+//      the items that hold such a vertex are looked at again.
+//   3. label: a cut item takes the label of the item that claimed its stop vertex
+//      (following the chain to an uncut one), an uncut item the label where it stopped;
+//      every claimed vertex takes its claimer's label.
+// Entry 0 of an item is its own vertex, entry 1 lies in an array of its own, entries
+// from 2 on in segments of kSeg words in a pool (a full segment is followed by the word
+// offset of the next).  Entries are vertex ids with kRec set on the reference's path
+// vertices.
+
+constexpr uint32_t kRec = 0x80000000u;
+constexpr int kSeg = 32;
+constexpr int kSpecBuf = 48;  // a lane holds <= kSeg entries at a turn's start, + at most K <= 16 in the turn
+constexpr uint32_t kNoClaim = 0xFFFFFFFFu;
+
+__device__ __forceinline__ int64_t spread_vertex(const SpreadOrder& S, int64_t u) {
+  int L = 0;
+  while (L + 1 < S.nlev && S.offset[L + 1] <= u) L++;
+  return S.start[L] + (u - S.offset[L]) * S.stride[L];
 }
 
+// Ordered compaction of spread positions [u0, u1) whose vertex is not labelled yet:
+// block b owns positions u0 + b*kCompactBlock + [0, kCompactBlock), 4 per thread.
+constexpr int kCompactThreads = 256;
+constexpr int kCompactBlock = 4 * kCompactThreads;
+
+__device__ __forceinline__ int compact_flags(const SpreadOrder& S, int64_t u0, int64_t u1, const uint8_t* lvl,
+                                             int stamp, int64_t vx[4]) {
+  const int64_t ub = u0 + (int64_t)blockIdx.x * kCompactBlock + 4 * threadIdx.x;
+  int n = 0;
+#pragma unroll
+  for (int j = 0; j < 4; j++) {
+    vx[j] = -1;
+    const int64_t u = ub + j;
+    if (u < u1) {
+      const int64_t i = spread_vertex(S, u);
+      if (lvl[i] >= stamp) {
+        vx[j] = i;
+        n++;
+      }
+    }
+  }
+  return n;
+}
+
+// exclusive block scan of one int per thread (kCompactThreads threads); returns the total
+__device__ __forceinline__ int block_excl_scan(int v, int& excl, int* s_warp) {
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  int incl = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int u = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= o) incl += u;
+  }
+  if (lane == 31) s_warp[w] = incl;
+  __syncthreads();
+  if (w == 0) {
+    const int nw = kCompactThreads / 32;
+    int x = lane < nw ? s_warp[lane] : 0;
+    int xi = x;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int u = __shfl_up_sync(0xffffffffu, xi, o);
+      if (lane >= o) xi += u;
+    }
+    if (lane < nw) s_warp[lane] = xi - x;
+    if (lane == nw - 1) s_warp[32] = xi;
+  }
+  __syncthreads();
+  excl = s_warp[w] + incl - v;
+  const int total = s_warp[32];
+  __syncthreads();
+  return total;
+}
+
+__global__ void __launch_bounds__(kCompactThreads) spread_count_kernel(const SpreadOrder S, int64_t u0, int64_t u1,
+                                                                      const uint8_t* __restrict__ lvl, int stamp,
+                                                                      int* __restrict__ counts) {
+  __shared__ int s_warp[33];
+  int64_t vx[4];
+  const int n = compact_flags(S, u0, u1, lvl, stamp, vx);
+  int excl;
+  const int total = block_excl_scan(n, excl, s_warp);
+  if (threadIdx.x == 0) counts[blockIdx.x] = total;
+}
+
+// one block: counts[0, nb) -> exclusive offsets in place, the total to *n_items
+__global__ void __launch_bounds__(1024) scan_counts_kernel(int* __restrict__ counts, int64_t nb,
+                                                           unsigned long long* __restrict__ n_items) {
+  __shared__ long long s_part[1024];
+  const int64_t per = (nb + 1023) / 1024;
+  const int64_t b0 = threadIdx.x * per, b1 = b0 + per < nb ? b0 + per : nb;
+  long long sum = 0;
+  for (int64_t b = b0; b < b1; b++) sum += counts[b];
+  s_part[threadIdx.x] = sum;
+  __syncthreads();
+  for (int o = 1; o < 1024; o <<= 1) {
+    const long long u = threadIdx.x >= o ? s_part[threadIdx.x - o] : 0;
+    __syncthreads();
+    s_part[threadIdx.x] += u;
+    __syncthreads();
+  }
+  long long run = s_part[threadIdx.x] - sum;
+  for (int64_t b = b0; b < b1; b++) {
+    const int c = counts[b];
+    counts[b] = (int)run;
+    run += c;
+  }
+  if (threadIdx.x == 1023) *n_items = (unsigned long long)s_part[1023];
+}
+
+__global__ void __launch_bounds__(kCompactThreads) spread_write_kernel(const SpreadOrder S, int64_t u0, int64_t u1,
+                                                                      const uint8_t* __restrict__ lvl, int stamp,
+                                                                      const int* __restrict__ offs,
+                                                                      int32_t* __restrict__ items) {
+  __shared__ int s_warp[33];
+  int64_t vx[4];
+  const int n = compact_flags(S, u0, u1, lvl, stamp, vx);
+  int excl;
+  block_excl_scan(n, excl, s_warp);
+  int64_t o = (int64_t)offs[blockIdx.x] + excl;
+#pragma unroll
+  for (int j = 0; j < 4; j++)
+    if (vx[j] >= 0) items[o++] = (int32_t)vx[j];
+}
+
+// Walks an item's entries in order.
+struct SeqWalk {
+  const SpecSet& Q;
+  int64_t k;
+  uint32_t seg = 0;
+  int i = 0;
+  __device__ __forceinline__ SeqWalk(const SpecSet& q, int64_t item) : Q(q), k(item) {}
+  __device__ __forceinline__ uint32_t next() {
+    const int j = i++;
+    if (j == 0) return (uint32_t)Q.vtx[k] | kRec;
+    if (j == 1) return Q.e1[k];
+    const int p = j - 2;
+    if (p == 0) seg = Q.head[k];
+    else if ((p & (kSeg - 1)) == 0) seg = Q.pool[seg + kSeg];
+    return Q.pool[seg + (p & (kSeg - 1))];
+  }
+};
+
+// Speculative streamlines of items [k0, k1) of the ordered list: they stop only at
+// vertices labelled before this batch (lvl < A.level), record their entries with a
+// holder node per entry, and make the first round's claims (every item alive, its
+// whole path effective).
 template <int K>
-__global__ void __launch_bounds__(128, 7) integrate_level_kernel(const Adv32 A, const int32_t* __restrict__ items,
-                                                              const unsigned long long* __restrict__ n_items,
-                                                              int32_t* __restrict__ lab, uint8_t* __restrict__ lvl,
-                                                              unsigned long long* __restrict__ work,
-                                                              unsigned long long* __restrict__ trips) {
+__global__ void __launch_bounds__(128, 7) speculate_kernel(const Adv32 A, const SpecSet Q, int64_t k0, int64_t k1,
+                                                           const int32_t* __restrict__ lab,
+                                                           uint32_t* __restrict__ claim,
+                                                           unsigned long long* __restrict__ work,
+                                                           unsigned long long* __restrict__ trips) {
   const VolDims& V = A.V;
   const int level = A.level;
-  const unsigned long long count = *n_items;
-  int path[kPathCap];
-  int np = 0;
-  int64_t end = 0;
+  const int lane = threadIdx.x & 31;
+  uint32_t buf[kSpecBuf];  // entries from 2 on, not yet in the pool
+  int nb = 0;
+  int cnt = 0;             // entries so far
+  uint32_t e1 = 0;         // entry 1
+  int64_t k = -1;          // the lane's item
+  int flushed = 0;         // pool entries written
+  uint32_t link = 0;       // word offset of the last full segment's link slot
   int phase = kLaneIdle;
   unsigned long long ntrips = 0;
   int x = 0, y = 0, z = 0;
   F3 cur = {0.f, 0.f, 0.f}, old = cur, g = cur;
   float gm = 0.f, step = 0.f, slim = 0.f, gm_end = 0.f;
   int iters = 0;
-  bool nb = false;
+  bool nb_near = false;
   float b[3] = {0.f, 0.f, 0.f};
   F3 c[8];
-  F3 anchor = cur;  // trapped-streamline test
+  F3 anchor = cur;
   int t_iters = 0, t_n = 0;
-  int64_t last_nv = -1;  // nearest vertex the stop test last passed
+  int64_t last_nv = -1;
+  int32_t endlab = kLabelNone;
+  auto mark_rec = [&]() {  // the reference pushes its nearest vertex: the last one passed
+    if (cnt == 2) e1 |= kRec;
+    else if (cnt > 2) buf[nb - 1] |= kRec;
+  };
   while (true) {
     {
       const unsigned long long t = claim_item(phase == kLaneIdle, work);
       if (phase == kLaneIdle) {
-        if (t >= count) {
+        k = k0 + (int64_t)t;
+        if (k >= k1 || *(volatile int*)Q.overflow) {
           phase = kLaneDone;
         } else {
-          const int64_t i = items[t];
-          split_index(V, i, x, y, z);
-          cur = {(float)x, (float)y, (float)z};
-          iters = A.P.iteration_limit;
-          anchor = cur;
-          t_iters = iters;
-          t_n = 0;
-          last_nv = -1;
-          np = 0;
-          path[np++] = (int)i;
-          phase = kLaneEnter;
+          const int64_t i = Q.vtx[k];
+          if (A.lvl[i] < level) {  // labelled by an earlier batch of this group
+            Q.alive[k] = 0;
+            Q.len[k] = 0;
+          } else {
+            split_index(V, i, x, y, z);
+            cur = {(float)x, (float)y, (float)z};
+            iters = A.P.iteration_limit;
+            anchor = cur;
+            t_iters = iters;
+            t_n = 0;
+            last_nv = i;
+            nb = 0;
+            cnt = 1;
+            e1 = 0;
+            flushed = 0;
+            endlab = kLabelNone;
+            phase = kLaneEnter;
+          }
         }
       }
     }
@@ -364,51 +512,284 @@ __global__ void __launch_bounds__(128, 7) integrate_level_kernel(const Adv32 A, 
       add_trips(ntrips, trips);
       break;
     }
-    // K steps; a lane that leaves its voxel enters the next one within the same turn,
-    // a lane whose streamline ended waits for the turn's end
     for (int r = 0; r < K; r++) {
       if (phase != kLaneEnter && phase != kLaneStep) continue;
-      const int ev = A.advance(phase, x, y, z, cur, old, iters, nb, b, c, g, gm, step, slim, gm_end, last_nv, ntrips);
+      const int64_t seen = last_nv;
+      const int ev = A.advance(phase, x, y, z, cur, old, iters, nb_near, b, c, g, gm, step, slim, gm_end, last_nv,
+                               ntrips);
+      if (last_nv != seen) {  // the stop test passed a new vertex
+        if (cnt == 1) e1 = (uint32_t)last_nv;
+        else buf[nb++] = (uint32_t)last_nv;
+        cnt++;
+      }
       if (ev == EV_NONE) continue;
       A.nearest3(cur, x, y, z);
-      end = vid(V, x, y, z);
-      if (np < kPathCap) path[np++] = (int)end;
+      if (ev == EV_HIT_PREASSIGNED) {
+        // stopped by a vertex labelled before the batch: its label is the streamline's
+        // (the vertex itself is not recorded, so every entry is a vertex unlabelled
+        // before the batch)
+        const int32_t l = lab[vid(V, x, y, z)];
+        endlab = l == -1 ? kLabelNone : l;
+      } else {
+        mark_rec();
+      }
       phase = ev == EV_OUT_OF_VOXEL ? kLaneEnter : kLaneEnd;
     }
-    {
-      if (phase == kLaneStep && A.P.trap_window > 0 && t_iters - iters >= A.P.trap_window) {
-        t_iters = iters;
-        if (A.trapped(cur, anchor, t_n)) {  // ends where the iteration limit would have
-          A.nearest3(cur, x, y, z);
-          end = vid(V, x, y, z);
-          if (np < kPathCap) path[np++] = (int)end;
-          phase = kLaneEnd;
-        }
+    if (phase == kLaneStep && A.P.trap_window > 0 && t_iters - iters >= A.P.trap_window) {
+      t_iters = iters;
+      if (A.trapped(cur, anchor, t_n)) {  // ends where the iteration limit would have
+        mark_rec();
+        phase = kLaneEnd;
       }
     }
-    if (phase == kLaneEnd) {
-      const uint8_t le = lvl[end];
-      const int32_t lb = lab[end];
-      int32_t dest = le < level ? lb : -1;
-      if (dest == -1) dest = kLabelNone;  // reached no region: assigned to nothing
-      // the path's level bytes are read eight at a time, so that one lane's write-back
-      // waits for a memory round trip per eight vertices rather than per vertex
-      for (int k0 = 0; k0 < np; k0 += 8) {
-        int pk[8];
-        uint8_t lk[8];
+    // flush: an ended streamline writes the rest of its entries, a long one a full
+    // segment (+ its link word); one pool and one holder-node allocation per warp and
+    // turn.  A segment is flushed early only with an entry to spare (an ending marks the
+    // last entry).
+    const bool ending = phase == kLaneEnd;
+    const int words = ending ? nb + (nb > kSeg ? 1 : 0) : (nb > kSeg ? kSeg + 1 : 0);
+    const int nodes = ending ? nb + (cnt >= 2 ? 2 : 1) : (nb > kSeg ? kSeg : 0);  // entries flushed now
+    int incl = words, nincl = nodes;
 #pragma unroll
-        for (int j = 0; j < 8; j++) {
-          pk[j] = k0 + j < np ? path[k0 + j] : -1;
-          lk[j] = pk[j] >= 0 ? lvl[pk[j]] : 0;
+    for (int o = 1; o < 32; o <<= 1) {
+      const int u = __shfl_up_sync(kFullMask, incl, o);
+      const int un = __shfl_up_sync(kFullMask, nincl, o);
+      if (lane >= o) {
+        incl += u;
+        nincl += un;
+      }
+    }
+    const int total = __shfl_sync(kFullMask, incl, 31), ntotal = __shfl_sync(kFullMask, nincl, 31);
+    unsigned long long base = 0, nbase = 0;
+    if (ntotal > 0) {
+      if (lane == 31) {
+        base = total > 0 ? atomicAdd(Q.cursor, (unsigned long long)total) : 0ull;
+        nbase = atomicAdd(Q.ncursor, (unsigned long long)ntotal);
+      }
+      base = __shfl_sync(kFullMask, base, 31);
+      nbase = __shfl_sync(kFullMask, nbase, 31);
+      if (base + (unsigned long long)total > Q.pool_words || nbase + (unsigned long long)ntotal > Q.node_cap) {
+        if (lane == 0) atomicExch(Q.overflow, 1);
+        phase = kLaneDone;  // the batch is redone smaller; its results are discarded
+        continue;
+      }
+    }
+    // a recorded entry: its holder node (and, for a path vertex, the first round's claim)
+    int32_t node = (int32_t)(nbase + (unsigned long long)(nincl - nodes));
+    auto hold = [&](uint32_t u, int idx) {
+      const uint32_t v = u & ~kRec;
+      Q.hitem[node] = (int32_t)k;
+      Q.hidx[node] = (uint32_t)idx | (u & kRec);
+      Q.hnext[node] = atomicExch(&Q.hhead[v], node);
+      node++;
+      if (u & kRec) atomicMin(&claim[v], (uint32_t)k);
+    };
+    if (words > 0) {
+      const uint32_t off = (uint32_t)(base + (unsigned long long)(incl - words));
+      if (flushed == 0) Q.head[k] = off;
+      else Q.pool[link] = off;
+      const int seg = nb > kSeg ? kSeg : nb;  // entries of the segment written now
+      for (int e = 0; e < seg; e++) {
+        Q.pool[off + e] = buf[e];
+        hold(buf[e], 2 + flushed + e);
+      }
+      if (ending) {
+        if (nb > kSeg) {  // the rest follows the full segment's link word
+          Q.pool[off + kSeg] = off + kSeg + 1;
+          for (int e = kSeg; e < nb; e++) {
+            Q.pool[off + 1 + e] = buf[e];
+            hold(buf[e], 2 + flushed + e);
+          }
         }
-#pragma unroll
-        for (int j = 0; j < 8; j++) {
-          if (pk[j] < 0 || lk[j] < level) continue;  // labelled in an earlier level: keep
-          atomicMin(reinterpret_cast<unsigned int*>(&lab[pk[j]]), (unsigned int)dest);
-          lvl[pk[j]] = (uint8_t)level;
+      } else {
+        link = off + kSeg;
+        flushed += kSeg;
+        for (int e = kSeg; e < nb; e++) buf[e - kSeg] = buf[e];
+        nb -= kSeg;
+      }
+    }
+    if (ending) {
+      hold((uint32_t)Q.vtx[k] | kRec, 0);
+      if (cnt >= 2) hold(e1, 1);
+      Q.e1[k] = e1;
+      Q.len[k] = cnt;
+      Q.endlab[k] = endlab;
+      Q.alive[k] = 1;
+      Q.cut[k] = -1;
+      nb = 0;
+      phase = kLaneIdle;
+    }
+  }
+}
+
+// After a pool overflow: the discarded batch's claims (on vertices not labelled yet) go.
+__global__ void spec_unclaim_all_kernel(const uint8_t* __restrict__ lvl, int level, uint32_t* __restrict__ claim,
+                                        int64_t N) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < N; i += (int64_t)gridDim.x * blockDim.x)
+    if (lvl[i] >= level) claim[i] = kNoClaim;
+}
+
+// Effective extent (entries) of an item's path: none if skipped, up to its cut, or all.
+__device__ __forceinline__ int spec_extent(uint8_t alive, int cut, int len) {
+  return alive ? (cut >= 0 ? cut : len) : 0;
+}
+
+// Marks v dirty (bitmap + list, the list appends aggregated per warp); every lane of the
+// warp calls it with its own `want`.
+__device__ __forceinline__ void mark_dirty(bool want, uint32_t v, uint32_t* __restrict__ bits,
+                                           uint32_t* __restrict__ list, unsigned long long* __restrict__ n_list) {
+  bool add = false;
+  if (want) {
+    const uint32_t bit = 1u << (v & 31);
+    add = !(atomicOr(&bits[v >> 5], bit) & bit);
+  }
+  const unsigned m = __ballot_sync(kFullMask, add);
+  if (!m) return;
+  const int lane = threadIdx.x & 31;
+  unsigned long long base = 0;
+  if (lane == __ffs(m) - 1) base = atomicAdd(n_list, (unsigned long long)__popc(m));
+  base = __shfl_sync(kFullMask, base, __ffs(m) - 1);
+  if (add) list[base + __popc(m & ((1u << lane) - 1u))] = v;
+}
+
+// New alive / cut of the items in [k0, k1) from the claims (with `ibits`, only the items
+// whose bit is set, a bit per item from k0).  A changed item marks the path vertices
+// between its old and new extent in nxt: their claims are recomputed next round.
+__global__ void spec_check_kernel(const SpecSet Q, int64_t k0, int64_t k1, const uint32_t* __restrict__ claim,
+                                  const uint32_t* __restrict__ ibits, uint32_t* __restrict__ nxt,
+                                  uint32_t* __restrict__ nxt_list, unsigned long long* __restrict__ n_nxt) {
+  const int64_t span = k1 - k0;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  // every lane of a warp runs the same number of loop trips (mark_dirty is warp-wide);
+  // a warp's 32 items share one word of ibits
+  for (int64_t t0 = blockIdx.x * (int64_t)blockDim.x; t0 < span; t0 += stride) {
+    const int64_t t = t0 + threadIdx.x;
+    const int64_t k = k0 + t;
+    const bool have = t < span;
+    const int n = have ? Q.len[k] : 0;
+    bool look = n > 0;
+    if (ibits) look = look && ((ibits[t >> 5] >> (t & 31)) & 1u);
+    uint8_t oa = 0, na = 0;
+    int oc = -1, nc = -1;
+    bool changed = false;
+    if (look) {
+      const uint32_t kk = (uint32_t)k;
+      oa = Q.alive[k];
+      oc = Q.cut[k];
+      na = claim[Q.vtx[k]] < kk ? 0 : 1;
+      SeqWalk w(Q, k);
+      w.next();
+      for (int e = 1; e < n; e++) {
+        const uint32_t v = w.next() & ~kRec;
+        if (claim[v] < kk) {
+          nc = e;
+          break;
         }
       }
-      phase = kLaneIdle;
+      changed = na != oa || nc != oc;
+      if (changed) {
+        Q.alive[k] = na;
+        Q.cut[k] = nc;
+      }
+    }
+    // the path vertices between the old and the new extent
+    const int xo = changed ? spec_extent(oa, oc, n) : 0, xn = changed ? spec_extent(na, nc, n) : 0;
+    const int lo = xo < xn ? xo : xn, hi = xo < xn ? xn : xo;
+    int trips = hi;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) trips = max(trips, __shfl_xor_sync(kFullMask, trips, o));
+    SeqWalk w(Q, k);
+    for (int e = 0; e < trips; e++) {
+      uint32_t u = 0;
+      if (e < hi) u = w.next();
+      mark_dirty(e >= lo && e < hi && (u & kRec), u & ~kRec, nxt, nxt_list, n_nxt);
+    }
+  }
+}
+
+// The claims of the dirty vertices, from their holders' current extents.
+__global__ void spec_reclaim_kernel(const SpecSet Q, const uint32_t* __restrict__ list,
+                                    const unsigned long long* __restrict__ n_list, uint32_t* __restrict__ claim) {
+  const unsigned long long n = *n_list;
+  for (unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; i < n;
+       i += (unsigned long long)gridDim.x * blockDim.x) {
+    const uint32_t v = list[i];
+    uint32_t m = kNoClaim;
+    for (int32_t h = Q.hhead[v]; h >= 0; h = Q.hnext[h]) {
+      const uint32_t ix = Q.hidx[h];
+      if (!(ix & kRec)) continue;
+      const int32_t k = Q.hitem[h];
+      if ((int)(ix & ~kRec) < spec_extent(Q.alive[k], Q.cut[k], Q.len[k]) && (uint32_t)k < m) m = (uint32_t)k;
+    }
+    claim[v] = m;
+  }
+}
+
+// The items that hold a dirty vertex (whose claim may have changed) are looked at next.
+__global__ void spec_holders_kernel(const SpecSet Q, int64_t k0, const uint32_t* __restrict__ list,
+                                    const unsigned long long* __restrict__ n_list, uint32_t* __restrict__ ibits) {
+  const unsigned long long n = *n_list;
+  for (unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; i < n;
+       i += (unsigned long long)gridDim.x * blockDim.x) {
+    for (int32_t h = Q.hhead[list[i]]; h >= 0; h = Q.hnext[h]) {
+      const int64_t t = Q.hitem[h] - k0;
+      atomicOr(&ibits[t >> 5], 1u << (t & 31));
+    }
+  }
+}
+
+// ptr: the item whose label a cut item takes (the claimer of its stop vertex), or itself
+__global__ void spec_ptr_kernel(const SpecSet Q, int64_t k0, int64_t k1, const uint32_t* __restrict__ claim) {
+  for (int64_t k = k0 + blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < k1; k += (int64_t)gridDim.x * blockDim.x) {
+    if (!Q.alive[k]) continue;
+    const int ct = Q.cut[k];
+    int32_t p = (int32_t)k;
+    if (ct >= 0) {
+      SeqWalk w(Q, k);
+      uint32_t u = 0;
+      for (int e = 0; e <= ct; e++) u = w.next();
+      p = (int32_t)claim[u & ~kRec];
+    }
+    Q.ptr[k] = p;
+  }
+}
+
+__global__ void spec_jump_kernel(const SpecSet Q, int64_t k0, int64_t k1) {
+  for (int64_t k = k0 + blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < k1; k += (int64_t)gridDim.x * blockDim.x)
+    if (Q.alive[k]) Q.ptr[k] = Q.ptr[Q.ptr[k]];
+}
+
+// Every claimed vertex takes its claimer's label (the label where the chain of cut
+// items through ptr ends); the batch's vertices are stamped.  A chain longer than
+// kChainSteps is left to pointer jumping: the item reports it in *long_chain and writes
+// nothing.
+constexpr int kChainSteps = 64;
+__global__ void spec_write_kernel(const SpecSet Q, int64_t k0, int64_t k1, uint8_t* __restrict__ lvl, int level,
+                                  const uint32_t* __restrict__ claim, int32_t* __restrict__ lab,
+                                  int* __restrict__ long_chain) {
+  for (int64_t k = k0 + blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < k1; k += (int64_t)gridDim.x * blockDim.x) {
+    if (!Q.alive[k]) continue;
+    int32_t p = Q.ptr[k];
+    for (int s = 0; s < kChainSteps; s++) {
+      const int32_t q = Q.ptr[p];
+      if (q == p) break;
+      p = q;
+    }
+    if (Q.ptr[p] != p) {
+      atomicExch(long_chain, 1);
+      continue;
+    }
+    const int32_t d = Q.endlab[p];
+    const int n = Q.cut[k] >= 0 ? Q.cut[k] : Q.len[k];
+    SeqWalk w(Q, k);
+    for (int e = 0; e < n; e++) {
+      const uint32_t u = w.next();
+      if (!(u & kRec)) continue;
+      const uint32_t v = u & ~kRec;
+      if (claim[v] == (uint32_t)k) {
+        lab[v] = d;
+        lvl[v] = (uint8_t)level;
+      }
     }
   }
 }
@@ -592,24 +973,20 @@ __global__ void boundary_set_kernel(const int32_t* __restrict__ lab, const uint8
   }
 }
 
-// One fix-up wave (:330-415): re-integrate, stopping only at certain terminals.  The
-// decided label is read from lab0, the labels as the first pass left them: at a
-// certain terminal that is the region's label (never changed), and at any other
-// ending (low gradient, iteration limit) it is a value no concurrent re-decision can
-// be rewriting, so every wave's outcome is independent of thread timing.
+// Fix-up streamlines (:340-392) in the reference's FP64 arithmetic: from each listed
+// vertex, integrate until a certain terminal region (or a low gradient / the iteration
+// limit); the streamline's final nearest vertex goes to endv.  The integration reads no
+// labels, so where a vertex's streamline ends does not depend on the wave order.
 template <int K>
-__global__ void __launch_bounds__(32) fixup_kernel(const Adv64 A, int32_t* __restrict__ lab,
-                                                    const int32_t* __restrict__ lab0, uint8_t* __restrict__ state,
-                                                    const int64_t* __restrict__ list, int n, int64_t* __restrict__ next,
-                                                    int* __restrict__ n_next, uint32_t* __restrict__ queued,
-                                                    unsigned long long* __restrict__ work,
-                                                    unsigned long long* __restrict__ trips) {
+__global__ void __launch_bounds__(32) fixup_end64_kernel(const Adv64 A, const int64_t* __restrict__ list, int n,
+                                                         int32_t* __restrict__ endv,
+                                                         unsigned long long* __restrict__ work,
+                                                         unsigned long long* __restrict__ trips) {
   const VolDims& V = A.V;
   int phase = kLaneIdle;
   unsigned long long ntrips = 0;
   int64_t v = 0;
   int x = 0, y = 0, z = 0;
-  int32_t init = 0;
   D3 cur = {0.0, 0.0, 0.0}, old = cur, g = cur;
   float gm = 0.f, step = 0.f;
   int iters = 0;
@@ -625,8 +1002,6 @@ __global__ void __launch_bounds__(32) fixup_kernel(const Adv64 A, int32_t* __res
         phase = kLaneDone;
       } else {
         v = list[k];
-        atomicAnd(&queued[v >> 5], ~(1u << (v & 31)));
-        init = lab[v];
         split_index(V, v, x, y, z);
         cur = {(double)x, (double)y, (double)z};
         iters = A.P.iteration_limit;
@@ -656,29 +1031,12 @@ __global__ void __launch_bounds__(32) fixup_kernel(const Adv64 A, int32_t* __res
     }
     if (phase != kLaneEnd) continue;
     phase = kLaneIdle;
-    const int64_t end = vid(V, x, y, z);
-    int32_t nl = lab0[end];
-    if (nl == -1) nl = kLabelNone;
-    lab[v] = nl;
-    state[v] = kStNonterminal;
-    if (nl == init) continue;
-    int vx, vy, vz;
-    split_index(V, v, vx, vy, vz);
-    const int64_t nbr[6] = {vx < V.X - 1 ? v + 1 : -1, vx > 0 ? v - 1 : -1, vy < V.Y - 1 ? v + V.X : -1,
-                            vy > 0 ? v - V.X : -1, vz < V.Z - 1 ? v + V.X * V.Y : -1, vz > 0 ? v - V.X * V.Y : -1};
-#pragma unroll
-    for (int j = 0; j < 6; j++) {
-      const int64_t u = nbr[j];
-      if (u < 0 || state[u] != kStUnassigned || lab[u] == nl) continue;
-      const uint32_t bit = 1u << (u & 31);
-      if (atomicOr(&queued[u >> 5], bit) & bit) continue;
-      next[atomicAdd(n_next, 1)] = u;
-    }
+    endv[v] = (int32_t)vid(V, x, y, z);
   }
 }
 
-// One FP32 fix-up wave.  A streamline whose FP32 ending is ambiguous goes to the FP64
-// list instead of being decided here:
+// Fix-up streamlines in FP32 (as fixup_end64_kernel).  A streamline whose FP32 ending
+// is ambiguous goes to the FP64 list instead:
 //   it stopped at a gradient magnitude within 2^-8 (relative) below the threshold
 //   (the FP64 stop test decides), or
 //   amb_mode 0: its final point lies within 1/64 voxel of the plane where the
@@ -687,20 +1045,18 @@ __global__ void __launch_bounds__(32) fixup_kernel(const Adv64 A, int32_t* __res
 //   amb_mode 2: its final voxel touches two different certain regions (any ending
 //     within half a voxel of a basin boundary).
 template <int K>
-__global__ void __launch_bounds__(128, 7) fixup32_kernel(const Adv32 A, int32_t* __restrict__ lab,
-                                                      const int32_t* __restrict__ lab0, uint8_t* __restrict__ state,
-                                                      const int64_t* __restrict__ list, int n,
-                                                      int64_t* __restrict__ next, int* __restrict__ n_next,
-                                                      uint32_t* __restrict__ queued, int64_t* __restrict__ amb,
-                                                      int* __restrict__ n_amb, int amb_mode,
-                                                      unsigned long long* __restrict__ work,
-                                                      unsigned long long* __restrict__ trips) {
+__global__ void __launch_bounds__(128, 7) fixup_end32_kernel(const Adv32 A, const int32_t* __restrict__ lab,
+                                                          const uint8_t* __restrict__ state,
+                                                          const int64_t* __restrict__ list, int n,
+                                                          int32_t* __restrict__ endv, int64_t* __restrict__ amb,
+                                                          int* __restrict__ n_amb, int amb_mode,
+                                                          unsigned long long* __restrict__ work,
+                                                          unsigned long long* __restrict__ trips) {
   const VolDims& V = A.V;
   int phase = kLaneIdle;
   unsigned long long ntrips = 0;
   int64_t v = 0;
   int x = 0, y = 0, z = 0;
-  int32_t init = 0;
   F3 cur = {0.f, 0.f, 0.f}, old = cur, g = cur;
   float gm = 0.f, step = 0.f, slim = 0.f, gm_end = 0.f;
   int iters = 0, ev = EV_NONE;
@@ -717,7 +1073,6 @@ __global__ void __launch_bounds__(128, 7) fixup32_kernel(const Adv32 A, int32_t*
         phase = kLaneDone;
       } else {
         v = list[k];
-        init = lab[v];
         split_index(V, v, x, y, z);
         cur = {(float)x, (float)y, (float)z};
         iters = A.P.iteration_limit;
@@ -752,7 +1107,7 @@ __global__ void __launch_bounds__(128, 7) fixup32_kernel(const Adv32 A, int32_t*
     if (phase != kLaneEnd) continue;
     phase = kLaneIdle;
     const int64_t end = vid(V, x, y, z);
-    const int32_t lend = lab0[end];
+    const int32_t lend = lab[end];
     // a low-gradient stop whose FP32 magnitude lies within 2^-8 (relative) of the
     // threshold: FP32 rounding could have taken the other side of the stop test.  A
     // streamline that decelerates into an extremum crosses the threshold well inside
@@ -774,7 +1129,7 @@ __global__ void __launch_bounds__(128, 7) fixup32_kernel(const Adv32 A, int32_t*
         ac[a] = alt_c;
         const int64_t u = vid(V, ac[0], ac[1], ac[2]);
         const uint8_t st = state[u];
-        if ((st == kStSeed || st == kStTerminal) && lab0[u] != le) ambiguous = true;
+        if ((st == kStSeed || st == kStTerminal) && lab[u] != le) ambiguous = true;
       }
     } else if (!ambiguous && ev == EV_HIT_PREASSIGNED) {
       const int64_t bb[3] = {(int)fminf(fmaxf(cur.x, 0.f), A.ext2[0]), (int)fminf(fmaxf(cur.y, 0.f), A.ext2[1]),
@@ -785,41 +1140,131 @@ __global__ void __launch_bounds__(128, 7) fixup32_kernel(const Adv32 A, int32_t*
         const int64_t u = vid(V, bb[0] + (q & 1), bb[1] + ((q >> 1) & 1), bb[2] + (q >> 2));
         const uint8_t st = state[u];
         if (st != kStSeed && st != kStTerminal) continue;
-        const int32_t l = lab0[u];
+        const int32_t l = lab[u];
         if (seen == kLabelNone) seen = l;
         else if (l != seen) ambiguous = true;
       }
     }
     if (ambiguous) {
-      amb[atomicAdd(n_amb, 1)] = v;  // keeps its queued bit until the FP64 wave
+      amb[atomicAdd(n_amb, 1)] = v;
       continue;
     }
-    atomicAnd(&queued[v >> 5], ~(1u << (v & 31)));
-    int32_t nl = lend;
-    if (nl == -1) nl = kLabelNone;
-    lab[v] = nl;
-    state[v] = kStNonterminal;
-    if (nl == init) continue;
-    int vx, vy, vz;
-    split_index(V, v, vx, vy, vz);
-    const int64_t nbr[6] = {vx < V.X - 1 ? v + 1 : -1, vx > 0 ? v - 1 : -1, vy < V.Y - 1 ? v + V.X : -1,
-                            vy > 0 ? v - V.X : -1, vz < V.Z - 1 ? v + V.X * V.Y : -1, vz > 0 ? v - V.X * V.Y : -1};
-    // the six neighbours' bytes and labels are read together (one memory round trip)
-    uint8_t su[6];
-    int32_t lu[6];
-#pragma unroll
-    for (int j = 0; j < 6; j++) {
-      su[j] = nbr[j] >= 0 ? state[nbr[j]] : (uint8_t)kStNonterminal;
-      lu[j] = nbr[j] >= 0 ? lab[nbr[j]] : nl;
+    endv[v] = (int32_t)end;
+  }
+}
+
+// ---- fix-up waves (:316-415) ---------------------------------------------------------------
+// The reference decides a wave's vertices one at a time in increasing id, each taking
+// the label its streamline's final vertex carries at that moment: a certain terminal's
+// region, or -- after a low-gradient stop or the iteration limit -- the current label of
+// an ordinary vertex, which an earlier decision of the same wave may have changed.  The
+// kernels below reproduce that order: a decision whose end vertex e is decided earlier
+// in the same wave (e < v) takes e's new label (chains followed by pointer jumping), any
+// other takes the label at the wave's start; a changed vertex reopens its neighbours
+// that were undecided at its moment (never decided before the wave, and not earlier in
+// it) and carry another label.
+
+// A slot in a list whose length is *n for every lane of the warp that wants one (one
+// atomic per warp); every lane must call it.  Returns -1 where `want` is false.
+__device__ __forceinline__ int warp_append(bool want, int* n) {
+  const unsigned m = __ballot_sync(kFullMask, want);
+  if (!m) return -1;
+  const int lane = threadIdx.x & 31, leader = __ffs(m) - 1;
+  int base = 0;
+  if (lane == leader) base = atomicAdd(n, __popc(m));
+  base = __shfl_sync(kFullMask, base, leader);
+  return want ? base + __popc(m & ((1u << lane) - 1u)) : -1;
+}
+
+// wave w's members: stamp, clear their queued bit, list the ones without an end yet
+__global__ void wave_mark_kernel(const int64_t* __restrict__ list, int n, int w, int32_t* __restrict__ inw,
+                                 uint32_t* __restrict__ queued, const int32_t* __restrict__ endv,
+                                 int64_t* __restrict__ todo, int* __restrict__ n_todo) {
+  for (int k0 = blockIdx.x * blockDim.x; k0 < n; k0 += gridDim.x * blockDim.x) {  // warp-uniform trips
+    const int k = k0 + threadIdx.x;
+    int64_t v = -1;
+    if (k < n) {
+      v = list[k];
+      inw[v] = w;
+      atomicAnd(&queued[v >> 5], ~(1u << (v & 31)));
+    }
+    const int slot = warp_append(v >= 0 && endv[v] < 0, n_todo);
+    if (slot >= 0) todo[slot] = v;
+  }
+}
+
+__global__ void wave_root_kernel(const int64_t* __restrict__ list, int n, int w, const int32_t* __restrict__ endv,
+                                 const int32_t* __restrict__ inw, const int32_t* __restrict__ lab,
+                                 const uint8_t* __restrict__ state, int32_t* __restrict__ rptr,
+                                 int32_t* __restrict__ rval) {
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+    const int32_t v = (int32_t)list[k];
+    const int32_t e = endv[v];
+    const uint8_t st = state[e];
+    if (st != kStSeed && st != kStTerminal && inw[e] == w && e < v) {
+      rptr[v] = e;
+    } else {
+      rptr[v] = v;
+      const int32_t l = lab[e];
+      rval[v] = l == -1 ? kLabelNone : l;
+    }
+  }
+}
+
+__global__ void wave_jump_kernel(const int64_t* __restrict__ list, int n, int32_t* __restrict__ rptr) {
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+    const int64_t v = list[k];
+    rptr[v] = rptr[rptr[v]];
+  }
+}
+
+__global__ void wave_enqueue_kernel(const int64_t* __restrict__ list, int n, int w, const VolDims V,
+                                    const int32_t* __restrict__ rptr, const int32_t* __restrict__ rval,
+                                    const int32_t* __restrict__ lab, const uint8_t* __restrict__ state,
+                                    const int32_t* __restrict__ inw, uint32_t* __restrict__ queued,
+                                    int64_t* __restrict__ next, int* __restrict__ n_next) {
+  for (int k0 = blockIdx.x * blockDim.x; k0 < n; k0 += gridDim.x * blockDim.x) {  // warp-uniform trips
+    const int k = k0 + threadIdx.x;
+    int64_t v = -1;
+    int32_t nl = 0;
+    if (k < n) {
+      v = list[k];
+      nl = rval[rptr[v]];
+      if (nl == lab[v]) v = -1;  // unchanged: reopens nothing
+    }
+    int64_t nbr[6] = {-1, -1, -1, -1, -1, -1};
+    if (v >= 0) {
+      int vx, vy, vz;
+      split_index(V, v, vx, vy, vz);
+      nbr[0] = vx < V.X - 1 ? v + 1 : -1;
+      nbr[1] = vx > 0 ? v - 1 : -1;
+      nbr[2] = vy < V.Y - 1 ? v + V.X : -1;
+      nbr[3] = vy > 0 ? v - V.X : -1;
+      nbr[4] = vz < V.Z - 1 ? v + V.X * V.Y : -1;
+      nbr[5] = vz > 0 ? v - V.X * V.Y : -1;
     }
 #pragma unroll
     for (int j = 0; j < 6; j++) {
       const int64_t u = nbr[j];
-      if (su[j] != kStUnassigned || lu[j] == nl) continue;
-      const uint32_t bit = 1u << (u & 31);
-      if (atomicOr(&queued[u >> 5], bit) & bit) continue;
-      next[atomicAdd(n_next, 1)] = u;
+      // (the inw test: u was decided before v in this wave)
+      bool add = u >= 0 && state[u] == kStUnassigned && lab[u] != nl && !(inw[u] == w && u < v);
+      if (add) {
+        const uint32_t bit = 1u << (u & 31);
+        add = !(atomicOr(&queued[u >> 5], bit) & bit);
+      }
+      const int slot = warp_append(add, n_next);
+      if (slot >= 0) next[slot] = u;
     }
+  }
+}
+
+__global__ void wave_apply_kernel(const int64_t* __restrict__ list, int n, const int32_t* __restrict__ rptr,
+                                  const int32_t* __restrict__ rval, int32_t* __restrict__ lab,
+                                  uint8_t* __restrict__ state) {
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+    const int64_t v = list[k];
+    lab[v] = rval[rptr[v]];
+    state[v] = kStNonterminal;
   }
 }
 
@@ -878,36 +1323,77 @@ __global__ void uf_roots_kernel(const int32_t* __restrict__ parent, int32_t* __r
   }
 }
 
-// MergeBoundaryExtrema: a component root joins the component of its first earlier
-// neighbour from another region (itself if there is none, i.e. an extremum's component)
-__global__ void clean_target_kernel(const int32_t* __restrict__ lab, const float* __restrict__ f, const VolDims V, int dir,
-                                    const int32_t* __restrict__ parent, int32_t* __restrict__ target) {
+// MergeBoundaryExtrema (:108-145, the loop of :168-176): the reference visits the
+// component roots in vertex order; a root with an earlier neighbour (in the comparer's
+// order) lies in a component without its region's extremum, and joins -- in the union-
+// find as it stands at that moment -- the current component of its earliest neighbour
+// whose current component carries another label.  `first` holds every vertex's root
+// of the same-label forest; md[r] the root r joined (r itself if none).  Only roots
+// with an earlier neighbour decide anything; they are listed in `roots`.
+__global__ void clean_roots_kernel(const int32_t* __restrict__ lab, const float* __restrict__ f, const VolDims V, int dir,
+                                   const int32_t* __restrict__ first, int32_t* __restrict__ md,
+                                   int32_t* __restrict__ roots, int* __restrict__ n_roots) {
   const int64_t N = V.X * V.Y * V.Z;
   for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < N; r += (int64_t)gridDim.x * blockDim.x) {
-    if (parent[r] != r) {
-      target[r] = (int32_t)r;  // only roots are followed; keep the rest defined
-      continue;
-    }
+    md[r] = (int32_t)r;
+    if (first[r] != r) continue;
     int x, y, z;
     split_index(V, r, x, y, z);
     const int64_t nbr[6] = {x < V.X - 1 ? r + 1 : -1, x > 0 ? r - 1 : -1, y < V.Y - 1 ? r + V.X : -1,
                             y > 0 ? r - V.X : -1, z < V.Z - 1 ? r + V.X * V.Y : -1, z > 0 ? r - V.X * V.Y : -1};
-    int64_t earliest = r;
-    for (int j = 0; j < 6; j++) {
-      const int64_t u = nbr[j];
-      if (u < 0 || !comes_before(f, dir, u, r) || lab[u] == lab[r]) continue;
-      if (comes_before(f, dir, u, earliest)) earliest = u;
-    }
-    target[r] = parent[earliest];
+    bool any = false;
+    for (int j = 0; j < 6; j++) any |= nbr[j] >= 0 && comes_before(f, dir, nbr[j], r);
+    if (any) roots[atomicAdd(n_roots, 1)] = (int32_t)r;
   }
 }
 
-__global__ void clean_resolve_kernel(const int32_t* __restrict__ lab, const VolDims V, const int32_t* __restrict__ parent,
-                                     const int32_t* __restrict__ target, int32_t* __restrict__ out) {
+// The current root of x's component at root r's turn: joins made by roots visited
+// before r (smaller ids) are followed.
+__device__ __forceinline__ int32_t clean_current(const int32_t* md, int32_t x, int32_t r) {
+  for (int guard = 0; guard < (1 << 20) && x < r; guard++) {
+    const int32_t y = md[x];
+    if (y == x) break;
+    x = y;
+  }
+  return x;
+}
+
+// One relaxation sweep of the roots' decisions (each depends only on the decisions of
+// smaller roots, so the sweeps reach the reference's sequential outcome; *changed
+// counts the decisions that moved).
+__global__ void clean_sweep_kernel(const int32_t* __restrict__ lab, const float* __restrict__ f, const VolDims V, int dir,
+                                   const int32_t* __restrict__ first, int32_t* __restrict__ md,
+                                   const int32_t* __restrict__ roots, const int* __restrict__ n_roots,
+                                   int* __restrict__ changed) {
+  const int n = *n_roots;
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+    const int32_t r = roots[k];
+    int x, y, z;
+    split_index(V, r, x, y, z);
+    const int64_t nbr[6] = {x < V.X - 1 ? r + 1 : -1, x > 0 ? r - 1 : -1, y < V.Y - 1 ? r + V.X : -1,
+                            y > 0 ? r - V.X : -1, z < V.Z - 1 ? r + V.X * V.Y : -1, z > 0 ? r - V.X * V.Y : -1};
+    const int32_t reg = lab[r];
+    int64_t earliest = r;
+    for (int j = 0; j < 6; j++) {
+      const int64_t u = nbr[j];
+      if (u < 0 || !comes_before(f, dir, u, r)) continue;
+      if (lab[clean_current(md, first[u], r)] == reg) continue;
+      if (comes_before(f, dir, u, earliest)) earliest = u;
+    }
+    const int32_t t = earliest == r ? r : clean_current(md, first[earliest], r);
+    if (md[r] != t) {
+      md[r] = t;
+      atomicAdd(changed, 1);
+    }
+  }
+}
+
+__global__ void clean_resolve_kernel(const int32_t* __restrict__ lab, const VolDims V, const int32_t* __restrict__ first,
+                                     const int32_t* __restrict__ md, int32_t* __restrict__ out) {
   const int64_t N = V.X * V.Y * V.Z;
   for (int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v < N; v += (int64_t)gridDim.x * blockDim.x) {
-    int32_t r = parent[v];
-    for (int64_t guard = 0; guard < N && target[r] != r; guard++) r = target[r];  // strictly earlier each hop
+    int32_t r = first[v];
+    for (int64_t guard = 0; guard < N && md[r] != r; guard++) r = md[r];
     const int32_t l = lab[v];
     const int32_t lr = lab[r];
     // vertices that reached no region keep "none"; the rest take their final root's region
@@ -933,54 +1419,109 @@ int trips_per_turn() {
   static const int k = trips_env("MSC_TRIPS_PER_TURN", 16);
   return k;
 }
+namespace {
+int grid_for(int64_t n, int num_sms) {
+  const int64_t blocks = (n + 255) / 256;
+  return (int)(blocks < (int64_t)num_sms * 8 ? (blocks > 0 ? blocks : 1) : (int64_t)num_sms * 8);
+}
+}  // namespace
+
 static int trips_per_turn_pass1() {
   static const int k = trips_env("MSC_TRIPS_PER_TURN_PASS1", trips_per_turn());
   return k;
 }
 
-cudaError_t launch_integrate_pass1(const float4* G, const VolDims& V, const IntegParams& P, const SpreadOrder& S,
-                                   int32_t* lab, uint8_t* lvl, unsigned long long* work, unsigned long long* trips,
-                                   int32_t* items, unsigned long long* n_items, int num_sms, cudaStream_t stream) {
-  const int64_t N = V.X * V.Y * V.Z;
-  if (cudaError_t e = cudaMemsetAsync(work, 0, sizeof(unsigned long long) * 48, stream)) return e;
+cudaError_t launch_init_levels(const int32_t* lab, uint8_t* lvl, int64_t N, int num_sms, cudaStream_t stream) {
   ::msc::count_launch();
   init_levels_kernel<<<num_sms * 8, 256, 0, stream>>>(lab, lvl, N);
-  // the levels up to a total of N/512 items form the first group (a fraction of the
-  // volume small enough that their mutual path compression does not matter)
-  const int64_t small = N / 512;
-  int stamp = 0;
-  for (int L0 = 0; L0 < S.nlev;) {
-    int L1 = L0 + 1;
-    while (L1 < S.nlev && S.offset[L1 + 1] - S.offset[L0] <= small) L1++;
-    const int64_t count = S.offset[L1] - S.offset[L0];
-    const int g0 = L0;
-    L0 = L1;
-    if (count <= 0) continue;
-    const Adv32 A = Adv32::make(G, V, P, lvl, ++stamp, nullptr);
-    const int64_t blocks = (count + 127) / 128;
-    const int grid = (int)(blocks < num_sms * kLaneCtasPerSm ? blocks : num_sms * kLaneCtasPerSm);
-    unsigned long long* w = work + (stamp - 1);
-    if (cudaError_t e = cudaMemsetAsync(n_items, 0, sizeof(unsigned long long), stream)) return e;
-    ::msc::count_launch();
-    compact_level_kernel<<<grid, 128, 0, stream>>>(S, g0, L1, lvl, stamp, items, n_items);
-    ::msc::count_launch();
-    switch (trips_per_turn_pass1()) {
-      case 16:
-        integrate_level_kernel<16><<<grid, 128, 0, stream>>>(A, items, n_items, lab, lvl, w, trips);
-        break;
-      case 2:
-        integrate_level_kernel<2><<<grid, 128, 0, stream>>>(A, items, n_items, lab, lvl, w, trips);
-        break;
-      case 4:
-        integrate_level_kernel<4><<<grid, 128, 0, stream>>>(A, items, n_items, lab, lvl, w, trips);
-        break;
-      default:
-        integrate_level_kernel<8><<<grid, 128, 0, stream>>>(A, items, n_items, lab, lvl, w, trips);
-    }
-    char what[64];
-    std::snprintf(what, sizeof(what), "level %d-%d (%lld)", g0, L1 - 1, (long long)count);
-    ::msc::label_trace(stream, P.step_mult, what);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_spread_compact(const SpreadOrder& S, int64_t u0, int64_t u1, const uint8_t* lvl, int stamp,
+                                  int* counts, int32_t* items, unsigned long long* n_items, cudaStream_t stream) {
+  const int64_t nb = (u1 - u0 + kCompactBlock - 1) / kCompactBlock;
+  if (nb <= 0 || nb > 0x7FFFFFFF) return cudaErrorInvalidValue;
+  ::msc::count_launch();
+  spread_count_kernel<<<(unsigned)nb, kCompactThreads, 0, stream>>>(S, u0, u1, lvl, stamp, counts);
+  ::msc::count_launch();
+  scan_counts_kernel<<<1, 1024, 0, stream>>>(counts, nb, n_items);
+  ::msc::count_launch();
+  spread_write_kernel<<<(unsigned)nb, kCompactThreads, 0, stream>>>(S, u0, u1, lvl, stamp, counts, items);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_speculate(const float4* G, const VolDims& V, const IntegParams& P, const SpecSet& Q, int64_t k0,
+                             int64_t k1, const int32_t* lab, const uint8_t* lvl, int stamp, uint32_t* claim,
+                             unsigned long long* work, unsigned long long* trips, int num_sms, cudaStream_t stream) {
+  if (k1 <= k0) return cudaSuccess;
+  const Adv32 A = Adv32::make(G, V, P, lvl, stamp, nullptr);
+  const int64_t blocks = (k1 - k0 + 127) / 128;
+  const int grid = (int)(blocks < num_sms * kLaneCtasPerSm ? blocks : num_sms * kLaneCtasPerSm);
+  ::msc::count_launch();
+  switch (trips_per_turn_pass1()) {
+    case 2:
+      speculate_kernel<2><<<grid, 128, 0, stream>>>(A, Q, k0, k1, lab, claim, work, trips);
+      break;
+    case 4:
+      speculate_kernel<4><<<grid, 128, 0, stream>>>(A, Q, k0, k1, lab, claim, work, trips);
+      break;
+    case 8:
+      speculate_kernel<8><<<grid, 128, 0, stream>>>(A, Q, k0, k1, lab, claim, work, trips);
+      break;
+    default:
+      speculate_kernel<16><<<grid, 128, 0, stream>>>(A, Q, k0, k1, lab, claim, work, trips);
   }
+  return cudaGetLastError();
+}
+
+cudaError_t launch_spec_round(const SpecSet& Q, int64_t k0, int64_t k1, uint32_t* claim, const SpecDirty* cur,
+                              const SpecDirty& nxt, uint32_t* ibits, int64_t ibits_words, int num_sms,
+                              cudaStream_t stream) {
+  if (cudaError_t e = cudaMemsetAsync(nxt.n, 0, sizeof(unsigned long long), stream)) return e;
+  if (cudaError_t e = cudaMemsetAsync(nxt.bits, 0, nxt.words * sizeof(uint32_t), stream)) return e;
+  // the first round's claims were made by the speculation
+  if (cur) {
+    if (cudaError_t e = cudaMemsetAsync(ibits, 0, ibits_words * sizeof(uint32_t), stream)) return e;
+    ::msc::count_launch();
+    spec_reclaim_kernel<<<num_sms * 8, 256, 0, stream>>>(Q, cur->list, cur->n, claim);
+    ::msc::count_launch();
+    spec_holders_kernel<<<num_sms * 8, 256, 0, stream>>>(Q, k0, cur->list, cur->n, ibits);
+  }
+  ::msc::count_launch();
+  spec_check_kernel<<<grid_for(k1 - k0, num_sms), 256, 0, stream>>>(Q, k0, k1, claim, cur ? ibits : nullptr,
+                                                                    nxt.bits, nxt.list, nxt.n);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_spec_unclaim_all(const uint8_t* lvl, int stamp, uint32_t* claim, int64_t N, int num_sms,
+                                    cudaStream_t stream) {
+  ::msc::count_launch();
+  spec_unclaim_all_kernel<<<num_sms * 8, 256, 0, stream>>>(lvl, stamp, claim, N);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_spec_ptr(const SpecSet& Q, int64_t k0, int64_t k1, const uint32_t* claim, int num_sms,
+                            cudaStream_t stream) {
+  ::msc::count_launch();
+  spec_ptr_kernel<<<grid_for(k1 - k0, num_sms), 256, 0, stream>>>(Q, k0, k1, claim);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_spec_jumps(const SpecSet& Q, int64_t k0, int64_t k1, int num_sms, cudaStream_t stream) {
+  // every chain of cut items ends at an uncut one within log2 steps
+  int jumps = 1;
+  for (int64_t n = k1 - k0; n > 1; n >>= 1) jumps++;
+  for (int j = 0; j < jumps; j++) {
+    ::msc::count_launch();
+    spec_jump_kernel<<<grid_for(k1 - k0, num_sms), 256, 0, stream>>>(Q, k0, k1);
+  }
+  return cudaGetLastError();
+}
+
+cudaError_t launch_spec_write(const SpecSet& Q, int64_t k0, int64_t k1, uint8_t* lvl, int stamp, const uint32_t* claim,
+                              int32_t* lab, int* long_chain, int num_sms, cudaStream_t stream) {
+  ::msc::count_launch();
+  spec_write_kernel<<<grid_for(k1 - k0, num_sms), 256, 0, stream>>>(Q, k0, k1, lvl, stamp, claim, lab, long_chain);
   return cudaGetLastError();
 }
 
@@ -991,9 +1532,9 @@ cudaError_t launch_boundary_set(const int32_t* lab, const uint8_t* state, const 
   return cudaGetLastError();
 }
 
-cudaError_t launch_fixup(const double* G, const VolDims& V, const IntegParams& P, int32_t* lab, const int32_t* lab0,
-                         uint8_t* state, const int64_t* list, int n, int64_t* next, int* n_next, uint32_t* queued,
-                         unsigned long long* work, unsigned long long* trips, int num_sms, cudaStream_t stream) {
+cudaError_t launch_fixup_end64(const double* G, const VolDims& V, const IntegParams& P, const uint8_t* state,
+                               const int64_t* list, int n, int32_t* endv, unsigned long long* work,
+                               unsigned long long* trips, int num_sms, cudaStream_t stream) {
   if (n <= 0) return cudaSuccess;
   Adv64 A{G, V, P, state};
   const int blocks = (n + 31) / 32;
@@ -1002,33 +1543,30 @@ cudaError_t launch_fixup(const double* G, const VolDims& V, const IntegParams& P
   // one-warp CTAs, at most four per SM: the FP64 re-decisions are few (~0.1% of the
   // re-decisions) and bound by each SM's FP64 pipe, which executes every warp
   // instruction in full however few lanes are active -- so a small wave is spread over
-  // as many SMs as it has warps, and a large one keeps a few items per lane (512^3
-  // labels: 1.10 s with 16 CTAs of 128 per SM, 1.07 s with one)
+  // as many SMs as it has warps, and a large one keeps a few items per lane
   // iterations per turn: MSC_TRIPS_PER_TURN_FP64 (2, 4, 8 or 16) overrides the default
-  // (512^3 k^-3 labels: the same time for 2, 8 and 16 -- the FP64 waves are as long as
-  // their slowest streamline, not bound by the hand-out)
   static const int k = trips_env("MSC_TRIPS_PER_TURN_FP64", 2);
   const int grid = blocks < num_sms * 4 ? blocks : num_sms * 4;
   switch (k) {
     case 4:
-      fixup_kernel<4><<<grid, 32, 0, stream>>>(A, lab, lab0, state, list, n, next, n_next, queued, work, trips);
+      fixup_end64_kernel<4><<<grid, 32, 0, stream>>>(A, list, n, endv, work, trips);
       break;
     case 16:
-      fixup_kernel<16><<<grid, 32, 0, stream>>>(A, lab, lab0, state, list, n, next, n_next, queued, work, trips);
+      fixup_end64_kernel<16><<<grid, 32, 0, stream>>>(A, list, n, endv, work, trips);
       break;
     case 8:
-      fixup_kernel<8><<<grid, 32, 0, stream>>>(A, lab, lab0, state, list, n, next, n_next, queued, work, trips);
+      fixup_end64_kernel<8><<<grid, 32, 0, stream>>>(A, list, n, endv, work, trips);
       break;
     default:
-      fixup_kernel<2><<<grid, 32, 0, stream>>>(A, lab, lab0, state, list, n, next, n_next, queued, work, trips);
+      fixup_end64_kernel<2><<<grid, 32, 0, stream>>>(A, list, n, endv, work, trips);
   }
   return cudaGetLastError();
 }
 
-cudaError_t launch_fixup32(const float4* G, const VolDims& V, const IntegParams& P, int32_t* lab, const int32_t* lab0,
-                           uint8_t* state, const int64_t* list, int n, int64_t* next, int* n_next, uint32_t* queued,
-                           int64_t* amb, int* n_amb, int amb_mode, unsigned long long* work,
-                           unsigned long long* trips, int num_sms, cudaStream_t stream) {
+cudaError_t launch_fixup_end32(const float4* G, const VolDims& V, const IntegParams& P, const int32_t* lab,
+                               const uint8_t* state, const int64_t* list, int n, int32_t* endv, int64_t* amb,
+                               int* n_amb, int amb_mode, unsigned long long* work, unsigned long long* trips,
+                               int num_sms, cudaStream_t stream) {
   if (n <= 0) return cudaSuccess;
   const Adv32 A = Adv32::make(G, V, P, nullptr, 0, state);
   const int blocks = (n + 127) / 128;
@@ -1037,39 +1575,78 @@ cudaError_t launch_fixup32(const float4* G, const VolDims& V, const IntegParams&
   const int grid = blocks < num_sms * kLaneCtasPerSm ? blocks : num_sms * kLaneCtasPerSm;
   switch (trips_per_turn()) {
     case 16:
-      fixup32_kernel<16><<<grid, 128, 0, stream>>>(A, lab, lab0, state, list, n, next, n_next, queued, amb,
-                                                     n_amb, amb_mode, work, trips);
+      fixup_end32_kernel<16><<<grid, 128, 0, stream>>>(A, lab, state, list, n, endv, amb, n_amb, amb_mode, work, trips);
       break;
     case 2:
-      fixup32_kernel<2><<<grid, 128, 0, stream>>>(A, lab, lab0, state, list, n, next, n_next, queued, amb,
-                                                     n_amb, amb_mode, work, trips);
+      fixup_end32_kernel<2><<<grid, 128, 0, stream>>>(A, lab, state, list, n, endv, amb, n_amb, amb_mode, work, trips);
       break;
     case 4:
-      fixup32_kernel<4><<<grid, 128, 0, stream>>>(A, lab, lab0, state, list, n, next, n_next, queued, amb,
-                                                     n_amb, amb_mode, work, trips);
+      fixup_end32_kernel<4><<<grid, 128, 0, stream>>>(A, lab, state, list, n, endv, amb, n_amb, amb_mode, work, trips);
       break;
     default:
-      fixup32_kernel<8><<<grid, 128, 0, stream>>>(A, lab, lab0, state, list, n, next, n_next, queued, amb,
-                                                     n_amb, amb_mode, work, trips);
+      fixup_end32_kernel<8><<<grid, 128, 0, stream>>>(A, lab, state, list, n, endv, amb, n_amb, amb_mode, work, trips);
   }
   return cudaGetLastError();
 }
 
-cudaError_t launch_clean(const int32_t* lab, const float* f, const VolDims& V, int dir, int32_t* parent, int32_t* target,
-                         int32_t* out, int num_sms, cudaStream_t stream) {
+cudaError_t launch_wave_mark(const int64_t* list, int n, int w, int32_t* inw, uint32_t* queued, const int32_t* endv,
+                             int64_t* todo, int* n_todo, int num_sms, cudaStream_t stream) {
+  if (n <= 0) return cudaSuccess;
+  ::msc::count_launch();
+  wave_mark_kernel<<<grid_for(n, num_sms), 256, 0, stream>>>(list, n, w, inw, queued, endv, todo, n_todo);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_wave_decide(const int64_t* list, int n, int w, const VolDims& V, const int32_t* endv,
+                               const int32_t* inw, int32_t* lab, uint8_t* state, int32_t* rptr, int32_t* rval,
+                               uint32_t* queued, int64_t* next, int* n_next, int num_sms, cudaStream_t stream) {
+  if (n <= 0) return cudaSuccess;
+  const int grid = grid_for(n, num_sms);
+  ::msc::count_launch();
+  wave_root_kernel<<<grid, 256, 0, stream>>>(list, n, w, endv, inw, lab, state, rptr, rval);
+  int jumps = 1;
+  for (int m = n; m > 1; m >>= 1) jumps++;
+  for (int j = 0; j < jumps; j++) {
+    ::msc::count_launch();
+    wave_jump_kernel<<<grid, 256, 0, stream>>>(list, n, rptr);
+  }
+  ::msc::count_launch();
+  wave_enqueue_kernel<<<grid, 256, 0, stream>>>(list, n, w, V, rptr, rval, lab, state, inw, queued, next, n_next);
+  ::msc::count_launch();
+  wave_apply_kernel<<<grid, 256, 0, stream>>>(list, n, rptr, rval, lab, state);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_clean(const int32_t* lab, const float* f, const VolDims& V, int dir, int32_t* parent, int32_t* first,
+                         int32_t* md, int32_t* roots, int* counters, int* pinned, int32_t* out, int num_sms,
+                         cudaStream_t stream, int* sweeps_out) {
   const int64_t N = V.X * V.Y * V.Z;
   const int grid = num_sms * 8;
   ::msc::count_launch();
   uf_init_kernel<<<grid, 256, 0, stream>>>(parent, N);
   ::msc::count_launch();
   uf_hook_kernel<<<grid, 256, 0, stream>>>(lab, f, V, dir, parent);
-  // roots into `target`; from there on `target` holds the roots and `parent` the merge targets
   ::msc::count_launch();
-  uf_roots_kernel<<<grid, 256, 0, stream>>>(parent, target, N);
+  uf_roots_kernel<<<grid, 256, 0, stream>>>(parent, first, N);
+  if (cudaError_t e = cudaMemsetAsync(counters, 0, 2 * sizeof(int), stream)) return e;
   ::msc::count_launch();
-  clean_target_kernel<<<grid, 256, 0, stream>>>(lab, f, V, dir, target, parent);
+  clean_roots_kernel<<<grid, 256, 0, stream>>>(lab, f, V, dir, first, md, roots, counters);
+  // sweeps until no decision moves (after sweep s the s smallest deciding roots are
+  // final; in practice a few sweeps), the count read through `pinned`
+  int sweeps = 0;
+  for (;;) {
+    if (cudaError_t e = cudaMemsetAsync(counters + 1, 0, sizeof(int), stream)) return e;
+    ::msc::count_launch();
+    clean_sweep_kernel<<<num_sms * 4, 256, 0, stream>>>(lab, f, V, dir, first, md, roots, counters, counters + 1);
+    if (cudaError_t e = cudaMemcpyAsync(pinned, counters + 1, sizeof(int), cudaMemcpyDeviceToHost, stream)) return e;
+    if (cudaError_t e = cudaStreamSynchronize(stream)) return e;
+    sweeps++;
+    if (*pinned == 0) break;
+    if (sweeps > N + 1) return cudaErrorUnknown;
+  }
+  if (sweeps_out) *sweeps_out = sweeps;
   ::msc::count_launch();
-  clean_resolve_kernel<<<grid, 256, 0, stream>>>(lab, V, target, parent, out);
+  clean_resolve_kernel<<<grid, 256, 0, stream>>>(lab, V, first, md, out);
   return cudaGetLastError();
 }
 

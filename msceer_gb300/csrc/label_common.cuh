@@ -116,23 +116,101 @@ struct SpreadOrder {
   int64_t start[48], stride[48], offset[49];
 };
 
-// `work`: 48 device counters (the levels' claimed items), zeroed here.  `trips`
-// (here and below): a device counter the kernels add their advection iterations to.
-// `items`: scratch for the largest level's vertices, `n_items` a device counter.
-cudaError_t launch_integrate_pass1(const float4* G, const VolDims& V, const IntegParams& P, const SpreadOrder& S,
-                                   int32_t* lab, uint8_t* lvl, unsigned long long* work, unsigned long long* trips,
-                                   int32_t* items, unsigned long long* n_items, int num_sms, cudaStream_t stream);
+// The first pass runs the spread order in batches (a group of levels, or part of one):
+// speculative streamlines of the batch's items record the vertices their stop test
+// passed, and the resolution kernels turn them into the labels the one-thread
+// reference assigns (integrate_kernels.cu).  SpecSet: the batch's items in visiting
+// order, their recorded sequences and the holder lists of the recorded vertices.
+struct SpecSet {
+  const int32_t* vtx;  // item vertex (its entry 0)
+  uint32_t* e1;        // entry 1
+  uint32_t* head;      // word offset in pool of the segment that holds entries 2, 3, ...
+  int32_t* len;        // recorded entries (0: the item was skipped)
+  int32_t* endlab;     // label where the streamline stopped, if labelled before the batch
+  int32_t* cut;        // -1, or the entry where an earlier item's path stops it
+  int32_t* ptr;        // the item whose label it takes
+  uint8_t* alive;      // runs (no earlier item labelled its vertex)
+  uint32_t* pool;      // entry segments
+  unsigned long long pool_words;
+  unsigned long long* cursor;  // next free pool word
+  int* overflow;               // set when the pool or the holder nodes ran out (the batch is redone smaller)
+  // holders: for every vertex the list of (item, entry index) that recorded it
+  int32_t* hhead;              // per vertex: its first holder node, -1 for none
+  int32_t* hitem;              // per node: the item
+  uint32_t* hidx;              // per node: the entry index, kRec-flagged for path vertices
+  int32_t* hnext;              // per node: the vertex's next node
+  unsigned long long node_cap;
+  unsigned long long* ncursor;  // next free node
+};
+// lvl: 0 for labelled vertices, 255 for the rest
+cudaError_t launch_init_levels(const int32_t* lab, uint8_t* lvl, int64_t N, int num_sms, cudaStream_t stream);
+// The vertices of spread positions [u0, u1) with lvl >= stamp, in order, into items;
+// their number to *n_items.  counts: (u1 - u0) / 1024 + 1 ints of scratch.
+cudaError_t launch_spread_compact(const SpreadOrder& S, int64_t u0, int64_t u1, const uint8_t* lvl, int stamp,
+                                  int* counts, int32_t* items, unsigned long long* n_items, cudaStream_t stream);
+// Speculative streamlines of items [k0, k1) (stopping at lvl < stamp); they build the
+// holder lists (hhead all -1 at launch) and make the first resolution round's claims.
+// `work`: a device counter, zero at launch; `trips`: advection iterations are added to it.
+cudaError_t launch_speculate(const float4* G, const VolDims& V, const IntegParams& P, const SpecSet& Q, int64_t k0,
+                             int64_t k1, const int32_t* lab, const uint8_t* lvl, int stamp, uint32_t* claim,
+                             unsigned long long* work, unsigned long long* trips, int num_sms, cudaStream_t stream);
+// After a pool overflow: drops the claims on vertices with lvl >= stamp.
+cudaError_t launch_spec_unclaim_all(const uint8_t* lvl, int stamp, uint32_t* claim, int64_t N, int num_sms,
+                                    cudaStream_t stream);
+// Vertices whose claims a resolution round recomputes: a bitmap (words uint32) and the
+// list of its set bits (*n entries).
+struct SpecDirty {
+  uint32_t* bits;
+  int64_t words;
+  uint32_t* list;
+  unsigned long long* n;
+};
+// Resolution rounds of items [k0, k1).  The first (cur == nullptr) looks at every item
+// (the speculation made its claims); a later one recomputes the claims of cur's
+// vertices from their holders and looks at the items that hold one of them (ibits: a
+// bitmap over the items, ibits_words words, cleared here).  An item whose alive / cut
+// changed marks the path vertices between its old and new extent in nxt (cleared here
+// first).  The rounds end when a round marks nothing.
+cudaError_t launch_spec_round(const SpecSet& Q, int64_t k0, int64_t k1, uint32_t* claim, const SpecDirty* cur,
+                              const SpecDirty& nxt, uint32_t* ibits, int64_t ibits_words, int num_sms,
+                              cudaStream_t stream);
+// Labels of the resolved batch [k0, k1), stamping its vertices with `stamp`: ptr, then
+// the write, which sets *long_chain (and writes nothing for that item) where a chain
+// of cut items is longer than it follows; pointer jumping then shortens the chains.
+cudaError_t launch_spec_ptr(const SpecSet& Q, int64_t k0, int64_t k1, const uint32_t* claim, int num_sms,
+                            cudaStream_t stream);
+cudaError_t launch_spec_jumps(const SpecSet& Q, int64_t k0, int64_t k1, int num_sms, cudaStream_t stream);
+cudaError_t launch_spec_write(const SpecSet& Q, int64_t k0, int64_t k1, uint8_t* lvl, int stamp, const uint32_t* claim,
+                              int32_t* lab, int* long_chain, int num_sms, cudaStream_t stream);
 cudaError_t launch_boundary_set(const int32_t* lab, const uint8_t* state, const VolDims& V, int64_t* list, int* n,
                                 uint32_t* queued, int num_sms, cudaStream_t stream);
-// `work`: a device counter of claimed items, zeroed by the launchers
-cudaError_t launch_fixup(const double* G, const VolDims& V, const IntegParams& P, int32_t* lab, const int32_t* lab0,
-                         uint8_t* state, const int64_t* list, int n, int64_t* next, int* n_next, uint32_t* queued,
-                         unsigned long long* work, unsigned long long* trips, int num_sms, cudaStream_t stream);
-cudaError_t launch_fixup32(const float4* G, const VolDims& V, const IntegParams& P, int32_t* lab, const int32_t* lab0,
-                           uint8_t* state, const int64_t* list, int n, int64_t* next, int* n_next, uint32_t* queued,
-                           int64_t* amb, int* n_amb, int amb_mode, unsigned long long* work,
-                           unsigned long long* trips, int num_sms, cudaStream_t stream);
-cudaError_t launch_clean(const int32_t* lab, const float* f, const VolDims& V, int dir, int32_t* parent, int32_t* target,
-                         int32_t* out, int num_sms, cudaStream_t stream);
+// Fix-up streamline ends (FP64 / FP32): endv[v] = the final nearest vertex of v's
+// streamline to a certain terminal region.  The FP32 kernel lists the streamlines whose
+// ending is ambiguous in amb (amb_mode: see the kernel) instead.  `work`: a device
+// counter of claimed items, zeroed by the launchers.
+cudaError_t launch_fixup_end64(const double* G, const VolDims& V, const IntegParams& P, const uint8_t* state,
+                               const int64_t* list, int n, int32_t* endv, unsigned long long* work,
+                               unsigned long long* trips, int num_sms, cudaStream_t stream);
+cudaError_t launch_fixup_end32(const float4* G, const VolDims& V, const IntegParams& P, const int32_t* lab,
+                               const uint8_t* state, const int64_t* list, int n, int32_t* endv, int64_t* amb,
+                               int* n_amb, int amb_mode, unsigned long long* work, unsigned long long* trips,
+                               int num_sms, cudaStream_t stream);
+// Fix-up wave w over `list`: stamps the members in inw, clears their queued bits and
+// lists the members without an end yet in todo (n_todo: a device counter).
+cudaError_t launch_wave_mark(const int64_t* list, int n, int w, int32_t* inw, uint32_t* queued, const int32_t* endv,
+                             int64_t* todo, int* n_todo, int num_sms, cudaStream_t stream);
+// Decides wave w in the reference's order (every member has its end), reopens
+// neighbours into next (n_next: a device counter) and writes the labels.
+cudaError_t launch_wave_decide(const int64_t* list, int n, int w, const VolDims& V, const int32_t* endv,
+                               const int32_t* inw, int32_t* lab, uint8_t* state, int32_t* rptr, int32_t* rval,
+                               uint32_t* queued, int64_t* next, int* n_next, int num_sms, cudaStream_t stream);
+// IsolatedCCRegionRemoverNEW::ComputeOutput: same-label components, then the reference's
+// vertex-ordered joins of the components without their region's extremum.  parent,
+// first, md, roots: N int32 of scratch each; counters: 2 ints; pinned: one int of
+// pinned host memory (the sweep count is read through it; the call synchronises
+// `stream` once per sweep).  sweeps_out (optional): sweeps made.
+cudaError_t launch_clean(const int32_t* lab, const float* f, const VolDims& V, int dir, int32_t* parent, int32_t* first,
+                         int32_t* md, int32_t* roots, int* counters, int* pinned, int32_t* out, int num_sms,
+                         cudaStream_t stream, int* sweeps_out);
 
 }  // namespace msc

@@ -115,6 +115,11 @@ __global__ void terminal_state_kernel(const int32_t* lab, uint8_t* state, int64_
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
     if (state[i] != msc::kStSeed) state[i] = lab[i] >= 0 ? msc::kStTerminal : msc::kStUnassigned;
 }
+// caller labels into the internal form: the reference's -1 ("none") reads as kLabelNone
+__global__ void none_in_kernel(const int32_t* in, int32_t* lab, int64_t n) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    lab[i] = in[i] == -1 ? msc::kLabelNone : in[i];
+}
 // stage snapshot: internal "reached no region" reads as the reference's -1
 __global__ void snapshot_kernel(const int32_t* lab, int32_t* out, int64_t n) {
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
@@ -277,13 +282,13 @@ struct LabelCtx {
   double* g64 = nullptr;
   int32_t* key = nullptr;
   int64_t *ext_cells = nullptr, *saddles = nullptr, *list_a = nullptr, *list_b = nullptr, *amb = nullptr;
-  int64_t *list_c = nullptr, *amb2 = nullptr;  // the FP64 re-decisions' reopened vertices; second ambiguous list
+  int64_t* list_c = nullptr;  // a fix-up wave's members without a streamline end yet
   uint32_t* queued = nullptr;
   uint8_t* tiles = nullptr;
-  int* counters = nullptr;  // [0] n_ext [1] n_sad [2] n_arcs [3] changed [4] err [5] n_list [6] n_next [7] n_amb
-                            // [8] FP64 reopened
-  unsigned long long* work = nullptr;  // [0, 48) claimed work items, [48, 51) advection iterations,
-                                       // [52] level items, [56] FP64 claims
+  int* counters = nullptr;  // [0] n_ext [1] n_sad [2] n_arcs [3] changed [4] err [5] n_list / wave members
+                            // without an end [6] n_next [7] n_amb [8, 10) cleaner
+  unsigned long long* work = nullptr;  // [0] claimed fix-up items, [48, 51) advection iterations (first
+                                       // pass, FP32, FP64), [56] FP64 claims
   void* hpin = nullptr;                // kPinnedBytes of pinned host memory (pinned_get)
   explicit LabelCtx(cudaStream_t s) : st(s), pool(s) {}
   ~LabelCtx() {
@@ -343,7 +348,6 @@ int setup_ctx(LabelCtx& c, const float* f, const uint8_t* grad, const int64_t* d
   LCUDA(c.pool.get(&c.list_a, N), "alloc");
   LCUDA(c.pool.get(&c.list_b, N), "alloc");
   LCUDA(c.pool.get(&c.amb, N), "alloc");
-  LCUDA(c.pool.get(&c.amb2, N), "alloc");
   LCUDA(c.pool.get(&c.list_c, N), "alloc");
   LCUDA(c.pool.get(&c.queued, N / 32 + 1), "alloc");
   LCUDA(c.pool.get(&c.tiles, 2 * c.ntiles), "alloc");
@@ -513,8 +517,11 @@ msc::IntegParams integ_params(const msc_integ_params* p, int dir) {
   return P;
 }
 
-// First integration pass of the vertices still unassigned (-1), deterministic, in
-// the reference's spread order, after zeroing the gradient at this direction's seeds.
+// First integration pass of the vertices still unassigned (-1), after zeroing the
+// gradient at this direction's seeds: the reference's spread order with one thread, run
+// as batches (a group of levels, or part of one) of speculative streamlines whose
+// resolution gives exactly the sequential outcome (integrate_kernels.cu).  A batch whose
+// recorded sequences do not fit their pools is redone as two halves.
 int first_pass(LabelCtx& c, DirLabels& d) {
   const int64_t N = c.N;
   cudaStream_t st = c.st;
@@ -535,14 +542,126 @@ int first_pass(LabelCtx& c, DirLabels& d) {
     S.nlev++;
   }
   uint8_t* lvl;
+  uint32_t* claim;
+  int* counts;
+  int32_t* vtx;
+  uint32_t* ibits;
+  unsigned long long* sc;  // [0] pool cursor [1] items [3] claimed items [4, 6) dirty-list lengths
+                           // [6] holder-node cursor
+  msc::SpecSet Q{};
+  const int64_t max_items = std::min<int64_t>(N, S.offset[S.nlev]);
+  const int64_t ibits_cap = max_items / 32 + 1;
+  Q.pool_words = std::min<unsigned long long>(2ull * (unsigned long long)N + (1ull << 20), 0xFFFFFF00ull);
+  Q.node_cap = std::min<unsigned long long>(3ull * (unsigned long long)N + (1ull << 20), 0x7FFFFF00ull);
   LCUDA(c.pool.get(&lvl, N), "alloc");
+  LCUDA(c.pool.get(&claim, N), "alloc");
+  LCUDA(c.pool.get(&counts, S.offset[S.nlev] / 1024 + 2), "alloc");
+  LCUDA(c.pool.get(&vtx, max_items), "alloc");
+  LCUDA(c.pool.get(&Q.e1, max_items), "alloc");
+  LCUDA(c.pool.get(&Q.head, max_items), "alloc");
+  LCUDA(c.pool.get(&Q.len, max_items), "alloc");
+  LCUDA(c.pool.get(&Q.endlab, max_items), "alloc");
+  LCUDA(c.pool.get(&Q.cut, max_items), "alloc");
+  LCUDA(c.pool.get(&Q.ptr, max_items), "alloc");
+  LCUDA(c.pool.get(&Q.alive, max_items), "alloc");
+  LCUDA(c.pool.get(&Q.pool, Q.pool_words), "alloc");
+  LCUDA(c.pool.get(&Q.hhead, N), "alloc");
+  LCUDA(c.pool.get(&Q.hitem, Q.node_cap), "alloc");
+  LCUDA(c.pool.get(&Q.hidx, Q.node_cap), "alloc");
+  LCUDA(c.pool.get(&Q.hnext, Q.node_cap), "alloc");
+  LCUDA(c.pool.get(&ibits, ibits_cap), "alloc");
+  LCUDA(c.pool.get(&sc, 7), "alloc");
+  LCUDA(c.pool.get(&Q.overflow, 1), "alloc");
+  msc::SpecDirty dirty[2];
+  for (int q = 0; q < 2; q++) {
+    dirty[q].words = N / 32 + 1;
+    dirty[q].n = sc + 4 + q;
+    LCUDA(c.pool.get(&dirty[q].bits, dirty[q].words), "alloc");
+    LCUDA(c.pool.get(&dirty[q].list, N), "alloc");
+  }
+  Q.vtx = vtx;
+  Q.cursor = sc;
+  Q.ncursor = sc + 6;
+  LCUDA(cudaMemsetAsync(claim, 0xFF, (size_t)N * sizeof(uint32_t), st), "memset");
   LCUDA(cudaMemsetAsync(c.work + 48, 0, 3 * sizeof(unsigned long long), st), "memset");
-  // the fix-up's list buffer (N int64) holds a level's vertices (at most N) meanwhile
+  LCUDA(msc::launch_init_levels(d.lab, lvl, N, c.sms, st), "levels");
   trace_mark(st, d.dir, "pass1 start");
-  LCUDA(msc::launch_integrate_pass1(c.g32, c.V, P, S, d.lab, lvl, c.work, c.work + 48,
-                                    reinterpret_cast<int32_t*>(c.list_a), c.work + 52, c.sms, st),
-        "integrate");
-  trace_mark(st, d.dir, "pass1");
+  // the levels up to N/512 visits together form the first batch; every later level is a
+  // batch of its own
+  const int64_t small = N / 512;
+  int stamp = 0;
+  int64_t rounds_total = 0, batches = 0;
+  auto next_stamp = [&]() -> int {
+    if (stamp >= 250) {  // stamps run out: every labelled vertex back to 0
+      LCUDA(msc::launch_init_levels(d.lab, lvl, N, c.sms, st), "levels");
+      stamp = 0;
+    }
+    ++stamp;
+    return MSC_OK;
+  };
+  for (int L0 = 0; L0 < S.nlev;) {
+    int L1 = L0 + 1;
+    while (L1 < S.nlev && S.offset[L1 + 1] - S.offset[L0] <= small) L1++;
+    const int64_t u0 = S.offset[L0], u1 = S.offset[L1];
+    const int g0 = L0;
+    L0 = L1;
+    if (u1 <= u0) continue;
+    if (int rc = next_stamp()) return rc;
+    LCUDA(msc::launch_spread_compact(S, u0, u1, lvl, stamp, counts, vtx, sc + 1, st), "compact");
+    unsigned long long n_items = 0;
+    if (int rc = read_dev(c, sc + 1, 1, &n_items)) return rc;
+    const int64_t n = (int64_t)n_items;
+    for (int64_t k0 = 0; k0 < n;) {
+      if (k0 > 0)
+        if (int rc = next_stamp()) return rc;
+      int64_t k1 = n;
+      for (;;) {
+        LCUDA(cudaMemsetAsync(sc, 0, sizeof(unsigned long long), st), "memset");
+        LCUDA(cudaMemsetAsync(sc + 3, 0, sizeof(unsigned long long), st), "memset");
+        LCUDA(cudaMemsetAsync(sc + 6, 0, sizeof(unsigned long long), st), "memset");
+        LCUDA(cudaMemsetAsync(Q.hhead, 0xFF, (size_t)N * sizeof(int32_t), st), "memset");
+        LCUDA(cudaMemsetAsync(Q.overflow, 0, sizeof(int), st), "memset");
+        LCUDA(msc::launch_speculate(c.g32, c.V, P, Q, k0, k1, d.lab, lvl, stamp, claim, sc + 3, c.work + 48, c.sms,
+                                    st),
+              "speculate");
+        int ovf = 0;
+        if (int rc = read_dev(c, Q.overflow, 1, &ovf)) return rc;
+        if (!ovf) break;
+        LCUDA(msc::launch_spec_unclaim_all(lvl, stamp, claim, N, c.sms, st), "unclaim");
+        if (k1 - k0 <= 1) return fail(MSC_ERR_OOM, "first pass: one streamline's record exceeds its pool");
+        k1 = k0 + (k1 - k0) / 2;
+      }
+      trace_mark(st, d.dir, "  speculated " + std::to_string(k1 - k0));
+      // resolution rounds: the first looks at every item, a later one at the items that
+      // hold a vertex whose claim may have changed; they end when a round changes no claim
+      for (int64_t r = 0;; r++) {
+        if (r > k1 - k0 + 2) return fail(MSC_ERR_ITER_LIMIT, "first-pass resolution did not converge");
+        LCUDA(msc::launch_spec_round(Q, k0, k1, claim, r == 0 ? nullptr : &dirty[r & 1], dirty[(r + 1) & 1], ibits,
+                                     (k1 - k0) / 32 + 1, c.sms, st),
+              "resolve");
+        unsigned long long nd = 0;
+        if (int rc = read_dev(c, dirty[(r + 1) & 1].n, 1, &nd)) return rc;
+        rounds_total++;
+        if (r == 0) trace_mark(st, d.dir, "  round 1: " + std::to_string(nd) + " dirty");
+        if (nd == 0) break;
+      }
+      trace_mark(st, d.dir, "  resolved");
+      LCUDA(msc::launch_spec_ptr(Q, k0, k1, claim, c.sms, st), "label");
+      LCUDA(cudaMemsetAsync(Q.overflow, 0, sizeof(int), st), "memset");
+      LCUDA(msc::launch_spec_write(Q, k0, k1, lvl, stamp, claim, d.lab, Q.overflow, c.sms, st), "label");
+      int long_chain = 0;
+      if (int rc = read_dev(c, Q.overflow, 1, &long_chain)) return rc;
+      if (long_chain) {  // a few long chains of cut items: jump, then write again
+        LCUDA(msc::launch_spec_jumps(Q, k0, k1, c.sms, st), "label");
+        LCUDA(msc::launch_spec_write(Q, k0, k1, lvl, stamp, claim, d.lab, Q.overflow, c.sms, st), "label");
+      }
+      batches++;
+      trace_mark(st, d.dir, "batch " + std::to_string(g0) + "-" + std::to_string(L1 - 1) + " items " +
+                                std::to_string(k1 - k0) + " rounds " + std::to_string(rounds_total));
+      k0 = k1;
+    }
+  }
+  trace_mark(st, d.dir, "pass1 (" + std::to_string(batches) + " batches, " + std::to_string(rounds_total) + " rounds)");
   return MSC_OK;
 }
 
@@ -556,17 +675,19 @@ int finish_direction(LabelCtx& c, DirLabels& d, int32_t* out, int32_t* stage_int
   const int sms = c.sms;
   const msc::IntegParams P = integ_params(p, d.dir);
 
-  // fix-up waves until no label changes reopen a neighbour: FP32 re-decisions, and
-  // FP64 ones for the streamlines whose FP32 ending was ambiguous; decisions read the
-  // first-pass labels (lab0).  The ambiguous streamlines wait (their vertices keep
-  // their queued bit) until the FP32 waves run dry, then go through FP64 together --
-  // a few FP64 launches per direction instead of one per wave, each as long as its
-  // longest streamline.  The order changes nothing: a decision reads lab0 only, and a
-  // changed vertex reopens a neighbour u exactly when u is undecided with lab0[u] !=
-  // the new label, so the set of re-decided vertices is the same closure.
-  int32_t* lab0;
-  LCUDA(c.pool.get(&lab0, N), "alloc");
-  LCUDA(cudaMemcpyAsync(lab0, d.lab, N * sizeof(int32_t), cudaMemcpyDeviceToDevice, st), "copy");
+  // fix-up waves until no decision reopens a neighbour (:316-415).  Each wave first
+  // integrates its members that have no streamline end yet -- in FP32, and the ones whose
+  // FP32 ending is ambiguous again in FP64 (or all in FP64: precision 1) -- then decides
+  // the wave in the reference's one-thread order (integrate_kernels.cu, wave kernels).
+  // An end does not depend on labels, so a vertex decided in several waves integrates
+  // once.
+  int32_t *endv, *inw, *rptr, *rval;
+  LCUDA(c.pool.get(&endv, N), "alloc");
+  LCUDA(c.pool.get(&inw, N), "alloc");
+  LCUDA(c.pool.get(&rptr, N), "alloc");
+  LCUDA(c.pool.get(&rval, N), "alloc");
+  LCUDA(cudaMemsetAsync(endv, 0xFF, N * sizeof(int32_t), st), "memset");
+  LCUDA(cudaMemsetAsync(inw, 0xFF, N * sizeof(int32_t), st), "memset");
   LCUDA(cudaMemsetAsync(c.queued, 0, (N / 32 + 1) * sizeof(uint32_t), st), "memset");
   LCUDA(cudaMemsetAsync(c.counters + 5, 0, 3 * sizeof(int), st), "memset");
   LCUDA(msc::launch_boundary_set(d.lab, d.state, V, c.list_a, c.counters + 5, c.queued, sms, st), "boundary set");
@@ -576,90 +697,36 @@ int finish_direction(LabelCtx& c, DirLabels& d, int32_t* out, int32_t* stage_int
   if (p->precision == 3) n_list = 0;  // first pass only
   int64_t* cur = c.list_a;
   int64_t* nxt = c.list_b;
+  int64_t* todo = c.list_c;
   stats[0] = stats[1] = 0;
-  int n_amb = 0;  // ambiguous streamlines waiting for FP64 (counters[7] on the device)
-  if (p->precision == 1) {
-    // all re-decisions in FP64, wave by wave
-    for (int64_t waves = 0; n_list > 0; waves++) {
-      if (waves > 2 * N + 2) return fail(MSC_ERR_ITER_LIMIT, "fix-up did not converge");
-      LCUDA(cudaMemsetAsync(c.counters + 6, 0, sizeof(int), st), "memset");
-      LCUDA(msc::launch_fixup(c.g64, V, P, d.lab, lab0, d.state, cur, n_list, nxt, c.counters + 6, c.queued, c.work,
-                              c.work + 50, sms, st),
+  for (int w = 0; n_list > 0; w++) {
+    if (w > 2 * N + 2) return fail(MSC_ERR_ITER_LIMIT, "fix-up did not converge");
+    // counters: [5] todo, [6] next wave, [7] ambiguous
+    LCUDA(cudaMemsetAsync(c.counters + 5, 0, 3 * sizeof(int), st), "memset");
+    LCUDA(msc::launch_wave_mark(cur, n_list, w, inw, c.queued, endv, todo, c.counters + 5, sms, st), "wave");
+    int n_todo = 0;
+    if (int rc = read_dev(c, c.counters + 5, 1, &n_todo)) return rc;
+    int n_amb = 0;
+    if (p->precision == 1) {
+      n_amb = n_todo;
+      LCUDA(msc::launch_fixup_end64(c.g64, V, P, d.state, todo, n_todo, endv, c.work, c.work + 50, sms, st), "fix-up");
+    } else if (n_todo > 0) {
+      LCUDA(msc::launch_fixup_end32(c.g32, V, P, d.lab, d.state, todo, n_todo, endv, c.amb, c.counters + 7,
+                                    p->precision == 2 ? 2 : 0, c.work, c.work + 49, sms, st),
             "fix-up");
-      stats[0] += n_list;
-      if (int rc = read_dev(c, c.counters + 6, 1, &n_list)) return rc;
-      std::swap(cur, nxt);
-      trace_mark(st, d.dir, "wave " + std::to_string(waves) + " next " + std::to_string(n_list));
+      if (int rc = read_dev(c, c.counters + 7, 1, &n_amb)) return rc;
+      LCUDA(msc::launch_fixup_end64(c.g64, V, P, d.state, c.amb, n_amb, endv, c.work + 56, c.work + 50, sms, st),
+            "fix-up FP64");
     }
-  } else {
-    // FP32 waves on `st`; the ambiguous streamlines they collect go through FP64 on a
-    // second stream while the FP32 waves go on (a FP64 wave is as long as its slowest
-    // streamline, ~15 ms at 512^3, and mostly leaves the GPU idle).  The two never share
-    // a list: the FP64 wave reads the ambiguous list the FP32 waves stopped filling
-    // (amb_run), writes the vertices it reopens to list_c, and claims with work[56];
-    // those vertices join the FP32 list when it runs dry.  Decisions read lab0 only and a
-    // vertex's queued bit keeps it in one list at a time, so the closure is the same.
-    cudaStream_t s64 = nullptr;
-    cudaEvent_t ev_in = nullptr, ev_out = nullptr;
-    struct Side {
-      cudaStream_t& s;
-      cudaEvent_t &a, &b;
-      ~Side() {
-        if (s) {
-          cudaStreamSynchronize(s);
-          cudaStreamDestroy(s);
-        }
-        if (a) cudaEventDestroy(a);
-        if (b) cudaEventDestroy(b);
-      }
-    } side{s64, ev_in, ev_out};
-    LCUDA(cudaStreamCreateWithFlags(&s64, cudaStreamNonBlocking), "cudaStreamCreate");
-    LCUDA(cudaEventCreateWithFlags(&ev_in, cudaEventDisableTiming), "cudaEventCreate");
-    LCUDA(cudaEventCreateWithFlags(&ev_out, cudaEventDisableTiming), "cudaEventCreate");
-    int64_t* amb_col = c.amb;   // filled by the FP32 waves (counters[7])
-    int64_t* amb_run = c.amb2;  // read by the FP64 wave in flight
-    bool in_flight = false;
-    for (int64_t waves = 0; n_list > 0 || n_amb > 0 || in_flight; waves++) {
-      if (waves > 2 * N + 2) return fail(MSC_ERR_ITER_LIMIT, "fix-up did not converge");
-      if (!in_flight && n_amb > 0) {
-        std::swap(amb_col, amb_run);
-        const int n_run = n_amb;
-        n_amb = 0;
-        LCUDA(cudaMemsetAsync(c.counters + 7, 0, 2 * sizeof(int), st), "memset");
-        LCUDA(cudaEventRecord(ev_in, st), "cudaEventRecord");
-        LCUDA(cudaStreamWaitEvent(s64, ev_in, 0), "cudaStreamWaitEvent");
-        LCUDA(msc::launch_fixup(c.g64, V, P, d.lab, lab0, d.state, amb_run, n_run, c.list_c, c.counters + 8,
-                                c.queued, c.work + 56, c.work + 50, sms, s64),
-              "fix-up FP64");
-        LCUDA(cudaEventRecord(ev_out, s64), "cudaEventRecord");
-        in_flight = true;
-        stats[1] += n_run;
-        trace_mark(st, d.dir, "fp64 start " + std::to_string(n_run));
-      }
-      if (n_list > 0) {
-        LCUDA(cudaMemsetAsync(c.counters + 6, 0, sizeof(int), st), "memset");
-        LCUDA(msc::launch_fixup32(c.g32, V, P, d.lab, lab0, d.state, cur, n_list, nxt, c.counters + 6, c.queued,
-                                  amb_col, c.counters + 7, p->precision == 2 ? 2 : 0, c.work, c.work + 49, sms, st),
-              "fix-up");
-        stats[0] += n_list;
-        int h[2];  // next wave's length, ambiguous streamlines waiting
-        if (int rc = read_dev(c, c.counters + 6, 2, h)) return rc;
-        n_list = h[0];
-        n_amb = h[1];
-        std::swap(cur, nxt);
-        trace_mark(st, d.dir, "wave " + std::to_string(waves) + " next " + std::to_string(n_list));
-      } else if (in_flight) {
-        // the FP32 waves ran dry: the FP64 wave's reopened vertices are the next list
-        LCUDA(cudaStreamWaitEvent(st, ev_out, 0), "cudaStreamWaitEvent");
-        int n64 = 0;
-        if (int rc = read_dev(c, c.counters + 8, 1, &n64)) return rc;
-        if (n64 > 0)
-          LCUDA(cudaMemcpyAsync(cur, c.list_c, (size_t)n64 * sizeof(int64_t), cudaMemcpyDeviceToDevice, st), "copy");
-        n_list = n64;
-        in_flight = false;
-        trace_mark(st, d.dir, "fp64 done next " + std::to_string(n_list));
-      }
-    }
+    stats[0] += n_todo;
+    stats[1] += n_amb;
+    LCUDA(msc::launch_wave_decide(cur, n_list, w, V, endv, inw, d.lab, d.state, rptr, rval, c.queued, nxt,
+                                  c.counters + 6, sms, st),
+          "wave decide");
+    if (int rc = read_dev(c, c.counters + 6, 1, &n_list)) return rc;
+    std::swap(cur, nxt);
+    trace_mark(st, d.dir, "wave " + std::to_string(w) + " integrated " + std::to_string(n_todo) + " (FP64 " +
+                              std::to_string(n_amb) + ") next " + std::to_string(n_list));
   }
   {
     unsigned long long h[3];
@@ -673,11 +740,16 @@ int finish_direction(LabelCtx& c, DirLabels& d, int32_t* out, int32_t* stage_int
   if (!out) return MSC_OK;
 
   // isolated-region cleaner
-  int32_t *parent, *target;  // (fewer than 2^31 vertices: setup_ctx)
+  int32_t *parent, *first, *md, *roots;  // (fewer than 2^31 vertices: setup_ctx)
   LCUDA(c.pool.get(&parent, N), "alloc");
-  LCUDA(c.pool.get(&target, N), "alloc");
-  LCUDA(msc::launch_clean(d.lab, c.f, V, d.dir, parent, target, out, sms, st), "clean");
-  trace_mark(st, d.dir, "clean");
+  LCUDA(c.pool.get(&first, N), "alloc");
+  LCUDA(c.pool.get(&md, N), "alloc");
+  LCUDA(c.pool.get(&roots, N), "alloc");
+  int sweeps = 0;
+  LCUDA(msc::launch_clean(d.lab, c.f, V, d.dir, parent, first, md, roots, c.counters + 8,
+                          reinterpret_cast<int*>(c.hpin), out, sms, st, &sweeps),
+        "clean");
+  trace_mark(st, d.dir, "clean (" + std::to_string(sweeps) + " sweeps)");
   return MSC_OK;
 }
 
@@ -1020,9 +1092,46 @@ int labels_host_impl(const float* fh, const int64_t* dims, const msc_integ_param
   return MSC_OK;
 }
 
+// The cleaner alone on caller labels (msc_clean_regions_3d).
+int clean_impl(const float* f, const int32_t* labels_in, const int64_t* dims, int direction, int32_t* labels_out,
+               cudaStream_t st) {
+  if (!f || !labels_in || !labels_out || !dims) return fail(MSC_ERR_NULL_POINTER, "null argument");
+  if (direction != -1 && direction != 1) return fail(MSC_ERR_BAD_DIMS, "direction must be -1 or +1");
+  if (dims[0] < 1 || dims[1] < 1 || dims[2] < 1 || dims[0] > (1 << 30) || dims[1] > (1 << 30) || dims[2] > (1 << 30))
+    return fail(MSC_ERR_BAD_DIMS, "invalid dims");
+  const int64_t N = dims[0] * dims[1] * dims[2];
+  if (N / dims[2] != dims[0] * dims[1] || N >= ((int64_t)1 << 31)) return fail(MSC_ERR_BAD_DIMS, "fewer than 2^31 vertices");
+  LabelCtx c(st);
+  if (!(c.hpin = pinned_get())) return fail(MSC_ERR_OOM, "pinned host words");
+  const msc::VolDims V{dims[0], dims[1], dims[2], 2 * dims[0] - 1, 2 * dims[1] - 1, 2 * dims[2] - 1,
+                       2 * dims[0] - 1, (2 * dims[0] - 1) * (2 * dims[1] - 1)};
+  const int sms = sm_count();
+  int32_t *lab, *parent, *first, *md, *roots;
+  int* counters;
+  LCUDA(c.pool.get(&lab, N), "alloc");
+  LCUDA(c.pool.get(&parent, N), "alloc");
+  LCUDA(c.pool.get(&first, N), "alloc");
+  LCUDA(c.pool.get(&md, N), "alloc");
+  LCUDA(c.pool.get(&roots, N), "alloc");
+  LCUDA(c.pool.get(&counters, 2), "alloc");
+  ::msc::count_launch();
+  none_in_kernel<<<sms * 8, 256, 0, st>>>(labels_in, lab, N);
+  LCUDA(msc::launch_clean(lab, f, V, direction, parent, first, md, roots, counters, reinterpret_cast<int*>(c.hpin),
+                          labels_out, sms, st, nullptr),
+        "clean");
+  LCUDA(cudaStreamSynchronize(st), "cudaStreamSynchronize");
+  return MSC_OK;
+}
+
 }  // namespace
 
 extern "C" {
+
+int msc_clean_regions_3d(const float* f, const int32_t* labels_in, const int64_t dims[3], int direction,
+                         int32_t* labels_out, msc_stream_t stream) {
+  return clean_impl(f, labels_in, dims, direction, labels_out, (cudaStream_t)stream);
+}
+
 
 const char* msc_labels_last_error_string(void) { return t_err.c_str(); }
 

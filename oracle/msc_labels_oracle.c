@@ -718,6 +718,14 @@ int oracle_terminal_regions_3d(const float* f, const uint8_t* grad, int64_t X, i
 	return 0;
 }
 
+/* The cleaner alone on labels (in place); dir -1 ASC, +1 DSC. */
+int oracle_clean_regions_3d(const float* f, int64_t X, int64_t Y, int64_t Z, int dir, int32_t* labels) {
+	lctx c;
+	if (ctx_init(&c, f, NULL, X, Y, Z, dir)) return -1;
+	clean_regions(&c, labels);
+	return 0;
+}
+
 /* ondemandaccurate's ASC then DSC 3-manifold labels (ondemandaccurate.cxx:795-948).
  * Both directions integrate the same gradient array, so the DSC pass sees the zeros
  * the ASC pass wrote at the minima, as in the reference.  dirs: bit 0 ASC, bit 1 DSC.

@@ -50,6 +50,8 @@ typedef struct {
 /* Certain terminal regions grown from the (merged) extrema; dir -1 ASC, +1 DSC. */
 int oracle_terminal_regions_3d(const float* f, const uint8_t* grad, int64_t X, int64_t Y, int64_t Z, int dir,
                                float presimp_threshold, int32_t* labels);
+/* The isolated-region cleaner alone, in place (IsolatedCCRegionRemoverNEW). */
+int oracle_clean_regions_3d(const float* f, int64_t X, int64_t Y, int64_t Z, int dir, int32_t* labels);
 /* Full labeling chain; dirs bit 0 ASC, bit 1 DSC (DSC after ASC on the shared gradient). */
 int oracle_labels_3d(const float* f, const uint8_t* grad, int64_t X, int64_t Y, int64_t Z, int dirs,
                      const oracle_label_params* P, int32_t* labels_asc, int32_t* labels_dsc,

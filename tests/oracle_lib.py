@@ -44,6 +44,7 @@ class Oracle:
         lib.oracle_labels_3d.argtypes = [_VP, _VP, _I64, _I64, _I64, ctypes.c_int, ctypes.POINTER(LabelParams),
                                          _VP, _VP, _VP]
         lib.oracle_terminal_regions_3d.argtypes = [_VP, _VP, _I64, _I64, _I64, ctypes.c_int, ctypes.c_float, _VP]
+        lib.oracle_clean_regions_3d.argtypes = [_VP, _I64, _I64, _I64, ctypes.c_int, _VP]
 
     def labels(self, f, grad, error_threshold, gradient_threshold, iteration_limit, max_step, presimp):
         """ASC and DSC labels (regions named by their smallest seed vertex) plus stages."""
@@ -59,6 +60,13 @@ class Oracle:
         out = {"asc": asc, "dsc": dsc}
         for i, k in enumerate(STAGES):
             out[k] = st[i * n:(i + 1) * n]
+        return out
+
+    def clean(self, f, labels, direction):
+        """IsolatedCCRegionRemoverNEW on a copy of `labels` (direction -1 ASC, +1 DSC)."""
+        f = np.ascontiguousarray(f, dtype=np.float32)
+        out = np.array(labels, dtype=np.int32, copy=True)
+        assert self.lib.oracle_clean_regions_3d(f.ctypes.data, *f.shape[::-1], int(direction), out.ctypes.data) == 0
         return out
 
     def central_diff(self, f: np.ndarray) -> np.ndarray:

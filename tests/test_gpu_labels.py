@@ -123,3 +123,22 @@ def test_labels_with_merge_threshold_vs_oracle(gpu, oracle, name):
         assert (got[k] == want[k]).all(), (k, float((got[k] != want[k]).mean()))
     for k in ("asc", "dsc"):
         assert float((got[k] != want[k]).mean()) <= TOL_FINAL
+
+
+@pytest.mark.parametrize("name", list(FIELDS))
+def test_cleaner_equals_oracle_exactly(gpu, oracle, name):
+    """IsolatedCCRegionRemoverNEW alone: the oracle's integrated labels in, the oracle's
+    cleaned labels out, bit for bit (the reference visits the component roots in vertex
+    order, and each join sees the joins made before it)."""
+    import torch
+    from msceer_gb300 import clean_regions, lower_star_grad
+    f = FIELDS[name]()
+    gt = 1e-6 * float(np.abs(f).max())
+    t = torch.from_numpy(f).to(gpu)
+    g = lower_star_grad(t).cpu().numpy()
+    want = oracle.labels(f, g, 1e-4, gt, 4000, 0.25, 0.0)
+    for d, k in ((-1, "asc"), (1, "dsc")):
+        integ = want[f"{k}_integrated"]
+        assert np.array_equal(oracle.clean(f, integ, d), want[k])  # the oracle's own cleaner, alone
+        got = clean_regions(t, torch.from_numpy(integ).to(gpu), d).cpu().numpy()
+        assert np.array_equal(got, want[k]), (k, int((got != want[k]).sum()))
