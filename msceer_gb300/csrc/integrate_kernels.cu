@@ -1159,7 +1159,7 @@ __global__ void __launch_bounds__(128, 7) fixup_end32_kernel(const Adv32 A, cons
 // region, or -- after a low-gradient stop or the iteration limit -- the current label of
 // an ordinary vertex, which an earlier decision of the same wave may have changed.  The
 // kernels below reproduce that order: a decision whose end vertex e is decided earlier
-// in the same wave (e < v) takes e's new label (chains followed by pointer jumping), any
+// in the same wave (e < v) takes e's new label (the chain of such ends followed), any
 // other takes the label at the wave's start; a changed vertex reopens its neighbours
 // that were undecided at its moment (never decided before the wave, and not earlier in
 // it) and carry another label.
@@ -1218,8 +1218,30 @@ __global__ void wave_jump_kernel(const int64_t* __restrict__ list, int n, int32_
   }
 }
 
+// Each member's new label: the value where its chain of same-wave ends stops.  A chain
+// longer than kChainSteps is left to pointer jumping (*long_chain is set).
+constexpr int kWaveChainSteps = 64;
+__global__ void wave_resolve_kernel(const int64_t* __restrict__ list, int n, const int32_t* __restrict__ rptr,
+                                    const int32_t* __restrict__ rval, int32_t* __restrict__ rfin,
+                                    int* __restrict__ long_chain) {
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+    const int64_t v = list[k];
+    int32_t p = rptr[v];
+    for (int s = 0; s < kWaveChainSteps; s++) {
+      const int32_t q = rptr[p];
+      if (q == p) break;
+      p = q;
+    }
+    if (rptr[p] != p) {
+      atomicExch(long_chain, 1);
+      continue;
+    }
+    rfin[v] = rval[p];
+  }
+}
+
 __global__ void wave_enqueue_kernel(const int64_t* __restrict__ list, int n, int w, const VolDims V,
-                                    const int32_t* __restrict__ rptr, const int32_t* __restrict__ rval,
+                                    const int32_t* __restrict__ rfin,
                                     const int32_t* __restrict__ lab, const uint8_t* __restrict__ state,
                                     const int32_t* __restrict__ inw, uint32_t* __restrict__ queued,
                                     int64_t* __restrict__ next, int* __restrict__ n_next) {
@@ -1229,7 +1251,7 @@ __global__ void wave_enqueue_kernel(const int64_t* __restrict__ list, int n, int
     int32_t nl = 0;
     if (k < n) {
       v = list[k];
-      nl = rval[rptr[v]];
+      nl = rfin[v];
       if (nl == lab[v]) v = -1;  // unchanged: reopens nothing
     }
     int64_t nbr[6] = {-1, -1, -1, -1, -1, -1};
@@ -1258,12 +1280,11 @@ __global__ void wave_enqueue_kernel(const int64_t* __restrict__ list, int n, int
   }
 }
 
-__global__ void wave_apply_kernel(const int64_t* __restrict__ list, int n, const int32_t* __restrict__ rptr,
-                                  const int32_t* __restrict__ rval, int32_t* __restrict__ lab,
-                                  uint8_t* __restrict__ state) {
+__global__ void wave_apply_kernel(const int64_t* __restrict__ list, int n, const int32_t* __restrict__ rfin,
+                                  int32_t* __restrict__ lab, uint8_t* __restrict__ state) {
   for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
     const int64_t v = list[k];
-    lab[v] = rval[rptr[v]];
+    lab[v] = rfin[v];
     state[v] = kStNonterminal;
   }
 }
@@ -1597,23 +1618,37 @@ cudaError_t launch_wave_mark(const int64_t* list, int n, int w, int32_t* inw, ui
   return cudaGetLastError();
 }
 
-cudaError_t launch_wave_decide(const int64_t* list, int n, int w, const VolDims& V, const int32_t* endv,
-                               const int32_t* inw, int32_t* lab, uint8_t* state, int32_t* rptr, int32_t* rval,
-                               uint32_t* queued, int64_t* next, int* n_next, int num_sms, cudaStream_t stream) {
+cudaError_t launch_wave_resolve(const int64_t* list, int n, int w, const int32_t* endv, const int32_t* inw,
+                                const int32_t* lab, const uint8_t* state, int32_t* rptr, int32_t* rval, int32_t* rfin,
+                                int* long_chain, bool jump, int num_sms, cudaStream_t stream) {
+  if (n <= 0) return cudaSuccess;
+  const int grid = grid_for(n, num_sms);
+  if (cudaError_t e = cudaMemsetAsync(long_chain, 0, sizeof(int), stream)) return e;
+  if (!jump) {
+    ::msc::count_launch();
+    wave_root_kernel<<<grid, 256, 0, stream>>>(list, n, w, endv, inw, lab, state, rptr, rval);
+  } else {
+    int jumps = 1;
+    for (int m = n; m > 1; m >>= 1) jumps++;
+    for (int j = 0; j < jumps; j++) {
+      ::msc::count_launch();
+      wave_jump_kernel<<<grid, 256, 0, stream>>>(list, n, rptr);
+    }
+  }
+  ::msc::count_launch();
+  wave_resolve_kernel<<<grid, 256, 0, stream>>>(list, n, rptr, rval, rfin, long_chain);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_wave_finish(const int64_t* list, int n, int w, const VolDims& V, const int32_t* rfin,
+                               const int32_t* inw, int32_t* lab, uint8_t* state, uint32_t* queued, int64_t* next,
+                               int* n_next, int num_sms, cudaStream_t stream) {
   if (n <= 0) return cudaSuccess;
   const int grid = grid_for(n, num_sms);
   ::msc::count_launch();
-  wave_root_kernel<<<grid, 256, 0, stream>>>(list, n, w, endv, inw, lab, state, rptr, rval);
-  int jumps = 1;
-  for (int m = n; m > 1; m >>= 1) jumps++;
-  for (int j = 0; j < jumps; j++) {
-    ::msc::count_launch();
-    wave_jump_kernel<<<grid, 256, 0, stream>>>(list, n, rptr);
-  }
+  wave_enqueue_kernel<<<grid, 256, 0, stream>>>(list, n, w, V, rfin, lab, state, inw, queued, next, n_next);
   ::msc::count_launch();
-  wave_enqueue_kernel<<<grid, 256, 0, stream>>>(list, n, w, V, rptr, rval, lab, state, inw, queued, next, n_next);
-  ::msc::count_launch();
-  wave_apply_kernel<<<grid, 256, 0, stream>>>(list, n, rptr, rval, lab, state);
+  wave_apply_kernel<<<grid, 256, 0, stream>>>(list, n, rfin, lab, state);
   return cudaGetLastError();
 }
 

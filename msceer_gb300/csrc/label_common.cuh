@@ -199,11 +199,17 @@ cudaError_t launch_fixup_end32(const float4* G, const VolDims& V, const IntegPar
 // lists the members without an end yet in todo (n_todo: a device counter).
 cudaError_t launch_wave_mark(const int64_t* list, int n, int w, int32_t* inw, uint32_t* queued, const int32_t* endv,
                              int64_t* todo, int* n_todo, int num_sms, cudaStream_t stream);
-// Decides wave w in the reference's order (every member has its end), reopens
-// neighbours into next (n_next: a device counter) and writes the labels.
-cudaError_t launch_wave_decide(const int64_t* list, int n, int w, const VolDims& V, const int32_t* endv,
-                               const int32_t* inw, int32_t* lab, uint8_t* state, int32_t* rptr, int32_t* rval,
-                               uint32_t* queued, int64_t* next, int* n_next, int num_sms, cudaStream_t stream);
+// Decides wave w in the reference's order (every member has its end): resolve gives
+// each member its new label in rfin (jump == false: from the ends; a member whose chain
+// of same-wave ends is too long sets *long_chain, and a second call with jump == true
+// shortens the chains first); finish reopens neighbours into next (n_next: a device
+// counter) and writes the labels.
+cudaError_t launch_wave_resolve(const int64_t* list, int n, int w, const int32_t* endv, const int32_t* inw,
+                                const int32_t* lab, const uint8_t* state, int32_t* rptr, int32_t* rval, int32_t* rfin,
+                                int* long_chain, bool jump, int num_sms, cudaStream_t stream);
+cudaError_t launch_wave_finish(const int64_t* list, int n, int w, const VolDims& V, const int32_t* rfin,
+                               const int32_t* inw, int32_t* lab, uint8_t* state, uint32_t* queued, int64_t* next,
+                               int* n_next, int num_sms, cudaStream_t stream);
 // IsolatedCCRegionRemoverNEW::ComputeOutput: same-label components, then the reference's
 // vertex-ordered joins of the components without their region's extremum.  parent,
 // first, md, roots: N int32 of scratch each; counters: 2 ints; pinned: one int of

@@ -286,7 +286,7 @@ struct LabelCtx {
   uint32_t* queued = nullptr;
   uint8_t* tiles = nullptr;
   int* counters = nullptr;  // [0] n_ext [1] n_sad [2] n_arcs [3] changed [4] err [5] n_list / wave members
-                            // without an end [6] n_next [7] n_amb [8, 10) cleaner
+                            // without an end [6] n_next [7] n_amb [8, 10) cleaner [10] long chain
   unsigned long long* work = nullptr;  // [0] claimed fix-up items, [48, 51) advection iterations (first
                                        // pass, FP32, FP64), [56] FP64 claims
   void* hpin = nullptr;                // kPinnedBytes of pinned host memory (pinned_get)
@@ -681,7 +681,8 @@ int finish_direction(LabelCtx& c, DirLabels& d, int32_t* out, int32_t* stage_int
   // the wave in the reference's one-thread order (integrate_kernels.cu, wave kernels).
   // An end does not depend on labels, so a vertex decided in several waves integrates
   // once.
-  int32_t *endv, *inw, *rptr, *rval;
+  int32_t *endv, *inw, *rptr, *rval, *rfin;
+  LCUDA(c.pool.get(&rfin, N), "alloc");
   LCUDA(c.pool.get(&endv, N), "alloc");
   LCUDA(c.pool.get(&inw, N), "alloc");
   LCUDA(c.pool.get(&rptr, N), "alloc");
@@ -715,13 +716,23 @@ int finish_direction(LabelCtx& c, DirLabels& d, int32_t* out, int32_t* stage_int
                                     p->precision == 2 ? 2 : 0, c.work, c.work + 49, sms, st),
             "fix-up");
       if (int rc = read_dev(c, c.counters + 7, 1, &n_amb)) return rc;
+      trace_mark(st, d.dir, "  fp32 ends");
       LCUDA(msc::launch_fixup_end64(c.g64, V, P, d.state, c.amb, n_amb, endv, c.work + 56, c.work + 50, sms, st),
             "fix-up FP64");
+      trace_mark(st, d.dir, "  fp64 ends");
     }
     stats[0] += n_todo;
     stats[1] += n_amb;
-    LCUDA(msc::launch_wave_decide(cur, n_list, w, V, endv, inw, d.lab, d.state, rptr, rval, c.queued, nxt,
-                                  c.counters + 6, sms, st),
+    int long_chain = 0;
+    LCUDA(msc::launch_wave_resolve(cur, n_list, w, endv, inw, d.lab, d.state, rptr, rval, rfin, c.counters + 10, false,
+                                   sms, st),
+          "wave decide");
+    if (int rc = read_dev(c, c.counters + 10, 1, &long_chain)) return rc;
+    if (long_chain)
+      LCUDA(msc::launch_wave_resolve(cur, n_list, w, endv, inw, d.lab, d.state, rptr, rval, rfin, c.counters + 10,
+                                     true, sms, st),
+            "wave decide");
+    LCUDA(msc::launch_wave_finish(cur, n_list, w, V, rfin, inw, d.lab, d.state, c.queued, nxt, c.counters + 6, sms, st),
           "wave decide");
     if (int rc = read_dev(c, c.counters + 6, 1, &n_list)) return rc;
     std::swap(cur, nxt);
