@@ -154,6 +154,22 @@ int msc_integrated_labels_3d(const float* f, const uint8_t* grad, const int64_t 
 int msc_integrated_labels_3d_stages(const float* f, const uint8_t* grad, const int64_t dims[3],
                                     const msc_integ_params* params, int32_t* labels_asc, int32_t* labels_dsc,
                                     int32_t* stages, msc_stream_t stream);
+/* The accurate .grad that ondemandaccurate writes for accurate ascending / descending
+ * 3-manifolds (needASC2 / needDSC2, ondemandaccurate.cxx:795-1063): the restriction label
+ * of every cell from the final labels (VertexLabelingToBoundaryLabeling::
+ * ComputeMINBoundary with labels_asc, ComputeMAXBoundary with labels_dsc,
+ * gi_labeling_to_bounary_labeling.h:48-199; either may be NULL, as when its manifold is
+ * not requested), the re-pairing of every vertex whose lower star holds a restricted
+ * cell (MyRobinsNoalloc<...,4,6>::ComputeLowerStar, gi_modified_robins.h:1281-1343,
+ * the star split by restriction label and boundaryValue) and the ascending-manifold
+ * closure of RecordGrad (:693-699).  f: device X*Y*Z floats; labels: device int32 per
+ * vertex as msc_integrated_labels_3d writes them; grad: device, the base .grad of
+ * msc_lower_star_grad_3d in, the accurate .grad out.  restriction_out (optional):
+ * device, msc_num_cells_3d(dims) bytes.  touched_out (optional): the number of
+ * re-paired vertices.  Blocking. */
+int msc_conforming_grad_3d(const float* f, const int32_t* labels_asc, const int32_t* labels_dsc, const int64_t dims[3],
+                           uint8_t* grad, uint8_t* restriction_out, int64_t* touched_out, msc_stream_t stream);
+
 /* The isolated-region cleaner alone: IsolatedCCRegionRemoverNEW::ComputeOutput
  * (gi_isolated_region_remover.h:155-192) on caller labels, as ondemandaccurate runs it
  * after the integration (ondemandaccurate.cxx:866-870, 942-946).  Same-label

@@ -11,6 +11,7 @@ from .api import (  # noqa: F401
     TopologicalRegularGrid3D,
     ascending_manifold_dims,
     clean_regions,
+    conforming_grad,
     integrated_labels,
     integrated_labels_batch,
     lower_star_grad,

@@ -45,6 +45,7 @@ SIGNATURES = {
     "msc_kernel_launches": (ctypes.c_int64, []),
     "msc_labels_last_error_string": (ctypes.c_char_p, []),
     "msc_clean_regions_3d": (ctypes.c_int, [_VP, _VP, _I64P, ctypes.c_int, _VP, _VP]),
+    "msc_conforming_grad_3d": (ctypes.c_int, [_VP, _VP, _VP, _I64P, _VP, _VP, _I64P, _VP]),
     "msc_labels_last_stats": (None, [_I64P]),
     "msc_labels_last_iterations": (None, [_I64P]),
     "msc_trim_scratch": (None, []),

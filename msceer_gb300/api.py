@@ -195,6 +195,30 @@ def integrated_labels(f, grad, error_threshold=1e-4, gradient_threshold=None, it
     return out
 
 
+def conforming_grad(f, grad, labels_asc=None, labels_dsc=None, restriction=False):
+    """ondemandaccurate's accurate 3-manifold .grad (msc_conforming_grad_3d): ``grad`` (the
+    base .grad of :func:`lower_star_grad`, CUDA uint8) is re-paired in place around the
+    boundaries of the final labels ``labels_asc`` / ``labels_dsc`` (CUDA int32, either
+    may be None).  Returns the number of re-paired vertices, and with ``restriction``
+    also the restriction byte of every cell."""
+    import torch
+
+    f = f.contiguous()
+    dims = _shape_dims(f.shape)
+    if len(dims) != 3 or not (f.is_cuda and grad.is_cuda):
+        raise ValueError("conforming_grad takes a CUDA 3D volume and its .grad")
+    rl = torch.empty(num_cells(dims), dtype=torch.uint8, device=f.device) if restriction else None
+    touched = ctypes.c_int64(0)
+    ptr = lambda t: ctypes.c_void_p(t.contiguous().data_ptr()) if t is not None else None  # noqa: E731
+    lib = _lib.load()
+    stream = torch.cuda.current_stream(f.device).cuda_stream
+    with torch.cuda.device(f.device):
+        rc = lib.msc_conforming_grad_3d(ptr(f), ptr(labels_asc), ptr(labels_dsc), _lib.dims_arg(dims), ptr(grad),
+                                        ptr(rl), ctypes.byref(touched), ctypes.c_void_p(stream))
+    _lib.check(rc, "msc_conforming_grad_3d")
+    return (touched.value, rl) if restriction else touched.value
+
+
 def clean_regions(f, labels, direction):
     """IsolatedCCRegionRemoverNEW on device labels (msc_clean_regions_3d): ``direction``
     -1 for ascending labels (lowest value first), +1 for descending ones.  ``f``: CUDA

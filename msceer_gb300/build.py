@@ -26,7 +26,7 @@ GENCODE = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-O3",
               "--expt-relaxed-constexpr", "-I", str(ROOT / "include")]
 CU_SOURCES = ["lstar_kernels.cu", "ldir_kernels.cu", "grad_kernels.cu", "label_kernels.cu", "integrate_kernels.cu",
-              "msc_capi.cu", "msc_labels_capi.cu", "msc_static_scratch.cu", "triage_kernels.cu", "triage_prep.cu",
+              "msc_capi.cu", "msc_labels_capi.cu", "conform_kernels.cu", "msc_static_scratch.cu", "triage_kernels.cu", "triage_prep.cu",
               "msc_triage_capi.cu"]
 
 

@@ -377,22 +377,13 @@ MSC_HD uint32_t lower_star_keys(int64_t x, int64_t y, int64_t z, int64_t X, int6
   return lower_star_mask<ND>(lower);
 }
 
-// Second half: expand every boundary class of the lower star L (keys in `col`) and
-// emit each owned cell's byte through `store(p, byte)`.  bx/by/bz: the vertex lies on
-// the first or last plane of that axis (ignored for an interior vertex).
-template <int ND, class Store>
-MSC_HD void expand_and_store(uint32_t L, uint64_t* col, int cs, bool interior, bool bx, bool by, bool bz,
-                             uint32_t enc_map, const Store& store) {
+// The bytes of every cell of a processed lower star L (owned by its vertex): assigned |
+// flag | pair code (7 if critical) | ldir, where ldir is 2 / 1 / 0 for critical 1- / 2- /
+// 3-cells and 3 otherwise (the roots of the ascending-manifold closure).
+template <int ND, class State, class Store>
+MSC_HD void store_cells(const State& st, uint32_t L, uint32_t Bany, uint32_t enc_map, const Store& store) {
   using N = Nb<ND>;
   constexpr int NPOS = N::NPOS;
-  LowerStarState<ND, KeyCol> st(KeyCol{col, cs});
-  uint32_t Bany = 0;
-  if (interior)
-    st.expand(L);
-  else
-    Bany = run_classes<ND>(st, L, bx, by, ND == 3 && bz);
-  // byte bit-planes: assigned | flag | pair code (7 if critical) | ldir, where ldir
-  // is 2 / 1 / 0 for critical 1- / 2- / 3-cells and 3 otherwise
   constexpr uint32_t D0 = N::dim_mask(0), D1 = N::dim_mask(1), D2 = N::dim_mask(2);
   const uint32_t K = st.K;
   uint32_t p0 = st.C0, p1 = st.C1, p2 = st.C2;
@@ -422,6 +413,86 @@ MSC_HD void expand_and_store(uint32_t L, uint64_t* col, int cs, bool interior, b
   }
 }
 
+// Second half: expand every boundary class of the lower star L (keys in `col`) and
+// emit each owned cell's byte through `store(p, byte)`.  bx/by/bz: the vertex lies on
+// the first or last plane of that axis (ignored for an interior vertex).
+template <int ND, class Store>
+MSC_HD void expand_and_store(uint32_t L, uint64_t* col, int cs, bool interior, bool bx, bool by, bool bz,
+                             uint32_t enc_map, const Store& store) {
+  LowerStarState<ND, KeyCol> st(KeyCol{col, cs});
+  uint32_t Bany = 0;
+  if (interior)
+    st.expand(L);
+  else
+    Bany = run_classes<ND>(st, L, bx, by, ND == 3 && bz);
+  store_cells<ND>(st, L, Bany, enc_map, store);
+}
+
+// The constrained re-pairing of ondemandaccurate's accurate 3-manifolds
+// (MyRobinsNoalloc<...,4,6>::ComputeLowerStar with a restriction map,
+// gi_modified_robins.h:1281-1343): the lower star L split by class
+// restriction_label * maxDim + boundaryValue (maxDim = 3; at most 24 classes, the last
+// taking every larger one), the classes expanded in increasing order.  rl[p]: the
+// restriction label of the cell at position p.
+template <int ND, class Store>
+MSC_HD void expand_and_store_keyed(uint32_t L, uint64_t* col, int cs, const uint8_t* rl, bool bx, bool by, bool bz,
+                                   uint32_t enc_map, const Store& store) {
+  using N = Nb<ND>;
+  constexpr int NPOS = N::NPOS;
+  LowerStarState<ND, KeyCol> st(KeyCol{col, cs});
+  const uint32_t B0 = bx ? N::axis_mask(0, 0) : 0u;
+  const uint32_t B1 = by ? N::axis_mask(1, 0) : 0u;
+  const uint32_t B2 = (ND == 3 && bz) ? N::axis_mask(2, 0) : 0u;
+  constexpr int kClasses = 24;
+  uint32_t cls[kClasses];
+#pragma unroll
+  for (int k = 0; k < kClasses; k++) cls[k] = 0u;
+  for (int p = 0; p < NPOS; p++) {
+    if (!((L >> p) & 1u)) continue;
+    const int bv = (int)((B0 >> p) & 1u) + (int)((B1 >> p) & 1u) + (int)((B2 >> p) & 1u);
+    int key = 3 * (int)rl[p] + bv;
+    if (key > kClasses - 1) key = kClasses - 1;
+    cls[key] |= 1u << p;
+  }
+  for (int k = 0; k < kClasses; k++)
+    if (cls[k]) st.expand(cls[k]);
+  store_cells<ND>(st, L, B0 | B1 | B2, enc_map, store);
+}
+
+// One vertex of the conforming re-pairing of ondemandaccurate's accurate 3-manifolds
+// (ondemandaccurate.cxx:1000-1063): a vertex whose own cell, or a cell of whose lower
+// star, carries a restriction label recomputes its lower star split by label
+// (expand_and_store_keyed); every other vertex keeps its pairs.  rlab(p, r): the
+// restriction label of the cell at position p (called for positions inside the
+// complex only).  Returns true if the vertex recomputed its lower star.
+template <int ND, class Load, class Restrict, class Store>
+MSC_HD bool conform_vertex(int64_t x, int64_t y, int64_t z, int64_t X, int64_t Y, int64_t Z, bool interior,
+                           const Load& load, const Restrict& rlab, uint64_t* col, int cs, uint32_t enc_map,
+                           const Store& store) {
+  using N = Nb<ND>;
+  constexpr int NPOS = N::NPOS;
+  const uint32_t okx = (x > 0 ? N::axis_mask(0, -1) : 0u) | N::axis_mask(0, 0) | (x < X - 1 ? N::axis_mask(0, 1) : 0u);
+  const uint32_t oky = (y > 0 ? N::axis_mask(1, -1) : 0u) | N::axis_mask(1, 0) | (y < Y - 1 ? N::axis_mask(1, 1) : 0u);
+  const uint32_t okz = (ND == 2) ? ~0u
+                                 : ((z > 0 ? N::axis_mask(2, -1) : 0u) | N::axis_mask(2, 0) |
+                                    (z < Z - 1 ? N::axis_mask(2, 1) : 0u));
+  const uint32_t ok = okx & oky & okz;
+  uint8_t rl[NPOS];
+  uint32_t R = 0;
+  for (int p = 0; p < NPOS; p++) {
+    uint8_t r = 0;
+    if ((ok >> p) & 1u) rlab(p, r);
+    rl[p] = r;
+    if (r) R |= 1u << p;
+  }
+  if (!R) return false;
+  bool nan = false;
+  const uint32_t L = lower_star_keys<ND>(x, y, z, X, Y, Z, interior, load, col, cs, nan);
+  if (!(R & L)) return false;  // (L holds the vertex itself)
+  expand_and_store_keyed<ND>(L, col, cs, rl, x == 0 || x == X - 1, y == 0 || y == Y - 1, z == 0 || z == Z - 1,
+                             enc_map, store);
+  return true;
+}
 
 // One vertex, end to end (both halves).  Returns true if a NaN was seen.
 template <int ND, class Load, class Store>

@@ -256,6 +256,46 @@ int grad_impl(int nd, const float* f, const int64_t* dims, uint8_t* g, cudaStrea
   return check_errors(s, stream);
 }
 
+// The accurate 3-manifold .grad of ondemandaccurate from a base .grad and the final
+// labels (msc_conforming_grad_3d).
+int conform_impl(const float* f, const int32_t* asc, const int32_t* dsc, const int64_t* dims, uint8_t* g,
+                 uint8_t* restrict_out, int64_t* touched_out, cudaStream_t stream) {
+  msc::GradDims D;
+  if (!make_dims(3, dims, &D)) return fail(MSC_ERR_BAD_DIMS, "invalid dims");
+  if (!f || !g) return fail(MSC_ERR_NULL_POINTER, "null buffer");
+  Scratch s;
+  if (int rc = alloc_scratch(s, stream)) return rc;
+  uint8_t* rl = restrict_out;
+  unsigned long long* touched = nullptr;
+  struct Free {
+    void* a;
+    void* b;
+    cudaStream_t st;
+    ~Free() {
+      if (a) cudaFreeAsync(a, st);
+      if (b) cudaFreeAsync(b, st);
+    }
+  } fr{nullptr, nullptr, stream};
+  if (!rl) {
+    MSC_CUDA(msc::scratch_alloc((void**)&rl, (size_t)D.ncells, stream), "scratch alloc(restriction labels)");
+    fr.a = rl;
+  }
+  MSC_CUDA(msc::scratch_alloc((void**)&touched, sizeof(unsigned long long), stream), "scratch alloc(counter)");
+  fr.b = touched;
+  MSC_CUDA(cudaMemsetAsync(touched, 0, sizeof(unsigned long long), stream), "cudaMemsetAsync");
+  const int sms = num_sms();
+  MSC_CUDA(msc::launch_restriction_labels(asc, dsc, f, D, rl, sms, stream), "restriction labels");
+  MSC_CUDA(msc::launch_conform(f, rl, g, D, touched, sms, stream), "conforming re-pairing");
+  if (int rc = ldir_impl(3, g, dims, stream, s, nullptr)) return rc;
+  if (touched_out) {
+    unsigned long long h = 0;
+    MSC_CUDA(cudaMemcpyAsync(&h, touched, sizeof(h), cudaMemcpyDeviceToHost, stream), "read counter");
+    MSC_CUDA(cudaStreamSynchronize(stream), "cudaStreamSynchronize");
+    *touched_out = (int64_t)h;
+  }
+  return check_errors(s, stream);
+}
+
 // Per-thread device staging for the host-buffer entries: grown on demand and kept
 // between calls so repeated calls do not pay for allocation.
 struct HostStaging {
@@ -682,6 +722,11 @@ int msc_central_diff_grad_2d_f64(const float* f, const int64_t dims[2], double* 
   make_dims(2, dims, &D);
   MSC_CUDA(msc::launch_central_diff(2, 2, f, g, D, num_sms(), (cudaStream_t)stream), "gradient kernel launch");
   return MSC_OK;
+}
+
+int msc_conforming_grad_3d(const float* f, const int32_t* labels_asc, const int32_t* labels_dsc, const int64_t dims[3],
+                           uint8_t* grad, uint8_t* restriction_out, int64_t* touched_out, msc_stream_t stream) {
+  return conform_impl(f, labels_asc, labels_dsc, dims, grad, restriction_out, touched_out, (cudaStream_t)stream);
 }
 
 int msc_steepest_lstar_host(const float* f_host, const int64_t dims[3], uint8_t* grad_host) {

@@ -99,4 +99,11 @@ cudaError_t launch_ldir_pass(int nd, uint8_t* g, const GradDims& D, const uint8_
                              int* changed, int* err, int num_sms, cudaStream_t stream);
 cudaError_t launch_central_diff(int nd, int layout, const float* f, void* out, const GradDims& D, int num_sms,
                                 cudaStream_t stream);
+// Conforming gradient (conform_kernels.cu): restriction bytes per cell from the final
+// ascending / descending labels (either may be null), then the re-pairing of the
+// touched vertices (`touched` counts them) and every cell's ldir back to its roots.
+cudaError_t launch_restriction_labels(const int32_t* asc, const int32_t* dsc, const float* f, const GradDims& D,
+                                      uint8_t* out, int num_sms, cudaStream_t stream);
+cudaError_t launch_conform(const float* f, const uint8_t* rlab, uint8_t* g, const GradDims& D,
+                           unsigned long long* touched, int num_sms, cudaStream_t stream);
 }  // namespace msc

@@ -302,13 +302,18 @@ static void write_pairs(const mesh_t* m, const lstar_t* L, uint8_t* g) {
 	}
 }
 
-/* ComputeLowerStar for one vertex (gi_modified_robins.h:1281-1343). */
-static void compute_lower_star(const mesh_t* m, const float* f, int64_t vx, int64_t vy, int64_t vz, uint8_t* g) {
+/* ComputeLowerStar for one vertex (gi_modified_robins.h:1281-1343): the star split by
+ * class restriction_label * maxDim + boundaryValue (maxDim = 3, gi_topological_regular_grid.h:
+ * 1262-1264; the label 0 everywhere without a restriction map), the classes expanded in
+ * increasing order. */
+#define N_CLASSES 24
+static void compute_lower_star_r(const mesh_t* m, const float* f, int64_t vx, int64_t vy, int64_t vz, uint8_t* g,
+                                 const uint8_t* restrict_lab) {
 	int64_t vc[3] = { 2 * vx, 2 * vy, 2 * vz };
 	int64_t vcell = cell_id(m, vc);
 	int64_t vid = vx * m->vs[0] + vy * m->vs[1] + vz * m->vs[2];
-	lstar_t cls[4];
-	for (int s = 0; s < 4; s++) cls[s].n = 0;
+	lstar_t cls[N_CLASSES];
+	for (int s = 0; s < N_CLASSES; s++) cls[s].n = 0;
 	int npos = (m->nd == 3) ? 27 : 9;
 	for (int p = 0; p < npos; p++) {
 		/* AdjacentCellsIterator order: x fastest over offsets -1..1 */
@@ -317,18 +322,23 @@ static void compute_lower_star(const mesh_t* m, const float* f, int64_t vx, int6
 		for (int a = 0; a < m->nd; a++) if (c[a] < 0 || c[a] >= m->d[a]) ok = 0;
 		if (!ok) continue;
 		if (extreme_vertex(m, f, c, 1) != vid) continue;   /* not in the lower star */
-		int bv = boundary_value(m, c);
-		lstar_t* L = &cls[bv];
+		int key = boundary_value(m, c) + (restrict_lab ? 3 * (int)restrict_lab[cell_id(m, c)] : 0);
+		if (key > N_CLASSES - 1) key = N_CLASSES - 1;
+		lstar_t* L = &cls[key];
 		L->id[L->n] = cell_id(m, c);
 		L->c[L->n][0] = c[0]; L->c[L->n][1] = c[1]; L->c[L->n][2] = c[2];
 		L->dim[L->n] = cell_dim(m, c);
 		L->n++;
 	}
-	for (int s = 0; s < 4; s++) {
+	for (int s = 0; s < N_CLASSES; s++) {
 		if (cls[s].n == 0) continue;
 		homotopy_expand(m, f, vcell, &cls[s]);
 		write_pairs(m, &cls[s], g);
 	}
+}
+
+static void compute_lower_star(const mesh_t* m, const float* f, int64_t vx, int64_t vy, int64_t vz, uint8_t* g) {
+	compute_lower_star_r(m, f, vx, vy, vz, g, NULL);
 }
 
 static int lstar_pairs(const mesh_t* m, const float* f, uint8_t* g, int nthreads) {
@@ -439,6 +449,96 @@ int oracle_grad_2d(const float* f, int64_t X, int64_t Y, uint8_t* g, int nt) {
 	int rc = oracle_lstar_pairs_2d(f, X, Y, g, nt);
 	if (!rc) rc = oracle_ldir_2d(X, Y, g);
 	if (!rc) rc = oracle_flag_2d(X, Y, g);
+	return rc;
+}
+
+/* ---- conforming gradient (ondemandaccurate's accurate 3-manifold .grad) --------- */
+
+/* VertexLabelingToBoundaryLabeling::ComputeMINBoundary (gi_labeling_to_bounary_labeling.h:48-116)
+ * with `asc`, then ComputeMAXBoundary (:118-199) with `dsc` (either may be NULL): edges
+ * whose two vertices carry different ascending labels (neither -1) get 1, then quads with
+ * such an edge, then hexes with such a quad; interior quads whose two hexes' highest
+ * vertices differ and carry different descending labels get +2, then interior edges
+ * with such a quad, then interior vertices with such an edge.  out: one byte per cell. */
+int oracle_boundary_labels_3d(const float* f, int64_t X, int64_t Y, int64_t Z, const int32_t* asc,
+                              const int32_t* dsc, uint8_t* out) {
+	mesh_t M; if (mesh_init(&M, 3, X, Y, Z)) return -1;
+	const mesh_t* m = &M;
+	memset(out, 0, (size_t)m->ncells);
+	if (asc) {
+		for (int dimc = 1; dimc <= 3; dimc++) {
+			for (int64_t i = 0; i < m->ncells; i++) {
+				int64_t c[3];
+				cell_coords(m, i, c);
+				if (cell_dim(m, c) != dimc) continue;
+				int64_t fc[6];
+				int nf = facets(m, i, c, fc);
+				if (dimc == 1) {
+					int32_t l1 = asc[vertex_number(m, fc[0])], l2 = asc[vertex_number(m, fc[1])];
+					if (l1 != -1 && l2 != -1 && l1 != l2) out[i] = 1;
+				} else {
+					for (int t = 0; t < nf; t++) if (out[fc[t]] == 1) { out[i] = 1; break; }
+				}
+			}
+		}
+	}
+	if (dsc) {
+		for (int dimc = 2; dimc >= 0; dimc--) {
+			for (int64_t i = 0; i < m->ncells; i++) {
+				int64_t c[3];
+				cell_coords(m, i, c);
+				if (cell_dim(m, c) != dimc || boundary_value(m, c) != 0) continue;
+				int64_t cf[6];
+				int ncf = cofacets(m, i, c, cf);
+				if (dimc == 2) {
+					int64_t c1[3], c2[3];
+					cell_coords(m, cf[0], c1);
+					cell_coords(m, cf[1], c2);
+					int64_t v1 = extreme_vertex(m, f, c1, 1), v2 = extreme_vertex(m, f, c2, 1);
+					if (v1 == v2) continue;
+					int32_t l1 = dsc[v1], l2 = dsc[v2];
+					if (l1 == -1 || l2 == -1) continue;
+					if (l1 != l2) out[i] = (uint8_t)(out[i] + 2);
+				} else {
+					for (int t = 0; t < ncf; t++) if (out[cf[t]] > 1) { out[i] = (uint8_t)(out[i] + 2); break; }
+				}
+			}
+		}
+	}
+	return 0;
+}
+
+/* The re-pairing of ondemandaccurate.cxx:1000-1063: every vertex that is restricted, or
+ * whose lower star holds a restricted cell, recomputes its lower star split by
+ * restriction label and boundaryValue (MyRobinsNoalloc<...,4,6>::ComputeLowerStar); then
+ * RecordGrad (:693-699): setAscendingManifoldDimensions and the boundary flag.  g: the
+ * base .grad in, the conforming .grad out. */
+int oracle_conform_3d(const float* f, int64_t X, int64_t Y, int64_t Z, const uint8_t* restrict_lab, uint8_t* g,
+                      int nthreads) {
+	mesh_t M; if (mesh_init(&M, 3, X, Y, Z)) return -1;
+	const mesh_t* m = &M;
+	int64_t nv = X * Y * Z;
+#ifdef _OPENMP
+	if (nthreads <= 0) nthreads = omp_get_max_threads();
+#pragma omp parallel for schedule(dynamic, 4096) num_threads(nthreads)
+#else
+	(void)nthreads;
+#endif
+	for (int64_t vi = 0; vi < nv; vi++) {
+		int64_t x = vi % X, y = (vi / X) % Y, z = vi / (X * Y);
+		int64_t vc[3] = { 2 * x, 2 * y, 2 * z };
+		int hasdiff = restrict_lab[cell_id(m, vc)] > 0;
+		for (int p = 0; p < 27 && !hasdiff; p++) {
+			int64_t c[3] = { vc[0] + (p % 3) - 1, vc[1] + (p / 3) % 3 - 1, vc[2] + (p / 9) - 1 };
+			int ok = 1;
+			for (int a = 0; a < 3; a++) if (c[a] < 0 || c[a] >= m->d[a]) ok = 0;
+			if (!ok) continue;
+			if (restrict_lab[cell_id(m, c)] > 0 && extreme_vertex(m, f, c, 1) == vi) hasdiff = 1;
+		}
+		if (hasdiff) compute_lower_star_r(m, f, x, y, z, g, restrict_lab);
+	}
+	int rc = ldir_mesh(m, g);
+	if (!rc) rc = flag_mesh(m, g);
 	return rc;
 }
 

@@ -33,6 +33,14 @@ int oracle_flag_2d(int64_t X, int64_t Y, uint8_t* grad);
 int oracle_grad_3d(const float* f, int64_t X, int64_t Y, int64_t Z, uint8_t* grad, int nthreads);
 int oracle_grad_2d(const float* f, int64_t X, int64_t Y, uint8_t* grad, int nthreads);
 
+/* Conforming gradient of ondemandaccurate's accurate 3-manifolds: the restriction labels
+ * of the final ascending (asc) / descending (dsc) labels (either may be NULL), then the
+ * constrained re-pairing of the touched vertices and the ldir / flag passes over g. */
+int oracle_boundary_labels_3d(const float* f, int64_t X, int64_t Y, int64_t Z, const int32_t* asc,
+                              const int32_t* dsc, uint8_t* out);
+int oracle_conform_3d(const float* f, int64_t X, int64_t Y, int64_t Z, const uint8_t* restrict_lab, uint8_t* g,
+                      int nthreads);
+
 /* Central-difference gradient, x,y,z (x,y) doubles per vertex, as the reference's
  * Vec3d array after ComputeGradFromImage(1). */
 int oracle_central_diff_3d(const float* f, int64_t X, int64_t Y, int64_t Z, double* g);

@@ -12,6 +12,11 @@
 //       DiscreteGradientLabeling::outputToFile             (gi_discrete_gradient_labeling.h:200)
 //   ref_lstar_grad_2d      == Accurate2D::DiscreteGradientBuilder::ComputeDiscreteGradient
 //       without saddle streamlines (gi_discrete_gradient_computer.h:538-686)
+//   ref_labels_3d[_threads] == ondemandaccurate/ondemandaccurate.cxx:795-948 (ASC and DSC
+//       3-manifold labels); with a .grad path also the accurate .grad of :795-1063 with
+//       needASC2 = needDSC2 = 1: VertexLabelingToBoundaryLabeling::ComputeMINBoundary /
+//       ComputeMAXBoundary, the constrained MyRobinsNoalloc<...,4,6>::ComputeLowerStar of
+//       the touched vertices and RecordGrad (:693-699)
 //
 // The only deviation from the shipped program: the mesh type is a thin subclass of
 // TopologicalRegularGrid3D that adds a no-op cellid2Coords(INDEX_TYPE, Vec2l&)
@@ -42,6 +47,7 @@
 #include "gi_extrema_region_builder.h"
 #include "gi_numeric_integrator_path_compressing.h"
 #include "gi_isolated_region_remover.h"
+#include "gi_labeling_to_bounary_labeling.h"
 
 using namespace GInt;
 
@@ -177,14 +183,36 @@ int ref_central_diff_3d(const float* f, long long X, long long Y, long long Z, d
 // reference's unique-id numbers mapped to the smallest seed vertex of their region
 // (the reference draws the numbers from unordered_map order).  stage (optional, 4*N):
 // terminal and integrated labels, ASC then DSC, mapped the same way.
+int ref_ondemand_3d(const float* f, long long X, long long Y, long long Z, float error_threshold,
+                    float gradient_threshold, int iteration_limit, float presimp, int* asc, int* dsc, int* stage,
+                    int nthreads, const char* grad_path, unsigned char* restrict_out);
 int ref_labels_3d(const float* f, long long X, long long Y, long long Z, float error_threshold,
                   float gradient_threshold, int iteration_limit, float presimp, int* asc, int* dsc, int* stage) {
+	return ref_ondemand_3d(f, X, Y, Z, error_threshold, gradient_threshold, iteration_limit, presimp, asc, dsc, stage,
+	                       1, nullptr, nullptr);
+}
+
+// The same at `nthreads` OpenMP threads: the reference's own run-to-run / thread-count
+// variation of the labels (its parallel first pass and fix-up race) is the yardstick
+// of the label tolerances.
+int ref_labels_3d_threads(const float* f, long long X, long long Y, long long Z, float error_threshold,
+                          float gradient_threshold, int iteration_limit, float presimp, int* asc, int* dsc,
+                          int* stage, int nthreads) {
+	return ref_ondemand_3d(f, X, Y, Z, error_threshold, gradient_threshold, iteration_limit, presimp, asc, dsc, stage,
+	                       nthreads, nullptr, nullptr);
+}
+
+// With grad_path: also the accurate .grad ondemandaccurate writes for needASC2 =
+// needDSC2 = 1 (and, optionally, the restriction labels, one byte per cell).
+int ref_ondemand_3d(const float* f, long long X, long long Y, long long Z, float error_threshold,
+                    float gradient_threshold, int iteration_limit, float presimp, int* asc, int* dsc, int* stage,
+                    int nthreads, const char* grad_path, unsigned char* restrict_out) {
 	using namespace refharness;
 	typedef IndexCompareLessThan<GridFuncType> ComparerASC;
 	typedef IndexCompareGreaterThan<GridFuncType> ComparerDSC;
 	typedef NumericIntegratorPathCompressingToTerminal<AdaptiveEulerAdvector3D<GridFuncType, -1>, GridFuncType> IntASC;
 	typedef NumericIntegratorPathCompressingToTerminal<AdaptiveEulerAdvector3D<GridFuncType, 1>, GridFuncType> IntDSC;
-	omp_set_num_threads(1);
+	omp_set_num_threads(nthreads > 0 ? nthreads : 1);
 	GridType* grid = new GridType(Vec3l(X, Y, Z), Vec3b(0, 0, 0));
 	std::vector<float> img(f, f + X * Y * Z);
 	GridFuncType* func = new GridFuncType(grid, img.data());
@@ -203,6 +231,11 @@ int ref_labels_3d(const float* f, long long X, long long Y, long long Z, float e
 	seg->SetMode(SimplifiedExtremumGraph<MeshType, TopoFuncType, GradType>::EXTGRAPHMODE::BOTH);
 	seg->ComputeMinMapFromGradient(presimp);
 	const long long N = X * Y * Z;
+	DenseLabeling<char>* restriction_labels = new DenseLabeling<char>(mesh->numCells());
+	restriction_labels->SetAll(0);
+	VertexLabelingToBoundaryLabeling<int, MaxVLType>* edge_map =
+		new VertexLabelingToBoundaryLabeling<int, MaxVLType>(mesh, restriction_labels);
+	edge_map->InitializeFirst();
 
 	auto canon = [&](const std::unordered_map<INT_TYPE, std::vector<INDEX_TYPE> >& idmap, DenseLabeling<int>* terminal) {
 		std::unordered_map<int, long long> c;
@@ -235,6 +268,7 @@ int ref_labels_3d(const float* f, long long X, long long Y, long long Z, float e
 			new IsolatedCCRegionRemoverNEW<ComparerASC, GridFuncType>(func, integ->GetOutputLabels());
 		cl->ComputeOutput();
 		write(asc, integ->GetOutputLabels(), c);
+		if (grad_path) edge_map->ComputeMINBoundary(integ->GetOutputLabels());
 	}
 	{
 		std::unordered_map<INDEX_TYPE, INT_TYPE> ext;
@@ -252,6 +286,35 @@ int ref_labels_3d(const float* f, long long X, long long Y, long long Z, float e
 			new IsolatedCCRegionRemoverNEW<ComparerDSC, GridFuncType>(func, integ->GetOutputLabels());
 		cl->ComputeOutput();
 		write(dsc, integ->GetOutputLabels(), c);
+		if (grad_path) edge_map->ComputeMAXBoundary(integ->GetOutputLabels(), maxv);
+	}
+	if (grad_path) {
+		// ondemandaccurate.cxx:1000-1063 (one thread): re-pair every vertex that is
+		// restricted or whose lower star holds a restricted cell, then RecordGrad
+		typedef MyRobinsNoalloc<MeshType, MaxVLType, GradType, 4, 6> RobinsType;
+		RobinsType* constrained = new RobinsType(mesh, maxv, restriction_labels, labeling);
+		MeshType::DCellsIterator verts(mesh, 0);
+		for (verts.begin(); verts.valid(); verts.advance()) {
+			INDEX_TYPE vert_GI = verts.value();
+			bool hasdiff = restriction_labels->GetLabel(vert_GI) > 0;
+			if (!hasdiff) {
+				MeshType::AdjacentCellsIterator edgeit(mesh);
+				for (edgeit.begin(vert_GI); edgeit.valid(); edgeit.advance()) {
+					INDEX_TYPE edge_GI = edgeit.value();
+					if (restriction_labels->GetLabel(edge_GI) > 0 && maxv->Cell2HighestVertex(edge_GI) == vert_GI) {
+						hasdiff = true;
+						break;
+					}
+				}
+			}
+			if (hasdiff) constrained->ComputeLowerStar(vert_GI);
+		}
+		TopologicalGradientUsingAlgorithms<MeshType, TopoFuncType, GradType>* alg =
+			new TopologicalGradientUsingAlgorithms<MeshType, TopoFuncType, GradType>(topofunc, mesh, labeling);
+		alg->setAscendingManifoldDimensions();
+		labeling->outputToFile(grad_path);
+		if (restrict_out)
+			for (long long i = 0; i < (long long)mesh->numCells(); i++) restrict_out[i] = (unsigned char)restriction_labels->GetLabel(i);
 	}
 	return 0;   // the reference objects are left to the process (their destructors double-free shared labels)
 }

@@ -3,7 +3,9 @@
 Run on a machine that has the reference sources (the oracle/Makefile `ref` target
 compiles oracle/_ref/libmsc_ref.so from them):
 
-    make -C oracle ref && python tests/golden/make_golden.py
+    make -C oracle ref && python tests/golden/make_golden.py [--large-only]
+
+(--large-only keeps grad_small.npz and rewrites grad_large.json).
 
 For every case it stores the float32 input and the bytes the reference's own
 steepest_lstar pipeline (3D) or 2D gradient builder wrote with
@@ -81,16 +83,18 @@ def summary(grad: np.ndarray, shape_xyz) -> dict:
 
 
 def main():
+    large_only = "--large-only" in sys.argv
     lib = ctypes.CDLL(str(REF))
     lib.ref_steepest_lstar_3d.argtypes = [ctypes.c_void_p, ctypes.c_longlong, ctypes.c_longlong,
                                           ctypes.c_longlong, ctypes.c_int, ctypes.c_char_p, ctypes.c_void_p]
     lib.ref_lstar_grad_2d.argtypes = [ctypes.c_void_p, ctypes.c_longlong, ctypes.c_longlong, ctypes.c_int,
                                       ctypes.c_char_p, ctypes.c_void_p]
     arrays = {}
-    for name, f in small_cases():
-        arrays[f"{name}__f"] = f
-        arrays[f"{name}__grad"] = run_ref(lib, f)
-    np.savez_compressed(HERE / "grad_small.npz", **arrays)
+    if not large_only:
+        for name, f in small_cases():
+            arrays[f"{name}__f"] = f
+            arrays[f"{name}__grad"] = run_ref(lib, f)
+        np.savez_compressed(HERE / "grad_small.npz", **arrays)
 
     big = {}
     # the bit-exact steepest_lstar workload: 64^3, 16 Gaussians, seed 0
@@ -106,6 +110,17 @@ def main():
     g = run_ref(lib, f)
     big["k3_2d_512x384"] = {"generator": "power_law_field((512,384), seed=5)",
                             "f_sha256": hashlib.sha256(f.tobytes()).hexdigest(), **summary(g, (512, 384))}
+    # the .grad scale workload: 512^3 and 8192^2 k^-3 fields, seed 0
+    f = fields.power_law_field((512, 512, 512), seed=0)
+    g = run_ref(lib, f)
+    big["k3_512cubed"] = {"generator": "power_law_field((512,512,512), seed=0)",
+                          "f_sha256": hashlib.sha256(f.tobytes()).hexdigest(), **summary(g, (512, 512, 512))}
+    del f, g
+    f = fields.power_law_field((8192, 8192), seed=0)
+    g = run_ref(lib, f)
+    big["k3_8192sq"] = {"generator": "power_law_field((8192,8192), seed=0)",
+                        "f_sha256": hashlib.sha256(f.tobytes()).hexdigest(), **summary(g, (8192, 8192))}
+    del f, g
     (HERE / "grad_large.json").write_text(json.dumps(big, indent=1) + "\n")
     print(f"wrote {len(arrays) // 2} small cases and {len(big)} large summaries")
 

@@ -45,6 +45,8 @@ class Oracle:
                                          _VP, _VP, _VP]
         lib.oracle_terminal_regions_3d.argtypes = [_VP, _VP, _I64, _I64, _I64, ctypes.c_int, ctypes.c_float, _VP]
         lib.oracle_clean_regions_3d.argtypes = [_VP, _I64, _I64, _I64, ctypes.c_int, _VP]
+        lib.oracle_boundary_labels_3d.argtypes = [_VP, _I64, _I64, _I64, _VP, _VP, _VP]
+        lib.oracle_conform_3d.argtypes = [_VP, _I64, _I64, _I64, _VP, _VP, ctypes.c_int]
 
     def labels(self, f, grad, error_threshold, gradient_threshold, iteration_limit, max_step, presimp):
         """ASC and DSC labels (regions named by their smallest seed vertex) plus stages."""
@@ -68,6 +70,25 @@ class Oracle:
         out = np.array(labels, dtype=np.int32, copy=True)
         assert self.lib.oracle_clean_regions_3d(f.ctypes.data, *f.shape[::-1], int(direction), out.ctypes.data) == 0
         return out
+
+    def boundary_labels(self, f, asc, dsc):
+        """VertexLabelingToBoundaryLabeling MIN (asc) then MAX (dsc) restriction labels."""
+        f = np.ascontiguousarray(f, dtype=np.float32)
+        n = int(np.prod([2 * d - 1 for d in f.shape]))
+        out = np.empty(n, np.uint8)
+        a = None if asc is None else np.ascontiguousarray(asc, dtype=np.int32)
+        d = None if dsc is None else np.ascontiguousarray(dsc, dtype=np.int32)
+        assert self.lib.oracle_boundary_labels_3d(f.ctypes.data, *f.shape[::-1], None if a is None else a.ctypes.data,
+                                                  None if d is None else d.ctypes.data, out.ctypes.data) == 0
+        return out
+
+    def conform(self, f, restrict, base_grad, nthreads=0):
+        """The accurate 3-manifold .grad from the base .grad and the restriction labels."""
+        f = np.ascontiguousarray(f, dtype=np.float32)
+        g = np.array(base_grad, dtype=np.uint8, copy=True)
+        r = np.ascontiguousarray(restrict, dtype=np.uint8)
+        assert self.lib.oracle_conform_3d(f.ctypes.data, *f.shape[::-1], r.ctypes.data, g.ctypes.data, nthreads) == 0
+        return g
 
     def central_diff(self, f: np.ndarray) -> np.ndarray:
         """(..., ND) float64 gradient, the reference's Vec3d array."""
@@ -129,6 +150,9 @@ def load_ref():
     lib.ref_central_diff_3d.argtypes = [_VP, ctypes.c_longlong, ctypes.c_longlong, ctypes.c_longlong, _VP]
     lib.ref_labels_3d.argtypes = [_VP, ctypes.c_longlong, ctypes.c_longlong, ctypes.c_longlong, ctypes.c_float,
                                   ctypes.c_float, ctypes.c_int, ctypes.c_float, _VP, _VP, _VP]
+    lib.ref_ondemand_3d.argtypes = [_VP, ctypes.c_longlong, ctypes.c_longlong, ctypes.c_longlong, ctypes.c_float,
+                                    ctypes.c_float, ctypes.c_int, ctypes.c_float, _VP, _VP, _VP, ctypes.c_int,
+                                    ctypes.c_char_p, _VP]
     return lib
 
 
@@ -146,6 +170,24 @@ def ref_labels(lib, f, error_threshold, gradient_threshold, iteration_limit, pre
     for i, k in enumerate(STAGES):
         out[k] = st[i * n:(i + 1) * n]
     return out
+
+
+def ref_ondemand(lib, f, error_threshold, gradient_threshold, iteration_limit, presimp):
+    """ondemandaccurate with needASC2 = needDSC2 = 1 at one thread: the final ASC / DSC
+    labels, the restriction labels and the accurate .grad it writes."""
+    f = np.ascontiguousarray(f, dtype=np.float32)
+    n = f.size
+    nc = int(np.prod([2 * d - 1 for d in f.shape]))
+    asc = np.empty(n, np.int32)
+    dsc = np.empty(n, np.int32)
+    restrict = np.empty(nc, np.uint8)
+    with tempfile.TemporaryDirectory() as td:
+        path = os.path.join(td, "o.grad").encode()
+        assert lib.ref_ondemand_3d(f.ctypes.data, *f.shape[::-1], error_threshold, gradient_threshold,
+                                   iteration_limit, presimp, asc.ctypes.data, dsc.ctypes.data, None, 1, path,
+                                   restrict.ctypes.data) == 0
+        grad = np.fromfile(path.decode(), dtype=np.uint8)
+    return {"asc": asc, "dsc": dsc, "restrict": restrict, "grad": grad}
 
 
 def ref_grad(lib, f: np.ndarray, nthreads: int = 4) -> np.ndarray:

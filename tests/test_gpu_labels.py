@@ -1,9 +1,12 @@
-"""The CUDA labeling chain against the FP64 oracle (itself equal to the reference
-at one thread).  Terminal regions are exact; integrated labels are compared as
-partitions (regions are named by their extremum vertex on both sides) and the
-fraction of differing vertices is bounded -- the reference's own multi-threaded
-runs differ from each other by ~1e-4 of the vertices before and ~3.5e-3 after
-its cleaner."""
+"""The CUDA labeling chain against the FP64 oracle (itself equal to the reference at
+one thread).  Terminal regions are exact; integrated labels are compared as partitions
+(regions are named by their extremum vertex on both sides).  The tolerance of every
+field is the reference's own variation there: the largest fraction of vertices by which
+its labels at 8 OpenMP threads differ from its labels at one thread
+(tests/golden/ref_label_noise.json, written by tests/golden/ref_label_noise.py)."""
+import json
+from pathlib import Path
+
 import numpy as np
 import pytest
 
@@ -12,9 +15,13 @@ from msceer_gb300 import fields
 
 pytestmark = pytest.mark.gpu
 
-# stated tolerances: fraction of vertices whose label differs from the FP64 oracle
-TOL_INTEGRATED = 0.02
-TOL_FINAL = 0.02
+NOISE = json.loads((Path(__file__).resolve().parent / "golden" / "ref_label_noise.json").read_text())["fields"]
+
+
+def tolerance(name, key):
+    """The reference's own 8-thread-vs-1-thread difference for field `name` and label set
+    `key` (asc / dsc final, or *_integrated)."""
+    return NOISE[name][key]
 
 
 def run_both(f, device, oracle, precision=0):
@@ -38,22 +45,36 @@ FIELDS = {
 }
 
 
+def check_against_oracle(name, got, want):
+    report = {k: float((got[k] != want[k]).mean())
+              for k in ("asc_terminal", "dsc_terminal", "asc_integrated", "dsc_integrated", "asc", "dsc")}
+    print(name, report, got.get("stats"))
+    assert report["asc_terminal"] == 0.0 and report["dsc_terminal"] == 0.0, report
+    for k in ("asc_integrated", "dsc_integrated", "asc", "dsc"):
+        assert report[k] <= tolerance(name, k), (k, report[k], tolerance(name, k))
+    # every label names an extremum vertex of the right kind
+    for k in ("asc", "dsc"):
+        assert (np.unique(got[k]) >= -1).all()
+    return report
+
+
 @pytest.mark.parametrize("precision", [0, 1])
 @pytest.mark.parametrize("name", list(FIELDS))
 def test_labels_vs_oracle(gpu, oracle, name, precision):
     f = FIELDS[name]()
     got, want = run_both(f, gpu, oracle, precision)
-    report = {}
-    for k in ("asc_terminal", "dsc_terminal", "asc_integrated", "dsc_integrated", "asc", "dsc"):
-        report[k] = float((got[k] != want[k]).mean())
-    print(name, "precision", precision, report, got["stats"])
-    assert report["asc_terminal"] == 0.0 and report["dsc_terminal"] == 0.0, report
-    assert report["asc_integrated"] <= TOL_INTEGRATED and report["dsc_integrated"] <= TOL_INTEGRATED, report
-    assert report["asc"] <= TOL_FINAL and report["dsc"] <= TOL_FINAL, report
-    # every label names an extremum vertex of the right kind
-    for k in ("asc", "dsc"):
-        labs = np.unique(got[k])
-        assert (labs >= -1).all()
+    check_against_oracle(name, got, want)
+
+
+def test_labeling_workload_256_cubed_vs_oracle(gpu, oracle):
+    """The 256^3 labeling workload: 64 Gaussians (seed 0), error threshold 1e-4, gradient
+    threshold 1e-6 max|f|, 4000 iterations of at most 0.25 voxel, both directions.  The
+    FP64 oracle takes about 1.5 minutes here (one thread, as the reference's
+    deterministic mode)."""
+    f = fields.gaussian_sum((256, 256, 256), 64, seed=0)
+    got, want = run_both(f, gpu, oracle, 0)
+    report = check_against_oracle("gauss256_cfg2", got, want)
+    assert report["asc"] <= 3.5e-3 and report["dsc"] <= 3.5e-3
 
 
 def test_batch_labels_on_concurrent_streams_equal_sequential(gpu):
@@ -122,7 +143,7 @@ def test_labels_with_merge_threshold_vs_oracle(gpu, oracle, name):
     for k in ("asc_terminal", "dsc_terminal"):
         assert (got[k] == want[k]).all(), (k, float((got[k] != want[k]).mean()))
     for k in ("asc", "dsc"):
-        assert float((got[k] != want[k]).mean()) <= TOL_FINAL
+        assert float((got[k] != want[k]).mean()) <= tolerance(name, k)
 
 
 @pytest.mark.parametrize("name", list(FIELDS))

@@ -25,6 +25,8 @@ def core(tmp_path_factory):
     lib.core_pairs_3d.argtypes = [ctypes.c_void_p, ctypes.c_int64, ctypes.c_int64, ctypes.c_int64,
                                   ctypes.c_void_p, ctypes.c_uint32]
     lib.core_pairs_2d.argtypes = [ctypes.c_void_p, ctypes.c_int64, ctypes.c_int64, ctypes.c_void_p, ctypes.c_uint32]
+    lib.core_conform_3d.argtypes = [ctypes.c_void_p, ctypes.c_int64, ctypes.c_int64, ctypes.c_int64, ctypes.c_void_p,
+                                    ctypes.c_void_p, ctypes.c_uint32]
     return lib
 
 
@@ -97,3 +99,34 @@ def test_core_2d(core, oracle):
     for shape in [(300, 211), (1, 40), (40, 1)]:
         f = fields.quantized(fields.power_law_field(shape, seed=2), 4)
         check(core, oracle, f)
+
+
+@pytest.mark.parametrize("shape", [(40, 36, 32), (31, 17, 9), (33, 2, 20)])
+def test_core_conform(core, oracle, shape):
+    """The conforming re-pairing of the kernel core against the oracle: the restriction
+    labels of the oracle's own final labels, the recomputed lower stars, then the
+    closure and flag of both must give the same bytes."""
+    f = fields.gaussian_sum(shape, 8, seed=5)
+    gt = 1e-6 * float(np.abs(f).max())
+    base = oracle.grad(f)
+    lab = oracle.labels(f, base, 1e-4, gt, 4000, 0.25, 0.0)
+    restrict = oracle.boundary_labels(f, lab["asc"], lab["dsc"])
+    assert (restrict > 0).any()
+    want = oracle.conform(f, restrict, base)
+    dims = f.shape[::-1]
+    got = base.copy()
+    n = core.core_conform_3d(np.ascontiguousarray(f).ctypes.data, *dims, restrict.ctypes.data, got.ctypes.data,
+                             enc_map(dims))
+    assert n > 0
+    # the recomputed cells carry closure roots: run the closure (and the flag) as the library does
+    d = [2 * v - 1 for v in dims]
+    ids = np.arange(got.size)
+    dim = sum(ci & 1 for ci in (ids % d[0], (ids // d[0]) % d[1], ids // (d[0] * d[1])))
+    crit = ((got >> 2) & 7) == 7
+    root = np.full(got.size, 3, dtype=np.uint8)
+    root[crit & (dim == 1)] = 2
+    root[crit & (dim == 2)] = 1
+    root[crit & (dim == 3)] = 0
+    got = (got & 0x1F) | (root << 5)
+    assert np.array_equal(oracle.ldir(got, dims), want), oracle_lib.describe_mismatch(oracle.ldir(got, dims), want,
+                                                                                       dims)

@@ -111,3 +111,24 @@ def test_label_oracle_against_compiled_reference(oracle):
         got = oracle.labels(f, oracle.grad(f), 1e-4, gt, 4000, 0.25, 0.0)
         for k in want:
             assert np.array_equal(got[k], want[k]), (f.shape, k, int((got[k] != want[k]).sum()))
+
+
+@pytest.mark.parametrize("make", [lambda: fields.gaussian_sum((40, 36, 32), 8, seed=5),
+                                  lambda: fields.power_law_field((32, 30, 28), seed=6)], ids=["gauss40", "k3_32"])
+def test_conforming_grad_oracle_against_reference(oracle, make):
+    """ondemandaccurate's accurate 3-manifold .grad: the oracle's restriction labels and
+    constrained re-pairing, fed the reference's own final labels, give the reference's
+    restriction labels and .grad byte for byte."""
+    ref = oracle_lib.load_ref()
+    if ref is None:
+        pytest.skip("the reference is not compiled on this machine")
+    f = make()
+    gt = 1e-6 * float(np.abs(f).max())
+    want = oracle_lib.ref_ondemand(ref, f, 1e-4, gt, 4000, 0.0)
+    restrict = oracle.boundary_labels(f, want["asc"], want["dsc"])
+    assert np.array_equal(restrict, want["restrict"]), int((restrict != want["restrict"]).sum())
+    assert (restrict > 0).any()
+    base = oracle.grad(f)
+    got = oracle.conform(f, restrict, base)
+    assert np.array_equal(got, want["grad"]), oracle_lib.describe_mismatch(got, want["grad"], f.shape[::-1])
+    assert not np.array_equal(got, base)   # the re-pairing changed something
