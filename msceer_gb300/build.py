@@ -1,7 +1,7 @@
 """Builds the native parts in-tree for sm_103a.
 
 * ``msceer_gb300/libmsc_gpu.so``  -- the CUDA kernels + C ABI (include/msc_gpu.h)
-* ``msceer_gb300/bin/steepest_lstar`` -- the drop-in CLI (C++ over the C ABI)
+* ``msceer_gb300/bin/steepest_lstar``, ``ondemandaccurate`` -- the drop-in CLIs (C++ over the C ABI)
 
 Translation units compile in parallel with one ``-gencode`` so a fresh machine
 builds in well under a minute.  ``python -m msceer_gb300.build`` runs it.
@@ -77,16 +77,19 @@ def build_library(verbose: bool = False, force: bool = False) -> Path:
 
 
 def build_cli(verbose: bool = False, force: bool = False) -> Path:
+    """The drop-in command lines (C++ over the C ABI): steepest_lstar, ondemandaccurate."""
     BIN.mkdir(exist_ok=True)
-    exe = BIN / "steepest_lstar"
-    src = PKG / "cli" / "steepest_lstar.cpp"
-    if force or _stale(exe, [src, LIB, ROOT / "include" / "msc_gpu.h"]):
-        cxx = os.environ.get("CXX", "g++")
-        cuda_lib = Path(_nvcc()).resolve().parent.parent / "lib64"
-        _run([cxx, "-O2", "-std=c++17", "-I", ROOT / "include", src, "-o", exe,
-              "-L", PKG, "-lmsc_gpu", f"-Wl,-rpath,$ORIGIN/..", "-L", cuda_lib, "-lcudart",
-              f"-Wl,-rpath,{cuda_lib}"], verbose)
-    return exe
+    cxx = os.environ.get("CXX", "g++")
+    cuda = Path(_nvcc()).resolve().parent.parent
+    cuda_lib = cuda / "lib64"
+    for name in ("steepest_lstar", "ondemandaccurate"):
+        exe = BIN / name
+        src = PKG / "cli" / f"{name}.cpp"
+        if force or _stale(exe, [src, LIB, ROOT / "include" / "msc_gpu.h"]):
+            _run([cxx, "-O2", "-std=c++17", "-I", ROOT / "include", "-I", cuda / "include", src, "-o", exe,
+                  "-L", PKG, "-lmsc_gpu", f"-Wl,-rpath,$ORIGIN/..", "-L", cuda_lib, "-lcudart",
+                  f"-Wl,-rpath,{cuda_lib}"], verbose)
+    return BIN / "steepest_lstar"
 
 
 def build_oracle(verbose: bool = False) -> None:

@@ -67,6 +67,15 @@ def test_cli_usage_message():
     assert "Usage: X Y Z filename per_x per_y per_z" in res.stdout
 
 
+def test_ondemandaccurate_usage_message():
+    build.build_cli()
+    exe = build.BIN / "ondemandaccurate"
+    for args in ([], ["64", "64", "64", "f.raw", "1e-4", "1e-6", "4000", "0", "0", "1", "1"]):  # 11: one short
+        res = subprocess.run([str(exe), *args], capture_output=True, text=True)
+        assert res.returncode == 0
+        assert "Usage: X Y Z filename error_threshold grad_threshold maxnumiter" in res.stdout
+
+
 def test_api_mesh_mirror():
     from msceer_gb300 import TopologicalRegularGrid3D, DiscreteGradientLabeling
     import numpy as np
