@@ -203,9 +203,13 @@ void msc_trim_scratch(void);
  * applications that hand out all device memory through their own pool and do not
  * let libraries call cudaMalloc.  Limit: 524,288 ldir tiles of 32x32x16 cells
  * (volumes up to about 1000^3 vertices); larger volumes return MSC_ERR_TOO_LARGE.
- * The first call on a device looks up the array's device address; make that call
- * before any stream capture.  Every call shares the array: calls whose work
- * overlaps on the GPU race.  Calls no cudaMalloc / cudaFree. */
+ * Dims as msc_ascending_manifold_dims_3d (an axis may have a single vertex).  The
+ * first call on a device looks up the array's device address and keeps it for the
+ * process (do not use the entry on a device after cudaDeviceReset).  The call
+ * synchronises `stream` once per pass, so it must not be made during stream capture.
+ * passes_out counts the tile passes of this multi-pass form (the allocating entry
+ * counts the launches of its single-pass form).  Every call shares the array: calls
+ * whose work overlaps on the GPU race.  Calls no cudaMalloc / cudaFree. */
 int msc_ascending_manifold_dims_3d_static(uint8_t* grad, const int64_t dims[3], msc_stream_t stream, int* passes_out);
 
 /* Host-memory convenience with steepest_lstar's semantics: copies f to the GPU,

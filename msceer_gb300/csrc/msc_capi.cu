@@ -85,6 +85,14 @@ bool make_dims(int nd, const int64_t* dims, msc::GradDims* D) {
   return true;
 }
 
+}  // namespace
+
+namespace msc {
+bool make_grad_dims(int nd, const int64_t* dims, GradDims* D) { return make_dims(nd, dims, D); }
+}  // namespace msc
+
+namespace {
+
 struct Scratch {
   int* words = nullptr;  // [0] error bits, [1] changed flag
   cudaStream_t stream = nullptr;

@@ -12,9 +12,11 @@
 // the library holds it until the process exits.  Its host-side name is only a
 // stand-in for the device object, so the host asks the runtime for the device
 // address once per device (cudaGetSymbolAddress, with that device current) and
-// passes that address to the kernels.  Every call shares the array and leaves the
-// last call's contents in it; each call clears what must start at zero.  Two calls
-// whose work overlaps on the GPU (e.g. on two streams) race on the shared array.
+// passes that address to the kernels; the address is kept for the process, so the
+// entry must not be used on a device after cudaDeviceReset there.  Every call shares
+// the array and leaves the last call's contents in it; each call clears what must
+// start at zero.  Two calls whose work overlaps on the GPU (e.g. on two streams) race
+// on the shared array.
 #include <cuda_runtime.h>
 
 #include <mutex>
@@ -69,18 +71,9 @@ extern "C" int msc_ascending_manifold_dims_3d_static(uint8_t* grad, const int64_
                                                       int* passes_out) {
   if (!grad || !dims) return msc::set_last_error(MSC_ERR_NULL_POINTER, "null argument");
   msc::GradDims D{};
-  for (int a = 0; a < 3; a++) {
-    if (dims[a] < 2 || dims[a] > ((int64_t)1 << 30)) return msc::set_last_error(MSC_ERR_BAD_DIMS, "invalid dims");
-    D.v[a] = dims[a];
-    D.d[a] = 2 * dims[a] - 1;
-  }
-  D.cs[0] = 1;
-  D.cs[1] = D.d[0];
-  D.cs[2] = D.d[0] * D.d[1];
-  D.ncells = D.d[0] * D.d[1] * D.d[2];
-  D.enc_map = 0x2C688u;  // identity: every axis has at least two vertices
-  D.dec_map = 0x2C688u;
+  if (!msc::make_grad_dims(3, dims, &D)) return msc::set_last_error(MSC_ERR_BAD_DIMS, "invalid dims");
   const int64_t ntiles = msc::ldir_num_tiles(3, D);
+  if (ntiles <= 0) return msc::set_last_error(MSC_ERR_BAD_DIMS, "invalid dims");
   if (ntiles > kStaticMaxTiles) {
     const std::string m = "volume needs " + std::to_string(ntiles) + " ldir tiles; the static scratch holds " +
                           std::to_string(kStaticMaxTiles) + " (use msc_ascending_manifold_dims_3d)";
@@ -120,6 +113,7 @@ extern "C" int msc_ascending_manifold_dims_3d_static(uint8_t* grad, const int64_
       (e = cudaStreamSynchronize(st)) != cudaSuccess)
     return msc::set_last_error(MSC_ERR_CUDA, cudaGetErrorString(e));
   if (err & msc::kErrLocalQueue) return msc::set_last_error(MSC_ERR_QUEUE_OVERFLOW, "ldir tile queue overflow");
+  if (err & msc::kErrPassLimit) return msc::set_last_error(MSC_ERR_ITER_LIMIT, "ldir closure did not converge");
   if (passes_out) *passes_out = passes;
   return MSC_OK;
 }
