@@ -21,14 +21,21 @@ against the plain labels), or timed as the step with --triage.
   e2e         the same metric through the C ABI host entry msc_ondemand_labels_host:
               H2D of f, .grad, labels, D2H of both label volumes per step
   grad        the .grad alone: Gvert/s and its per-kernel breakdown
+  grad_2d     the .grad of the 8192^2 k^-3 field (2D): Gvert/s, kernels, roofline
   roofline    the dominant .grad kernel's algorithmic bytes / its measured duration
               against the measured HBM copy bandwidth (MEASURED_PEAKS.json)
+  mismatch_vs_fp64_oracle  the labeling workload (256^3, 64 Gaussians, seed 0): the
+              fraction of vertices whose plain / learned labels differ from the FP64
+              oracle's (the reference's one-thread algorithm, run on the host during
+              the timing), beside the reference's own 8-thread-vs-1-thread variation
   cpu_baseline  the CPU port of the reference algorithm (oracle/) on bounded samples
-              of the same volume: .grad on a z-slab (all threads), labels on small
-              sub-volumes (one process per core)
+              of the same volume: .grad on a z-slab (all threads), labels of full
+              x-y slabs (one single-threaded process per core)
 
 `--impl reference` times the reference's CPU algorithm alone (the port: the
 reference's own sources are not on the GPU host) on the same metric.
+`--grad-only` times the .grad alone (`--2d`: of the 8192^2 field); `--workload labels`
+makes the 256^3 labeling workload the step.
 """
 from __future__ import annotations
 
@@ -69,6 +76,10 @@ def parse_args():
     p.add_argument("--no-triage", action="store_true", help="skip the learned triage altogether")
     p.add_argument("--grad-only", action="store_true", help="time the .grad alone as the step")
     p.add_argument("--no-batch", action="store_true", help="skip the 64-volume batching measurement")
+    p.add_argument("--2d", dest="two_d", action="store_true", help="with --grad-only: the 8192^2 .grad")
+    p.add_argument("--workload", choices=["k3", "labels"], default="k3",
+                   help="k3: the 512^3 k^-3 field (default); labels: the 256^3 64-Gaussian labeling workload")
+    p.add_argument("--no-oracle", action="store_true", help="skip the FP64-oracle label comparison")
     return p.parse_args()
 
 
@@ -166,6 +177,30 @@ class ClockSampler:
                 "reasons": reasons, "samples": len(rows)}
 
 
+NOISE_FILE = ROOT / "tests" / "golden" / "ref_label_noise.json"
+
+
+def labels_field(seed: int = 0) -> np.ndarray:
+    """The labeling workload: 256^3 float32, 64 Gaussians + U[-1e-3, 1e-3] noise."""
+    from msceer_gb300 import fields
+    return fields.gaussian_sum((256, 256, 256), 64, seed=seed)
+
+
+def _oracle_labels_job(path: str, q) -> None:
+    """FP64 oracle labels of the labeling workload (a spawned process): the reference's
+    one-thread algorithm, written to `path`; its labeling time goes to `q`."""
+    import oracle_lib
+    f = labels_field()
+    orc = oracle_lib.load()
+    g = orc.grad(f, nthreads=0)
+    gt = 1e-6 * float(np.abs(f).max())
+    t0 = time.perf_counter()
+    lab = orc.labels(f, g, INTEG["error_threshold"], gt, INTEG["iteration_limit"], INTEG["max_step"],
+                     INTEG["presimp_threshold"])
+    np.savez(path, asc=lab["asc"], dsc=lab["dsc"])
+    q.put(time.perf_counter() - t0)
+
+
 def _label_crop_worker(args):
     """One oracle labeling of a sub-volume (run in a spawned process)."""
     crop, = args
@@ -201,11 +236,11 @@ def cpu_baseline(f: np.ndarray, grad_only: bool = False):
         out["value"] = g_grad
         out["sample"] = desc
         return out
-    c = 40
+    c = 4  # z-planes per slab: full x-y extent, so streamlines run as long as in the volume
     crops = []
     for i in range(nthreads):
-        z0, y0, x0 = (i * 37) % (n - c), (i * 53) % (n - c), (i * 71) % (n - c)
-        crops.append((np.ascontiguousarray(f[z0:z0 + c, y0:y0 + c, x0:x0 + c]),))
+        z0 = (i * (n - c)) // max(1, nthreads - 1) if nthreads > 1 else 0
+        crops.append((np.ascontiguousarray(f[z0:z0 + c]),))
     ctx = mp.get_context("spawn")
     t1 = time.perf_counter()
     with ctx.Pool(nthreads) as pool:
@@ -216,16 +251,29 @@ def cpu_baseline(f: np.ndarray, grad_only: bool = False):
     g_lab = nv / busy / 1e9
     out["labels_gvps"] = g_lab
     out["value"] = 1.0 / (1.0 / g_grad + 1.0 / g_lab)
-    out["sample"] = (desc + f"; labels (FP64 oracle, path compression) of {len(crops)} sub-volumes of {c}^3 in "
-                     f"{len(crops)} spawned processes, slowest {busy:.2f} s (pool wall {wall:.2f} s); "
-                     "value = harmonic combination of the two rates")
+    out["sample"] = (desc + f"; labels (FP64 oracle, one thread each) of {len(crops)} z-slabs "
+                     f"{f.shape[2]}x{f.shape[1]}x{c} in {len(crops)} spawned processes, slowest {busy:.2f} s "
+                     f"(pool wall {wall:.2f} s); value = harmonic combination of the two rates")
     return out
+
+
+def bench_volume(args, rank):
+    """The step's volume: (f, dims (x, y[, z]), edge, description)."""
+    if args.grad_only and args.two_d:
+        from msceer_gb300 import fields
+        return fields.power_law_field((8192, 8192), seed=rank), (8192, 8192), 8192, \
+            "8192^2 float32 k^-3 Gaussian random field"
+    if args.workload == "labels":
+        return labels_field(seed=rank), (256, 256, 256), 256, \
+            "256^3 float32 sum of 64 Gaussians + noise (the labeling workload)"
+    n = args.size
+    return make_volume(n, seed=rank), (n, n, n), n, f"{n}^3 float32 k^-3 Gaussian random field"
 
 
 def run_reference(args, ws, rank):
     if rank != 0:
         return
-    f = make_volume(args.size)
+    f, dims, n, wl_name = bench_volume(args, 0)
     vals = []
     r = None
     for i in range(args.warmup + args.steps):
@@ -238,7 +286,7 @@ def run_reference(args, ws, rank):
             "scaling": "weak", "vs_baseline": None, "dtype": "f32" if args.grad_only else "f32+f64",
             "data": "synthetic", "impl": "reference",
             "config": {"workload": f"{'.grad' if args.grad_only else '.grad + integrated labels'}, "
-                                   f"{args.size}^3 k^-3 GRF seed 0, bounded CPU samples per step",
+                                   f"{wl_name}, seed 0, bounded CPU samples per step",
                        "sample": r["sample"]},
             "cpu_baseline": {"value": v, "unit": UNIT, "cores": r["cores"], "kind": "port", "sample": r["sample"]},
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
@@ -250,10 +298,66 @@ def _events(n):
     return [torch.cuda.Event(enable_timing=True) for _ in range(n)]
 
 
+def grad_stage_times(f_dev, g_dev, dims, reps, stream, dev):
+    """CUDA-event times (ms) of the .grad's two stages and of the whole .grad, averaged
+    over `reps` runs, and the ldir stage's kernel launches over those runs."""
+    import torch
+    from msceer_gb300 import ascending_manifold_dims, lower_star_grad, lower_star_pairs
+    s0, s1, s2 = _events(3)
+    t_pairs = t_ldir = t_grad = 0.0
+    nlaunch = 0
+    for _ in range(reps):
+        s0.record(stream)
+        lower_star_pairs(f_dev, out=g_dev)
+        s1.record(stream)
+        nlaunch += ascending_manifold_dims(g_dev, dims)
+        s2.record(stream)
+        torch.cuda.synchronize(dev)
+        t_pairs += s0.elapsed_time(s1)
+        t_ldir += s1.elapsed_time(s2)
+    for _ in range(reps):
+        s0.record(stream)
+        lower_star_grad(f_dev, out=g_dev)
+        s1.record(stream)
+        torch.cuda.synchronize(dev)
+        t_grad += s0.elapsed_time(s1)
+    return t_pairs / reps, t_ldir / reps, t_grad / reps, nlaunch
+
+
+def grad_kernels(V, C, t_pairs, t_ldir, nlaunch, reps, n, peak, peak_kind):
+    """Per-stage algorithmic bandwidth of the .grad and the roofline of its dominant stage."""
+    alg_pairs = 4 * V + C            # read f once, write every .grad byte once
+    alg_ldir = 2 * C                 # the ascending-manifold stage reads and writes the .grad
+    kernels = {
+        "lstar_kernel": {"launches_per_step": 1, "ms_per_launch": t_pairs,
+                         "algorithmic_bytes": alg_pairs, "gbs": alg_pairs / (t_pairs * 1e-3) / 1e9},
+        "ldir_stage": {"launches_per_step": nlaunch / reps, "ms_per_stage": t_ldir,
+                       "algorithmic_bytes": alg_ldir, "gbs": alg_ldir / (t_ldir * 1e-3) / 1e9,
+                       "kernels": "ldir_tile_kernel + ldir_check_kernel + ldir_walk_kernel"},
+    }
+    dom = "lstar_kernel" if t_pairs >= t_ldir else "ldir_stage"
+    kd = kernels[dom]
+    roofline = {"kernel": dom, "bound": "hbm", "achieved": kd["gbs"], "peak": peak, "unit": "GB/s",
+                "frac": kd["gbs"] / peak, "peak_kind": f"{peak_kind} hbm_gbs", "traffic": TRAFFIC_PER_LAUNCH.get((dom, n)),
+                "scope": "dominant kernel of the .grad; the label integration that dominates the full step is "
+                         "FP32/FP64 issue-bound, neither HBM nor tensor bound"}
+    return kernels, roofline
+
+
 def run_ours(args, ws, rank, local):
     import torch
-    from msceer_gb300 import _lib, ascending_manifold_dims, integrated_labels, lower_star_grad, lower_star_pairs, \
-        num_cells, triage
+    from msceer_gb300 import _lib, integrated_labels, lower_star_grad, num_cells, triage
+
+    # the FP64 oracle of the labeling workload runs on the host while the GPU is timed
+    oracle_job = None
+    if rank == 0 and not args.grad_only and not args.no_oracle:
+        import multiprocessing as mp
+        ctx = mp.get_context("spawn")
+        oq = ctx.Queue()
+        opath = os.path.join(tempfile.mkdtemp(prefix="msc_oracle_"), "labels.npz")
+        oproc = ctx.Process(target=_oracle_labels_job, args=(opath, oq))
+        oproc.start()
+        oracle_job = (oproc, oq, opath)
 
     dev = torch.device("cuda", local)
     torch.cuda.set_device(dev)
@@ -264,10 +368,8 @@ def run_ours(args, ws, rank, local):
         pg = dist
     lib = _lib.load()
 
-    n = args.size
-    f_np = make_volume(n, seed=rank)  # each replica its own volume
-    dims = (n, n, n)
-    V = n ** 3
+    f_np, dims, n, wl_name = bench_volume(args, rank)  # each replica its own volume
+    V = int(np.prod(dims))
     C = num_cells(dims)
     f_host = torch.from_numpy(f_np).pin_memory()
     f_dev = f_host.to(dev)
@@ -319,48 +421,34 @@ def run_ours(args, ws, rank, local):
 
     # the .grad alone and its stages, on the launching stream
     reps = max(3, min(args.steps, 10))
-    s0, s1, s2 = _events(3)
-    t_pairs = t_ldir = t_grad = 0.0
-    nlaunch = 0
-    for _ in range(reps):
-        s0.record(stream)
-        lower_star_pairs(f_dev, out=g_dev)
-        s1.record(stream)
-        nlaunch += ascending_manifold_dims(g_dev, dims)
-        s2.record(stream)
-        torch.cuda.synchronize(dev)
-        t_pairs += s0.elapsed_time(s1)
-        t_ldir += s1.elapsed_time(s2)
-    t_pairs /= reps
-    t_ldir /= reps
-    for _ in range(reps):
-        s0.record(stream)
-        lower_star_grad(f_dev, out=g_dev)
-        s1.record(stream)
-        torch.cuda.synchronize(dev)
-        t_grad += s0.elapsed_time(s1)
-    t_grad /= reps
+    t_pairs, t_ldir, t_grad, nlaunch = grad_stage_times(f_dev, g_dev, dims, reps, stream, dev)
 
     line_extra = {}
     if not args.grad_only:
-        # the other mode once (the plain full integration beside a triaged step, or the
-        # triage beside the plain step) and the triage's label difference from the plain
-        def once(use_net):
+        # the other mode with the same warm-up and step count (the plain full
+        # integration beside a triaged step, or the triage beside the plain step) and the
+        # triage's label difference from the plain labels
+        def timed(use_net):
+            def one():
+                lower_star_grad(f_dev, out=g_dev)
+                return triage.triage_labels(f_dev, g_dev, use_net, **integ) if use_net is not None else \
+                    integrated_labels(f_dev, g_dev, **integ)
+            for _ in range(args.warmup):
+                one()
             torch.cuda.synchronize(dev)
             p0, p1 = _events(2)
             p0.record(stream)
-            lower_star_grad(f_dev, out=g_dev)
-            r = triage.triage_labels(f_dev, g_dev, use_net, **integ) if use_net is not None else \
-                integrated_labels(f_dev, g_dev, **integ)
+            for _ in range(args.steps):
+                r = one()
             p1.record(stream)
             torch.cuda.synchronize(dev)
-            return r, p0.elapsed_time(p1)
+            return r, p0.elapsed_time(p1) / args.steps
         if step_net is not None:
-            plain, ms_plain = once(None)
+            plain, ms_plain = timed(None)
             learned, ms_learned = res, ms
         else:
             plain, ms_plain = res, ms
-            learned, ms_learned = once(net) if net is not None else (None, None)
+            learned, ms_learned = timed(net) if net is not None else (None, None)
         line_extra["plain"] = {"value": V / (ms_plain * 1e-3) / 1e9, "unit": UNIT, "ms_per_step": ms_plain,
                                "redecided": plain["stats"]}
         line_extra["labels"] = {"mode": "learned triage" if step_net is not None else "plain full integration"}
@@ -381,7 +469,7 @@ def run_ours(args, ws, rank, local):
         fp32_peak = FP32_LANES_PER_SM * sms * 2 * SM_MAX_MHZ * 1e6 / 1e12
         achieved = it32 * FLOP_PER_ITERATION / (labels_ms * 1e-3) / 1e12
         line_extra["integration"] = {
-            "kernels": "integrate_level_kernel + fixup32_kernel (FP32), fixup_kernel (FP64 re-decisions)",
+            "kernels": "speculate_kernel + fixup_end32_kernel (FP32), fixup_end64_kernel (FP64 re-decisions)",
             "bound": "fp32 issue", "iterations_fp32": it32, "iterations_fp64": it64,
             "flop_per_iteration": FLOP_PER_ITERATION, "labels_ms": labels_ms,
             "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s", "frac": achieved / fp32_peak,
@@ -390,7 +478,7 @@ def run_ours(args, ws, rank, local):
                      "kernel included, so a lower bound for the integration kernels)"}
 
     # end to end through the C ABI host entry, pinned host buffers
-    e2e_reps = max(1, min(args.steps, 3))
+    e2e_reps = max(1, args.steps)
     if args.grad_only:
         g_host = torch.empty(C, dtype=torch.uint8).pin_memory()
         fn = lambda: _lib.check(lib.msc_steepest_lstar_host(ctypes.c_void_p(f_host.data_ptr()), _lib.dims_arg(dims),  # noqa: E731
@@ -449,33 +537,63 @@ def run_ours(args, ws, rank, local):
         del vols, outs, singles
 
     peak, peak_kind = load_peaks()
-    alg_pairs = 4 * V + C            # read f once, write every .grad byte once
-    alg_ldir = 2 * C                 # the ascending-manifold stage reads and writes the .grad
-    kernels = {
-        "lstar_kernel": {"launches_per_step": 1, "ms_per_launch": t_pairs,
-                         "algorithmic_bytes": alg_pairs, "gbs": alg_pairs / (t_pairs * 1e-3) / 1e9},
-        "ldir_stage": {"launches_per_step": nlaunch / reps, "ms_per_stage": t_ldir,
-                       "algorithmic_bytes": alg_ldir, "gbs": alg_ldir / (t_ldir * 1e-3) / 1e9,
-                       "kernels": "ldir_tile_kernel + ldir_check_kernel + ldir_walk_kernel"},
-    }
-    dom = "lstar_kernel" if t_pairs >= t_ldir else "ldir_stage"
-    kd = kernels[dom]
-    traffic = TRAFFIC_PER_LAUNCH.get((dom, n))
-    roofline = {"kernel": dom, "bound": "hbm", "achieved": kd["gbs"], "peak": peak, "unit": "GB/s",
-                "frac": kd["gbs"] / peak, "peak_kind": f"{peak_kind} hbm_gbs", "traffic": traffic,
-                "scope": "dominant kernel of the .grad; the label integration that dominates the full step is "
-                         "FP32/FP64 issue-bound, neither HBM nor tensor bound"}
+    kernels, roofline = grad_kernels(V, C, t_pairs, t_ldir, nlaunch, reps, n, peak, peak_kind)
+
+    # the 2D scale workload: the .grad of the 8192^2 k^-3 field
+    grad_2d = None
+    if not args.grad_only and not args.no_batch:
+        from msceer_gb300 import fields
+        f2 = torch.from_numpy(fields.power_law_field((8192, 8192), seed=rank)).to(dev)
+        g2 = torch.empty(num_cells((8192, 8192)), dtype=torch.uint8, device=dev)
+        for _ in range(args.warmup):
+            lower_star_grad(f2, out=g2)
+        p2, l2, t2, nl2 = grad_stage_times(f2, g2, (8192, 8192), reps, stream, dev)
+        V2, C2 = 8192 * 8192, num_cells((8192, 8192))
+        k2, r2 = grad_kernels(V2, C2, p2, l2, nl2, reps, 8192, peak, peak_kind)
+        grad_2d = {"workload": "8192^2 float32 k^-3 Gaussian random field, seed = rank", "vertices": V2, "cells": C2,
+                   "value": V2 / (t2 * 1e-3) / 1e9, "unit": UNIT, "ms_per_step": t2, "kernels": k2, "roofline": r2}
+        del f2, g2
+
+    # the labeling workload against the FP64 oracle: plain and learned labels
+    mismatch = None
+    if oracle_job is not None:
+        fl = torch.from_numpy(labels_field()).to(dev)
+        gl = lower_star_grad(fl)
+        gtl = 1e-6 * float(fl.abs().max())
+        integ_l = dict(INTEG, gradient_threshold=gtl)
+        plain_l = integrated_labels(fl, gl, **integ_l)
+        learned_l = triage.triage_labels(fl, gl, net, **integ_l) if net is not None else None
+        oproc, oq, opath = oracle_job
+        oproc.join()
+        t_oracle = oq.get() if oproc.exitcode == 0 else None
+        if oproc.exitcode == 0:
+            want = np.load(opath)
+            mismatch = {"workload": "256^3 float32, 64 Gaussians + U[-1e-3,1e-3] noise, seed 0; error 1e-4, gradient "
+                                    "threshold 1e-6 max|f|, 4000 iterations, 0.25 voxel",
+                        "plain": {k: float((plain_l[k].cpu().numpy() != want[k]).mean()) for k in ("asc", "dsc")},
+                        "oracle": "FP64 single-thread restatement, equal to the reference at one thread",
+                        "oracle_seconds": t_oracle}
+            if learned_l is not None:
+                mismatch["learned"] = {k: float((learned_l[k].cpu().numpy() != want[k]).mean()) for k in ("asc", "dsc")}
+            if NOISE_FILE.exists():
+                nz = json.loads(NOISE_FILE.read_text())
+                mismatch["reference_own_variation"] = {
+                    "what": f"the reference at {nz['threads']} threads vs one thread, largest of {nz['runs']} runs",
+                    **{k: nz["fields"]["gauss256_cfg2"][k] for k in ("asc", "dsc")}}
+            os.unlink(opath)
+        del fl, gl, plain_l, learned_l
 
     if rank == 0:
         mode = ".grad only" if args.grad_only else (
             ".grad + learned-triage labels" if step_net is not None else ".grad + plain integrated labels")
+        wl = f"{mode}, {wl_name}, seed = rank"
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
                 "vs_baseline": None, "dtype": "f32" if args.grad_only else "f32+f64", "data": "synthetic",
-                "config": {"workload": f"{mode}, {n}^3 float32 k^-3 Gaussian random field, seed = rank",
+                "config": {"workload": wl,
                            "vertices": V, "cells": C, "parallelism": f"replicas x{ws}",
                            "labels": "error 1e-4, gradient threshold 1e-6 max|f|, 4000 iterations, 0.25 voxel",
-                           "l2": "inputs larger than L2 (f 512 MiB, .grad 1 GiB at 512^3); no flush"},
+                           "l2": f"inputs larger than L2 (f {4 * V >> 20} MiB, .grad {C >> 20} MiB); no flush"},
                 "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                         "ms_per_step": t_e2e * 1e3, "api": api},
                 "grad": {"value": V / (t_grad * 1e-3) / 1e9, "unit": UNIT, "ms_per_step": t_grad},
@@ -484,6 +602,10 @@ def run_ours(args, ws, rank, local):
                 "gpu_launches": launches,
                 "clocks": clocks}
         line.update(line_extra)
+        if grad_2d is not None:
+            line["grad_2d"] = grad_2d
+        if mismatch is not None:
+            line["mismatch_vs_fp64_oracle"] = mismatch
         if batch is not None:
             line["batch"] = batch
         if ws == 1 and not args.no_cpu_baseline:
