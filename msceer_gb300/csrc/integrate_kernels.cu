@@ -256,8 +256,9 @@ __device__ __forceinline__ void split_index(const VolDims& V, int64_t v, int& x,
 constexpr int kPathCap = 48;
 constexpr unsigned kFullMask = 0xffffffffu;
 
-// resident CTAs of 128 threads per SM for the lane-refilling kernels
-constexpr int kLaneCtasPerSm = 16;
+// CTAs of 128 threads per SM launched for the lane-refilling FP32 kernels (their
+// registers allow 7 resident per SM); MSC_LANE_CTAS_PER_SM overrides it for tuning.
+int lane_ctas_per_sm();
 
 // Claims a work item for every lane of the warp that asks for one (`want`); returns
 // the item of the calling lane (meaningless where it did not ask).
@@ -1436,6 +1437,14 @@ static int trips_env(const char* name, int dflt) {
   const int v = e ? std::atoi(e) : dflt;
   return (v == 2 || v == 4 || v == 8 || v == 16) ? v : dflt;
 }
+int lane_ctas_per_sm() {
+  static const int k = [] {
+    const char* e = std::getenv("MSC_LANE_CTAS_PER_SM");
+    const int v = e ? std::atoi(e) : 0;
+    return v >= 1 && v <= 32 ? v : 16;
+  }();
+  return k;
+}
 int trips_per_turn() {
   static const int k = trips_env("MSC_TRIPS_PER_TURN", 16);
   return k;
@@ -1477,7 +1486,8 @@ cudaError_t launch_speculate(const float4* G, const VolDims& V, const IntegParam
   if (k1 <= k0) return cudaSuccess;
   const Adv32 A = Adv32::make(G, V, P, lvl, stamp, nullptr);
   const int64_t blocks = (k1 - k0 + 127) / 128;
-  const int grid = (int)(blocks < num_sms * kLaneCtasPerSm ? blocks : num_sms * kLaneCtasPerSm);
+  const int cap = num_sms * lane_ctas_per_sm();
+  const int grid = (int)(blocks < cap ? blocks : cap);
   ::msc::count_launch();
   switch (trips_per_turn_pass1()) {
     case 2:
@@ -1593,7 +1603,8 @@ cudaError_t launch_fixup_end32(const float4* G, const VolDims& V, const IntegPar
   const int blocks = (n + 127) / 128;
   if (cudaError_t e = cudaMemsetAsync(work, 0, sizeof(unsigned long long), stream)) return e;
   ::msc::count_launch();
-  const int grid = blocks < num_sms * kLaneCtasPerSm ? blocks : num_sms * kLaneCtasPerSm;
+  const int cap = num_sms * lane_ctas_per_sm();
+  const int grid = blocks < cap ? blocks : cap;
   switch (trips_per_turn()) {
     case 16:
       fixup_end32_kernel<16><<<grid, 128, 0, stream>>>(A, lab, state, list, n, endv, amb, n_amb, amb_mode, work, trips);
