@@ -635,7 +635,7 @@ __global__ void __launch_bounds__(BS) ldir_tile_kernel(const LdirBatch B, uint8_
     }
     __syncthreads();
 
-    // write back the interior, a row per warp instruction, and save the whole box
+    // write back the interior, a row per warp instruction
     constexpr int NI = TX * TY * (ND == 3 ? TZ : 1);
     for (int k = tid; k < NI; k += BS) {
       const int ix = k % TX, r = k / TX;
