@@ -534,7 +534,29 @@ def run_ours(args, ws, rank, local):
         batch = {"workload": "64 k^-3 volumes, edges log-uniform in [32, 256], seeds 0..63, .grad",
                  "vertices": nvb, "batched": {"value": nvb / (tb * 1e-3) / 1e9, "unit": UNIT, "ms": tb},
                  "looped": {"value": nvb / (tl * 1e-3) / 1e9, "unit": UNIT, "ms": tl}, "bit_identical": same}
-        del vols, outs, singles
+        # the labels of the same volumes: several volumes at a time on their own streams
+        # against one call after another, and the whole .grad + labels step of the batch
+        from msceer_gb300 import integrated_labels_batch
+        lab_kw = dict(INTEG)
+        integrated_labels_batch(vols, outs, threads=8, **lab_kw)
+        torch.cuda.synchronize(dev)
+        t0 = time.perf_counter()
+        lab_b = integrated_labels_batch(vols, outs, threads=8, **lab_kw)
+        torch.cuda.synchronize(dev)
+        tlb = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        lab_l = [integrated_labels(v, o, **lab_kw) for v, o in zip(vols, outs)]
+        torch.cuda.synchronize(dev)
+        tll = time.perf_counter() - t0
+        same_l = all(torch.equal(a[k], b[k]) for a, b in zip(lab_b, lab_l) for k in ("asc", "dsc"))
+        batch["labels"] = {"how": "8 volumes at a time on their own CUDA streams and host threads vs one call "
+                                  "after another (each call synchronises only its own stream)",
+                           "batched": {"value": nvb / tlb / 1e9, "unit": UNIT, "ms": tlb * 1e3},
+                           "looped": {"value": nvb / tll / 1e9, "unit": UNIT, "ms": tll * 1e3},
+                           "bit_identical": same_l,
+                           "step": {"what": ".grad batched + labels batched", "value": nvb / (tb * 1e-3 + tlb) / 1e9,
+                                    "unit": UNIT}}
+        del vols, outs, singles, lab_b, lab_l
 
     peak, peak_kind = load_peaks()
     kernels, roofline = grad_kernels(V, C, t_pairs, t_ldir, nlaunch, reps, n, peak, peak_kind)
