@@ -230,7 +230,8 @@ def cpu_baseline(f: np.ndarray, grad_only: bool = False):
     t_grad = time.perf_counter() - t0
     g_grad = slab.size / t_grad / 1e9
     out = {"unit": UNIT, "cores": nthreads, "kind": "port", "grad_gvps": g_grad}
-    desc = (f".grad of a z-slab {slab.shape[2]}x{slab.shape[1]}x{slab.shape[0]} ({slab.size} vertices) with "
+    shape = "x".join(str(e) for e in slab.shape[::-1])
+    desc = (f".grad of a {'z-slab' if slab.ndim == 3 else 'y-band'} {shape} ({slab.size} vertices) with "
             f"{nthreads} OpenMP threads: {t_grad:.2f} s")
     if grad_only:
         out["value"] = g_grad
@@ -481,9 +482,10 @@ def run_ours(args, ws, rank, local):
     e2e_reps = max(1, args.steps)
     if args.grad_only:
         g_host = torch.empty(C, dtype=torch.uint8).pin_memory()
-        fn = lambda: _lib.check(lib.msc_steepest_lstar_host(ctypes.c_void_p(f_host.data_ptr()), _lib.dims_arg(dims),  # noqa: E731
-                                                            ctypes.c_void_p(g_host.data_ptr())), "msc_steepest_lstar_host")
-        h2d, d2h, api = 4 * V, C, "msc_steepest_lstar_host"
+        api = "msc_steepest_lstar_host" if len(dims) == 3 else "msc_lower_star_grad_2d_host"
+        fn = lambda: _lib.check(getattr(lib, api)(ctypes.c_void_p(f_host.data_ptr()), _lib.dims_arg(dims),  # noqa: E731
+                                                  ctypes.c_void_p(g_host.data_ptr())), api)
+        h2d, d2h = 4 * V, C
     else:
         a_host = torch.empty(V, dtype=torch.int32).pin_memory()
         d_host = torch.empty(V, dtype=torch.int32).pin_memory()

@@ -41,12 +41,6 @@ struct LdirTile {
   static constexpr int NW = (NL + 31) / 32;
   // dynamic shared memory of the pass kernel: queue (u16) | bytes | visited bits | changed bits
   static constexpr size_t smem_bytes() { return (size_t)NL * 2 + ((NL + 3) / 4) * 4 + (size_t)NW * 8; }
-  // of the tile kernel: queue (u16; NL items at most plus one pending claim per thread,
-  // QX >= the block size) | bytes | value-2 marks | visited bits
-  static constexpr int QX = 1024;
-  static constexpr size_t tile_smem_bytes() {
-    return (size_t)(NL + QX) * 2 + ((NL + 3) / 4) * 8 + (size_t)NW * 4;
-  }
 };
 
 // local index -> local coords
@@ -55,43 +49,6 @@ __device__ __forceinline__ void lcoords(int i, int& lx, int& ly, int& lz) {
   lx = i % T::LX;
   ly = (i / T::LX) % T::LY;
   lz = i / (T::LX * T::LY);
-}
-
-// k-th halo cell of the box -> box index (z slabs, then y rows, then x columns)
-template <class T, int ND>
-__device__ __forceinline__ int halo_cell(int h) {
-  constexpr int H = T::H, LX = T::LX, LY = T::LY, LZ = T::LZ;
-  int lz = 0;
-  if (ND == 3) {
-    constexpr int SLAB = 2 * H * LX * LY;  // z < H and z >= LZ - H
-    if (h < SLAB) {
-      const int s = h / (LX * LY), r = h % (LX * LY);
-      lz = s < H ? s : LZ - 2 * H + s;
-      return r + LX * LY * lz;
-    }
-    h -= SLAB;
-  }
-  constexpr int P = 2 * H * LX + 2 * H * (LY - 2 * H);  // halo cells of one inner plane
-  lz = (ND == 3 ? H : 0) + h / P;
-  int r = h % P;
-  int lx, ly;
-  if (r < 2 * H * LX) {
-    const int s = r / LX;
-    ly = s < H ? s : LY - 2 * H + s;
-    lx = r % LX;
-  } else {
-    r -= 2 * H * LX;
-    const int s = r / (LY - 2 * H);
-    lx = s < H ? s : LX - 2 * H + s;
-    ly = H + r % (LY - 2 * H);
-  }
-  return lx + LX * (ly + LY * lz);
-}
-
-template <class T, int ND>
-__host__ __device__ constexpr int halo_count() {
-  return (ND == 3 ? 2 * T::H * T::LX * T::LY : 0) +
-         (ND == 3 ? (T::LZ - 2 * T::H) : 1) * (2 * T::H * T::LX + 2 * T::H * (T::LY - 2 * T::H));
 }
 
 // Queue append for the lanes of a warp that are converged here: one shared-memory
@@ -108,24 +65,6 @@ __device__ __forceinline__ void warp_push(uint16_t* sq, int* qtail, int cap, int
   if (want) {
     const int slot = base + __popc(m & ((1u << lane) - 1u));
     if (slot < cap) sq[slot] = (uint16_t)item; else atomicOr(err, kErrLocalQueue);
-  }
-}
-
-// warp_push for a queue that other threads read while it grows (the tile kernel's
-// barrier-free walk): the item is stored through a volatile pointer.
-__device__ __forceinline__ void warp_push_live(uint16_t* sq, int* qtail, int cap, int* err, bool want, int item) {
-  const unsigned act = __activemask();
-  const unsigned m = __ballot_sync(act, want);
-  if (!m) return;
-  const int lane = threadIdx.x & 31;
-  const int leader = __ffs(m) - 1;
-  int base = 0;
-  if (lane == leader) base = atomicAdd(qtail, __popc(m));
-  base = __shfl_sync(act, base, leader);
-  if (want) {
-    const int slot = base + __popc(m & ((1u << lane) - 1u));
-    if (slot < cap) reinterpret_cast<volatile uint16_t*>(sq)[slot] = (uint16_t)item;
-    else atomicOr(err, kErrLocalQueue);
   }
 }
 
@@ -369,18 +308,18 @@ __global__ void __launch_bounds__(BS) ldir_pass_kernel(uint8_t* __restrict__ g, 
   }
 }
 
-// ---- single-pass form: one tile pass, a halo check, a global frontier walk -------------------
+// ---- single-pass form: one bit-row tile pass, a halo check, a global frontier walk -----------
 //
 // A tile's walk is complete for every item of its interior (all of an item's rule
 // reaches lies within 2 cells), so after one pass over all tiles the only missing
 // marks are those a tile made in its halo that the halo's owner did not make itself.
-// The pass therefore saves each tile's final box; the check kernel lowers every
-// global cell that some tile's saved halo holds lower, and queues the lowered items,
-// whose walk may need to continue beyond that tile's box; the walk kernel finishes
-// those walks in global memory.  Concurrent lowering of a byte uses a compare-and-swap
-// on its aligned 32-bit word (the low five bits never change, so the ldir field only
-// ever decreases); bytes whose word is not wholly inside the .grad array go through a
-// bounded spin lock instead.
+// The pass records, per tile, the halo cells its closure holds lower than the .grad
+// held them; the check kernel lowers every such cell that its owner still holds
+// higher and queues the lowered items, whose walks may continue beyond that tile's
+// box; the walk kernel finishes those walks in global memory.  Concurrent lowering of
+// a byte uses a compare-and-swap on its aligned 32-bit word (the low five bits never
+// change, so the ldir field only ever decreases); bytes whose word is not wholly
+// inside the .grad array go through a bounded spin lock instead.
 
 struct GradView {
   uint8_t* g;
@@ -426,77 +365,6 @@ __device__ __forceinline__ bool lower_ldir(const GradView& G, int64_t c, unsigne
   return lowered;
 }
 
-// Both closures in the same walk.  The value-2 closure (items: edges) keeps its marks
-// in a byte plane of its own, m2, and the value-1 closure (items: quads) in the .grad
-// bytes, so the two never race on a byte and run in the same BFS levels; an item's
-// dimension says which closure it walks.  The final byte is the .grad byte with ldir
-// lowered to 2 where m2 is set.
-template <class T, int ND>
-struct LdirWalk2 {
-  uint8_t* sg;
-  uint8_t* m2;
-  uint16_t* sq;
-  uint32_t* vis;
-  int* qtail;
-  int* err;
-  int lmin[3], lmax[3];
-  uint32_t dec_map;
-
-  __device__ __forceinline__ int visit(int i, int l[3], int a, int sgn, bool r2) {
-    constexpr int LE[3] = {T::LX, T::LY, T::LZ};
-    const int la = l[a] + sgn;
-    if (la < lmin[a] || la >= lmax[a]) return -1;
-    const int t = i + sgn * T::ls(a);
-    const uint8_t bt = sg[t];
-    const unsigned code = (bt >> 2) & 7u;
-    if (!(bt & 1u) || code == 7u) return -1;  // unassigned or critical
-    if (r2) m2[t] |= 1u;
-    else if ((bt >> 5) != 1u) sg[t] = (uint8_t)((bt & 0x1Fu) | (1u << 5));
-    const int pc = map3(dec_map, (int)code);
-    const int pa = pc >> 1, psg = (pc & 1) ? -1 : 1;
-    int lp[3] = {l[0], l[1], l[2]};
-    lp[a] += sgn;
-    lp[pa] += psg;
-    if (lp[pa] < 0 || lp[pa] >= LE[pa]) return -1;  // partner outside the box
-    const int tp = t + psg * T::ls(pa);
-    if (tp == i) return -1;
-    const uint8_t bp = sg[tp];
-    if (r2) {
-      const int pdim = (lp[0] & 1) + (lp[1] & 1) + (ND == 3 ? (lp[2] & 1) : 0);
-      if (pdim != 1) {  // a hex: the value-2 path ends here
-        m2[tp] |= 1u;
-        return -1;
-      }
-      if ((bp >> 5) == 2u || (m2[tp] & 1u)) return -1;  // a root, or marked already
-    } else {
-      if ((bp >> 5) == 1u) return -1;
-    }
-    const uint32_t bit = 1u << (tp & 31);
-    if (atomicOr(&vis[tp >> 5], bit) & bit) return -1;
-    if (r2) m2[tp] |= 1u;
-    else sg[tp] = (uint8_t)((bp & 0x1Fu) | (1u << 5));
-    return tp;
-  }
-
-  __device__ __forceinline__ void step(int i) {
-    int l[3];
-    lcoords<T>(i, l[0], l[1], l[2]);
-    const bool r2 = ((l[0] & 1) + (l[1] & 1) + (ND == 3 ? (l[2] & 1) : 0)) == 1;
-#pragma unroll
-    for (int a = 0; a < ND; a++) {
-#pragma unroll
-      for (int s = 0; s < 2; s++) {
-        // cofacets only along even axes, +axis first
-        const int nx = (l[a] & 1) ? -1 : visit(i, l, a, s == 0 ? 1 : -1, r2);
-        warp_push_live(sq, qtail, T::NL, err, nx >= 0, nx);
-      }
-    }
-  }
-};
-
-constexpr uint16_t kTileQueueEmpty = 0xFFFF;        // an unfilled slot (NL < 65535)
-constexpr uint32_t kTileQueueSpinLimit = 1u << 24;  // bound of a wait for a slot (~0.5 s)
-
 __device__ __forceinline__ int batch_volume(const LdirBatch& B, int64_t flat_tile) {
   int lo = 0, hi = B.n - 1;
   while (lo < hi) {
@@ -506,151 +374,229 @@ __device__ __forceinline__ int batch_volume(const LdirBatch& B, int64_t flat_til
   return lo;
 }
 
-template <int ND, int TX, int TY, int TZ, int BS>
-__global__ void __launch_bounds__(BS) ldir_tile_kernel(const LdirBatch B, uint8_t* __restrict__ saved,
+// The tile pass works on bit rows.  A box is 32 cells along x (28 owned plus the
+// 2-cell halo on each side) by LY x LZ rows, and every per-cell property the walks
+// need is one 32-bit word per row (bit = x offset in the box).  Both closures advance
+// one BFS level at a time over every row at once:
+//   T = NC & cof(F)     cofacets of the frontier along its even axes: bit shifts within
+//                       a row for x, the neighbour rows for y and z
+//   P = partner(T)      for each pair direction, T & PC[direction] moved one cell
+//   value 2 marks the quads of T, the hexes of P and the new edges of P
+//   value 1 marks the hexes of T and the new quads of P
+// The frontier F is the new edges (value-2 items) and quads (value-1 items): the two
+// walks' items, cofacets and partners never share a dimension, so one frontier and
+// one partner step serve both.  Visiting order does not change a monotone closure, so
+// the marks equal those of the item-by-item walk.  The closures of rough fields are
+// shallow (14 levels for value 2, 12 for value 1 over a whole 128^3 k^-3 volume), so
+// a tile costs a few dozen passes over its rows.
+constexpr int kBitLX = 32;
+template <int ND, int LY, int LZ>
+struct BitTile {
+  static constexpr int TX = kBitLX - 4, TY = LY - 4, TZ = ND == 3 ? LZ - 4 : 1;
+  static constexpr int R = LY * LZ;  // rows of the box
+  // halo rows (every cell in the halo) and inner rows (halo cells at x = 0, 1, 30, 31)
+  static constexpr int NHR = ND == 3 ? 4 * LY + 4 * (LZ - 4) : 4;
+  static constexpr int NIR = ND == 3 ? (LY - 4) * (LZ - 4) : LY - 4;
+  // a tile's record: the {value 2, value 1} masks of each halo row's lowered cells,
+  // then one byte per inner row (bits 0-3: value 2 at x = 0, 1, 30, 31; 4-7: value 1)
+  static constexpr int64_t REC = ((int64_t)NHR * 8 + NIR + 15) / 16 * 16;
+  // shared memory word planes: NC, PC[6] (partner at +x, -x, +y, -y, +z, -z), F, T, M2, M1
+  static constexpr size_t smem_bytes() { return (size_t)11 * R * 4; }
+  static_assert(ND == 3 || LZ == 1, "2D boxes have one z row");
+  static_assert(LY % 2 == 0 && LZ % 2 == (ND == 3 ? 0 : 1), "tile origins must be even");
+};
+
+// record slot of halo row (ly, lz); -1 for an inner row
+template <int ND, int LY, int LZ>
+__device__ __forceinline__ int halo_row_slot(int ly, int lz) {
+  if (ND == 3) {
+    if (lz < 2) return lz * LY + ly;
+    if (lz >= LZ - 2) return (lz - (LZ - 4)) * LY + ly;
+  }
+  const int base = ND == 3 ? 4 * LY + (lz - 2) * 4 : 0;
+  if (ly < 2) return base + ly;
+  if (ly >= LY - 2) return base + ly - (LY - 4);
+  return -1;
+}
+
+template <int ND, int LY, int LZ>
+__device__ __forceinline__ void halo_row_of(int h, int& ly, int& lz) {
+  if (ND == 3 && h < 4 * LY) {
+    const int s = h / LY;
+    lz = s < 2 ? s : LZ - 4 + s;
+    ly = h % LY;
+    return;
+  }
+  const int k = ND == 3 ? h - 4 * LY : h;
+  const int q = k & 3;
+  lz = ND == 3 ? 2 + (k >> 2) : 0;
+  ly = q < 2 ? q : LY - 4 + q;
+}
+
+template <int ND, int LY, int LZ, int BS, int MINB>
+__global__ void __launch_bounds__(BS, MINB) ldir_tile_kernel(const LdirBatch B, uint8_t* __restrict__ rec,
                                                        int* __restrict__ err) {
-  using T = LdirTile<ND, TX, TY, TZ>;
-  constexpr int NL = T::NL;
-  static_assert(NL < 65536, "local ids are 16-bit");
-  extern __shared__ __align__(16) unsigned char s_dyn[];
-  // queue (u16) | .grad bytes | value-2 marks | visited bits
-  constexpr int QCAP = NL + T::QX;
-  static_assert(BS <= T::QX, "one pending queue claim per thread");
-  uint16_t* sq = reinterpret_cast<uint16_t*>(s_dyn);
-  uint8_t* sg = s_dyn + (size_t)QCAP * 2;
-  uint8_t* m2 = sg + ((NL + 3) / 4) * 4;
-  uint32_t* s_vis = reinterpret_cast<uint32_t*>(m2 + ((NL + 3) / 4) * 4);
-  __shared__ int s_qtail, s_head, s_done;
-
-  const int tid = threadIdx.x;
-
-  LdirWalk2<T, ND> W;
-  W.sg = sg;
-  W.m2 = m2;
-  W.sq = sq;
-  W.vis = s_vis;
-  W.qtail = &s_qtail;
-  W.err = err;
+  using T = BitTile<ND, LY, LZ>;
+  constexpr int R = T::R;
+  constexpr int NWARP = BS / 32;
+  constexpr int RPT = (R + BS - 1) / BS;  // rows per thread in a level
+  constexpr int KR = 4;                   // rows per warp with loads in flight
+  constexpr uint32_t EVENX = 0x55555555u, ODDX = 0xAAAAAAAAu;
+  extern __shared__ __align__(16) uint32_t s_plane[];
+  uint32_t* sNC = s_plane;
+  uint32_t* sPC = s_plane + R;
+  uint32_t* sF = s_plane + 7 * R;
+  uint32_t* sT = s_plane + 8 * R;
+  uint32_t* sM2 = s_plane + 9 * R;
+  uint32_t* sM1 = s_plane + 10 * R;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
 
   for (int64_t flat = blockIdx.x; flat < B.total_tiles; flat += gridDim.x) {
     const LdirVol& vol = B.v[batch_volume(B, flat)];
     uint8_t* __restrict__ g = vol.g;
     const GradDims& D = vol.D;
-    W.dec_map = D.dec_map;
     const int64_t dX = D.d[0], dY = D.d[1], dZ = D.d[2];
-    const int64_t ntx = (dX + TX - 1) / TX, nty = (dY + TY - 1) / TY;
+    const int64_t ntx = (dX + T::TX - 1) / T::TX, nty = (dY + T::TY - 1) / T::TY;
     const int64_t tile = flat - vol.tile0;
-    const int64_t tx = tile % ntx, ty = (tile / ntx) % nty, tz = (ND == 3) ? tile / (ntx * nty) : 0;
-    const int64_t o[3] = {tx * TX - T::H, ty * TY - T::H, (ND == 3) ? tz * TZ - T::H : 0};
-    const int64_t dd[3] = {dX, dY, dZ};
-    constexpr int LE[3] = {T::LX, T::LY, T::LZ};
+    const int64_t tx = tile % ntx, ty = (tile / ntx) % nty, tz = ND == 3 ? tile / (ntx * nty) : 0;
+    const int64_t o1 = ty * T::TY - 2, o2 = ND == 3 ? tz * T::TZ - 2 : 0;
+    const int64_t gx = tx * T::TX - 2 + lane;
+    const bool xin = gx >= 0 && gx < dX;
+
+    // stage: a warp per row, a lane per cell; each property becomes a bit row.  Cells
+    // outside the complex read as 0 (unassigned).  Marked items seed the frontier.  A
+    // warp keeps KR rows' loads in flight before it folds them.
+    for (int r0 = warp; r0 < R; r0 += NWARP * KR) {
+      uint8_t bk[KR];
 #pragma unroll
-    for (int a = 0; a < 3; a++) {
-      W.lmin[a] = (int)(o[a] < 0 ? -o[a] : 0);
-      const int64_t hi = dd[a] - o[a];
-      W.lmax[a] = (int)(hi < LE[a] ? hi : LE[a]);
+      for (int k = 0; k < KR; k++) {
+        const int r = r0 + k * NWARP;
+        const int ly = r % LY, lz = r / LY;
+        const int64_t gy = o1 + ly, gz = o2 + lz;
+        bk[k] = 0;
+        if (r < R && xin && gy >= 0 && gy < dY && gz >= 0 && gz < dZ) bk[k] = g[gx + gy * D.cs[1] + gz * D.cs[2]];
+      }
+#pragma unroll
+      for (int k = 0; k < KR; k++) {
+        const int r = r0 + k * NWARP;
+        if (r >= R) break;
+        const int ly = r % LY, lz = r / LY;
+        const uint8_t b = bk[k];
+        const unsigned code = (b >> 2) & 7u, ld = b >> 5;
+        const bool asg = b & 1u;
+        const bool nc = asg && code != 7u;
+        const int pc = nc ? map3(D.dec_map, (int)code) : 7;
+        const int dim = (lane & 1) + (ly & 1) + (lz & 1);
+        const uint32_t mnc = __ballot_sync(~0u, nc);
+        const uint32_t m2 = __ballot_sync(~0u, asg && dim == 1 && ld == 2u);
+        const uint32_t m1 = __ballot_sync(~0u, asg && dim == 2 && ld == 1u);
+        uint32_t pcm[6];
+#pragma unroll
+        for (int c = 0; c < 6; c++) pcm[c] = __ballot_sync(~0u, pc == c);
+        if (lane == 0) {
+          sNC[r] = mnc;
+#pragma unroll
+          for (int c = 0; c < 6; c++) sPC[c * R + r] = pcm[c];
+          sF[r] = m2 | m1;
+          sM2[r] = m2;
+          sM1[r] = m1;
+        }
+      }
     }
-    if (tid == 0) {
-      s_qtail = 0;
-      s_head = 0;
-      s_done = 0;
-    }
-    for (int w = tid; w < T::NW; w += BS) s_vis[w] = 0;
-    for (int k = tid; k < QCAP; k += BS) sq[k] = kTileQueueEmpty;
     __syncthreads();
 
-    // stage the box (cells outside the complex read as 0 = unassigned), many loads in
-    // flight per thread, and queue every marked item -- the roots -- as a seed
-    constexpr int PER = (NL + BS - 1) / BS;
-    constexpr int U = 8;
+    // BFS levels until no row gains an item; every level adds an item, so the bound
+    // is never reached by a valid gradient
+    for (int level = 0;; level++) {
 #pragma unroll 1
-    for (int j0 = 0; j0 < PER; j0 += U) {
-      uint8_t v[U];
+      for (int k = 0; k < RPT; k++) {
+        const int r = tid + k * BS;
+        if (r < R) {
+          const int ly = r % LY, lz = r / LY;
+          const uint32_t f = sF[r] & EVENX;
+          uint32_t c = (f << 1) | (f >> 1);
+          if (ly & 1) c |= sF[r - 1] | (ly + 1 < LY ? sF[r + 1] : 0u);
+          if (ND == 3 && (lz & 1)) c |= sF[r - LY] | (lz + 1 < LZ ? sF[r + LY] : 0u);
+          sT[r] = c & sNC[r];
+        }
+      }
+      __syncthreads();
+      int grew = 0;
+#pragma unroll 1
+      for (int k = 0; k < RPT; k++) {
+        const int r = tid + k * BS;
+        if (r < R) {
+          const int ly = r % LY, lz = r / LY;
+          const uint32_t t = sT[r];
+          uint32_t p = ((t & sPC[r]) << 1) | ((t & sPC[R + r]) >> 1);
+          if (ly > 0) p |= sT[r - 1] & sPC[2 * R + r - 1];
+          if (ly + 1 < LY) p |= sT[r + 1] & sPC[3 * R + r + 1];
+          if (ND == 3) {
+            if (lz > 0) p |= sT[r - LY] & sPC[4 * R + r - LY];
+            if (lz + 1 < LZ) p |= sT[r + LY] & sPC[5 * R + r + LY];
+          }
+          const int odd = (ly & 1) + (lz & 1);
+          const uint32_t edges = odd == 0 ? ODDX : (odd == 1 ? EVENX : 0u);
+          const uint32_t quads = odd == 0 ? 0u : (odd == 1 ? ODDX : EVENX);
+          const uint32_t hexes = odd == 2 ? ODDX : 0u;
+          const uint32_t m2 = sM2[r], m1 = sM1[r];
+          const uint32_t e2 = p & edges & ~m2, e1 = p & quads & ~m1;
+          sM2[r] = m2 | (t & quads) | (p & hexes) | e2;
+          sM1[r] = m1 | (t & hexes) | e1;
+          sF[r] = e2 | e1;
+          grew |= (e2 | e1) != 0u;
+        }
+      }
+      if (!__syncthreads_or(grew)) break;
+      if (level > 64 * R) {
+        if (tid == 0) atomicOr(err, kErrPassLimit);
+        break;
+      }
+    }
+
+    // write back the owned cells this tile lowered and record the halo cells it holds
+    // lower than the .grad does (their owners may hold them lower by now: the check
+    // compares again)
+    uint8_t* trec = rec + flat * T::REC;
+    for (int r0 = warp; r0 < R; r0 += NWARP * KR) {
+      uint8_t bk[KR];
+      bool m2k[KR], m1k[KR];
 #pragma unroll
-      for (int u = 0; u < U; u++) {
-        const int k = (j0 + u) * BS + tid;
-        v[u] = 0;
-        if (j0 + u < PER && k < NL) {
-          const int lx = k % T::LX, row = k / T::LX;
-          const int ly = row % T::LY, lz = row / T::LY;
-          if (lx >= W.lmin[0] && lx < W.lmax[0] && ly >= W.lmin[1] && ly < W.lmax[1] && lz >= W.lmin[2] &&
-              lz < W.lmax[2])
-            v[u] = g[(o[0] + lx) + (o[1] + ly) * D.cs[1] + (o[2] + lz) * D.cs[2]];
-        }
+      for (int k = 0; k < KR; k++) {
+        const int r = r0 + k * NWARP;
+        const int ly = r % LY, lz = r / LY;
+        const int64_t gy = o1 + ly, gz = o2 + lz;
+        m2k[k] = r < R && ((sM2[r] >> lane) & 1u);
+        m1k[k] = r < R && ((sM1[r] >> lane) & 1u);
+        bk[k] = 0;
+        if ((m2k[k] || m1k[k]) && xin && gy >= 0 && gy < dY && gz >= 0 && gz < dZ)
+          bk[k] = g[gx + gy * D.cs[1] + gz * D.cs[2]];
       }
 #pragma unroll
-      for (int u = 0; u < U; u++) {
-        const int k = (j0 + u) * BS + tid;
-        const bool valid = j0 + u < PER && k < NL;
-        int dim = 0;
-        if (valid) {
-          sg[k] = v[u];
-          m2[k] = (uint8_t)(v[u] & 0xE0u);  // staged ldir above the value-2 mark bit
-          const int lx = k % T::LX, row = k / T::LX;
-          const int ly = row % T::LY, lz = row / T::LY;
-          dim = (lx & 1) + (ly & 1) + (ND == 3 ? (lz & 1) : 0);
+      for (int k = 0; k < KR; k++) {
+        const int r = r0 + k * NWARP;
+        if (r >= R) break;
+        const int ly = r % LY, lz = r / LY;
+        const int64_t gy = o1 + ly, gz = o2 + lz;
+        const uint8_t b = bk[k];  // 0 (unassigned) outside the complex
+        const bool low2 = m2k[k] && (b & 1u) && (b >> 5) > 2u;
+        const bool low1 = m1k[k] && (b & 1u) && (b >> 5) > 1u;
+        const int slot = halo_row_slot<ND, LY, LZ>(ly, lz);
+        if (slot >= 0) {
+          const uint32_t w2 = __ballot_sync(~0u, low2), w1 = __ballot_sync(~0u, low1);
+          if (lane < 2) reinterpret_cast<uint32_t*>(trec)[2 * slot + lane] = lane == 0 ? w2 : w1;
+        } else {
+          const bool own = lane >= 2 && lane < kBitLX - 2;
+          if (own && (low2 || low1))
+            g[gx + gy * D.cs[1] + gz * D.cs[2]] = (uint8_t)((b & 0x1Fu) | ((low1 ? 1u : 2u) << 5));
+          const uint32_t w2 = __ballot_sync(~0u, low2 && !own), w1 = __ballot_sync(~0u, low1 && !own);
+          if (lane == 0) {
+            const int i = ND == 3 ? (lz - 2) * (LY - 4) + (ly - 2) : ly - 2;
+            const uint32_t q2 = (w2 & 3u) | ((w2 >> 28) & 0xCu), q1 = (w1 & 3u) | ((w1 >> 28) & 0xCu);
+            trec[T::NHR * 8 + i] = (uint8_t)(q2 | (q1 << 4));
+          }
         }
-        const unsigned ld = v[u] >> 5;
-        const bool seed = valid && (v[u] & 1u) && ((dim == 1 && ld == 2u) || (dim == 2 && ld == 1u));
-        warp_push(sq, &s_qtail, NL, err, seed, k);
       }
-    }
-    __syncthreads();
-
-    // both closures; the fixpoint does not depend on the order, so rather than BFS
-    // levels separated by barriers every thread takes the next queue slot as soon as
-    // its item is walked.  A slot below s_qtail is filled by its producer; a thread
-    // whose slot is beyond every reserved one stops once every reserved item is done
-    // (an item counts as done only after its pushes were reserved).
-    {
-      int h = atomicAdd(&s_head, 1);
-      volatile uint16_t* vq = sq;
-      volatile int* vdone = &s_done;
-      volatile int* vtail = &s_qtail;
-      for (uint32_t spin = 0;; spin++) {
-        const uint16_t it = h < QCAP ? (uint16_t)vq[h] : (uint16_t)kTileQueueEmpty;
-        if (it != kTileQueueEmpty) {
-          W.step(it);
-          __threadfence_block();
-          atomicAdd(&s_done, 1);
-          h = atomicAdd(&s_head, 1);
-          spin = 0;
-          continue;
-        }
-        const int d = *vdone;
-        const int t = *vtail;
-        if (d == t && h >= t) break;
-        if (spin > kTileQueueSpinLimit) {  // cannot happen by construction: report, stop
-          atomicOr(err, kErrPassLimit);
-          break;
-        }
-        __nanosleep(32);
-      }
-    }
-
-    // fold the value-2 marks into the bytes
-    for (int k = tid; k < NL; k += BS) {
-      const uint8_t b = sg[k];
-      if ((m2[k] & 1u) && (b >> 5) == 3u) sg[k] = (uint8_t)((b & 0x1Fu) | (2u << 5));
-    }
-    __syncthreads();
-
-    // write back the interior, a row per warp instruction
-    constexpr int NI = TX * TY * (ND == 3 ? TZ : 1);
-    for (int k = tid; k < NI; k += BS) {
-      const int ix = k % TX, r = k / TX;
-      const int iy = r % TY, iz = r / TY;
-      const int64_t gx = o[0] + T::H + ix, gy = o[1] + T::H + iy, gz = o[2] + (ND == 3 ? T::H : 0) + iz;
-      if (gx < dX && gy < dY && gz < dZ)
-        g[gx + gy * D.cs[1] + gz * D.cs[2]] = sg[(ix + T::H) + T::LX * ((iy + T::H) + T::LY * (iz + (ND == 3 ? T::H : 0)))];
-    }
-    // save the halo cells this tile lowered (0 for the rest), in halo order
-    constexpr int NH = halo_count<T, ND>();
-    uint8_t* sv = saved + flat * (int64_t)NH;
-    for (int h = tid; h < NH; h += BS) {
-      const int k = halo_cell<T, ND>(h);
-      const uint8_t b = sg[k];
-      sv[h] = ((unsigned)(b >> 5) < (unsigned)(m2[k] >> 5)) ? b : (uint8_t)0;
     }
     __syncthreads();
   }
@@ -672,41 +618,86 @@ __device__ __forceinline__ GradView volume_view(const LdirVol& v, int* lock, int
   return GradView{v.g, reinterpret_cast<uintptr_t>(v.g), reinterpret_cast<uintptr_t>(v.g + v.D.ncells), lock, err};
 }
 
-template <int ND, int TX, int TY, int TZ>
-__global__ void ldir_check_kernel(const LdirBatch B, const uint8_t* __restrict__ saved, int64_t* __restrict__ queue,
+// A tile's box origin and volume, found once per record unit by the whole warp.
+struct TileAt {
+  int vi;
+  int64_t o[3];
+};
+template <int ND, int LY, int LZ>
+__device__ __forceinline__ TileAt tile_at(const LdirBatch& B, int64_t flat) {
+  using T = BitTile<ND, LY, LZ>;
+  TileAt t;
+  t.vi = batch_volume(B, flat);
+  const LdirVol& vol = B.v[t.vi];
+  const int64_t ntx = (vol.D.d[0] + T::TX - 1) / T::TX, nty = (vol.D.d[1] + T::TY - 1) / T::TY;
+  const int64_t tile = flat - vol.tile0;
+  int64_t tx, ty, tz;
+  if (tile < ((int64_t)1 << 32)) {  // 32-bit division (tile counts of real volumes)
+    const uint32_t u = (uint32_t)tile, nx = (uint32_t)ntx, ny = (uint32_t)nty;
+    const uint32_t r = u / nx;
+    tx = u - r * nx;
+    ty = ND == 3 ? r % ny : r;
+    tz = ND == 3 ? r / ny : 0;
+  } else {
+    const int64_t r = tile / ntx;
+    tx = tile - r * ntx;
+    ty = ND == 3 ? r % nty : r;
+    tz = ND == 3 ? r / nty : 0;
+  }
+  t.o[0] = tx * T::TX - 2;
+  t.o[1] = ty * T::TY - 2;
+  t.o[2] = ND == 3 ? tz * T::TZ - 2 : 0;
+  return t;
+}
+
+// Lower one recorded halo cell (box coords lx, ly, lz) in its owner's .grad where the
+// owner holds it higher, and queue it when it became an item.
+__device__ __forceinline__ void check_cell(const LdirBatch& B, const TileAt& t, int lx, int ly, int lz, unsigned v,
+                                           int64_t* queue, int* n_queue, int cap, int* lock, int* err) {
+  const LdirVol& vol = B.v[t.vi];
+  const int64_t gx = t.o[0] + lx, gy = t.o[1] + ly, gz = t.o[2] + lz;
+  const int64_t c = gx + gy * vol.D.cs[1] + gz * vol.D.cs[2];
+  if ((unsigned)(vol.g[c] >> 5) <= v) return;
+  if (!lower_ldir(volume_view(vol, lock, err), c, v)) return;
+  const int dim = (int)((gx & 1) + (gy & 1) + (gz & 1));
+  if ((dim == 1 && v == 2u) || (dim == 2 && v == 1u))
+    push_item(queue, n_queue, cap, err, ((int64_t)t.vi << kVolShift) | c);
+}
+
+// A warp per halo row record (a lane per cell) or per 32 inner-row bytes (a lane per row).
+template <int ND, int LY, int LZ>
+__global__ void ldir_check_kernel(const LdirBatch B, const uint8_t* __restrict__ rec, int64_t* __restrict__ queue,
                                   int* __restrict__ n_queue, int cap, int* lock, int* err) {
-  using T = LdirTile<ND, TX, TY, TZ>;
-  constexpr int NH = halo_count<T, ND>();
-  static_assert(NH % 16 == 0, "halo records are read 16 bytes at a time");
-  const int64_t total = B.total_tiles * NH;
-  // 16 saved bytes per step: almost all are zero (not lowered by their tile)
-  for (int64_t e0 = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) * 16; e0 < total;
-       e0 += (int64_t)gridDim.x * blockDim.x * 16) {
-    const uint4 q = *reinterpret_cast<const uint4*>(saved + e0);
-    if (!((q.x | q.y | q.z | q.w) & 0x01010101u)) continue;
+  using T = BitTile<ND, LY, LZ>;
+  constexpr int U = T::NHR + (T::NIR + 31) / 32;  // units of a tile
+  const int lane = threadIdx.x & 31;
+  const int64_t nunits = B.total_tiles * U;
+  const int64_t wstride = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t u = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; u < nunits; u += wstride) {
+    const int64_t flat = u / U;
+    const int j = (int)(u - flat * U);
+    const uint8_t* trec = rec + flat * T::REC;
+    if (j < T::NHR) {
+      const uint32_t w2 = reinterpret_cast<const uint32_t*>(trec)[2 * j];
+      const uint32_t w1 = reinterpret_cast<const uint32_t*>(trec)[2 * j + 1];
+      if (!(w2 | w1)) continue;
+      const TileAt t = tile_at<ND, LY, LZ>(B, flat);
+      if (!((w2 | w1) >> lane & 1u)) continue;
+      int ly, lz;
+      halo_row_of<ND, LY, LZ>(j, ly, lz);
+      check_cell(B, t, lane, ly, lz, (w1 >> lane & 1u) ? 1u : 2u, queue, n_queue, cap, lock, err);
+    } else {
+      const int i = (j - T::NHR) * 32 + lane;
+      const unsigned m = i < T::NIR ? trec[T::NHR * 8 + i] : 0u;
+      if (!__any_sync(~0u, m != 0u)) continue;
+      const TileAt t = tile_at<ND, LY, LZ>(B, flat);
+      if (!m) continue;
+      const int ly = 2 + i % (LY - 4), lz = ND == 3 ? 2 + i / (LY - 4) : 0;
 #pragma unroll 1
-    for (int j = 0; j < 16; j++) {
-      const int64_t e = e0 + j;
-      const uint8_t s = saved[e];
-      if (!(s & 1u)) continue;  // not lowered by its tile
-      const int64_t flat = e / NH;
-      const int b = halo_cell<T, ND>((int)(e % NH));
-      const int vi = batch_volume(B, flat);
-      const LdirVol& vol = B.v[vi];
-      const GradDims& D = vol.D;
-      const int64_t ntx = (D.d[0] + TX - 1) / TX, nty = (D.d[1] + TY - 1) / TY;
-      const int64_t tile = flat - vol.tile0;
-      const int64_t tx = tile % ntx, ty = (tile / ntx) % nty, tz = (ND == 3) ? tile / (ntx * nty) : 0;
-      const int lx = b % T::LX, ly = (b / T::LX) % T::LY, lz = b / (T::LX * T::LY);
-      const int64_t gx = tx * TX - T::H + lx, gy = ty * TY - T::H + ly, gz = (ND == 3) ? tz * TZ - T::H + lz : 0;
-      const int64_t c = gx + gy * D.cs[1] + gz * D.cs[2];
-      const unsigned v = s >> 5;
-      if ((unsigned)(vol.g[c] >> 5) <= v) continue;
-      const GradView G = volume_view(vol, lock, err);
-      if (!lower_ldir(G, c, v)) continue;
-      const int dim = (int)((gx & 1) + (gy & 1) + (gz & 1));
-      if ((dim == 1 && v == 2u) || (dim == 2 && v == 1u))
-        push_item(queue, n_queue, cap, err, ((int64_t)vi << kVolShift) | c);
+      for (int q = 0; q < 4; q++) {
+        const unsigned a2 = (m >> q) & 1u, a1 = (m >> (4 + q)) & 1u;
+        if (a2 | a1) check_cell(B, t, q < 2 ? q : kBitLX - 4 + q, ly, lz, a1 ? 1u : 2u, queue, n_queue, cap, lock, err);
+      }
     }
   }
 }
@@ -782,10 +773,16 @@ __global__ void __launch_bounds__(128) ldir_walk_kernel(const LdirBatch B, const
 }
 
 namespace {
+// multi-pass tiles
 constexpr int kTX3 = 32, kTY3 = 32, kTZ3 = 16, kBS3 = 512;
 constexpr int kTX2 = 128, kTY2 = 64, kBS2 = 256;
 using Tile3 = LdirTile<3, kTX3, kTY3, kTZ3>;
 using Tile2 = LdirTile<2, kTX2, kTY2, 1>;
+// single-pass bit-row tiles: 28 x 32 x 32 owned cells in 3D, 28 x 252 in 2D
+constexpr int kBitLY3 = 36, kBitLZ3 = 36, kBitBS3 = 512;
+constexpr int kBitLY2 = 256, kBitBS2 = 256;
+using Bit3 = BitTile<3, kBitLY3, kBitLZ3>;
+using Bit2 = BitTile<2, kBitLY2, 1>;
 }  // namespace
 
 int64_t ldir_num_tiles(int nd, const GradDims& D) {
@@ -793,7 +790,14 @@ int64_t ldir_num_tiles(int nd, const GradDims& D) {
   return ((D.d[0] + kTX2 - 1) / kTX2) * ((D.d[1] + kTY2 - 1) / kTY2);
 }
 
-int64_t ldir_halo_bytes(int nd) { return nd == 3 ? halo_count<Tile3, 3>() : halo_count<Tile2, 2>(); }
+int64_t ldir_bit_tiles(int nd, const GradDims& D) {
+  if (nd == 3)
+    return ((D.d[0] + Bit3::TX - 1) / Bit3::TX) * ((D.d[1] + Bit3::TY - 1) / Bit3::TY) *
+           ((D.d[2] + Bit3::TZ - 1) / Bit3::TZ);
+  return ((D.d[0] + Bit2::TX - 1) / Bit2::TX) * ((D.d[1] + Bit2::TY - 1) / Bit2::TY);
+}
+
+int64_t ldir_halo_bytes(int nd) { return nd == 3 ? Bit3::REC : Bit2::REC; }
 
 cudaError_t make_ldir_batch(int nd, int n, uint8_t* const* g, const GradDims* D, LdirBatch* B) {
   if (n < 1 || n > kMaxBatch || (nd == 2 && n != 1)) return cudaErrorInvalidValue;
@@ -803,44 +807,45 @@ cudaError_t make_ldir_batch(int nd, int n, uint8_t* const* g, const GradDims* D,
     B->v[i].g = g[i];
     B->v[i].D = D[i];
     B->v[i].tile0 = off;
-    off += ldir_num_tiles(nd, D[i]);
+    off += ldir_bit_tiles(nd, D[i]);
   }
   B->total_tiles = off;
   return cudaSuccess;
 }
 
-cudaError_t launch_ldir_tile(int nd, const LdirBatch& B, uint8_t* saved, int* err, int num_sms, cudaStream_t stream,
-                             int ctas_per_sm) {
-  const int64_t cap = (int64_t)num_sms * ctas_per_sm;
+template <class K>
+static cudaError_t launch_bit_tiles(K k, int bs, size_t sm, const LdirBatch& B, uint8_t* rec, int* err, int num_sms,
+                                    cudaStream_t stream, int ctas_per_sm) {
+  cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  if (e != cudaSuccess) return e;
+  int fit = 0;
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&fit, k, bs, sm);
+  if (e != cudaSuccess) return e;
+  const int per_sm = ctas_per_sm < fit ? ctas_per_sm : (fit > 0 ? fit : 1);
+  const int64_t cap = (int64_t)num_sms * per_sm;
   const int grid = (int)(B.total_tiles < cap ? B.total_tiles : cap);
   if (grid <= 0) return cudaSuccess;
-  if (nd == 3) {
-    auto k = ldir_tile_kernel<3, kTX3, kTY3, kTZ3, kBS3>;
-    const size_t sm = Tile3::tile_smem_bytes();
-    cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-    if (e != cudaSuccess) return e;
-    ::msc::count_launch();
-    k<<<grid, kBS3, sm, stream>>>(B, saved, err);
-  } else {
-    auto k = ldir_tile_kernel<2, kTX2, kTY2, 1, kBS2>;
-    const size_t sm = Tile2::tile_smem_bytes();
-    cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-    if (e != cudaSuccess) return e;
-    ::msc::count_launch();
-    k<<<grid, kBS2, sm, stream>>>(B, saved, err);
-  }
+  ::msc::count_launch();
+  k<<<grid, bs, sm, stream>>>(B, rec, err);
   return cudaGetLastError();
 }
 
-cudaError_t launch_ldir_check(int nd, const LdirBatch& B, const uint8_t* saved, int64_t* queue, int* n_queue, int cap,
+cudaError_t launch_ldir_tile(int nd, const LdirBatch& B, uint8_t* rec, int* err, int num_sms, cudaStream_t stream,
+                             int ctas_per_sm) {
+  if (nd == 3)
+    return launch_bit_tiles(ldir_tile_kernel<3, kBitLY3, kBitLZ3, kBitBS3, 3>, kBitBS3, Bit3::smem_bytes(), B, rec, err,
+                            num_sms, stream, ctas_per_sm);
+  return launch_bit_tiles(ldir_tile_kernel<2, kBitLY2, 1, kBitBS2, 4>, kBitBS2, Bit2::smem_bytes(), B, rec, err, num_sms,
+                          stream, ctas_per_sm);
+}
+
+cudaError_t launch_ldir_check(int nd, const LdirBatch& B, const uint8_t* rec, int64_t* queue, int* n_queue, int cap,
                               int* lock, int* err, int num_sms, cudaStream_t stream) {
-  if (nd == 3) {
-    ::msc::count_launch();
-    ldir_check_kernel<3, kTX3, kTY3, kTZ3><<<num_sms * 8, 256, 0, stream>>>(B, saved, queue, n_queue, cap, lock, err);
-  } else {
-    ::msc::count_launch();
-    ldir_check_kernel<2, kTX2, kTY2, 1><<<num_sms * 8, 256, 0, stream>>>(B, saved, queue, n_queue, cap, lock, err);
-  }
+  ::msc::count_launch();
+  if (nd == 3)
+    ldir_check_kernel<3, kBitLY3, kBitLZ3><<<num_sms * 8, 256, 0, stream>>>(B, rec, queue, n_queue, cap, lock, err);
+  else
+    ldir_check_kernel<2, kBitLY2, 1><<<num_sms * 8, 256, 0, stream>>>(B, rec, queue, n_queue, cap, lock, err);
   return cudaGetLastError();
 }
 

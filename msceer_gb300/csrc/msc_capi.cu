@@ -162,9 +162,9 @@ int ldir_passes(int nd, uint8_t* g, const msc::GradDims& D, cudaStream_t stream,
   return MSC_OK;
 }
 
-// Single-pass form: one tile pass that saves every tile's final box, a check of the
-// saved halos against the owners' cells, and global walks from the items the check
-// lowered.  Should a frontier queue overflow, the multi-pass form finishes the
+// Single-pass form: one tile pass that records the halo cells every tile lowered, a
+// check of those records against the owners' cells, and global walks from the items
+// the check lowered.  Should a frontier queue overflow, the multi-pass form finishes the
 // closure from wherever it stands (the closure is monotone, so any intermediate
 // state is a valid start).
 // Frontier queue capacity for `ntiles` tiles; MSC_LDIR_QUEUE_CAP lowers it (tests of
@@ -186,7 +186,7 @@ int ldir_batch_impl(int nd, const msc::LdirBatch& B, cudaStream_t stream, Scratc
   uint8_t* saved = nullptr;
   int64_t* queues = nullptr;
   int* ctr = nullptr;  // [0] queue a [1] queue b [2] lock [3] frontier overflow / CAS limit
-  MSC_CUDA(msc::scratch_alloc((void**)&saved, (size_t)(ntiles * box), stream), "scratch alloc(saved boxes)");
+  MSC_CUDA(msc::scratch_alloc((void**)&saved, (size_t)(ntiles * box), stream), "scratch alloc(halo records)");
   struct FreeAll {
     void* p[3];
     cudaStream_t st;

@@ -73,10 +73,13 @@ struct LstarBatch {
 cudaError_t make_lstar_batch(int n, const float* const* f, uint8_t* const* g, const GradDims* D, LstarBatch* B);
 cudaError_t launch_lstar_batch(const LstarBatch& B, int* err, int num_sms, cudaStream_t stream,
                                int blocks_per_sm = 64);
+// tiles of the multi-pass ldir kernel, and of the single-pass (bit-row) tile kernel
 int64_t ldir_num_tiles(int nd, const GradDims& D);
+int64_t ldir_bit_tiles(int nd, const GradDims& D);
 // The mesh description of the C ABI's dims (false for invalid or overflowing dims),
 // with the pair-code maps of single-vertex axes (msc_capi.cu).
 bool make_grad_dims(int nd, const int64_t* dims, GradDims* D);
+// halo record bytes of one single-pass tile
 int64_t ldir_halo_bytes(int nd);
 struct LdirVol {
   uint8_t* g;
