@@ -22,6 +22,8 @@ against the plain labels), or timed as the step with --triage.
               H2D of f, .grad, labels, D2H of both label volumes per step
   grad        the .grad alone: Gvert/s and its per-kernel breakdown
   grad_2d     the .grad of the 8192^2 k^-3 field (2D): Gvert/s, kernels, roofline
+  ms_graph    the Morse-Smale complex nodes and arcs of the step's .grad on the device
+              (msc_ms_graph_3d, extractmsc's arc flags): counts, ms, Gvert/s
   roofline    the dominant .grad kernel's algorithmic bytes / its measured duration
               against the measured HBM copy bandwidth (MEASURED_PEAKS.json)
   mismatch_vs_fp64_oracle  the labeling workload (256^3, 64 Gaussians, seed 0): the
@@ -578,6 +580,27 @@ def run_ours(args, ws, rank, local):
                    "value": V2 / (t2 * 1e-3) / 1e9, "unit": UNIT, "ms_per_step": t2, "kernels": k2, "roofline": r2}
         del f2, g2
 
+    # the Morse-Smale complex graph of the bench volume's .grad (extractmsc's
+    # ComputeFromGrad: arcs from 1-saddles and maxima, no geometry)
+    graph = None
+    if not args.no_batch:
+        from msceer_gb300 import ms_graph
+        lower_star_grad(f_dev, out=g_dev)
+        res = ms_graph(g_dev, f_dev, (1, 0, 1))
+        torch.cuda.synchronize(dev)
+        m0, m1 = _events(2)
+        m0.record(stream)
+        for _ in range(reps):
+            res = ms_graph(g_dev, f_dev, (1, 0, 1))
+        m1.record(stream)
+        torch.cuda.synchronize(dev)
+        tg = m0.elapsed_time(m1) / reps
+        graph = {"workload": f"MorseSmaleComplexBasic::ComputeFromGrad of the step's .grad, arcs from 1-saddles "
+                             f"and maxima (extractmsc's flags), no arc geometry",
+                 "nodes": int(res["node_cell"].numel()), "arcs": int(res["arc_lower"].numel()), "ms": tg,
+                 "value": V / (tg * 1e-3) / 1e9, "unit": UNIT}
+        del res
+
     # the labeling workload against the FP64 oracle: plain and learned labels
     mismatch = None
     if oracle_job is not None:
@@ -628,6 +651,8 @@ def run_ours(args, ws, rank, local):
         line.update(line_extra)
         if grad_2d is not None:
             line["grad_2d"] = grad_2d
+        if graph is not None:
+            line["ms_graph"] = graph
         if mismatch is not None:
             line["mismatch_vs_fp64_oracle"] = mismatch
         if batch is not None:

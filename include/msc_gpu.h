@@ -170,6 +170,29 @@ int msc_integrated_labels_3d_stages(const float* f, const uint8_t* grad, const i
 int msc_conforming_grad_3d(const float* f, const int32_t* labels_asc, const int32_t* labels_dsc, const int64_t dims[3],
                            uint8_t* grad, uint8_t* restriction_out, int64_t* touched_out, msc_stream_t stream);
 
+/* The Morse-Smale complex graph of a device .grad: the nodes and arcs
+ * MorseSmaleComplexBasic::ComputeFromGrad builds without arc geometry
+ * (gi_morse_smale_complex_basic.h:676-716), as extractmsc does after loading the .grad
+ * (extractmsc/extractmsc.cxx:482-504), read from device memory instead of a file.
+ * Nodes: every critical cell in cell-id order -- cell id, dimension, boundaryValue and
+ * value (f at the cell's highest vertex).  Arcs: for every node of dimension d >= 1
+ * with build_arcs[d - 1] set, the V-paths traced down from it (rec_tdcr_candidates,
+ * :550-577), node by node in depth-first facet order; lower / upper are node indices,
+ * persistence = value(upper) - value(lower).  grad, f and every output array: device.
+ * counts (host): [0] nodes, [1] arcs, always written.  The node arrays are written when
+ * all four are non-NULL and node_cap >= counts[0]; the arc arrays when arc_lower and
+ * arc_upper are non-NULL and arc_cap >= counts[1] (arc_persistence may be NULL) -- a
+ * call with capacities 0 sizes the arrays for a second call.  MSC_ERR_QUEUE_OVERFLOW if
+ * one node's trace branches beyond 64 pending paths, MSC_ERR_ITER_LIMIT if it visits
+ * more than 2^24 cells (only a .grad with a cycle, i.e. not a gradient, gets there).
+ * Blocking.  The reference's node
+ * and arc objects also carry list links and manifold ids; callers build those from
+ * these arrays. */
+int msc_ms_graph_3d(const uint8_t* grad, const float* f, const int64_t dims[3], const int build_arcs[3],
+                    int64_t node_cap, int64_t* node_cell, float* node_value, uint8_t* node_dim,
+                    uint8_t* node_boundary, int64_t arc_cap, int32_t* arc_lower, int32_t* arc_upper,
+                    float* arc_persistence, int64_t counts[2], msc_stream_t stream);
+
 /* The isolated-region cleaner alone: IsolatedCCRegionRemoverNEW::ComputeOutput
  * (gi_isolated_region_remover.h:155-192) on caller labels, as ondemandaccurate runs it
  * after the integration (ondemandaccurate.cxx:866-870, 942-946).  Same-label

@@ -17,6 +17,7 @@ from .api import (  # noqa: F401
     lower_star_grad,
     lower_star_grad_batch,
     lower_star_pairs,
+    ms_graph,
     num_cells,
     steepest_lstar,
 )

@@ -58,6 +58,9 @@ SIGNATURES = {
     "msc_ondemand_labels_host": (ctypes.c_int, [_VP, _I64P, _VP, _VP, _VP, _VP]),
     "msc_steepest_lstar_host": (ctypes.c_int, [_VP, _I64P, _VP]),
     "msc_lower_star_grad_2d_host": (ctypes.c_int, [_VP, _I64P, _VP]),
+    # grad f dims build node_cap cell value dim boundary arc_cap lower upper persistence counts stream
+    "msc_ms_graph_3d": (ctypes.c_int, [_VP, _VP, _I64P, _VP, ctypes.c_int64, _VP, _VP, _VP, _VP, ctypes.c_int64, _VP,
+                                       _VP, _VP, _I64P, _VP]),
 }
 
 

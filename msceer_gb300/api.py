@@ -219,6 +219,46 @@ def conforming_grad(f, grad, labels_asc=None, labels_dsc=None, restriction=False
     return (touched.value, rl) if restriction else touched.value
 
 
+def ms_graph(grad, f, build_arcs=(1, 0, 1)):
+    """MorseSmaleComplexBasic::ComputeFromGrad without arc geometry on a device .grad
+    (msc_ms_graph_3d): the critical cells as nodes and the traced V-paths as arcs.
+    ``grad``: CUDA uint8 .grad of ``f`` (CUDA float32 (Z, Y, X)); ``build_arcs``: the
+    reference's SetBuildArcs flags (arcs from 1-saddles, 2-saddles, maxima; extractmsc
+    uses (1, 0, 1)).  Returns a dict of CUDA tensors: node_cell (int64), node_value
+    (float32), node_dim / node_boundary (uint8), arc_lower / arc_upper (int32 node
+    indices) and arc_persistence (float32)."""
+    import torch
+
+    f = f.contiguous()
+    dims = _shape_dims(f.shape)
+    if len(dims) != 3 or not (f.is_cuda and grad.is_cuda) or grad.numel() != num_cells(dims):
+        raise ValueError("ms_graph takes a CUDA 3D volume and its .grad")
+    lib = _lib.load()
+    dev = f.device
+    stream = torch.cuda.current_stream(dev).cuda_stream
+    b = (ctypes.c_int * 3)(*[int(x) for x in build_arcs])
+    counts = (ctypes.c_int64 * 2)()
+    ptr = lambda t: ctypes.c_void_p(t.data_ptr())  # noqa: E731
+    with torch.cuda.device(dev):
+        rc = lib.msc_ms_graph_3d(ptr(grad), ptr(f), _lib.dims_arg(dims), b, 0, None, None, None, None, 0, None, None,
+                                 None, counts, ctypes.c_void_p(stream))
+        _lib.check(rc, "msc_ms_graph_3d")
+        nn, na = counts[0], counts[1]
+        out = {"node_cell": torch.empty(nn, dtype=torch.int64, device=dev),
+               "node_value": torch.empty(nn, dtype=torch.float32, device=dev),
+               "node_dim": torch.empty(nn, dtype=torch.uint8, device=dev),
+               "node_boundary": torch.empty(nn, dtype=torch.uint8, device=dev),
+               "arc_lower": torch.empty(na, dtype=torch.int32, device=dev),
+               "arc_upper": torch.empty(na, dtype=torch.int32, device=dev),
+               "arc_persistence": torch.empty(na, dtype=torch.float32, device=dev)}
+        rc = lib.msc_ms_graph_3d(ptr(grad), ptr(f), _lib.dims_arg(dims), b, nn, ptr(out["node_cell"]),
+                                 ptr(out["node_value"]), ptr(out["node_dim"]), ptr(out["node_boundary"]), na,
+                                 ptr(out["arc_lower"]), ptr(out["arc_upper"]), ptr(out["arc_persistence"]), counts,
+                                 ctypes.c_void_p(stream))
+        _lib.check(rc, "msc_ms_graph_3d")
+    return out
+
+
 def clean_regions(f, labels, direction):
     """IsolatedCCRegionRemoverNEW on device labels (msc_clean_regions_3d): ``direction``
     -1 for ascending labels (lowest value first), +1 for descending ones.  ``f``: CUDA

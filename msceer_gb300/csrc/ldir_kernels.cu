@@ -664,33 +664,54 @@ __device__ __forceinline__ void check_cell(const LdirBatch& B, const TileAt& t, 
     push_item(queue, n_queue, cap, err, ((int64_t)t.vi << kVolShift) | c);
 }
 
-// A warp per halo row record (a lane per cell) or per 32 inner-row bytes (a lane per row).
+// A block per tile: a warp per halo row record (a lane per cell, KU rows' loads in
+// flight), then a thread per inner row byte.
 template <int ND, int LY, int LZ>
-__global__ void ldir_check_kernel(const LdirBatch B, const uint8_t* __restrict__ rec, int64_t* __restrict__ queue,
-                                  int* __restrict__ n_queue, int cap, int* lock, int* err) {
+__global__ void __launch_bounds__(256) ldir_check_kernel(const LdirBatch B, const uint8_t* __restrict__ rec,
+                                                         int64_t* __restrict__ queue, int* __restrict__ n_queue,
+                                                         int cap, int* lock, int* err) {
   using T = BitTile<ND, LY, LZ>;
-  constexpr int U = T::NHR + (T::NIR + 31) / 32;  // units of a tile
-  const int lane = threadIdx.x & 31;
-  const int64_t nunits = B.total_tiles * U;
-  const int64_t wstride = ((int64_t)gridDim.x * blockDim.x) >> 5;
-  for (int64_t u = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; u < nunits; u += wstride) {
-    const int64_t flat = u / U;
-    const int j = (int)(u - flat * U);
+  constexpr int KU = 4;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
+  for (int64_t flat = blockIdx.x; flat < B.total_tiles; flat += gridDim.x) {
     const uint8_t* trec = rec + flat * T::REC;
-    if (j < T::NHR) {
-      const uint32_t w2 = reinterpret_cast<const uint32_t*>(trec)[2 * j];
-      const uint32_t w1 = reinterpret_cast<const uint32_t*>(trec)[2 * j + 1];
-      if (!(w2 | w1)) continue;
-      const TileAt t = tile_at<ND, LY, LZ>(B, flat);
-      if (!((w2 | w1) >> lane & 1u)) continue;
-      int ly, lz;
-      halo_row_of<ND, LY, LZ>(j, ly, lz);
-      check_cell(B, t, lane, ly, lz, (w1 >> lane & 1u) ? 1u : 2u, queue, n_queue, cap, lock, err);
-    } else {
-      const int i = (j - T::NHR) * 32 + lane;
-      const unsigned m = i < T::NIR ? trec[T::NHR * 8 + i] : 0u;
-      if (!__any_sync(~0u, m != 0u)) continue;
-      const TileAt t = tile_at<ND, LY, LZ>(B, flat);
+    const uint32_t* wrec = reinterpret_cast<const uint32_t*>(trec);
+    const TileAt t = tile_at<ND, LY, LZ>(B, flat);
+    const LdirVol& vol = B.v[t.vi];
+    for (int j0 = warp; j0 < T::NHR; j0 += nwarp * KU) {
+      uint32_t w2[KU], w1[KU];
+      uint8_t own[KU];
+      int64_t cell[KU];
+#pragma unroll
+      for (int k = 0; k < KU; k++) {
+        const int j = j0 + k * nwarp;
+        w2[k] = j < T::NHR ? wrec[2 * j] : 0u;
+        w1[k] = j < T::NHR ? wrec[2 * j + 1] : 0u;
+      }
+#pragma unroll
+      for (int k = 0; k < KU; k++) {
+        const int j = j0 + k * nwarp;
+        own[k] = 0;
+        cell[k] = -1;
+        if (((w2[k] | w1[k]) >> lane) & 1u) {
+          int ly, lz;
+          halo_row_of<ND, LY, LZ>(j, ly, lz);
+          cell[k] = (t.o[0] + lane) + (t.o[1] + ly) * vol.D.cs[1] + (t.o[2] + lz) * vol.D.cs[2];
+          own[k] = vol.g[cell[k]];
+        }
+      }
+#pragma unroll
+      for (int k = 0; k < KU; k++) {
+        if (cell[k] < 0) continue;
+        const unsigned v = ((w1[k] >> lane) & 1u) ? 1u : 2u;
+        if ((unsigned)(own[k] >> 5) <= v) continue;
+        int ly, lz;
+        halo_row_of<ND, LY, LZ>(j0 + k * nwarp, ly, lz);
+        check_cell(B, t, lane, ly, lz, v, queue, n_queue, cap, lock, err);
+      }
+    }
+    for (int i = threadIdx.x; i < T::NIR; i += blockDim.x) {
+      const unsigned m = trec[T::NHR * 8 + i];
       if (!m) continue;
       const int ly = 2 + i % (LY - 4), lz = ND == 3 ? 2 + i / (LY - 4) : 0;
 #pragma unroll 1
@@ -839,13 +860,20 @@ cudaError_t launch_ldir_tile(int nd, const LdirBatch& B, uint8_t* rec, int* err,
                           stream, ctas_per_sm);
 }
 
+static int check_grid(const LdirBatch& B, int num_sms) {
+  const int64_t cap = (int64_t)num_sms * 8;
+  return (int)(B.total_tiles < cap ? (B.total_tiles > 0 ? B.total_tiles : 1) : cap);
+}
+
 cudaError_t launch_ldir_check(int nd, const LdirBatch& B, const uint8_t* rec, int64_t* queue, int* n_queue, int cap,
                               int* lock, int* err, int num_sms, cudaStream_t stream) {
   ::msc::count_launch();
   if (nd == 3)
-    ldir_check_kernel<3, kBitLY3, kBitLZ3><<<num_sms * 8, 256, 0, stream>>>(B, rec, queue, n_queue, cap, lock, err);
+    ldir_check_kernel<3, kBitLY3, kBitLZ3><<<check_grid(B, num_sms), 256, 0, stream>>>(B, rec, queue, n_queue, cap,
+                                                                                       lock, err);
   else
-    ldir_check_kernel<2, kBitLY2, 1><<<num_sms * 8, 256, 0, stream>>>(B, rec, queue, n_queue, cap, lock, err);
+    ldir_check_kernel<2, kBitLY2, 1><<<check_grid(B, num_sms), 256, 0, stream>>>(B, rec, queue, n_queue, cap, lock,
+                                                                                 err);
   return cudaGetLastError();
 }
 

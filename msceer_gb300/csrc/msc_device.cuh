@@ -17,6 +17,8 @@ namespace msc {
 // its memory between calls (msc_trim_scratch hands the unused part back).
 cudaError_t scratch_pool(cudaMemPool_t* out);
 cudaError_t scratch_alloc(void** p, size_t bytes, cudaStream_t stream);
+// Records the calling thread's error text for msc_last_error_string(); returns code.
+int set_last_error(int code, const char* msg);
 void count_launch();
 void add_launches(long long n);
 long long launches_so_far();

@@ -582,3 +582,114 @@ int oracle_central_diff_2d(const float* f, int64_t X, int64_t Y, double* g) {
 	return 0;
 }
 
+
+/* ---- Morse-Smale complex graph (MorseSmaleComplexBasic::ComputeFromGrad) ------------- */
+
+typedef struct {
+	const mesh_t* m;
+	const uint8_t* g;
+	const int64_t* node_cell;  /* critical cells, increasing */
+	int64_t n_nodes;
+	int64_t arc_cap, n_arcs;
+	int32_t* lower;
+	int32_t* upper;
+	int64_t visits;  /* a .grad with a cycle (invalid input) would recurse forever */
+	int depth, overflow;
+} ms_trace_t;
+
+/* nodeIdForCell (gi_morse_smale_complex_basic.h:212): the node of a critical cell */
+static int64_t ms_node_of(const ms_trace_t* t, int64_t cell) {
+	int64_t lo = 0, hi = t->n_nodes - 1;
+	while (lo <= hi) {
+		int64_t mid = (lo + hi) / 2;
+		if (t->node_cell[mid] == cell) return mid;
+		if (t->node_cell[mid] < cell) lo = mid + 1; else hi = mid - 1;
+	}
+	return -1;
+}
+
+/* rec_tdcr_candidates (gi_morse_smale_complex_basic.h:550-577): facets in order; a
+ * critical facet ends a V-path (an arc to its node), a facet on the restricted
+ * manifold (ldir == temp_dim) continues at its pair when that pair is another cell of
+ * the traced cell's dimension. */
+static void ms_trace_down(ms_trace_t* t, int64_t cell, int temp_dim, int32_t start) {
+	int64_t c[3], fc[6];
+	if (++t->visits > ((int64_t)1 << 26) || t->depth >= (1 << 14)) { t->overflow = 1; return; }
+	cell_coords(t->m, cell, c);
+	const int dim = cell_dim(t->m, c);
+	const int nf = facets(t->m, cell, c, fc);
+	for (int i = 0; i < nf; i++) {
+		const uint8_t b = t->g[fc[i]];
+		const uint8_t code = (uint8_t)((b & GB_PAIR_MSK) >> GB_PAIR_SH);
+		if (code == 7) {
+			const int64_t lower = ms_node_of(t, fc[i]);
+			if (lower < 0) continue;
+			if (t->n_arcs < t->arc_cap) {
+				t->lower[t->n_arcs] = (int32_t)lower;
+				t->upper[t->n_arcs] = start;
+			}
+			t->n_arcs++;
+		} else if (code < 6 && (int)((b & GB_LDIR_MSK) >> GB_LDIR_SH) == temp_dim) {
+			const int64_t p = decode_pair(t->m, fc[i], code);
+			if (p < 0 || p >= t->m->ncells) continue;
+			int64_t pc[3];
+			cell_coords(t->m, p, pc);
+			if (p != cell && cell_dim(t->m, pc) == dim) {
+				t->depth++;
+				ms_trace_down(t, p, temp_dim, start);
+				t->depth--;
+			}
+		}
+	}
+}
+
+int oracle_ms_graph_3d(const uint8_t* grad, const float* f, int64_t X, int64_t Y, int64_t Z, const int build[3],
+                       int64_t node_cap, int64_t* node_cell, float* node_value, uint8_t* node_dim,
+                       uint8_t* node_boundary, int64_t arc_cap, int32_t* arc_lower, int32_t* arc_upper,
+                       float* arc_persistence, int64_t counts[2]) {
+	mesh_t m;
+	if (mesh_init(&m, 3, X, Y, Z)) return -1;
+	/* the nodes: every critical cell, in AllCellsIterator (cell id) order */
+	int64_t n = 0;
+	for (int64_t i = 0; i < m.ncells; i++)
+		if (((grad[i] & GB_PAIR_MSK) >> GB_PAIR_SH) == 7) n++;
+	int64_t* cells = (int64_t*)malloc(sizeof(int64_t) * (size_t)(n + 1));
+	float* val = (float*)malloc(sizeof(float) * (size_t)(n + 1));
+	if (!cells || !val) { free(cells); free(val); return -2; }
+	n = 0;
+	for (int64_t i = 0; i < m.ncells; i++) {
+		if (((grad[i] & GB_PAIR_MSK) >> GB_PAIR_SH) != 7) continue;
+		int64_t c[3];
+		cell_coords(&m, i, c);
+		cells[n] = i;
+		/* createNode: value = cellValue = f at Cell2HighestVertex */
+		val[n] = f[extreme_vertex(&m, f, c, 1)];
+		if (n < node_cap) {
+			node_cell[n] = i;
+			node_value[n] = val[n];
+			node_dim[n] = (uint8_t)cell_dim(&m, c);
+			node_boundary[n] = (uint8_t)boundary_value(&m, c);
+		}
+		n++;
+	}
+	/* the arcs: AddArcsThreadLocalNoGeom over the nodes in order (:600-620) */
+	ms_trace_t t = { &m, grad, cells, n, arc_cap, 0, arc_lower, arc_upper, 0, 0, 0 };
+	for (int64_t j = 0; j < n; j++) {
+		int64_t c[3];
+		cell_coords(&m, cells[j], c);
+		const int d = cell_dim(&m, c);
+		if (d == 0 || !build[d - 1]) continue;
+		const int temp_dim = (int)((grad[cells[j]] & GB_LDIR_MSK) >> GB_LDIR_SH) + 1;
+		const int64_t a0 = t.n_arcs;
+		t.visits = 0;
+		ms_trace_down(&t, cells[j], temp_dim, (int32_t)j);
+		if (t.overflow) { free(cells); free(val); return -3; }
+		for (int64_t a = a0; a < t.n_arcs && a < arc_cap; a++)
+			if (arc_persistence) arc_persistence[a] = val[arc_upper[a]] - val[arc_lower[a]];
+	}
+	counts[0] = n;
+	counts[1] = t.n_arcs;
+	free(cells);
+	free(val);
+	return 0;
+}

@@ -41,6 +41,18 @@ int oracle_boundary_labels_3d(const float* f, int64_t X, int64_t Y, int64_t Z, c
 int oracle_conform_3d(const float* f, int64_t X, int64_t Y, int64_t Z, const uint8_t* restrict_lab, uint8_t* g,
                       int nthreads);
 
+/* Morse-Smale complex graph of a finished .grad: MorseSmaleComplexBasic::ComputeFromGrad
+ * without arc geometry (gi_morse_smale_complex_basic.h:676-716).  Nodes are the
+ * critical cells in cell order: cell id, dimension, boundaryValue and value (f at the
+ * cell's highest vertex).  Arcs are traced down from every node whose dimension d has
+ * build[d - 1] set, in node order and depth-first facet order; arc_persistence is
+ * value(upper) - value(lower).  Counts go to counts[0] (nodes) and counts[1] (arcs);
+ * the arrays are filled up to node_cap / arc_cap entries. */
+int oracle_ms_graph_3d(const uint8_t* grad, const float* f, int64_t X, int64_t Y, int64_t Z, const int build[3],
+                       int64_t node_cap, int64_t* node_cell, float* node_value, uint8_t* node_dim,
+                       uint8_t* node_boundary, int64_t arc_cap, int32_t* arc_lower, int32_t* arc_upper,
+                       float* arc_persistence, int64_t counts[2]);
+
 /* Central-difference gradient, x,y,z (x,y) doubles per vertex, as the reference's
  * Vec3d array after ComputeGradFromImage(1). */
 int oracle_central_diff_3d(const float* f, int64_t X, int64_t Y, int64_t Z, double* g);

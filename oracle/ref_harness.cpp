@@ -17,6 +17,10 @@
 //       needASC2 = needDSC2 = 1: VertexLabelingToBoundaryLabeling::ComputeMINBoundary /
 //       ComputeMAXBoundary, the constrained MyRobinsNoalloc<...,4,6>::ComputeLowerStar of
 //       the touched vertices and RecordGrad (:693-699)
+//   ref_ms_graph_3d        == extractmsc/extractmsc.cxx:482-504: a .grad loaded into
+//       DiscreteGradientLabeling, LazyMaximumVertexLabeling + TopologicalMaxVertexMeshFunction,
+//       MorseSmaleComplexBasic::ComputeFromGrad with the given arc build flags and no
+//       arc geometry (gi_morse_smale_complex_basic.h:676-716)
 //
 // The only deviation from the shipped program: the mesh type is a thin subclass of
 // TopologicalRegularGrid3D that adds a no-op cellid2Coords(INDEX_TYPE, Vec2l&)
@@ -48,6 +52,7 @@
 #include "gi_numeric_integrator_path_compressing.h"
 #include "gi_isolated_region_remover.h"
 #include "gi_labeling_to_bounary_labeling.h"
+#include "gi_morse_smale_complex_basic.h"
 
 using namespace GInt;
 
@@ -317,6 +322,52 @@ int ref_ondemand_3d(const float* f, long long X, long long Y, long long Z, float
 			for (long long i = 0; i < (long long)mesh->numCells(); i++) restrict_out[i] = (unsigned char)restriction_labels->GetLabel(i);
 	}
 	return 0;   // the reference objects are left to the process (their destructors double-free shared labels)
+}
+
+
+// Nodes (cell, value, dim, boundary) and arcs (lower, upper, persistence) of
+// MorseSmaleComplexBasic::ComputeFromGrad on a finished .grad; counts[0] nodes,
+// counts[1] arcs, arrays filled up to their caps.
+int ref_ms_graph_3d(const float* f, long long X, long long Y, long long Z, const unsigned char* grad, const int* build,
+                    int nthreads, long long node_cap, long long* node_cell, float* node_value, unsigned char* node_dim,
+                    unsigned char* node_boundary, long long arc_cap, int* arc_lower, int* arc_upper,
+                    float* arc_persistence, long long* counts) {
+	using namespace refharness;
+	typedef LazyMaximumVertexLabeling<MeshType, GridFuncType> LazyMaxVLType;
+	typedef TopologicalMaxVertexMeshFunction<MeshType, LazyMaxVLType, GridFuncType, float> LazyTopoFuncType;
+	typedef MorseSmaleComplexBasic<float, MeshType, LazyTopoFuncType, GradType> MscType;
+	if (nthreads > 0) omp_set_num_threads(nthreads);
+	GridType* grid = new GridType(Vec3l(X, Y, Z), Vec3b(0, 0, 0));
+	std::vector<float> img(f, f + X * Y * Z);
+	GridFuncType* func = new GridFuncType(grid, img.data());
+	MeshType* mesh = new MeshType(grid);
+	LazyMaxVLType* maxv = new LazyMaxVLType(mesh, func);
+	maxv->ComputeOutput();
+	LazyTopoFuncType* topofunc = new LazyTopoFuncType();
+	topofunc->setMeshAndFuncAndMaxVLabeling(mesh, func, maxv);
+	GradType* labeling = new GradType(mesh);
+	std::memcpy(labeling->m_dgrad->LabelArray(), grad, (size_t)mesh->numCells());
+	MscType* msc = new MscType(labeling, mesh, topofunc);
+	msc->SetBuildArcGeometry(Vec3b(false, false, false));
+	msc->SetBuildArcs(Vec3b(build[0] != 0, build[1] != 0, build[2] != 0));
+	msc->ComputeFromGrad();
+	const long long nn = msc->numNodes(), na = msc->numArcs();
+	for (long long i = 0; i < nn && i < node_cap; i++) {
+		const auto& n = msc->getNode((INT_TYPE)i);
+		node_cell[i] = (long long)n.cellindex;
+		node_value[i] = n.value;
+		node_dim[i] = (unsigned char)n.dim;
+		node_boundary[i] = (unsigned char)n.boundary;
+	}
+	for (long long i = 0; i < na && i < arc_cap; i++) {
+		const auto& a = msc->getArc((INT_TYPE)i);
+		arc_lower[i] = (int)a.lower;
+		arc_upper[i] = (int)a.upper;
+		arc_persistence[i] = a.persistence;
+	}
+	counts[0] = nn;
+	counts[1] = na;
+	return 0;   // the reference objects are left to the process, as above
 }
 
 }  // extern "C"

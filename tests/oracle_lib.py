@@ -47,6 +47,8 @@ class Oracle:
         lib.oracle_clean_regions_3d.argtypes = [_VP, _I64, _I64, _I64, ctypes.c_int, _VP]
         lib.oracle_boundary_labels_3d.argtypes = [_VP, _I64, _I64, _I64, _VP, _VP, _VP]
         lib.oracle_conform_3d.argtypes = [_VP, _I64, _I64, _I64, _VP, _VP, ctypes.c_int]
+        lib.oracle_ms_graph_3d.argtypes = [_VP, _VP, _I64, _I64, _I64, _VP, _I64, _VP, _VP, _VP, _VP, _I64, _VP, _VP,
+                                           _VP, _VP]
 
     def labels(self, f, grad, error_threshold, gradient_threshold, iteration_limit, max_step, presimp):
         """ASC and DSC labels (regions named by their smallest seed vertex) plus stages."""
@@ -89,6 +91,17 @@ class Oracle:
         r = np.ascontiguousarray(restrict, dtype=np.uint8)
         assert self.lib.oracle_conform_3d(f.ctypes.data, *f.shape[::-1], r.ctypes.data, g.ctypes.data, nthreads) == 0
         return g
+
+    def ms_graph(self, f, grad, build=(1, 0, 1)):
+        """MorseSmaleComplexBasic::ComputeFromGrad (no arc geometry): a dict of node and arc arrays."""
+        f = np.ascontiguousarray(f, dtype=np.float32)
+        grad = np.ascontiguousarray(grad, dtype=np.uint8)
+        b = (ctypes.c_int * 3)(*build)
+        counts = np.zeros(2, np.int64)
+        self.lib.oracle_ms_graph_3d(grad.ctypes.data, f.ctypes.data, *f.shape[::-1], b, 0, None, None, None, None, 0,
+                                    None, None, None, counts.ctypes.data)
+        return _ms_graph_call(lambda *a: self.lib.oracle_ms_graph_3d(grad.ctypes.data, f.ctypes.data, *f.shape[::-1],
+                                                                     b, *a), counts)
 
     def central_diff(self, f: np.ndarray) -> np.ndarray:
         """(..., ND) float64 gradient, the reference's Vec3d array."""
@@ -138,6 +151,34 @@ def load() -> Oracle:
     return Oracle(ctypes.CDLL(str(ORACLE_SO)))
 
 
+def _ms_graph_call(fn, counts):
+    nn, na = int(counts[0]), int(counts[1])
+    out = {"node_cell": np.empty(nn, np.int64), "node_value": np.empty(nn, np.float32),
+           "node_dim": np.empty(nn, np.uint8), "node_boundary": np.empty(nn, np.uint8),
+           "arc_lower": np.empty(na, np.int32), "arc_upper": np.empty(na, np.int32),
+           "arc_persistence": np.empty(na, np.float32)}
+    c2 = np.zeros(2, np.int64)
+    assert fn(nn, out["node_cell"].ctypes.data, out["node_value"].ctypes.data, out["node_dim"].ctypes.data,
+              out["node_boundary"].ctypes.data, na, out["arc_lower"].ctypes.data, out["arc_upper"].ctypes.data,
+              out["arc_persistence"].ctypes.data, c2.ctypes.data) == 0
+    assert tuple(c2) == (nn, na)
+    return out
+
+
+def ref_ms_graph(lib, f, grad, build=(1, 0, 1), nthreads=1):
+    """The reference's MorseSmaleComplexBasic::ComputeFromGrad on a .grad (extractmsc's
+    setup), as ms_graph returns it."""
+    f = np.ascontiguousarray(f, dtype=np.float32)
+    grad = np.ascontiguousarray(grad, dtype=np.uint8)
+    b = (ctypes.c_int * 3)(*build)
+    counts = np.zeros(2, np.int64)
+    dims = f.shape[::-1]
+    lib.ref_ms_graph_3d(f.ctypes.data, *dims, grad.ctypes.data, b, nthreads, 0, None, None, None, None, 0, None, None,
+                        None, counts.ctypes.data)
+    return _ms_graph_call(lambda *a: lib.ref_ms_graph_3d(f.ctypes.data, *dims, grad.ctypes.data, b, nthreads, *a),
+                          counts)
+
+
 def load_ref():
     """The reference compiled from its own sources, or None where it is absent."""
     if not REF_SO.exists():
@@ -148,6 +189,9 @@ def load_ref():
     lib.ref_lstar_grad_2d.argtypes = [_VP, ctypes.c_longlong, ctypes.c_longlong, ctypes.c_int,
                                       ctypes.c_char_p, _VP]
     lib.ref_central_diff_3d.argtypes = [_VP, ctypes.c_longlong, ctypes.c_longlong, ctypes.c_longlong, _VP]
+    lib.ref_ms_graph_3d.argtypes = [_VP, ctypes.c_longlong, ctypes.c_longlong, ctypes.c_longlong, _VP, _VP,
+                                    ctypes.c_int, ctypes.c_longlong, _VP, _VP, _VP, _VP, ctypes.c_longlong, _VP, _VP,
+                                    _VP, _VP]
     lib.ref_labels_3d.argtypes = [_VP, ctypes.c_longlong, ctypes.c_longlong, ctypes.c_longlong, ctypes.c_float,
                                   ctypes.c_float, ctypes.c_int, ctypes.c_float, _VP, _VP, _VP]
     lib.ref_ondemand_3d.argtypes = [_VP, ctypes.c_longlong, ctypes.c_longlong, ctypes.c_longlong, ctypes.c_float,

@@ -132,3 +132,39 @@ def test_conforming_grad_oracle_against_reference(oracle, make):
     got = oracle.conform(f, restrict, base)
     assert np.array_equal(got, want["grad"]), oracle_lib.describe_mismatch(got, want["grad"], f.shape[::-1])
     assert not np.array_equal(got, base)   # the re-pairing changed something
+
+
+MS_GRAPH_CASES = json.loads((GOLDEN / "ms_graph.json").read_text())
+
+
+def _digests(graph):
+    return {k: hashlib.sha256(np.ascontiguousarray(v).tobytes()).hexdigest() for k, v in graph.items()}
+
+
+@pytest.mark.parametrize("key", sorted(MS_GRAPH_CASES))
+def test_ms_graph_oracle_against_golden(oracle, key):
+    """MorseSmaleComplexBasic::ComputeFromGrad restated: nodes and arcs (with
+    multiplicity and order) equal the reference's on its own .grad, by SHA-256."""
+    spec = MS_GRAPH_CASES[key]
+    f = _regenerate(spec).astype(np.float32)
+    g = oracle.grad(f)
+    assert hashlib.sha256(g.tobytes()).hexdigest() == spec["grad_sha256"]
+    got = oracle.ms_graph(f, g, spec["build_arcs"])
+    assert (got["node_cell"].size, got["arc_lower"].size) == (spec["nodes"], spec["arcs"])
+    d = _digests(got)
+    same_f = hashlib.sha256(f.tobytes()).hexdigest() == spec["f_sha256"]
+    keys = spec["sha256"] if same_f else [k for k in spec["sha256"] if k not in ("node_value", "arc_persistence")]
+    assert {k: d[k] for k in keys} == {k: spec["sha256"][k] for k in keys}
+
+
+@pytest.mark.parametrize("build", [(1, 0, 1), (1, 1, 1), (0, 1, 0)])
+def test_ms_graph_oracle_against_reference(oracle, build):
+    ref = oracle_lib.load_ref()
+    if ref is None:
+        pytest.skip("the reference is not compiled on this machine")
+    for f in (fields.power_law_field((30, 26, 22), seed=11), fields.gaussian_sum((28, 24, 20), 12, seed=12)):
+        g = oracle.grad(f)
+        got = oracle.ms_graph(f, g, build)
+        want = oracle_lib.ref_ms_graph(ref, f, g, build)
+        for k in want:
+            assert np.array_equal(got[k], want[k]), k
