@@ -138,6 +138,27 @@ __global__ void __launch_bounds__(kScanThreads) excl_scan_kernel(T* __restrict__
   if (threadIdx.x == 0) *sum = carry;
 }
 
+// The same for long arrays, in three launches: the sum of every kScanThreads-element
+// chunk, the one-block scan of those sums, then every chunk scanned from its offset.
+template <class T>
+__global__ void __launch_bounds__(kScanThreads) chunk_sum_kernel(const T* __restrict__ a, int64_t n,
+                                                                 T* __restrict__ sums) {
+  __shared__ T s_warp[32];
+  const int64_t i = (int64_t)blockIdx.x * kScanThreads + threadIdx.x;
+  T tot = 0;
+  block_excl_scan<T>(i < n ? a[i] : (T)0, s_warp, &tot);
+  if (threadIdx.x == 0) sums[blockIdx.x] = tot;
+}
+template <class T>
+__global__ void __launch_bounds__(kScanThreads) chunk_scan_kernel(T* __restrict__ a, int64_t n,
+                                                                  const T* __restrict__ offs) {
+  __shared__ T s_warp[32];
+  const int64_t i = (int64_t)blockIdx.x * kScanThreads + threadIdx.x;
+  const T v = i < n ? a[i] : (T)0;
+  const T off = block_excl_scan<T>(v, s_warp, nullptr);
+  if (i < n) a[i] = offs[blockIdx.x] + off;
+}
+
 __global__ void __launch_bounds__(kCritThreads) crit_write_kernel(const uint8_t* __restrict__ g, int64_t ncells,
                                                                   const int64_t* __restrict__ offsets,
                                                                   int64_t* __restrict__ node_cell) {
@@ -235,14 +256,13 @@ __device__ int trace_node(const MsMesh& M, const int64_t* __restrict__ node_cell
         if (code == 7u) {
           child[nc++] = fc | kEmit;
         } else if (code < 6u && ldir(b) == temp_dim) {
-          // the pair's coordinates: the facet's, moved one cell along the code's axis
-          int64_t pc[3] = {c[0], c[1], c[2]};
-          pc[a] += s == 0 ? 1 : -1;
-          const int pa = (int)(code >> 1);
-          pc[pa] += (code & 1u) ? -1 : 1;
-          if (pc[pa] < 0 || pc[pa] >= M.d[pa]) continue;  // points out of the complex: not a gradient
-          const int64_t p = (code & 1u) ? fc - M.cs[pa] : fc + M.cs[pa];
-          if (p == t) continue;
+          // the pair: the cell at the code's stride (UncompressByteTo6NeighborOffset;
+          // with a single-vertex axis two axes share a stride and the code names the
+          // first), inside the array for any byte
+          const int64_t p = (code & 1u) ? fc - M.cs[code >> 1] : fc + M.cs[code >> 1];
+          if (p == t || p < 0 || p >= M.ncells) continue;
+          int64_t pc[3];
+          coords(M, p, pc);
           if (dim_of(pc) == dim) child[nc++] = p;
         }
       }
@@ -319,6 +339,24 @@ int grid_for(int64_t n, int threads) {
   return (int)(b < 1 ? 1 : (b < cap ? b : cap));
 }
 
+// a[0, n) -> exclusive offsets in place, *sum (device) = the total
+int scan_in_place(Pool& P, int64_t* a, int64_t n, int64_t* sum, cudaStream_t stream) {
+  const int64_t nch = (n + kScanThreads - 1) / kScanThreads;
+  int64_t* csum = nullptr;
+  GCUDA(P.get((void**)&csum, (size_t)(nch + 1) * sizeof(int64_t)), "scratch alloc(chunk sums)");
+  if (nch > 0) {
+    count_launch();
+    chunk_sum_kernel<int64_t><<<(unsigned)nch, kScanThreads, 0, stream>>>(a, n, csum);
+  }
+  count_launch();
+  excl_scan_kernel<int64_t><<<1, kScanThreads, 0, stream>>>(csum, nch, sum);
+  if (nch > 0) {
+    count_launch();
+    chunk_scan_kernel<int64_t><<<(unsigned)nch, kScanThreads, 0, stream>>>(a, n, csum);
+  }
+  return MSC_OK;
+}
+
 int ms_graph_impl(const uint8_t* g, const float* f, const int64_t* dims, const int* build, int64_t node_cap,
                   int64_t* node_cell, float* node_value, uint8_t* node_dim, uint8_t* node_boundary, int64_t arc_cap,
                   int32_t* arc_lower, int32_t* arc_upper, float* arc_pers, int64_t* counts_out,
@@ -352,8 +390,7 @@ int ms_graph_impl(const uint8_t* g, const float* f, const int64_t* dims, const i
   GCUDA(cudaMemsetAsync(err, 0, sizeof(int), stream), "cudaMemsetAsync(status)");
   count_launch();
   crit_count_kernel<<<(unsigned)nblk, kCritThreads, 0, stream>>>(g, D.ncells, blk);
-  count_launch();
-  excl_scan_kernel<int64_t><<<1, kScanThreads, 0, stream>>>(blk, nblk, sums);
+  if (int rc = scan_in_place(P, blk, nblk, sums, stream)) return rc;
   GCUDA(cudaGetLastError(), "critical-cell count launch");
   int64_t h[2] = {0, 0};
   GCUDA(cudaMemcpyAsync(h, sums, sizeof(int64_t), cudaMemcpyDeviceToHost, stream), "read node count");
@@ -376,8 +413,7 @@ int ms_graph_impl(const uint8_t* g, const float* f, const int64_t* dims, const i
     count_launch();
     arc_count_kernel<<<grid_for(n, 128), 128, 0, stream>>>(M, cells, n, bmask, acnt, err);
   }
-  count_launch();
-  excl_scan_kernel<int64_t><<<1, kScanThreads, 0, stream>>>(acnt, n, sums + 1);
+  if (int rc = scan_in_place(P, acnt, n, sums + 1, stream)) return rc;
   GCUDA(cudaGetLastError(), "arc count launch");
   int st = 0;
   GCUDA(cudaMemcpyAsync(h + 1, sums + 1, sizeof(int64_t), cudaMemcpyDeviceToHost, stream), "read arc count");
