@@ -1049,11 +1049,13 @@ template <int K>
 __global__ void __launch_bounds__(128, 7) fixup_end32_kernel(const Adv32 A, const int32_t* __restrict__ lab,
                                                           const uint8_t* __restrict__ state,
                                                           const int64_t* __restrict__ list, int n,
+                                                          const int* __restrict__ n_dev,
                                                           int32_t* __restrict__ endv, int64_t* __restrict__ amb,
                                                           int* __restrict__ n_amb, int amb_mode,
                                                           unsigned long long* __restrict__ work,
                                                           unsigned long long* __restrict__ trips) {
   const VolDims& V = A.V;
+  if (n_dev) n = *n_dev;  // a list whose length the stream wrote before this launch
   int phase = kLaneIdle;
   unsigned long long ntrips = 0;
   int64_t v = 0;
@@ -1151,6 +1153,24 @@ __global__ void __launch_bounds__(128, 7) fixup_end32_kernel(const Adv32 A, cons
       continue;
     }
     endv[v] = (int32_t)end;
+  }
+}
+
+// Every vertex that is not a certain terminal (seed or terminal region): the vertices a
+// fix-up wave can hold, whose streamline ends are computed ahead of the waves.
+__global__ void uncertain_list_kernel(const uint8_t* __restrict__ state, int64_t N, int64_t* __restrict__ list,
+                                      int* __restrict__ n) {
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t v0 = blockIdx.x * (int64_t)blockDim.x; v0 < N; v0 += stride) {
+    const int64_t v = v0 + threadIdx.x;
+    const bool want = v < N && state[v] != kStSeed && state[v] != kStTerminal;
+    const unsigned m = __ballot_sync(kFullMask, want);
+    if (!m) continue;
+    const int lane = threadIdx.x & 31, leader = __ffs(m) - 1;
+    int base = 0;
+    if (lane == leader) base = atomicAdd(n, __popc(m));
+    base = __shfl_sync(kFullMask, base, leader);
+    if (want) list[base + __popc(m & ((1u << lane) - 1u))] = v;
   }
 }
 
@@ -1594,29 +1614,48 @@ cudaError_t launch_fixup_end64(const double* G, const VolDims& V, const IntegPar
   return cudaGetLastError();
 }
 
+cudaError_t launch_uncertain_list(const uint8_t* state, int64_t N, int64_t* list, int* n, int num_sms,
+                                  cudaStream_t stream) {
+  ::msc::count_launch();
+  uncertain_list_kernel<<<grid_for(N, num_sms), 256, 0, stream>>>(state, N, list, n);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_fixup_end32(const float4* G, const VolDims& V, const IntegParams& P, const int32_t* lab,
                                const uint8_t* state, const int64_t* list, int n, int32_t* endv, int64_t* amb,
                                int* n_amb, int amb_mode, unsigned long long* work, unsigned long long* trips,
-                               int num_sms, cudaStream_t stream) {
+                               int num_sms, cudaStream_t stream, const int* n_dev) {
   if (n <= 0) return cudaSuccess;
   const Adv32 A = Adv32::make(G, V, P, nullptr, 0, state);
   const int blocks = (n + 127) / 128;
   if (cudaError_t e = cudaMemsetAsync(work, 0, sizeof(unsigned long long), stream)) return e;
   ::msc::count_launch();
-  const int cap = num_sms * lane_ctas_per_sm();
+  // the ends computed beside the first pass leave it most CTA slots (MSC_EARLY_ENDS_CTAS
+  // per SM, 1-16): at 512^3 both directions' labels took 486 / 500 / 526 / 524 ms with
+  // 2 / 4 / 8 / 16, and 549 ms with the ends integrated per wave
+  static const int early_ctas = [] {
+    const char* e = std::getenv("MSC_EARLY_ENDS_CTAS");
+    const int v = e ? std::atoi(e) : 2;
+    return v >= 1 && v <= 16 ? v : 2;
+  }();
+  const int cap = num_sms * (n_dev ? early_ctas : lane_ctas_per_sm());
   const int grid = blocks < cap ? blocks : cap;
   switch (trips_per_turn()) {
     case 16:
-      fixup_end32_kernel<16><<<grid, 128, 0, stream>>>(A, lab, state, list, n, endv, amb, n_amb, amb_mode, work, trips);
+      fixup_end32_kernel<16><<<grid, 128, 0, stream>>>(A, lab, state, list, n, n_dev, endv, amb, n_amb, amb_mode, work,
+                                                          trips);
       break;
     case 2:
-      fixup_end32_kernel<2><<<grid, 128, 0, stream>>>(A, lab, state, list, n, endv, amb, n_amb, amb_mode, work, trips);
+      fixup_end32_kernel<2><<<grid, 128, 0, stream>>>(A, lab, state, list, n, n_dev, endv, amb, n_amb, amb_mode, work,
+                                                          trips);
       break;
     case 4:
-      fixup_end32_kernel<4><<<grid, 128, 0, stream>>>(A, lab, state, list, n, endv, amb, n_amb, amb_mode, work, trips);
+      fixup_end32_kernel<4><<<grid, 128, 0, stream>>>(A, lab, state, list, n, n_dev, endv, amb, n_amb, amb_mode, work,
+                                                          trips);
       break;
     default:
-      fixup_end32_kernel<8><<<grid, 128, 0, stream>>>(A, lab, state, list, n, endv, amb, n_amb, amb_mode, work, trips);
+      fixup_end32_kernel<8><<<grid, 128, 0, stream>>>(A, lab, state, list, n, n_dev, endv, amb, n_amb, amb_mode, work,
+                                                          trips);
   }
   return cudaGetLastError();
 }

@@ -93,6 +93,12 @@ cudaError_t launch_extremum_info(const float* f, const VolDims& V, int dir, cons
 cudaError_t launch_group_seeds(const int32_t* rep, const int64_t* seed, int n_ext, int32_t* name, int32_t* lab,
                                uint8_t* state, int num_sms, cudaStream_t stream);
 int64_t terminal_num_tiles(const VolDims& V);
+// One round of the certain terminal regions' global frontier walk from the vertices
+// qin[0, *n_in) (n_host: the same count on the host, for the grid); vertices beyond a
+// thread's stack go to qout.
+cudaError_t launch_terminal_walk(const float* f, int32_t* lab, const VolDims& V, int dir, const int64_t* qin,
+                                 const int* n_in, int n_host, int64_t* qout, int* n_out, int cap, int* err,
+                                 int num_sms, cudaStream_t stream);
 cudaError_t launch_terminal_pass(const float* f, int32_t* lab, const VolDims& V, int dir, const uint8_t* dirty_in,
                                  uint8_t* dirty_out, int* changed, int* err, int num_sms, cudaStream_t stream);
 
@@ -191,10 +197,14 @@ cudaError_t launch_boundary_set(const int32_t* lab, const uint8_t* state, const 
 cudaError_t launch_fixup_end64(const double* G, const VolDims& V, const IntegParams& P, const uint8_t* state,
                                const int64_t* list, int n, int32_t* endv, unsigned long long* work,
                                unsigned long long* trips, int num_sms, cudaStream_t stream);
+// n_dev (optional): the list's length in device memory, n then only sizes the grid
 cudaError_t launch_fixup_end32(const float4* G, const VolDims& V, const IntegParams& P, const int32_t* lab,
                                const uint8_t* state, const int64_t* list, int n, int32_t* endv, int64_t* amb,
                                int* n_amb, int amb_mode, unsigned long long* work, unsigned long long* trips,
-                               int num_sms, cudaStream_t stream);
+                               int num_sms, cudaStream_t stream, const int* n_dev = nullptr);
+// the vertices that are not certain terminals (fix-up candidates), appended to list
+cudaError_t launch_uncertain_list(const uint8_t* state, int64_t N, int64_t* list, int* n, int num_sms,
+                                  cudaStream_t stream);
 // Fix-up wave w over `list`: stamps the members in inw, clears their queued bits and
 // lists the members without an end yet in todo (n_todo: a device counter).
 cudaError_t launch_wave_mark(const int64_t* list, int n, int w, int32_t* inw, uint32_t* queued, const int32_t* endv,

@@ -468,6 +468,105 @@ __global__ void __launch_bounds__(BS) terminal_pass_kernel(const float* __restri
   }
 }
 
+// ---- K5b on a global frontier ---------------------------------------------------------
+//
+// A vertex joins a certain terminal region when all its earlier 6-neighbours carry that
+// region's label (InspectPriorRegions), so its label is a function of its earlier
+// neighbours' labels alone and the regions are the unique fixpoint, whatever the
+// order of the inspections.  Here every newly labelled vertex inspects its later
+// 6-neighbours in global memory, depth-first with a short per-thread stack (what does
+// not fit goes to the next round's frontier); the first round starts from the seeds.
+// A vertex that an inspection finds not yet decided is inspected again when its last
+// earlier neighbour gets its label.  The labels are set by compare-and-swap from -1,
+// so every vertex enters a frontier at most once.
+
+// Comparer::Compare(a, b), "a comes before b": value, then index (ascending labels: the
+// lower value; descending: the higher)
+__device__ __forceinline__ bool walk_before(const float* __restrict__ f, int dir, int64_t a, int64_t b) {
+  const float fa = f[a], fb = f[b];
+  if (dir < 0) {
+    if (fb > fa) return true;
+    if (fa > fb) return false;
+    return b > a;
+  }
+  if (fa > fb) return true;
+  if (fb > fa) return false;
+  return a > b;
+}
+
+__global__ void __launch_bounds__(128) terminal_walk_kernel(const float* __restrict__ f, int32_t* __restrict__ lab,
+                                                            const VolDims V, int dir, const int64_t* __restrict__ qin,
+                                                            const int* __restrict__ n_in, int64_t* __restrict__ qout,
+                                                            int* __restrict__ n_out, int cap, int* __restrict__ err) {
+  constexpr int SD = 16;
+  const int n = *n_in;
+  const int64_t X = V.X, XY = V.X * V.Y;
+  const int64_t E[3] = {V.X, V.Y, V.Z};
+  const int64_t S[3] = {1, V.X, XY};
+  volatile int32_t* vl = lab;
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+    int64_t stack[SD];
+    int sp = 0;
+    stack[sp++] = qin[k];
+    while (sp > 0) {
+      const int64_t v = stack[--sp];
+      const uint32_t u32 = (uint32_t)v, x32 = (uint32_t)X, y32 = (uint32_t)V.Y;  // fewer than 2^31 vertices
+      const uint32_t r = u32 / x32;
+      const int64_t vc[3] = {(int64_t)(u32 - r * x32), (int64_t)(r % y32), (int64_t)(r / y32)};
+#pragma unroll
+      for (int a = 0; a < 3; a++) {
+#pragma unroll
+        for (int s = 0; s < 2; s++) {
+          const int64_t wa = vc[a] + (s == 0 ? 1 : -1);
+          if (wa < 0 || wa >= E[a]) continue;
+          const int64_t w = v + (s == 0 ? S[a] : -S[a]);
+          if (vl[w] != -1 || !walk_before(f, dir, v, w)) continue;
+          // InspectPriorRegions of w (gi_extrema_region_builder.h:806-857)
+          int64_t wc[3] = {vc[0], vc[1], vc[2]};
+          wc[a] = wa;
+          int32_t l = -1;
+          bool ok = true;
+#pragma unroll
+          for (int b = 0; b < 3 && ok; b++) {
+#pragma unroll
+            for (int t = 0; t < 2; t++) {
+              const int64_t ua = wc[b] + (t == 0 ? 1 : -1);
+              if (ua < 0 || ua >= E[b]) continue;
+              const int64_t u = w + (t == 0 ? S[b] : -S[b]);
+              if (!walk_before(f, dir, u, w)) continue;
+              const int32_t lu = vl[u];
+              if (lu < 0 || (l >= 0 && lu != l)) {
+                ok = false;
+                break;
+              }
+              l = lu;
+            }
+          }
+          if (!ok || l < 0) continue;
+          if (atomicCAS(&lab[w], -1, l) != -1) continue;
+          if (sp < SD) {
+            stack[sp++] = w;
+          } else {
+            const int slot = atomicAdd(n_out, 1);
+            if (slot < cap) qout[slot] = w; else atomicOr(err, kErrLocalQueue);
+          }
+        }
+      }
+    }
+  }
+}
+
+cudaError_t launch_terminal_walk(const float* f, int32_t* lab, const VolDims& V, int dir, const int64_t* qin,
+                                 const int* n_in, int n_host, int64_t* qout, int* n_out, int cap, int* err,
+                                 int num_sms, cudaStream_t stream) {
+  if (n_host <= 0) return cudaSuccess;
+  const int blocks = (n_host + 127) / 128;
+  const int grid = blocks < num_sms * 16 ? blocks : num_sms * 16;
+  ::msc::count_launch();
+  terminal_walk_kernel<<<grid, 128, 0, stream>>>(f, lab, V, dir, qin, n_in, qout, n_out, cap, err);
+  return cudaGetLastError();
+}
+
 namespace {
 constexpr int kVTX = 32, kVTY = 16, kVTZ = 8, kVBS = 512;
 using VB = VBox<kVTX, kVTY, kVTZ>;

@@ -287,13 +287,22 @@ struct LabelCtx {
   uint8_t* tiles = nullptr;
   int* counters = nullptr;  // [0] n_ext [1] n_sad [2] n_arcs [3] changed [4] err [5] n_list / wave members
                             // without an end [6] n_next [7] n_amb [8, 10) cleaner [10] long chain
+                            // [12] vertices whose ends are computed ahead of the waves
+                            // [13], [14] terminal-walk frontier lengths
   unsigned long long* work = nullptr;  // [0] claimed fix-up items, [48, 51) advection iterations (first
                                        // pass, FP32, FP64), [56] FP64 claims
   void* hpin = nullptr;                // kPinnedBytes of pinned host memory (pinned_get)
+  // the streamline ends computed ahead of the fix-up waves, beside the first pass
+  cudaStream_t ends_st = nullptr;
+  cudaEvent_t ends_go = nullptr, ends_done = nullptr;
   explicit LabelCtx(cudaStream_t s) : st(s), pool(s) {}
   ~LabelCtx() {
+    if (ends_st) cudaStreamSynchronize(ends_st);
     cudaStreamSynchronize(st);  // no copy into hpin in flight
     pinned_put(hpin);
+    if (ends_go) cudaEventDestroy(ends_go);
+    if (ends_done) cudaEventDestroy(ends_done);
+    if (ends_st) cudaStreamDestroy(ends_st);
   }
   LabelCtx(const LabelCtx&) = delete;
   LabelCtx& operator=(const LabelCtx&) = delete;
@@ -320,6 +329,7 @@ struct DirLabels {
   uint8_t* state = nullptr;
   int64_t* seed = nullptr;
   int n_ext = 0;
+  bool seeds_zeroed = false;  // the gradient at this direction's seeds is zero on the stream
 };
 
 int setup_ctx(LabelCtx& c, const float* f, const uint8_t* grad, const int64_t* dims, const msc_integ_params* p) {
@@ -366,6 +376,14 @@ int setup_ctx(LabelCtx& c, const float* f, const uint8_t* grad, const int64_t* d
 
 // Extremum graph, merge, seeds and certain terminal regions of one direction; leaves
 // d.lab (terminal labels, -1 elsewhere) and d.state.
+bool terminal_tiles_on() {
+  static const bool on = [] {
+    const char* e = std::getenv("MSC_TERMINAL_TILES");
+    return e && std::atoi(e) == 1;
+  }();
+  return on;
+}
+
 int prepare_direction(LabelCtx& c, DirLabels& d, int32_t* stage_terminal) {
   const int64_t N = c.N;
   const msc::VolDims& V = c.V;
@@ -472,7 +490,29 @@ int prepare_direction(LabelCtx& c, DirLabels& d, int32_t* stage_terminal) {
 
   if (d.before_terminal)
     if (int rc = d.before_terminal()) return rc;
-  // certain terminal regions: tile passes to the fixpoint
+  // certain terminal regions: a global frontier walk from the seeds to the fixpoint
+  // (MSC_TERMINAL_TILES=1: tile passes instead)
+  if (!terminal_tiles_on()) {
+    int64_t* cur = c.list_a;
+    int64_t* nxt = c.list_b;
+    LCUDA(cudaMemcpyAsync(cur, d.seed, (size_t)n_ext * sizeof(int64_t), cudaMemcpyDeviceToDevice, st), "copy");
+    int n = n_ext;
+    std::memcpy(c.hpin, &n, sizeof(int));
+    LCUDA(cudaMemcpyAsync(c.counters + 13, c.hpin, sizeof(int), cudaMemcpyHostToDevice, st), "write count");
+    int* n_cur = c.counters + 13;
+    int* n_nxt = c.counters + 14;
+    int rounds = 0;
+    while (n > 0) {
+      if (rounds++ > N) return fail(MSC_ERR_ITER_LIMIT, "terminal regions did not converge");
+      LCUDA(cudaMemsetAsync(n_nxt, 0, sizeof(int), st), "memset");
+      LCUDA(msc::launch_terminal_walk(c.f, d.lab, V, dir, cur, n_cur, n, nxt, n_nxt, (int)N, c.counters + 4, c.sms, st),
+            "regions");
+      if (int rc = read_dev(c, n_nxt, 1, &n)) return rc;
+      std::swap(cur, nxt);
+      std::swap(n_cur, n_nxt);
+    }
+    trace_mark(st, dir, "terminal walk x" + std::to_string(rounds));
+  } else {
   const uint8_t* din = nullptr;
   uint8_t* dout = c.tiles;
   for (int64_t passes = 0;; passes++) {
@@ -489,6 +529,7 @@ int prepare_direction(LabelCtx& c, DirLabels& d, int32_t* stage_terminal) {
     if (passes > c.ntiles + 2) return fail(MSC_ERR_ITER_LIMIT, "terminal regions did not converge");
     din = dout;
     dout = (dout == c.tiles) ? c.tiles + c.ntiles : c.tiles;
+  }
   }
   if (stage_terminal) {
     ::msc::count_launch();
@@ -525,9 +566,10 @@ msc::IntegParams integ_params(const msc_integ_params* p, int dir) {
 int first_pass(LabelCtx& c, DirLabels& d) {
   const int64_t N = c.N;
   cudaStream_t st = c.st;
-  if (d.n_ext > 0) {
+  if (d.n_ext > 0 && !d.seeds_zeroed) {
     ::msc::count_launch();
     zero_seed_grad_kernel<<<(d.n_ext + 255) / 256, 256, 0, st>>>(d.seed, d.n_ext, c.g32, c.g64);
+    d.seeds_zeroed = true;
   }
   const msc::IntegParams P = integ_params(c.p, d.dir);
   msc::SpreadOrder S{};
@@ -667,7 +709,14 @@ int first_pass(LabelCtx& c, DirLabels& d) {
 
 // Boundary fix-up of the vertices still marked unassigned in d.state, then the
 // cleaner; `out` receives the final labels.
-int finish_direction(LabelCtx& c, DirLabels& d, int32_t* out, int32_t* stage_integrated, int64_t stats[2]) {
+struct EarlyEnds {
+  bool on = false;
+  int32_t* endv = nullptr;
+  int64_t* list = nullptr;
+};
+
+int finish_direction(LabelCtx& c, DirLabels& d, int32_t* out, int32_t* stage_integrated, int64_t stats[2],
+                     const EarlyEnds* early = nullptr) {
   const int64_t N = c.N;
   const msc::VolDims& V = c.V;
   cudaStream_t st = c.st;
@@ -683,11 +732,27 @@ int finish_direction(LabelCtx& c, DirLabels& d, int32_t* out, int32_t* stage_int
   // once.
   int32_t *endv, *inw, *rptr, *rval, *rfin;
   LCUDA(c.pool.get(&rfin, N), "alloc");
-  LCUDA(c.pool.get(&endv, N), "alloc");
   LCUDA(c.pool.get(&inw, N), "alloc");
   LCUDA(c.pool.get(&rptr, N), "alloc");
   LCUDA(c.pool.get(&rval, N), "alloc");
-  LCUDA(cudaMemsetAsync(endv, 0xFF, N * sizeof(int32_t), st), "memset");
+  int64_t early_n = 0, early_amb = 0;
+  if (early) {
+    // the ends computed beside the first pass, and in FP64 those whose FP32 ending was
+    // ambiguous
+    endv = early->endv;
+    LCUDA(cudaStreamWaitEvent(st, c.ends_done, 0), "cudaStreamWaitEvent");
+    int h[2] = {0, 0};
+    if (int rc = read_dev(c, c.counters + 7, 1, &h[0])) return rc;
+    if (int rc = read_dev(c, c.counters + 12, 1, &h[1])) return rc;
+    trace_mark(st, d.dir, "ends of " + std::to_string(h[1]) + " (FP64 " + std::to_string(h[0]) + ")");
+    LCUDA(msc::launch_fixup_end64(c.g64, V, P, d.state, c.amb, h[0], endv, c.work + 56, c.work + 50, sms, st),
+          "fix-up FP64");
+    early_amb = h[0];
+    early_n = h[1];
+  } else {
+    LCUDA(c.pool.get(&endv, N), "alloc");
+    LCUDA(cudaMemsetAsync(endv, 0xFF, N * sizeof(int32_t), st), "memset");
+  }
   LCUDA(cudaMemsetAsync(inw, 0xFF, N * sizeof(int32_t), st), "memset");
   LCUDA(cudaMemsetAsync(c.queued, 0, (N / 32 + 1) * sizeof(uint32_t), st), "memset");
   LCUDA(cudaMemsetAsync(c.counters + 5, 0, 3 * sizeof(int), st), "memset");
@@ -699,7 +764,8 @@ int finish_direction(LabelCtx& c, DirLabels& d, int32_t* out, int32_t* stage_int
   int64_t* cur = c.list_a;
   int64_t* nxt = c.list_b;
   int64_t* todo = c.list_c;
-  stats[0] = stats[1] = 0;
+  stats[0] = early_n;
+  stats[1] = early_amb;
   for (int w = 0; n_list > 0; w++) {
     if (w > 2 * N + 2) return fail(MSC_ERR_ITER_LIMIT, "fix-up did not converge");
     // counters: [5] todo, [6] next wave, [7] ambiguous
@@ -764,9 +830,61 @@ int finish_direction(LabelCtx& c, DirLabels& d, int32_t* out, int32_t* stage_int
   return MSC_OK;
 }
 
+// Every fix-up streamline ends where it reaches a certain terminal region (or stops),
+// whatever the labels, and the certain terminals are known before the first pass.  So
+// the ends of all the vertices a wave can hold -- those that are not certain terminals
+// -- are computed in one launch on a stream of their own while the first pass runs:
+// the waves then only decide.  A wave that integrated its own members would end with
+// the slowest of its streamlines, ten waves and more per direction; one launch over
+// all of them keeps only the one longest streamline in the tail, and the launch fills
+// the gaps the first pass leaves (its resolution rounds are small launches between
+// host reads).  The extra ends (vertices no wave takes) cost about a fifth more
+// integration.  MSC_EARLY_ENDS=0 integrates per wave instead.
+bool early_ends_on() {
+  static const bool on = [] {
+    const char* e = std::getenv("MSC_EARLY_ENDS");
+    return !(e && std::atoi(e) == 0);
+  }();
+  return on;
+}
+
+int start_early_ends(LabelCtx& c, DirLabels& d, EarlyEnds& e) {
+  const int64_t N = c.N;
+  cudaStream_t st = c.st;
+  LCUDA(c.pool.get(&e.endv, N), "alloc");
+  LCUDA(c.pool.get(&e.list, N), "alloc");
+  LCUDA(cudaMemsetAsync(e.endv, 0xFF, N * sizeof(int32_t), st), "memset");
+  LCUDA(cudaMemsetAsync(c.counters + 12, 0, sizeof(int), st), "memset");
+  LCUDA(cudaMemsetAsync(c.counters + 7, 0, sizeof(int), st), "memset");
+  // the streamlines see the gradient the first pass sees: zero at this direction's seeds
+  if (d.n_ext > 0 && !d.seeds_zeroed) {
+    ::msc::count_launch();
+    zero_seed_grad_kernel<<<(d.n_ext + 255) / 256, 256, 0, st>>>(d.seed, d.n_ext, c.g32, c.g64);
+    d.seeds_zeroed = true;
+  }
+  if (!c.ends_st) {
+    LCUDA(cudaStreamCreateWithFlags(&c.ends_st, cudaStreamNonBlocking), "cudaStreamCreate");
+    LCUDA(cudaEventCreateWithFlags(&c.ends_go, cudaEventDisableTiming), "cudaEventCreate");
+    LCUDA(cudaEventCreateWithFlags(&c.ends_done, cudaEventDisableTiming), "cudaEventCreate");
+  }
+  LCUDA(cudaEventRecord(c.ends_go, st), "cudaEventRecord");
+  LCUDA(cudaStreamWaitEvent(c.ends_st, c.ends_go, 0), "cudaStreamWaitEvent");
+  const msc::IntegParams P = integ_params(c.p, d.dir);
+  LCUDA(msc::launch_uncertain_list(d.state, N, e.list, c.counters + 12, c.sms, c.ends_st), "fix-up candidates");
+  LCUDA(msc::launch_fixup_end32(c.g32, c.V, P, d.lab, d.state, e.list, (int)N, e.endv, c.amb, c.counters + 7,
+                                c.p->precision == 2 ? 2 : 0, c.work, c.work + 49, c.sms, c.ends_st, c.counters + 12),
+        "fix-up ends");
+  LCUDA(cudaEventRecord(c.ends_done, c.ends_st), "cudaEventRecord");
+  e.on = true;
+  return MSC_OK;
+}
+
 int integrate_direction(LabelCtx& c, DirLabels& d, int32_t* out, int32_t* stage_integrated, int64_t stats[2]) {
+  EarlyEnds e;
+  if (early_ends_on() && (c.p->precision == 0 || c.p->precision == 2))
+    if (int rc = start_early_ends(c, d, e)) return rc;
   if (int rc = first_pass(c, d)) return rc;
-  return finish_direction(c, d, out, stage_integrated, stats);
+  return finish_direction(c, d, out, stage_integrated, stats, e.on ? &e : nullptr);
 }
 
 int finish_errors(LabelCtx& c) {
