@@ -657,19 +657,21 @@ __device__ __forceinline__ void mark_dirty(bool want, uint32_t v, uint32_t* __re
 // whose bit is set, a bit per item from k0).  A changed item marks the path vertices
 // between its old and new extent in nxt: their claims are recomputed next round.
 __global__ void spec_check_kernel(const SpecSet Q, int64_t k0, int64_t k1, const uint32_t* __restrict__ claim,
-                                  const uint32_t* __restrict__ ibits, uint32_t* __restrict__ nxt,
+                                  const uint32_t* __restrict__ ibits, const uint32_t* __restrict__ ilist,
+                                  const unsigned long long* __restrict__ n_ilist, uint32_t* __restrict__ nxt,
                                   uint32_t* __restrict__ nxt_list, unsigned long long* __restrict__ n_nxt) {
-  const int64_t span = k1 - k0;
+  // the items: every one of the batch, or those listed in ilist (a later round)
+  const int64_t span = ilist ? (int64_t)*n_ilist : k1 - k0;
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
   // every lane of a warp runs the same number of loop trips (mark_dirty is warp-wide);
   // a warp's 32 items share one word of ibits
   for (int64_t t0 = blockIdx.x * (int64_t)blockDim.x; t0 < span; t0 += stride) {
-    const int64_t t = t0 + threadIdx.x;
+    const bool have = t0 + threadIdx.x < span;
+    const int64_t t = ilist ? (have ? (int64_t)ilist[t0 + threadIdx.x] : 0) : t0 + threadIdx.x;
     const int64_t k = k0 + t;
-    const bool have = t < span;
     const int n = have ? Q.len[k] : 0;
     bool look = n > 0;
-    if (ibits) look = look && ((ibits[t >> 5] >> (t & 31)) & 1u);
+    if (ibits && !ilist) look = look && ((ibits[t >> 5] >> (t & 31)) & 1u);
     uint8_t oa = 0, na = 0;
     int oc = -1, nc = -1;
     bool changed = false;
@@ -735,6 +737,35 @@ __global__ void spec_holders_kernel(const SpecSet Q, int64_t k0, const uint32_t*
     for (int32_t h = Q.hhead[list[i]]; h >= 0; h = Q.hnext[h]) {
       const int64_t t = Q.hitem[h] - k0;
       atomicOr(&ibits[t >> 5], 1u << (t & 31));
+    }
+  }
+}
+
+// The items whose bit is set in ibits (a later round's items), as a list: a thread per
+// bitmap word, one append per warp.
+__global__ void spec_bits_list_kernel(const uint32_t* __restrict__ ibits, int64_t words, uint32_t* __restrict__ list,
+                                      unsigned long long* __restrict__ n) {
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  const int lane = threadIdx.x & 31;
+  for (int64_t w0 = blockIdx.x * (int64_t)blockDim.x; w0 < words; w0 += stride) {
+    const int64_t w = w0 + threadIdx.x;
+    uint32_t m = w < words ? ibits[w] : 0u;
+    const unsigned c = __popc(m);
+    unsigned incl = c;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const unsigned y = __shfl_up_sync(kFullMask, incl, o);
+      if (lane >= o) incl += y;
+    }
+    const unsigned total = __shfl_sync(kFullMask, incl, 31);
+    if (!total) continue;
+    unsigned long long base = 0;
+    if (lane == 31) base = atomicAdd(n, (unsigned long long)total);
+    base = __shfl_sync(kFullMask, base, 31) + (incl - c);
+    while (m) {
+      const int b = __ffs(m) - 1;
+      m &= m - 1;
+      list[base++] = (uint32_t)(w * 32 + b);
     }
   }
 }
@@ -1526,21 +1557,28 @@ cudaError_t launch_speculate(const float4* G, const VolDims& V, const IntegParam
 }
 
 cudaError_t launch_spec_round(const SpecSet& Q, int64_t k0, int64_t k1, uint32_t* claim, const SpecDirty* cur,
-                              const SpecDirty& nxt, uint32_t* ibits, int64_t ibits_words, int num_sms,
-                              cudaStream_t stream) {
+                              const SpecDirty& nxt, uint32_t* ibits, int64_t ibits_words, uint32_t* ilist,
+                              unsigned long long* n_ilist, int num_sms, cudaStream_t stream) {
   if (cudaError_t e = cudaMemsetAsync(nxt.n, 0, sizeof(unsigned long long), stream)) return e;
   if (cudaError_t e = cudaMemsetAsync(nxt.bits, 0, nxt.words * sizeof(uint32_t), stream)) return e;
-  // the first round's claims were made by the speculation
-  if (cur) {
-    if (cudaError_t e = cudaMemsetAsync(ibits, 0, ibits_words * sizeof(uint32_t), stream)) return e;
+  // the first round's claims were made by the speculation, and it looks at every item
+  if (!cur) {
     ::msc::count_launch();
-    spec_reclaim_kernel<<<num_sms * 8, 256, 0, stream>>>(Q, cur->list, cur->n, claim);
-    ::msc::count_launch();
-    spec_holders_kernel<<<num_sms * 8, 256, 0, stream>>>(Q, k0, cur->list, cur->n, ibits);
+    spec_check_kernel<<<grid_for(k1 - k0, num_sms), 256, 0, stream>>>(Q, k0, k1, claim, nullptr, nullptr, nullptr,
+                                                                      nxt.bits, nxt.list, nxt.n);
+    return cudaGetLastError();
   }
+  if (cudaError_t e = cudaMemsetAsync(ibits, 0, ibits_words * sizeof(uint32_t), stream)) return e;
+  if (cudaError_t e = cudaMemsetAsync(n_ilist, 0, sizeof(unsigned long long), stream)) return e;
   ::msc::count_launch();
-  spec_check_kernel<<<grid_for(k1 - k0, num_sms), 256, 0, stream>>>(Q, k0, k1, claim, cur ? ibits : nullptr,
-                                                                    nxt.bits, nxt.list, nxt.n);
+  spec_reclaim_kernel<<<num_sms * 8, 256, 0, stream>>>(Q, cur->list, cur->n, claim);
+  ::msc::count_launch();
+  spec_holders_kernel<<<num_sms * 8, 256, 0, stream>>>(Q, k0, cur->list, cur->n, ibits);
+  ::msc::count_launch();
+  spec_bits_list_kernel<<<grid_for(ibits_words, num_sms), 256, 0, stream>>>(ibits, ibits_words, ilist, n_ilist);
+  ::msc::count_launch();
+  spec_check_kernel<<<num_sms * 8, 256, 0, stream>>>(Q, k0, k1, claim, ibits, ilist, n_ilist, nxt.bits, nxt.list,
+                                                     nxt.n);
   return cudaGetLastError();
 }
 

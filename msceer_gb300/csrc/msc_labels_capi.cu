@@ -589,7 +589,7 @@ int first_pass(LabelCtx& c, DirLabels& d) {
   int32_t* vtx;
   uint32_t* ibits;
   unsigned long long* sc;  // [0] pool cursor [1] items [3] claimed items [4, 6) dirty-list lengths
-                           // [6] holder-node cursor
+                           // [6] holder-node cursor [7] a round's listed items
   msc::SpecSet Q{};
   const int64_t max_items = std::min<int64_t>(N, S.offset[S.nlev]);
   const int64_t ibits_cap = max_items / 32 + 1;
@@ -612,7 +612,9 @@ int first_pass(LabelCtx& c, DirLabels& d) {
   LCUDA(c.pool.get(&Q.hidx, Q.node_cap), "alloc");
   LCUDA(c.pool.get(&Q.hnext, Q.node_cap), "alloc");
   LCUDA(c.pool.get(&ibits, ibits_cap), "alloc");
-  LCUDA(c.pool.get(&sc, 7), "alloc");
+  uint32_t* ilist;
+  LCUDA(c.pool.get(&ilist, max_items + 32), "alloc");
+  LCUDA(c.pool.get(&sc, 8), "alloc");
   LCUDA(c.pool.get(&Q.overflow, 1), "alloc");
   msc::SpecDirty dirty[2];
   for (int q = 0; q < 2; q++) {
@@ -675,16 +677,20 @@ int first_pass(LabelCtx& c, DirLabels& d) {
       }
       trace_mark(st, d.dir, "  speculated " + std::to_string(k1 - k0));
       // resolution rounds: the first looks at every item, a later one at the items that
-      // hold a vertex whose claim may have changed; they end when a round changes no claim
-      for (int64_t r = 0;; r++) {
-        if (r > k1 - k0 + 2) return fail(MSC_ERR_ITER_LIMIT, "first-pass resolution did not converge");
-        LCUDA(msc::launch_spec_round(Q, k0, k1, claim, r == 0 ? nullptr : &dirty[r & 1], dirty[(r + 1) & 1], ibits,
-                                     (k1 - k0) / 32 + 1, c.sms, st),
-              "resolve");
+      // hold a vertex whose claim may have changed; they end when a round changes no
+      // claim.  After the first two, rounds go in groups of four between counter reads
+      // (a round after the last one finds nothing to do).
+      for (int64_t r = 0;;) {
+        if (r > k1 - k0 + 8) return fail(MSC_ERR_ITER_LIMIT, "first-pass resolution did not converge");
+        const int group = r < 2 ? 1 : 4;
+        for (int q = 0; q < group; q++, r++)
+          LCUDA(msc::launch_spec_round(Q, k0, k1, claim, r == 0 ? nullptr : &dirty[r & 1], dirty[(r + 1) & 1], ibits,
+                                       (k1 - k0) / 32 + 1, ilist, sc + 7, c.sms, st),
+                "resolve");
         unsigned long long nd = 0;
-        if (int rc = read_dev(c, dirty[(r + 1) & 1].n, 1, &nd)) return rc;
-        rounds_total++;
-        if (r == 0) trace_mark(st, d.dir, "  round 1: " + std::to_string(nd) + " dirty");
+        if (int rc = read_dev(c, dirty[r & 1].n, 1, &nd)) return rc;
+        rounds_total += group;
+        if (r == 1) trace_mark(st, d.dir, "  round 1: " + std::to_string(nd) + " dirty");
         if (nd == 0) break;
       }
       trace_mark(st, d.dir, "  resolved");
