@@ -344,6 +344,14 @@ def grad_kernels(V, C, t_pairs, t_ldir, nlaunch, reps, n, peak, peak_kind):
                 "frac": kd["gbs"] / peak, "peak_kind": f"{peak_kind} hbm_gbs", "traffic": TRAFFIC_PER_LAUNCH.get((dom, n)),
                 "scope": "dominant kernel of the .grad; the label integration that dominates the full step is "
                          "FP32/FP64 issue-bound, neither HBM nor tensor bound"}
+    # the bound these kernels actually meet: instruction issue (per-unit counts from ncu)
+    per, unit = WARP_INST_PER_UNIT[dom]
+    units = V if unit == "vertex" else C
+    t = kd.get("ms_per_launch", kd.get("ms_per_stage")) * 1e-3
+    issue_peak = SMS * SCHEDULERS_PER_SM * SM_MAX_MHZ * 1e6
+    roofline["issue"] = {"warp_inst_per_" + unit: per, "achieved_warp_inst_per_s": per * units / t,
+                         "peak_warp_inst_per_s": issue_peak, "frac": per * units / t / issue_peak,
+                         "source": "smsp__inst_executed.sum of the 256^3 ncu capture x units / CUDA-event time"}
     return kernels, roofline
 
 
@@ -664,18 +672,29 @@ def run_ours(args, ws, rank, local):
         pg.destroy_process_group()
 
 
-# dram__bytes_read.sum + dram__bytes_write.sum per launch from the committed ncu
-# summaries under profiles/ (None until captured)
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per launch from one ncu
-# --set full capture of the kernels at 256^3 (f and .grad together 201 MB, above the
+# --set full capture of each kernel at 256^3 (f and .grad together 201 MB, above the
 # L2), scaled to 512^3 by the vertex count (x 8): the traffic grows with the volume.
-# ldir_stage = tile + check kernels (the walk's share is below 3% of the stage's time).
+# ldir_stage = tile + check kernels (the walk is below 5% of the stage's time).
+_T_LSTAR = 67.342e6 + 78.792e6
+_T_LDIR = 133.928e6 + 96.585e6 + 147.920e6 + 9.383e6
 TRAFFIC_PER_LAUNCH: dict = {
-    ("lstar_kernel", 256): 67.168e6 + 78.372e6,
-    ("ldir_stage", 256): 158.404e6 + 159.985e6 + 224.759e6 + 12.212e6,
-    ("lstar_kernel", 512): (67.168e6 + 78.372e6) * 8,
-    ("ldir_stage", 512): (158.404e6 + 159.985e6 + 224.759e6 + 12.212e6) * 8,
+    ("lstar_kernel", 256): _T_LSTAR,
+    ("ldir_stage", 256): _T_LDIR,
+    ("lstar_kernel", 512): _T_LSTAR * 8,
+    ("ldir_stage", 512): _T_LDIR * 8,
 }
+# Warp instructions per unit from the same captures (smsp__inst_executed.sum): the .grad
+# kernels are integer-issue bound, so their ceiling is the SMs' issue rate (152 SMs x 4
+# schedulers x clock), not HBM.  lstar_kernel: 1.320 G per 256^3 launch (per vertex);
+# ldir stage: tile 1.806 G + check 0.111 G per 256^3 (per cell).
+WARP_INST_PER_UNIT: dict = {
+    "lstar_kernel": (1.320036e9 / 256 ** 3, "vertex"),
+    "ldir_stage": ((1.805696e9 + 0.110793e9) / 511 ** 3, "cell"),
+}
+SCHEDULERS_PER_SM = 4
+SMS = 152
+
 # FP32 operations of one adaptive-Euler iteration as the reference's advector states
 # it: two trilinear interpolations in the (1 - t) a + t b form (2 x 73), |g| (6), the
 # step clamp (2), the full and two half steps with the error test and the move (29).

@@ -274,37 +274,58 @@ __device__ int trace_node(const MsMesh& M, const int64_t* __restrict__ node_cell
   return 0;
 }
 
-__global__ void arc_count_kernel(const MsMesh M, const int64_t* __restrict__ node_cell, int64_t n, int build,
+// The nodes whose arcs are traced (dimension d >= 1 with build bit d - 1), listed so
+// that the tracing threads of a warp all trace (in cell order a warp's nodes mix all
+// four dimensions, and minima and unbuilt dimensions left most lanes idle).
+__global__ void traced_list_kernel(const MsMesh M, const int64_t* __restrict__ node_cell, int64_t n, int build,
+                                   int32_t* __restrict__ list, unsigned long long* __restrict__ n_list) {
+  const int lane = threadIdx.x & 31;
+  for (int64_t i0 = blockIdx.x * (int64_t)blockDim.x; i0 < n; i0 += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i = i0 + threadIdx.x;
+    bool want = false;
+    if (i < n) {
+      int64_t c[3];
+      coords(M, node_cell[i], c);
+      const int d = dim_of(c);
+      want = d > 0 && ((build >> (d - 1)) & 1);
+    }
+    const unsigned m = __ballot_sync(0xffffffffu, want);
+    if (!m) continue;
+    const int leader = __ffs(m) - 1;
+    unsigned long long base = 0;
+    if (lane == leader) base = atomicAdd(n_list, (unsigned long long)__popc(m));
+    base = __shfl_sync(0xffffffffu, base, leader);
+    if (want) list[base + __popc(m & ((1u << lane) - 1u))] = (int32_t)i;
+  }
+}
+
+__global__ void arc_count_kernel(const MsMesh M, const int64_t* __restrict__ node_cell, int64_t n,
+                                 const int32_t* __restrict__ list, const unsigned long long* __restrict__ n_list,
                                  int64_t* __restrict__ counts, int* __restrict__ err) {
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-    int64_t c[3];
-    coords(M, node_cell[i], c);
-    const int d = dim_of(c);
+  const int64_t nl = (int64_t)*n_list;
+  for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < nl; j += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i = list[j];
     int64_t k = 0;
-    if (d > 0 && ((build >> (d - 1)) & 1)) {
-      const int e = trace_node<false>(M, node_cell, n, i, &k, 0, nullptr, nullptr, nullptr, nullptr);
-      if (e) {
-        atomicOr(err, e);
-        k = 0;
-      }
+    const int e = trace_node<false>(M, node_cell, n, i, &k, 0, nullptr, nullptr, nullptr, nullptr);
+    if (e) {
+      atomicOr(err, e);
+      k = 0;
     }
     counts[i] = k;
   }
 }
 
-__global__ void arc_write_kernel(const MsMesh M, const int64_t* __restrict__ node_cell, int64_t n, int build,
+__global__ void arc_write_kernel(const MsMesh M, const int64_t* __restrict__ node_cell, int64_t n,
+                                 const int32_t* __restrict__ list, const unsigned long long* __restrict__ n_list,
                                  const int64_t* __restrict__ offsets, const float* __restrict__ value,
                                  int32_t* __restrict__ lower, int32_t* __restrict__ upper, float* __restrict__ pers,
                                  int* __restrict__ err) {
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-    int64_t c[3];
-    coords(M, node_cell[i], c);
-    const int d = dim_of(c);
+  const int64_t nl = (int64_t)*n_list;
+  for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < nl; j += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i = list[j];
     int64_t k = 0;
-    if (d > 0 && ((build >> (d - 1)) & 1)) {
-      const int e = trace_node<true>(M, node_cell, n, i, &k, offsets[i], value, lower, upper, pers);
-      if (e) atomicOr(err, e);
-    }
+    const int e = trace_node<true>(M, node_cell, n, i, &k, offsets[i], value, lower, upper, pers);
+    if (e) atomicOr(err, e);
   }
 }
 
@@ -408,10 +429,18 @@ int ms_graph_impl(const uint8_t* g, const float* f, const int64_t* dims, const i
   count_launch();
   crit_write_kernel<<<(unsigned)nblk, kCritThreads, 0, stream>>>(g, D.ncells, blk, cells);
   int64_t* acnt = nullptr;
+  int32_t* tlist = nullptr;
+  unsigned long long* n_tlist = nullptr;
   GCUDA(P.get((void**)&acnt, (size_t)n * sizeof(int64_t)), "scratch alloc(arc counts)");
+  GCUDA(P.get((void**)&tlist, (size_t)n * sizeof(int32_t)), "scratch alloc(traced nodes)");
+  GCUDA(P.get((void**)&n_tlist, sizeof(unsigned long long)), "scratch alloc(traced count)");
+  GCUDA(cudaMemsetAsync(acnt, 0, (size_t)n * sizeof(int64_t), stream), "cudaMemsetAsync(arc counts)");
+  GCUDA(cudaMemsetAsync(n_tlist, 0, sizeof(unsigned long long), stream), "cudaMemsetAsync(traced count)");
   if (n > 0) {
     count_launch();
-    arc_count_kernel<<<grid_for(n, 128), 128, 0, stream>>>(M, cells, n, bmask, acnt, err);
+    traced_list_kernel<<<grid_for(n, 256), 256, 0, stream>>>(M, cells, n, bmask, tlist, n_tlist);
+    count_launch();
+    arc_count_kernel<<<grid_for(n, 128), 128, 0, stream>>>(M, cells, n, tlist, n_tlist, acnt, err);
   }
   if (int rc = scan_in_place(P, acnt, n, sums + 1, stream)) return rc;
   GCUDA(cudaGetLastError(), "arc count launch");
@@ -439,8 +468,8 @@ int ms_graph_impl(const uint8_t* g, const float* f, const int64_t* dims, const i
   }
   if (arcs_out && n > 0) {
     count_launch();
-    arc_write_kernel<<<grid_for(n, 128), 128, 0, stream>>>(M, cells, n, bmask, acnt, vals, arc_lower, arc_upper,
-                                                           arc_pers, err);
+    arc_write_kernel<<<grid_for(n, 128), 128, 0, stream>>>(M, cells, n, tlist, n_tlist, acnt, vals, arc_lower,
+                                                           arc_upper, arc_pers, err);
   }
   GCUDA(cudaGetLastError(), "node / arc write launch");
   GCUDA(cudaMemcpyAsync(&st, err, sizeof(int), cudaMemcpyDeviceToHost, stream), "read status");
