@@ -1011,10 +1011,11 @@ __global__ void boundary_set_kernel(const int32_t* __restrict__ lab, const uint8
 // labels, so where a vertex's streamline ends does not depend on the wave order.
 template <int K>
 __global__ void __launch_bounds__(32) fixup_end64_kernel(const Adv64 A, const int64_t* __restrict__ list, int n,
-                                                         int32_t* __restrict__ endv,
+                                                         const int* __restrict__ n_dev, int32_t* __restrict__ endv,
                                                          unsigned long long* __restrict__ work,
                                                          unsigned long long* __restrict__ trips) {
   const VolDims& V = A.V;
+  if (n_dev) n = *n_dev;  // a list whose length the stream wrote before this launch
   int phase = kLaneIdle;
   unsigned long long ntrips = 0;
   int64_t v = 0;
@@ -1623,7 +1624,7 @@ cudaError_t launch_boundary_set(const int32_t* lab, const uint8_t* state, const 
 
 cudaError_t launch_fixup_end64(const double* G, const VolDims& V, const IntegParams& P, const uint8_t* state,
                                const int64_t* list, int n, int32_t* endv, unsigned long long* work,
-                               unsigned long long* trips, int num_sms, cudaStream_t stream) {
+                               unsigned long long* trips, int num_sms, cudaStream_t stream, const int* n_dev) {
   if (n <= 0) return cudaSuccess;
   Adv64 A{G, V, P, state};
   const int blocks = (n + 31) / 32;
@@ -1635,19 +1636,19 @@ cudaError_t launch_fixup_end64(const double* G, const VolDims& V, const IntegPar
   // as many SMs as it has warps, and a large one keeps a few items per lane
   // iterations per turn: MSC_TRIPS_PER_TURN_FP64 (2, 4, 8 or 16) overrides the default
   static const int k = trips_env("MSC_TRIPS_PER_TURN_FP64", 2);
-  const int grid = blocks < num_sms * 4 ? blocks : num_sms * 4;
+  const int grid = (blocks < num_sms * 4 && !n_dev) ? blocks : num_sms * 4;
   switch (k) {
     case 4:
-      fixup_end64_kernel<4><<<grid, 32, 0, stream>>>(A, list, n, endv, work, trips);
+      fixup_end64_kernel<4><<<grid, 32, 0, stream>>>(A, list, n, n_dev, endv, work, trips);
       break;
     case 16:
-      fixup_end64_kernel<16><<<grid, 32, 0, stream>>>(A, list, n, endv, work, trips);
+      fixup_end64_kernel<16><<<grid, 32, 0, stream>>>(A, list, n, n_dev, endv, work, trips);
       break;
     case 8:
-      fixup_end64_kernel<8><<<grid, 32, 0, stream>>>(A, list, n, endv, work, trips);
+      fixup_end64_kernel<8><<<grid, 32, 0, stream>>>(A, list, n, n_dev, endv, work, trips);
       break;
     default:
-      fixup_end64_kernel<2><<<grid, 32, 0, stream>>>(A, list, n, endv, work, trips);
+      fixup_end64_kernel<2><<<grid, 32, 0, stream>>>(A, list, n, n_dev, endv, work, trips);
   }
   return cudaGetLastError();
 }

@@ -197,7 +197,7 @@ cudaError_t launch_boundary_set(const int32_t* lab, const uint8_t* state, const 
 // counter of claimed items, zeroed by the launchers.
 cudaError_t launch_fixup_end64(const double* G, const VolDims& V, const IntegParams& P, const uint8_t* state,
                                const int64_t* list, int n, int32_t* endv, unsigned long long* work,
-                               unsigned long long* trips, int num_sms, cudaStream_t stream);
+                               unsigned long long* trips, int num_sms, cudaStream_t stream, const int* n_dev = nullptr);
 // n_dev (optional): the list's length in device memory, n then only sizes the grid
 cudaError_t launch_fixup_end32(const float4* G, const VolDims& V, const IntegParams& P, const int32_t* lab,
                                const uint8_t* state, const int64_t* list, int n, int32_t* endv, int64_t* amb,

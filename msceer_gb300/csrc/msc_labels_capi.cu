@@ -743,16 +743,14 @@ int finish_direction(LabelCtx& c, DirLabels& d, int32_t* out, int32_t* stage_int
   LCUDA(c.pool.get(&rval, N), "alloc");
   int64_t early_n = 0, early_amb = 0;
   if (early) {
-    // the ends computed beside the first pass, and in FP64 those whose FP32 ending was
-    // ambiguous
+    // the ends computed beside the first pass (FP32, and FP64 where the FP32 ending was
+    // ambiguous)
     endv = early->endv;
     LCUDA(cudaStreamWaitEvent(st, c.ends_done, 0), "cudaStreamWaitEvent");
     int h[2] = {0, 0};
     if (int rc = read_dev(c, c.counters + 7, 1, &h[0])) return rc;
     if (int rc = read_dev(c, c.counters + 12, 1, &h[1])) return rc;
     trace_mark(st, d.dir, "ends of " + std::to_string(h[1]) + " (FP64 " + std::to_string(h[0]) + ")");
-    LCUDA(msc::launch_fixup_end64(c.g64, V, P, d.state, c.amb, h[0], endv, c.work + 56, c.work + 50, sms, st),
-          "fix-up FP64");
     early_amb = h[0];
     early_n = h[1];
   } else {
@@ -880,6 +878,10 @@ int start_early_ends(LabelCtx& c, DirLabels& d, EarlyEnds& e) {
   LCUDA(msc::launch_fixup_end32(c.g32, c.V, P, d.lab, d.state, e.list, (int)N, e.endv, c.amb, c.counters + 7,
                                 c.p->precision == 2 ? 2 : 0, c.work, c.work + 49, c.sms, c.ends_st, c.counters + 12),
         "fix-up ends");
+  // and in FP64 the ones whose FP32 ending was ambiguous (their count stays on the device)
+  LCUDA(msc::launch_fixup_end64(c.g64, c.V, P, d.state, c.amb, 1, e.endv, c.work + 56, c.work + 50, c.sms, c.ends_st,
+                                c.counters + 7),
+        "fix-up FP64 ends");
   LCUDA(cudaEventRecord(c.ends_done, c.ends_st), "cudaEventRecord");
   e.on = true;
   return MSC_OK;
@@ -944,7 +946,16 @@ void run_dsc_job(int dev, cudaEvent_t inputs_ready, const float* f, const uint8_
   auto body = [&]() -> int {
     LCUDA(cudaSetDevice(dev), "cudaSetDevice");
     cudaStream_t sb = nullptr;
-    LCUDA(cudaStreamCreateWithFlags(&sb, cudaStreamNonBlocking), "cudaStreamCreate");
+    // the descending labels take about twice the ascending ones' work (their streamlines
+    // are longer), so their stream goes first where both have blocks waiting
+    // (MSC_DSC_PRIORITY=0: the default priority)
+    int lo = 0, hi = 0;
+    LCUDA(cudaDeviceGetStreamPriorityRange(&lo, &hi), "cudaDeviceGetStreamPriorityRange");
+    static const bool prio = [] {
+      const char* e = std::getenv("MSC_DSC_PRIORITY");
+      return !(e && std::atoi(e) == 0);
+    }();
+    LCUDA(cudaStreamCreateWithPriority(&sb, cudaStreamNonBlocking, prio ? hi : lo), "cudaStreamCreate");
     struct Destroy {
       cudaStream_t s;
       ~Destroy() {
