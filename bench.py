@@ -22,6 +22,8 @@ against the plain labels), or timed as the step with --triage.
               H2D of f, .grad, labels, D2H of both label volumes per step
   grad        the .grad alone: Gvert/s and its per-kernel breakdown
   grad_2d     the .grad of the 8192^2 k^-3 field (2D): Gvert/s, kernels, roofline
+  conforming_grad  ondemandaccurate's accurate 3-manifold .grad of the step (restriction
+              labels from its final labels, re-pairing, ldir): ms, touched vertices
   ms_graph    the Morse-Smale complex nodes and arcs of the step's .grad on the device
               (msc_ms_graph_3d, extractmsc's arc flags): counts, ms, Gvert/s
   roofline    the dominant .grad kernel's algorithmic bytes / its measured duration
@@ -421,6 +423,7 @@ def run_ours(args, ws, rank, local):
         e0, e1 = _events(2)
         l0 = lib.msc_kernel_launches()
         e0.record(stream)
+        res = None
         for _ in range(args.steps):
             res = step()
         e1.record(stream)
@@ -588,6 +591,30 @@ def run_ours(args, ws, rank, local):
                    "value": V2 / (t2 * 1e-3) / 1e9, "unit": UNIT, "ms_per_step": t2, "kernels": k2, "roofline": r2}
         del f2, g2
 
+    # ondemandaccurate's accurate 3-manifold .grad of the step: restriction labels from
+    # the step's final labels, the re-pairing of the touched vertices, the ldir stage
+    conform = None
+    if not args.grad_only and not args.no_batch and isinstance(res, dict) and "asc" in res:
+        from msceer_gb300 import conforming_grad
+        lower_star_grad(f_dev, out=g_dev)
+        base = g_dev.clone()
+        touched = conforming_grad(f_dev, g_dev, res["asc"], res["dsc"])
+        torch.cuda.synchronize(dev)
+        tc = 0.0
+        for _ in range(reps):
+            g_dev.copy_(base)
+            c0, c1 = _events(2)
+            c0.record(stream)
+            conforming_grad(f_dev, g_dev, res["asc"], res["dsc"])
+            c1.record(stream)
+            torch.cuda.synchronize(dev)
+            tc += c0.elapsed_time(c1)
+        tc /= reps
+        conform = {"workload": "msc_conforming_grad_3d on the step's .grad with its final labels (needASC2 = "
+                               "needDSC2 = 1)", "touched_vertices": int(touched), "ms": tc,
+                   "value": V / (tc * 1e-3) / 1e9, "unit": UNIT}
+        del base
+
     # the Morse-Smale complex graph of the bench volume's .grad (extractmsc's
     # ComputeFromGrad: arcs from 1-saddles and maxima, no geometry)
     graph = None
@@ -661,6 +688,8 @@ def run_ours(args, ws, rank, local):
             line["grad_2d"] = grad_2d
         if graph is not None:
             line["ms_graph"] = graph
+        if conform is not None:
+            line["conforming_grad"] = conform
         if mismatch is not None:
             line["mismatch_vs_fp64_oracle"] = mismatch
         if batch is not None:
