@@ -1142,7 +1142,6 @@ __global__ void __launch_bounds__(128, 7) fixup_end32_kernel(const Adv32 A, cons
     if (phase != kLaneEnd) continue;
     phase = kLaneIdle;
     const int64_t end = vid(V, x, y, z);
-    const int32_t lend = lab[end];
     // a low-gradient stop whose FP32 magnitude lies within 2^-8 (relative) of the
     // threshold: FP32 rounding could have taken the other side of the stop test.  A
     // streamline that decelerates into an extremum crosses the threshold well inside
@@ -1152,7 +1151,9 @@ __global__ void __launch_bounds__(128, 7) fixup_end32_kernel(const Adv32 A, cons
       const float pc[3] = {cur.x, cur.y, cur.z};
       const int64_t ext[3] = {V.X, V.Y, V.Z};
       const int64_t ev3[3] = {x, y, z};
-      const int32_t le = lend;
+      // the end is a certain terminal here, whose label no pass changes (the ends can
+      // run beside the first pass, which writes the labels of uncertain vertices only)
+      const int32_t le = lab[end];
 #pragma unroll
       for (int a = 0; a < 3; a++) {
         const float q = pc[a] + 0.5f;
