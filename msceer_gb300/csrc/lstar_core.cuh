@@ -404,9 +404,14 @@ MSC_HD void store_cells(const State& st, uint32_t L, uint32_t Bany, uint32_t enc
   p0 |= K; p1 |= K; p2 |= K;
   const uint32_t l0 = ~K | (K & (D0 | D2));
   const uint32_t l1 = ~K | (K & (D0 | D1));
-#pragma unroll
-  for (int p = 0; p < NPOS; p++) {
-    if (!((L >> p) & 1u)) continue;
+  // a loop over the owned cells only (about 8 of the 27 positions): a short body that
+  // stays in the instruction cache, where 27 unrolled position blocks did not
+  (void)NPOS;
+  uint32_t m = L;
+#pragma unroll 1
+  while (m) {
+    const int p = ffs32(m) - 1;
+    m &= m - 1;
     const uint32_t b = 1u | (((Bany >> p) & 1u) << 1) | (((p0 >> p) & 1u) << 2) | (((p1 >> p) & 1u) << 3) |
                        (((p2 >> p) & 1u) << 4) | (((l0 >> p) & 1u) << 5) | (((l1 >> p) & 1u) << 6);
     store(p, (uint8_t)b);
