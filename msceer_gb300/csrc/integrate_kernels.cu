@@ -280,6 +280,38 @@ __device__ __forceinline__ void add_trips(unsigned long long n, unsigned long lo
   if ((threadIdx.x & 31) == 0 && n) atomicAdd(trips, n);
 }
 
+// Slots in a list whose length is *n for `cnt` entries of every thread of the block (one
+// atomic per block): returns the thread's first slot.  Every thread of the block calls
+// it, as often as the others (s_part: kAppendWarps + 1 ints of shared memory).  Lists
+// that most vertices enter (the boundary set, a wave's reopened neighbours: ~10^8 at
+// 512^3) made millions of atomics on one counter with an append per warp, and those
+// serialise in L2.
+constexpr int kAppendWarps = 8;  // blocks of 256 threads
+__device__ __forceinline__ int block_append(int cnt, int* __restrict__ n, int* s_part) {
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  int incl = cnt;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int u = __shfl_up_sync(kFullMask, incl, o);
+    if (lane >= o) incl += u;
+  }
+  if (lane == 31) s_part[w] = incl;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int run = 0;
+    for (int j = 0; j < kAppendWarps; j++) {
+      const int t = s_part[j];
+      s_part[j] = run;
+      run += t;
+    }
+    s_part[kAppendWarps] = run > 0 ? atomicAdd(n, run) : 0;
+  }
+  __syncthreads();
+  const int slot = s_part[kAppendWarps] + s_part[w] + incl - cnt;
+  __syncthreads();  // s_part is reused by the next call
+  return slot;
+}
+
 // ---- first pass: speculation, then the reference's sequential outcome ------------------
 //
 // The reference's first pass (:150-240) visits the vertices one at a time in its spread
@@ -976,11 +1008,14 @@ struct Adv64 {
 // Vertices assigned in pass 1 with a differently labelled 6-neighbour (:279-307).
 __global__ void boundary_set_kernel(const int32_t* __restrict__ lab, const uint8_t* __restrict__ state, const VolDims V,
                                     int64_t* __restrict__ list, int* __restrict__ n, uint32_t* __restrict__ queued) {
+  __shared__ int s_part[kAppendWarps + 1];
   const int64_t N = V.X * V.Y * V.Z;
   const int lane = threadIdx.x & 31;
   // a warp covers 32 consecutive vertices starting at a multiple of 32 (block size and
-  // grid stride are multiples of 32), i.e. exactly one word of `queued`
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i - lane < N; i += (int64_t)gridDim.x * blockDim.x) {
+  // grid stride are multiples of 32), i.e. exactly one word of `queued`; every thread of
+  // a block makes the same number of trips (block_append)
+  for (int64_t b0 = blockIdx.x * (int64_t)blockDim.x; b0 < N; b0 += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i = b0 + threadIdx.x;
     bool diff = false;
     if (i < N && state[i] == kStUnassigned) {
       int x, y, z;
@@ -993,15 +1028,10 @@ __global__ void boundary_set_kernel(const int32_t* __restrict__ lab, const uint8
       if (z < V.Z - 1) diff |= lab[i + V.X * V.Y] != l;
       if (z > 0) diff |= lab[i - V.X * V.Y] != l;
     }
-    const unsigned m = __ballot_sync(kFullMask, diff);  // (the loop bound is warp-uniform)
-    if (!m) continue;
-    int base = 0;
-    if (lane == 0) {
-      atomicOr(&queued[i >> 5], m);
-      base = atomicAdd(n, __popc(m));
-    }
-    base = __shfl_sync(kFullMask, base, 0);
-    if (diff) list[base + __popc(m & ((1u << lane) - 1u))] = i;
+    const unsigned m = __ballot_sync(kFullMask, diff);
+    if (lane == 0 && m) atomicOr(&queued[i >> 5], m);
+    const int slot = block_append(diff ? 1 : 0, n, s_part);
+    if (diff) list[slot] = i;
   }
 }
 
@@ -1193,17 +1223,13 @@ __global__ void __launch_bounds__(128, 7) fixup_end32_kernel(const Adv32 A, cons
 // fix-up wave can hold, whose streamline ends are computed ahead of the waves.
 __global__ void uncertain_list_kernel(const uint8_t* __restrict__ state, int64_t N, int64_t* __restrict__ list,
                                       int* __restrict__ n) {
+  __shared__ int s_part[kAppendWarps + 1];
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
   for (int64_t v0 = blockIdx.x * (int64_t)blockDim.x; v0 < N; v0 += stride) {
     const int64_t v = v0 + threadIdx.x;
     const bool want = v < N && state[v] != kStSeed && state[v] != kStTerminal;
-    const unsigned m = __ballot_sync(kFullMask, want);
-    if (!m) continue;
-    const int lane = threadIdx.x & 31, leader = __ffs(m) - 1;
-    int base = 0;
-    if (lane == leader) base = atomicAdd(n, __popc(m));
-    base = __shfl_sync(kFullMask, base, leader);
-    if (want) list[base + __popc(m & ((1u << lane) - 1u))] = v;
+    const int slot = block_append(want ? 1 : 0, n, s_part);
+    if (want) list[slot] = v;
   }
 }
 
@@ -1299,7 +1325,8 @@ __global__ void wave_enqueue_kernel(const int64_t* __restrict__ list, int n, int
                                     const int32_t* __restrict__ lab, const uint8_t* __restrict__ state,
                                     const int32_t* __restrict__ inw, uint32_t* __restrict__ queued,
                                     int64_t* __restrict__ next, int* __restrict__ n_next) {
-  for (int k0 = blockIdx.x * blockDim.x; k0 < n; k0 += gridDim.x * blockDim.x) {  // warp-uniform trips
+  __shared__ int s_part[kAppendWarps + 1];
+  for (int k0 = blockIdx.x * blockDim.x; k0 < n; k0 += gridDim.x * blockDim.x) {  // block-uniform trips
     const int k = k0 + threadIdx.x;
     int64_t v = -1;
     int32_t nl = 0;
@@ -1319,6 +1346,7 @@ __global__ void wave_enqueue_kernel(const int64_t* __restrict__ list, int n, int
       nbr[4] = vz < V.Z - 1 ? v + V.X * V.Y : -1;
       nbr[5] = vz > 0 ? v - V.X * V.Y : -1;
     }
+    int cnt = 0;
 #pragma unroll
     for (int j = 0; j < 6; j++) {
       const int64_t u = nbr[j];
@@ -1328,9 +1356,13 @@ __global__ void wave_enqueue_kernel(const int64_t* __restrict__ list, int n, int
         const uint32_t bit = 1u << (u & 31);
         add = !(atomicOr(&queued[u >> 5], bit) & bit);
       }
-      const int slot = warp_append(add, n_next);
-      if (slot >= 0) next[slot] = u;
+      if (!add) nbr[j] = -1;
+      cnt += add;
     }
+    int slot = block_append(cnt, n_next, s_part);
+#pragma unroll
+    for (int j = 0; j < 6; j++)
+      if (nbr[j] >= 0) next[slot++] = nbr[j];
   }
 }
 
@@ -1408,17 +1440,24 @@ __global__ void uf_roots_kernel(const int32_t* __restrict__ parent, int32_t* __r
 __global__ void clean_roots_kernel(const int32_t* __restrict__ lab, const float* __restrict__ f, const VolDims V, int dir,
                                    const int32_t* __restrict__ first, int32_t* __restrict__ md,
                                    int32_t* __restrict__ roots, int* __restrict__ n_roots) {
+  __shared__ int s_part[kAppendWarps + 1];
   const int64_t N = V.X * V.Y * V.Z;
-  for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < N; r += (int64_t)gridDim.x * blockDim.x) {
-    md[r] = (int32_t)r;
-    if (first[r] != r) continue;
-    int x, y, z;
-    split_index(V, r, x, y, z);
-    const int64_t nbr[6] = {x < V.X - 1 ? r + 1 : -1, x > 0 ? r - 1 : -1, y < V.Y - 1 ? r + V.X : -1,
-                            y > 0 ? r - V.X : -1, z < V.Z - 1 ? r + V.X * V.Y : -1, z > 0 ? r - V.X * V.Y : -1};
+  for (int64_t b0 = blockIdx.x * (int64_t)blockDim.x; b0 < N; b0 += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t r = b0 + threadIdx.x;  // (block-uniform trips: block_append)
     bool any = false;
-    for (int j = 0; j < 6; j++) any |= nbr[j] >= 0 && comes_before(f, dir, nbr[j], r);
-    if (any) roots[atomicAdd(n_roots, 1)] = (int32_t)r;
+    if (r < N) {
+      md[r] = (int32_t)r;
+      if (first[r] == r) {
+        int x, y, z;
+        split_index(V, r, x, y, z);
+        const int64_t nbr[6] = {x < V.X - 1 ? r + 1 : -1, x > 0 ? r - 1 : -1, y < V.Y - 1 ? r + V.X : -1,
+                                y > 0 ? r - V.X : -1, z < V.Z - 1 ? r + V.X * V.Y : -1,
+                                z > 0 ? r - V.X * V.Y : -1};
+        for (int j = 0; j < 6; j++) any |= nbr[j] >= 0 && comes_before(f, dir, nbr[j], r);
+      }
+    }
+    const int slot = block_append(any ? 1 : 0, n_roots, s_part);
+    if (any) roots[slot] = (int32_t)r;
   }
 }
 
