@@ -20,11 +20,20 @@ template <int ND, int LAYOUT>  // LAYOUT: 0 = xyz f32 (ND floats), 1 = xyzw f32,
 __global__ void __launch_bounds__(256) central_diff_kernel(const float* __restrict__ f, void* __restrict__ out,
                                                            const int64_t X, const int64_t Y, const int64_t Z) {
   const int64_t n = X * Y * Z;
+  const bool small = n <= (int64_t)0xFFFFFFFF;  // 32-bit index arithmetic (64-bit division is slow)
   for (int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v < n; v += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t x = v % X;
-    const int64_t r = v / X;
-    const int64_t y = r % Y;
-    const int64_t z = r / Y;
+    int64_t x, y, z;
+    if (small) {
+      const uint32_t u = (uint32_t)v, r = u / (uint32_t)X;
+      x = u - r * (uint32_t)X;
+      y = r % (uint32_t)Y;
+      z = r / (uint32_t)Y;
+    } else {
+      const int64_t r = v / X;
+      x = v - r * X;
+      y = r % Y;
+      z = r / Y;
+    }
     const bool ix = x > 0 && x < X - 1;
     const bool iy = y > 0 && y < Y - 1;
     const bool iz = (ND == 3) && z > 0 && z < Z - 1;

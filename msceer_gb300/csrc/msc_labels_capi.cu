@@ -323,7 +323,7 @@ int read_dev(LabelCtx& c, const T* d, int n, T* out) {
 struct DirLabels {
   int dir = -1;
   std::function<int()> on_seeds;         // called once the seeds are on the stream (prepare_direction)
-  std::function<int()> before_terminal;  // called before the terminal-region walk (prepare_direction)
+  std::function<int()> before_integration;  // called at the end of prepare_direction
   int64_t trips[3] = {0, 0, 0};  // advection iterations: first pass, FP32 fix-up, FP64 re-decisions
   int32_t* lab = nullptr;
   uint8_t* state = nullptr;
@@ -488,8 +488,6 @@ int prepare_direction(LabelCtx& c, DirLabels& d, int32_t* stage_terminal) {
   if (d.on_seeds)
     if (int rc = d.on_seeds()) return rc;
 
-  if (d.before_terminal)
-    if (int rc = d.before_terminal()) return rc;
   // certain terminal regions: a global frontier walk from the seeds to the fixpoint
   // (MSC_TERMINAL_TILES=1: tile passes instead)
   if (!terminal_tiles_on()) {
@@ -537,6 +535,8 @@ int prepare_direction(LabelCtx& c, DirLabels& d, int32_t* stage_terminal) {
   }
   ::msc::count_launch();
   terminal_state_kernel<<<c.grid, 256, 0, st>>>(d.lab, d.state, N);
+  if (d.before_integration)
+    if (int rc = d.before_integration()) return rc;
   return MSC_OK;
 }
 
@@ -972,10 +972,10 @@ void run_dsc_job(int dev, cudaEvent_t inputs_ready, const float* f, const uint8_
       trace_mark(sb, 1, "setup");
       DirLabels d;
       d.dir = 1;
-      // the ascending job's seeds before this direction's terminal-region walk: the walk
-      // holds most of every SM's shared memory, and the ascending merge's small kernels
-      // launched beside it waited for it to end
-      d.before_terminal = [&]() -> int {
+      // the ascending job's seeds, zeroed in this direction's gradient before its
+      // streamlines start (the terminal regions before them do not read the gradient, and
+      // grow while the ascending job merges its extrema)
+      d.before_integration = [&]() -> int {
         {
           std::unique_lock<std::mutex> lk(asc->mu);
           asc->cv.wait(lk, [&] { return asc->ready; });
