@@ -16,8 +16,11 @@ struct VolDims {
 // A saddle arc between two extrema (MergeArc, gi_extrema_region_builder.h:43-61).
 struct Arc {
   int64_t saddle;
-  int32_t e1, e2;
+  int32_t e1, e2;  // extremum ids
   float sval, pers;
+  int64_t c1, c2;  // the extrema's cells, their highest vertices and values there (what
+  int64_t h1, h2;  // the host merge compares)
+  float f1, f2;
 };
 
 // Per-vertex integration state (DestType, gi_basic_types.h:43-49, plus "seed": a
@@ -149,7 +152,9 @@ struct SpecSet {
   unsigned long long* ncursor;  // next free node
 };
 // lvl: 0 for labelled vertices, 255 for the rest
-cudaError_t launch_init_levels(const int32_t* lab, uint8_t* lvl, int64_t N, int num_sms, cudaStream_t stream);
+// (n_unlabelled, optional: the number of the rest is added to it)
+cudaError_t launch_init_levels(const int32_t* lab, uint8_t* lvl, int64_t N, int num_sms, cudaStream_t stream,
+                               unsigned long long* n_unlabelled = nullptr);
 // The vertices of spread positions [u0, u1) with lvl >= stamp, in order, into items;
 // their number to *n_items.  counts: (u1 - u0) / 1024 + 1 ints of scratch.
 cudaError_t launch_spread_compact(const SpreadOrder& S, int64_t u0, int64_t u1, const uint8_t* lvl, int stamp,
@@ -187,8 +192,10 @@ cudaError_t launch_spec_round(const SpecSet& Q, int64_t k0, int64_t k1, uint32_t
 cudaError_t launch_spec_ptr(const SpecSet& Q, int64_t k0, int64_t k1, const uint32_t* claim, int num_sms,
                             cudaStream_t stream);
 cudaError_t launch_spec_jumps(const SpecSet& Q, int64_t k0, int64_t k1, int num_sms, cudaStream_t stream);
+// (n_labelled: the vertices it labels are added to it)
 cudaError_t launch_spec_write(const SpecSet& Q, int64_t k0, int64_t k1, uint8_t* lvl, int stamp, const uint32_t* claim,
-                              int32_t* lab, int* long_chain, int num_sms, cudaStream_t stream);
+                              int32_t* lab, int* long_chain, unsigned long long* n_labelled, int num_sms,
+                              cudaStream_t stream);
 cudaError_t launch_boundary_set(const int32_t* lab, const uint8_t* state, const VolDims& V, int64_t* list, int* n,
                                 uint32_t* queued, int num_sms, cudaStream_t stream);
 // Fix-up streamline ends (FP64 / FP32): endv[v] = the final nearest vertex of v's

@@ -151,7 +151,8 @@ __global__ void trace_arcs_kernel(const uint8_t* __restrict__ g, const float* __
     const int64_t e2 = trace_vpath(g, V, dir, ends[1], err);
     if (e1 == e2) continue;
     const float sval = f[highest_vertex(V, f, sad)];
-    const float f1 = f[highest_vertex(V, f, e1)], f2 = f[highest_vertex(V, f, e2)];
+    const int64_t h1 = highest_vertex(V, f, e1), h2 = highest_vertex(V, f, e2);
+    const float f1 = f[h1], f2 = f[h2];
     float d1 = f1 - sval, d2 = f2 - sval;
     if (d1 < 0) d1 *= -1;
     if (d2 < 0) d2 *= -1;
@@ -166,6 +167,12 @@ __global__ void trace_arcs_kernel(const uint8_t* __restrict__ g, const float* __
     arcs[slot].e2 = ext_id_of_key[(k2[0] >> 1) + (k2[1] >> 1) * V.X + (k2[2] >> 1) * V.X * V.Y];
     arcs[slot].sval = sval;
     arcs[slot].pers = pers;
+    arcs[slot].c1 = e1;
+    arcs[slot].c2 = e2;
+    arcs[slot].h1 = h1;
+    arcs[slot].h2 = h2;
+    arcs[slot].f1 = f1;
+    arcs[slot].f2 = f2;
   }
 }
 

@@ -126,15 +126,6 @@ __global__ void snapshot_kernel(const int32_t* lab, int32_t* out, int64_t n) {
     out[i] = lab[i] == msc::kLabelNone ? -1 : lab[i];
 }
 // the extrema that the mergeable arcs touch, gathered for the host merge
-__global__ void gather_extrema_kernel(const int32_t* ids, int m, const int64_t* cells, const int64_t* hv,
-                                      const float* fval, int64_t* oc, int64_t* ohv, float* of) {
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < m; i += gridDim.x * blockDim.x) {
-    const int32_t e = ids[i];
-    oc[i] = cells[e];
-    ohv[i] = hv[e];
-    of[i] = fval[e];
-  }
-}
 // the host merge's changed representatives: rep[pairs[2k]] = pairs[2k + 1]
 __global__ void scatter_rep_kernel(const int32_t* pairs, int m, int32_t* rep) {
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < m; i += gridDim.x * blockDim.x) rep[pairs[2 * i]] = pairs[2 * i + 1];
@@ -322,7 +313,7 @@ int read_dev(LabelCtx& c, const T* d, int n, T* out) {
 // One direction's labels between the phases.
 struct DirLabels {
   int dir = -1;
-  std::function<int()> on_seeds;         // called once the seeds are on the stream (prepare_direction)
+  std::function<int()> on_seeds;         // called once the seed list is on the stream (prepare_direction)
   std::function<int()> before_integration;  // called at the end of prepare_direction
   int64_t trips[3] = {0, 0, 0};  // advection iterations: first pass, FP32 fix-up, FP64 re-decisions
   int32_t* lab = nullptr;
@@ -412,6 +403,9 @@ int prepare_direction(LabelCtx& c, DirLabels& d, int32_t* stage_terminal) {
   LCUDA(c.pool.get(&name, n_ext + 1), "alloc");
   LCUDA(c.pool.get(&arcs, n_sad + 1), "alloc");
   LCUDA(msc::launch_extremum_info(c.f, V, dir, c.ext_cells, n_ext, hv, fval, d.seed, c.sms, st), "extremum info");
+  // the seed list is final here (the merge below changes representatives, not seeds)
+  if (d.on_seeds)
+    if (int rc = d.on_seeds()) return rc;
   LCUDA(msc::launch_trace_arcs(c.grad, c.f, V, dir, c.saddles, n_sad, c.key, c.p->presimp_threshold, arcs,
                                c.counters + 2, c.counters + 4, c.sms, st),
         "trace arcs");
@@ -440,26 +434,20 @@ int prepare_direction(LabelCtx& c, DirLabels& d, int32_t* stage_terminal) {
     std::sort(ids.begin(), ids.end());
     ids.erase(std::unique(ids.begin(), ids.end()), ids.end());
     const int m = (int)ids.size();
+    // the arcs carry their extrema's cells, highest vertices and values: no gather and
+    // no second wait for the GPU (whose SMs the other direction's launches may hold)
+    std::vector<int64_t> hcells(m), hhv(m);
+    std::vector<float> hf(m);
     for (msc::Arc& a : ha) {
       a.e1 = (int32_t)(std::lower_bound(ids.begin(), ids.end(), a.e1) - ids.begin());
       a.e2 = (int32_t)(std::lower_bound(ids.begin(), ids.end(), a.e2) - ids.begin());
+      hcells[a.e1] = a.c1;
+      hhv[a.e1] = a.h1;
+      hf[a.e1] = a.f1;
+      hcells[a.e2] = a.c2;
+      hhv[a.e2] = a.h2;
+      hf[a.e2] = a.f2;
     }
-    int32_t* dids;
-    int64_t *dcells, *dhv;
-    float* dfv;
-    LCUDA(c.pool.get(&dids, 2 * (size_t)m), "alloc");
-    LCUDA(c.pool.get(&dcells, m), "alloc");
-    LCUDA(c.pool.get(&dhv, m), "alloc");
-    LCUDA(c.pool.get(&dfv, m), "alloc");
-    LCUDA(cudaMemcpyAsync(dids, ids.data(), m * sizeof(int32_t), cudaMemcpyHostToDevice, st), "write ids");
-    ::msc::count_launch();
-    gather_extrema_kernel<<<(m + 255) / 256, 256, 0, st>>>(dids, m, c.ext_cells, hv, fval, dcells, dhv, dfv);
-    std::vector<int64_t> hcells(m), hhv(m);
-    std::vector<float> hf(m);
-    LCUDA(cudaMemcpyAsync(hcells.data(), dcells, m * sizeof(int64_t), cudaMemcpyDeviceToHost, st), "read");
-    LCUDA(cudaMemcpyAsync(hhv.data(), dhv, m * sizeof(int64_t), cudaMemcpyDeviceToHost, st), "read");
-    LCUDA(cudaMemcpyAsync(hf.data(), dfv, m * sizeof(float), cudaMemcpyDeviceToHost, st), "read");
-    LCUDA(cudaStreamSynchronize(st), "sync");
     std::vector<int32_t> hrep;
     host_merge(dir, c.p->presimp_threshold, ha, hcells, hhv, hf, hrep);
     std::vector<int32_t> pairs;
@@ -470,11 +458,12 @@ int prepare_direction(LabelCtx& c, DirLabels& d, int32_t* stage_terminal) {
       }
     const int np = (int)pairs.size() / 2;
     if (np > 0) {
-      // dids holds 2m entries: room for the pairs
-      LCUDA(cudaMemcpyAsync(dids, pairs.data(), 2 * np * sizeof(int32_t), cudaMemcpyHostToDevice, st), "write rep");
+      int32_t* dpairs;
+      LCUDA(c.pool.get(&dpairs, 2 * (size_t)np), "alloc");
+      // (from pageable memory the copy has taken the data when the call returns)
+      LCUDA(cudaMemcpyAsync(dpairs, pairs.data(), 2 * np * sizeof(int32_t), cudaMemcpyHostToDevice, st), "write rep");
       ::msc::count_launch();
-      scatter_rep_kernel<<<(np + 255) / 256, 256, 0, st>>>(dids, np, rep);
-      LCUDA(cudaStreamSynchronize(st), "sync");
+      scatter_rep_kernel<<<(np + 255) / 256, 256, 0, st>>>(dpairs, np, rep);
     }
     trace_mark(st, dir, "merge " + std::to_string(n_arcs) + " arcs, " + std::to_string(np) + " changed");
   }
@@ -485,8 +474,6 @@ int prepare_direction(LabelCtx& c, DirLabels& d, int32_t* stage_terminal) {
   LCUDA(cudaMemsetAsync(d.state, 0, (size_t)N, st), "memset");
   LCUDA(msc::launch_group_seeds(rep, d.seed, n_ext, name, d.lab, d.state, c.sms, st), "seeds");
   trace_mark(st, dir, "seeds");
-  if (d.on_seeds)
-    if (int rc = d.on_seeds()) return rc;
 
   // certain terminal regions: a global frontier walk from the seeds to the fixpoint
   // (MSC_TERMINAL_TILES=1: tile passes instead)
@@ -626,9 +613,14 @@ int first_pass(LabelCtx& c, DirLabels& d) {
   Q.vtx = vtx;
   Q.cursor = sc;
   Q.ncursor = sc + 6;
+  // [0] vertices unlabelled at the start, [1] labelled by the batches so far: once every
+  // one is labelled, the remaining levels of the order hold no item
+  unsigned long long* lcount;
+  LCUDA(c.pool.get(&lcount, 2), "alloc");
+  LCUDA(cudaMemsetAsync(lcount, 0, 2 * sizeof(unsigned long long), st), "memset");
   LCUDA(cudaMemsetAsync(claim, 0xFF, (size_t)N * sizeof(uint32_t), st), "memset");
   LCUDA(cudaMemsetAsync(c.work + 48, 0, 3 * sizeof(unsigned long long), st), "memset");
-  LCUDA(msc::launch_init_levels(d.lab, lvl, N, c.sms, st), "levels");
+  LCUDA(msc::launch_init_levels(d.lab, lvl, N, c.sms, st, lcount), "levels");
   trace_mark(st, d.dir, "pass1 start");
   // the levels up to N/512 visits together form the first batch; every later level is a
   // batch of its own
@@ -696,18 +688,22 @@ int first_pass(LabelCtx& c, DirLabels& d) {
       trace_mark(st, d.dir, "  resolved");
       LCUDA(msc::launch_spec_ptr(Q, k0, k1, claim, c.sms, st), "label");
       LCUDA(cudaMemsetAsync(Q.overflow, 0, sizeof(int), st), "memset");
-      LCUDA(msc::launch_spec_write(Q, k0, k1, lvl, stamp, claim, d.lab, Q.overflow, c.sms, st), "label");
+      LCUDA(msc::launch_spec_write(Q, k0, k1, lvl, stamp, claim, d.lab, Q.overflow, lcount + 1, c.sms, st), "label");
       int long_chain = 0;
       if (int rc = read_dev(c, Q.overflow, 1, &long_chain)) return rc;
       if (long_chain) {  // a few long chains of cut items: jump, then write again
         LCUDA(msc::launch_spec_jumps(Q, k0, k1, c.sms, st), "label");
-        LCUDA(msc::launch_spec_write(Q, k0, k1, lvl, stamp, claim, d.lab, Q.overflow, c.sms, st), "label");
+        LCUDA(msc::launch_spec_write(Q, k0, k1, lvl, stamp, claim, d.lab, Q.overflow, lcount + 1, c.sms, st),
+              "label");
       }
       batches++;
       trace_mark(st, d.dir, "batch " + std::to_string(g0) + "-" + std::to_string(L1 - 1) + " items " +
                                 std::to_string(k1 - k0) + " rounds " + std::to_string(rounds_total));
       k0 = k1;
     }
+    unsigned long long cnt[2] = {0, 0};
+    if (int rc = read_dev(c, lcount, 2, cnt)) return rc;
+    if (cnt[1] >= cnt[0]) break;  // every vertex labelled
   }
   trace_mark(st, d.dir, "pass1 (" + std::to_string(batches) + " batches, " + std::to_string(rounds_total) + " rounds)");
   return MSC_OK;
@@ -1060,7 +1056,7 @@ int labels_concurrent(const float* f, const uint8_t* grad, const int64_t* dims, 
     DirLabels d;
     d.dir = -1;
     // the minima' seeds go to run_dsc_job (which zeroes them in its gradient copy) as
-    // soon as they exist, before this direction's terminal regions
+    // soon as they exist, before this direction's extremum merge and terminal regions
     bool published = false;
     d.on_seeds = [&]() -> int {
       LCUDA(cudaEventRecord(seeds_done, st), "cudaEventRecord");
