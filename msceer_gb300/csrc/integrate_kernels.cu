@@ -830,11 +830,9 @@ __global__ void spec_jump_kernel(const SpecSet Q, int64_t k0, int64_t k1) {
 constexpr int kChainSteps = 64;
 __global__ void spec_write_kernel(const SpecSet Q, int64_t k0, int64_t k1, uint8_t* __restrict__ lvl, int level,
                                   const uint32_t* __restrict__ claim, int32_t* __restrict__ lab,
-                                  int* __restrict__ long_chain, unsigned long long* __restrict__ n_labelled) {
-  unsigned long long cnt = 0;  // vertices this launch labels (not already stamped by an earlier write)
-  for (int64_t k0t = k0 + blockIdx.x * (int64_t)blockDim.x; k0t < k1; k0t += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t k = k0t + threadIdx.x;  // (warp-uniform trips: add_trips at the end)
-    if (k >= k1 || !Q.alive[k]) continue;
+                                  int* __restrict__ long_chain) {
+  for (int64_t k = k0 + blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < k1; k += (int64_t)gridDim.x * blockDim.x) {
+    if (!Q.alive[k]) continue;
     int32_t p = Q.ptr[k];
     for (int s = 0; s < kChainSteps; s++) {
       const int32_t q = Q.ptr[p];
@@ -853,24 +851,40 @@ __global__ void spec_write_kernel(const SpecSet Q, int64_t k0, int64_t k1, uint8
       if (!(u & kRec)) continue;
       const uint32_t v = u & ~kRec;
       if (claim[v] == (uint32_t)k) {
-        cnt += lvl[v] != (uint8_t)level;
         lab[v] = d;
         lvl[v] = (uint8_t)level;
       }
     }
   }
-  add_trips(cnt, n_labelled);
 }
 
-__global__ void init_levels_kernel(const int32_t* __restrict__ lab, uint8_t* __restrict__ lvl, int64_t N,
-                                   unsigned long long* __restrict__ n_unlabelled) {
+__global__ void init_levels_kernel(const int32_t* __restrict__ lab, uint8_t* __restrict__ lvl, int64_t N) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < N; i += (int64_t)gridDim.x * blockDim.x)
+    lvl[i] = lab[i] == -1 ? 255 : 0;
+}
+
+// The vertices not labelled yet (lvl 255): 16 bytes a thread, one atomic per warp.
+__global__ void count_unlabelled_kernel(const uint8_t* __restrict__ lvl, int64_t N,
+                                        unsigned long long* __restrict__ n) {
   unsigned long long cnt = 0;
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < N; i += (int64_t)gridDim.x * blockDim.x) {
-    const bool un = lab[i] == -1;
-    lvl[i] = un ? 255 : 0;
-    cnt += un;
+  const int64_t n16 = N / 16;
+  const uint4* l4 = reinterpret_cast<const uint4*>(lvl);
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n16; i += (int64_t)gridDim.x * blockDim.x) {
+    const uint4 q = l4[i];
+    const uint32_t w[4] = {q.x, q.y, q.z, q.w};
+#pragma unroll
+    for (int j = 0; j < 4; j++) {
+      // bytes equal to 0xFF: all bits set
+      uint32_t m = w[j] & (w[j] >> 1);
+      m &= m >> 2;
+      m &= m >> 4;
+      cnt += __popc(m & 0x01010101u);
+    }
   }
-  if (n_unlabelled) add_trips(cnt, n_unlabelled);
+  for (int64_t i = n16 * 16 + blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < N;
+       i += (int64_t)gridDim.x * blockDim.x)
+    cnt += lvl[i] == 255;
+  add_trips(cnt, n);
 }
 
 // ---- FP64 advector (fix-up), the reference's arithmetic --------------------------------
@@ -1563,10 +1577,17 @@ static int trips_per_turn_pass1() {
   return k;
 }
 
-cudaError_t launch_init_levels(const int32_t* lab, uint8_t* lvl, int64_t N, int num_sms, cudaStream_t stream,
-                               unsigned long long* n_unlabelled) {
+cudaError_t launch_count_unlabelled(const uint8_t* lvl, int64_t N, unsigned long long* n, int num_sms,
+                                    cudaStream_t stream) {
+  if (cudaError_t e = cudaMemsetAsync(n, 0, sizeof(unsigned long long), stream)) return e;
   ::msc::count_launch();
-  init_levels_kernel<<<num_sms * 8, 256, 0, stream>>>(lab, lvl, N, n_unlabelled);
+  count_unlabelled_kernel<<<num_sms * 4, 256, 0, stream>>>(lvl, N, n);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_init_levels(const int32_t* lab, uint8_t* lvl, int64_t N, int num_sms, cudaStream_t stream) {
+  ::msc::count_launch();
+  init_levels_kernel<<<num_sms * 8, 256, 0, stream>>>(lab, lvl, N);
   return cudaGetLastError();
 }
 
@@ -1660,11 +1681,9 @@ cudaError_t launch_spec_jumps(const SpecSet& Q, int64_t k0, int64_t k1, int num_
 }
 
 cudaError_t launch_spec_write(const SpecSet& Q, int64_t k0, int64_t k1, uint8_t* lvl, int stamp, const uint32_t* claim,
-                              int32_t* lab, int* long_chain, unsigned long long* n_labelled, int num_sms,
-                              cudaStream_t stream) {
+                              int32_t* lab, int* long_chain, int num_sms, cudaStream_t stream) {
   ::msc::count_launch();
-  spec_write_kernel<<<grid_for(k1 - k0, num_sms), 256, 0, stream>>>(Q, k0, k1, lvl, stamp, claim, lab, long_chain,
-                                                                    n_labelled);
+  spec_write_kernel<<<grid_for(k1 - k0, num_sms), 256, 0, stream>>>(Q, k0, k1, lvl, stamp, claim, lab, long_chain);
   return cudaGetLastError();
 }
 

@@ -152,9 +152,10 @@ struct SpecSet {
   unsigned long long* ncursor;  // next free node
 };
 // lvl: 0 for labelled vertices, 255 for the rest
-// (n_unlabelled, optional: the number of the rest is added to it)
-cudaError_t launch_init_levels(const int32_t* lab, uint8_t* lvl, int64_t N, int num_sms, cudaStream_t stream,
-                               unsigned long long* n_unlabelled = nullptr);
+cudaError_t launch_init_levels(const int32_t* lab, uint8_t* lvl, int64_t N, int num_sms, cudaStream_t stream);
+// *n = the vertices with lvl 255 (not labelled yet)
+cudaError_t launch_count_unlabelled(const uint8_t* lvl, int64_t N, unsigned long long* n, int num_sms,
+                                    cudaStream_t stream);
 // The vertices of spread positions [u0, u1) with lvl >= stamp, in order, into items;
 // their number to *n_items.  counts: (u1 - u0) / 1024 + 1 ints of scratch.
 cudaError_t launch_spread_compact(const SpreadOrder& S, int64_t u0, int64_t u1, const uint8_t* lvl, int stamp,
@@ -192,10 +193,8 @@ cudaError_t launch_spec_round(const SpecSet& Q, int64_t k0, int64_t k1, uint32_t
 cudaError_t launch_spec_ptr(const SpecSet& Q, int64_t k0, int64_t k1, const uint32_t* claim, int num_sms,
                             cudaStream_t stream);
 cudaError_t launch_spec_jumps(const SpecSet& Q, int64_t k0, int64_t k1, int num_sms, cudaStream_t stream);
-// (n_labelled: the vertices it labels are added to it)
 cudaError_t launch_spec_write(const SpecSet& Q, int64_t k0, int64_t k1, uint8_t* lvl, int stamp, const uint32_t* claim,
-                              int32_t* lab, int* long_chain, unsigned long long* n_labelled, int num_sms,
-                              cudaStream_t stream);
+                              int32_t* lab, int* long_chain, int num_sms, cudaStream_t stream);
 cudaError_t launch_boundary_set(const int32_t* lab, const uint8_t* state, const VolDims& V, int64_t* list, int* n,
                                 uint32_t* queued, int num_sms, cudaStream_t stream);
 // Fix-up streamline ends (FP64 / FP32): endv[v] = the final nearest vertex of v's

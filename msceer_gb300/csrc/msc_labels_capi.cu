@@ -321,6 +321,7 @@ struct DirLabels {
   int64_t* seed = nullptr;
   int n_ext = 0;
   bool seeds_zeroed = false;  // the gradient at this direction's seeds is zero on the stream
+  bool trips_zeroed = false;  // the iteration counters (work[48, 51)) are zero on the stream
 };
 
 int setup_ctx(LabelCtx& c, const float* f, const uint8_t* grad, const int64_t* dims, const msc_integ_params* p) {
@@ -613,14 +614,16 @@ int first_pass(LabelCtx& c, DirLabels& d) {
   Q.vtx = vtx;
   Q.cursor = sc;
   Q.ncursor = sc + 6;
-  // [0] vertices unlabelled at the start, [1] labelled by the batches so far: once every
-  // one is labelled, the remaining levels of the order hold no item
-  unsigned long long* lcount;
-  LCUDA(c.pool.get(&lcount, 2), "alloc");
-  LCUDA(cudaMemsetAsync(lcount, 0, 2 * sizeof(unsigned long long), st), "memset");
+  // the vertices still unlabelled after a level (a byte scan): once there are none, the
+  // remaining levels of the order hold no item (the last covers all N positions)
+  unsigned long long* n_left;
+  LCUDA(c.pool.get(&n_left, 1), "alloc");
   LCUDA(cudaMemsetAsync(claim, 0xFF, (size_t)N * sizeof(uint32_t), st), "memset");
-  LCUDA(cudaMemsetAsync(c.work + 48, 0, 3 * sizeof(unsigned long long), st), "memset");
-  LCUDA(msc::launch_init_levels(d.lab, lvl, N, c.sms, st, lcount), "levels");
+  if (!d.trips_zeroed) {
+    LCUDA(cudaMemsetAsync(c.work + 48, 0, 3 * sizeof(unsigned long long), st), "memset");
+    d.trips_zeroed = true;
+  }
+  LCUDA(msc::launch_init_levels(d.lab, lvl, N, c.sms, st), "levels");
   trace_mark(st, d.dir, "pass1 start");
   // the levels up to N/512 visits together form the first batch; every later level is a
   // batch of its own
@@ -688,22 +691,22 @@ int first_pass(LabelCtx& c, DirLabels& d) {
       trace_mark(st, d.dir, "  resolved");
       LCUDA(msc::launch_spec_ptr(Q, k0, k1, claim, c.sms, st), "label");
       LCUDA(cudaMemsetAsync(Q.overflow, 0, sizeof(int), st), "memset");
-      LCUDA(msc::launch_spec_write(Q, k0, k1, lvl, stamp, claim, d.lab, Q.overflow, lcount + 1, c.sms, st), "label");
+      LCUDA(msc::launch_spec_write(Q, k0, k1, lvl, stamp, claim, d.lab, Q.overflow, c.sms, st), "label");
       int long_chain = 0;
       if (int rc = read_dev(c, Q.overflow, 1, &long_chain)) return rc;
       if (long_chain) {  // a few long chains of cut items: jump, then write again
         LCUDA(msc::launch_spec_jumps(Q, k0, k1, c.sms, st), "label");
-        LCUDA(msc::launch_spec_write(Q, k0, k1, lvl, stamp, claim, d.lab, Q.overflow, lcount + 1, c.sms, st),
-              "label");
+        LCUDA(msc::launch_spec_write(Q, k0, k1, lvl, stamp, claim, d.lab, Q.overflow, c.sms, st), "label");
       }
       batches++;
       trace_mark(st, d.dir, "batch " + std::to_string(g0) + "-" + std::to_string(L1 - 1) + " items " +
                                 std::to_string(k1 - k0) + " rounds " + std::to_string(rounds_total));
       k0 = k1;
     }
-    unsigned long long cnt[2] = {0, 0};
-    if (int rc = read_dev(c, lcount, 2, cnt)) return rc;
-    if (cnt[1] >= cnt[0]) break;  // every vertex labelled
+    LCUDA(msc::launch_count_unlabelled(lvl, N, n_left, c.sms, st), "count");
+    unsigned long long left = 0;
+    if (int rc = read_dev(c, n_left, 1, &left)) return rc;
+    if (left == 0) break;  // every vertex labelled
   }
   trace_mark(st, d.dir, "pass1 (" + std::to_string(batches) + " batches, " + std::to_string(rounds_total) + " rounds)");
   return MSC_OK;
@@ -856,6 +859,10 @@ int start_early_ends(LabelCtx& c, DirLabels& d, EarlyEnds& e) {
   LCUDA(cudaMemsetAsync(e.endv, 0xFF, N * sizeof(int32_t), st), "memset");
   LCUDA(cudaMemsetAsync(c.counters + 12, 0, sizeof(int), st), "memset");
   LCUDA(cudaMemsetAsync(c.counters + 7, 0, sizeof(int), st), "memset");
+  // the iteration counters before the ends launch adds to them (the first pass leaves
+  // them alone then)
+  LCUDA(cudaMemsetAsync(c.work + 48, 0, 3 * sizeof(unsigned long long), st), "memset");
+  d.trips_zeroed = true;
   // the streamlines see the gradient the first pass sees: zero at this direction's seeds
   if (d.n_ext > 0 && !d.seeds_zeroed) {
     ::msc::count_launch();
