@@ -282,13 +282,13 @@ __device__ __forceinline__ void add_trips(unsigned long long n, unsigned long lo
 
 // Slots in a list whose length is *n for `cnt` entries of every thread of the block (one
 // atomic per block): returns the thread's first slot.  Every thread of the block calls
-// it, as often as the others (s_part: kAppendWarps + 1 ints of shared memory).  Lists
-// that most vertices enter (the boundary set, a wave's reopened neighbours: ~10^8 at
-// 512^3) made millions of atomics on one counter with an append per warp, and those
-// serialise in L2.
-constexpr int kAppendWarps = 8;  // blocks of 256 threads
+// it, as often as the others (s_part: kAppendWarps + 1 ints of shared memory; blocks
+// of whole warps).  Lists that most vertices enter (the boundary set, a wave's reopened
+// neighbours: ~10^8 at 512^3) made millions of atomics on one counter with an append
+// per warp, and those serialise in L2.
+constexpr int kAppendWarps = 32;  // up to 1024 threads
 __device__ __forceinline__ int block_append(int cnt, int* __restrict__ n, int* s_part) {
-  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = (int)(blockDim.x >> 5);
   int incl = cnt;
 #pragma unroll
   for (int o = 1; o < 32; o <<= 1) {
@@ -299,7 +299,7 @@ __device__ __forceinline__ int block_append(int cnt, int* __restrict__ n, int* s
   __syncthreads();
   if (threadIdx.x == 0) {
     int run = 0;
-    for (int j = 0; j < kAppendWarps; j++) {
+    for (int j = 0; j < nw; j++) {
       const int t = s_part[j];
       s_part[j] = run;
       run += t;
