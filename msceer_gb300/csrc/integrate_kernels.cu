@@ -685,120 +685,108 @@ __device__ __forceinline__ void mark_dirty(bool want, uint32_t v, uint32_t* __re
   if (add) list[base + __popc(m & ((1u << lane) - 1u))] = v;
 }
 
-// New alive / cut of the items in [k0, k1) from the claims (with `ibits`, only the items
-// whose bit is set, a bit per item from k0).  A changed item marks the path vertices
-// between its old and new extent in nxt: their claims are recomputed next round.
-__global__ void spec_check_kernel(const SpecSet Q, int64_t k0, int64_t k1, const uint32_t* __restrict__ claim,
-                                  const uint32_t* __restrict__ ibits, const uint32_t* __restrict__ ilist,
-                                  const unsigned long long* __restrict__ n_ilist, uint32_t* __restrict__ nxt,
-                                  uint32_t* __restrict__ nxt_list, unsigned long long* __restrict__ n_nxt) {
-  // the items: every one of the batch, or those listed in ilist (a later round)
-  const int64_t span = ilist ? (int64_t)*n_ilist : k1 - k0;
-  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-  // every lane of a warp runs the same number of loop trips (mark_dirty is warp-wide);
-  // a warp's 32 items share one word of ibits
-  for (int64_t t0 = blockIdx.x * (int64_t)blockDim.x; t0 < span; t0 += stride) {
-    const bool have = t0 + threadIdx.x < span;
-    const int64_t t = ilist ? (have ? (int64_t)ilist[t0 + threadIdx.x] : 0) : t0 + threadIdx.x;
-    const int64_t k = k0 + t;
-    const int n = have ? Q.len[k] : 0;
-    bool look = n > 0;
-    if (ibits && !ilist) look = look && ((ibits[t >> 5] >> (t & 31)) & 1u);
-    uint8_t oa = 0, na = 0;
-    int oc = -1, nc = -1;
-    bool changed = false;
-    if (look) {
-      const uint32_t kk = (uint32_t)k;
-      oa = Q.alive[k];
-      oc = Q.cut[k];
-      na = claim[Q.vtx[k]] < kk ? 0 : 1;
-      SeqWalk w(Q, k);
-      w.next();
-      for (int e = 1; e < n; e++) {
-        const uint32_t v = w.next() & ~kRec;
-        if (claim[v] < kk) {
-          nc = e;
-          break;
-        }
-      }
-      changed = na != oa || nc != oc;
-      if (changed) {
-        Q.alive[k] = na;
-        Q.cut[k] = nc;
+// New alive / cut of item t of the batch (t < 0: none; every lane of the warp calls it)
+// from the claims.  A changed item marks the path vertices between its old and new
+// extent in nxt: their claims are recomputed next round.
+__device__ __forceinline__ void check_item(const SpecSet& Q, int64_t k0, int64_t t, const uint32_t* __restrict__ claim,
+                                           uint32_t* __restrict__ nxt, uint32_t* __restrict__ nxt_list,
+                                           unsigned long long* __restrict__ n_nxt) {
+  const int64_t k = k0 + (t >= 0 ? t : 0);
+  const int n = t >= 0 ? Q.len[k] : 0;
+  const bool look = n > 0;
+  uint8_t oa = 0, na = 0;
+  int oc = -1, nc = -1;
+  bool changed = false;
+  if (look) {
+    const uint32_t kk = (uint32_t)k;
+    oa = Q.alive[k];
+    oc = Q.cut[k];
+    na = claim[Q.vtx[k]] < kk ? 0 : 1;
+    SeqWalk w(Q, k);
+    w.next();
+    for (int e = 1; e < n; e++) {
+      const uint32_t v = w.next() & ~kRec;
+      if (claim[v] < kk) {
+        nc = e;
+        break;
       }
     }
-    // the path vertices between the old and the new extent
-    const int xo = changed ? spec_extent(oa, oc, n) : 0, xn = changed ? spec_extent(na, nc, n) : 0;
-    const int lo = xo < xn ? xo : xn, hi = xo < xn ? xn : xo;
-    int trips = hi;
+    changed = na != oa || nc != oc;
+    if (changed) {
+      Q.alive[k] = na;
+      Q.cut[k] = nc;
+    }
+  }
+  // the path vertices between the old and the new extent
+  const int xo = changed ? spec_extent(oa, oc, n) : 0, xn = changed ? spec_extent(na, nc, n) : 0;
+  const int lo = xo < xn ? xo : xn, hi = xo < xn ? xn : xo;
+  int trips = hi;
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) trips = max(trips, __shfl_xor_sync(kFullMask, trips, o));
-    SeqWalk w(Q, k);
-    for (int e = 0; e < trips; e++) {
-      uint32_t u = 0;
-      if (e < hi) u = w.next();
-      mark_dirty(e >= lo && e < hi && (u & kRec), u & ~kRec, nxt, nxt_list, n_nxt);
+  for (int o = 16; o > 0; o >>= 1) trips = max(trips, __shfl_xor_sync(kFullMask, trips, o));
+  SeqWalk w(Q, k);
+  for (int e = 0; e < trips; e++) {
+    uint32_t u = 0;
+    if (e < hi) u = w.next();
+    mark_dirty(e >= lo && e < hi && (u & kRec), u & ~kRec, nxt, nxt_list, n_nxt);
+  }
+}
+
+// A resolution round's items: every one of the batch (ibits == nullptr: the first
+// round), or those whose bit is set in ibits (a bit per item from k0, ibits_words
+// words), each bit cleared as it is taken so that the bitmap is clear again after the
+// round.
+__global__ void spec_check_kernel(const SpecSet Q, int64_t k0, int64_t k1, const uint32_t* __restrict__ claim,
+                                  uint32_t* __restrict__ ibits, int64_t ibits_words, uint32_t* __restrict__ nxt,
+                                  uint32_t* __restrict__ nxt_list, unsigned long long* __restrict__ n_nxt) {
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  // every lane of a warp runs the same number of check_item calls (mark_dirty is warp-wide)
+  if (!ibits) {
+    const int64_t span = k1 - k0;
+    for (int64_t t0 = blockIdx.x * (int64_t)blockDim.x; t0 < span; t0 += stride) {
+      const int64_t t = t0 + threadIdx.x;
+      check_item(Q, k0, t < span ? t : -1, claim, nxt, nxt_list, n_nxt);
+    }
+    return;
+  }
+  for (int64_t w0 = blockIdx.x * (int64_t)blockDim.x; w0 < ibits_words; w0 += stride) {
+    const int64_t wd = w0 + threadIdx.x;
+    uint32_t m = 0;
+    if (wd < ibits_words) {
+      m = ibits[wd];
+      if (m) ibits[wd] = 0;
+    }
+    while (__any_sync(kFullMask, m != 0)) {
+      int64_t t = -1;
+      if (m) {
+        t = wd * 32 + (__ffs(m) - 1);
+        m &= m - 1;
+      }
+      check_item(Q, k0, t, claim, nxt, nxt_list, n_nxt);
     }
   }
 }
 
-// The claims of the dirty vertices, from their holders' current extents.
-__global__ void spec_reclaim_kernel(const SpecSet Q, const uint32_t* __restrict__ list,
-                                    const unsigned long long* __restrict__ n_list, uint32_t* __restrict__ claim) {
+// The claims of a round's dirty vertices from their holders' current extents, the
+// holders marked in ibits for the round's check, and the vertices' dirty bits cleared
+// (the bitmap takes the next-but-one round's marks).
+__global__ void spec_reclaim_kernel(const SpecSet Q, int64_t k0, const uint32_t* __restrict__ list,
+                                    const unsigned long long* __restrict__ n_list, uint32_t* __restrict__ bits,
+                                    uint32_t* __restrict__ claim, uint32_t* __restrict__ ibits) {
   const unsigned long long n = *n_list;
   for (unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; i < n;
        i += (unsigned long long)gridDim.x * blockDim.x) {
     const uint32_t v = list[i];
+    atomicAnd(&bits[v >> 5], ~(1u << (v & 31)));
     uint32_t m = kNoClaim;
     for (int32_t h = Q.hhead[v]; h >= 0; h = Q.hnext[h]) {
+      const int32_t k = Q.hitem[h];
+      const int64_t t = k - k0;
+      atomicOr(&ibits[t >> 5], 1u << (t & 31));
       const uint32_t ix = Q.hidx[h];
       if (!(ix & kRec)) continue;
-      const int32_t k = Q.hitem[h];
       if ((int)(ix & ~kRec) < spec_extent(Q.alive[k], Q.cut[k], Q.len[k]) && (uint32_t)k < m) m = (uint32_t)k;
     }
     claim[v] = m;
-  }
-}
-
-// The items that hold a dirty vertex (whose claim may have changed) are looked at next.
-__global__ void spec_holders_kernel(const SpecSet Q, int64_t k0, const uint32_t* __restrict__ list,
-                                    const unsigned long long* __restrict__ n_list, uint32_t* __restrict__ ibits) {
-  const unsigned long long n = *n_list;
-  for (unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; i < n;
-       i += (unsigned long long)gridDim.x * blockDim.x) {
-    for (int32_t h = Q.hhead[list[i]]; h >= 0; h = Q.hnext[h]) {
-      const int64_t t = Q.hitem[h] - k0;
-      atomicOr(&ibits[t >> 5], 1u << (t & 31));
-    }
-  }
-}
-
-// The items whose bit is set in ibits (a later round's items), as a list: a thread per
-// bitmap word, one append per warp.
-__global__ void spec_bits_list_kernel(const uint32_t* __restrict__ ibits, int64_t words, uint32_t* __restrict__ list,
-                                      unsigned long long* __restrict__ n) {
-  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-  const int lane = threadIdx.x & 31;
-  for (int64_t w0 = blockIdx.x * (int64_t)blockDim.x; w0 < words; w0 += stride) {
-    const int64_t w = w0 + threadIdx.x;
-    uint32_t m = w < words ? ibits[w] : 0u;
-    const unsigned c = __popc(m);
-    unsigned incl = c;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-      const unsigned y = __shfl_up_sync(kFullMask, incl, o);
-      if (lane >= o) incl += y;
-    }
-    const unsigned total = __shfl_sync(kFullMask, incl, 31);
-    if (!total) continue;
-    unsigned long long base = 0;
-    if (lane == 31) base = atomicAdd(n, (unsigned long long)total);
-    base = __shfl_sync(kFullMask, base, 31) + (incl - c);
-    while (m) {
-      const int b = __ffs(m) - 1;
-      m &= m - 1;
-      list[base++] = (uint32_t)(w * 32 + b);
-    }
   }
 }
 
@@ -1630,28 +1618,21 @@ cudaError_t launch_speculate(const float4* G, const VolDims& V, const IntegParam
 }
 
 cudaError_t launch_spec_round(const SpecSet& Q, int64_t k0, int64_t k1, uint32_t* claim, const SpecDirty* cur,
-                              const SpecDirty& nxt, uint32_t* ibits, int64_t ibits_words, uint32_t* ilist,
-                              unsigned long long* n_ilist, int num_sms, cudaStream_t stream) {
+                              const SpecDirty& nxt, uint32_t* ibits, int64_t ibits_words, int num_sms,
+                              cudaStream_t stream) {
   if (cudaError_t e = cudaMemsetAsync(nxt.n, 0, sizeof(unsigned long long), stream)) return e;
-  if (cudaError_t e = cudaMemsetAsync(nxt.bits, 0, nxt.words * sizeof(uint32_t), stream)) return e;
   // the first round's claims were made by the speculation, and it looks at every item
   if (!cur) {
     ::msc::count_launch();
-    spec_check_kernel<<<grid_for(k1 - k0, num_sms), 256, 0, stream>>>(Q, k0, k1, claim, nullptr, nullptr, nullptr,
-                                                                      nxt.bits, nxt.list, nxt.n);
+    spec_check_kernel<<<grid_for(k1 - k0, num_sms), 256, 0, stream>>>(Q, k0, k1, claim, nullptr, 0, nxt.bits,
+                                                                      nxt.list, nxt.n);
     return cudaGetLastError();
   }
-  if (cudaError_t e = cudaMemsetAsync(ibits, 0, ibits_words * sizeof(uint32_t), stream)) return e;
-  if (cudaError_t e = cudaMemsetAsync(n_ilist, 0, sizeof(unsigned long long), stream)) return e;
   ::msc::count_launch();
-  spec_reclaim_kernel<<<num_sms * 8, 256, 0, stream>>>(Q, cur->list, cur->n, claim);
+  spec_reclaim_kernel<<<num_sms * 8, 256, 0, stream>>>(Q, k0, cur->list, cur->n, cur->bits, claim, ibits);
   ::msc::count_launch();
-  spec_holders_kernel<<<num_sms * 8, 256, 0, stream>>>(Q, k0, cur->list, cur->n, ibits);
-  ::msc::count_launch();
-  spec_bits_list_kernel<<<grid_for(ibits_words, num_sms), 256, 0, stream>>>(ibits, ibits_words, ilist, n_ilist);
-  ::msc::count_launch();
-  spec_check_kernel<<<num_sms * 8, 256, 0, stream>>>(Q, k0, k1, claim, ibits, ilist, n_ilist, nxt.bits, nxt.list,
-                                                     nxt.n);
+  spec_check_kernel<<<grid_for(ibits_words, num_sms), 256, 0, stream>>>(Q, k0, k1, claim, ibits, ibits_words,
+                                                                        nxt.bits, nxt.list, nxt.n);
   return cudaGetLastError();
 }
 

@@ -170,23 +170,23 @@ cudaError_t launch_speculate(const float4* G, const VolDims& V, const IntegParam
 cudaError_t launch_spec_unclaim_all(const uint8_t* lvl, int stamp, uint32_t* claim, int64_t N, int num_sms,
                                     cudaStream_t stream);
 // Vertices whose claims a resolution round recomputes: a bitmap (words uint32) and the
-// list of its set bits (*n entries).
+// list of its set bits (*n entries).  The round that takes the list clears the bits.
 struct SpecDirty {
   uint32_t* bits;
   int64_t words;
   uint32_t* list;
   unsigned long long* n;
 };
-// Resolution rounds of items [k0, k1).  The first (cur == nullptr) looks at every item
-// (the speculation made its claims); a later one recomputes the claims of cur's
-// vertices from their holders and looks at the items that hold one of them (ibits: a
-// bitmap over the items, ibits_words words, cleared here, then listed in ilist /
-// n_ilist).  An item whose alive / cut changed marks the path vertices between its old
-// and new extent in nxt (cleared here first).  The rounds end when a round marks
-// nothing; a round after that one finds no items and marks nothing.
+// Resolution rounds of items [k0, k1), three stream operations each.  The first (cur ==
+// nullptr) looks at every item (the speculation made its claims); a later one
+// recomputes the claims of cur's vertices from their holders and looks at the items
+// that hold one of them (ibits: a bitmap over the items, ibits_words words, clear
+// between rounds).  An item whose alive / cut changed marks the path vertices between
+// its old and new extent in nxt (whose bitmap must be clear).  The rounds end when a
+// round marks nothing; a round after that one finds no items and marks nothing.
 cudaError_t launch_spec_round(const SpecSet& Q, int64_t k0, int64_t k1, uint32_t* claim, const SpecDirty* cur,
-                              const SpecDirty& nxt, uint32_t* ibits, int64_t ibits_words, uint32_t* ilist,
-                              unsigned long long* n_ilist, int num_sms, cudaStream_t stream);
+                              const SpecDirty& nxt, uint32_t* ibits, int64_t ibits_words, int num_sms,
+                              cudaStream_t stream);
 // Labels of the resolved batch [k0, k1), stamping its vertices with `stamp`: ptr, then
 // the write, which sets *long_chain (and writes nothing for that item) where a chain
 // of cut items is longer than it follows; pointer jumping then shortens the chains.

@@ -577,7 +577,7 @@ int first_pass(LabelCtx& c, DirLabels& d) {
   int32_t* vtx;
   uint32_t* ibits;
   unsigned long long* sc;  // [0] pool cursor [1] items [3] claimed items [4, 6) dirty-list lengths
-                           // [6] holder-node cursor [7] a round's listed items
+                           // [6] holder-node cursor
   msc::SpecSet Q{};
   const int64_t max_items = std::min<int64_t>(N, S.offset[S.nlev]);
   const int64_t ibits_cap = max_items / 32 + 1;
@@ -600,8 +600,7 @@ int first_pass(LabelCtx& c, DirLabels& d) {
   LCUDA(c.pool.get(&Q.hidx, Q.node_cap), "alloc");
   LCUDA(c.pool.get(&Q.hnext, Q.node_cap), "alloc");
   LCUDA(c.pool.get(&ibits, ibits_cap), "alloc");
-  uint32_t* ilist;
-  LCUDA(c.pool.get(&ilist, max_items + 32), "alloc");
+  LCUDA(cudaMemsetAsync(ibits, 0, (size_t)ibits_cap * sizeof(uint32_t), st), "memset");  // (clear between rounds)
   LCUDA(c.pool.get(&sc, 8), "alloc");
   LCUDA(c.pool.get(&Q.overflow, 1), "alloc");
   msc::SpecDirty dirty[2];
@@ -609,6 +608,7 @@ int first_pass(LabelCtx& c, DirLabels& d) {
     dirty[q].words = N / 32 + 1;
     dirty[q].n = sc + 4 + q;
     LCUDA(c.pool.get(&dirty[q].bits, dirty[q].words), "alloc");
+    LCUDA(cudaMemsetAsync(dirty[q].bits, 0, (size_t)dirty[q].words * sizeof(uint32_t), st), "memset");
     LCUDA(c.pool.get(&dirty[q].list, N), "alloc");
   }
   Q.vtx = vtx;
@@ -680,7 +680,7 @@ int first_pass(LabelCtx& c, DirLabels& d) {
         const int group = r < 2 ? 1 : 4;
         for (int q = 0; q < group; q++, r++)
           LCUDA(msc::launch_spec_round(Q, k0, k1, claim, r == 0 ? nullptr : &dirty[r & 1], dirty[(r + 1) & 1], ibits,
-                                       (k1 - k0) / 32 + 1, ilist, sc + 7, c.sms, st),
+                                       (k1 - k0) / 32 + 1, c.sms, st),
                 "resolve");
         unsigned long long nd = 0;
         if (int rc = read_dev(c, dirty[r & 1].n, 1, &nd)) return rc;
