@@ -895,14 +895,33 @@ __device__ __forceinline__ double clampd_ext(double v, int64_t n) {
 }
 
 struct Adv64 {
-  const double* G;  // x,y,z doubles per vertex (ComputeGradFromImage(1), zeroed at the seeds)
+  // The corner gradients are formed from the image where a voxel is entered, as
+  // ComputeGradFromImage(1) forms them (gi_regular_grid_trilinear_function.h:285-341;
+  // central_diff_kernel's f64 variant, the same operations), and are zero at the
+  // vertices whose bit `zeroed` sets (SetGradExplicit at the seeds): the few FP64
+  // streamlines do not need the gradient of every vertex stored in FP64.
+  const float* f;
+  const uint32_t* zeroed;
   VolDims V;
   IntegParams P;
   const uint8_t* state;  // fix-up stop: certain terminal
 
   __device__ __forceinline__ D3 corner(int64_t x, int64_t y, int64_t z) const {
-    const double* p = G + 3 * vid(V, x, y, z);
-    return {p[0], p[1], p[2]};
+    const int64_t v = vid(V, x, y, z);
+    if ((zeroed[v >> 5] >> (v & 31)) & 1u) return {0.0, 0.0, 0.0};
+    const float c = __ldg(f + v);
+    // 0 + (-0.5f * f[-1]) + (0.0f * f[0]) + (0.5f * f[+1]), each product a float, summed
+    // in double; 0 + (0.0f * f[0]) on a first or last plane
+    auto comp = [&](bool inside, int64_t s) -> double {
+      if (!inside) return 0.0 + (double)(0.0f * c);
+      const float a = __ldg(f + v - s), b = __ldg(f + v + s);
+      double r = 0.0;
+      r += (double)(-0.5f * a);
+      r += (double)(0.0f * c);
+      r += (double)(0.5f * b);
+      return r;
+    };
+    return {comp(x > 0 && x < V.X - 1, 1), comp(y > 0 && y < V.Y - 1, V.X), comp(z > 0 && z < V.Z - 1, V.X * V.Y)};
   }
   __device__ __forceinline__ void surround(const int64_t b[3], bool clamp, D3 c[8]) const {
     int64_t vv[3][2];
@@ -1675,11 +1694,12 @@ cudaError_t launch_boundary_set(const int32_t* lab, const uint8_t* state, const 
   return cudaGetLastError();
 }
 
-cudaError_t launch_fixup_end64(const double* G, const VolDims& V, const IntegParams& P, const uint8_t* state,
+cudaError_t launch_fixup_end64(const float* f, const uint32_t* zeroed, const VolDims& V, const IntegParams& P,
+                               const uint8_t* state,
                                const int64_t* list, int n, int32_t* endv, unsigned long long* work,
                                unsigned long long* trips, int num_sms, cudaStream_t stream, const int* n_dev) {
   if (n <= 0) return cudaSuccess;
-  Adv64 A{G, V, P, state};
+  Adv64 A{f, zeroed, V, P, state};
   const int blocks = (n + 31) / 32;
   if (cudaError_t e = cudaMemsetAsync(work, 0, sizeof(unsigned long long), stream)) return e;
   ::msc::count_launch();

@@ -201,7 +201,9 @@ cudaError_t launch_boundary_set(const int32_t* lab, const uint8_t* state, const 
 // streamline to a certain terminal region.  The FP32 kernel lists the streamlines whose
 // ending is ambiguous in amb (amb_mode: see the kernel) instead.  `work`: a device
 // counter of claimed items, zeroed by the launchers.
-cudaError_t launch_fixup_end64(const double* G, const VolDims& V, const IntegParams& P, const uint8_t* state,
+// f: the image; zeroed: a bit per vertex whose gradient is zero (the seeds)
+cudaError_t launch_fixup_end64(const float* f, const uint32_t* zeroed, const VolDims& V, const IntegParams& P,
+                               const uint8_t* state,
                                const int64_t* list, int n, int32_t* endv, unsigned long long* work,
                                unsigned long long* trips, int num_sms, cudaStream_t stream, const int* n_dev = nullptr);
 // n_dev (optional): the list's length in device memory, n then only sizes the grid

@@ -130,14 +130,13 @@ __global__ void snapshot_kernel(const int32_t* lab, int32_t* out, int64_t n) {
 __global__ void scatter_rep_kernel(const int32_t* pairs, int m, int32_t* rep) {
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < m; i += gridDim.x * blockDim.x) rep[pairs[2 * i]] = pairs[2 * i + 1];
 }
-// SetGradExplicit(seed, 0) (gi_numeric_integrator_path_compressing.h:118-123), both copies
-__global__ void zero_seed_grad_kernel(const int64_t* seed, int n, float4* g32, double* g64) {
+// SetGradExplicit(seed, 0) (gi_numeric_integrator_path_compressing.h:118-123): the FP32
+// gradient, and the bit that makes the FP64 advector's corner gradient zero
+__global__ void zero_seed_grad_kernel(const int64_t* seed, int n, float4* g32, uint32_t* zeroed) {
   for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < n; e += gridDim.x * blockDim.x) {
     const int64_t s = seed[e];
     g32[s] = make_float4(0.f, 0.f, 0.f, 0.f);
-    g64[3 * s] = 0.0;
-    g64[3 * s + 1] = 0.0;
-    g64[3 * s + 2] = 0.0;
+    atomicOr(&zeroed[s >> 5], 1u << (s & 31));
   }
 }
 
@@ -270,7 +269,7 @@ struct LabelCtx {
   const uint8_t* grad = nullptr;
   const msc_integ_params* p = nullptr;
   float4* g32 = nullptr;
-  double* g64 = nullptr;
+  uint32_t* zeroed = nullptr;  // a bit per vertex whose gradient is zeroed (the FP64 advector's)
   int32_t* key = nullptr;
   int64_t *ext_cells = nullptr, *saddles = nullptr, *list_a = nullptr, *list_b = nullptr, *amb = nullptr;
   int64_t* list_c = nullptr;  // a fix-up wave's members without a streamline end yet
@@ -343,7 +342,7 @@ int setup_ctx(LabelCtx& c, const float* f, const uint8_t* grad, const int64_t* d
   c.ntiles = msc::terminal_num_tiles(c.V);
   const int64_t N = c.N;
   LCUDA(c.pool.get(&c.g32, N), "alloc");
-  LCUDA(c.pool.get(&c.g64, 3 * N), "alloc");
+  LCUDA(c.pool.get(&c.zeroed, N / 32 + 1), "alloc");
   LCUDA(c.pool.get(&c.key, N), "alloc");
   LCUDA(c.pool.get(&c.ext_cells, N), "alloc");
   LCUDA(c.pool.get(&c.saddles, 3 * N), "alloc");
@@ -362,7 +361,7 @@ int setup_ctx(LabelCtx& c, const float* f, const uint8_t* grad, const int64_t* d
     GD.d[a] = 2 * dims[a] - 1;
   }
   LCUDA(msc::launch_central_diff(3, 1, f, c.g32, GD, c.sms, c.st), "gradient f32");
-  LCUDA(msc::launch_central_diff(3, 2, f, c.g64, GD, c.sms, c.st), "gradient f64");
+  LCUDA(cudaMemsetAsync(c.zeroed, 0, (size_t)(N / 32 + 1) * sizeof(uint32_t), c.st), "memset");
   return MSC_OK;
 }
 
@@ -556,7 +555,7 @@ int first_pass(LabelCtx& c, DirLabels& d) {
   cudaStream_t st = c.st;
   if (d.n_ext > 0 && !d.seeds_zeroed) {
     ::msc::count_launch();
-    zero_seed_grad_kernel<<<(d.n_ext + 255) / 256, 256, 0, st>>>(d.seed, d.n_ext, c.g32, c.g64);
+    zero_seed_grad_kernel<<<(d.n_ext + 255) / 256, 256, 0, st>>>(d.seed, d.n_ext, c.g32, c.zeroed);
     d.seeds_zeroed = true;
   }
   const msc::IntegParams P = integ_params(c.p, d.dir);
@@ -779,14 +778,14 @@ int finish_direction(LabelCtx& c, DirLabels& d, int32_t* out, int32_t* stage_int
     int n_amb = 0;
     if (p->precision == 1) {
       n_amb = n_todo;
-      LCUDA(msc::launch_fixup_end64(c.g64, V, P, d.state, todo, n_todo, endv, c.work, c.work + 50, sms, st), "fix-up");
+      LCUDA(msc::launch_fixup_end64(c.f, c.zeroed, V, P, d.state, todo, n_todo, endv, c.work, c.work + 50, sms, st), "fix-up");
     } else if (n_todo > 0) {
       LCUDA(msc::launch_fixup_end32(c.g32, V, P, d.lab, d.state, todo, n_todo, endv, c.amb, c.counters + 7,
                                     p->precision == 2 ? 2 : 0, c.work, c.work + 49, sms, st),
             "fix-up");
       if (int rc = read_dev(c, c.counters + 7, 1, &n_amb)) return rc;
       trace_mark(st, d.dir, "  fp32 ends");
-      LCUDA(msc::launch_fixup_end64(c.g64, V, P, d.state, c.amb, n_amb, endv, c.work + 56, c.work + 50, sms, st),
+      LCUDA(msc::launch_fixup_end64(c.f, c.zeroed, V, P, d.state, c.amb, n_amb, endv, c.work + 56, c.work + 50, sms, st),
             "fix-up FP64");
       trace_mark(st, d.dir, "  fp64 ends");
     }
@@ -866,7 +865,7 @@ int start_early_ends(LabelCtx& c, DirLabels& d, EarlyEnds& e) {
   // the streamlines see the gradient the first pass sees: zero at this direction's seeds
   if (d.n_ext > 0 && !d.seeds_zeroed) {
     ::msc::count_launch();
-    zero_seed_grad_kernel<<<(d.n_ext + 255) / 256, 256, 0, st>>>(d.seed, d.n_ext, c.g32, c.g64);
+    zero_seed_grad_kernel<<<(d.n_ext + 255) / 256, 256, 0, st>>>(d.seed, d.n_ext, c.g32, c.zeroed);
     d.seeds_zeroed = true;
   }
   if (!c.ends_st) {
@@ -882,7 +881,7 @@ int start_early_ends(LabelCtx& c, DirLabels& d, EarlyEnds& e) {
                                 c.p->precision == 2 ? 2 : 0, c.work, c.work + 49, c.sms, c.ends_st, c.counters + 12),
         "fix-up ends");
   // and in FP64 the ones whose FP32 ending was ambiguous (their count stays on the device)
-  LCUDA(msc::launch_fixup_end64(c.g64, c.V, P, d.state, c.amb, 1, e.endv, c.work + 56, c.work + 50, c.sms, c.ends_st,
+  LCUDA(msc::launch_fixup_end64(c.f, c.zeroed, c.V, P, d.state, c.amb, 1, e.endv, c.work + 56, c.work + 50, c.sms, c.ends_st,
                                 c.counters + 7),
         "fix-up FP64 ends");
   LCUDA(cudaEventRecord(c.ends_done, c.ends_st), "cudaEventRecord");
@@ -987,7 +986,7 @@ void run_dsc_job(int dev, cudaEvent_t inputs_ready, const float* f, const uint8_
         if (asc->n > 0) {
           LCUDA(cudaStreamWaitEvent(sb, asc->done, 0), "cudaStreamWaitEvent");
           ::msc::count_launch();
-          zero_seed_grad_kernel<<<(asc->n + 255) / 256, 256, 0, sb>>>(asc->seed, asc->n, c.g32, c.g64);
+          zero_seed_grad_kernel<<<(asc->n + 255) / 256, 256, 0, sb>>>(asc->seed, asc->n, c.g32, c.zeroed);
         }
         trace_mark(sb, 1, "asc seeds zeroed");
         return MSC_OK;
