@@ -778,14 +778,16 @@ int finish_direction(LabelCtx& c, DirLabels& d, int32_t* out, int32_t* stage_int
     int n_amb = 0;
     if (p->precision == 1) {
       n_amb = n_todo;
-      LCUDA(msc::launch_fixup_end64(c.f, c.zeroed, V, P, d.state, todo, n_todo, endv, c.work, c.work + 50, sms, st), "fix-up");
+      LCUDA(msc::launch_fixup_end64(c.f, c.zeroed, V, P, d.state, todo, n_todo, endv, c.work, c.work + 50, sms, st),
+            "fix-up");
     } else if (n_todo > 0) {
       LCUDA(msc::launch_fixup_end32(c.g32, V, P, d.lab, d.state, todo, n_todo, endv, c.amb, c.counters + 7,
                                     p->precision == 2 ? 2 : 0, c.work, c.work + 49, sms, st),
             "fix-up");
       if (int rc = read_dev(c, c.counters + 7, 1, &n_amb)) return rc;
       trace_mark(st, d.dir, "  fp32 ends");
-      LCUDA(msc::launch_fixup_end64(c.f, c.zeroed, V, P, d.state, c.amb, n_amb, endv, c.work + 56, c.work + 50, sms, st),
+      LCUDA(msc::launch_fixup_end64(c.f, c.zeroed, V, P, d.state, c.amb, n_amb, endv, c.work + 56, c.work + 50, sms,
+                                    st),
             "fix-up FP64");
       trace_mark(st, d.dir, "  fp64 ends");
     }
@@ -881,8 +883,8 @@ int start_early_ends(LabelCtx& c, DirLabels& d, EarlyEnds& e) {
                                 c.p->precision == 2 ? 2 : 0, c.work, c.work + 49, c.sms, c.ends_st, c.counters + 12),
         "fix-up ends");
   // and in FP64 the ones whose FP32 ending was ambiguous (their count stays on the device)
-  LCUDA(msc::launch_fixup_end64(c.f, c.zeroed, c.V, P, d.state, c.amb, 1, e.endv, c.work + 56, c.work + 50, c.sms, c.ends_st,
-                                c.counters + 7),
+  LCUDA(msc::launch_fixup_end64(c.f, c.zeroed, c.V, P, d.state, c.amb, 1, e.endv, c.work + 56, c.work + 50, c.sms,
+                                c.ends_st, c.counters + 7),
         "fix-up FP64 ends");
   LCUDA(cudaEventRecord(c.ends_done, c.ends_st), "cudaEventRecord");
   e.on = true;
