@@ -24,6 +24,12 @@
  * The reference numbers regions by "unique id" in unordered_map iteration order, so
  * label values carry no meaning across runs; this oracle names every region by its
  * smallest seed vertex (the extremum vertex when nothing merged), -1 = unlabelled.
+ *
+ * Also the saddle streamline digitizers of the needASC1 / needDSC1 modes
+ * (ondemandaccurate.cxx:254-505, gi_numeric_streamline_integrator.h:525-1080) at one
+ * thread, on the same advector with the TerminateNearAssignedHex / Vert checkers
+ * (gi_advection_checker.h:60-100): oracle_saddle_lines_3d, equal byte for byte to the
+ * reference compiled here (oracle/ref_harness_lines.cpp, tests/golden/saddle_lines.json).
  */
 #include "msc_oracle.h"
 
@@ -398,6 +404,11 @@ typedef struct {
 	float ethresh, gthresh;
 	double max_step;
 	int step_mult;            /* StepMultiplier: -1 ascending (downhill), +1 descending */
+	/* the saddle-line digitizers' checkers (cell_mode 1: TerminateNearAssignedHex,
+	 * 2: TerminateNearAssignedVert, gi_advection_checker.h:60-100), over cells[] */
+	const uint8_t* cells;
+	int cell_target;
+	int cell_mode;
 } adv_t;
 
 static inline v3d vload(const double* G, int64_t v) { v3d r = { G[3 * v], G[3 * v + 1], G[3 * v + 2] }; return r; }
@@ -447,6 +458,18 @@ static int64_t nearest_vertex(const lctx* c, v3d p, int clamp) {
 }
 
 static int checker(const adv_t* A, v3d np, int clamp) {
+	if (A->cell_mode) {
+		/* nearboundary: stop at once; else the hex holding the point (floor * 2 + 1) or
+		 * the vertex nearest it (floor(p + 0.5) * 2) carries the target label */
+		if (clamp) return EV_HIT_PREASSIGNED;
+		const lctx* c = A->c;
+		const double p[3] = { np.x, np.y, np.z };
+		int64_t k[3];
+		for (int a = 0; a < 3; a++)
+			k[a] = A->cell_mode == 1 ? (int64_t)floor(p[a]) * 2 + 1 : (int64_t)floor(p[a] + 0.5) * 2;
+		const int64_t id = k[0] + c->dX * (k[1] + c->dY * k[2]);
+		return A->cells[id] == A->cell_target ? EV_HIT_PREASSIGNED : EV_NONE;
+	}
 	int64_t id = nearest_vertex(A->c, np, clamp);
 	uint8_t t = A->desttype[id];
 	if (A->terminal_only) return t == DT_CERTAIN_TERMINAL ? EV_HIT_PREASSIGNED : EV_NONE;
@@ -540,6 +563,177 @@ static int64_t trace(const adv_t* A, int64_t v, int limit, int64_t** path, int64
 	}
 }
 
+/* ---- saddle streamline digitizers (ondemandaccurate needASC1 / needDSC1) ----------
+ *
+ * ondemandaccurate.cxx:254-382 (ReIntegrateUpFrom2Saddles) and :383-505
+ * (ReIntegrateDownFrom1Saddles) at one thread, with
+ * DigitizingNumericStreamlineIntegrator3dASC / 3dDSC (gi_numeric_streamline_integrator.h:
+ * 525-796, 797-1080): saddles in decreasing value (ascending lines from 2-saddles) or
+ * increasing value (descending lines from 1-saddles), ties by decreasing cell id; around
+ * each saddle a breadth-first walk of at most five cells through its cofacets (facets)
+ * and their pairs collects the hexes (vertices) to start streamlines from, at their
+ * centroids; every streamline labels the hex-face-hex (vertex-edge-vertex) chain it
+ * crosses with the target label, each segment stopping at the first cell already
+ * labelled, and stops itself near a labelled hex (vertex) or near the boundary; then
+ * the saddle itself takes the label. */
+
+/* DigitizeSegmentInternal: the segment a -> b of one voxel advection (its result is not
+ * used by the caller) */
+static void digitize_segment(const lctx* c, v3d a0, v3d b0, int dsc, uint8_t* cells, int target) {
+	double a[3] = { a0.x, a0.y, a0.z }, b[3] = { b0.x, b0.y, b0.z };
+	if (dsc) for (int d = 0; d < 3; d++) { a[d] += 0.5; b[d] += 0.5; }
+	const double a2b[3] = { b[0] - a[0], b[1] - a[1], b[2] - a[2] };
+	int64_t idx[3];
+	double tt[3];
+	int n = 0;
+	for (int d = 0; d < 3; d++) {
+		const int va = (int)floor(a[d]), vb = (int)floor(b[d]);
+		if (va == vb) continue;
+		const int plane = va > vb ? va : vb;
+		const double t = ((double)plane - a[d]) / (b[d] - a[d]);
+		tt[n] = t;
+		if (t < 0 || t > 1) return;
+		int64_t k[3];
+		for (int e = 0; e < 3; e++) {
+			const double q = a2b[e] * t;
+			k[e] = (int64_t)floor(q + a[e]) * 2 + (e == d ? 0 : 1) - (dsc ? 1 : 0);
+		}
+		idx[n++] = k[0] + c->dX * (k[1] + c->dY * k[2]);
+	}
+	if (n == 0) return;
+	for (int i = 0; i < n; i++)
+		for (int j = i; j < n; j++)
+			if (tt[i] > tt[j]) {
+				int64_t ti = idx[i]; idx[i] = idx[j]; idx[j] = ti;
+				double td = tt[i]; tt[i] = tt[j]; tt[j] = td;
+			}
+	int64_t start;
+	{
+		int64_t k[3];
+		for (int e = 0; e < 3; e++) k[e] = (int64_t)floor(a[e]) * 2 + (dsc ? 0 : 1);
+		start = k[0] + c->dX * (k[1] + c->dY * k[2]);
+	}
+	for (int i = 0; i < n; i++) {
+		const int64_t face = idx[i];
+		int64_t around[6];
+		const int m = dsc ? cfacets(c, face, around) : ccofacets(c, face, around);
+		int has_start = 0;
+		int64_t next = -1;
+		for (int j = 0; j < m; j++) {
+			if (around[j] == start) has_start = 1;
+			else next = around[j];
+		}
+		if (!has_start) continue;
+		if (cells[start] == target) return;
+		cells[start] = (uint8_t)target;
+		if (cells[face] == target) return;
+		cells[face] = (uint8_t)target;
+		start = next;
+	}
+}
+
+/* IntegrateStreamline of the digitizing integrators, from `seed` (grid coordinates) */
+static void digitize_streamline(const adv_t* A, v3d seed, int limit, uint8_t* cells, int target) {
+	const lctx* c = A->c;
+	int64_t x = (int64_t)(seed.x + 0.5), y = (int64_t)(seed.y + 0.5), z = (int64_t)(seed.z + 0.5);
+	v3d cur = seed;
+	int iters = limit;
+	for (;;) {
+		const v3d old = cur;
+		int ev;
+		if (dist_to_boundary(c, x, y, z) <= 1) {
+			ev = advect(A, &cur, &iters, 1);
+			v3d q = { clampd(cur.x + 0.5, c->X), clampd(cur.y + 0.5, c->Y), clampd(cur.z + 0.5, c->Z) };
+			x = (int64_t)q.x; y = (int64_t)q.y; z = (int64_t)q.z;
+		} else {
+			ev = advect(A, &cur, &iters, 0);
+			x = (int64_t)(cur.x + 0.5); y = (int64_t)(cur.y + 0.5); z = (int64_t)(cur.z + 0.5);
+			digitize_segment(c, old, cur, A->cell_mode == 2, cells, target);
+		}
+		if (ev == EV_LOW_GRADIENT || ev == EV_HIT_EXTREMUM || ev == EV_HIT_PREASSIGNED || ev == EV_OVER_MAX_ITERATIONS)
+			return;
+	}
+}
+
+typedef struct { float key; int64_t id; } crit_t;
+static int crit_less(const void* pa, const void* pb) {  /* std::pair<float, INDEX_TYPE> order */
+	const crit_t* a = (const crit_t*)pa;
+	const crit_t* b = (const crit_t*)pb;
+	if (a->key < b->key) return -1;
+	if (b->key < a->key) return 1;
+	return (a->id > b->id) - (a->id < b->id);
+}
+
+/* a small set of cell ids (the breadth-first walk visits at most a few dozen) */
+typedef struct { int64_t v[256]; int n; } cellset_t;
+static int cs_has(const cellset_t* s, int64_t id) {
+	for (int i = 0; i < s->n; i++) if (s->v[i] == id) return 1;
+	return 0;
+}
+static void cs_add(cellset_t* s, int64_t id) {
+	if (!cs_has(s, id) && s->n < 256) s->v[s->n++] = id;
+}
+
+/* dsc 0: ascending lines from the 2-saddles (target labels on hexes and faces);
+ * 1: descending lines from the 1-saddles (vertices and edges) */
+static void saddle_lines(const lctx* c, const double* G, const oracle_label_params* P, int dsc, uint8_t* cells,
+                         int target) {
+	const int64_t NC = c->dX * c->dY * c->dZ;
+	const int sdim = dsc ? 1 : 2, tdim = dsc ? 0 : 3;
+	int64_t nc = 0, cap = 1024;
+	crit_t* cr = (crit_t*)malloc(sizeof(crit_t) * (size_t)cap);
+	for (int64_t id = 0; id < NC; id++) {
+		int64_t k[3];
+		ccoords(c, id, k);
+		if (cdim(k) != sdim || !gcrit(c, id)) continue;
+		if (nc == cap) { cap *= 2; cr = (crit_t*)realloc(cr, sizeof(crit_t) * (size_t)cap); }
+		const float v = c->f[highest_vertex(c, id)];
+		cr[nc].key = dsc ? -1 * v : v;
+		cr[nc].id = id;
+		nc++;
+	}
+	qsort(cr, (size_t)nc, sizeof(crit_t), crit_less);
+	adv_t A = { c, G, NULL, 0, P->error_threshold, P->gradient_threshold, P->max_step, dsc ? -1 : 1,
+	            cells, target, dsc ? 2 : 1 };
+	for (int64_t li = nc - 1; li >= 0; li--) {
+		const int64_t sad = cr[li].id;
+		int64_t result[256], queue[256];
+		int nr = 0, qh = 0, qt = 0;
+		cellset_t visited;
+		visited.n = 0;
+		queue[qt++] = sad;
+		for (int counter = 4; qh < qt && counter >= 0; counter--) {
+			const int64_t cur = queue[qh++];
+			cs_add(&visited, cur);
+			int64_t around[6];
+			const int m = dsc ? cfacets(c, cur, around) : ccofacets(c, cur, around);
+			for (int j = 0; j < m; j++) {
+				const int64_t t = around[j];
+				if (cs_has(&visited, t)) continue;
+				if (gcrit(c, t)) {
+					if (nr < 256) result[nr++] = t;
+					cs_add(&visited, t);
+				} else {
+					const int64_t pr = gpair(c, t);
+					if (nr < 256) result[nr++] = t;
+					cs_add(&visited, t);
+					cs_add(&visited, pr);
+					if (qt < 256) queue[qt++] = pr;
+				}
+			}
+		}
+		for (int i = 0; i < nr; i++) {
+			int64_t k[3];
+			ccoords(c, result[i], k);
+			if (cdim(k) != tdim) continue;
+			const v3d seed = { (double)k[0] * 0.5, (double)k[1] * 0.5, (double)k[2] * 0.5 };
+			digitize_streamline(&A, seed, P->iteration_limit, cells, target);
+		}
+		cells[sad] = (uint8_t)target;
+	}
+	free(cr);
+}
+
 static int cmp_i64(const void* a, const void* b) {
 	int64_t x = *(const int64_t*)a, y = *(const int64_t*)b;
 	return (x > y) - (x < y);
@@ -552,7 +746,8 @@ static void integrate(const lctx* c, double* G, int32_t* lab, const int64_t* zer
 	uint8_t* dt = (uint8_t*)malloc((size_t)N);
 	for (int64_t i = 0; i < N; i++) dt[i] = lab[i] == -1 ? DT_UNASSIGNED : DT_CERTAIN_TERMINAL;
 	for (int64_t i = 0; i < nzero; i++) { G[3 * zero_grad[i]] = 0; G[3 * zero_grad[i] + 1] = 0; G[3 * zero_grad[i] + 2] = 0; }
-	adv_t A = { c, G, dt, 0, P->error_threshold, P->gradient_threshold, P->max_step, c->dir < 0 ? -1 : 1 };
+	adv_t A = { c, G, dt, 0, P->error_threshold, P->gradient_threshold, P->max_step, c->dir < 0 ? -1 : 1,
+	            NULL, 0, 0 };
 	int64_t pcap = 256, plen;
 	int64_t* path = (int64_t*)malloc(sizeof(int64_t) * (size_t)pcap);
 	/* first pass, strided visiting order (:166-174) with one thread */
@@ -763,5 +958,19 @@ int oracle_labels_3d(const float* f, const uint8_t* grad, int64_t X, int64_t Y, 
 		free(canon);
 	}
 	free(G); free(start); free(seeds);
+	return 0;
+}
+
+int oracle_saddle_lines_3d(const float* f, const uint8_t* grad, int64_t X, int64_t Y, int64_t Z, int which,
+                           const oracle_label_params* P, uint8_t* cells) {
+	if (!P || !cells || X < 2 || Y < 2 || Z < 2) return -1;
+	const int64_t N = X * Y * Z;
+	double* G = (double*)malloc(sizeof(double) * 3 * (size_t)N);
+	oracle_central_diff_3d(f, X, Y, Z, G);
+	lctx c;
+	ctx_init(&c, f, grad, X, Y, Z, 1);
+	if (which & 1) saddle_lines(&c, G, P, 0, cells, 4);
+	if (which & 2) saddle_lines(&c, G, P, 1, cells, 5);
+	free(G);
 	return 0;
 }

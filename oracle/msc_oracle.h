@@ -77,6 +77,14 @@ int oracle_labels_3d(const float* f, const uint8_t* grad, int64_t X, int64_t Y, 
                      const oracle_label_params* P, int32_t* labels_asc, int32_t* labels_dsc,
                      int32_t* stage_labels);
 
+/* The saddle streamline digitizers of ondemandaccurate's needASC1 / needDSC1 modes at one
+ * thread on the gradient of f (no seed zeroed): which bit 0 the ascending lines from the
+ * 2-saddles (label 4 on hexes and faces), bit 1 the descending lines from the 1-saddles
+ * (label 5 on vertices and edges), in that order, into cells (one byte per cell, in and
+ * out).  Test infrastructure. */
+int oracle_saddle_lines_3d(const float* f, const uint8_t* grad, int64_t X, int64_t Y, int64_t Z, int which,
+                           const oracle_label_params* P, uint8_t* cells);
+
 #ifdef __cplusplus
 }
 #endif

@@ -17,6 +17,8 @@
 //       needASC2 = needDSC2 = 1: VertexLabelingToBoundaryLabeling::ComputeMINBoundary /
 //       ComputeMAXBoundary, the constrained MyRobinsNoalloc<...,4,6>::ComputeLowerStar of
 //       the touched vertices and RecordGrad (:693-699)
+//   ref_saddle_lines_3d    == ondemandaccurate/ondemandaccurate.cxx:254-505 at one thread
+//       (in ref_harness_lines.cpp)
 //   ref_ms_graph_3d        == extractmsc/extractmsc.cxx:482-504: a .grad loaded into
 //       DiscreteGradientLabeling, LazyMaximumVertexLabeling + TopologicalMaxVertexMeshFunction,
 //       MorseSmaleComplexBasic::ComputeFromGrad with the given arc build flags and no

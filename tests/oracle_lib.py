@@ -49,6 +49,22 @@ class Oracle:
         lib.oracle_conform_3d.argtypes = [_VP, _I64, _I64, _I64, _VP, _VP, ctypes.c_int]
         lib.oracle_ms_graph_3d.argtypes = [_VP, _VP, _I64, _I64, _I64, _VP, _I64, _VP, _VP, _VP, _VP, _I64, _VP, _VP,
                                            _VP, _VP]
+        lib.oracle_saddle_lines_3d.argtypes = [_VP, _VP, _I64, _I64, _I64, ctypes.c_int, ctypes.POINTER(LabelParams),
+                                               _VP]
+
+    def saddle_lines(self, f, grad, which, error_threshold, gradient_threshold, iteration_limit, max_step,
+                     cells=None):
+        """ondemandaccurate's saddle streamline digitizers (which: 1 ascending from the
+        2-saddles, label 4; 2 descending from the 1-saddles, label 5; 3 both) at one
+        thread, into a copy of `cells` (one byte per cell; zeros when not given)."""
+        f = np.ascontiguousarray(f, dtype=np.float32)
+        grad = np.ascontiguousarray(grad, dtype=np.uint8)
+        nc = int(np.prod([2 * d - 1 for d in f.shape]))
+        out = np.zeros(nc, np.uint8) if cells is None else np.array(cells, dtype=np.uint8, copy=True)
+        p = LabelParams(error_threshold, gradient_threshold, iteration_limit, max_step, 0.0)
+        assert self.lib.oracle_saddle_lines_3d(f.ctypes.data, grad.ctypes.data, *f.shape[::-1], which,
+                                               ctypes.byref(p), out.ctypes.data) == 0
+        return out
 
     def labels(self, f, grad, error_threshold, gradient_threshold, iteration_limit, max_step, presimp):
         """ASC and DSC labels (regions named by their smallest seed vertex) plus stages."""
@@ -197,7 +213,21 @@ def load_ref():
     lib.ref_ondemand_3d.argtypes = [_VP, ctypes.c_longlong, ctypes.c_longlong, ctypes.c_longlong, ctypes.c_float,
                                     ctypes.c_float, ctypes.c_int, ctypes.c_float, _VP, _VP, _VP, ctypes.c_int,
                                     ctypes.c_char_p, _VP]
+    if hasattr(lib, "ref_saddle_lines_3d"):
+        lib.ref_saddle_lines_3d.argtypes = [_VP, ctypes.c_longlong, ctypes.c_longlong, ctypes.c_longlong,
+                                            ctypes.c_int, ctypes.c_float, ctypes.c_float, ctypes.c_int, _VP]
     return lib
+
+
+def ref_saddle_lines(lib, f, which, error_threshold, gradient_threshold, iteration_limit, cells=None):
+    """The reference's saddle streamline digitizers at one thread (built with
+    MAX_STEP_IN_GRID_CELLS = 0.25), as Oracle.saddle_lines returns them."""
+    f = np.ascontiguousarray(f, dtype=np.float32)
+    nc = int(np.prod([2 * d - 1 for d in f.shape]))
+    out = np.zeros(nc, np.uint8) if cells is None else np.array(cells, dtype=np.uint8, copy=True)
+    assert lib.ref_saddle_lines_3d(f.ctypes.data, *f.shape[::-1], which, error_threshold, gradient_threshold,
+                                   iteration_limit, out.ctypes.data) == 0
+    return out
 
 
 def ref_labels(lib, f, error_threshold, gradient_threshold, iteration_limit, presimp):

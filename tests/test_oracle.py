@@ -168,3 +168,48 @@ def test_ms_graph_oracle_against_reference(oracle, build):
         want = oracle_lib.ref_ms_graph(ref, f, g, build)
         for k in want:
             assert np.array_equal(got[k], want[k]), k
+
+
+SADDLE_LINES_CASES = json.loads((GOLDEN / "saddle_lines.json").read_text())
+
+
+def _preset_cells(nc, spec):
+    cells = np.zeros(nc, np.uint8)
+    if spec is None:
+        return cells
+    rng = np.random.default_rng(spec[0])
+    idx = rng.choice(nc, nc // spec[1], replace=False)
+    cells[idx] = rng.choice(np.array([1, 2, 4, 5], np.uint8), idx.size)
+    return cells
+
+
+@pytest.mark.parametrize("key", sorted(SADDLE_LINES_CASES))
+def test_saddle_lines_oracle_against_golden(oracle, key):
+    """ondemandaccurate's saddle streamline digitizers (needASC1 / needDSC1) restated:
+    the cell labels equal the reference's, by SHA-256 (on the same floats of f)."""
+    spec = SADDLE_LINES_CASES[key]
+    f = _regenerate(spec).astype(np.float32)
+    g = oracle.grad(f)
+    assert hashlib.sha256(g.tobytes()).hexdigest() == spec["grad_sha256"]
+    if hashlib.sha256(f.tobytes()).hexdigest() != spec["f_sha256"]:
+        pytest.skip("this host regenerates other floats for the field (FFT); the streamlines follow them")
+    gt = 1e-6 * float(np.abs(f).max())
+    got = oracle.saddle_lines(f, g, spec["which"], 1e-4, gt, 4000, 0.25, _preset_cells(g.size, spec["preset"]))
+    assert int((got > 0).sum()) == spec["labelled"]
+    assert hashlib.sha256(got.tobytes()).hexdigest() == spec["sha256"]
+
+
+@pytest.mark.parametrize("which", [1, 2, 3])
+def test_saddle_lines_oracle_against_reference(oracle, which):
+    ref = oracle_lib.load_ref()
+    if ref is None or not hasattr(ref, "ref_saddle_lines_3d"):
+        pytest.skip("the reference is not compiled on this machine")
+    for f, preset in ((fields.power_law_field((30, 26, 22), seed=13), None),
+                      (fields.gaussian_sum((28, 24, 20), 10, seed=14), (5, 50))):
+        g = oracle.grad(f)
+        gt = 1e-6 * float(np.abs(f).max())
+        cells = _preset_cells(g.size, preset)
+        got = oracle.saddle_lines(f, g, which, 1e-4, gt, 4000, 0.25, cells)
+        want = oracle_lib.ref_saddle_lines(ref, f, which, 1e-4, gt, 4000, cells)
+        assert (want > 0).sum() > 0
+        assert np.array_equal(got, want), int((got != want).sum())
