@@ -974,3 +974,51 @@ int oracle_saddle_lines_3d(const float* f, const uint8_t* grad, int64_t X, int64
 	free(G);
 	return 0;
 }
+
+/* ondemandaccurate's accurate .grad for the flags a1 d1 a2 d2 (needASC1, needDSC1,
+ * needASC2, needDSC2) at one thread (ondemandaccurate.cxx:772-1145): the 3-manifold
+ * labels asked for (ascending before descending, each zeroing the gradient at its
+ * seeds) and their boundaries (oracle_boundary_labels_3d), then the saddle lines on the
+ * gradient those integrations left, then the re-pairing and the ldir stage
+ * (oracle_conform_3d).  restrict_out: the restriction labels, one byte per cell;
+ * grad_out: the .grad.  Test infrastructure. */
+int oracle_ondemand_grad_3d(const float* f, const uint8_t* grad, int64_t X, int64_t Y, int64_t Z,
+                            const oracle_label_params* P, int a1, int d1, int a2, int d2, uint8_t* restrict_out,
+                            uint8_t* grad_out) {
+	if (!P || !restrict_out || !grad_out || X < 2 || Y < 2 || Z < 2) return -1;
+	const int64_t N = X * Y * Z, NC = (2 * X - 1) * (2 * Y - 1) * (2 * Z - 1);
+	memset(restrict_out, 0, (size_t)NC);
+	memcpy(grad_out, grad, (size_t)NC);
+	if (!(a1 || d1 || a2 || d2)) return 0;
+	double* G = (double*)malloc(sizeof(double) * 3 * (size_t)N);
+	oracle_central_diff_3d(f, X, Y, Z, G);
+	int32_t* lab[2] = { NULL, NULL };
+	if (a2 || d2) {
+		int64_t* seeds = (int64_t*)malloc(sizeof(int64_t) * (size_t)(N + 16));
+		int64_t* start = (int64_t*)malloc(sizeof(int64_t) * (size_t)(N + 16));
+		for (int pass = 0; pass < 2; pass++) {
+			if (!(pass == 0 ? a2 : d2)) continue;
+			lab[pass] = (int32_t*)malloc(sizeof(int32_t) * (size_t)N);
+			lctx c;
+			ctx_init(&c, f, grad, X, Y, Z, pass == 0 ? -1 : 1);
+			const int64_t nu = build_seeds(&c, P->presimp_threshold, seeds, start);
+			terminal_regions(&c, seeds, start, nu, lab[pass]);
+			integrate(&c, G, lab[pass], seeds, start[nu], P);
+			clean_regions(&c, lab[pass]);
+		}
+		free(seeds);
+		free(start);
+		oracle_boundary_labels_3d(f, X, Y, Z, lab[0], lab[1], restrict_out);
+	}
+	if (a1 || d1) {
+		lctx c;
+		ctx_init(&c, f, grad, X, Y, Z, 1);
+		if (a1) saddle_lines(&c, G, P, 0, restrict_out, 4);
+		if (d1) saddle_lines(&c, G, P, 1, restrict_out, 5);
+	}
+	oracle_conform_3d(f, X, Y, Z, restrict_out, grad_out, 1);
+	free(G);
+	free(lab[0]);
+	free(lab[1]);
+	return 0;
+}

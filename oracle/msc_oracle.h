@@ -84,6 +84,11 @@ int oracle_labels_3d(const float* f, const uint8_t* grad, int64_t X, int64_t Y, 
  * out).  Test infrastructure. */
 int oracle_saddle_lines_3d(const float* f, const uint8_t* grad, int64_t X, int64_t Y, int64_t Z, int which,
                            const oracle_label_params* P, uint8_t* cells);
+/* ondemandaccurate's accurate .grad for its flags a1 d1 a2 d2 at one thread: the
+ * restriction labels (one byte per cell) and the .grad (from `grad`, the plain one). */
+int oracle_ondemand_grad_3d(const float* f, const uint8_t* grad, int64_t X, int64_t Y, int64_t Z,
+                            const oracle_label_params* P, int a1, int d1, int a2, int d2, uint8_t* restrict_out,
+                            uint8_t* grad_out);
 
 #ifdef __cplusplus
 }

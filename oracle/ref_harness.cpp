@@ -19,6 +19,10 @@
 //       the touched vertices and RecordGrad (:693-699)
 //   ref_saddle_lines_3d    == ondemandaccurate/ondemandaccurate.cxx:254-505 at one thread
 //       (in ref_harness_lines.cpp)
+//   ref_ondemand_modes_3d  == ondemandaccurate/ondemandaccurate.cxx:772-1145 at one thread
+//       for any of its needASC1 / needDSC1 / needASC2 / needDSC2 flags: the 3-manifold
+//       labels and boundaries asked for, then the saddle lines on the gradient those
+//       integrations left, then the re-pairing and RecordGrad
 //   ref_ms_graph_3d        == extractmsc/extractmsc.cxx:482-504: a .grad loaded into
 //       DiscreteGradientLabeling, LazyMaximumVertexLabeling + TopologicalMaxVertexMeshFunction,
 //       MorseSmaleComplexBasic::ComputeFromGrad with the given arc build flags and no
@@ -75,6 +79,11 @@ typedef DiscreteGradientLabeling<MeshType> GradType;
 typedef RegularGridMaxMinVertexLabeling3D<MeshType, GridFuncType> MaxVLType;
 typedef TopologicalMaxVertexMeshFunction<MeshType, MaxVLType, GridFuncType, float> TopoFuncType;
 typedef SlidingWindowRobinsNoalloc<GridType, GridFuncType, MeshType, MaxVLType, GradType> NewRobinsType;
+
+// the saddle loops of the needASC1 / needDSC1 modes (ref_harness_lines.cpp)
+void saddle_lines(GridType* grid, GridFuncType* func, MeshType* mesh, GradType* labeling, TopoFuncType* topofunc,
+                  DenseLabeling<char>* lab, int which, float error_threshold, float gradient_threshold,
+                  int iteration_limit);
 
 }  // namespace refharness
 
@@ -369,6 +378,102 @@ int ref_ms_graph_3d(const float* f, long long X, long long Y, long long Z, const
 	}
 	counts[0] = nn;
 	counts[1] = na;
+	return 0;   // the reference objects are left to the process, as above
+}
+
+// ondemandaccurate's accurate .grad for the flags a1 d1 a2 d2 (needASC1, needDSC1,
+// needASC2, needDSC2) at one thread, with its restriction labels (one byte per cell).
+int ref_ondemand_modes_3d(const float* f, long long X, long long Y, long long Z, float error_threshold,
+                          float gradient_threshold, int iteration_limit, float presimp, int a1, int d1, int a2, int d2,
+                          const char* grad_path, unsigned char* restrict_out) {
+	using namespace refharness;
+	typedef IndexCompareLessThan<GridFuncType> ComparerASC;
+	typedef IndexCompareGreaterThan<GridFuncType> ComparerDSC;
+	typedef NumericIntegratorPathCompressingToTerminal<AdaptiveEulerAdvector3D<GridFuncType, -1>, GridFuncType> IntASC;
+	typedef NumericIntegratorPathCompressingToTerminal<AdaptiveEulerAdvector3D<GridFuncType, 1>, GridFuncType> IntDSC;
+	omp_set_num_threads(1);
+	GridType* grid = new GridType(Vec3l(X, Y, Z), Vec3b(0, 0, 0));
+	std::vector<float> img(f, f + X * Y * Z);
+	GridFuncType* func = new GridFuncType(grid, img.data());
+	MeshType* mesh = new MeshType(grid);
+	MaxVLType* maxv = new MaxVLType(mesh, func);
+	maxv->ComputeOutput();
+	TopoFuncType* topofunc = new TopoFuncType();
+	topofunc->setMeshAndFuncAndMaxVLabeling(mesh, func, maxv);
+	GradType* labeling = new GradType(mesh);
+	labeling->ClearAllGradient();
+	NewRobinsType* robins = new NewRobinsType(grid, func, mesh, maxv, labeling);
+	robins->ComputePairing_sliding();
+	DenseLabeling<char>* restriction_labels = new DenseLabeling<char>(mesh->numCells());
+	restriction_labels->SetAll(0);
+	if (a1 || d1 || a2 || d2) {
+		func->ComputeGradFromImage(1);
+		if (a2 || d2) {
+			SimplifiedExtremumGraph<MeshType, TopoFuncType, GradType>* seg =
+				new SimplifiedExtremumGraph<MeshType, TopoFuncType, GradType>(mesh, topofunc, labeling);
+			seg->SetMode(a2 && d2 ? SimplifiedExtremumGraph<MeshType, TopoFuncType, GradType>::EXTGRAPHMODE::BOTH
+			             : a2 ? SimplifiedExtremumGraph<MeshType, TopoFuncType, GradType>::EXTGRAPHMODE::MINS
+			                  : SimplifiedExtremumGraph<MeshType, TopoFuncType, GradType>::EXTGRAPHMODE::MAXS);
+			seg->ComputeMinMapFromGradient(presimp);
+			VertexLabelingToBoundaryLabeling<int, MaxVLType>* edge_map =
+				new VertexLabelingToBoundaryLabeling<int, MaxVLType>(mesh, restriction_labels);
+			edge_map->InitializeFirst();
+			if (a2) {
+				std::unordered_map<INDEX_TYPE, INT_TYPE> ext;
+				for (auto p : seg->mMinGraph->mCellIndexToListIdMap) ext[p.first] = seg->mMinGraph->Representative(p.second);
+				GridSimplifiedExtremalRegionBuilder<ComparerASC, GridFuncType, MeshType>* rb =
+					new GridSimplifiedExtremalRegionBuilder<ComparerASC, GridFuncType, MeshType>(func, grid, mesh);
+				rb->BeginIntegration(ext);
+				IntASC* integ = new IntASC(func, grid, error_threshold, gradient_threshold, iteration_limit);
+				integ->BeginIntegration(rb->GetIdMap(), rb->GetOutputLabels(), false);
+				IsolatedCCRegionRemoverNEW<ComparerASC, GridFuncType>* cl =
+					new IsolatedCCRegionRemoverNEW<ComparerASC, GridFuncType>(func, integ->GetOutputLabels());
+				cl->ComputeOutput();
+				edge_map->ComputeMINBoundary(integ->GetOutputLabels());
+			}
+			if (d2) {
+				std::unordered_map<INDEX_TYPE, INT_TYPE> ext;
+				for (auto p : seg->mMaxGraph->mCellIndexToListIdMap)
+					ext[maxv->Cell2HighestVertex(p.first)] = seg->mMaxGraph->Representative(p.second);
+				GridSimplifiedExtremalRegionBuilder<ComparerDSC, GridFuncType, MeshType>* rb =
+					new GridSimplifiedExtremalRegionBuilder<ComparerDSC, GridFuncType, MeshType>(func, grid, mesh);
+				rb->BeginIntegration(ext);
+				IntDSC* integ = new IntDSC(func, grid, error_threshold, gradient_threshold, iteration_limit);
+				integ->BeginIntegration(rb->GetIdMap(), rb->GetOutputLabels(), false);
+				IsolatedCCRegionRemoverNEW<ComparerDSC, GridFuncType>* cl =
+					new IsolatedCCRegionRemoverNEW<ComparerDSC, GridFuncType>(func, integ->GetOutputLabels());
+				cl->ComputeOutput();
+				edge_map->ComputeMAXBoundary(integ->GetOutputLabels(), maxv);
+			}
+		}
+		if (a1 || d1)
+			saddle_lines(grid, func, mesh, labeling, topofunc, restriction_labels, (a1 ? 1 : 0) | (d1 ? 2 : 0),
+			             error_threshold, gradient_threshold, iteration_limit);
+		typedef MyRobinsNoalloc<MeshType, MaxVLType, GradType, 4, 6> RobinsType;
+		RobinsType* constrained = new RobinsType(mesh, maxv, restriction_labels, labeling);
+		MeshType::DCellsIterator verts(mesh, 0);
+		for (verts.begin(); verts.valid(); verts.advance()) {
+			INDEX_TYPE vert_GI = verts.value();
+			bool hasdiff = restriction_labels->GetLabel(vert_GI) > 0;
+			if (!hasdiff) {
+				MeshType::AdjacentCellsIterator cells(mesh);
+				for (cells.begin(vert_GI); cells.valid(); cells.advance()) {
+					INDEX_TYPE cell_GI = cells.value();
+					if (restriction_labels->GetLabel(cell_GI) > 0 && maxv->Cell2HighestVertex(cell_GI) == vert_GI) {
+						hasdiff = true;
+						break;
+					}
+				}
+			}
+			if (hasdiff) constrained->ComputeLowerStar(vert_GI);
+		}
+	}
+	TopologicalGradientUsingAlgorithms<MeshType, TopoFuncType, GradType>* alg =
+		new TopologicalGradientUsingAlgorithms<MeshType, TopoFuncType, GradType>(topofunc, mesh, labeling);
+	alg->setAscendingManifoldDimensions();
+	labeling->outputToFile(grad_path);
+	if (restrict_out)
+		for (long long i = 0; i < (long long)mesh->numCells(); i++) restrict_out[i] = (unsigned char)restriction_labels->GetLabel(i);
 	return 0;   // the reference objects are left to the process, as above
 }
 

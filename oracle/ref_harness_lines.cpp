@@ -54,36 +54,17 @@ typedef SlidingWindowRobinsNoalloc<GridType, GridFuncType, MeshType, MaxVLType, 
 
 }  // namespace refharness
 
-extern "C" {
+namespace refharness {
 
-// The saddle streamline digitizers at one thread on the gradient of f: which bit 0 the
-// ascending lines from the 2-saddles (label 4), bit 1 the descending lines from the
-// 1-saddles (label 5), in that order, into cells (one byte per cell, in and out).
-int ref_saddle_lines_3d(const float* f, long long X, long long Y, long long Z, int which, float error_threshold,
-                        float gradient_threshold, int iteration_limit, unsigned char* cells) {
-	using namespace refharness;
+// The saddle loops of ReIntegrateUpFrom2Saddles (which bit 0, label 4) and
+// ReIntegrateDownFrom1Saddles (bit 1, label 5) at one thread, on the given objects.
+void saddle_lines(GridType* grid, GridFuncType* func, MeshType* mesh, GradType* labeling, TopoFuncType* topofunc,
+                  DenseLabeling<char>* lab, int which, float error_threshold, float gradient_threshold,
+                  int iteration_limit) {
 	typedef DigitizingNumericStreamlineIntegrator3dASC<MeshType, GridFuncType, AdaptiveEulerAdvector3D<GridFuncType, 1> >
 		DigASC;
 	typedef DigitizingNumericStreamlineIntegrator3dDSC<MeshType, GridFuncType, AdaptiveEulerAdvector3D<GridFuncType, -1> >
 		DigDSC;
-	omp_set_num_threads(1);
-	GridType* grid = new GridType(Vec3l(X, Y, Z), Vec3b(0, 0, 0));
-	std::vector<float> img(f, f + X * Y * Z);
-	GridFuncType* func = new GridFuncType(grid, img.data());
-	MeshType* mesh = new MeshType(grid);
-	MaxVLType* maxv = new MaxVLType(mesh, func);
-	maxv->ComputeOutput();
-	TopoFuncType* topofunc = new TopoFuncType();
-	topofunc->setMeshAndFuncAndMaxVLabeling(mesh, func, maxv);
-	GradType* labeling = new GradType(mesh);
-	labeling->ClearAllGradient();
-	NewRobinsType* robins = new NewRobinsType(grid, func, mesh, maxv, labeling);
-	robins->ComputePairing_sliding();
-	func->ComputeGradFromImage(1);
-	const INDEX_TYPE NC = mesh->numCells();
-	DenseLabeling<char>* lab = new DenseLabeling<char>(NC);
-	for (INDEX_TYPE i = 0; i < NC; i++) lab->SetLabel(i, (char)cells[i]);
-
 	// the saddles of dimension sdim by the reference's keys, the last processed first
 	auto saddles = [&](int sdim, bool negate) {
 		std::vector<std::pair<float, INDEX_TYPE> > cr;
@@ -163,6 +144,37 @@ int ref_saddle_lines_3d(const float* f, long long X, long long Y, long long Z, i
 			dig->set_label(cr[li].second);
 		}
 	}
+}
+
+}  // namespace refharness
+
+extern "C" {
+
+// The saddle streamline digitizers at one thread on the gradient of f: which bit 0 the
+// ascending lines from the 2-saddles (label 4), bit 1 the descending lines from the
+// 1-saddles (label 5), in that order, into cells (one byte per cell, in and out).
+int ref_saddle_lines_3d(const float* f, long long X, long long Y, long long Z, int which, float error_threshold,
+                        float gradient_threshold, int iteration_limit, unsigned char* cells) {
+	using namespace refharness;
+	omp_set_num_threads(1);
+	GridType* grid = new GridType(Vec3l(X, Y, Z), Vec3b(0, 0, 0));
+	std::vector<float> img(f, f + X * Y * Z);
+	GridFuncType* func = new GridFuncType(grid, img.data());
+	MeshType* mesh = new MeshType(grid);
+	MaxVLType* maxv = new MaxVLType(mesh, func);
+	maxv->ComputeOutput();
+	TopoFuncType* topofunc = new TopoFuncType();
+	topofunc->setMeshAndFuncAndMaxVLabeling(mesh, func, maxv);
+	GradType* labeling = new GradType(mesh);
+	labeling->ClearAllGradient();
+	NewRobinsType* robins = new NewRobinsType(grid, func, mesh, maxv, labeling);
+	robins->ComputePairing_sliding();
+	func->ComputeGradFromImage(1);
+	const INDEX_TYPE NC = mesh->numCells();
+	DenseLabeling<char>* lab = new DenseLabeling<char>(NC);
+	for (INDEX_TYPE i = 0; i < NC; i++) lab->SetLabel(i, (char)cells[i]);
+
+	saddle_lines(grid, func, mesh, labeling, topofunc, lab, which, error_threshold, gradient_threshold, iteration_limit);
 	for (INDEX_TYPE i = 0; i < NC; i++) cells[i] = (unsigned char)lab->GetLabel(i);
 	return 0;   // the reference objects are left to the process, as above
 }

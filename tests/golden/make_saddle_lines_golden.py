@@ -1,4 +1,5 @@
-"""Generates tests/golden/saddle_lines.json from the MSCEER reference itself.
+"""Generates tests/golden/saddle_lines.json and tests/golden/ondemand_modes.json from
+the MSCEER reference itself.
 
 Run where the reference sources are present (`make -C oracle ref` compiles
 oracle/_ref/libmsc_ref.so from them):
@@ -12,6 +13,9 @@ from the given cell labels; the oracle's restatement is checked equal first.  Th
 fixture stores the SHA-256 of the cell labels; the input is regenerated from its
 generator (f_sha256 says whether a machine regenerated the same floats: the FFT-based
 fields can differ in their last bits between hosts, and the streamlines with them).
+ondemand_modes.json holds, per case and flags (needASC1, needDSC1, needASC2,
+needDSC2), the SHA-256 of the restriction labels and of the accurate .grad the
+reference's ondemandaccurate writes at one thread (the oracle checked equal first).
 """
 from __future__ import annotations
 
@@ -41,6 +45,11 @@ CASES = [
     ("k3_24x20x18_both", "power_law_field((24,20,18), seed=2)", 3, None),
 ]
 ERROR, ITERS, MAX_STEP = 1e-4, 4000, 0.25
+MODE_CASES = [
+    ("gauss12_28x26x24", "gaussian_sum((28,26,24), 12, seed=2)"),
+    ("gauss32_36x32x30", "gaussian_sum((36,32,30), 32, seed=6)"),
+]
+MODES = [(1, 0, 0, 0), (0, 1, 0, 0), (1, 1, 1, 1), (1, 0, 1, 0), (0, 1, 0, 1), (0, 0, 1, 1)]
 
 
 def preset_cells(nc: int, spec):
@@ -76,6 +85,21 @@ def main() -> None:
                      "sha256": digest(want)}
         print(name, out[name]["labelled"])
     (HERE / "saddle_lines.json").write_text(json.dumps(out, indent=1) + "\n")
+    modes = {}
+    for name, gen in MODE_CASES:
+        f = eval("fields." + gen).astype(np.float32)
+        g = oracle_lib.ref_grad(ref, f)
+        gt = 1e-6 * float(np.abs(f).max())
+        entry = {"generator": gen, "f_sha256": digest(f), "grad_sha256": digest(g), "modes": {}}
+        for flags in MODES:
+            rr, rg = oracle_lib.ref_ondemand_modes(ref, f, flags, ERROR, gt, ITERS)
+            orr, org = orc.ondemand_grad(f, g, flags, ERROR, gt, ITERS, MAX_STEP)
+            assert np.array_equal(orr, rr) and np.array_equal(org, rg), (name, flags)
+            entry["modes"]["".join(map(str, flags))] = {"restricted": int((rr > 0).sum()), "restrict_sha256": digest(rr),
+                                                        "grad_sha256": digest(rg)}
+        modes[name] = entry
+        print(name, {k: v["restricted"] for k, v in entry["modes"].items()})
+    (HERE / "ondemand_modes.json").write_text(json.dumps(modes, indent=1) + "\n")
 
 
 if __name__ == "__main__":

@@ -51,6 +51,21 @@ class Oracle:
                                            _VP, _VP]
         lib.oracle_saddle_lines_3d.argtypes = [_VP, _VP, _I64, _I64, _I64, ctypes.c_int, ctypes.POINTER(LabelParams),
                                                _VP]
+        lib.oracle_ondemand_grad_3d.argtypes = [_VP, _VP, _I64, _I64, _I64, ctypes.POINTER(LabelParams),
+                                                ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, _VP, _VP]
+
+    def ondemand_grad(self, f, grad, flags, error_threshold, gradient_threshold, iteration_limit, max_step,
+                      presimp=0.0):
+        """ondemandaccurate's accurate .grad for flags (needASC1, needDSC1, needASC2,
+        needDSC2) at one thread: (restriction labels, .grad)."""
+        f = np.ascontiguousarray(f, dtype=np.float32)
+        grad = np.ascontiguousarray(grad, dtype=np.uint8)
+        restrict = np.empty(grad.size, np.uint8)
+        out = np.empty(grad.size, np.uint8)
+        p = LabelParams(error_threshold, gradient_threshold, iteration_limit, max_step, presimp)
+        assert self.lib.oracle_ondemand_grad_3d(f.ctypes.data, grad.ctypes.data, *f.shape[::-1], ctypes.byref(p),
+                                                *[int(x) for x in flags], restrict.ctypes.data, out.ctypes.data) == 0
+        return restrict, out
 
     def saddle_lines(self, f, grad, which, error_threshold, gradient_threshold, iteration_limit, max_step,
                      cells=None):
@@ -213,10 +228,30 @@ def load_ref():
     lib.ref_ondemand_3d.argtypes = [_VP, ctypes.c_longlong, ctypes.c_longlong, ctypes.c_longlong, ctypes.c_float,
                                     ctypes.c_float, ctypes.c_int, ctypes.c_float, _VP, _VP, _VP, ctypes.c_int,
                                     ctypes.c_char_p, _VP]
+    if hasattr(lib, "ref_ondemand_modes_3d"):
+        lib.ref_ondemand_modes_3d.argtypes = [_VP, ctypes.c_longlong, ctypes.c_longlong, ctypes.c_longlong,
+                                              ctypes.c_float, ctypes.c_float, ctypes.c_int, ctypes.c_float,
+                                              ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_char_p,
+                                              _VP]
     if hasattr(lib, "ref_saddle_lines_3d"):
         lib.ref_saddle_lines_3d.argtypes = [_VP, ctypes.c_longlong, ctypes.c_longlong, ctypes.c_longlong,
                                             ctypes.c_int, ctypes.c_float, ctypes.c_float, ctypes.c_int, _VP]
     return lib
+
+
+def ref_ondemand_modes(lib, f, flags, error_threshold, gradient_threshold, iteration_limit, presimp=0.0):
+    """The reference's ondemandaccurate for flags (needASC1, needDSC1, needASC2,
+    needDSC2) at one thread: (restriction labels, the .grad it writes)."""
+    f = np.ascontiguousarray(f, dtype=np.float32)
+    nc = int(np.prod([2 * d - 1 for d in f.shape]))
+    restrict = np.empty(nc, np.uint8)
+    with tempfile.TemporaryDirectory() as td:
+        path = os.path.join(td, "o.grad").encode()
+        assert lib.ref_ondemand_modes_3d(f.ctypes.data, *f.shape[::-1], error_threshold, gradient_threshold,
+                                         iteration_limit, presimp, *[int(x) for x in flags], path,
+                                         restrict.ctypes.data) == 0
+        grad = np.fromfile(path.decode(), dtype=np.uint8)
+    return restrict, grad
 
 
 def ref_saddle_lines(lib, f, which, error_threshold, gradient_threshold, iteration_limit, cells=None):

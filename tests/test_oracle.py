@@ -213,3 +213,40 @@ def test_saddle_lines_oracle_against_reference(oracle, which):
         want = oracle_lib.ref_saddle_lines(ref, f, which, 1e-4, gt, 4000, cells)
         assert (want > 0).sum() > 0
         assert np.array_equal(got, want), int((got != want).sum())
+
+
+ONDEMAND_MODE_CASES = json.loads((GOLDEN / "ondemand_modes.json").read_text())
+
+
+@pytest.mark.parametrize("key", sorted(ONDEMAND_MODE_CASES))
+def test_ondemand_modes_oracle_against_golden(oracle, key):
+    """ondemandaccurate's accurate .grad for every combination of needASC1 / needDSC1 /
+    needASC2 / needDSC2 in the fixture: restriction labels and .grad equal the
+    reference's, by SHA-256 (on the same floats of f)."""
+    spec = ONDEMAND_MODE_CASES[key]
+    f = _regenerate(spec).astype(np.float32)
+    g = oracle.grad(f)
+    assert hashlib.sha256(g.tobytes()).hexdigest() == spec["grad_sha256"]
+    if hashlib.sha256(f.tobytes()).hexdigest() != spec["f_sha256"]:
+        pytest.skip("this host regenerates other floats for the field; the streamlines follow them")
+    gt = 1e-6 * float(np.abs(f).max())
+    for flags, want in spec["modes"].items():
+        restrict, grad = oracle.ondemand_grad(f, g, [int(c) for c in flags], 1e-4, gt, 4000, 0.25)
+        assert int((restrict > 0).sum()) == want["restricted"], flags
+        assert hashlib.sha256(restrict.tobytes()).hexdigest() == want["restrict_sha256"], flags
+        assert hashlib.sha256(grad.tobytes()).hexdigest() == want["grad_sha256"], flags
+
+
+@pytest.mark.parametrize("flags", [(1, 0, 0, 0), (0, 1, 0, 0), (1, 1, 1, 1), (0, 1, 1, 0)])
+def test_ondemand_modes_oracle_against_reference(oracle, flags):
+    ref = oracle_lib.load_ref()
+    if ref is None or not hasattr(ref, "ref_ondemand_modes_3d"):
+        pytest.skip("the reference is not compiled on this machine")
+    f = fields.power_law_field((26, 22, 20), seed=17)
+    g = oracle.grad(f)
+    gt = 1e-6 * float(np.abs(f).max())
+    restrict, grad = oracle.ondemand_grad(f, g, flags, 1e-4, gt, 4000, 0.25)
+    want_r, want_g = oracle_lib.ref_ondemand_modes(ref, f, flags, 1e-4, gt, 4000)
+    assert (want_r > 0).sum() > 0
+    assert np.array_equal(restrict, want_r), int((restrict != want_r).sum())
+    assert np.array_equal(grad, want_g), oracle_lib.describe_mismatch(grad, want_g, f.shape[::-1])
