@@ -963,10 +963,18 @@ int oracle_labels_3d(const float* f, const uint8_t* grad, int64_t X, int64_t Y, 
 
 int oracle_saddle_lines_3d(const float* f, const uint8_t* grad, int64_t X, int64_t Y, int64_t Z, int which,
                            const oracle_label_params* P, uint8_t* cells) {
+	return oracle_saddle_lines_zeroed_3d(f, grad, NULL, X, Y, Z, which, P, cells);
+}
+
+int oracle_saddle_lines_zeroed_3d(const float* f, const uint8_t* grad, const uint32_t* zeroed, int64_t X, int64_t Y,
+                                  int64_t Z, int which, const oracle_label_params* P, uint8_t* cells) {
 	if (!P || !cells || X < 2 || Y < 2 || Z < 2) return -1;
 	const int64_t N = X * Y * Z;
 	double* G = (double*)malloc(sizeof(double) * 3 * (size_t)N);
 	oracle_central_diff_3d(f, X, Y, Z, G);
+	if (zeroed)
+		for (int64_t v = 0; v < N; v++)
+			if ((zeroed[v >> 5] >> (v & 31)) & 1u) { G[3 * v] = 0; G[3 * v + 1] = 0; G[3 * v + 2] = 0; }
 	lctx c;
 	ctx_init(&c, f, grad, X, Y, Z, 1);
 	if (which & 1) saddle_lines(&c, G, P, 0, cells, 4);

@@ -84,6 +84,10 @@ int oracle_labels_3d(const float* f, const uint8_t* grad, int64_t X, int64_t Y, 
  * out).  Test infrastructure. */
 int oracle_saddle_lines_3d(const float* f, const uint8_t* grad, int64_t X, int64_t Y, int64_t Z, int which,
                            const oracle_label_params* P, uint8_t* cells);
+/* The same with the gradient zero at the vertices whose bit `zeroed` sets (bit v & 31 of
+ * word v >> 5), as the integrations before the lines leave it at their seeds. */
+int oracle_saddle_lines_zeroed_3d(const float* f, const uint8_t* grad, const uint32_t* zeroed, int64_t X, int64_t Y,
+                                  int64_t Z, int which, const oracle_label_params* P, uint8_t* cells);
 /* ondemandaccurate's accurate .grad for its flags a1 d1 a2 d2 at one thread: the
  * restriction labels (one byte per cell) and the .grad (from `grad`, the plain one). */
 int oracle_ondemand_grad_3d(const float* f, const uint8_t* grad, int64_t X, int64_t Y, int64_t Z,

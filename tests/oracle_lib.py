@@ -51,6 +51,8 @@ class Oracle:
                                            _VP, _VP]
         lib.oracle_saddle_lines_3d.argtypes = [_VP, _VP, _I64, _I64, _I64, ctypes.c_int, ctypes.POINTER(LabelParams),
                                                _VP]
+        lib.oracle_saddle_lines_zeroed_3d.argtypes = [_VP, _VP, _VP, _I64, _I64, _I64, ctypes.c_int,
+                                                      ctypes.POINTER(LabelParams), _VP]
         lib.oracle_ondemand_grad_3d.argtypes = [_VP, _VP, _I64, _I64, _I64, ctypes.POINTER(LabelParams),
                                                 ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, _VP, _VP]
 
@@ -68,17 +70,25 @@ class Oracle:
         return restrict, out
 
     def saddle_lines(self, f, grad, which, error_threshold, gradient_threshold, iteration_limit, max_step,
-                     cells=None):
+                     cells=None, zeroed=None):
         """ondemandaccurate's saddle streamline digitizers (which: 1 ascending from the
         2-saddles, label 4; 2 descending from the 1-saddles, label 5; 3 both) at one
-        thread, into a copy of `cells` (one byte per cell; zeros when not given)."""
+        thread, into a copy of `cells` (one byte per cell; zeros when not given); the
+        gradient is zero at the vertices whose bit the uint32 bitmap `zeroed` sets."""
         f = np.ascontiguousarray(f, dtype=np.float32)
         grad = np.ascontiguousarray(grad, dtype=np.uint8)
         nc = int(np.prod([2 * d - 1 for d in f.shape]))
         out = np.zeros(nc, np.uint8) if cells is None else np.array(cells, dtype=np.uint8, copy=True)
         p = LabelParams(error_threshold, gradient_threshold, iteration_limit, max_step, 0.0)
-        assert self.lib.oracle_saddle_lines_3d(f.ctypes.data, grad.ctypes.data, *f.shape[::-1], which,
-                                               ctypes.byref(p), out.ctypes.data) == 0
+        if zeroed is None:
+            rc = self.lib.oracle_saddle_lines_3d(f.ctypes.data, grad.ctypes.data, *f.shape[::-1], which,
+                                                 ctypes.byref(p), out.ctypes.data)
+        else:
+            zeroed = np.ascontiguousarray(zeroed, dtype=np.uint32)
+            assert zeroed.size * 32 >= f.size
+            rc = self.lib.oracle_saddle_lines_zeroed_3d(f.ctypes.data, grad.ctypes.data, zeroed.ctypes.data,
+                                                        *f.shape[::-1], which, ctypes.byref(p), out.ctypes.data)
+        assert rc == 0
         return out
 
     def labels(self, f, grad, error_threshold, gradient_threshold, iteration_limit, max_step, presimp):
