@@ -193,6 +193,24 @@ int msc_ms_graph_3d(const uint8_t* grad, const float* f, const int64_t dims[3], 
                     uint8_t* node_boundary, int64_t arc_cap, int32_t* arc_lower, int32_t* arc_upper,
                     float* arc_persistence, int64_t counts[2], msc_stream_t stream);
 
+/* The saddle streamline digitizers of ondemandaccurate's needASC1 / needDSC1 modes
+ * (ReIntegrateUpFrom2Saddles / ReIntegrateDownFrom1Saddles, ondemandaccurate.cxx:254-505,
+ * with DigitizingNumericStreamlineIntegrator3dASC / 3dDSC,
+ * gi_numeric_streamline_integrator.h:525-1080): streamlines from the cells around every
+ * critical saddle, label 4 on the hex-face chains of the ascending lines from the
+ * 2-saddles (which bit 0), label 5 on the vertex-edge chains of the descending lines
+ * from the 1-saddles (bit 1, after the ascending ones), with the one-thread run's
+ * result.  f, grad (the .grad of f) and cells (one byte per cell, in and out: cells
+ * labelled 4 / 5 on entry stop the lines of that label): device.  zeroed: NULL, or a
+ * device bitmap (bit v & 31 of word v >> 5, at least ceil(X*Y*Z / 32) words) of the
+ * vertices where the gradient is zero (the seeds of the 3-manifold integrations before
+ * the lines).  params: error_threshold, gradient_threshold, iteration_limit, max_step.
+ * stats (host, optional): streamlines, recorded voxel steps, voxel steps kept, rounds.
+ * Fewer than 2^32 cells; the records take 136 bytes per label-free voxel step.
+ * Blocking. */
+int msc_saddle_lines_3d(const float* f, const uint8_t* grad, const uint32_t* zeroed, const int64_t dims[3], int which,
+                        const msc_integ_params* params, uint8_t* cells, int64_t stats[4], msc_stream_t stream);
+
 /* The isolated-region cleaner alone: IsolatedCCRegionRemoverNEW::ComputeOutput
  * (gi_isolated_region_remover.h:155-192) on caller labels, as ondemandaccurate runs it
  * after the integration (ondemandaccurate.cxx:866-870, 942-946).  Same-label

@@ -19,6 +19,7 @@ from .api import (  # noqa: F401
     lower_star_pairs,
     ms_graph,
     num_cells,
+    saddle_lines,
     steepest_lstar,
 )
 

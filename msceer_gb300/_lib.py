@@ -61,6 +61,8 @@ SIGNATURES = {
     # grad f dims build node_cap cell value dim boundary arc_cap lower upper persistence counts stream
     "msc_ms_graph_3d": (ctypes.c_int, [_VP, _VP, _I64P, _VP, ctypes.c_int64, _VP, _VP, _VP, _VP, ctypes.c_int64, _VP,
                                        _VP, _VP, _I64P, _VP]),
+    # f grad zeroed dims which params cells stats stream
+    "msc_saddle_lines_3d": (ctypes.c_int, [_VP, _VP, _VP, _I64P, ctypes.c_int, _VP, _VP, _I64P, _VP]),
 }
 
 

@@ -259,6 +259,43 @@ def ms_graph(grad, f, build_arcs=(1, 0, 1)):
     return out
 
 
+def saddle_lines(f, grad, cells=None, which=3, zeroed=None, error_threshold=1e-4, gradient_threshold=None,
+                 iteration_limit=4000, max_step=0.25):
+    """ondemandaccurate's saddle streamline digitizers (needASC1 / needDSC1) on a device
+    volume (msc_saddle_lines_3d): ``which`` bit 0 the ascending lines from the 2-saddles
+    (label 4 on hexes and faces), bit 1 the descending lines from the 1-saddles (label 5
+    on vertices and edges).  ``cells``: CUDA uint8, one byte per cell (zeros when not
+    given), updated in a copy; ``zeroed``: CUDA int32/uint32 bitmap of vertices with a
+    zero gradient, or None.  Returns (cells, stats) with stats = (streamlines, recorded
+    voxel steps, kept voxel steps, rounds)."""
+    import torch
+
+    if not (f.is_cuda and grad.is_cuda):
+        raise ValueError("saddle_lines takes CUDA tensors")
+    f = f.contiguous()
+    dims = _shape_dims(f.shape)
+    if len(dims) != 3 or grad.numel() != num_cells(dims):
+        raise ValueError("saddle_lines takes a 3D volume and its .grad")
+    if gradient_threshold is None:
+        gradient_threshold = 1e-6 * float(f.abs().max())
+    out = (torch.zeros(grad.numel(), dtype=torch.uint8, device=f.device) if cells is None
+           else cells.to(device=f.device, dtype=torch.uint8).contiguous().clone())
+    if zeroed is not None:
+        zeroed = zeroed.contiguous()
+        if not zeroed.is_cuda or zeroed.element_size() != 4 or zeroed.numel() * 32 < f.numel():
+            raise ValueError("zeroed must be a CUDA 32-bit bitmap of at least one bit per vertex")
+    p = _lib.IntegParams(error_threshold, gradient_threshold, iteration_limit, max_step, 0.0, 0)
+    stats = (ctypes.c_int64 * 4)()
+    lib = _lib.load()
+    stream = torch.cuda.current_stream(f.device).cuda_stream
+    ptr = lambda t: ctypes.c_void_p(t.data_ptr()) if t is not None else None  # noqa: E731
+    with torch.cuda.device(f.device):
+        rc = lib.msc_saddle_lines_3d(ptr(f), ptr(grad), ptr(zeroed), _lib.dims_arg(dims), int(which), ctypes.byref(p),
+                                     ptr(out), stats, ctypes.c_void_p(stream))
+    _lib.check(rc, "msc_saddle_lines_3d")
+    return out, tuple(int(x) for x in stats)
+
+
 def clean_regions(f, labels, direction):
     """IsolatedCCRegionRemoverNEW on device labels (msc_clean_regions_3d): ``direction``
     -1 for ascending labels (lowest value first), +1 for descending ones.  ``f``: CUDA

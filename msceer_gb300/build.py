@@ -27,7 +27,7 @@ NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompil
               "--expt-relaxed-constexpr", "-I", str(ROOT / "include")]
 CU_SOURCES = ["lstar_kernels.cu", "ldir_kernels.cu", "grad_kernels.cu", "label_kernels.cu", "integrate_kernels.cu",
               "msc_capi.cu", "msc_labels_capi.cu", "conform_kernels.cu", "msc_static_scratch.cu", "triage_kernels.cu", "triage_prep.cu",
-              "msc_triage_capi.cu", "ms_graph.cu"]
+              "msc_triage_capi.cu", "ms_graph.cu", "saddle_lines.cu"]
 
 
 def _nvcc() -> str:

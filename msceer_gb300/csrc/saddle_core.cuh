@@ -396,7 +396,8 @@ SL_HD int saddle_seeds(const Grid& G, const uint8_t* grad, int64_t sad, int dsc,
       if (!grad_critical(grad, t)) {
         const int64_t pr = grad_pair(G, grad, t);
         visit(pr);
-        if (qt < kMaxSeeds + 1) queue[qt++] = pr;
+        // a pair outside the grid only comes from a damaged .grad: not walked
+        if (qt < kMaxSeeds + 1 && (uint64_t)pr < (uint64_t)(G.dX * G.dY * G.dZ)) queue[qt++] = pr;
       }
     }
   }

@@ -60,6 +60,21 @@ def test_argument_errors_before_any_device_work(lib):
     assert "MSC_ERR_NULL_POINTER" in str(e.value)
 
 
+def test_saddle_lines_argument_errors_before_any_device_work(lib):
+    """msc_saddle_lines_3d rejects bad dims, null buffers and a bad `which` before it
+    touches the device."""
+    buf = ctypes.create_string_buffer(64)
+    b = ctypes.c_void_p(ctypes.addressof(buf))
+    p = _lib.IntegParams(1e-4, 1e-6, 4000, 0.25, 0.0, 0)
+    sl = lib.msc_saddle_lines_3d
+    assert sl(b, b, None, _lib.dims_arg((1, 4, 4)), 3, ctypes.byref(p), b, None, None) == -1
+    assert sl(None, b, None, _lib.dims_arg((4, 4, 4)), 3, ctypes.byref(p), b, None, None) == -2
+    assert sl(b, b, None, _lib.dims_arg((4, 4, 4)), 3, None, b, None, None) == -2
+    assert sl(b, b, None, _lib.dims_arg((4, 4, 4)), 4, ctypes.byref(p), b, None, None) == -1
+    assert b"which" in lib.msc_last_error_string()
+    assert sl(b, b, None, _lib.dims_arg((2048, 2048, 1100)), 3, ctypes.byref(p), b, None, None) == -8
+
+
 def test_cli_usage_message():
     exe = build.build_cli()
     res = subprocess.run([str(exe)], capture_output=True, text=True)
