@@ -90,7 +90,8 @@ __device__ __forceinline__ bool vertex_greater(const float* f, int64_t a, int64_
 // 1. the critical saddles of dimension sdim: (ordered key << 32 | cell id), appended
 // one atomic per warp (the loop is warp-uniform)
 __global__ void saddle_keys_kernel(const uint8_t* __restrict__ grad, const float* __restrict__ f, Grid G, int dsc,
-                                   uint64_t* __restrict__ keys, unsigned long long* __restrict__ n_keys) {
+                                   uint64_t* __restrict__ keys, int64_t key_cap,
+                                   unsigned long long* __restrict__ n_keys) {
   const int64_t nc = G.dX * G.dY * G.dZ;
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
   const int64_t rounds = (nc + stride - 1) / stride;
@@ -128,7 +129,8 @@ __global__ void saddle_keys_kernel(const uint8_t* __restrict__ grad, const float
     const int leader = __ffs(m) - 1;
     if ((int)lane == leader) base = atomicAdd(n_keys, (unsigned long long)__popc(m));
     base = __shfl_sync(0xffffffffu, base, leader);
-    if (take) keys[base + __popc(m & ((1u << lane) - 1u))] = key;
+    const unsigned long long at = base + __popc(m & ((1u << lane) - 1u));
+    if (take && at < (unsigned long long)key_cap) keys[at] = key;  // the host rejects a count above the cap
   }
 }
 
@@ -252,19 +254,21 @@ int lines_direction(const Field& F, const Params& P, const uint8_t* grad, int ds
   const int64_t key_cap = nc / 2 + 1;
   SCUDA(pool.get(&keys, (size_t)key_cap), "scratch alloc(saddle keys)");
   count_launch();
-  saddle_keys_kernel<<<grid_for(nc), kThreads, 0, st>>>(grad, F.f, G, dsc, keys, counters);
+  saddle_keys_kernel<<<grid_for(nc), kThreads, 0, st>>>(grad, F.f, G, dsc, keys, key_cap, counters);
   SCUDA(cudaGetLastError(), "saddle_keys_kernel");
   unsigned long long h_n = 0;
   SCUDA(cudaMemcpyAsync(&h_n, counters, sizeof(h_n), cudaMemcpyDeviceToHost, st), "read saddle count");
   SCUDA(cudaStreamSynchronize(st), "cudaStreamSynchronize");
   const int64_t n = (int64_t)h_n;
   if (n == 0) return MSC_OK;
+  if (n > key_cap) return fail(MSC_ERR_QUEUE_OVERFLOW, "more saddles than cells of their dimension");
   SCUDA(pool.get(&sorted, (size_t)n), "scratch alloc(sorted keys)");
   size_t tmp_bytes = 0, scan_bytes = 0;
   SCUDA(cub::DeviceRadixSort::SortKeys(nullptr, tmp_bytes, keys, sorted, n, 0, 64, st), "sort size");
-  int64_t* items;
+  int64_t *items, *item_base;
   SCUDA(pool.get(&items, (size_t)n + 1), "scratch alloc(items)");
-  SCUDA(cub::DeviceScan::ExclusiveSum(nullptr, scan_bytes, items, items, n + 1, st), "scan size");
+  SCUDA(pool.get(&item_base, (size_t)n + 1), "scratch alloc(items)");
+  SCUDA(cub::DeviceScan::ExclusiveSum(nullptr, scan_bytes, items, item_base, n + 1, st), "scan size");
   void* tmp;
   SCUDA(pool.get(reinterpret_cast<uint8_t**>(&tmp), tmp_bytes > scan_bytes ? tmp_bytes : scan_bytes),
         "scratch alloc(sort)");
@@ -274,9 +278,9 @@ int lines_direction(const Field& F, const Params& P, const uint8_t* grad, int ds
   seed_count_kernel<<<grid_for(n), kThreads, 0, st>>>(grad, G, dsc, sorted, n, items);
   SCUDA(cudaMemsetAsync(items + n, 0, sizeof(int64_t), st), "cudaMemsetAsync");
   size_t sb = scan_bytes;
-  SCUDA(cub::DeviceScan::ExclusiveSum(tmp, sb, items, items, n + 1, st), "scan items");
+  SCUDA(cub::DeviceScan::ExclusiveSum(tmp, sb, items, item_base, n + 1, st), "scan items");
   int64_t n_items = 0;
-  SCUDA(cudaMemcpyAsync(&n_items, items + n, sizeof(int64_t), cudaMemcpyDeviceToHost, st), "read item count");
+  SCUDA(cudaMemcpyAsync(&n_items, item_base + n, sizeof(int64_t), cudaMemcpyDeviceToHost, st), "read item count");
   SCUDA(cudaStreamSynchronize(st), "cudaStreamSynchronize");
   if (n_items >= (int64_t)0xFFFFFFFEll) return fail(MSC_ERR_TOO_LARGE, "more than 2^32 - 2 streamlines and saddles");
   const int64_t n_lines = n_items - n;
@@ -288,8 +292,8 @@ int lines_direction(const Field& F, const Params& P, const uint8_t* grad, int ds
   SCUDA(pool.get(&sad_cell, (size_t)n), "scratch alloc(saddles)");
   SCUDA(pool.get(&sad_item, (size_t)n), "scratch alloc(saddles)");
   count_launch();
-  seed_write_kernel<<<grid_for(n), kThreads, 0, st>>>(grad, G, dsc, sorted, n, items, line_item, line_seed, sad_cell,
-                                                       sad_item);
+  seed_write_kernel<<<grid_for(n), kThreads, 0, st>>>(grad, G, dsc, sorted, n, item_base, line_item, line_seed,
+                                                       sad_cell, sad_item);
   // 3. label-free records: count, scan, record
   int64_t* offsets;
   SCUDA(pool.get(&offsets, (size_t)n_lines + 1), "scratch alloc(offsets)");
