@@ -421,46 +421,67 @@ struct StepRec {
   int64_t chk[kMaxChecks];
 };
 
-// IntegrateStreamline of the digitizing integrators without labels: the streamline
-// from `seed` to its label-free end, one record per voxel step (rec(const StepRec&)
-// returns false to stop early, e.g. when a record buffer is full).  Returns the number
-// of steps, or -1 when a step overflowed its check list.
+// Where a label-free streamline stands between voxel steps (to trace it in pieces).
+struct LineState {
+  V3 cur;
+  int iters;
+  int64_t x, y, z;  // its nearest vertex
+  bool done;        // it has ended
+};
+
+SL_HD LineState line_start(const Params& P, V3 seed) {
+  return {seed, P.limit, (int64_t)dadd(seed.x, 0.5), (int64_t)dadd(seed.y, 0.5), (int64_t)dadd(seed.z, 0.5), false};
+}
+
+// IntegrateStreamline of the digitizing integrators without labels, from *S for at most
+// max_steps voxel steps, one record per step (rec(const StepRec&) returns false to stop
+// early, e.g. when a record buffer is full).  Returns the number of steps recorded, or
+// -1 when a step overflowed its check list.
 template <class Rec>
-SL_HD int trace_line(const Field& F, const Params& P, int dsc, V3 seed, Rec rec) {
-  int64_t x = (int64_t)dadd(seed.x, 0.5), y = (int64_t)dadd(seed.y, 0.5), z = (int64_t)dadd(seed.z, 0.5);
+SL_HD int trace_more(const Field& F, const Params& P, int dsc, LineState* S, int max_steps, Rec rec) {
   const int64_t ext[3] = {F.g.X, F.g.Y, F.g.Z};
-  V3 cur = seed;
-  int iters = P.limit, nsteps = 0;
-  for (;;) {
+  int nsteps = 0;
+  while (!S->done && nsteps < max_steps) {
     StepRec s;
-    s.old = cur;
-    s.it0 = iters;
-    const int64_t xyz[3] = {x, y, z};
+    s.old = S->cur;
+    s.it0 = S->iters;
+    const int64_t xyz[3] = {S->x, S->y, S->z};
     int64_t dist = INT64_MAX;
     for (int a = 0; a < 3; a++) {
       const int64_t d = xyz[a] < ext[a] - 1 - xyz[a] ? xyz[a] : ext[a] - 1 - xyz[a];
       if (d < dist) dist = d;
     }
     s.nearb = dist <= 1;
-    s.ev = voxel_step(F, P, dsc, &cur, &iters, s.nearb, s.chk, &s.nchk, -1);
+    s.ev = voxel_step(F, P, dsc, &S->cur, &S->iters, s.nearb, s.chk, &s.nchk, -1);
     if (s.ev == kEvOverflow) return -1;
-    s.end = cur;
-    nsteps++;
+    s.end = S->cur;
     if (!rec(s)) return nsteps;
-    if (s.nearb || s.ev != kEvOutOfVoxel) return nsteps;
-    x = (int64_t)dadd(cur.x, 0.5);
-    y = (int64_t)dadd(cur.y, 0.5);
-    z = (int64_t)dadd(cur.z, 0.5);
+    nsteps++;
+    if (s.nearb || s.ev != kEvOutOfVoxel) S->done = true;
+    S->x = (int64_t)dadd(S->cur.x, 0.5);
+    S->y = (int64_t)dadd(S->cur.y, 0.5);
+    S->z = (int64_t)dadd(S->cur.z, 0.5);
   }
+  return nsteps;
+}
+
+// The whole label-free streamline from `seed`.
+template <class Rec>
+SL_HD int trace_line(const Field& F, const Params& P, int dsc, V3 seed, Rec rec) {
+  LineState S = line_start(P, seed);
+  return trace_more(F, P, dsc, &S, INT32_MAX, rec);
 }
 
 // One streamline's walk over its records against the claims of the previous round
 // (claim(cell): the smallest key of a live write of the cell, 0 for a cell labelled
 // before the lines, kNoClaim for none): emit(cell, key) for each live write, in order.
-// Returns the number of steps the streamline keeps.
+// Returns the number of steps the streamline keeps; *ran_off (when given) tells whether
+// the walk went past the last record of a streamline that goes on (records traced in
+// pieces: it needs more).
 template <class Steps, class Claim, class Emit>
 SL_HD int walk_line(const Field& F, const Params& P, int dsc, uint32_t item, Steps steps, int nsteps, Claim claim,
-                    Emit emit) {
+                    Emit emit, bool* ran_off = nullptr) {
+  if (ran_off) *ran_off = false;
   for (int t = 0; t < nsteps; t++) {
     const StepRec& s = steps(t);
     if (s.nearb) return t + 1;
@@ -483,6 +504,7 @@ SL_HD int walk_line(const Field& F, const Params& P, int dsc, uint32_t item, Ste
     }
     if (hit >= 0 || s.ev != kEvOutOfVoxel) return t + 1;
   }
+  if (ran_off) *ran_off = true;
   return nsteps;
 }
 

@@ -5,6 +5,7 @@
 // plain loops -- so the scheme's result is checked against the one-thread oracle
 // without a GPU.
 #include <algorithm>
+#include <climits>
 #include <cstdint>
 #include <vector>
 
@@ -69,18 +70,32 @@ std::vector<int64_t> saddle_order(const float* f, const uint8_t* grad, const Gri
 
 struct Line {
   uint32_t item;
-  size_t first, n;
+  LineState state;
+  std::vector<StepRec> recs;
+  int budget;  // voxel steps of the next piece
 };
 
-// stats: [streamlines, recorded steps, kept steps, rounds]
+// budget 0: every streamline traced to its end before the rounds; budget b > 0: traced
+// b voxel steps at first, and a streamline whose walk runs past its last record traced
+// on (twice the previous piece) before the next round.
+// stats: [streamlines, recorded steps, kept steps, rounds, pieces traced]
 int run_lines(const Field& F, const Params& P, const uint8_t* grad, int dsc, uint8_t target, uint8_t* cells,
-              int64_t* stats) {
+              int budget, int64_t* stats) {
   const Grid& G = F.g;
   const std::vector<int64_t> order = saddle_order(F.f, grad, G, dsc);
   std::vector<Line> lines;
-  std::vector<StepRec> recs;
   std::vector<std::pair<int64_t, uint32_t>> saddle_writes;
   uint32_t item = 0;
+  int64_t pieces = 0;
+  auto trace = [&](Line& L) {
+    pieces++;
+    const int r = trace_more(F, P, dsc, &L.state, L.budget > 0 ? L.budget : INT32_MAX, [&](const StepRec& s) {
+      L.recs.push_back(s);
+      return true;
+    });
+    if (L.budget < (1 << 28)) L.budget *= 2;
+    return r >= 0;
+  };
   for (const int64_t sad : order) {
     int64_t seeds[kMaxSeeds];
     const int ns = saddle_seeds(G, grad, sad, dsc, seeds);
@@ -88,14 +103,8 @@ int run_lines(const Field& F, const Params& P, const uint8_t* grad, int dsc, uin
       int64_t k[3];
       cell_coords(G, seeds[i], k);
       const V3 seed = {(double)k[0] * 0.5, (double)k[1] * 0.5, (double)k[2] * 0.5};
-      Line L{item++, recs.size(), 0};
-      const int r = trace_line(F, P, dsc, seed, [&](const StepRec& s) {
-        recs.push_back(s);
-        return true;
-      });
-      if (r < 0) return -1;
-      L.n = recs.size() - L.first;
-      lines.push_back(L);
+      lines.push_back(Line{item++, line_start(P, seed), {}, budget});
+      if (!trace(lines.back())) return -1;
     }
     saddle_writes.push_back({sad, item++});
   }
@@ -104,40 +113,53 @@ int run_lines(const Field& F, const Params& P, const uint8_t* grad, int dsc, uin
   for (int64_t c = 0; c < nc; c++)
     if (cells[c] == target) base[c] = 0;
   std::vector<uint64_t> claim = base, next;
+  std::vector<Line*> more;
   int64_t rounds = 0, kept = 0;
   for (;;) {
     next = base;
     for (const auto& w : saddle_writes) next[w.first] = std::min(next[w.first], event_key(w.second, 0, 0));
     kept = 0;
-    for (const Line& L : lines)
+    more.clear();
+    for (Line& L : lines) {
+      bool ran_off = false;
       kept += walk_line(
-          F, P, dsc, L.item, [&](int t) -> const StepRec& { return recs[L.first + t]; }, (int)L.n,
-          [&](int64_t c) { return claim[c]; }, [&](int64_t c, uint64_t key) { next[c] = std::min(next[c], key); });
+          F, P, dsc, L.item, [&](int t) -> const StepRec& { return L.recs[t]; }, (int)L.recs.size(),
+          [&](int64_t c) { return claim[c]; }, [&](int64_t c, uint64_t key) { next[c] = std::min(next[c], key); },
+          &ran_off);
+      if (ran_off && !L.state.done) more.push_back(&L);
+    }
     rounds++;
-    if (next == claim) break;
+    if (next == claim && more.empty()) break;
     claim.swap(next);
+    for (Line* L : more)
+      if (!trace(*L)) return -1;
   }
   for (int64_t c = 0; c < nc; c++)
     if (claim[c] != kNoClaim) cells[c] = target;
+  int64_t recorded = 0;
+  for (const Line& L : lines) recorded += (int64_t)L.recs.size();
   stats[0] += (int64_t)lines.size();
-  stats[1] += (int64_t)recs.size();
+  stats[1] += recorded;
   stats[2] += kept;
   stats[3] = std::max(stats[3], rounds);
+  stats[4] += pieces;
   return 0;
 }
 
 }  // namespace
 
 // which: 1 ascending lines from the 2-saddles (label 4), 2 descending lines from the
-// 1-saddles (label 5), 3 both (ascending first); cells updated in place.
+// 1-saddles (label 5), 3 both (ascending first); cells updated in place.  budget: 0
+// traces every streamline whole before the rounds, b > 0 in pieces of b, 2b, ... voxel
+// steps.  stats: [streamlines, recorded steps, kept steps, rounds, pieces traced].
 extern "C" int core_saddle_lines_3d(const float* f, const uint8_t* grad, const uint32_t* zeroed, int64_t X,
                                     int64_t Y, int64_t Z, int which, float ethresh, float gthresh, double max_step,
-                                    int limit, uint8_t* cells, int64_t* stats) {
-  if (X < 2 || Y < 2 || Z < 2 || limit < 0 || limit >= (1 << 27)) return -1;
+                                    int limit, int budget, uint8_t* cells, int64_t* stats) {
+  if (X < 2 || Y < 2 || Z < 2 || limit < 0 || limit >= (1 << 27) || budget < 0) return -1;
   const Field F{f, zeroed, make_grid(X, Y, Z)};
   const Params P{ethresh, gthresh, max_step, limit};
-  for (int i = 0; i < 4; i++) stats[i] = 0;
-  if ((which & 1) && run_lines(F, P, grad, 0, 4, cells, stats)) return -2;
-  if ((which & 2) && run_lines(F, P, grad, 1, 5, cells, stats)) return -2;
+  for (int i = 0; i < 5; i++) stats[i] = 0;
+  if ((which & 1) && run_lines(F, P, grad, 0, 4, cells, budget, stats)) return -2;
+  if ((which & 2) && run_lines(F, P, grad, 1, 5, cells, budget, stats)) return -2;
   return 0;
 }

@@ -50,7 +50,7 @@ def host_core(tmp_path_factory):
     lib = ctypes.CDLL(str(out))
     vp, i64 = ctypes.c_void_p, ctypes.c_int64
     lib.core_saddle_lines_3d.argtypes = [vp, vp, vp, i64, i64, i64, ctypes.c_int, ctypes.c_float, ctypes.c_float,
-                                         ctypes.c_double, ctypes.c_int, vp, vp]
+                                         ctypes.c_double, ctypes.c_int, ctypes.c_int, vp, vp]
     return lib
 
 
@@ -88,11 +88,11 @@ def test_device_lines_equal_oracle_and_host_form(gpu, oracle, host_core, case, w
     assert np.array_equal(dg, g)
     assert np.array_equal(got, want), int((got != want).sum())
     host = cells.copy()
-    hs = np.zeros(4, np.int64)
+    hs = np.zeros(5, np.int64)
     assert host_core.core_saddle_lines_3d(f.ctypes.data, g.ctypes.data, None if zeroed is None else zeroed.ctypes.data,
-                                          *f.shape[::-1], which, 1e-4, gt, 0.25, 4000, host.ctypes.data,
+                                          *f.shape[::-1], which, 1e-4, gt, 0.25, 4000, 0, host.ctypes.data,
                                           hs.ctypes.data) == 0
-    assert tuple(stats) == tuple(int(x) for x in hs)
+    assert tuple(stats) == tuple(int(x) for x in hs[:4])
 
 
 def test_device_lines_larger_field(gpu, oracle):

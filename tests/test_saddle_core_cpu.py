@@ -29,7 +29,7 @@ def core(tmp_path_factory):
                     str(HERE / "saddle_core_host.cpp")], check=True)
     lib = ctypes.CDLL(str(out))
     lib.core_saddle_lines_3d.argtypes = [_VP, _VP, _VP, _I64, _I64, _I64, ctypes.c_int, ctypes.c_float,
-                                         ctypes.c_float, ctypes.c_double, ctypes.c_int, _VP, _VP]
+                                         ctypes.c_float, ctypes.c_double, ctypes.c_int, ctypes.c_int, _VP, _VP]
     return lib
 
 
@@ -44,14 +44,15 @@ def preset_cells(nc, spec):
     return cells
 
 
-def run_core(core, f, g, which, cells, zeroed=None):
-    """(cells after the lines, [streamlines, recorded steps, kept steps, rounds])."""
+def run_core(core, f, g, which, cells, zeroed=None, budget=0):
+    """(cells after the lines, [streamlines, recorded steps, kept steps, rounds, pieces]);
+    budget 0 traces the streamlines whole before the rounds, b > 0 in growing pieces."""
     out = np.array(cells, dtype=np.uint8, copy=True)
-    stats = np.zeros(4, np.int64)
+    stats = np.zeros(5, np.int64)
     gt = 1e-6 * float(np.abs(f).max())
     zp = None if zeroed is None else zeroed.ctypes.data
     rc = core.core_saddle_lines_3d(f.ctypes.data, g.ctypes.data, zp, *f.shape[::-1], which, 1e-4, gt, 0.25, 4000,
-                                   out.ctypes.data, stats.ctypes.data)
+                                   budget, out.ctypes.data, stats.ctypes.data)
     assert rc == 0
     return out, stats
 
@@ -87,6 +88,11 @@ def test_parallel_lines_against_oracle(core, oracle, case, which):
     assert (want != cells).sum() > 0
     assert np.array_equal(got, want), int((got != want).sum())
     assert stats[0] > 0 and stats[3] >= 2
+    # traced in pieces (4, 8, 16, ... voxel steps, continued only where a walk runs past
+    # its records): the same labels from fewer recorded steps
+    lazy, ls = run_core(core, f, g, which, cells, budget=4)
+    assert np.array_equal(lazy, want), int((lazy != want).sum())
+    assert ls[1] <= stats[1] and ls[2] == stats[2] and ls[4] >= ls[0]
 
 
 @pytest.mark.parametrize("which", [1, 2, 3])
