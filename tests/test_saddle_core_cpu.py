@@ -57,14 +57,15 @@ def run_core(core, f, g, which, cells, zeroed=None, budget=0):
     return out, stats
 
 
+@pytest.mark.parametrize("budget", [0, 2])
 @pytest.mark.parametrize("key", sorted(CASES))
-def test_parallel_lines_against_golden(core, oracle, key):
+def test_parallel_lines_against_golden(core, oracle, key, budget):
     spec = CASES[key]
     f = eval("fields." + spec["generator"], {"fields": fields}).astype(np.float32)
     if hashlib.sha256(f.tobytes()).hexdigest() != spec["f_sha256"]:
         pytest.skip("this host regenerates other floats for the field (FFT); the streamlines follow them")
     g = oracle.grad(f)
-    got, stats = run_core(core, f, g, spec["which"], preset_cells(g.size, spec["preset"]))
+    got, stats = run_core(core, f, g, spec["which"], preset_cells(g.size, spec["preset"]), budget=budget)
     assert int((got > 0).sum()) == spec["labelled"]
     assert hashlib.sha256(got.tobytes()).hexdigest() == spec["sha256"]
     assert stats[3] >= 2 and stats[2] <= stats[1]
